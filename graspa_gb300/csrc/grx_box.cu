@@ -1,0 +1,489 @@
+// grx_box.cu -- box lifecycle, component upload, Ewald k-vector table, structure
+// factors and FP64 totals (drift checks).
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "grx_host.h"
+
+namespace grx {
+
+static thread_local char g_err[512] = "";
+static std::atomic<uint64_t> g_launches{0};
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+grx_status cuda_status(cudaError_t e, const char* what) {
+  set_error("%s: %s", what, cudaGetErrorString(e));
+  if (e == cudaErrorMemoryAllocation) return GRX_ERR_OUT_OF_MEMORY;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return GRX_ERR_NO_DEVICE;
+  return GRX_ERR_CUDA;
+}
+
+void count_launch(uint64_t n) { g_launches += n; }
+
+int sm_count(grx_box* b) {
+  if (!b->num_sms) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, b->device);
+    b->num_sms = v > 0 ? v : 1;
+  }
+  return b->num_sms;
+}
+
+grx_status ensure_scratch(grx_box* b, size_t bytes) {
+  if (bytes <= b->scratch_bytes) return GRX_OK;
+  if (b->scratch) cudaFree(b->scratch);
+  b->scratch = nullptr;
+  b->scratch_bytes = 0;
+  size_t want = std::max(bytes, (size_t)1 << 20);
+  GRX_CHECK_CUDA(cudaMalloc(&b->scratch, want), "scratch allocation");
+  b->scratch_bytes = want;
+  return GRX_OK;
+}
+
+grx_status ensure_pinned(grx_box* b, size_t bytes) {
+  if (bytes <= b->pinned_bytes) return GRX_OK;
+  if (b->pinned) cudaFreeHost(b->pinned);
+  b->pinned = nullptr;
+  b->pinned_bytes = 0;
+  size_t want = std::max(bytes, (size_t)1 << 16);
+  GRX_CHECK_CUDA(cudaMallocHost(&b->pinned, want), "pinned staging allocation");
+  b->pinned_bytes = want;
+  return GRX_OK;
+}
+
+grx_status ensure_results(grx_box* b, size_t n) {
+  if (n <= b->results_cap) return GRX_OK;
+  if (b->d_results) cudaFree(b->d_results);
+  b->d_results = nullptr;
+  b->results_cap = 0;
+  size_t want = std::max(n, (size_t)1024);
+  GRX_CHECK_CUDA(cudaMalloc(&b->d_results, want * sizeof(grx_widom_result)), "result buffer");
+  b->results_cap = want;
+  return GRX_OK;
+}
+
+void refresh_dev(grx_box* b) {
+  BoxDev& d = b->dev;
+  d.ncomp = b->ncomp;
+  d.nhost = b->nhost;
+  for (int c = 0; c <= b->ncomp; ++c) d.comp_off[c] = (int)b->off[c];
+  d.comp_size = b->d_size;
+  d.pos64 = b->pos64;
+  d.hi = b->hi;
+  d.lo = b->lo;
+  d.meta = b->meta;
+  d.scale = b->scale;
+  d.charge = b->charge;
+  d.ff64 = b->ff64;
+  d.ffc10 = b->ffc10;
+  d.ff32 = b->ff32;
+  d.nvec = b->nvec;
+  d.nact = b->nact;
+  d.kact = b->kact;
+  d.ktemp = b->ktemp;
+  d.s_fw = b->s_fw;
+  d.s_ads = b->s_ads;
+  d.s_tmp = b->s_tmp;
+}
+
+static double hi_part(double x) { return std::nearbyint(x * GRX_GRID_COORD) / GRX_GRID_COORD; }
+
+// Host minimum image (PBC(), maths.cuh:427-450), used for exclusion constants.
+static void pbc_host(const BoxDev& b, double* d) {
+  if (b.cubic) {
+    for (int k = 0; k < 3; ++k) {
+      const int kk = 4 * k;
+      d[k] -= (double)(int)(d[k] * b.inv[kk] + ((d[k] >= 0.0) ? 0.5 : -0.5)) * b.cell[kk];
+    }
+  } else {
+    double s[3];
+    s[0] = b.inv[0] * d[0] + b.inv[3] * d[1] + b.inv[6] * d[2];
+    s[1] = b.inv[1] * d[0] + b.inv[4] * d[1] + b.inv[7] * d[2];
+    s[2] = b.inv[2] * d[0] + b.inv[5] * d[1] + b.inv[8] * d[2];
+    for (int k = 0; k < 3; ++k) s[k] -= (double)(int)(s[k] + ((s[k] >= 0.0) ? 0.5 : -0.5));
+    d[0] = b.cell[0] * s[0] + b.cell[3] * s[1] + b.cell[6] * s[2];
+    d[1] = b.cell[1] * s[0] + b.cell[4] * s[1] + b.cell[7] * s[2];
+    d[2] = b.cell[2] * s[0] + b.cell[5] * s[1] + b.cell[8] * s[2];
+  }
+}
+
+// Active k slots and their prefactors: the slot unranking and cutoff test of
+// Fourier_Ewald_Diff (Ewald_Energy_Functions.h:294-333) and the factor of :359-361.
+static void build_kvectors(grx_box* b, const grx_box_geometry& g) {
+  const int kxm = g.kmax[0], kym = g.kmax[1], kzm = g.kmax[2];
+  b->nvec = (kxm + 1) * (2 * kym + 1) * (2 * kzm + 1);
+  b->h_kact.clear();
+  b->h_ktemp.clear();
+  const double* ic = g.inverse_cell;
+  const double PI = 3.14159265358979323846;
+  const double prefactor = g.prefactor * (2.0 * PI / g.volume);
+  const double alpha_sq = g.alpha * g.alpha;
+  for (int kxyz = 0; kxyz < b->nvec; ++kxyz) {
+    const int kz = kxyz % (2 * kzm + 1) - kzm;
+    const int kxy = kxyz / (2 * kzm + 1);
+    const int kx = kxy / (2 * kym + 1);
+    const int ky = kxy % (2 * kym + 1) - kym;
+    double ksqr = (double)(kx * kx + ky * ky + kz * kz);
+    if (g.use_lammps_ewald) {
+      const double* C = g.cell;
+      const double lx = C[0], ly = C[4], lz = C[8], xy = C[3], xz = C[6], yz = C[7];
+      const double ux = 2 * PI / lx, uy = 2 * PI * (-xy) / lx / ly;
+      const double uz = 2 * PI * (xy * yz - ly * xz) / lx / ly / lz;
+      const double vy = 2 * PI / ly, vz = 2 * PI * (-yz) / ly / lz, wz = 2 * PI / lz;
+      const double kvx = kx * ux, kvy = kx * uy + ky * vy, kvz = kx * uz + ky * vz + kz * wz;
+      ksqr = kvx * kvx + kvy * kvy + kvz * kvz;
+    }
+    if (!((ksqr > 1e-10) && (ksqr < g.reciprocal_cutoff))) continue;
+    double kv[3];
+    // reciprocal vectors are the rows of the inverse cell: ax = (inv[0], inv[3], inv[6])
+    const double ax[3] = {ic[0], ic[3], ic[6]};
+    const double ay[3] = {ic[1], ic[4], ic[7]};
+    const double az[3] = {ic[2], ic[5], ic[8]};
+    for (int d = 0; d < 3; ++d)
+      kv[d] = ax[d] * 2.0 * PI * (double)kx + ay[d] * 2.0 * PI * (double)ky +
+              az[d] * 2.0 * PI * (double)kz;
+    const double rksq = kv[0] * kv[0] + kv[1] * kv[1] + kv[2] * kv[2];
+    const double factor = (kx == 0) ? (1.0 * prefactor) : (2.0 * prefactor);
+    b->h_kact.push_back(make_int4(kx, ky, kz, kxyz));
+    b->h_ktemp.push_back(factor * std::exp((-0.25 / alpha_sq) * rksq) / rksq);
+  }
+  b->nact = (int)b->h_kact.size();
+}
+
+}  // namespace grx
+
+using namespace grx;
+
+extern "C" {
+
+const char* grx_status_string(grx_status s) {
+  switch (s) {
+    case GRX_OK: return "ok";
+    case GRX_ERR_INVALID_ARG: return "invalid argument";
+    case GRX_ERR_CUDA: return "CUDA error";
+    case GRX_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case GRX_ERR_TIMEOUT: return "device wait timed out";
+    case GRX_ERR_CAPACITY: return "capacity exceeded";
+    case GRX_ERR_NO_DEVICE: return "no CUDA device";
+    case GRX_ERR_UNSUPPORTED: return "unsupported";
+  }
+  return "unknown status";
+}
+
+const char* grx_last_error(void) { return g_err; }
+
+uint64_t grx_launch_count(void) { return g_launches.load(); }
+
+grx_status grx_device_count(int32_t* n) {
+  int v = 0;
+  cudaError_t e = cudaGetDeviceCount(&v);
+  if (e != cudaSuccess) {
+    *n = 0;
+    return cuda_status(e, "cudaGetDeviceCount");
+  }
+  *n = v;
+  return GRX_OK;
+}
+
+grx_status grx_box_create(const grx_box_desc* desc, grx_box** out) {
+  GRX_REQUIRE(desc && out, "grx_box_create: null argument");
+  *out = nullptr;
+  const grx_forcefield& ff = desc->forcefield;
+  const grx_box_geometry& g = desc->geometry;
+  GRX_REQUIRE(desc->ncomponents >= 1 && desc->ncomponents <= GRX_MAX_COMPONENTS,
+              "grx_box_create: ncomponents out of range");
+  GRX_REQUIRE(desc->nhost_components >= 0 && desc->nhost_components <= desc->ncomponents,
+              "grx_box_create: nhost_components out of range");
+  GRX_REQUIRE(ff.ntypes >= 1 && ff.ntypes <= GRX_MAX_TYPES, "grx_box_create: ntypes out of range");
+  GRX_REQUIRE(ff.epsilon && ff.sigma && ff.shift, "grx_box_create: force-field tables missing");
+  GRX_REQUIRE(g.volume > 0.0, "grx_box_create: non-positive volume");
+  GRX_REQUIRE(g.kmax[0] >= 0 && g.kmax[1] >= 0 && g.kmax[2] >= 0 && g.kmax[0] < 64 &&
+                  g.kmax[1] < 64 && g.kmax[2] < 64,
+              "grx_box_create: kmax out of range");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    set_error("grx_box_create: no CUDA device");
+    return GRX_ERR_NO_DEVICE;
+  }
+  grx_box* b = new grx_box();
+  cudaGetDevice(&b->device);
+  b->ncomp = desc->ncomponents;
+  b->nhost = desc->nhost_components;
+  size_t acc = 0;
+  for (int c = 0; c < b->ncomp; ++c) {
+    b->cap[c] = desc->capacity[c];
+    b->molsize[c] = desc->molsize[c];
+    if (b->molsize[c] == 0 || b->molsize[c] > b->cap[c] + (b->cap[c] == 0)) {
+      delete b;
+      set_error("grx_box_create: component %d needs molsize >= 1 and capacity >= molsize", c);
+      return GRX_ERR_INVALID_ARG;
+    }
+    b->off[c] = acc;
+    acc += (b->cap[c] + 31) / 32 * 32;  // keep every component 128 B aligned
+  }
+  b->off[b->ncomp] = acc;
+  b->total_cap = std::max<size_t>(acc, 32);
+  b->h_pos.assign(3 * b->total_cap, 0.0);
+  b->h_charge.assign(b->total_cap, 0.0);
+  b->h_scale_coul.assign(b->total_cap, 1.0);
+
+  BoxDev& d = b->dev;
+  for (int k = 0; k < 9; ++k) {
+    d.cell[k] = g.cell[k];
+    d.inv[k] = g.inverse_cell[k];
+    const double h = hi_part(g.cell[k]);
+    d.cell_hi[k] = (float)h;
+    d.cell_lo[k] = (float)(g.cell[k] - h);
+    d.invf[k] = (float)g.inverse_cell[k];
+  }
+  d.cubic = g.cubic;
+  d.alpha = g.alpha;
+  d.prefactor = g.prefactor;
+  d.volume = g.volume;
+  d.ntypes = ff.ntypes;
+  d.use_1264 = ff.use_1264;
+  d.no_charges = ff.no_charges;
+  d.vdw_real_bias = ff.vdw_real_bias;
+  d.cut_vdw2 = ff.cutoff_vdw_sq;
+  d.cut_coul2 = ff.cutoff_coul_sq;
+  d.overlap = ff.overlap_criteria;
+  const double cmax = std::max(ff.cutoff_vdw_sq, ff.no_charges ? 0.0 : ff.cutoff_coul_sq);
+  d.screen2 = (float)(cmax * (1.0 + 1e-5) + 1e-3);
+  d.cut_vdw2f = (float)ff.cutoff_vdw_sq;
+  d.cut_coul2f = (float)ff.cutoff_coul_sq;
+  for (int k = 0; k < 3; ++k) d.kmax[k] = g.kmax[k];
+
+  const int nt2 = ff.ntypes * ff.ntypes;
+  std::vector<FFPair64> f64(nt2);
+  std::vector<double> c10(nt2, 0.0);
+  std::vector<float4> f32(nt2);
+  for (int r = 0; r < nt2; ++r) {
+    f64[r].a = ff.epsilon[r];
+    f64[r].b = ff.sigma[r];
+    f64[r].c = ff.z ? ff.z[r] : 0.0;
+    f64[r].shift = ff.shift[r];
+    if (ff.c10) c10[r] = ff.c10[r];
+    const double s2 = ff.sigma[r] * ff.sigma[r];
+    f32[r] = make_float4((float)(4.0 * ff.epsilon[r]), s2 > 0 ? (float)(1.0 / s2) : INFINITY,
+                         (float)ff.shift[r], (float)(1.21 * s2));
+  }
+  build_kvectors(b, g);
+
+  auto fail = [&](cudaError_t e, const char* what) {
+    grx_status s = cuda_status(e, what);
+    grx_box_destroy(b);
+    return s;
+  };
+  cudaError_t e;
+  const size_t n = b->total_cap;
+  if ((e = cudaMalloc(&b->pos64, n * sizeof(double4))) != cudaSuccess) return fail(e, "alloc pos64");
+  if ((e = cudaMalloc(&b->hi, n * sizeof(float4))) != cudaSuccess) return fail(e, "alloc hi");
+  if ((e = cudaMalloc(&b->lo, n * sizeof(float4))) != cudaSuccess) return fail(e, "alloc lo");
+  if ((e = cudaMalloc(&b->meta, n * sizeof(int2))) != cudaSuccess) return fail(e, "alloc meta");
+  if ((e = cudaMalloc(&b->scale, n * sizeof(double))) != cudaSuccess) return fail(e, "alloc scale");
+  if ((e = cudaMalloc(&b->charge, n * sizeof(double))) != cudaSuccess) return fail(e, "alloc charge");
+  if ((e = cudaMalloc(&b->d_size, GRX_MAX_COMPONENTS * sizeof(int))) != cudaSuccess) return fail(e, "alloc sizes");
+  if ((e = cudaMalloc(&b->ff64, nt2 * sizeof(FFPair64))) != cudaSuccess) return fail(e, "alloc ff64");
+  if ((e = cudaMalloc(&b->ffc10, nt2 * sizeof(double))) != cudaSuccess) return fail(e, "alloc ffc10");
+  if ((e = cudaMalloc(&b->ff32, nt2 * sizeof(float4))) != cudaSuccess) return fail(e, "alloc ff32");
+  const size_t nv = std::max(b->nvec, 1), na = std::max(b->nact, 1);
+  if ((e = cudaMalloc(&b->kact, na * sizeof(int4))) != cudaSuccess) return fail(e, "alloc kact");
+  if ((e = cudaMalloc(&b->ktemp, na * sizeof(double))) != cudaSuccess) return fail(e, "alloc ktemp");
+  if ((e = cudaMalloc(&b->s_fw, nv * sizeof(double2))) != cudaSuccess) return fail(e, "alloc s_fw");
+  if ((e = cudaMalloc(&b->s_ads, nv * sizeof(double2))) != cudaSuccess) return fail(e, "alloc s_ads");
+  if ((e = cudaMalloc(&b->s_tmp, nv * sizeof(double2))) != cudaSuccess) return fail(e, "alloc s_tmp");
+  cudaMemset(b->pos64, 0, n * sizeof(double4));
+  cudaMemset(b->hi, 0, n * sizeof(float4));
+  cudaMemset(b->lo, 0, n * sizeof(float4));
+  cudaMemset(b->meta, 0, n * sizeof(int2));
+  cudaMemset(b->scale, 0, n * sizeof(double));
+  cudaMemset(b->charge, 0, n * sizeof(double));
+  cudaMemset(b->d_size, 0, GRX_MAX_COMPONENTS * sizeof(int));
+  cudaMemset(b->s_fw, 0, nv * sizeof(double2));
+  cudaMemset(b->s_ads, 0, nv * sizeof(double2));
+  cudaMemset(b->s_tmp, 0, nv * sizeof(double2));
+  cudaMemcpy(b->ff64, f64.data(), nt2 * sizeof(FFPair64), cudaMemcpyHostToDevice);
+  cudaMemcpy(b->ffc10, c10.data(), nt2 * sizeof(double), cudaMemcpyHostToDevice);
+  cudaMemcpy(b->ff32, f32.data(), nt2 * sizeof(float4), cudaMemcpyHostToDevice);
+  if (b->nact) {
+    cudaMemcpy(b->kact, b->h_kact.data(), b->nact * sizeof(int4), cudaMemcpyHostToDevice);
+    cudaMemcpy(b->ktemp, b->h_ktemp.data(), b->nact * sizeof(double), cudaMemcpyHostToDevice);
+  }
+  if ((e = cudaDeviceSynchronize()) != cudaSuccess) return fail(e, "box upload");
+  refresh_dev(b);
+  *out = b;
+  return GRX_OK;
+}
+
+grx_status grx_box_destroy(grx_box* b) {
+  if (!b) return GRX_OK;
+  void* ptrs[] = {b->pos64, b->hi, b->lo, b->meta, b->scale, b->charge, b->d_size, b->ff64,
+                  b->ffc10, b->ff32, b->kact, b->ktemp, b->s_fw, b->s_ads, b->s_tmp,
+                  b->scratch, b->d_results};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (b->pinned) cudaFreeHost(b->pinned);
+  delete b;
+  return GRX_OK;
+}
+
+grx_status grx_box_set_stream(grx_box* b, void* s) {
+  GRX_REQUIRE(b, "grx_box_set_stream: null box");
+  b->stream = (cudaStream_t)s;
+  return GRX_OK;
+}
+
+grx_status grx_box_set_component(grx_box* b, int32_t comp, const grx_atoms* a, int32_t rigid) {
+  GRX_REQUIRE(b && a, "grx_box_set_component: null argument");
+  GRX_REQUIRE(comp >= 0 && comp < b->ncomp, "grx_box_set_component: component out of range");
+  const size_t nst = std::max(a->n_stored, a->size);
+  if (nst > b->cap[comp] || a->size > b->cap[comp]) {
+    set_error("grx_box_set_component: %zu atoms exceed capacity %zu of component %d", nst,
+              b->cap[comp], comp);
+    return GRX_ERR_CAPACITY;
+  }
+  GRX_REQUIRE(nst == 0 || (a->pos && a->charge && a->type && a->molid),
+              "grx_box_set_component: atom arrays missing");
+  // stage the caller's arrays (host or device) on the host
+  std::vector<double> pos(3 * nst), sc(nst, 1.0), q(nst), scc(nst, 1.0);
+  std::vector<size_t> ty(nst), mol(nst);
+  if (nst) {
+    GRX_CHECK_CUDA(cudaMemcpy(pos.data(), a->pos, 3 * nst * sizeof(double), cudaMemcpyDefault), "read pos");
+    GRX_CHECK_CUDA(cudaMemcpy(q.data(), a->charge, nst * sizeof(double), cudaMemcpyDefault), "read charge");
+    GRX_CHECK_CUDA(cudaMemcpy(ty.data(), a->type, nst * sizeof(size_t), cudaMemcpyDefault), "read type");
+    GRX_CHECK_CUDA(cudaMemcpy(mol.data(), a->molid, nst * sizeof(size_t), cudaMemcpyDefault), "read molid");
+    if (a->scale)
+      GRX_CHECK_CUDA(cudaMemcpy(sc.data(), a->scale, nst * sizeof(double), cudaMemcpyDefault), "read scale");
+    if (a->scale_coul)
+      GRX_CHECK_CUDA(cudaMemcpy(scc.data(), a->scale_coul, nst * sizeof(double), cudaMemcpyDefault),
+                     "read scale_coul");
+  }
+  for (size_t i = 0; i < nst; ++i)
+    if (ty[i] >= (size_t)b->dev.ntypes) {
+      set_error("grx_box_set_component: atom %zu has type %zu >= ntypes %d", i, ty[i], b->dev.ntypes);
+      return GRX_ERR_INVALID_ARG;
+    }
+  std::vector<double4> p64(nst);
+  std::vector<float4> h(nst), l(nst);
+  std::vector<int2> m(nst);
+  const size_t o = b->off[comp];
+  bool charged = false;
+  for (size_t i = 0; i < nst; ++i) {
+    const double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+    const double qe = q[i] * scc[i];
+    p64[i] = make_double4(x, y, z, qe);
+    const double hx = hi_part(x), hy = hi_part(y), hz = hi_part(z);
+    h[i] = make_float4((float)hx, (float)hy, (float)hz, (float)qe);
+    l[i] = make_float4((float)(x - hx), (float)(y - hy), (float)(z - hz), (float)sc[i]);
+    m[i] = make_int2((int)ty[i], (int)mol[i]);
+    if (q[i] != 0.0) charged = true;
+    b->h_pos[3 * (o + i)] = x; b->h_pos[3 * (o + i) + 1] = y; b->h_pos[3 * (o + i) + 2] = z;
+    b->h_charge[o + i] = q[i];
+    b->h_scale_coul[o + i] = scc[i];
+  }
+  b->size[comp] = (int)a->size;
+  b->rigid[comp] = rigid;
+  b->has_charge[comp] = charged ? 1 : 0;
+  if (nst) {
+    GRX_CHECK_CUDA(cudaMemcpy(b->pos64 + o, p64.data(), nst * sizeof(double4), cudaMemcpyHostToDevice), "upload pos64");
+    GRX_CHECK_CUDA(cudaMemcpy(b->hi + o, h.data(), nst * sizeof(float4), cudaMemcpyHostToDevice), "upload hi");
+    GRX_CHECK_CUDA(cudaMemcpy(b->lo + o, l.data(), nst * sizeof(float4), cudaMemcpyHostToDevice), "upload lo");
+    GRX_CHECK_CUDA(cudaMemcpy(b->meta + o, m.data(), nst * sizeof(int2), cudaMemcpyHostToDevice), "upload meta");
+    GRX_CHECK_CUDA(cudaMemcpy(b->scale + o, sc.data(), nst * sizeof(double), cudaMemcpyHostToDevice), "upload scale");
+    GRX_CHECK_CUDA(cudaMemcpy(b->charge + o, q.data(), nst * sizeof(double), cudaMemcpyHostToDevice), "upload charge");
+  }
+  GRX_CHECK_CUDA(cudaMemcpy(b->d_size, b->size, GRX_MAX_COMPONENTS * sizeof(int), cudaMemcpyHostToDevice),
+                 "upload sizes");
+  // rigid exclusion constants from the first molecule: Calculate_Intra_Molecule_Exclusion
+  // and Calculate_Self_Exclusion (ewald_preparation.h:261-298), FP64.
+  b->excl_intra[comp] = 0.0;
+  b->excl_self[comp] = 0.0;
+  const size_t ms = b->molsize[comp];
+  if (rigid && nst >= ms && ms > 0) {
+    double e = 0.0;
+    for (size_t i = 0; i + 1 < ms; ++i) {
+      const double fa = scc[i] * q[i];
+      for (size_t j = i + 1; j < ms; ++j) {
+        const double fb = scc[j] * q[j];
+        double dv[3] = {pos[3 * i] - pos[3 * j], pos[3 * i + 1] - pos[3 * j + 1], pos[3 * i + 2] - pos[3 * j + 2]};
+        pbc_host(b->dev, dv);
+        const double r = std::sqrt(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
+        e += b->dev.prefactor * fa * fb * std::erf(b->dev.alpha * r) / r;
+      }
+    }
+    const double ps = b->dev.prefactor * b->dev.alpha / std::sqrt(3.14159265358979323846);
+    double s = 0.0;
+    for (size_t i = 0; i < ms; ++i) s += ps * scc[i] * q[i] * scc[i] * q[i];
+    b->excl_intra[comp] = e;
+    b->excl_self[comp] = s;
+  }
+  b->sk_valid = false;
+  return GRX_OK;
+}
+
+grx_status grx_box_get_component_size(grx_box* b, int32_t comp, size_t* size) {
+  GRX_REQUIRE(b && size && comp >= 0 && comp < b->ncomp, "grx_box_get_component_size: bad argument");
+  int v = 0;
+  GRX_CHECK_CUDA(cudaMemcpy(&v, b->d_size + comp, sizeof(int), cudaMemcpyDeviceToHost), "read size");
+  b->size[comp] = v;
+  *size = (size_t)v;
+  return GRX_OK;
+}
+
+grx_status grx_box_get_positions(grx_box* b, int32_t comp, double* out, size_t n) {
+  GRX_REQUIRE(b && out && comp >= 0 && comp < b->ncomp, "grx_box_get_positions: bad argument");
+  GRX_REQUIRE(n <= b->cap[comp], "grx_box_get_positions: n exceeds capacity");
+  std::vector<double4> p(n);
+  if (n)
+    GRX_CHECK_CUDA(cudaMemcpy(p.data(), b->pos64 + b->off[comp], n * sizeof(double4), cudaMemcpyDeviceToHost),
+                   "read positions");
+  std::vector<double> flat(3 * n);
+  for (size_t i = 0; i < n; ++i) { flat[3 * i] = p[i].x; flat[3 * i + 1] = p[i].y; flat[3 * i + 2] = p[i].z; }
+  if (n) GRX_CHECK_CUDA(cudaMemcpy(out, flat.data(), 3 * n * sizeof(double), cudaMemcpyDefault), "write positions");
+  return GRX_OK;
+}
+
+grx_status grx_box_get_exclusion(grx_box* b, int32_t comp, double* intra, double* self) {
+  GRX_REQUIRE(b && intra && self && comp >= 0 && comp < b->ncomp, "grx_box_get_exclusion: bad argument");
+  *intra = b->excl_intra[comp];
+  *self = b->excl_self[comp];
+  return GRX_OK;
+}
+
+grx_status grx_ewald_sizes(grx_box* b, int64_t* nvec, int64_t* nactive) {
+  GRX_REQUIRE(b && nvec && nactive, "grx_ewald_sizes: null argument");
+  *nvec = b->nvec;
+  *nactive = b->nact;
+  return GRX_OK;
+}
+
+grx_status grx_ewald_set_structure_factors(grx_box* b, const double* s_fw, const double* s_ads) {
+  GRX_REQUIRE(b && s_fw && s_ads, "grx_ewald_set_structure_factors: null argument");
+  GRX_CHECK_CUDA(cudaMemcpy(b->s_fw, s_fw, b->nvec * sizeof(double2), cudaMemcpyDefault), "set S_fw");
+  GRX_CHECK_CUDA(cudaMemcpy(b->s_ads, s_ads, b->nvec * sizeof(double2), cudaMemcpyDefault), "set S_ads");
+  GRX_CHECK_CUDA(cudaMemcpy(b->s_tmp, s_ads, b->nvec * sizeof(double2), cudaMemcpyDefault), "set S_tmp");
+  b->sk_valid = true;
+  return GRX_OK;
+}
+
+grx_status grx_ewald_get_structure_factors(grx_box* b, double* s_fw, double* s_ads, double* s_tmp) {
+  GRX_REQUIRE(b, "grx_ewald_get_structure_factors: null box");
+  GRX_CHECK_CUDA(cudaStreamSynchronize(b->stream), "sync");
+  if (s_fw) GRX_CHECK_CUDA(cudaMemcpy(s_fw, b->s_fw, b->nvec * sizeof(double2), cudaMemcpyDefault), "get S_fw");
+  if (s_ads) GRX_CHECK_CUDA(cudaMemcpy(s_ads, b->s_ads, b->nvec * sizeof(double2), cudaMemcpyDefault), "get S_ads");
+  if (s_tmp) GRX_CHECK_CUDA(cudaMemcpy(s_tmp, b->s_tmp, b->nvec * sizeof(double2), cudaMemcpyDefault), "get S_tmp");
+  return GRX_OK;
+}
+
+}  // extern "C"

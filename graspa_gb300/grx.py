@@ -1,0 +1,421 @@
+"""ctypes binding of libgrx.so (include/grx.h) and a small Box wrapper.
+
+This is the Python face of the C ABI, used by the tests and the benchmark the way
+gRASPA's pybind module (src_clean/pybind.h) exposes its structs. All energy work
+runs in libgrx.so on the GPU; there is no CPU fallback: loading fails loudly when
+the library or a CUDA device is missing.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libgrx.so")
+
+GRX_FP64, GRX_MIXED, GRX_FP32 = 0, 1, 2
+PRECISIONS = {"fp64": GRX_FP64, "mixed": GRX_MIXED, "fp32": GRX_FP32}
+MOVE_TRANSLATION, MOVE_ROTATION, MOVE_SINGLE_INSERTION, MOVE_SINGLE_DELETION = 0, 1, 2, 3
+MOVE_INSERTION, MOVE_DELETION, MOVE_REINSERTION = 5, 6, 7
+MAX_COMPONENTS = 8
+
+_dp = C.POINTER(C.c_double)
+_szp = C.POINTER(C.c_size_t)
+_u8p = C.POINTER(C.c_uint8)
+
+
+class GrxError(RuntimeError):
+    pass
+
+
+class BoxGeometry(C.Structure):
+    _fields_ = [("cell", C.c_double * 9), ("inverse_cell", C.c_double * 9), ("volume", C.c_double),
+                ("cubic", C.c_int32), ("use_lammps_ewald", C.c_int32), ("kmax", C.c_int32 * 3),
+                ("pad_", C.c_int32), ("alpha", C.c_double), ("prefactor", C.c_double),
+                ("reciprocal_cutoff", C.c_double)]
+
+
+class ForceField(C.Structure):
+    _fields_ = [("ntypes", C.c_int32), ("use_1264", C.c_int32), ("epsilon", _dp), ("sigma", _dp),
+                ("z", _dp), ("shift", _dp), ("c10", _dp), ("no_charges", C.c_int32),
+                ("vdw_real_bias", C.c_int32), ("overlap_criteria", C.c_double),
+                ("cutoff_vdw_sq", C.c_double), ("cutoff_coul_sq", C.c_double)]
+
+
+class BoxDesc(C.Structure):
+    _fields_ = [("geometry", BoxGeometry), ("forcefield", ForceField), ("ncomponents", C.c_int32),
+                ("nhost_components", C.c_int32), ("capacity", C.c_size_t * MAX_COMPONENTS),
+                ("molsize", C.c_size_t * MAX_COMPONENTS)]
+
+
+class Atoms(C.Structure):
+    _fields_ = [("pos", _dp), ("scale", _dp), ("charge", _dp), ("scale_coul", _dp), ("type", _szp),
+                ("molid", _szp), ("size", C.c_size_t), ("n_stored", C.c_size_t)]
+
+
+class Trials(C.Structure):
+    _fields_ = [("pos", _dp), ("scale", _dp), ("charge", _dp), ("scale_coul", _dp), ("type", _szp),
+                ("molid", C.c_size_t), ("ntrials", C.c_size_t), ("chainsize", C.c_size_t)]
+
+
+class TrialEnergy(C.Structure):
+    _fields_ = [("hg_vdw", C.c_double), ("hg_real", C.c_double), ("gg_vdw", C.c_double),
+                ("gg_real", C.c_double)]
+
+
+class Energy(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("hh_vdw", "hh_real", "hg_vdw", "hg_real", "gg_vdw", "gg_real",
+                                          "hh_ewald", "hg_ewald", "gg_ewald")]
+
+
+class WidomDesc(C.Structure):
+    _fields_ = [("component", C.c_int32), ("ntrials", C.c_int32), ("norient", C.c_int32),
+                ("pad_", C.c_int32), ("scale", C.c_double), ("scale_coul", C.c_double),
+                ("beta", C.c_double), ("tail_delta", C.c_double), ("seed", C.c_uint64),
+                ("stream", C.c_uint32), ("pad2_", C.c_uint32)]
+
+
+class WidomResult(C.Structure):
+    _fields_ = [("rosenbluth", C.c_double), ("w_first", C.c_double), ("w_chain", C.c_double),
+                ("e_first", C.c_double * 4), ("e_chain", C.c_double * 4), ("ewald", C.c_double * 2),
+                ("sel_first", C.c_int64), ("sel_orient", C.c_int64), ("n_ok_first", C.c_int64),
+                ("n_ok_orient", C.c_int64), ("success", C.c_int32), ("pad_", C.c_int32)]
+
+
+WIDOM_RESULT_DTYPE = np.dtype([("rosenbluth", "f8"), ("w_first", "f8"), ("w_chain", "f8"),
+                               ("e_first", "f8", 4), ("e_chain", "f8", 4), ("ewald", "f8", 2),
+                               ("sel_first", "i8"), ("sel_orient", "i8"), ("n_ok_first", "i8"),
+                               ("n_ok_orient", "i8"), ("success", "i4"), ("pad_", "i4")])
+assert WIDOM_RESULT_DTYPE.itemsize == C.sizeof(WidomResult)
+
+# every symbol include/grx.h declares
+EXPORTS = [
+    "grx_status_string", "grx_last_error", "grx_device_count", "grx_box_create", "grx_box_destroy",
+    "grx_box_set_stream", "grx_box_set_component", "grx_box_get_component_size", "grx_box_get_positions",
+    "grx_box_get_exclusion", "grx_trial_energies", "grx_single_body_energy", "grx_ewald_sizes",
+    "grx_ewald_total", "grx_ewald_set_structure_factors", "grx_ewald_get_structure_factors",
+    "grx_ewald_delta", "grx_ewald_commit", "grx_total_energy", "grx_cbmc_select",
+    "grx_widom_insertions", "grx_widom_insertions_async", "grx_launch_count",
+]
+
+_lib = None
+
+
+def build():
+    from . import build as _b
+    return _b.build()
+
+
+def load(path=LIB_PATH):
+    """Load libgrx.so; raises if it is missing (no fallback path exists)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise GrxError(f"libgrx.so not built at {path}; run graspa_gb300.build")
+    L = C.CDLL(path)
+    P = C.POINTER
+    L.grx_status_string.restype = C.c_char_p
+    L.grx_status_string.argtypes = [C.c_int32]
+    L.grx_last_error.restype = C.c_char_p
+    L.grx_device_count.argtypes = [P(C.c_int32)]
+    L.grx_box_create.argtypes = [P(BoxDesc), P(C.c_void_p)]
+    L.grx_box_destroy.argtypes = [C.c_void_p]
+    L.grx_box_set_stream.argtypes = [C.c_void_p, C.c_void_p]
+    L.grx_box_set_component.argtypes = [C.c_void_p, C.c_int32, P(Atoms), C.c_int32]
+    L.grx_box_get_component_size.argtypes = [C.c_void_p, C.c_int32, P(C.c_size_t)]
+    L.grx_box_get_positions.argtypes = [C.c_void_p, C.c_int32, _dp, C.c_size_t]
+    L.grx_box_get_exclusion.argtypes = [C.c_void_p, C.c_int32, _dp, _dp]
+    L.grx_trial_energies.argtypes = [C.c_void_p, P(Trials), C.c_int32, C.c_int64, C.c_int64, C.c_int32,
+                                     P(TrialEnergy), _u8p]
+    L.grx_single_body_energy.argtypes = [C.c_void_p, P(Trials), P(Trials), C.c_int32, C.c_int32, C.c_int32,
+                                         C.c_int32, _dp, _u8p]
+    L.grx_ewald_sizes.argtypes = [C.c_void_p, P(C.c_int64), P(C.c_int64)]
+    L.grx_ewald_total.argtypes = [C.c_void_p, _dp]
+    L.grx_ewald_set_structure_factors.argtypes = [C.c_void_p, _dp, _dp]
+    L.grx_ewald_get_structure_factors.argtypes = [C.c_void_p, _dp, _dp, _dp]
+    L.grx_ewald_delta.argtypes = [C.c_void_p, C.c_int32, C.c_int32, _dp, _dp, C.c_size_t, _dp, _dp,
+                                  C.c_size_t, C.c_double, _dp]
+    L.grx_ewald_commit.argtypes = [C.c_void_p, C.c_int32]
+    L.grx_total_energy.argtypes = [C.c_void_p, P(Energy)]
+    L.grx_cbmc_select.argtypes = [_dp, C.c_int32, C.c_uint64, C.c_uint32, C.c_uint64, C.c_int32,
+                                  P(C.c_int32), _dp]
+    L.grx_widom_insertions.argtypes = [C.c_void_p, P(WidomDesc), C.c_uint64, C.c_size_t, C.c_int32, C.c_void_p]
+    L.grx_widom_insertions_async.argtypes = [C.c_void_p, P(WidomDesc), C.c_uint64, C.c_size_t, C.c_int32,
+                                             C.c_void_p]
+    L.grx_launch_count.restype = C.c_uint64
+    _lib = L
+    return L
+
+
+def check(status, what=""):
+    if status != 0:
+        L = load()
+        raise GrxError(f"{what}: {L.grx_status_string(status).decode()} ({L.grx_last_error().decode()})")
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _sz(a):
+    return a.ctypes.data_as(_szp)
+
+
+def geometry_from_system(system):
+    """Boxsize geometry: inverse, volume, cubic flag (maths.cuh inverse_matrix /
+    matrix_determinant, read_data.cpp:2020-2025) and the LAMMPS reciprocal cutoff
+    (read_data.cpp:664-687)."""
+    g = BoxGeometry()
+    cell = np.array(system["cell"], dtype=np.float64)
+    x = cell
+    m11, m21, m31 = x[0], x[3], x[6]
+    m12, m22, m32 = x[1], x[4], x[7]
+    m13, m23, m33 = x[2], x[5], x[8]
+    det = m11 * (m22 * m33 - m23 * m32) - m12 * (m21 * m33 - m23 * m31) + m13 * (m21 * m32 - m22 * m31)
+    inv = [0.0] * 9
+    inv[0] = (m22 * m33 - m32 * m23) / det
+    inv[3] = -(m21 * m33 - m31 * m23) / det
+    inv[6] = (m21 * m32 - m31 * m22) / det
+    inv[1] = -(m12 * m33 - m32 * m13) / det
+    inv[4] = (m11 * m33 - m31 * m13) / det
+    inv[7] = -(m11 * m32 - m31 * m12) / det
+    inv[2] = (m12 * m23 - m22 * m13) / det
+    inv[5] = -(m11 * m23 - m21 * m13) / det
+    inv[8] = (m11 * m22 - m21 * m12) / det
+    for i in range(9):
+        g.cell[i] = float(cell[i])
+        g.inverse_cell[i] = inv[i]
+    g.volume = det
+    g.cubic = 0 if (abs(x[3]) + abs(x[6]) + abs(x[7])) > 1e-10 else 1
+    g.use_lammps_ewald = int(system.get("use_lammps_ewald", 1))
+    for i in range(3):
+        g.kmax[i] = int(system["kmax"][i])
+    g.alpha = float(system["alpha"])
+    g.prefactor = float(system.get("prefactor", 138935.483496))
+    if system.get("reciprocal_cutoff") is not None:
+        g.reciprocal_cutoff = float(system["reciprocal_cutoff"])
+    else:
+        two_pi = 2 * 3.14159265358979323846
+        lx, ly, lz = x[0], x[4], x[8]
+        kvx = g.kmax[0] * (two_pi / lx)
+        kvy = g.kmax[0] * (two_pi * (-0.0) / lx / ly) + g.kmax[1] * (two_pi / ly)
+        kvz = g.kmax[0] * 0.0 + g.kmax[1] * 0.0 + g.kmax[2] * (two_pi / lz)
+        g.reciprocal_cutoff = max(kvx * kvx, kvy * kvy, kvz * kvz) * 1.00001
+    return g
+
+
+class Box:
+    """Device-resident box (one grx_box)."""
+
+    def __init__(self, system, capacity=None):
+        L = load()
+        self.L = L
+        self.system = system
+        nt = int(system["ntypes"])
+        self._eps = np.ascontiguousarray(system["epsilon"], dtype=np.float64)
+        self._sig = np.ascontiguousarray(system["sigma"], dtype=np.float64)
+        self._shift = np.ascontiguousarray(system["shift"], dtype=np.float64)
+        d = BoxDesc()
+        d.geometry = geometry_from_system(system)
+        ff = ForceField()
+        ff.ntypes = nt
+        ff.use_1264 = 0
+        ff.epsilon, ff.sigma, ff.shift = _d(self._eps), _d(self._sig), _d(self._shift)
+        ff.z = _dp()
+        ff.c10 = _dp()
+        ff.no_charges = int(system.get("no_charges", 0))
+        ff.vdw_real_bias = int(system.get("vdw_real_bias", 1))
+        ff.overlap_criteria = float(system.get("overlap_criteria", 1e6))
+        ff.cutoff_vdw_sq = float(system["cutoff_vdw"]) ** 2
+        ff.cutoff_coul_sq = float(system["cutoff_coul"]) ** 2
+        d.forcefield = ff
+        cs = system["comp_start"]
+        ncomp = len(cs) - 1
+        d.ncomponents = ncomp
+        d.nhost_components = int(system["nhost"])
+        for c in range(ncomp):
+            n = cs[c + 1] - cs[c]
+            ms = int(system["molsize"][c])
+            cap = capacity[c] if capacity is not None else max(n, ms)
+            d.capacity[c] = max(cap, ms)
+            d.molsize[c] = ms
+        self.desc = d
+        self.ncomp = ncomp
+        self.nhost = int(system["nhost"])
+        h = C.c_void_p()
+        check(L.grx_box_create(C.byref(d), C.byref(h)), "grx_box_create")
+        self.h = h
+        for c in range(ncomp):
+            self.set_component(c)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.grx_box_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_component(self, c, rigid=None):
+        s = self.system
+        a0, a1 = s["comp_start"][c], s["comp_start"][c + 1]
+        n = a1 - a0
+        ms = int(s["molsize"][c])
+        pos = np.ascontiguousarray(np.asarray(s["pos"], dtype=np.float64)[a0:a1]).reshape(-1, 3)
+        q = np.ascontiguousarray(np.asarray(s["charge"], dtype=np.float64)[a0:a1])
+        ty = np.ascontiguousarray(np.asarray(s["type"])[a0:a1], dtype=np.uint64)
+        mol = np.ascontiguousarray(np.asarray(s["molid"])[a0:a1], dtype=np.uint64)
+        sc = np.ascontiguousarray(np.asarray(s["scale"], dtype=np.float64)[a0:a1])
+        scc = np.ascontiguousarray(np.asarray(s["scale_coul"], dtype=np.float64)[a0:a1])
+        stored = n
+        if n == 0 and c >= self.nhost and c in s.get("templates", {}):
+            # an empty adsorbate component still stores its molecule template
+            tm = s["templates"][c]
+            pos = np.ascontiguousarray(tm["pos"], dtype=np.float64)
+            q = np.ascontiguousarray(tm["charge"], dtype=np.float64)
+            ty = np.ascontiguousarray(tm["type"], dtype=np.uint64)
+            mol = np.zeros(ms, dtype=np.uint64)
+            sc = np.ones(ms)
+            scc = np.ones(ms)
+            stored = ms
+        pos = np.ascontiguousarray(pos.reshape(-1))
+        a = Atoms(_d(pos), _d(sc), _d(q), _d(scc), _sz(ty), _sz(mol), n, stored)
+        if rigid is None:
+            rigid = 1 if c >= self.nhost else 0
+        check(self.L.grx_box_set_component(self.h, c, C.byref(a), int(rigid)), "grx_box_set_component")
+
+    # --- Ewald ---------------------------------------------------------
+    def ewald_sizes(self):
+        nv, na = C.c_int64(), C.c_int64()
+        check(self.L.grx_ewald_sizes(self.h, C.byref(nv), C.byref(na)), "grx_ewald_sizes")
+        return nv.value, na.value
+
+    def ewald_total(self):
+        out = np.zeros(8)
+        check(self.L.grx_ewald_total(self.h, _d(out)), "grx_ewald_total")
+        return out
+
+    def structure_factors(self):
+        nv, _ = self.ewald_sizes()
+        a, b, t = np.zeros(2 * nv), np.zeros(2 * nv), np.zeros(2 * nv)
+        check(self.L.grx_ewald_get_structure_factors(self.h, _d(a), _d(b), _d(t)), "get S(k)")
+        return a, b, t
+
+    def set_structure_factors(self, s_fw, s_ads):
+        s_fw = np.ascontiguousarray(s_fw, dtype=np.float64)
+        s_ads = np.ascontiguousarray(s_ads, dtype=np.float64)
+        check(self.L.grx_ewald_set_structure_factors(self.h, _d(s_fw), _d(s_ads)), "set S(k)")
+
+    def ewald_delta(self, comp, move_type, old_pos, old_qs, new_pos, new_qs, scale_coul_new=1.0):
+        op = np.ascontiguousarray(old_pos, dtype=np.float64).reshape(-1)
+        oq = np.ascontiguousarray(old_qs, dtype=np.float64)
+        npos = np.ascontiguousarray(new_pos, dtype=np.float64).reshape(-1)
+        nq = np.ascontiguousarray(new_qs, dtype=np.float64)
+        out = np.zeros(2)
+        check(self.L.grx_ewald_delta(self.h, comp, move_type, _d(op), _d(oq), len(oq), _d(npos), _d(nq), len(nq),
+                                     scale_coul_new, _d(out)), "grx_ewald_delta")
+        return out
+
+    def ewald_commit(self, comp):
+        check(self.L.grx_ewald_commit(self.h, comp), "grx_ewald_commit")
+
+    def exclusion(self, comp):
+        a, b = C.c_double(), C.c_double()
+        check(self.L.grx_box_get_exclusion(self.h, comp, C.byref(a), C.byref(b)), "exclusion")
+        return a.value, b.value
+
+    def total_energy(self):
+        e = Energy()
+        check(self.L.grx_total_energy(self.h, C.byref(e)), "grx_total_energy")
+        return {n: getattr(e, n) for n, _ in Energy._fields_}
+
+    # --- pair energies -------------------------------------------------
+    def trial_energies(self, pos, charge, types, molid, ntrials, chainsize, component, prec=GRX_FP64,
+                       scale=None, scale_coul=None, excl_comp=-1, excl_molid=-1):
+        nb = ntrials * chainsize
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1)
+        charge = np.ascontiguousarray(charge, dtype=np.float64)
+        types = np.ascontiguousarray(types, dtype=np.uint64)
+        scale = np.ones(nb) if scale is None else np.ascontiguousarray(scale, dtype=np.float64)
+        scale_coul = np.ones(nb) if scale_coul is None else np.ascontiguousarray(scale_coul, dtype=np.float64)
+        t = Trials(_d(pos), _d(scale), _d(charge), _d(scale_coul), _sz(types), molid, ntrials, chainsize)
+        out = (TrialEnergy * ntrials)()
+        flag = np.zeros(ntrials, dtype=np.uint8)
+        check(self.L.grx_trial_energies(self.h, C.byref(t), component, excl_comp, excl_molid, prec, out,
+                                        flag.ctypes.data_as(_u8p)), "grx_trial_energies")
+        e = np.array([[o.hg_vdw, o.hg_real, o.gg_vdw, o.gg_real] for o in out])
+        return e, flag
+
+    def single_body(self, old, new, component, do_new=1, do_old=1, prec=GRX_FP64):
+        """old/new: dict(pos, charge, type, molid[, scale, scale_coul])."""
+        keep = []
+
+        def mk(m):
+            ms = len(m["charge"])
+            pos = np.ascontiguousarray(m["pos"], dtype=np.float64).reshape(-1)
+            q = np.ascontiguousarray(m["charge"], dtype=np.float64)
+            ty = np.ascontiguousarray(m["type"], dtype=np.uint64)
+            sc = np.ascontiguousarray(m.get("scale", np.ones(ms)), dtype=np.float64)
+            scc = np.ascontiguousarray(m.get("scale_coul", np.ones(ms)), dtype=np.float64)
+            keep.extend([pos, q, ty, sc, scc])
+            return Trials(_d(pos), _d(sc), _d(q), _d(scc), _sz(ty), int(m["molid"]), 1, ms)
+        to, tn = mk(old), mk(new)
+        out = np.zeros(6)
+        flag = np.zeros(1, dtype=np.uint8)
+        check(self.L.grx_single_body_energy(self.h, C.byref(to), C.byref(tn), component, do_new, do_old, prec,
+                                            _d(out), flag.ctypes.data_as(_u8p)), "grx_single_body_energy")
+        return out, int(flag[0])
+
+    # --- CBMC ----------------------------------------------------------
+    def widom(self, desc, first_move, n, prec=GRX_MIXED, out=None):
+        res = np.zeros(n, dtype=WIDOM_RESULT_DTYPE) if out is None else out
+        check(self.L.grx_widom_insertions(self.h, C.byref(desc), first_move, n, prec,
+                                          C.c_void_p(res.ctypes.data)), "grx_widom_insertions")
+        return res
+
+    def widom_async(self, desc, first_move, n, prec, dev_ptr):
+        check(self.L.grx_widom_insertions_async(self.h, C.byref(desc), first_move, n, prec, C.c_void_p(dev_ptr)),
+              "grx_widom_insertions_async")
+
+    def set_stream(self, stream_ptr):
+        check(self.L.grx_box_set_stream(self.h, C.c_void_p(stream_ptr)), "grx_box_set_stream")
+
+
+def beta_from_temperature(T):
+    """1/(kB T) in internal units, the expression of Setup_Box_Temperature_Pressure
+    (fxn_main.h:117) with the Units constants of data_struct.h:54-64."""
+    kB, mass, length, time = 1.380649e-23, 1.6605402e-27, 1e-10, 1e-12
+    return 1.0 / (kB / (mass * pow(length, 2) / pow(time, 2)) * T)
+
+
+def widom_desc(system, component, ntrials=10, norient=10, temperature=None, seed=42, stream=0,
+               scale=1.0, scale_coul=1.0, tail_delta=0.0):
+    T = temperature if temperature is not None else system.get("temperature", 300.0)
+    d = WidomDesc()
+    d.component = component
+    d.ntrials = ntrials
+    d.norient = norient
+    d.scale = scale
+    d.scale_coul = scale_coul
+    d.beta = beta_from_temperature(T)
+    d.tail_delta = tail_delta
+    d.seed = seed
+    d.stream = stream
+    return d
+
+
+def cbmc_select(logw, seed, stream, move, word):
+    L = load()
+    lw = np.ascontiguousarray(logw, dtype=np.float64)
+    sel = C.c_int32()
+    s = C.c_double()
+    check(L.grx_cbmc_select(_d(lw), len(lw), seed, stream, move, word, C.byref(sel), C.byref(s)), "grx_cbmc_select")
+    return sel.value, s.value
+
+
+def launch_count():
+    return load().grx_launch_count()

@@ -1,0 +1,219 @@
+"""Seeded synthetic systems for the benchmark configurations.
+
+No dataset is involved: each generator builds the framework, force field and
+adsorbate templates from the stated sizes and distributions with a seeded
+Philox bit generator (numpy.random.Philox), so the same seed gives the same
+system on every machine.
+
+A system is a plain dict (the layout the C-ABI wrapper and the test oracle both
+read):
+  cell[9]            column-major cell matrix (gRASPA Boxsize.Cell layout)
+  kmax[3], alpha     Ewald parameters (LAMMPS-style explicit alpha/kmax)
+  ntypes, type_names, epsilon/sigma/shift (ntypes^2, internal units, mixed)
+  cutoff_vdw, cutoff_coul  (Angstrom, not squared)
+  nhost              number of host (framework) components
+  comp_start         component offsets into the atom arrays
+  pos (N,3), scale, charge, scale_coul, type, molid   per atom
+  molsize            atoms per molecule for every component
+  templates          {component: dict(pos, charge, type)} molecule definitions
+"""
+import math
+
+import numpy as np
+
+K_PER_INTERNAL = 1.20272430057   # energy unit conversion used for epsilon (K -> 10 J/mol)
+COULOMB_PREFACTOR = 138935.483496
+
+
+def _rng(seed):
+    return np.random.Generator(np.random.Philox(seed))
+
+
+def mix_lorentz_berthelot(eps_K, sigma, shifted, cutoff):
+    """Lorentz-Berthelot mixing with optional cutoff shift (gRASPA read_data.cpp
+    Mixing_Rule_Epsilon / Mixing_rule_Sigma / Get_Shifted_Value)."""
+    n = len(eps_K)
+    eps = np.zeros(n * n)
+    sig = np.zeros(n * n)
+    shift = np.zeros(n * n)
+    rc2 = cutoff * cutoff
+    for i in range(n):
+        for j in range(n):
+            ep = math.sqrt(eps_K[i] * eps_K[j]) / K_PER_INTERNAL
+            sg = 0.5 * (sigma[i] + sigma[j])
+            eps[i * n + j] = ep
+            sig[i * n + j] = sg
+            if shifted[i] and shifted[j]:
+                t = rc2 / (sg * sg)
+                rri3 = 1.0 / (t * t * t)
+                shift[i * n + j] = 4.0 * ep * (rri3 * (rri3 - 1.0))
+    return eps, sig, shift
+
+
+def orthorhombic_cell(a, b, c):
+    return [a, 0.0, 0.0, 0.0, b, 0.0, 0.0, 0.0, c]
+
+
+def triclinic_cell(a, b, c, alpha_deg, beta_deg, gamma_deg):
+    """Cell matrix from lengths and angles (gRASPA read_data.cpp:1536-1547 layout)."""
+    deg = 180.0 / 3.14159265358979323846
+    al, be, ga = alpha_deg / deg, beta_deg / deg, gamma_deg / deg
+    ay = b * math.sin(ga)
+    tempd = (math.cos(al) - math.cos(ga) * math.cos(be)) / math.sin(ga)
+    az = c * math.sqrt(max(1 - math.cos(be) ** 2 - tempd ** 2, 1e-12))
+    return [a, 0.0, 0.0, b * math.cos(ga), ay, 0.0, c * math.cos(be), c * tempd, az]
+
+
+def perpendicular_widths(cell):
+    h = np.array(cell, dtype=np.float64).reshape(3, 3).T   # columns a, b, c
+    vol = abs(np.linalg.det(h))
+    a, b, c = h[:, 0], h[:, 1], h[:, 2]
+    return np.array([vol / np.linalg.norm(np.cross(b, c)), vol / np.linalg.norm(np.cross(c, a)),
+                     vol / np.linalg.norm(np.cross(a, b))])
+
+
+def co2_template():
+    """Rigid linear CO2, C first then the two O at +/-1.16 A (the bead order of
+    gRASPA's Examples/Henrys_coefficient/CO2.def)."""
+    return dict(pos=np.array([[0.0, 0.0, 0.0], [0.0, 0.0, 1.16], [0.0, 0.0, -1.16]]),
+                charge=np.array([0.70, -0.35, -0.35]), names=["C_co2", "O_co2", "O_co2"])
+
+
+def silica_co2(seed=42, cells=(2, 2, 3), cutoff=12.0, alpha=0.265, kmax=(9, 9, 6), n_co2=0):
+    """Widom / GCMC system of the CO2 + synthetic all-silica configuration.
+
+    Framework: cells of 20.09 x 19.74 x 13.14 A, 96 Si + 192 O per cell. Si sit on a
+    jittered lattice (+/-0.1 A): per cell a 6 x 6 x 4 grid of sites (3.35 x 3.29 x
+    3.29 A spacing) whose two middle planes along a (i = 2, 3) are left empty, so
+    4 x 6 x 4 = 96 sites remain and every cell carries one 10 A slit pore between
+    silica walls. Every Si bonds to its +b and +c neighbours (2 bonds per Si, 192
+    per cell); each bond carries one O at its midpoint (Si-O 1.65 A) jittered by
+    +/-0.1 A. Charges Si +2.05, O -1.025 (neutral). LJ: Si 22 K / 2.30 A, O 53 K /
+    3.30 A; CO2 C 27 K / 2.80 A, q +0.70, O 79 K / 3.05 A, q -0.35;
+    Lorentz-Berthelot, shifted at the cutoff.
+    """
+    g = _rng(seed)
+    ca, cb, cc = 20.09, 19.74, 13.14
+    na, nb, nc = cells
+    A, B, Cc = ca * na, cb * nb, cc * nc
+    keep_i = [0, 1, 4, 5]
+    gy, gz = 6 * nb, 4 * nc
+    L = np.array([A, B, Cc])
+    si = {}
+    for ci in range(na):
+        for ii in keep_i:
+            for j in range(gy):
+                for k in range(gz):
+                    si[(ci, ii, j, k)] = np.array([(ci * 6 + ii + 0.5) * ca / 6,
+                                                   (j + 0.5) * B / gy, (k + 0.5) * Cc / gz])
+    keys = sorted(si)
+    jit = g.uniform(-0.1, 0.1, size=(len(keys), 3))
+    for n, key in enumerate(keys):
+        si[key] = si[key] + jit[n]
+    oxy = []
+    for (ci, ii, j, k) in keys:
+        p = si[(ci, ii, j, k)]
+        for q in (si[(ci, ii, (j + 1) % gy, k)], si[(ci, ii, j, (k + 1) % gz)]):
+            d = q - p
+            d -= L * np.round(d / L)
+            oxy.append(p + 0.5 * d)
+    oxy = np.array(oxy) + g.uniform(-0.1, 0.1, size=(len(oxy), 3))
+    si = np.array([si[k] for k in keys])
+    fw = np.concatenate([si, oxy])
+    fw = fw - L * np.floor(fw / L)
+    nsi, no = len(si), len(oxy)
+    names = ["Si", "O", "C_co2", "O_co2"]
+    eps_K = [22.0, 53.0, 27.0, 79.0]
+    sig = [2.30, 3.30, 2.80, 3.05]
+    eps, sg, shift = mix_lorentz_berthelot(eps_K, sig, [1, 1, 1, 1], cutoff)
+    fw_type = np.array([0] * nsi + [1] * no)
+    fw_q = np.array([2.05] * nsi + [-1.025] * no)
+    tmpl = co2_template()
+    tmpl["type"] = np.array([2, 3, 3])
+    system = dict(
+        name="co2_silica", cell=orthorhombic_cell(A, B, Cc), kmax=list(kmax), alpha=alpha,
+        use_lammps_ewald=1, prefactor=COULOMB_PREFACTOR, ntypes=4, type_names=names,
+        epsilon=eps, sigma=sg, shift=shift, cutoff_vdw=cutoff, cutoff_coul=cutoff,
+        overlap_criteria=1e6, no_charges=0, vdw_real_bias=1, temperature=300.0, nhost=1,
+        molsize=[len(fw), 3], templates={1: tmpl})
+    _set_atoms(system, fw, fw_type, fw_q, [np.zeros((0, 3))])
+    if n_co2:
+        place_molecules(system, 1, n_co2, g)
+    return system
+
+
+def _set_atoms(system, fw_pos, fw_type, fw_q, guest_pos_list):
+    """Concatenate framework + guest components into the per-atom arrays."""
+    pos = [np.asarray(fw_pos, dtype=np.float64)]
+    typ = [np.asarray(fw_type, dtype=np.int64)]
+    q = [np.asarray(fw_q, dtype=np.float64)]
+    molid = [np.zeros(len(fw_pos), dtype=np.int64)]
+    comp_start = [0, len(fw_pos)]
+    for c, gp in enumerate(guest_pos_list, start=1):
+        tm = system["templates"][c]
+        ms = len(tm["charge"])
+        gp = np.asarray(gp, dtype=np.float64).reshape(-1, 3)
+        nmol = len(gp) // ms
+        pos.append(gp)
+        typ.append(np.tile(tm["type"], nmol))
+        q.append(np.tile(tm["charge"], nmol))
+        molid.append(np.repeat(np.arange(nmol, dtype=np.int64), ms))
+        comp_start.append(comp_start[-1] + len(gp))
+    system["pos"] = np.concatenate(pos)
+    system["type"] = np.concatenate(typ)
+    system["charge"] = np.concatenate(q)
+    system["molid"] = np.concatenate(molid)
+    n = len(system["pos"])
+    system["scale"] = np.ones(n)
+    system["scale_coul"] = np.ones(n)
+    system["comp_start"] = comp_start
+
+
+def guest_positions(system, comp):
+    s, e = system["comp_start"][comp], system["comp_start"][comp + 1]
+    return system["pos"][s:e]
+
+
+def place_molecules(system, comp, n, g, min_dist=2.6, max_tries=200000):
+    """Place n rigid molecules of component `comp` at random positions/orientations
+    that keep every atom `min_dist` from framework and other guest atoms."""
+    tm = system["templates"][comp]
+    cell = np.array(system["cell"]).reshape(3, 3).T
+    inv = np.linalg.inv(cell)
+    fw = system["pos"][: system["comp_start"][system["nhost"]]]
+    placed = [guest_positions(system, c) for c in range(1, len(system["comp_start"]) - 1)]
+    new = []
+    tries = 0
+    while len(new) < n and tries < max_tries:
+        tries += 1
+        com = cell @ g.uniform(0, 1, 3)
+        q = g.normal(size=4)
+        q /= np.linalg.norm(q)
+        w, x, y, z = q
+        R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                      [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                      [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+        mol = (tm["pos"] - tm["pos"][0]) @ R.T + com
+        others = [fw] + [p for p in placed if len(p)] + ([np.concatenate(new)] if new else [])
+        allp = np.concatenate(others) if others else np.zeros((0, 3))
+        ok = True
+        for a in mol:
+            d = allp - a
+            s = d @ inv.T
+            s -= np.round(s)
+            d = s @ cell.T
+            if len(d) and np.min(np.einsum("ij,ij->i", d, d)) < min_dist * min_dist:
+                ok = False
+                break
+        if ok:
+            new.append(mol)
+    guests = []
+    for c in range(1, len(system["comp_start"]) - 1):
+        gp = guest_positions(system, c)
+        if c == comp and new:
+            gp = np.concatenate([gp] + new)
+        guests.append(gp)
+    fw_type = system["type"][: len(fw)]
+    fw_q = system["charge"][: len(fw)]
+    _set_atoms(system, fw, fw_type, fw_q, guests)
+    return len(new)

@@ -1,0 +1,284 @@
+/*
+ * grx.h -- C ABI of the GB300 CBMC trial-energy engine (libgrx.so).
+ *
+ * The engine replaces the bodies of gRASPA's energy calls on the Monte Carlo hot
+ * path: the CBMC trial pair energies, the single-molecule move delta, the Ewald
+ * Fourier-space delta and structure-factor commit, Rosenbluth trial selection,
+ * and the FP64 totals used for drift checks. Each entry point below names the
+ * gRASPA interface (file:line in src_clean/) whose contract it keeps.
+ *
+ * Conventions (the reference's):
+ *   - energies in internal units (10 J/mol); epsilon tables already divided by
+ *     1.20272430057 (read_data.cpp:1200); cutoffs passed SQUARED
+ *     (ForceField.CutOffVDW / CutOffCoul, data_struct.h:850-851);
+ *   - cell matrices column-major as Boxsize.Cell (read_data.cpp:1545-1547);
+ *   - positions are double3 triples (Atoms.pos), types and molecule ids size_t.
+ *
+ * Memory: every pointer argument may be host or device memory (CUDA unified
+ * addressing; the library copies with cudaMemcpyDefault). The library owns all
+ * device allocations of a box from grx_box_create until grx_box_destroy.
+ * Errors: every call returns a grx_status; nothing calls exit() or traps.
+ * Threading: a box must not be used by two host threads at once; distinct boxes
+ * are independent. All work of a box is issued on the box's CUDA stream
+ * (grx_box_set_stream); calls return after that work has finished unless the
+ * name ends in _async.
+ */
+#ifndef GRX_H
+#define GRX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t grx_status;
+#define GRX_OK 0
+#define GRX_ERR_INVALID_ARG 1
+#define GRX_ERR_CUDA 2
+#define GRX_ERR_OUT_OF_MEMORY 3
+#define GRX_ERR_TIMEOUT 4
+#define GRX_ERR_CAPACITY 5
+#define GRX_ERR_NO_DEVICE 6
+#define GRX_ERR_UNSUPPORTED 7
+
+#define GRX_MAX_COMPONENTS 8
+#define GRX_MAX_TYPES 32
+#define GRX_MAX_TRIAL_BEADS 256
+#define GRX_MAX_MOLSIZE 64
+
+/* Arithmetic of the pair and Ewald evaluation.
+ *   GRX_FP64  : every operation in FP64 (the reference's arithmetic).
+ *   GRX_MIXED : FP32 cutoff screening on split hi/lo coordinates; pairs inside
+ *               the cutoff re-evaluated from an FP64 displacement; LJ in FP32
+ *               (FP64 inside 1.1 sigma), real-space Coulomb and all sums in
+ *               FP64; Ewald delta in FP64. Boltzmann weights agree with FP64
+ *               to beta*|dE| <= 1e-6.
+ *   GRX_FP32  : FP32 pair math with FP64 sums; fastest, error reported, not
+ *               within 1e-6 for charged systems. */
+typedef enum { GRX_FP64 = 0, GRX_MIXED = 1, GRX_FP32 = 2 } grx_precision;
+
+/* Move types, numbered as gRASPA's MoveTypes (data_struct.h:20). */
+enum {
+  GRX_MOVE_TRANSLATION = 0,
+  GRX_MOVE_ROTATION = 1,
+  GRX_MOVE_SINGLE_INSERTION = 2,
+  GRX_MOVE_SINGLE_DELETION = 3,
+  GRX_MOVE_SPECIAL_ROTATION = 4,
+  GRX_MOVE_INSERTION = 5,
+  GRX_MOVE_DELETION = 6,
+  GRX_MOVE_REINSERTION = 7
+};
+
+typedef struct grx_box grx_box; /* opaque, device-resident state of one box */
+
+/* Geometry + Ewald parameters of a box: the fields of Boxsize
+ * (data_struct.h:865-886) that the path reads. */
+typedef struct {
+  double cell[9];
+  double inverse_cell[9];
+  double volume;
+  int32_t cubic;
+  int32_t use_lammps_ewald;
+  int32_t kmax[3];
+  int32_t pad_;
+  double alpha;
+  double prefactor;          /* 138935.483496 (read_data.cpp:611) */
+  double reciprocal_cutoff;  /* Boxsize.ReciprocalCutOff */
+} grx_box_geometry;
+
+/* Force field: ForceField (data_struct.h:838-855); tables ntypes*ntypes. */
+typedef struct {
+  int32_t ntypes;
+  int32_t use_1264;
+  const double* epsilon;
+  const double* sigma;
+  const double* z;     /* may be NULL (zeros) */
+  const double* shift;
+  const double* c10;   /* may be NULL (zeros) */
+  int32_t no_charges;
+  int32_t vdw_real_bias;
+  double overlap_criteria;
+  double cutoff_vdw_sq;
+  double cutoff_coul_sq;
+} grx_forcefield;
+
+typedef struct {
+  grx_box_geometry geometry;
+  grx_forcefield forcefield;
+  int32_t ncomponents;        /* NComponents.x */
+  int32_t nhost_components;   /* NComponents.y */
+  size_t capacity[GRX_MAX_COMPONENTS];  /* Atoms.Allocate_size per component */
+  size_t molsize[GRX_MAX_COMPONENTS];   /* Moleculesize per component */
+} grx_box_desc;
+
+/* Atoms of one component: Atoms (data_struct.h:788-799). */
+typedef struct {
+  const double* pos;        /* 3*n */
+  const double* scale;
+  const double* charge;
+  const double* scale_coul;
+  const size_t* type;
+  const size_t* molid;
+  size_t size;              /* live atoms (Atoms.size) */
+  size_t n_stored;          /* atoms present in the arrays (>= size; an empty
+                               component still stores its molecule template) */
+} grx_atoms;
+
+/* Trial beads of one CBMC step: Simulations.New after
+ * get_random_trial_position / get_random_trial_orientation (mc_widom.h:122-303). */
+typedef struct {
+  const double* pos;        /* 3 * ntrials * chainsize */
+  const double* scale;
+  const double* charge;
+  const double* scale_coul;
+  const size_t* type;
+  size_t molid;             /* NewMol.MolID[0] */
+  size_t ntrials;
+  size_t chainsize;
+} grx_trials;
+
+typedef struct {
+  double hg_vdw, hg_real, gg_vdw, gg_real;
+} grx_trial_energy;
+
+typedef struct {
+  double hh_vdw, hh_real, hg_vdw, hg_real, gg_vdw, gg_real;
+  double hh_ewald, hg_ewald, gg_ewald;   /* Fourier - self - exclusion, per block */
+} grx_energy;
+
+/* One batched Widom / CBMC insertion job into a static box (insertion branch of
+ * Insertion_Body, mc_swap_utilities.h:3-132, called by InsertionMove::WidomMove,
+ * move_struct.h:90-95). */
+typedef struct {
+  int32_t component;        /* inserted adsorbate component */
+  int32_t ntrials;          /* NumberWidomTrials */
+  int32_t norient;          /* NumberWidomTrialsOrientations */
+  int32_t pad_;
+  double scale;             /* proposed_scale.x (1 for a full molecule) */
+  double scale_coul;        /* proposed_scale.y */
+  double beta;              /* 1/(kB T), internal units */
+  double tail_delta;        /* TailCorrectionDifference of one insertion */
+  uint64_t seed;            /* Philox4x32-10 key */
+  uint32_t stream;          /* counter word 3 (box / job id) */
+  uint32_t pad2_;
+} grx_widom_desc;
+
+typedef struct {
+  double rosenbluth;
+  double w_first;
+  double w_chain;
+  double e_first[4];        /* hg_vdw hg_real gg_vdw gg_real of the chosen first bead */
+  double e_chain[4];
+  double ewald[2];          /* {same - exclusion, 2*cross} */
+  int64_t sel_first;        /* chosen first-bead trial (index into all trials) */
+  int64_t sel_orient;
+  int64_t n_ok_first;       /* trials without overlap */
+  int64_t n_ok_orient;
+  int32_t success;
+  int32_t pad_;
+} grx_widom_result;
+
+/* ---- lifecycle ---------------------------------------------------------- */
+const char* grx_status_string(grx_status s);
+const char* grx_last_error(void);  /* detail of the last failing call (thread-local) */
+grx_status grx_device_count(int32_t* n);
+
+/* Allocates the device state of one box (replaces the per-box allocations of
+ * fxn_main.h:46-113,163-280 / main.cpp:243-300). */
+grx_status grx_box_create(const grx_box_desc* desc, grx_box** out);
+grx_status grx_box_destroy(grx_box* box);
+/* All later work of the box goes to this stream (cudaStream_t, NULL = default). */
+grx_status grx_box_set_stream(grx_box* box, void* cuda_stream);
+
+/* Uploads one component's atoms (the device copies of Simulations.d_a[comp],
+ * fxn_main.h:46-113). For rigid components the FP64 exclusion constants are
+ * computed from the first molecule (Calculate_Exclusion_Energy_Rigid,
+ * ewald_preparation.h:351-366). */
+grx_status grx_box_set_component(grx_box* box, int32_t comp, const grx_atoms* atoms,
+                                 int32_t rigid);
+grx_status grx_box_get_component_size(grx_box* box, int32_t comp, size_t* size);
+grx_status grx_box_get_positions(grx_box* box, int32_t comp, double* pos_out, size_t n);
+grx_status grx_box_get_exclusion(grx_box* box, int32_t comp, double* intra, double* self);
+
+/* ---- pair energies ------------------------------------------------------ */
+/* Per-trial host-guest and guest-guest VDW + real Coulomb energies and overlap
+ * flags: Calculate_Multiple_Trial_Energy_VDWReal (VDW_Coulomb.cu:1183-1352) plus
+ * the per-trial block sums of Host_sum_Widom_HGGG_SEPARATE (mc_widom.h:42-87),
+ * i.e. the pair part of CBMC_PairwiseInteractions (mc_widom.h:89-119). Atoms of
+ * (component, trials->molid) and of (exclude_comp, exclude_molid) are skipped
+ * (ExcludeList[0]); pass -1 for no exclusion. */
+grx_status grx_trial_energies(grx_box* box, const grx_trials* trials, int32_t component,
+                              int64_t exclude_comp, int64_t exclude_molid,
+                              grx_precision prec, grx_trial_energy* out, uint8_t* overlap);
+
+/* New-minus-old energy of one moved molecule split HH/HG/GG and the overlap flag
+ * of the new configuration: Calculate_Single_Body_Energy_VDWReal
+ * (VDW_Coulomb.cu:626-841) with the host sums of SingleBody_Calculation
+ * (mc_single_particle.h:172-200). out6 = hh_vdw hh_real hg_vdw hg_real gg_vdw gg_real. */
+grx_status grx_single_body_energy(grx_box* box, const grx_trials* old_mol,
+                                  const grx_trials* new_mol, int32_t component,
+                                  int32_t do_new, int32_t do_old, grx_precision prec,
+                                  double* out6, uint8_t* overlap);
+
+/* ---- Ewald -------------------------------------------------------------- */
+/* Number of k slots, (kmax.x+1)(2kmax.y+1)(2kmax.z+1), and of active slots. */
+grx_status grx_ewald_sizes(grx_box* box, int64_t* nvec, int64_t* nactive);
+/* Builds the framework and adsorbate structure factors from the current atoms in
+ * FP64 and returns the Fourier totals (Ewald_Total, ewald_preparation.h:5-259,
+ * device form Ewald_TotalEnergy, Ewald_Energy_Functions.h:1272).
+ * out8 = fourier_gg fourier_hh fourier_hg self_all self_host excl_all excl_host n_active */
+grx_status grx_ewald_total(grx_box* box, double* out8);
+/* Structure factors in the reference layout (Complex[nvec], re/im interleaved):
+ * Boxsize.FrameworkEik / AdsorbateEik (Allocate_Copy_Ewald_Vector, fxn_main.h:235-280). */
+grx_status grx_ewald_set_structure_factors(grx_box* box, const double* s_fw, const double* s_ads);
+grx_status grx_ewald_get_structure_factors(grx_box* box, double* s_fw, double* s_ads,
+                                           double* s_temp);
+/* Fourier delta of one move: GPU_EwaldDifference_General
+ * (Ewald_Energy_Functions.h:438-580) with Initialize_WaveVector_General (:162) and
+ * Fourier_Ewald_Diff (:280). old/new atoms are the moved molecule before / after
+ * (positions, charge*scaleCoul). Stages S_same + dS into the temporary vector.
+ * out2 = {same-type delta minus rigid exclusion, 2 * cross-type delta}. */
+grx_status grx_ewald_delta(grx_box* box, int32_t component, int32_t move_type,
+                           const double* old_pos, const double* old_qs, size_t n_old,
+                           const double* new_pos, const double* new_qs, size_t n_new,
+                           double scale_coul_new, double* out2);
+/* Accept: make the staged structure factor current (Update_Vector_Ewald,
+ * Ewald_Energy_Functions.h:423-433). */
+grx_status grx_ewald_commit(grx_box* box, int32_t component);
+
+/* ---- totals ------------------------------------------------------------- */
+/* FP64 totals for drift checks: Total_VDW_Coulomb_Energy (VDW_Coulomb.cu:1580)
+ * + Ewald_TotalEnergy (Ewald_Energy_Functions.h:1272), split as MoveEnergy. */
+grx_status grx_total_energy(grx_box* box, grx_energy* out);
+
+/* ---- CBMC --------------------------------------------------------------- */
+/* Rosenbluth selection of SelectTrialPosition (mc_widom.h:14-39) with the
+ * uniform drawn from the engine's Philox stream (seed, stream, move, slot 2048,
+ * word). Returns the selected index and the unshifted weight sum. */
+grx_status grx_cbmc_select(const double* logw, int32_t n, uint64_t seed, uint32_t stream,
+                           uint64_t move, int32_t word, int32_t* selected, double* sum);
+
+/* Batched CBMC Widom insertions into a static box, fully on the device: trial
+ * positions, pair energies, Rosenbluth selection, orientations, pair energies,
+ * selection and the Ewald delta of the chosen configuration, one result per
+ * insertion (Widom_Move_FirstBead_PARTIAL + Widom_Move_Chain_PARTIAL,
+ * mc_widom.h:385-614, and Insertion_Body's Ewald/tail factors,
+ * mc_swap_utilities.h:94-108). Insertion i uses Philox move index first_move+i.
+ * Requires current structure factors (grx_ewald_total or _set_). */
+grx_status grx_widom_insertions(grx_box* box, const grx_widom_desc* desc,
+                                uint64_t first_move, size_t n, grx_precision prec,
+                                grx_widom_result* results);
+/* Same, asynchronous on the box stream; `results` must be device memory. */
+grx_status grx_widom_insertions_async(grx_box* box, const grx_widom_desc* desc,
+                                      uint64_t first_move, size_t n, grx_precision prec,
+                                      grx_widom_result* results);
+
+/* Number of kernel launches this process issued through the library. */
+uint64_t grx_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GRX_H */
