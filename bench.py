@@ -212,6 +212,8 @@ def accuracy_check(box, grx, system, n=200):
 
 
 def run_grx(args):
+    global N_INSERT
+    N_INSERT = args.insertions
     rank, world, local = dist_env()
     import torch
     torch.cuda.set_device(local)
@@ -271,6 +273,12 @@ def run_grx(args):
     clk = clocks.stop()
     value = te_per_step * args.steps * world / tot
     t_launch = float(np.mean(times))
+    if args.profile:
+        if rank == 0:
+            print(json.dumps({"profile_run": True, "value": value, "ms_per_step": 1000 * tot / args.steps,
+                              "insertions": N_INSERT, "launches": int(launches)}), flush=True)
+        box.close()
+        return
 
     # plain FP64 single-box form of the same workload (fewer steps: it is slower)
     fp64_steps = max(1, min(args.steps, 3))
@@ -345,6 +353,10 @@ def main():
     ap.add_argument("--impl", default="grx", choices=["grx", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64", "fp32"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--insertions", type=int, default=N_INSERT,
+                    help="insertions per step (the benchmark workload is 20000)")
+    ap.add_argument("--profile", action="store_true",
+                    help="only the timed mixed-precision steps (for profiler launch lists)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -179,7 +179,16 @@ def test_single_body_translation(grx_lib):
         import ctypes
         O.lib().ora_single_body(ctypes.byref(S.box), ctypes.byref(S.ff), ctypes.byref(S.atoms), ctypes.byref(to),
                                 ctypes.byref(tn), 1, 1, 1, O._d(ref), rf.ctypes.data_as(O._u8p))
-        assert fp64_close(got, ref), (got, ref)
+        # new - old cancels: measure against the size of the two halves
+        ref_new, ref_old = np.zeros(6), np.zeros(6)
+        O.lib().ora_single_body(ctypes.byref(S.box), ctypes.byref(S.ff), ctypes.byref(S.atoms), ctypes.byref(to),
+                                ctypes.byref(tn), 1, 1, 0, O._d(ref_new), rf.ctypes.data_as(O._u8p))
+        O.lib().ora_single_body(ctypes.byref(S.box), ctypes.byref(S.ff), ctypes.byref(S.atoms), ctypes.byref(to),
+                                ctypes.byref(tn), 1, 0, 1, O._d(ref_old), rf.ctypes.data_as(O._u8p))
+        scale = np.maximum(np.abs(ref_new) + np.abs(ref_old), 1.0)
+        assert np.all(np.abs(got - ref) <= 1e-12 * scale), (got - ref)
+        O.lib().ora_single_body(ctypes.byref(S.box), ctypes.byref(S.ff), ctypes.byref(S.atoms), ctypes.byref(to),
+                                ctypes.byref(tn), 1, 1, 1, O._d(ref), rf.ctypes.data_as(O._u8p))
         assert flag == rf[0]
         gm, _ = box.single_body(old, new, 1, prec=grx_lib.GRX_MIXED)
         assert mixed_close(gm.sum(), ref.sum())
