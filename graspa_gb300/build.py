@@ -16,7 +16,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libgrx.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["grx_box.cu", "grx_pair.cu", "grx_ewald.cu", "grx_widom.cu"]
-HEADERS = ["grx_internal.cuh", "grx_host.h"]
+HEADERS = ["grx_internal.cuh", "grx_host.h", "grx_warp.cuh"]
 
 
 def nvcc():

@@ -95,6 +95,25 @@ void refresh_dev(grx_box* b) {
   d.s_fw = b->s_fw;
   d.s_ads = b->s_ads;
   d.s_tmp = b->s_tmp;
+  d.host_end = (int)b->off[b->nhost];
+  d.tile_c = b->tile_c;
+  d.tile_r = b->tile_r;
+  d.ntiles = b->ntiles;
+  d.ctab = b->ctab;
+  d.ctab_base = b->ctab_base;
+  d.ctab_n = b->ctab_n;
+  d.ctabf = b->ctabf;
+  d.qdf = b->qdf;
+  d.ffdf = b->ffdf;
+  d.ffdf2 = b->ffdf2;
+  d.ewA = b->ewA;
+  d.ewF = b->ewF;
+  d.ewT = b->ewT;
+}
+
+static float2 split_df(double x) {
+  const float h = (float)x;
+  return make_float2(h, (float)(x - (double)h));
 }
 
 static double hi_part(double x) { return std::nearbyint(x * GRX_GRID_COORD) / GRX_GRID_COORD; }
@@ -116,6 +135,167 @@ static void pbc_host(const BoxDev& b, double* d) {
     d[1] = b.cell[1] * s[0] + b.cell[4] * s[1] + b.cell[7] * s[2];
     d[2] = b.cell[2] * s[0] + b.cell[5] * s[1] + b.cell[8] * s[2];
   }
+}
+
+// Real-space Coulomb kernel g(s) = erfc(alpha sqrt(s)) / sqrt(s) as piecewise quintic
+// polynomials in s = r^2. Pieces follow the FP32 bit pattern of s (64 per octave) from
+// s = 0.25 A^2 to just past the cutoff, so the device finds its piece with one shift of
+// the FP32 bits. Each piece is the degree-5 interpolant at Chebyshev nodes, fitted in
+// long double from erfcl; the worst relative error found on a dense sample is kept in
+// ctab_maxrel (about 1e-14 for the benchmark systems).
+static grx_status build_coulomb_table(grx_box* b, double alpha, double cut2) {
+  const float s_lo = 0.25f;
+  uint32_t lo_bits, hi_bits;
+  std::memcpy(&lo_bits, &s_lo, 4);
+  const float s_hi = (float)(cut2 * (1.0 + 1e-4) + 1e-2);
+  std::memcpy(&hi_bits, &s_hi, 4);
+  const int base = (int)(lo_bits >> 17);
+  const int n = (int)(hi_bits >> 17) - base + 2;
+  std::vector<double> tab(8 * (size_t)n);
+  const long double PI = 3.141592653589793238462643383279502884L;
+  auto g = [&](long double sv) { const long double r = sqrtl(sv); return erfcl((long double)alpha * r) / r; };
+  double maxrel = 0.0;
+  for (int k = 0; k < n; ++k) {
+    const uint32_t ab = (uint32_t)(base + k) << 17, bb = (uint32_t)(base + k + 1) << 17;
+    float fa, fb;
+    std::memcpy(&fa, &ab, 4);
+    std::memcpy(&fb, &bb, 4);
+    const long double s0 = fa, w = (long double)fb - (long double)fa;
+    long double A[6][7];
+    for (int j = 0; j < 6; ++j) {
+      const long double t = 0.5L - 0.5L * cosl((2 * j + 1) * PI / 12.0L);
+      long double p = 1.0L;
+      for (int c = 0; c < 6; ++c) { A[j][c] = p; p *= t; }
+      A[j][6] = g(s0 + w * t);
+    }
+    for (int c = 0; c < 6; ++c) {  // Gaussian elimination, partial pivoting
+      int piv = c;
+      for (int r = c + 1; r < 6; ++r)
+        if (fabsl(A[r][c]) > fabsl(A[piv][c])) piv = r;
+      for (int q = 0; q < 7; ++q) std::swap(A[c][q], A[piv][q]);
+      for (int r = 0; r < 6; ++r) {
+        if (r == c) continue;
+        const long double f = A[r][c] / A[c][c];
+        for (int q = c; q < 7; ++q) A[r][q] -= f * A[c][q];
+      }
+    }
+    double* e = &tab[8 * (size_t)k];
+    e[0] = (double)s0;
+    e[1] = (double)(1.0L / w);
+    for (int c = 0; c < 6; ++c) e[2 + c] = (double)(A[c][6] / A[c][c]);
+    for (int m = 0; m <= 16; ++m) {
+      const double sv = e[0] + (double)w * (m / 16.0);
+      const double t = (sv - e[0]) * e[1];
+      const double pv = e[2] + t * (e[3] + t * (e[4] + t * (e[5] + t * (e[6] + t * e[7]))));
+      const long double ex = g(sv);
+      maxrel = std::max(maxrel, (double)fabsl((pv - ex) / ex));
+    }
+  }
+  b->ctab_base = base;
+  b->ctab_n = n;
+  b->ctab_maxrel = maxrel;
+  // double-float copy: s0 and 1/width are exact floats (width is a power of two)
+  std::vector<float4> tf(4 * (size_t)n);
+  for (int k = 0; k < n; ++k) {
+    const double* e = &tab[8 * (size_t)k];
+    float2 c[6];
+    for (int j = 0; j < 6; ++j) {
+      const float h = (float)e[2 + j];
+      c[j] = make_float2(h, (float)(e[2 + j] - (double)h));
+    }
+    tf[4 * k + 0] = make_float4((float)e[0], (float)e[1], c[0].x, c[0].y);
+    tf[4 * k + 1] = make_float4(c[1].x, c[1].y, c[2].x, c[2].y);
+    tf[4 * k + 2] = make_float4(c[3].x, c[3].y, c[4].x, c[4].y);
+    tf[4 * k + 3] = make_float4(c[5].x, c[5].y, 0.0f, 0.0f);
+  }
+  GRX_CHECK_CUDA(cudaMalloc(&b->ctab, tab.size() * sizeof(double)), "alloc Coulomb table");
+  GRX_CHECK_CUDA(cudaMemcpy(b->ctab, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice),
+                 "upload Coulomb table");
+  GRX_CHECK_CUDA(cudaMalloc(&b->ctabf, tf.size() * sizeof(float4)), "alloc Coulomb table (float pairs)");
+  GRX_CHECK_CUDA(cudaMemcpy(b->ctabf, tf.data(), tf.size() * sizeof(float4), cudaMemcpyHostToDevice),
+                 "upload Coulomb table (float pairs)");
+  return GRX_OK;
+}
+
+static uint64_t spread3(uint32_t v) {  // 10-bit value -> every third bit
+  uint64_t x = v & 0x3ff;
+  x = (x | (x << 16)) & 0x30000ff;
+  x = (x | (x << 8)) & 0x300f00f;
+  x = (x | (x << 4)) & 0x30c30c3;
+  x = (x | (x << 2)) & 0x9249249;
+  return x;
+}
+
+// Morton order of atoms by wrapped fractional coordinates (storage slot -> caller index).
+static void morton_order(const BoxDev& d, const double* pos, size_t n, std::vector<int>& order) {
+  std::vector<uint64_t> code(n);
+  for (size_t i = 0; i < n; ++i) {
+    uint32_t q[3];
+    for (int k = 0; k < 3; ++k) {
+      double sk = d.inv[k] * pos[3 * i] + d.inv[3 + k] * pos[3 * i + 1] + d.inv[6 + k] * pos[3 * i + 2];
+      sk -= std::floor(sk);
+      q[k] = (uint32_t)std::min(1023.0, std::max(0.0, sk * 1024.0));
+    }
+    code[i] = spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
+  }
+  order.resize(n);
+  for (size_t i = 0; i < n; ++i) order[i] = (int)i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return code[a] < code[c]; });
+}
+
+// Tiles of 32 consecutive host atoms with a bounding sphere (centre from minimum
+// images relative to the tile's first atom, radius rounded up).
+static grx_status build_tiles(grx_box* b) {
+  b->h_tile_c.clear();
+  b->h_tile_r.clear();
+  for (int c = 0; c < b->nhost; ++c) {
+    const int n = b->size[c];
+    const size_t o = b->off[c];
+    for (int t0 = 0; t0 < n; t0 += 32) {
+      const int t1 = std::min(n, t0 + 32);
+      const double* a0 = &b->h_pos[3 * (o + t0)];
+      double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+      std::vector<double> u(3 * (t1 - t0));
+      for (int i = t0; i < t1; ++i) {
+        double dv[3] = {b->h_pos[3 * (o + i)] - a0[0], b->h_pos[3 * (o + i) + 1] - a0[1],
+                        b->h_pos[3 * (o + i) + 2] - a0[2]};
+        pbc_host(b->dev, dv);
+        for (int k = 0; k < 3; ++k) {
+          u[3 * (i - t0) + k] = a0[k] + dv[k];
+          lo[k] = std::min(lo[k], a0[k] + dv[k]);
+          hi[k] = std::max(hi[k], a0[k] + dv[k]);
+        }
+      }
+      const double cx = 0.5 * (lo[0] + hi[0]), cy = 0.5 * (lo[1] + hi[1]), cz = 0.5 * (lo[2] + hi[2]);
+      double r2 = 0.0;
+      for (int i = 0; i < t1 - t0; ++i) {
+        const double dx = u[3 * i] - cx, dy = u[3 * i + 1] - cy, dz = u[3 * i + 2] - cz;
+        r2 = std::max(r2, dx * dx + dy * dy + dz * dz);
+      }
+      const float rad = (float)(std::sqrt(r2) * (1.0 + 1e-6) + 1e-4);
+      b->h_tile_c.push_back(make_float4((float)cx, (float)cy, (float)cz, rad));
+      b->h_tile_r.push_back(make_int4((int)(o + t0), (int)(o + t1), c, 0));
+    }
+  }
+  b->ntiles = (int)b->h_tile_c.size();
+  if ((size_t)b->ntiles > b->tile_cap) {
+    if (b->tile_c) cudaFree(b->tile_c);
+    if (b->tile_r) cudaFree(b->tile_r);
+    b->tile_c = nullptr;
+    b->tile_r = nullptr;
+    b->tile_cap = 0;
+    GRX_CHECK_CUDA(cudaMalloc(&b->tile_c, b->ntiles * sizeof(float4)), "alloc tiles");
+    GRX_CHECK_CUDA(cudaMalloc(&b->tile_r, b->ntiles * sizeof(int4)), "alloc tile ranges");
+    b->tile_cap = b->ntiles;
+  }
+  if (b->ntiles) {
+    GRX_CHECK_CUDA(cudaMemcpy(b->tile_c, b->h_tile_c.data(), b->ntiles * sizeof(float4), cudaMemcpyHostToDevice),
+                   "upload tiles");
+    GRX_CHECK_CUDA(cudaMemcpy(b->tile_r, b->h_tile_r.data(), b->ntiles * sizeof(int4), cudaMemcpyHostToDevice),
+                   "upload tile ranges");
+  }
+  refresh_dev(b);
+  return GRX_OK;
 }
 
 // Active k slots and their prefactors: the slot unranking and cutoff test of
@@ -258,11 +438,19 @@ grx_status grx_box_create(const grx_box_desc* desc, grx_box** out) {
   d.cut_vdw2 = ff.cutoff_vdw_sq;
   d.cut_coul2 = ff.cutoff_coul_sq;
   d.overlap = ff.overlap_criteria;
+  d.overlapf = (float)ff.overlap_criteria;
   const double cmax = std::max(ff.cutoff_vdw_sq, ff.no_charges ? 0.0 : ff.cutoff_coul_sq);
-  d.screen2 = (float)(cmax * (1.0 + 1e-5) + 1e-3);
+  // FP32 screening on the hi parts (within 2^-13 A of the coordinates): guard band of
+  // 2e-3 A on the radius covers the rounding of both atoms and the FP32 arithmetic.
+  d.screen2 = (float)((std::sqrt(cmax) + 2e-3) * (std::sqrt(cmax) + 2e-3));
+  d.cut_vdw2_df = split_df(ff.cutoff_vdw_sq);
+  d.cut_coul2_df = split_df(ff.cutoff_coul_sq);
   d.cut_vdw2f = (float)ff.cutoff_vdw_sq;
   d.cut_coul2f = (float)ff.cutoff_coul_sq;
   for (int k = 0; k < 3; ++k) d.kmax[k] = g.kmax[k];
+  for (int k = 0; k < 9; ++k) d.cellf[k] = (float)g.cell[k];
+  d.cull = g.cubic ? 1 : 0;  // single-image rounding is the true minimum image only here
+  d.cull_r = (float)(std::sqrt((double)d.screen2) + 0.01);
 
   const int nt2 = ff.ntypes * ff.ntypes;
   std::vector<FFPair64> f64(nt2);
@@ -277,6 +465,15 @@ grx_status grx_box_create(const grx_box_desc* desc, grx_box** out) {
     const double s2 = ff.sigma[r] * ff.sigma[r];
     f32[r] = make_float4((float)(4.0 * ff.epsilon[r]), s2 > 0 ? (float)(1.0 / s2) : INFINITY,
                          (float)ff.shift[r], (float)(1.21 * s2));
+  }
+  std::vector<float4> fdf(nt2);
+  std::vector<float2> fdf2(nt2);
+  for (int r = 0; r < nt2; ++r) {
+    const double s2 = ff.sigma[r] * ff.sigma[r];
+    const float2 e4 = split_df(4.0 * ff.epsilon[r]);
+    const float2 is2 = s2 > 0 ? split_df(1.0 / s2) : make_float2(INFINITY, 0.0f);
+    fdf[r] = make_float4(e4.x, e4.y, is2.x, is2.y);
+    fdf2[r] = split_df(ff.shift[r]);
   }
   build_kvectors(b, g);
 
@@ -297,12 +494,18 @@ grx_status grx_box_create(const grx_box_desc* desc, grx_box** out) {
   if ((e = cudaMalloc(&b->ff64, nt2 * sizeof(FFPair64))) != cudaSuccess) return fail(e, "alloc ff64");
   if ((e = cudaMalloc(&b->ffc10, nt2 * sizeof(double))) != cudaSuccess) return fail(e, "alloc ffc10");
   if ((e = cudaMalloc(&b->ff32, nt2 * sizeof(float4))) != cudaSuccess) return fail(e, "alloc ff32");
+  if ((e = cudaMalloc(&b->ffdf, nt2 * sizeof(float4))) != cudaSuccess) return fail(e, "alloc ffdf");
+  if ((e = cudaMalloc(&b->ffdf2, nt2 * sizeof(float2))) != cudaSuccess) return fail(e, "alloc ffdf2");
+  if ((e = cudaMalloc(&b->qdf, n * sizeof(float2))) != cudaSuccess) return fail(e, "alloc qdf");
   const size_t nv = std::max(b->nvec, 1), na = std::max(b->nact, 1);
   if ((e = cudaMalloc(&b->kact, na * sizeof(int4))) != cudaSuccess) return fail(e, "alloc kact");
   if ((e = cudaMalloc(&b->ktemp, na * sizeof(double))) != cudaSuccess) return fail(e, "alloc ktemp");
   if ((e = cudaMalloc(&b->s_fw, nv * sizeof(double2))) != cudaSuccess) return fail(e, "alloc s_fw");
   if ((e = cudaMalloc(&b->s_ads, nv * sizeof(double2))) != cudaSuccess) return fail(e, "alloc s_ads");
   if ((e = cudaMalloc(&b->s_tmp, nv * sizeof(double2))) != cudaSuccess) return fail(e, "alloc s_tmp");
+  if ((e = cudaMalloc(&b->ewA, na * sizeof(float4))) != cudaSuccess) return fail(e, "alloc ewA");
+  if ((e = cudaMalloc(&b->ewF, na * sizeof(float4))) != cudaSuccess) return fail(e, "alloc ewF");
+  if ((e = cudaMalloc(&b->ewT, na * sizeof(float2))) != cudaSuccess) return fail(e, "alloc ewT");
   cudaMemset(b->pos64, 0, n * sizeof(double4));
   cudaMemset(b->hi, 0, n * sizeof(float4));
   cudaMemset(b->lo, 0, n * sizeof(float4));
@@ -316,11 +519,21 @@ grx_status grx_box_create(const grx_box_desc* desc, grx_box** out) {
   cudaMemcpy(b->ff64, f64.data(), nt2 * sizeof(FFPair64), cudaMemcpyHostToDevice);
   cudaMemcpy(b->ffc10, c10.data(), nt2 * sizeof(double), cudaMemcpyHostToDevice);
   cudaMemcpy(b->ff32, f32.data(), nt2 * sizeof(float4), cudaMemcpyHostToDevice);
+  cudaMemcpy(b->ffdf, fdf.data(), nt2 * sizeof(float4), cudaMemcpyHostToDevice);
+  cudaMemcpy(b->ffdf2, fdf2.data(), nt2 * sizeof(float2), cudaMemcpyHostToDevice);
+  cudaMemset(b->qdf, 0, n * sizeof(float2));
   if (b->nact) {
     cudaMemcpy(b->kact, b->h_kact.data(), b->nact * sizeof(int4), cudaMemcpyHostToDevice);
     cudaMemcpy(b->ktemp, b->h_ktemp.data(), b->nact * sizeof(double), cudaMemcpyHostToDevice);
   }
   if ((e = cudaDeviceSynchronize()) != cudaSuccess) return fail(e, "box upload");
+  if (!ff.no_charges) {
+    grx_status st = build_coulomb_table(b, g.alpha, ff.cutoff_coul_sq);
+    if (st) {
+      grx_box_destroy(b);
+      return st;
+    }
+  }
   refresh_dev(b);
   *out = b;
   return GRX_OK;
@@ -330,7 +543,8 @@ grx_status grx_box_destroy(grx_box* b) {
   if (!b) return GRX_OK;
   void* ptrs[] = {b->pos64, b->hi, b->lo, b->meta, b->scale, b->charge, b->d_size, b->ff64,
                   b->ffc10, b->ff32, b->kact, b->ktemp, b->s_fw, b->s_ads, b->s_tmp,
-                  b->scratch, b->d_results};
+                  b->scratch, b->d_results, b->tile_c, b->tile_r, b->ctab, b->ctabf, b->qdf,
+                  b->ffdf, b->ffdf2, b->ewA, b->ewF, b->ewT};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (b->pinned) cudaFreeHost(b->pinned);
@@ -369,44 +583,9 @@ grx_status grx_box_set_component(grx_box* b, int32_t comp, const grx_atoms* a, i
       GRX_CHECK_CUDA(cudaMemcpy(scc.data(), a->scale_coul, nst * sizeof(double), cudaMemcpyDefault),
                      "read scale_coul");
   }
-  for (size_t i = 0; i < nst; ++i)
-    if (ty[i] >= (size_t)b->dev.ntypes) {
-      set_error("grx_box_set_component: atom %zu has type %zu >= ntypes %d", i, ty[i], b->dev.ntypes);
-      return GRX_ERR_INVALID_ARG;
-    }
-  std::vector<double4> p64(nst);
-  std::vector<float4> h(nst), l(nst);
-  std::vector<int2> m(nst);
-  const size_t o = b->off[comp];
-  bool charged = false;
-  for (size_t i = 0; i < nst; ++i) {
-    const double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
-    const double qe = q[i] * scc[i];
-    p64[i] = make_double4(x, y, z, qe);
-    const double hx = hi_part(x), hy = hi_part(y), hz = hi_part(z);
-    h[i] = make_float4((float)hx, (float)hy, (float)hz, (float)qe);
-    l[i] = make_float4((float)(x - hx), (float)(y - hy), (float)(z - hz), (float)sc[i]);
-    m[i] = make_int2((int)ty[i], (int)mol[i]);
-    if (q[i] != 0.0) charged = true;
-    b->h_pos[3 * (o + i)] = x; b->h_pos[3 * (o + i) + 1] = y; b->h_pos[3 * (o + i) + 2] = z;
-    b->h_charge[o + i] = q[i];
-    b->h_scale_coul[o + i] = scc[i];
-  }
-  b->size[comp] = (int)a->size;
-  b->rigid[comp] = rigid;
-  b->has_charge[comp] = charged ? 1 : 0;
-  if (nst) {
-    GRX_CHECK_CUDA(cudaMemcpy(b->pos64 + o, p64.data(), nst * sizeof(double4), cudaMemcpyHostToDevice), "upload pos64");
-    GRX_CHECK_CUDA(cudaMemcpy(b->hi + o, h.data(), nst * sizeof(float4), cudaMemcpyHostToDevice), "upload hi");
-    GRX_CHECK_CUDA(cudaMemcpy(b->lo + o, l.data(), nst * sizeof(float4), cudaMemcpyHostToDevice), "upload lo");
-    GRX_CHECK_CUDA(cudaMemcpy(b->meta + o, m.data(), nst * sizeof(int2), cudaMemcpyHostToDevice), "upload meta");
-    GRX_CHECK_CUDA(cudaMemcpy(b->scale + o, sc.data(), nst * sizeof(double), cudaMemcpyHostToDevice), "upload scale");
-    GRX_CHECK_CUDA(cudaMemcpy(b->charge + o, q.data(), nst * sizeof(double), cudaMemcpyHostToDevice), "upload charge");
-  }
-  GRX_CHECK_CUDA(cudaMemcpy(b->d_size, b->size, GRX_MAX_COMPONENTS * sizeof(int), cudaMemcpyHostToDevice),
-                 "upload sizes");
-  // rigid exclusion constants from the first molecule: Calculate_Intra_Molecule_Exclusion
-  // and Calculate_Self_Exclusion (ewald_preparation.h:261-298), FP64.
+  // rigid exclusion constants from the first molecule in caller order:
+  // Calculate_Intra_Molecule_Exclusion and Calculate_Self_Exclusion
+  // (ewald_preparation.h:261-298), FP64.
   b->excl_intra[comp] = 0.0;
   b->excl_self[comp] = 0.0;
   const size_t ms = b->molsize[comp];
@@ -423,10 +602,68 @@ grx_status grx_box_set_component(grx_box* b, int32_t comp, const grx_atoms* a, i
       }
     }
     const double ps = b->dev.prefactor * b->dev.alpha / std::sqrt(3.14159265358979323846);
-    double s = 0.0;
-    for (size_t i = 0; i < ms; ++i) s += ps * scc[i] * q[i] * scc[i] * q[i];
+    double sv = 0.0;
+    for (size_t i = 0; i < ms; ++i) sv += ps * scc[i] * q[i] * scc[i] * q[i];
     b->excl_intra[comp] = e;
-    b->excl_self[comp] = s;
+    b->excl_self[comp] = sv;
+  }
+  // host (framework) atoms are stored in Morton order so that 32-atom tiles are compact
+  b->perm[comp].clear();
+  if (comp < b->nhost && a->size > 1) {
+    std::vector<int> order;
+    morton_order(b->dev, pos.data(), a->size, order);
+    b->perm[comp] = order;
+    std::vector<double> pos2(pos), sc2(sc), q2(q), scc2(scc);
+    std::vector<size_t> ty2(ty), mol2(mol);
+    for (size_t j = 0; j < a->size; ++j) {
+      const size_t k = (size_t)order[j];
+      for (int d = 0; d < 3; ++d) pos2[3 * j + d] = pos[3 * k + d];
+      sc2[j] = sc[k]; q2[j] = q[k]; scc2[j] = scc[k]; ty2[j] = ty[k]; mol2[j] = mol[k];
+    }
+    pos.swap(pos2); sc.swap(sc2); q.swap(q2); scc.swap(scc2); ty.swap(ty2); mol.swap(mol2);
+  }
+  for (size_t i = 0; i < nst; ++i)
+    if (ty[i] >= (size_t)b->dev.ntypes) {
+      set_error("grx_box_set_component: atom %zu has type %zu >= ntypes %d", i, ty[i], b->dev.ntypes);
+      return GRX_ERR_INVALID_ARG;
+    }
+  std::vector<double4> p64(nst);
+  std::vector<float4> h(nst), l(nst);
+  std::vector<int2> m(nst);
+  std::vector<float2> qd(nst);
+  const size_t o = b->off[comp];
+  bool charged = false;
+  for (size_t i = 0; i < nst; ++i) {
+    const double x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+    const double qe = q[i] * scc[i];
+    p64[i] = make_double4(x, y, z, qe);
+    const double hx = hi_part(x), hy = hi_part(y), hz = hi_part(z);
+    h[i] = make_float4((float)hx, (float)hy, (float)hz, (float)qe);
+    l[i] = make_float4((float)(x - hx), (float)(y - hy), (float)(z - hz), (float)sc[i]);
+    m[i] = make_int2((int)ty[i], (int)mol[i]);
+    qd[i] = split_df(qe);
+    if (q[i] != 0.0) charged = true;
+    b->h_pos[3 * (o + i)] = x; b->h_pos[3 * (o + i) + 1] = y; b->h_pos[3 * (o + i) + 2] = z;
+    b->h_charge[o + i] = q[i];
+    b->h_scale_coul[o + i] = scc[i];
+  }
+  b->size[comp] = (int)a->size;
+  b->rigid[comp] = rigid;
+  b->has_charge[comp] = charged ? 1 : 0;
+  if (nst) {
+    GRX_CHECK_CUDA(cudaMemcpy(b->pos64 + o, p64.data(), nst * sizeof(double4), cudaMemcpyHostToDevice), "upload pos64");
+    GRX_CHECK_CUDA(cudaMemcpy(b->hi + o, h.data(), nst * sizeof(float4), cudaMemcpyHostToDevice), "upload hi");
+    GRX_CHECK_CUDA(cudaMemcpy(b->lo + o, l.data(), nst * sizeof(float4), cudaMemcpyHostToDevice), "upload lo");
+    GRX_CHECK_CUDA(cudaMemcpy(b->meta + o, m.data(), nst * sizeof(int2), cudaMemcpyHostToDevice), "upload meta");
+    GRX_CHECK_CUDA(cudaMemcpy(b->scale + o, sc.data(), nst * sizeof(double), cudaMemcpyHostToDevice), "upload scale");
+    GRX_CHECK_CUDA(cudaMemcpy(b->charge + o, q.data(), nst * sizeof(double), cudaMemcpyHostToDevice), "upload charge");
+    GRX_CHECK_CUDA(cudaMemcpy(b->qdf + o, qd.data(), nst * sizeof(float2), cudaMemcpyHostToDevice), "upload qdf");
+  }
+  GRX_CHECK_CUDA(cudaMemcpy(b->d_size, b->size, GRX_MAX_COMPONENTS * sizeof(int), cudaMemcpyHostToDevice),
+                 "upload sizes");
+  if (comp < b->nhost) {
+    grx_status st = build_tiles(b);
+    if (st) return st;
   }
   b->sk_valid = false;
   return GRX_OK;
@@ -449,7 +686,12 @@ grx_status grx_box_get_positions(grx_box* b, int32_t comp, double* out, size_t n
     GRX_CHECK_CUDA(cudaMemcpy(p.data(), b->pos64 + b->off[comp], n * sizeof(double4), cudaMemcpyDeviceToHost),
                    "read positions");
   std::vector<double> flat(3 * n);
-  for (size_t i = 0; i < n; ++i) { flat[3 * i] = p[i].x; flat[3 * i + 1] = p[i].y; flat[3 * i + 2] = p[i].z; }
+  const std::vector<int>& perm = b->perm[comp];
+  for (size_t i = 0; i < n; ++i) {
+    const size_t k = (i < perm.size()) ? (size_t)perm[i] : i;  // storage slot -> caller index
+    if (k >= n) continue;
+    flat[3 * k] = p[i].x; flat[3 * k + 1] = p[i].y; flat[3 * k + 2] = p[i].z;
+  }
   if (n) GRX_CHECK_CUDA(cudaMemcpy(out, flat.data(), 3 * n * sizeof(double), cudaMemcpyDefault), "write positions");
   return GRX_OK;
 }
@@ -474,6 +716,7 @@ grx_status grx_ewald_set_structure_factors(grx_box* b, const double* s_fw, const
   GRX_CHECK_CUDA(cudaMemcpy(b->s_ads, s_ads, b->nvec * sizeof(double2), cudaMemcpyDefault), "set S_ads");
   GRX_CHECK_CUDA(cudaMemcpy(b->s_tmp, s_ads, b->nvec * sizeof(double2), cudaMemcpyDefault), "set S_tmp");
   b->sk_valid = true;
+  b->ewdf_valid = false;
   return GRX_OK;
 }
 

@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(GRX_THREADS) ewald_delta_kernel(BoxDev b, cons
   extern __shared__ double2 eik_s[];
   __shared__ double sbuf[32];
   const int na = mv->n_old + mv->n_new;
-  const int kx1 = b.kmax[0] + 1, ky1 = b.kmax[1] + 1, kz1 = b.kmax[2] + 1;
+  const int kx1 = b.kmax[0] + 1, ky1 = b.kmax[1] + 1;
   double2* ex = eik_s;
   double2* ey = ex + kx1 * na;
   double2* ez = ey + ky1 * na;
@@ -327,6 +327,7 @@ grx_status grx_ewald_total(grx_box* b, double* out8) {
   out8[3] = sa; out8[4] = sh; out8[5] = -ea; out8[6] = -eh;
   out8[7] = (double)b->nact;
   b->sk_valid = true;
+  b->ewdf_valid = false;
   return GRX_OK;
 }
 
@@ -431,6 +432,7 @@ grx_status grx_ewald_commit(grx_box* b, int32_t comp) {
   double2* dst = comp < b->nhost ? b->s_fw : b->s_ads;
   commit_kernel<<<std::max(1, std::min((b->nact + 255) / 256, sm_count(b))), 256, 0, b->stream>>>(b->dev, dst, b->s_tmp);
   count_launch();
+  b->ewdf_valid = false;
   GRX_CHECK_CUDA(cudaGetLastError(), "commit launch");
   GRX_CHECK_CUDA(cudaStreamSynchronize(b->stream), "commit");
   return GRX_OK;

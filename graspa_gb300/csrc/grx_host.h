@@ -48,6 +48,28 @@ struct grx_box {
   std::vector<double> h_ktemp;
   bool sk_valid = false;
 
+  // spatial tiles of host atoms and the storage permutation of host components
+  std::vector<float4> h_tile_c;
+  std::vector<int4> h_tile_r;
+  float4* tile_c = nullptr;
+  int4* tile_r = nullptr;
+  size_t tile_cap = 0;
+  int ntiles = 0;
+  std::vector<int> perm[GRX_MAX_COMPONENTS];  // storage slot -> caller index
+  // double-float copies for the mixed-precision pair path
+  float2* qdf = nullptr;     // q * scaleCoul per atom as hi/lo floats
+  float4* ffdf = nullptr;    // per type pair {4eps hi, lo, 1/sigma^2 hi, lo}
+  float2* ffdf2 = nullptr;   // per type pair {shift hi, lo}
+  float4* ctabf = nullptr;   // Coulomb table, 4 float4 per piece
+  float4* ewA = nullptr;     // per active k: temp * S_ads as double-float complex
+  float4* ewF = nullptr;     // per active k: temp * S_fw
+  float2* ewT = nullptr;     // per active k: temp
+  bool ewdf_valid = false;
+  // Coulomb table
+  double* ctab = nullptr;
+  int ctab_n = 0, ctab_base = 0;
+  double ctab_maxrel = 0.0;
+
   // scratch (grown on demand)
   double* scratch = nullptr;
   size_t scratch_bytes = 0;

@@ -46,6 +46,7 @@ struct BoxDev {
   double cut_coul2;
   double overlap;
   float screen2;     // FP32 screening radius^2 with guard band
+  float overlapf;    // OverlapCriteria as float
   float cut_vdw2f;
   float cut_coul2f;
   const FFPair64* ff64;  // ntypes^2
@@ -62,6 +63,29 @@ struct BoxDev {
   const int2* meta;
   const double* scale;
   const double* charge;  // bare charge (Atoms.charge), templates for trial beads
+  int host_end;          // storage index where guest components begin
+  // spatial tiles of host atoms (32 atoms each, Morton order)
+  const float4* tile_c;  // bounding sphere {x, y, z, radius}
+  const int4* tile_r;    // {first atom, end atom, component, 0}
+  int ntiles;
+  int cull;              // tile culling on (orthorhombic cells only)
+  float cull_r;          // screening radius used by the tile test
+  float cellf[9];
+  // real-space Coulomb table: g(s) = erfc(alpha sqrt s)/sqrt s, piecewise quintic in
+  // s = r^2, 64 pieces per octave indexed by the FP32 bit pattern of s
+  const double* ctab;    // per piece {s0, 1/width, c0..c5}
+  int ctab_base;
+  int ctab_n;
+  // double-float data of the mixed-precision dense path
+  const float4* ctabf;   // per piece {s0, 1/width, c0 hi, c0 lo}, {c1 hi, lo, c2 hi, lo}, ...
+  const float2* qdf;     // q * scaleCoul, hi/lo
+  const float4* ffdf;    // {4 eps hi, lo, 1/sigma^2 hi, lo}
+  const float2* ffdf2;   // {shift hi, lo}
+  float2 cut_vdw2_df;
+  float2 cut_coul2_df;
+  const float4* ewA;     // per active k {re hi, re lo, im hi, im lo} of temp * S_ads
+  const float4* ewF;     // ... of temp * S_fw
+  const float2* ewT;     // temp as double-float
   // ewald
   int kmax[3];
   int nvec;

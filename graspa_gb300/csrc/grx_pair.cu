@@ -5,35 +5,35 @@
 #include <vector>
 
 #include "grx_host.h"
+#include "grx_warp.cuh"
 
 namespace grx {
 
-// Trial energies, one pass of up to GRX_THREADS beads over an atom slice per
-// block; block partials per bead go to part[block][bead][4] and overlap flags are
-// OR-ed into flags[bead].
+// Trial energies of one bead per block (compacted pair engine, grx_warp.cuh);
+// per-bead sums go to part[bead][4] and the overlap flag to flags[bead].
 template <int PREC>
-__global__ void __launch_bounds__(GRX_THREADS) trial_pass_kernel(BoxDev b, const Bead* beads, int nb,
-                                                                 int component, int newmol,
-                                                                 int excl_comp, int excl_mol,
+__global__ void __launch_bounds__(GRX_THREADS) trial_bead_kernel(BoxDev b, const Bead* beads, int component,
+                                                                 int newmol, int excl_comp, int excl_mol,
                                                                  double* part, int* flags) {
-  __shared__ double sp[GRX_THREADS * 4];
-  const int nl = blockDim.x / nb;
-  const int tid = threadIdx.x;
-  double acc[4] = {0, 0, 0, 0};
-  int flag = 0;
-  if (tid < nl * nb) {
-    const Bead bd = beads[tid % nb];
-    bead_pass<PREC>(b, bd, blockIdx.x * nl + tid / nb, gridDim.x * nl, component, newmol, excl_comp,
-                    excl_mol, acc, flag);
-    if (flag) atomicOr(&flags[tid % nb], 1);
-  }
-  for (int q = 0; q < 4; ++q) sp[tid * 4 + q] = acc[q];
+  __shared__ double ipart[kMaxItems * 4];
+  __shared__ int iflag[kMaxItems];
+  __shared__ int qbuf[(GRX_THREADS / 32) * kQueue];
+  __shared__ int counter;
+  if (threadIdx.x == 0) counter = 0;
   __syncthreads();
-  for (int w = tid; w < nb * 4; w += blockDim.x) {
-    const int bead = w >> 2, q = w & 3;
+  const int nch = chunks_for(1, b.ntiles, GRX_THREADS / 32);
+  block_bead_pass<PREC>(b, beads + blockIdx.x, 1, component, newmol, excl_comp, excl_mol, qbuf, ipart, iflag,
+                        &counter, nch);
+  __syncthreads();
+  if (threadIdx.x < 4) {
     double s = 0.0;
-    for (int l = 0; l < nl; ++l) s += sp[(l * nb + bead) * 4 + q];
-    part[((size_t)blockIdx.x * nb + bead) * 4 + q] = s;
+    for (int c = 0; c < nch; ++c) s += ipart[c * 4 + threadIdx.x];
+    part[blockIdx.x * 4 + threadIdx.x] = s;
+  }
+  if (threadIdx.x == 0) {
+    int f = 0;
+    for (int c = 0; c < nch; ++c) f |= iflag[c];
+    flags[blockIdx.x] = f;
   }
 }
 
@@ -138,9 +138,9 @@ static grx_status stage_beads(const grx_trials* t, size_t first_bead, size_t nbe
 }
 
 template <int PREC>
-static void launch_trial_pass(grx_box* b, int nblk, const Bead* beads, int nb, int comp, int newmol,
-                              int ec, int em, double* part, int* flags) {
-  trial_pass_kernel<PREC><<<nblk, GRX_THREADS, 0, b->stream>>>(b->dev, beads, nb, comp, newmol, ec, em, part, flags);
+static void launch_trial_pass(grx_box* b, const Bead* beads, int nb, int comp, int newmol, int ec, int em,
+                              double* part, int* flags) {
+  trial_bead_kernel<PREC><<<nb, GRX_THREADS, 0, b->stream>>>(b->dev, beads, comp, newmol, ec, em, part, flags);
 }
 
 }  // namespace grx
@@ -162,8 +162,6 @@ grx_status grx_trial_energies(grx_box* b, const grx_trials* t, int32_t component
   refresh_dev(b);
   const size_t ch = t->chainsize;
   const size_t per_chunk = std::max<size_t>(1, GRX_MAX_TRIAL_BEADS / ch);
-  size_t total_atoms = 0;
-  for (int c = 0; c < b->ncomp; ++c) total_atoms += b->cap[c];
   std::vector<double> host_out;
   std::vector<int> host_flag;
   for (size_t t0 = 0; t0 < t->ntrials; t0 += per_chunk) {
@@ -172,9 +170,7 @@ grx_status grx_trial_energies(grx_box* b, const grx_trials* t, int32_t component
     std::vector<Bead> beads;
     grx_status st = stage_beads(t, t0 * ch, nb, beads);
     if (st) return st;
-    const int nl = GRX_THREADS / nb;
-    int nblk = (int)std::min<size_t>((total_atoms + (size_t)nl * 16 - 1) / ((size_t)nl * 16), 2 * (size_t)sm_count(b));
-    nblk = std::max(nblk, 1);
+    const int nblk = 1;
     const size_t bead_bytes = (nb * sizeof(Bead) + 255) / 256 * 256;
     const size_t part_bytes = ((size_t)nblk * nb * 4 * sizeof(double) + 255) / 256 * 256;
     const size_t flag_bytes = ((size_t)nb * sizeof(int) + 255) / 256 * 256;
@@ -190,9 +186,9 @@ grx_status grx_trial_energies(grx_box* b, const grx_trials* t, int32_t component
     GRX_CHECK_CUDA(cudaMemcpyAsync(d_beads, beads.data(), nb * sizeof(Bead), cudaMemcpyHostToDevice, b->stream), "upload beads");
     GRX_CHECK_CUDA(cudaMemsetAsync(flags, 0, nb * sizeof(int), b->stream), "clear flags");
     const int ec = (int)exclude_comp, em = (int)exclude_molid;
-    if (prec == GRX_FP64) launch_trial_pass<GRX_FP64>(b, nblk, d_beads, nb, component, (int)t->molid, ec, em, part, flags);
-    else if (prec == GRX_MIXED) launch_trial_pass<GRX_MIXED>(b, nblk, d_beads, nb, component, (int)t->molid, ec, em, part, flags);
-    else launch_trial_pass<GRX_FP32>(b, nblk, d_beads, nb, component, (int)t->molid, ec, em, part, flags);
+    if (prec == GRX_FP64) launch_trial_pass<GRX_FP64>(b, d_beads, nb, component, (int)t->molid, ec, em, part, flags);
+    else if (prec == GRX_MIXED) launch_trial_pass<GRX_MIXED>(b, d_beads, nb, component, (int)t->molid, ec, em, part, flags);
+    else launch_trial_pass<GRX_FP32>(b, d_beads, nb, component, (int)t->molid, ec, em, part, flags);
     trial_reduce_kernel<<<(int)((ntr * 4 + 127) / 128), 128, 0, b->stream>>>(part, flags, nblk, nb, (int)ch, d_out, d_tflag);
     count_launch(2);
     GRX_CHECK_CUDA(cudaGetLastError(), "trial energy launch");

@@ -1,0 +1,363 @@
+// grx_warp.cuh -- the trial-bead pair engine: tile culling, FP32 screening, warp
+// compaction of in-cutoff pairs and dense evaluation.
+//
+// A work item is (one trial bead, one range of host tiles [+ the guest atoms]) and is
+// processed by one warp. For every 32-atom tile the warp first tests the tile's
+// bounding sphere against the cutoff (orthorhombic cells), then screens the 32 pairs
+// (split-coordinate FP32 in the mixed/FP32 forms, full FP64 in the FP64 form). Pairs
+// inside the screening radius are appended to a per-warp ring buffer in shared
+// memory; every 32 queued pairs are evaluated by all 32 lanes together, so the costly
+// part (FP64 displacement, LJ, real-space Coulomb) runs without idle lanes. The
+// order of every sum is fixed by the ballot order, so results are deterministic.
+#pragma once
+
+#include "grx_internal.cuh"
+#include "grx_df.cuh"
+
+namespace grx {
+
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kQueue = 64;  // ring buffer entries per warp
+
+// g(s) = erfc(alpha sqrt s)/sqrt s from the piecewise quintic table; pieces are found
+// from the FP32 bits of s. Below the table (s < 0.25 A^2) the library erfc is used.
+__device__ __forceinline__ double coul_table(const BoxDev& b, float s32, double s64) {
+  const int k = (__float_as_int(s32) >> 17) - b.ctab_base;
+  if (k < 0 || k >= b.ctab_n) {
+    const double r = sqrt(s64);
+    return erfc(b.alpha * r) / r;
+  }
+  const double2* c = reinterpret_cast<const double2*>(b.ctab + 8 * k);
+  const double2 c01 = __ldg(c), c23 = __ldg(c + 1), c45 = __ldg(c + 2), c67 = __ldg(c + 3);
+  const double t = (s64 - c01.x) * c01.y;
+  return c23.x + t * (c23.y + t * (c45.x + t * (c45.y + t * (c67.x + t * c67.y))));
+}
+
+// Round to the nearest integer with two FP32 instructions (|x| < 2^22): adding
+// 1.5*2^23 moves the fraction out of the mantissa. Differs from the reference's
+// int-cast rounding only at exact half-cell ties, which lie beyond the cutoff.
+__device__ __forceinline__ float rnd(float x) {
+  return __fsub_rn(__fadd_rn(x, 12582912.0f), 12582912.0f);
+}
+
+// Minimum-image displacement on split coordinates: the image shift is applied to the
+// hi part with the grid-exact cell (exact) and to the lo part with the remainder.
+__device__ __forceinline__ void image_split(const BoxDev& b, float3& dh, float3& dl) {
+  const float x = dh.x + dl.x, y = dh.y + dl.y, z = dh.z + dl.z;
+  if (b.cubic) {
+    const float nx = rnd(x * b.invf[0]), ny = rnd(y * b.invf[4]), nz = rnd(z * b.invf[8]);
+    dh.x = __fmaf_rn(-nx, b.cell_hi[0], dh.x); dl.x = __fmaf_rn(-nx, b.cell_lo[0], dl.x);
+    dh.y = __fmaf_rn(-ny, b.cell_hi[4], dh.y); dl.y = __fmaf_rn(-ny, b.cell_lo[4], dl.y);
+    dh.z = __fmaf_rn(-nz, b.cell_hi[8], dh.z); dl.z = __fmaf_rn(-nz, b.cell_lo[8], dl.z);
+  } else {
+    const float nx = rnd(b.invf[0] * x + b.invf[3] * y + b.invf[6] * z);
+    const float ny = rnd(b.invf[1] * x + b.invf[4] * y + b.invf[7] * z);
+    const float nz = rnd(b.invf[2] * x + b.invf[5] * y + b.invf[8] * z);
+    dh.x = __fmaf_rn(-nz, b.cell_hi[6], __fmaf_rn(-ny, b.cell_hi[3], __fmaf_rn(-nx, b.cell_hi[0], dh.x)));
+    dh.y = __fmaf_rn(-nz, b.cell_hi[7], __fmaf_rn(-ny, b.cell_hi[4], __fmaf_rn(-nx, b.cell_hi[1], dh.y)));
+    dh.z = __fmaf_rn(-nz, b.cell_hi[8], __fmaf_rn(-ny, b.cell_hi[5], __fmaf_rn(-nx, b.cell_hi[2], dh.z)));
+    dl.x -= nx * b.cell_lo[0] + ny * b.cell_lo[3] + nz * b.cell_lo[6];
+    dl.y -= nx * b.cell_lo[1] + ny * b.cell_lo[4] + nz * b.cell_lo[7];
+    dl.z -= nx * b.cell_lo[2] + ny * b.cell_lo[5] + nz * b.cell_lo[8];
+  }
+}
+
+// Screening test of one pair (true when it may lie inside a cutoff). FP64 form: the
+// exact FP64 test. Mixed / FP32 forms: FP32 on the hi parts alone (16 bytes per
+// atom), against a radius padded for the hi rounding.
+template <int PREC>
+__device__ __forceinline__ bool pair_screen(const BoxDev& b, int i, const Bead& bd) {
+  if (PREC == GRX_FP64) {
+    const double4 p = b.pos64[i];
+    double x = p.x - bd.x, y = p.y - bd.y, z = p.z - bd.z;
+    pbc64(b, x, y, z);
+    const double rr = x * x + y * y + z * z;
+    return rr < b.cut_vdw2 || (!b.no_charges && rr < b.cut_coul2);
+  } else {
+    const float4 ah = b.hi[i];
+    float x = ah.x - bd.h.x, y = ah.y - bd.h.y, z = ah.z - bd.h.z;
+    if (b.cubic) {
+      x = __fmaf_rn(-rnd(x * b.invf[0]), b.cellf[0], x);
+      y = __fmaf_rn(-rnd(y * b.invf[4]), b.cellf[4], y);
+      z = __fmaf_rn(-rnd(z * b.invf[8]), b.cellf[8], z);
+    } else {
+      const float nx = rnd(b.invf[0] * x + b.invf[3] * y + b.invf[6] * z);
+      const float ny = rnd(b.invf[1] * x + b.invf[4] * y + b.invf[7] * z);
+      const float nz = rnd(b.invf[2] * x + b.invf[5] * y + b.invf[8] * z);
+      x -= nx * b.cellf[0] + ny * b.cellf[3] + nz * b.cellf[6];
+      y -= nx * b.cellf[1] + ny * b.cellf[4] + nz * b.cellf[7];
+      z -= nx * b.cellf[2] + ny * b.cellf[5] + nz * b.cellf[8];
+    }
+    return x * x + y * y + z * z < b.screen2;
+  }
+}
+
+// 4 eps [(sigma^2/r^2)^6 - (sigma^2/r^2)^3] - shift in double-float (full molecules),
+// used by the mixed form inside 1.1 sigma where FP32 rounding of the steep repulsion
+// would exceed the error budget.
+__device__ __forceinline__ df lj_df(const BoxDev& b, int row, df rr) {
+  const float4 f = b.ffdf[row];
+  const float2 sh = b.ffdf2[row];
+  const df t = df_mul(rr, df{f.z, f.w});
+  const df t3 = df_mul(df_mul(t, t), t);
+  const df rri3 = df_recip(t3);
+  const df term = df_mul(df{f.x, f.y}, df_mul(rri3, df_add_f(rri3, -1.0f)));
+  return df_add(term, df{-sh.x, -sh.y});
+}
+
+// g(s) = erfc(alpha sqrt s)/sqrt s from the double-float table. The piece width is a
+// power of two, so t = (s - s0)/width is formed exactly from the two halves of s.
+__device__ __forceinline__ df coul_table_df(const BoxDev& b, df s) {
+  const int k = (__float_as_int(s.hi) >> 17) - b.ctab_base;
+  const float4* c = b.ctabf + 4 * k;
+  const float4 c0 = __ldg(c), c1 = __ldg(c + 1), c2 = __ldg(c + 2), c3 = __ldg(c + 3);
+  const df t = {__fmul_rn(__fsub_rn(s.hi, c0.x), c0.y), __fmul_rn(s.lo, c0.y)};
+  df p = {c3.x, c3.y};
+  p = df_add(df_mul(p, t), df{c2.z, c2.w});
+  p = df_add(df_mul(p, t), df{c2.x, c2.y});
+  p = df_add(df_mul(p, t), df{c1.z, c1.w});
+  p = df_add(df_mul(p, t), df{c1.x, c1.y});
+  p = df_add(df_mul(p, t), df{c0.z, c0.w});
+  return p;
+}
+
+// Accumulators of one lane: FP64 for the FP64 and FP32 forms, double-float for mixed.
+template <int PREC> struct LaneAcc { double v = 0.0, r = 0.0; };
+template <> struct LaneAcc<GRX_MIXED> { df v = {0.f, 0.f}, r = {0.f, 0.f}; };
+
+template <int PREC> __device__ __forceinline__ double acc_value(const LaneAcc<PREC>& a, bool vdw) {
+  if constexpr (PREC == GRX_MIXED) return vdw ? df_to(a.v) : df_to(a.r);
+  else return vdw ? a.v : a.r;
+}
+
+// Dense evaluation of one screened pair: exact cutoff tests, LJ, real Coulomb,
+// overlap flag (VDW_Coulomb.cu:1287-1322). pq = prefactor * q_bead (double-float
+// in the mixed form).
+template <int PREC>
+__device__ __forceinline__ void pair_dense(const BoxDev& b, int i, const Bead& bd, df pq,
+                                           LaneAcc<PREC>& acc, int& flag) {
+  const int2 mt = b.meta[i];
+  const int row = mt.x * b.ntypes + bd.type;
+  if constexpr (PREC == GRX_FP64) {
+    const double4 p = b.pos64[i];
+    double x = p.x - bd.x, y = p.y - bd.y, z = p.z - bd.z;
+    pbc64(b, x, y, z);
+    const double rr = x * x + y * y + z * z;
+    if (rr < b.cut_vdw2) {
+      const double e = vdw64(b, row, rr, b.scale[i] * bd.scale);
+      if (e > b.overlap) flag = 1;
+      if (rr < 0.01) flag = 1;
+      acc.v += e;
+    }
+    if (!b.no_charges && rr < b.cut_coul2) acc.r += coul64(b, p.w * bd.q, rr);
+  } else {
+    const float4 ah = b.hi[i];
+    const float4 al = b.lo[i];
+    float3 dh = make_float3(ah.x - bd.h.x, ah.y - bd.h.y, ah.z - bd.h.z);
+    float3 dl = make_float3(al.x - bd.l.x, al.y - bd.l.y, al.z - bd.l.z);
+    image_split(b, dh, dl);
+    if constexpr (PREC == GRX_MIXED) {
+      const df s = df_norm2_split(dh, dl);
+      if (df_lt(s, df{b.cut_vdw2_df.x, b.cut_vdw2_df.y})) {
+        const float4 f = b.ff32[row];
+        const bool unit = (al.w == 1.0f) && (bd.scale == 1.0) && !b.use_1264;
+        df e;
+        if (unit && s.hi > f.w) e = df{vdw32(f, s.hi), 0.0f};
+        else if (unit) e = lj_df(b, row, s);
+        else e = df_from(vdw64(b, row, df_to(s), b.scale[i] * bd.scale));
+        if (e.hi > b.overlapf) flag = 1;
+        if (s.hi < 0.01f) flag = 1;
+        acc.v = df_add(acc.v, e);
+      }
+      if (!b.no_charges && df_lt(s, df{b.cut_coul2_df.x, b.cut_coul2_df.y})) {
+        df g;
+        const int k = (__float_as_int(s.hi) >> 17) - b.ctab_base;
+        if (k >= 0 && k < b.ctab_n) g = coul_table_df(b, s);
+        else { const double rr = df_to(s), r = sqrt(rr); g = df_from(erfc(b.alpha * r) / r); }
+        const float2 qa = b.qdf[i];
+        acc.r = df_add(acc.r, df_mul(g, df_mul(df{qa.x, qa.y}, pq)));
+      }
+    } else {  // GRX_FP32
+      const float fx = dh.x + dl.x, fy = dh.y + dl.y, fz = dh.z + dl.z;
+      const float rr32 = fx * fx + fy * fy + fz * fz;
+      if (rr32 < b.cut_vdw2f) {
+        const float sc = al.w * (float)bd.scale;
+        float e;
+        if (sc == 1.0f && !b.use_1264) e = vdw32(b.ff32[row], rr32);
+        else e = (float)vdw64(b, row, (double)rr32, (double)sc);
+        if (e > b.overlapf) flag = 1;
+        if (rr32 < 0.01f) flag = 1;
+        acc.v += (double)e;
+      }
+      if (!b.no_charges && rr32 < b.cut_coul2f) acc.r += (double)coul32(b, ah.w * (float)bd.q, rr32);
+    }
+  }
+}
+
+// One work item: bead `bd` against host tiles [t0, t1) and, when `guests`, every live
+// guest atom. acc = {hg_vdw, hg_real, gg_vdw, gg_real} (valid on every lane, summed
+// later); flag is per lane.
+template <int PREC>
+__device__ __forceinline__ void warp_item(const BoxDev& b, const Bead& bd, int t0, int t1, bool guests,
+                                          int component, int newmol, int excl_comp, int excl_mol, int* q,
+                                          LaneAcc<PREC>& hacc, LaneAcc<PREC>& gacc, int& flag) {
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  unsigned head = 0, tail = 0;
+  const df pq = df_from(b.prefactor * bd.q);
+  const float bx = (float)bd.x, by = (float)bd.y, bz = (float)bd.z;
+  LaneAcc<PREC>& la = hacc;
+  for (int t = t0; t < t1; ++t) {
+    if (b.cull) {
+      const float4 tc = b.tile_c[t];
+      float dx = tc.x - bx, dy = tc.y - by, dz = tc.z - bz;
+      dx -= (float)(int)(dx * b.invf[0] + ((dx >= 0.f) ? 0.5f : -0.5f)) * b.cellf[0];
+      dy -= (float)(int)(dy * b.invf[4] + ((dy >= 0.f) ? 0.5f : -0.5f)) * b.cellf[4];
+      dz -= (float)(int)(dz * b.invf[8] + ((dz >= 0.f) ? 0.5f : -0.5f)) * b.cellf[8];
+      const float lim = b.cull_r + tc.w;
+      if (dx * dx + dy * dy + dz * dz > lim * lim) continue;
+    }
+    const int4 tr = b.tile_r[t];
+    const int i = tr.x + lane;
+    bool in = false;
+    if (i < tr.y) {
+      bool skip = false;
+      if (tr.z == component || tr.z == excl_comp) {
+        const int mol = b.meta[i].y;
+        skip = (tr.z == excl_comp && mol == excl_mol) || (tr.z == component && mol == newmol);
+      }
+      if (!skip) in = pair_screen<PREC>(b, i, bd);
+    }
+    const unsigned m = __ballot_sync(kFull, in);
+    if (in) q[(tail + __popc(m & lt)) & (kQueue - 1)] = i;
+    tail += __popc(m);
+    if (tail - head >= 32) {
+      __syncwarp();
+      const int j = q[(head + lane) & (kQueue - 1)];
+      __syncwarp();
+      pair_dense<PREC>(b, j, bd, pq, la, flag);
+      head += 32;
+    }
+  }
+  __syncwarp();
+  if (lane < (int)(tail - head)) pair_dense<PREC>(b, q[(head + lane) & (kQueue - 1)], bd, pq, la, flag);
+  __syncwarp();
+  if (!guests) return;
+  head = tail = 0;
+  for (int c = b.nhost; c < b.ncomp; ++c) {
+    const int n = b.comp_size[c];
+    const int off = b.comp_off[c];
+    const bool check = (c == component) || (c == excl_comp);
+    for (int i0 = 0; i0 < n; i0 += 32) {
+      const int i = off + i0 + lane;
+      bool in = false;
+      if (i0 + lane < n) {
+        bool skip = false;
+        if (check) {
+          const int mol = b.meta[i].y;
+          skip = (c == excl_comp && mol == excl_mol) || (c == component && mol == newmol);
+        }
+        if (!skip) in = pair_screen<PREC>(b, i, bd);
+      }
+      const unsigned m = __ballot_sync(kFull, in);
+      if (in) q[(tail + __popc(m & lt)) & (kQueue - 1)] = i;
+      tail += __popc(m);
+      if (tail - head >= 32) {
+        __syncwarp();
+        const int j = q[(head + lane) & (kQueue - 1)];
+        __syncwarp();
+        pair_dense<PREC>(b, j, bd, pq, gacc, flag);
+        head += 32;
+      }
+    }
+  }
+  __syncwarp();
+  if (lane < (int)(tail - head)) pair_dense<PREC>(b, q[(head + lane) & (kQueue - 1)], bd, pq, gacc, flag);
+  __syncwarp();
+}
+
+// Fixed-order warp sums (lane 0 receives the total). The double-float form keeps the
+// reduction on the FP32 pipe; one conversion to FP64 happens on lane 0 only.
+__device__ __forceinline__ double warp_sum(double x) {
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(kFull, x, o);
+  return x;
+}
+
+__device__ __forceinline__ df warp_sum_df(df x) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const df y = {__shfl_down_sync(kFull, x.hi, o), __shfl_down_sync(kFull, x.lo, o)};
+    x = df_add(x, y);
+  }
+  return x;
+}
+
+template <int PREC>
+__device__ __forceinline__ void warp_store(const LaneAcc<PREC>& h, const LaneAcc<PREC>& g, double* out4) {
+  const int lane = threadIdx.x & 31;
+  if constexpr (PREC == GRX_MIXED) {
+    const df a = warp_sum_df(h.v), c = warp_sum_df(h.r), d = warp_sum_df(g.v), e = warp_sum_df(g.r);
+    if (lane == 0) { out4[0] = df_to(a); out4[1] = df_to(c); out4[2] = df_to(d); out4[3] = df_to(e); }
+  } else {
+    const double a = warp_sum(h.v), c = warp_sum(h.r), d = warp_sum(g.v), e = warp_sum(g.r);
+    if (lane == 0) { out4[0] = a; out4[1] = c; out4[2] = d; out4[3] = e; }
+  }
+}
+
+// Host-tile chunks per bead so that a pass has at least ~4 items per warp.
+__host__ __device__ __forceinline__ int chunks_for(int nb, int ntiles, int nwarps) {
+  int c = (4 * nwarps + nb - 1) / nb;
+  if (c > ntiles) c = ntiles;
+  if (c < 1) c = 1;
+  return c;
+}
+
+constexpr int kMaxItems = 320;
+
+// One pass of `nb` beads (shared memory) over every atom by a whole block. Items are
+// taken dynamically by warps; per-item partials land in ipart[item*4 + q] and
+// iflag[item] (item = bead * nchunk + chunk). Caller syncs before reading them.
+template <int PREC>
+__device__ __forceinline__ void block_bead_pass(const BoxDev& b, const Bead* beads, int nb, int component,
+                                                int newmol, int excl_comp, int excl_mol, int* qbuf,
+                                                double* ipart, int* iflag, int* counter, int nchunk) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int* q = qbuf + warp * kQueue;
+  const int items = nb * nchunk;
+  const int nt = b.ntiles;
+  for (;;) {
+    int item = 0;
+    if (lane == 0) item = atomicAdd(counter, 1);
+    item = __shfl_sync(kFull, item, 0);
+    if (item >= items) break;
+    const int bead = item / nchunk, chunk = item - bead * nchunk;
+    const int t0 = (int)((long long)nt * chunk / nchunk), t1 = (int)((long long)nt * (chunk + 1) / nchunk);
+    const Bead bd = beads[bead];
+    LaneAcc<PREC> hacc, gacc;
+    int flag = 0;
+    warp_item<PREC>(b, bd, t0, t1, chunk == nchunk - 1, component, newmol, excl_comp, excl_mol, q, hacc, gacc,
+                    flag);
+    const unsigned fm = __ballot_sync(kFull, flag != 0);
+    warp_store<PREC>(hacc, gacc, ipart + item * 4);
+    if (lane == 0) iflag[item] = fm ? 1 : 0;
+  }
+}
+
+// Per-trial sums of one pass: trial t = beads [t*chain, (t+1)*chain), chunks in order.
+__device__ __forceinline__ void reduce_items(const double* ipart, const int* iflag, int ntr, int chain,
+                                             int nchunk, double* te, int* tflag) {
+  for (int w = threadIdx.x; w < ntr * 4; w += blockDim.x) {
+    const int t = w >> 2, k = w & 3;
+    double s = 0.0;
+    int f = 0;
+    for (int a = 0; a < chain; ++a)
+      for (int c = 0; c < nchunk; ++c) {
+        const int item = (t * chain + a) * nchunk + c;
+        s += ipart[item * 4 + k];
+        f |= iflag[item];
+      }
+    te[4 * t + k] = s;
+    if (k == 0) tflag[t] = f;
+  }
+}
+
+}  // namespace grx

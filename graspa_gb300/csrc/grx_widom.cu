@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "grx_host.h"
+#include "grx_warp.cuh"
 
 namespace grx {
 
@@ -87,6 +88,67 @@ __device__ bool select_trial(const double* te, const int* tflag, int nt, double 
   return true;
 }
 
+// The same selection computed by warp 0: the exponentials are evaluated one trial
+// per lane, the sums and the cumulative search stay sequential in trial order on
+// lane 0, so the result is identical to select_trial. Results are valid on lane 0.
+__device__ bool select_trial_warp(const double* te, const int* tflag, int nt, double beta, int bias,
+                                  double u, double navg, int& sel, double& wavg, int& nok, double* ws,
+                                  double* wa) {
+  const int lane = threadIdx.x & 31;
+  double lw[2];
+  bool ok[2];
+  double mx = -INFINITY;
+  int cnt = 0;
+  for (int r = 0; r < 2; ++r) {
+    const int t = lane + 32 * r;
+    ok[r] = t < nt && !tflag[t];
+    lw[r] = -INFINITY;
+    if (ok[r]) {
+      double tot = te[4 * t] + te[4 * t + 2];
+      if (bias) tot += te[4 * t + 1] + te[4 * t + 3];
+      lw[r] = __dmul_rn(-beta, tot);
+      mx = fmax(mx, lw[r]);
+      ++cnt;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  }
+  for (int r = 0; r < 2; ++r) {
+    const int t = lane + 32 * r;
+    if (t < nt) {
+      ws[t] = ok[r] ? exp(__dsub_rn(lw[r], mx)) : 0.0;
+      wa[t] = ok[r] ? exp(lw[r]) : 0.0;
+    }
+  }
+  __syncwarp();
+  nok = cnt;
+  if (lane != 0 || cnt == 0) return false;
+  double sum = 0.0;
+  for (int t = 0; t < nt; ++t)
+    if (!tflag[t]) sum += ws[t];
+  const double wsel = u * sum;
+  int s = -1, left = cnt;
+  double cum = 0.0;
+  for (int t = 0; t < nt; ++t) {
+    if (tflag[t]) continue;
+    cum += ws[t];
+    s = t;
+    --left;
+    if (!(cum < wsel) || left == 0) break;
+  }
+  double w = 0.0;
+  for (int t = 0; t < nt; ++t)
+    if (!tflag[t]) w += wa[t];
+  if (w < 1e-150) return false;
+  sel = s;
+  double avg = w / navg;
+  if (!bias) avg *= exp(-beta * (te[4 * s + 1] + te[4 * s + 3]));
+  wavg = avg;
+  return true;
+}
+
 // Rotate_Quaternions (mc_utilities.h:423-457): uniform rotation from (u, v, w).
 __device__ __forceinline__ void rotate_quaternion(double& x, double& y, double& z, double u, double v,
                                                   double w) {
@@ -110,33 +172,20 @@ __device__ __forceinline__ void rotate_quaternion(double& x, double& y, double& 
   x = nx; y = ny; z = nz;
 }
 
-// Sum the per-thread partials of one pass into per-trial energies and flags.
-__device__ __forceinline__ void reduce_pass(const double* sp, int nb, int chain, double* te) {
-  const int nl = GRX_THREADS / nb;
-  const int ntr = nb / chain;
-  for (int w = threadIdx.x; w < ntr * 4; w += blockDim.x) {
-    const int t = w >> 2, q = w & 3;
-    double s = 0.0;
-    for (int a = 0; a < chain; ++a) {
-      double sb = 0.0;
-      for (int l = 0; l < nl; ++l) sb += sp[(l * nb + t * chain + a) * 4 + q];
-      s += sb;
-    }
-    te[4 * t + q] = s;
-  }
-}
-
 template <int PREC>
-__global__ void __launch_bounds__(GRX_THREADS, 2) widom_kernel(BoxDev b, WidomArgs a, grx_widom_result* out) {
+__global__ void __launch_bounds__(GRX_THREADS, 3) widom_kernel(BoxDev b, WidomArgs a, grx_widom_result* out) {
   __shared__ Bead beads[GRX_MAX_TRIAL_BEADS];
-  __shared__ double sp[GRX_THREADS * 4];
+  __shared__ double ipart[kMaxItems * 4];
+  __shared__ int iflag[kMaxItems];
+  __shared__ int qbuf[(GRX_THREADS / 32) * kQueue];
+  __shared__ int counter;
   __shared__ double te[kMaxTrials * 4];
-  __shared__ int bflag[GRX_MAX_TRIAL_BEADS];
   __shared__ int tflag[kMaxTrials];
   __shared__ double sbuf[32];
   __shared__ double newx[GRX_MAX_MOLSIZE], newy[GRX_MAX_MOLSIZE], newz[GRX_MAX_MOLSIZE], newq[GRX_MAX_MOLSIZE];
   __shared__ grx_widom_result res;
   __shared__ int s_ok;
+  __shared__ double sel_ws[kMaxTrials], sel_wa[kMaxTrials];
   extern __shared__ double2 eik_s[];
 
   const int tid = threadIdx.x;
@@ -152,6 +201,7 @@ __global__ void __launch_bounds__(GRX_THREADS, 2) widom_kernel(BoxDev b, WidomAr
       res.sel_first = -1;
       res.sel_orient = -1;
       s_ok = 0;
+      counter = 0;
     }
     // 1. first-bead trials (mc_widom.h:133-139)
     const int nt = a.ntrials;
@@ -161,29 +211,22 @@ __global__ void __launch_bounds__(GRX_THREADS, 2) widom_kernel(BoxDev b, WidomAr
       make_bead(beads[tid], b.cell[0] * u01(r[0]), b.cell[4] * u01(r[1]), b.cell[8] * u01(r[2]),
                 b.charge[off] * a.scale_coul, a.scale, b.meta[off].x);
     }
-    if (tid < GRX_MAX_TRIAL_BEADS) bflag[tid] = 0;
     __syncthreads();
     // 2. pair energies of the first-bead trials
     {
-      const int nb = nt, nl = GRX_THREADS / nb;
-      double acc[4] = {0, 0, 0, 0};
-      int flag = 0;
-      if (tid < nl * nb) {
-        bead_pass<PREC>(b, beads[tid % nb], tid / nb, nl, a.comp, a.newmol, -1, -1, acc, flag);
-        if (flag) atomicOr(&bflag[tid % nb], 1);
-      }
-      for (int q = 0; q < 4; ++q) sp[tid * 4 + q] = acc[q];
+      const int nch = chunks_for(nt, b.ntiles, GRX_THREADS / 32);
+      block_bead_pass<PREC>(b, beads, nt, a.comp, a.newmol, -1, -1, qbuf, ipart, iflag, &counter, nch);
       __syncthreads();
-      reduce_pass(sp, nb, 1, te);
-      if (tid < nt) tflag[tid] = bflag[tid];
+      reduce_items(ipart, iflag, nt, 1, nch, te, tflag);
       __syncthreads();
     }
     // 3. select the first bead
-    if (tid == 0) {
+    if (tid < 32) {
       int sel = -1, nok = 0;
       double w = 0.0;
-      const bool ok = select_trial(te, tflag, nt, a.beta, b.vdw_real_bias, u01(selw[0]), (double)nt, sel, w, nok);
-      res.n_ok_first = nok;
+      const bool ok = select_trial_warp(te, tflag, nt, a.beta, b.vdw_real_bias, u01(selw[0]), (double)nt, sel, w,
+                                        nok, sel_ws, sel_wa);
+      if (tid == 0) res.n_ok_first = nok;
       if (ok && w > 1e-150) {
         s_ok = 1;
         res.sel_first = sel;
@@ -209,31 +252,21 @@ __global__ void __launch_bounds__(GRX_THREADS, 2) widom_kernel(BoxDev b, WidomAr
         make_bead(beads[tid], fx + vx, fy + vy, fz + vz, b.charge[off + 1 + at] * a.scale_coul, a.scale,
                   b.meta[off + 1 + at].x);
       }
-      if (tid < GRX_MAX_TRIAL_BEADS) bflag[tid] = 0;
+      if (tid == 0) counter = 0;
       __syncthreads();
       // 5. pair energies of the orientations
-      const int nl = GRX_THREADS / nb;
-      double acc[4] = {0, 0, 0, 0};
-      int flag = 0;
-      if (tid < nl * nb) {
-        bead_pass<PREC>(b, beads[tid % nb], tid / nb, nl, a.comp, a.newmol, -1, -1, acc, flag);
-        if (flag) atomicOr(&bflag[tid % nb], 1);
-      }
-      for (int q = 0; q < 4; ++q) sp[tid * 4 + q] = acc[q];
+      const int nch = chunks_for(nb, b.ntiles, GRX_THREADS / 32);
+      block_bead_pass<PREC>(b, beads, nb, a.comp, a.newmol, -1, -1, qbuf, ipart, iflag, &counter, nch);
       __syncthreads();
-      reduce_pass(sp, nb, chain, te);
-      if (tid < no) {
-        int f = 0;
-        for (int at = 0; at < chain; ++at) f |= bflag[tid * chain + at];
-        tflag[tid] = f;
-      }
+      reduce_items(ipart, iflag, no, chain, nch, te, tflag);
       __syncthreads();
-      if (tid == 0) {
+      if (tid < 32) {
         int sel = -1, nok = 0;
         double w = 0.0;
-        const bool ok = select_trial(te, tflag, no, a.beta, b.vdw_real_bias, u01(selw[1]), (double)no, sel, w, nok);
-        res.n_ok_orient = nok;
-        if (ok) {
+        const bool ok = select_trial_warp(te, tflag, no, a.beta, b.vdw_real_bias, u01(selw[1]), (double)no, sel, w,
+                                          nok, sel_ws, sel_wa);
+        if (tid == 0) res.n_ok_orient = nok;
+        if (tid == 0 && ok) {
           res.sel_orient = sel;
           res.w_chain = w;
           for (int q = 0; q < 4; ++q) res.e_chain[q] = te[4 * sel + q];
@@ -243,7 +276,7 @@ __global__ void __launch_bounds__(GRX_THREADS, 2) widom_kernel(BoxDev b, WidomAr
             const Bead& bd = beads[sel * chain + at];
             newx[1 + at] = bd.x; newy[1 + at] = bd.y; newz[1 + at] = bd.z; newq[1 + at] = bd.q;
           }
-        } else {
+        } else if (tid == 0) {
           s_ok = 0;
         }
       }
@@ -276,28 +309,80 @@ __global__ void __launch_bounds__(GRX_THREADS, 2) widom_kernel(BoxDev b, WidomAr
       }
       __syncthreads();
       double same = 0.0, cross = 0.0;
-      for (int j = tid; j < b.nact; j += blockDim.x) {
-        const int4 k = b.kact[j];
-        double2 cn = make_double2(0.0, 0.0);
-        for (int at = 0; at < ms; ++at) {
-          double2 y = ey[at + ms * abs(k.y)];
-          if (k.y < 0) y.y = -y.y;
-          double2 z = ez[at + ms * abs(k.z)];
-          if (k.z < 0) z.y = -z.y;
-          const double2 t = cmul(cmul(ex[at + ms * k.x], y), z);
-          cn.x += newq[at] * t.x;
-          cn.y += newq[at] * t.y;
+      if constexpr (PREC == GRX_FP64) {
+        for (int j = tid; j < b.nact; j += blockDim.x) {
+          const int4 k = b.kact[j];
+          double2 cn = make_double2(0.0, 0.0);
+          for (int at = 0; at < ms; ++at) {
+            double2 y = ey[at + ms * abs(k.y)];
+            if (k.y < 0) y.y = -y.y;
+            double2 z = ez[at + ms * abs(k.z)];
+            if (k.z < 0) z.y = -z.y;
+            const double2 t = cmul(cmul(ex[at + ms * k.x], y), z);
+            cn.x += newq[at] * t.x;
+            cn.y += newq[at] * t.y;
+          }
+          const double tmp = b.ktemp[j];
+          const double2 ov = b.s_ads[k.w];
+          const double2 nv = make_double2(ov.x + cn.x, ov.y + cn.y);
+          same += tmp * (nv.x * nv.x + nv.y * nv.y);
+          same -= tmp * (ov.x * ov.x + ov.y * ov.y);
+          const double2 xv = b.s_fw[k.w];
+          cross += tmp * (xv.x * cn.x + xv.y * cn.y);
         }
-        const double tmp = b.ktemp[j];
-        const double2 ov = b.s_ads[k.w];
-        const double2 nv = make_double2(ov.x + cn.x, ov.y + cn.y);
-        same += tmp * (nv.x * nv.x + nv.y * nv.y);
-        same -= tmp * (ov.x * ov.x + ov.y * ov.y);
-        const double2 xv = b.s_fw[k.w];
-        cross += tmp * (xv.x * cn.x + xv.y * cn.y);
+        same = block_sum(same, sbuf);
+        cross = block_sum(cross, sbuf);
+      } else {
+        // double-float copies of the eik tables (same shared buffer, after the FP64 ones)
+        float4* fx = reinterpret_cast<float4*>(ez + (b.kmax[2] + 1) * ms);
+        const int ntab = (b.kmax[0] + b.kmax[1] + b.kmax[2] + 3) * ms;
+        for (int e = tid; e < ntab; e += blockDim.x) {
+          const df re = df_from(ex[e].x), im = df_from(ex[e].y);
+          fx[e] = make_float4(re.hi, re.lo, im.hi, im.lo);
+        }
+        __shared__ float2 qd[GRX_MAX_MOLSIZE];
+        if (tid < ms) { const df q = df_from(newq[tid]); qd[tid] = make_float2(q.hi, q.lo); }
+        __syncthreads();
+        const float4* fy = fx + kx1 * ms;
+        const float4* fz = fy + ky1 * ms;
+        df sm = {0.f, 0.f}, cr = {0.f, 0.f};
+        for (int j = tid; j < b.nact; j += blockDim.x) {
+          const int4 k = b.kact[j];
+          df cre = {0.f, 0.f}, cim = {0.f, 0.f};
+          const int ay = abs(k.y), az = abs(k.z);
+          const float sy = k.y < 0 ? -1.f : 1.f, sz = k.z < 0 ? -1.f : 1.f;
+          for (int at = 0; at < ms; ++at) {
+            const float4 X = fx[at + ms * k.x], Y = fy[at + ms * ay], Z = fz[at + ms * az];
+            const df xr = {X.x, X.y}, xi = {X.z, X.w};
+            const df yr = {Y.x, Y.y}, yi = {sy * Y.z, sy * Y.w};
+            const df zr = {Z.x, Z.y}, zi = {sz * Z.z, sz * Z.w};
+            // (x*y)*z, then charge
+            const df pr = df_add(df_mul(xr, yr), df_mul(df{-xi.hi, -xi.lo}, yi));
+            const df pi = df_add(df_mul(xr, yi), df_mul(xi, yr));
+            const df tr = df_add(df_mul(pr, zr), df_mul(df{-pi.hi, -pi.lo}, zi));
+            const df ti = df_add(df_mul(pr, zi), df_mul(pi, zr));
+            const df q = {qd[at].x, qd[at].y};
+            cre = df_add(cre, df_mul(q, tr));
+            cim = df_add(cim, df_mul(q, ti));
+          }
+          const float4 A = b.ewA[j], F = b.ewF[j];
+          const float2 T = b.ewT[j];
+          // same: 2 Re(A dS*) + temp |dS|^2 ; cross: Re(F dS*)
+          const df reA = df_add(df_mul(df{A.x, A.y}, cre), df_mul(df{A.z, A.w}, cim));
+          const df n2 = df_add(df_mul(cre, cre), df_mul(cim, cim));
+          sm = df_add(sm, df_add(df{2.f * reA.hi, 2.f * reA.lo}, df_mul(df{T.x, T.y}, n2)));
+          cr = df_add(cr, df_add(df_mul(df{F.x, F.y}, cre), df_mul(df{F.z, F.w}, cim)));
+        }
+        // block sums: warp tree in double-float, then FP64 over the 8 warp partials
+        sm = warp_sum_df(sm);
+        cr = warp_sum_df(cr);
+        __shared__ double wsum[2][GRX_THREADS / 32];
+        if ((tid & 31) == 0) { wsum[0][tid >> 5] = df_to(sm); wsum[1][tid >> 5] = df_to(cr); }
+        __syncthreads();
+        if (tid == 0) {
+          for (int w = 0; w < GRX_THREADS / 32; ++w) { same += wsum[0][w]; cross += wsum[1][w]; }
+        }
       }
-      same = block_sum(same, sbuf);
-      cross = block_sum(cross, sbuf);
       if (tid == 0) {
         if (a.rigid) same -= a.excl * (a.scale_coul * a.scale_coul - 0.0);
         res.ewald[0] = same;
@@ -316,6 +401,21 @@ __global__ void __launch_bounds__(GRX_THREADS, 2) widom_kernel(BoxDev b, WidomAr
       out[m] = res;
     }
     __syncthreads();
+  }
+}
+
+// temp * S(k) of both blocks in double-float, per active k (the box's static part of
+// the Fourier delta: dE_same = sum 2 Re(A dS*) + temp |dS|^2, dE_cross = sum Re(F dS*)).
+__global__ void ewald_df_refresh_kernel(BoxDev b, float4* ewA, float4* ewF, float2* ewT) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < b.nact; j += gridDim.x * blockDim.x) {
+    const int slot = b.kact[j].w;
+    const double t = b.ktemp[j];
+    const double2 sa = b.s_ads[slot], sf = b.s_fw[slot];
+    const df ar = df_from(t * sa.x), ai = df_from(t * sa.y), fr = df_from(t * sf.x), fi = df_from(t * sf.y);
+    ewA[j] = make_float4(ar.hi, ar.lo, ai.hi, ai.lo);
+    ewF[j] = make_float4(fr.hi, fr.lo, fi.hi, fi.lo);
+    const df tt = df_from(t);
+    ewT[j] = make_float2(tt.hi, tt.lo);
   }
 }
 
@@ -365,8 +465,15 @@ static grx_status widom_launch(grx_box* b, const grx_widom_desc* d, uint64_t fir
   a.stream = d->stream;
   a.first_move = first_move;
   a.n = (int64_t)n;
-  const size_t smem = (size_t)(b->dev.kmax[0] + b->dev.kmax[1] + b->dev.kmax[2] + 3) * ms * sizeof(double2);
-  const int grid = (int)std::min<size_t>(n, (size_t)sm_count(b) * 2);
+  const size_t smem = (size_t)(b->dev.kmax[0] + b->dev.kmax[1] + b->dev.kmax[2] + 3) * ms *
+                      (sizeof(double2) + sizeof(float4));
+  if (!b->ewdf_valid && b->nact > 0) {
+    ewald_df_refresh_kernel<<<std::max(1, std::min((b->nact + 255) / 256, sm_count(b))), 256, 0, b->stream>>>(
+        b->dev, b->ewA, b->ewF, b->ewT);
+    count_launch();
+    b->ewdf_valid = true;
+  }
+  const int grid = (int)std::min<size_t>(n, (size_t)sm_count(b) * 3);
   if (prec == GRX_FP64) widom_kernel<GRX_FP64><<<grid, GRX_THREADS, smem, b->stream>>>(b->dev, a, dev_results);
   else if (prec == GRX_MIXED) widom_kernel<GRX_MIXED><<<grid, GRX_THREADS, smem, b->stream>>>(b->dev, a, dev_results);
   else widom_kernel<GRX_FP32><<<grid, GRX_THREADS, smem, b->stream>>>(b->dev, a, dev_results);
