@@ -95,7 +95,7 @@ EXPORTS = [
     "grx_box_get_exclusion", "grx_trial_energies", "grx_single_body_energy", "grx_ewald_sizes",
     "grx_ewald_total", "grx_ewald_set_structure_factors", "grx_ewald_get_structure_factors",
     "grx_ewald_delta", "grx_ewald_commit", "grx_total_energy", "grx_cbmc_select",
-    "grx_widom_insertions", "grx_widom_insertions_async", "grx_launch_count",
+    "grx_widom_insertions", "grx_widom_insertions_async", "grx_launch_count", "grx_trial_energies_noalloc",
 ]
 
 _lib = None
@@ -144,6 +144,8 @@ def load(path=LIB_PATH):
     L.grx_widom_insertions_async.argtypes = [C.c_void_p, P(WidomDesc), C.c_uint64, C.c_size_t, C.c_int32,
                                              C.c_void_p]
     L.grx_launch_count.restype = C.c_uint64
+    L.grx_trial_energies_noalloc.argtypes = [C.c_void_p, P(Trials), C.c_int32, C.c_int64, C.c_int64, C.c_int32,
+                                             P(TrialEnergy), _u8p]
     _lib = L
     return L
 
@@ -347,6 +349,23 @@ class Box:
         flag = np.zeros(ntrials, dtype=np.uint8)
         check(self.L.grx_trial_energies(self.h, C.byref(t), component, excl_comp, excl_molid, prec, out,
                                         flag.ctypes.data_as(_u8p)), "grx_trial_energies")
+        e = np.array([[o.hg_vdw, o.hg_real, o.gg_vdw, o.gg_real] for o in out])
+        return e, flag
+
+    def trial_energies_noalloc(self, pos, charge, types, molid, ntrials, chainsize, component, prec=GRX_FP64,
+                               excl_comp=-1, excl_molid=-1):
+        """grx_trial_energies_noalloc: the same call with its scratch in a fixed device array."""
+        nb = ntrials * chainsize
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1)
+        charge = np.ascontiguousarray(charge, dtype=np.float64)
+        types = np.ascontiguousarray(types, dtype=np.uint64)
+        ones = np.ones(nb)
+        t = Trials(_d(pos), _d(ones), _d(charge), _d(ones), _sz(types), molid, ntrials, chainsize)
+        out = (TrialEnergy * ntrials)()
+        flag = np.zeros(ntrials, dtype=np.uint8)
+        st = self.L.grx_trial_energies_noalloc(self.h, C.byref(t), component, excl_comp, excl_molid, prec, out,
+                                               flag.ctypes.data_as(_u8p))
+        check(st, "grx_trial_energies_noalloc")
         e = np.array([[o.hg_vdw, o.hg_real, o.gg_vdw, o.gg_real] for o in out])
         return e, flag
 

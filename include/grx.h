@@ -275,6 +275,25 @@ grx_status grx_widom_insertions_async(grx_box* box, const grx_widom_desc* desc,
                                       uint64_t first_move, size_t n, grx_precision prec,
                                       grx_widom_result* results);
 
+/* ---- allocation-free trial energies ------------------------------------- */
+/* grx_trial_energies without any device allocation at call time. No counterpart
+ * in the reference: it exists for callers that cannot let a call allocate device
+ * memory, such as a Monte Carlo loop that must never stall the GPU (cudaMalloc and
+ * cudaFree can synchronize the whole device) or a host application that owns all
+ * device memory through its own pool. Same arguments, semantics and results as
+ * grx_trial_energies; the scratch lives in one fixed device array of
+ * GRX_NOALLOC_SCRATCH_BYTES held by every GPU that loads the library until exit.
+ * Limit: ntrials * chainsize <= GRX_NOALLOC_MAX_BEADS, else GRX_ERR_CAPACITY.
+ * The first call on a device looks up the array's device address (make it before
+ * any stream capture). All calls share the array: calls that overlap on the GPU
+ * race, so issue them one after another. The box is created beforehand with
+ * grx_box_create. */
+#define GRX_NOALLOC_MAX_BEADS 256
+#define GRX_NOALLOC_SCRATCH_BYTES 65536
+grx_status grx_trial_energies_noalloc(grx_box* box, const grx_trials* trials, int32_t component,
+                                      int64_t exclude_comp, int64_t exclude_molid,
+                                      grx_precision prec, grx_trial_energy* out, uint8_t* overlap);
+
 /* Number of kernel launches this process issued through the library. */
 uint64_t grx_launch_count(void);
 
