@@ -256,10 +256,13 @@ static grx_status build_tiles(grx_box* b) {
       const double* a0 = &b->h_pos[3 * (o + t0)];
       double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
       std::vector<double> u(3 * (t1 - t0));
+      int compact = 1;  // stored positions need no lattice shift relative to the first atom
       for (int i = t0; i < t1; ++i) {
         double dv[3] = {b->h_pos[3 * (o + i)] - a0[0], b->h_pos[3 * (o + i) + 1] - a0[1],
                         b->h_pos[3 * (o + i) + 2] - a0[2]};
+        const double raw[3] = {dv[0], dv[1], dv[2]};
         pbc_host(b->dev, dv);
+        if (raw[0] != dv[0] || raw[1] != dv[1] || raw[2] != dv[2]) compact = 0;
         for (int k = 0; k < 3; ++k) {
           u[3 * (i - t0) + k] = a0[k] + dv[k];
           lo[k] = std::min(lo[k], a0[k] + dv[k]);
@@ -274,7 +277,7 @@ static grx_status build_tiles(grx_box* b) {
       }
       const float rad = (float)(std::sqrt(r2) * (1.0 + 1e-6) + 1e-4);
       b->h_tile_c.push_back(make_float4((float)cx, (float)cy, (float)cz, rad));
-      b->h_tile_r.push_back(make_int4((int)(o + t0), (int)(o + t1), c, 0));
+      b->h_tile_r.push_back(make_int4((int)(o + t0), (int)(o + t1), c, compact));
     }
   }
   b->ntiles = (int)b->h_tile_c.size();

@@ -210,7 +210,7 @@ __device__ __forceinline__ double vdw64(const BoxDev& b, int row, double rr, dou
 __device__ __forceinline__ float vdw32(float4 f, float rr) {
   const float t = rr * f.y;
   const float t3 = t * t * t;
-  const float rri3 = __frcp_rn(t3);
+  const float rri3 = __fdividef(1.0f, t3);
   return f.x * (rri3 * (rri3 - 1.0f)) - f.z;
 }
 
@@ -231,7 +231,9 @@ struct Bead {
   float3 h, l;         // split position
   double q;            // charge * scaleCoul
   double scale;        // LJ lambda
+  float2 pq;           // prefactor * q as double-float
   int type;
+  int unit;            // scale == 1
 };
 
 __device__ __forceinline__ void split_coord(double x, float& h, float& l) {
@@ -241,12 +243,16 @@ __device__ __forceinline__ void split_coord(double x, float& h, float& l) {
 }
 
 __device__ __forceinline__ void make_bead(Bead& bd, double x, double y, double z, double q,
-                                          double scale, int type) {
+                                          double scale, int type, double prefactor) {
   bd.x = x; bd.y = y; bd.z = z;
   split_coord(x, bd.h.x, bd.l.x);
   split_coord(y, bd.h.y, bd.l.y);
   split_coord(z, bd.h.z, bd.l.z);
   bd.q = q; bd.scale = scale; bd.type = type;
+  const double pq = prefactor * q;
+  const float ph = __double2float_rn(pq);
+  bd.pq = make_float2(ph, __double2float_rn(pq - (double)ph));
+  bd.unit = scale == 1.0;
 }
 
 // Energy of one (atom, bead) pair. Returns true when the pair is inside a cutoff;

@@ -80,13 +80,13 @@ grx_status scratch_address(unsigned char** out) {
 // and charge products as the staging of grx_trial_energies.
 __global__ void noalloc_beads_kernel(const double* pos, const double* scale, const double* charge,
                                      const double* scale_coul, const size_t* type, int nb, int has_scale,
-                                     int has_charge, int has_scale_coul, Bead* beads) {
+                                     int has_charge, int has_scale_coul, double prefactor, Bead* beads) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= nb) return;
   const double sc = has_scale ? scale[j] : 1.0;
   const double q = has_charge ? charge[j] : 0.0;
   const double scc = has_scale_coul ? scale_coul[j] : 1.0;
-  make_bead(beads[j], pos[3 * j], pos[3 * j + 1], pos[3 * j + 2], q * scc, sc, (int)type[j]);
+  make_bead(beads[j], pos[3 * j], pos[3 * j + 1], pos[3 * j + 2], q * scc, sc, (int)type[j], prefactor);
 }
 
 template <int PREC>
@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(GRX_THREADS) noalloc_bead_pass_kernel(BoxDev b
   __syncthreads();
   if (threadIdx.x < 4) {
     double s = 0.0;
-    for (int c = 0; c < nch; ++c) s += ipart[c * 4 + threadIdx.x];
+    for (int c = 0; c < nch; ++c) s += item_get<PREC>(ipart, c * 4 + threadIdx.x);
     part[blockIdx.x * 4 + threadIdx.x] = s;
   }
   if (threadIdx.x == 0) {
@@ -180,7 +180,8 @@ extern "C" grx_status grx_trial_energies_noalloc(grx_box* b, const grx_trials* t
   GRX_CHECK_CUDA(cudaMemcpyAsync(type, t->type, nb * sizeof(size_t), cudaMemcpyDefault, s), "noalloc: stage type");
   GRX_CHECK_CUDA(cudaMemsetAsync(flags, 0, nb * sizeof(int), s), "noalloc: clear flags");
   noalloc_beads_kernel<<<(nb + 127) / 128, 128, 0, s>>>(pos, scale, charge, scale_coul, type, nb, t->scale != nullptr,
-                                                        t->charge != nullptr, t->scale_coul != nullptr, beads);
+                                                        t->charge != nullptr, t->scale_coul != nullptr,
+                                                        b->dev.prefactor, beads);
   const int ec = (int)exclude_comp, em = (int)exclude_molid, nm = (int)t->molid;
   if (prec == GRX_FP64)
     noalloc_bead_pass_kernel<GRX_FP64><<<nb, GRX_THREADS, 0, s>>>(b->dev, beads, component, nm, ec, em, part, flags);

@@ -27,7 +27,7 @@ __global__ void __launch_bounds__(GRX_THREADS) trial_bead_kernel(BoxDev b, const
   __syncthreads();
   if (threadIdx.x < 4) {
     double s = 0.0;
-    for (int c = 0; c < nch; ++c) s += ipart[c * 4 + threadIdx.x];
+    for (int c = 0; c < nch; ++c) s += item_get<PREC>(ipart, c * 4 + threadIdx.x);
     part[blockIdx.x * 4 + threadIdx.x] = s;
   }
   if (threadIdx.x == 0) {
@@ -111,7 +111,8 @@ static void host_split(double x, float& h, float& l) {
   l = (float)(x - hd);
 }
 
-static grx_status stage_beads(const grx_trials* t, size_t first_bead, size_t nbeads, std::vector<Bead>& out) {
+static grx_status stage_beads(const grx_trials* t, size_t first_bead, size_t nbeads, double prefactor,
+                              std::vector<Bead>& out) {
   const size_t nall = t->ntrials * t->chainsize;
   std::vector<double> pos(3 * nall), sc(nall, 1.0), q(nall, 0.0), scc(nall, 1.0);
   std::vector<size_t> ty(nall, 0);
@@ -133,6 +134,10 @@ static grx_status stage_beads(const grx_trials* t, size_t first_bead, size_t nbe
     bd.q = q[j] * scc[j];
     bd.scale = sc[j];
     bd.type = (int)ty[j];
+    const double pq = prefactor * bd.q;
+    const float ph = (float)pq;
+    bd.pq = make_float2(ph, (float)(pq - (double)ph));
+    bd.unit = bd.scale == 1.0;
   }
   return GRX_OK;
 }
@@ -168,7 +173,7 @@ grx_status grx_trial_energies(grx_box* b, const grx_trials* t, int32_t component
     const size_t ntr = std::min(per_chunk, t->ntrials - t0);
     const int nb = (int)(ntr * ch);
     std::vector<Bead> beads;
-    grx_status st = stage_beads(t, t0 * ch, nb, beads);
+    grx_status st = stage_beads(t, t0 * ch, nb, b->dev.prefactor, beads);
     if (st) return st;
     const int nblk = 1;
     const size_t bead_bytes = (nb * sizeof(Bead) + 255) / 256 * 256;
@@ -218,9 +223,9 @@ grx_status grx_single_body_energy(grx_box* b, const grx_trials* old_mol, const g
   GRX_REQUIRE(do_new || do_old, "grx_single_body_energy: nothing to do");
   refresh_dev(b);
   std::vector<Bead> nb_, ob_;
-  grx_status st = stage_beads(new_mol, 0, ms, nb_);
+  grx_status st = stage_beads(new_mol, 0, ms, b->dev.prefactor, nb_);
   if (st) return st;
-  st = stage_beads(old_mol, 0, ms, ob_);
+  st = stage_beads(old_mol, 0, ms, b->dev.prefactor, ob_);
   if (st) return st;
   nb_.insert(nb_.end(), ob_.begin(), ob_.end());
   size_t total_atoms = 0;

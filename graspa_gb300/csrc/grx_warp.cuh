@@ -112,13 +112,11 @@ __device__ __forceinline__ df coul_table_df(const BoxDev& b, df s) {
   const float4* c = b.ctabf + 4 * k;
   const float4 c0 = __ldg(c), c1 = __ldg(c + 1), c2 = __ldg(c + 2), c3 = __ldg(c + 3);
   const df t = {__fmul_rn(__fsub_rn(s.hi, c0.x), c0.y), __fmul_rn(s.lo, c0.y)};
-  df p = {c3.x, c3.y};
-  p = df_add(df_mul(p, t), df{c2.z, c2.w});
-  p = df_add(df_mul(p, t), df{c2.x, c2.y});
-  p = df_add(df_mul(p, t), df{c1.z, c1.w});
-  p = df_add(df_mul(p, t), df{c1.x, c1.y});
-  p = df_add(df_mul(p, t), df{c0.z, c0.w});
-  return p;
+  // Over one piece the terms of order >= 2 are ~1e-4 of g, so they are summed in
+  // FP32 (error ~1e-12 of g); the first two orders are kept in double-float.
+  const float tail = __fmaf_rn(__fmaf_rn(__fmaf_rn(c3.x, t.hi, c2.z), t.hi, c2.x), t.hi, c1.z);
+  const df p1 = df_add(df_mul_f(t, tail), df{c1.x, c1.y});
+  return df_add(df_mul(p1, t), df{c0.z, c0.w});
 }
 
 // Accumulators of one lane: FP64 for the FP64 and FP32 forms, double-float for mixed.
@@ -160,7 +158,7 @@ __device__ __forceinline__ void pair_dense(const BoxDev& b, int i, const Bead& b
       const df s = df_norm2_split(dh, dl);
       if (df_lt(s, df{b.cut_vdw2_df.x, b.cut_vdw2_df.y})) {
         const float4 f = b.ff32[row];
-        const bool unit = (al.w == 1.0f) && (bd.scale == 1.0) && !b.use_1264;
+        const bool unit = (al.w == 1.0f) && bd.unit && !b.use_1264;
         df e;
         if (unit && s.hi > f.w) e = df{vdw32(f, s.hi), 0.0f};
         else if (unit) e = lj_df(b, row, s);
@@ -175,7 +173,7 @@ __device__ __forceinline__ void pair_dense(const BoxDev& b, int i, const Bead& b
         if (k >= 0 && k < b.ctab_n) g = coul_table_df(b, s);
         else { const double rr = df_to(s), r = sqrt(rr); g = df_from(erfc(b.alpha * r) / r); }
         const float2 qa = b.qdf[i];
-        acc.r = df_add(acc.r, df_mul(g, df_mul(df{qa.x, qa.y}, pq)));
+        acc.r = df_add(acc.r, df_mul(g, df{qa.x, qa.y}));  // prefactor * q_bead applied once per item
       }
     } else {  // GRX_FP32
       const float fx = dh.x + dl.x, fy = dh.y + dl.y, fz = dh.z + dl.z;
@@ -204,39 +202,70 @@ __device__ __forceinline__ void warp_item(const BoxDev& b, const Bead& bd, int t
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
   unsigned head = 0, tail = 0;
-  const df pq = df_from(b.prefactor * bd.q);
-  const float bx = (float)bd.x, by = (float)bd.y, bz = (float)bd.z;
+  const df pq = {bd.pq.x, bd.pq.y};
+  const float bx = bd.h.x + bd.l.x, by = bd.h.y + bd.l.y, bz = bd.h.z + bd.l.z;
   LaneAcc<PREC>& la = hacc;
-  for (int t = t0; t < t1; ++t) {
-    if (b.cull) {
-      const float4 tc = b.tile_c[t];
+  // Tiles are tested 32 at a time, one per lane; survivors are then screened one
+  // tile at a time by the whole warp. When a tile lies inside one periodic image of
+  // the bead (orthorhombic cells, stored positions unwrapped-compact), the image shift
+  // is applied once to the bead instead of once per atom.
+  for (int base = t0; base < t1; base += 32) {
+    const int tl = base + lane;
+    bool pass = tl < t1;
+    float nx = 0.f, ny = 0.f, nz = 0.f;
+    bool one_image = false;
+    if (pass && b.cull) {
+      const float4 tc = b.tile_c[tl];
       float dx = tc.x - bx, dy = tc.y - by, dz = tc.z - bz;
-      dx -= (float)(int)(dx * b.invf[0] + ((dx >= 0.f) ? 0.5f : -0.5f)) * b.cellf[0];
-      dy -= (float)(int)(dy * b.invf[4] + ((dy >= 0.f) ? 0.5f : -0.5f)) * b.cellf[4];
-      dz -= (float)(int)(dz * b.invf[8] + ((dz >= 0.f) ? 0.5f : -0.5f)) * b.cellf[8];
+      nx = rnd(dx * b.invf[0]); ny = rnd(dy * b.invf[4]); nz = rnd(dz * b.invf[8]);
+      dx = __fmaf_rn(-nx, b.cellf[0], dx);
+      dy = __fmaf_rn(-ny, b.cellf[4], dy);
+      dz = __fmaf_rn(-nz, b.cellf[8], dz);
       const float lim = b.cull_r + tc.w;
-      if (dx * dx + dy * dy + dz * dz > lim * lim) continue;
+      pass = dx * dx + dy * dy + dz * dz <= lim * lim;
+      const float m = tc.w + 1e-2f;
+      one_image = b.tile_r[tl].w != 0 && fabsf(dx) + m < 0.5f * b.cellf[0] &&
+                  fabsf(dy) + m < 0.5f * b.cellf[4] && fabsf(dz) + m < 0.5f * b.cellf[8];
     }
-    const int4 tr = b.tile_r[t];
-    const int i = tr.x + lane;
-    bool in = false;
-    if (i < tr.y) {
-      bool skip = false;
-      if (tr.z == component || tr.z == excl_comp) {
-        const int mol = b.meta[i].y;
-        skip = (tr.z == excl_comp && mol == excl_mol) || (tr.z == component && mol == newmol);
+    unsigned mask = __ballot_sync(kFull, pass);
+    while (mask) {
+      const int src = __ffs(mask) - 1;
+      mask &= mask - 1;
+      const int t = base + src;
+      const bool oi = __shfl_sync(kFull, one_image, src);
+      const float tnx = __shfl_sync(kFull, nx, src), tny = __shfl_sync(kFull, ny, src),
+                  tnz = __shfl_sync(kFull, nz, src);
+      const int4 tr = b.tile_r[t];
+      const int i = tr.x + lane;
+      bool in = false;
+      if (i < tr.y) {
+        bool skip = false;
+        if (tr.z == component || tr.z == excl_comp) {
+          const int mol = b.meta[i].y;
+          skip = (tr.z == excl_comp && mol == excl_mol) || (tr.z == component && mol == newmol);
+        }
+        if (!skip) {
+          if (PREC != GRX_FP64 && oi) {
+            const float4 ah = b.hi[i];
+            const float x = ah.x - __fmaf_rn(tnx, b.cell_hi[0], bd.h.x);
+            const float y = ah.y - __fmaf_rn(tny, b.cell_hi[4], bd.h.y);
+            const float z = ah.z - __fmaf_rn(tnz, b.cell_hi[8], bd.h.z);
+            in = x * x + y * y + z * z < b.screen2;
+          } else {
+            in = pair_screen<PREC>(b, i, bd);
+          }
+        }
       }
-      if (!skip) in = pair_screen<PREC>(b, i, bd);
-    }
-    const unsigned m = __ballot_sync(kFull, in);
-    if (in) q[(tail + __popc(m & lt)) & (kQueue - 1)] = i;
-    tail += __popc(m);
-    if (tail - head >= 32) {
-      __syncwarp();
-      const int j = q[(head + lane) & (kQueue - 1)];
-      __syncwarp();
-      pair_dense<PREC>(b, j, bd, pq, la, flag);
-      head += 32;
+      const unsigned m = __ballot_sync(kFull, in);
+      if (in) q[(tail + __popc(m & lt)) & (kQueue - 1)] = i;
+      tail += __popc(m);
+      if (tail - head >= 32) {
+        __syncwarp();
+        const int j = q[(head + lane) & (kQueue - 1)];
+        __syncwarp();
+        pair_dense<PREC>(b, j, bd, pq, la, flag);
+        head += 32;
+      }
     }
   }
   __syncwarp();
@@ -292,11 +321,23 @@ __device__ __forceinline__ df warp_sum_df(df x) {
 }
 
 template <int PREC>
-__device__ __forceinline__ void warp_store(const LaneAcc<PREC>& h, const LaneAcc<PREC>& g, double* out4) {
+__device__ __forceinline__ void warp_store(const LaneAcc<PREC>& h, const LaneAcc<PREC>& g, double* out4, df pq,
+                                           bool with_guests) {
   const int lane = threadIdx.x & 31;
   if constexpr (PREC == GRX_MIXED) {
-    const df a = warp_sum_df(h.v), c = warp_sum_df(h.r), d = warp_sum_df(g.v), e = warp_sum_df(g.r);
-    if (lane == 0) { out4[0] = df_to(a); out4[1] = df_to(c); out4[2] = df_to(d); out4[3] = df_to(e); }
+    // the mixed form accumulates sum q_atom * g(r); the bead factor prefactor*q_bead
+    // is applied here, once
+    const df a = warp_sum_df(h.v), c = warp_sum_df(h.r);
+    df d = {0.f, 0.f}, e = {0.f, 0.f};
+    if (with_guests) { d = warp_sum_df(g.v); e = warp_sum_df(g.r); }
+    if (lane == 0) {  // stored as float pairs in the 8-byte slots (item_get converts)
+      float2* o = reinterpret_cast<float2*>(out4);
+      const df cq = df_mul(c, pq), eq = df_mul(e, pq);
+      o[0] = make_float2(a.hi, a.lo);
+      o[1] = make_float2(cq.hi, cq.lo);
+      o[2] = make_float2(d.hi, d.lo);
+      o[3] = make_float2(eq.hi, eq.lo);
+    }
   } else {
     const double a = warp_sum(h.v), c = warp_sum(h.r), d = warp_sum(g.v), e = warp_sum(g.r);
     if (lane == 0) { out4[0] = a; out4[1] = c; out4[2] = d; out4[3] = e; }
@@ -337,25 +378,50 @@ __device__ __forceinline__ void block_bead_pass(const BoxDev& b, const Bead* bea
     warp_item<PREC>(b, bd, t0, t1, chunk == nchunk - 1, component, newmol, excl_comp, excl_mol, q, hacc, gacc,
                     flag);
     const unsigned fm = __ballot_sync(kFull, flag != 0);
-    warp_store<PREC>(hacc, gacc, ipart + item * 4);
+    warp_store<PREC>(hacc, gacc, ipart + item * 4, df{bd.pq.x, bd.pq.y},
+                     chunk == nchunk - 1 && b.comp_off[b.ncomp] > b.host_end);
     if (lane == 0) iflag[item] = fm ? 1 : 0;
   }
 }
 
+// Item partials: FP64 in the FP64 / FP32 forms, a float pair in the mixed form.
+template <int PREC>
+__device__ __forceinline__ double item_get(const double* ipart, int idx) {
+  if constexpr (PREC == GRX_MIXED) {
+    const float2 v = reinterpret_cast<const float2*>(ipart)[idx];
+    return (double)v.x + (double)v.y;
+  } else {
+    return ipart[idx];
+  }
+}
+
 // Per-trial sums of one pass: trial t = beads [t*chain, (t+1)*chain), chunks in order.
+template <int PREC>
 __device__ __forceinline__ void reduce_items(const double* ipart, const int* iflag, int ntr, int chain,
                                              int nchunk, double* te, int* tflag) {
   for (int w = threadIdx.x; w < ntr * 4; w += blockDim.x) {
     const int t = w >> 2, k = w & 3;
-    double s = 0.0;
     int f = 0;
-    for (int a = 0; a < chain; ++a)
-      for (int c = 0; c < nchunk; ++c) {
-        const int item = (t * chain + a) * nchunk + c;
-        s += ipart[item * 4 + k];
-        f |= iflag[item];
-      }
-    te[4 * t + k] = s;
+    if constexpr (PREC == GRX_MIXED) {
+      df s = {0.f, 0.f};
+      for (int a = 0; a < chain; ++a)
+        for (int c = 0; c < nchunk; ++c) {
+          const int item = (t * chain + a) * nchunk + c;
+          const float2 v = reinterpret_cast<const float2*>(ipart)[item * 4 + k];
+          s = df_add(s, df{v.x, v.y});
+          f |= iflag[item];
+        }
+      te[4 * t + k] = df_to(s);
+    } else {
+      double s = 0.0;
+      for (int a = 0; a < chain; ++a)
+        for (int c = 0; c < nchunk; ++c) {
+          const int item = (t * chain + a) * nchunk + c;
+          s += ipart[item * 4 + k];
+          f |= iflag[item];
+        }
+      te[4 * t + k] = s;
+    }
     if (k == 0) tflag[t] = f;
   }
 }

@@ -209,7 +209,7 @@ __global__ void __launch_bounds__(GRX_THREADS, 3) widom_kernel(BoxDev b, WidomAr
       uint32_t r[4];
       draw4(a.seed, a.stream, move, SLOT_FIRST + tid, r);
       make_bead(beads[tid], b.cell[0] * u01(r[0]), b.cell[4] * u01(r[1]), b.cell[8] * u01(r[2]),
-                b.charge[off] * a.scale_coul, a.scale, b.meta[off].x);
+                b.charge[off] * a.scale_coul, a.scale, b.meta[off].x, b.prefactor);
     }
     __syncthreads();
     // 2. pair energies of the first-bead trials
@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(GRX_THREADS, 3) widom_kernel(BoxDev b, WidomAr
       const int nch = chunks_for(nt, b.ntiles, GRX_THREADS / 32);
       block_bead_pass<PREC>(b, beads, nt, a.comp, a.newmol, -1, -1, qbuf, ipart, iflag, &counter, nch);
       __syncthreads();
-      reduce_items(ipart, iflag, nt, 1, nch, te, tflag);
+      reduce_items<PREC>(ipart, iflag, nt, 1, nch, te, tflag);
       __syncthreads();
     }
     // 3. select the first bead
@@ -250,7 +250,7 @@ __global__ void __launch_bounds__(GRX_THREADS, 3) widom_kernel(BoxDev b, WidomAr
         double vx = pa.x - t0.x, vy = pa.y - t0.y, vz = pa.z - t0.z;
         rotate_quaternion(vx, vy, vz, u01(r[0]), u01(r[1]), u01(r[2]));
         make_bead(beads[tid], fx + vx, fy + vy, fz + vz, b.charge[off + 1 + at] * a.scale_coul, a.scale,
-                  b.meta[off + 1 + at].x);
+                  b.meta[off + 1 + at].x, b.prefactor);
       }
       if (tid == 0) counter = 0;
       __syncthreads();
@@ -258,7 +258,7 @@ __global__ void __launch_bounds__(GRX_THREADS, 3) widom_kernel(BoxDev b, WidomAr
       const int nch = chunks_for(nb, b.ntiles, GRX_THREADS / 32);
       block_bead_pass<PREC>(b, beads, nb, a.comp, a.newmol, -1, -1, qbuf, ipart, iflag, &counter, nch);
       __syncthreads();
-      reduce_items(ipart, iflag, no, chain, nch, te, tflag);
+      reduce_items<PREC>(ipart, iflag, no, chain, nch, te, tflag);
       __syncthreads();
       if (tid < 32) {
         int sel = -1, nok = 0;
