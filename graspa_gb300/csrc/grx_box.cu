@@ -651,6 +651,7 @@ grx_status grx_box_set_component(grx_box* b, int32_t comp, const grx_atoms* a, i
     b->h_scale_coul[o + i] = scc[i];
   }
   b->size[comp] = (int)a->size;
+  b->stored[comp] = nst;
   b->rigid[comp] = rigid;
   b->has_charge[comp] = charged ? 1 : 0;
   if (nst) {

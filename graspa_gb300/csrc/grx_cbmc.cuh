@@ -1,0 +1,347 @@
+// grx_cbmc.cuh -- block-level CBMC stages shared by the Widom and GCMC kernels.
+//
+// Every function here is called by all threads of a block (GRX_THREADS) with the
+// same arguments; each ends with the block synchronised and its results in the
+// shared-memory workspace CbmcWork. The stages restate gRASPA's CBMC move pieces:
+//   gen_first_trials  get_random_trial_position      mc_widom.h:122-213
+//   gen_orientations  get_random_trial_orientation   mc_widom.h:215-303
+//   trial_pass        Calculate_Multiple_Trial_Energy_VDWReal + host sums
+//                     (VDW_Coulomb.cu:1183-1352, mc_widom.h:42-87)
+//   step_weight       SelectTrialPosition + CBMC_FirstBead_Finish / chain finish
+//                     (mc_widom.h:14-39, 305-383, 568-611)
+//   ewald_move        Initialize_WaveVector_General + Fourier_Ewald_Diff
+//                     (Ewald_Energy_Functions.h:162-185, 280-397)
+#pragma once
+
+#include "grx_warp.cuh"
+
+namespace grx {
+
+constexpr int kMaxTrials = 64;
+constexpr int kMolWork = 32;  // atoms of one molecule held in shared memory
+
+struct CbmcWork {
+  Bead beads[GRX_MAX_TRIAL_BEADS];
+  double ipart[kMaxItems * 4];
+  int iflag[kMaxItems];
+  int qbuf[(GRX_THREADS / 32) * kQueue];
+  double te[kMaxTrials * 4];
+  int tflag[kMaxTrials];
+  double sel_ws[kMaxTrials], sel_wa[kMaxTrials];
+  // moved atoms of the Ewald delta: [0, n_old) leave (charge stored negated),
+  // [n_old, n_old + n_new) arrive
+  double mx[2 * kMolWork], my[2 * kMolWork], mz[2 * kMolWork], mq[2 * kMolWork];
+  double sbuf[32];
+  double wsum[2][GRX_THREADS / 32];
+  float2 qd[2 * kMolWork];
+  int counter;
+  int ok;       // step constructed
+  int sel;      // chosen (or retraced) trial index
+  int nok;      // trials without overlap
+  double w;     // averaged weight of the step
+};
+
+// ---------------------------------------------------------------- trials
+// First-bead trial positions: Cell diagonal x Philox uniforms (mc_widom.h:133-139);
+// with `retrace`, trial 0 is the existing bead (deletion, mc_widom.h:141-156).
+__device__ __forceinline__ void gen_first_trials(const BoxDev& b, CbmcWork& W, uint64_t seed, uint32_t stream,
+                                                 uint64_t move, int nt, double q, double scale, int type,
+                                                 bool retrace, double ox, double oy, double oz) {
+  const int t = threadIdx.x;
+  if (t < nt) {
+    if (retrace && t == 0) {
+      make_bead(W.beads[0], ox, oy, oz, q, scale, type, b.prefactor);
+    } else {
+      uint32_t r[4];
+      draw4(seed, stream, move, SLOT_FIRST + t, r);
+      make_bead(W.beads[t], b.cell[0] * u01(r[0]), b.cell[4] * u01(r[1]), b.cell[8] * u01(r[2]), q, scale, type,
+                b.prefactor);
+    }
+  }
+  __syncthreads();
+}
+
+// Rotate_Quaternions (mc_utilities.h:423-457): uniform rotation from (u, v, w).
+__device__ __forceinline__ void rotate_quaternion(double& x, double& y, double& z, double u, double v,
+                                                  double w) {
+  const double pi = 3.14159265358979323846;
+  double s1, c1, s2, c2;
+  sincos(2 * pi * v, &s1, &c1);
+  sincos(2 * pi * w, &s2, &c2);
+  const double q0 = sqrt(1 - u) * s1;
+  const double q1 = sqrt(1 - u) * c1;
+  const double q2 = sqrt(u) * s2;
+  const double q3 = sqrt(u) * c2;
+  const double a01 = q0 * q1, a02 = q0 * q2, a03 = q0 * q3;
+  const double a11 = q1 * q1, a12 = q1 * q2, a13 = q1 * q3;
+  const double a22 = q2 * q2, a23 = q2 * q3, a33 = q3 * q3;
+  const double r0 = 1.0 - 2.0 * (a22 + a33), r1 = 2.0 * (a12 - a03), r2 = 2.0 * (a13 + a02);
+  const double r3 = 2.0 * (a12 + a03), r4 = 1.0 - 2.0 * (a11 + a33), r5 = 2.0 * (a23 - a01);
+  const double r6 = 2.0 * (a13 - a02), r7 = 2.0 * (a23 + a01), r8 = 1.0 - 2.0 * (a11 + a22);
+  const double nx = x * r0 + y * r1 + z * r2;
+  const double ny = x * r3 + y * r4 + z * r5;
+  const double nz = x * r6 + y * r7 + z * r8;
+  x = nx; y = ny; z = nz;
+}
+
+// Trial orientations about the chosen first bead (fx, fy, fz): the vectors from the
+// component's slot-0 atom to its chain atoms, rotated by Philox quaternions. With
+// `retrace`, orientation 0 is the existing chain (ox/oy/oz arrays, chain atoms).
+__device__ __forceinline__ void gen_orientations(const BoxDev& b, CbmcWork& W, uint64_t seed, uint32_t stream,
+                                                 uint64_t move, int no, int chain, int off, double scale_coul,
+                                                 double scale, double fx, double fy, double fz, bool retrace,
+                                                 const double* ox, const double* oy, const double* oz) {
+  const int tid = threadIdx.x;
+  if (tid < no * chain) {
+    const int o = tid / chain, at = tid % chain;
+    const double q = b.charge[off + 1 + at] * scale_coul;
+    const int type = b.meta[off + 1 + at].x;
+    if (retrace && o == 0) {
+      make_bead(W.beads[tid], ox[at], oy[at], oz[at], q, scale, type, b.prefactor);
+    } else {
+      uint32_t r[4];
+      draw4(seed, stream, move, SLOT_ORIENT + o, r);
+      const double4 t0 = b.pos64[off];
+      const double4 pa = b.pos64[off + 1 + at];
+      double vx = pa.x - t0.x, vy = pa.y - t0.y, vz = pa.z - t0.z;
+      rotate_quaternion(vx, vy, vz, u01(r[0]), u01(r[1]), u01(r[2]));
+      make_bead(W.beads[tid], fx + vx, fy + vy, fz + vz, q, scale, type, b.prefactor);
+    }
+  }
+  __syncthreads();
+}
+
+// Energies of ntr = nb / chain trials of `chain` beads each (W.beads) against every
+// atom, with the atoms of (comp, newmol) excluded: W.te[4 t + k], W.tflag[t].
+template <int PREC>
+__device__ __forceinline__ void trial_pass(const BoxDev& b, CbmcWork& W, int nb, int chain, int comp, int newmol) {
+  if (threadIdx.x == 0) W.counter = 0;
+  __syncthreads();
+  const int nch = chunks_for(nb, b.ntiles, GRX_THREADS / 32);
+  block_bead_pass<PREC>(b, W.beads, nb, comp, newmol, -1, -1, W.qbuf, W.ipart, W.iflag, &W.counter, nch);
+  __syncthreads();
+  reduce_items<PREC>(W.ipart, W.iflag, nb / chain, chain, nch, W.te, W.tflag);
+  __syncthreads();
+}
+
+// CBMC weight of one growth step (warp 0 computes, results in W.ok/sel/w/nok).
+// Insertion: log-sum-exp selection with the uniform u (SelectTrialPosition) and the
+// 1e-150 failure test. Retrace (deletion): the first trial without overlap is the
+// existing configuration and no selection is drawn. Exponentials are evaluated one
+// trial per lane; sums and the cumulative search stay sequential in trial order.
+__device__ __forceinline__ void step_weight(CbmcWork& W, int nt, double beta, int bias, double u, double navg,
+                                            bool retrace) {
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+    double lw[2];
+    bool ok[2];
+    double mx = -INFINITY;
+    int cnt = 0;
+    for (int r = 0; r < 2; ++r) {
+      const int t = lane + 32 * r;
+      ok[r] = t < nt && !W.tflag[t];
+      lw[r] = -INFINITY;
+      if (ok[r]) {
+        double tot = W.te[4 * t] + W.te[4 * t + 2];
+        if (bias) tot += W.te[4 * t + 1] + W.te[4 * t + 3];
+        lw[r] = __dmul_rn(-beta, tot);
+        mx = fmax(mx, lw[r]);
+        ++cnt;
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+      cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+    }
+    for (int r = 0; r < 2; ++r) {
+      const int t = lane + 32 * r;
+      if (t < nt) {
+        W.sel_ws[t] = ok[r] ? exp(__dsub_rn(lw[r], mx)) : 0.0;
+        W.sel_wa[t] = ok[r] ? exp(lw[r]) : 0.0;
+      }
+    }
+    __syncwarp();
+    if (lane == 0) {
+      W.nok = cnt;
+      W.ok = 0;
+      if (cnt > 0) {
+        int s = -1;
+        if (retrace) {
+          for (int t = 0; t < nt; ++t)
+            if (!W.tflag[t]) { s = t; break; }
+        } else {
+          double sum = 0.0;
+          for (int t = 0; t < nt; ++t)
+            if (!W.tflag[t]) sum += W.sel_ws[t];
+          const double wsel = u * sum;
+          int left = cnt;
+          double cum = 0.0;
+          for (int t = 0; t < nt; ++t) {
+            if (W.tflag[t]) continue;
+            cum += W.sel_ws[t];
+            s = t;
+            --left;
+            if (!(cum < wsel) || left == 0) break;
+          }
+        }
+        double w = 0.0;
+        for (int t = 0; t < nt; ++t)
+          if (!W.tflag[t]) w += W.sel_wa[t];
+        if (retrace || !(w < 1e-150)) {
+          double avg = w / navg;
+          if (!bias) avg *= exp(-beta * (W.te[4 * s + 1] + W.te[4 * s + 3]));
+          W.ok = 1;
+          W.sel = s;
+          W.w = avg;
+        }
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------- Ewald
+// Fourier delta of the na moved atoms in W.mx/my/mz/mq (old atoms carry -q):
+// dS(k) = sum q e^{ik.r}; same = sum temp (|S + dS|^2 - |S|^2), cross = sum temp
+// Re(S_cross dS*), S_same = adsorbate block (guest moves). The FP64 form follows
+// the reference arithmetic; the other forms evaluate dS and both sums in
+// double-float on the FP32 pipe against temp*S tables (ewA, ewF). When s_out is
+// given, S_same + dS is staged there (FP64) for a later commit. Results on thread 0.
+template <int PREC>
+__device__ __forceinline__ void ewald_move(const BoxDev& b, CbmcWork& W, int na, double2* eik, double2* s_out,
+                                           double& same, double& cross) {
+  const int tid = threadIdx.x;
+  const int kx1 = b.kmax[0] + 1, ky1 = b.kmax[1] + 1;
+  double2* ex = eik;
+  double2* ey = ex + kx1 * na;
+  double2* ez = ey + ky1 * na;
+  const double PI2 = 2.0 * 3.14159265358979323846;
+  if (tid < 3 * na) {  // eik recurrence per atom and axis (Initialize_Vectors_thread)
+    const int at = tid % na, d = tid / na;
+    const double s = (b.inv[d] * W.mx[at] + b.inv[3 + d] * W.my[at] + b.inv[6 + d] * W.mz[at]) * PI2;
+    double2* tab = d == 0 ? ex : (d == 1 ? ey : ez);
+    const int km = b.kmax[d];
+    tab[at] = make_double2(1.0, 0.0);
+    if (km >= 1) {
+      double sn, cs;
+      sincos(s, &sn, &cs);
+      const double2 e1 = make_double2(cs, sn);
+      double2 e = e1;
+      tab[at + na] = e1;
+      for (int k = 2; k <= km; ++k) {
+        e = cmul(e, e1);
+        tab[at + k * na] = e;
+      }
+    }
+  }
+  __syncthreads();
+  same = 0.0;
+  cross = 0.0;
+  if constexpr (PREC == GRX_FP64) {
+    for (int j = tid; j < b.nact; j += blockDim.x) {
+      const int4 k = b.kact[j];
+      double2 dsk = make_double2(0.0, 0.0);
+      for (int at = 0; at < na; ++at) {
+        double2 y = ey[at + na * abs(k.y)];
+        if (k.y < 0) y.y = -y.y;
+        double2 z = ez[at + na * abs(k.z)];
+        if (k.z < 0) z.y = -z.y;
+        const double2 t = cmul(cmul(ex[at + na * k.x], y), z);
+        dsk.x += W.mq[at] * t.x;
+        dsk.y += W.mq[at] * t.y;
+      }
+      const double tmp = b.ktemp[j];
+      const double2 ov = b.s_ads[k.w];
+      const double2 nv = make_double2(ov.x + dsk.x, ov.y + dsk.y);
+      same += tmp * (nv.x * nv.x + nv.y * nv.y);
+      same -= tmp * (ov.x * ov.x + ov.y * ov.y);
+      const double2 xv = b.s_fw[k.w];
+      cross += tmp * (xv.x * dsk.x + xv.y * dsk.y);
+      if (s_out) s_out[k.w] = nv;
+    }
+    same = block_sum(same, W.sbuf);
+    cross = block_sum(cross, W.sbuf);
+  } else {
+    float4* fx = reinterpret_cast<float4*>(ez + (b.kmax[2] + 1) * na);
+    const int ntab = (b.kmax[0] + b.kmax[1] + b.kmax[2] + 3) * na;
+    for (int e = tid; e < ntab; e += blockDim.x) {
+      const df re = df_from(ex[e].x), im = df_from(ex[e].y);
+      fx[e] = make_float4(re.hi, re.lo, im.hi, im.lo);
+    }
+    if (tid < na) { const df q = df_from(W.mq[tid]); W.qd[tid] = make_float2(q.hi, q.lo); }
+    __syncthreads();
+    const float4* fy = fx + kx1 * na;
+    const float4* fz = fy + ky1 * na;
+    df sm = {0.f, 0.f}, cr = {0.f, 0.f};
+    for (int j = tid; j < b.nact; j += blockDim.x) {
+      const int4 k = b.kact[j];
+      df cre = {0.f, 0.f}, cim = {0.f, 0.f};
+      const int ay = abs(k.y), az = abs(k.z);
+      const float sy = k.y < 0 ? -1.f : 1.f, sz = k.z < 0 ? -1.f : 1.f;
+      for (int at = 0; at < na; ++at) {
+        const float4 X = fx[at + na * k.x], Y = fy[at + na * ay], Z = fz[at + na * az];
+        const df xr = {X.x, X.y}, xi = {X.z, X.w};
+        const df yr = {Y.x, Y.y}, yi = {sy * Y.z, sy * Y.w};
+        const df zr = {Z.x, Z.y}, zi = {sz * Z.z, sz * Z.w};
+        const df pr = df_add(df_mul(xr, yr), df_mul(df{-xi.hi, -xi.lo}, yi));
+        const df pi = df_add(df_mul(xr, yi), df_mul(xi, yr));
+        const df tr = df_add(df_mul(pr, zr), df_mul(df{-pi.hi, -pi.lo}, zi));
+        const df ti = df_add(df_mul(pr, zi), df_mul(pi, zr));
+        const df q = {W.qd[at].x, W.qd[at].y};
+        cre = df_add(cre, df_mul(q, tr));
+        cim = df_add(cim, df_mul(q, ti));
+      }
+      const float4 A = b.ewA[j], F = b.ewF[j];
+      const float2 T = b.ewT[j];
+      const df reA = df_add(df_mul(df{A.x, A.y}, cre), df_mul(df{A.z, A.w}, cim));
+      const df n2 = df_add(df_mul(cre, cre), df_mul(cim, cim));
+      sm = df_add(sm, df_add(df{2.f * reA.hi, 2.f * reA.lo}, df_mul(df{T.x, T.y}, n2)));
+      cr = df_add(cr, df_add(df_mul(df{F.x, F.y}, cre), df_mul(df{F.z, F.w}, cim)));
+      if (s_out) {  // compensated update: FP64 S plus the double-float dS
+        const double2 ov = b.s_ads[k.w];
+        s_out[k.w] = make_double2(ov.x + df_to(cre), ov.y + df_to(cim));
+      }
+    }
+    sm = warp_sum_df(sm);
+    cr = warp_sum_df(cr);
+    if ((tid & 31) == 0) { W.wsum[0][tid >> 5] = df_to(sm); W.wsum[1][tid >> 5] = df_to(cr); }
+    __syncthreads();
+    if (tid == 0)
+      for (int w = 0; w < GRX_THREADS / 32; ++w) { same += W.wsum[0][w]; cross += W.wsum[1][w]; }
+  }
+  __syncthreads();
+}
+
+// Make the staged structure factor current and refresh its double-float table.
+__device__ __forceinline__ void commit_sk(const BoxDev& b, const double2* s_tmp) {
+  float4* ewA = const_cast<float4*>(b.ewA);
+  for (int j = threadIdx.x; j < b.nact; j += blockDim.x) {
+    const int slot = b.kact[j].w;
+    const double2 v = s_tmp[slot];
+    b.s_ads[slot] = v;
+    const double t = b.ktemp[j];
+    const df ar = df_from(t * v.x), ai = df_from(t * v.y);
+    ewA[j] = make_float4(ar.hi, ar.lo, ai.hi, ai.lo);
+  }
+  __syncthreads();
+}
+
+// Write one atom into the box storage (all representations).
+__device__ __forceinline__ void store_atom(const BoxDev& b, int idx, double x, double y, double z, double charge,
+                                           double scale_coul, double scale, int type, int molid) {
+  const double qe = charge * scale_coul;
+  const_cast<double4*>(b.pos64)[idx] = make_double4(x, y, z, qe);
+  float hx, lx, hy, ly, hz, lz;
+  split_coord(x, hx, lx);
+  split_coord(y, hy, ly);
+  split_coord(z, hz, lz);
+  const_cast<float4*>(b.hi)[idx] = make_float4(hx, hy, hz, (float)qe);
+  const_cast<float4*>(b.lo)[idx] = make_float4(lx, ly, lz, (float)scale);
+  const_cast<int2*>(b.meta)[idx] = make_int2(type, molid);
+  const_cast<double*>(b.scale)[idx] = scale;
+  const_cast<double*>(b.charge)[idx] = charge;
+  const df q = df_from(qe);
+  const_cast<float2*>(b.qdf)[idx] = make_float2(q.hi, q.lo);
+}
+
+}  // namespace grx

@@ -20,6 +20,7 @@ struct grx_box {
   int size[GRX_MAX_COMPONENTS] = {};
   int rigid[GRX_MAX_COMPONENTS] = {};
   int has_charge[GRX_MAX_COMPONENTS] = {};
+  size_t stored[GRX_MAX_COMPONENTS] = {};  // atoms written to storage (template included)
   double excl_intra[GRX_MAX_COMPONENTS] = {};
   double excl_self[GRX_MAX_COMPONENTS] = {};
   size_t total_cap = 0;

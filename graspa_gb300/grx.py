@@ -88,6 +88,20 @@ WIDOM_RESULT_DTYPE = np.dtype([("rosenbluth", "f8"), ("w_first", "f8"), ("w_chai
                                ("n_ok_orient", "i8"), ("success", "i4"), ("pad_", "i4")])
 assert WIDOM_RESULT_DTYPE.itemsize == C.sizeof(WidomResult)
 
+
+class GcmcDesc(C.Structure):
+    _fields_ = [("component", C.c_int32), ("ntrials", C.c_int32), ("norient", C.c_int32),
+                ("pad_", C.c_int32), ("p_translation", C.c_double), ("p_rotation", C.c_double),
+                ("p_swap", C.c_double), ("max_translation", C.c_double * 3), ("max_rotation", C.c_double * 3),
+                ("beta", C.c_double), ("pressure", C.c_double), ("fugacity_coeff", C.c_double),
+                ("mol_fraction", C.c_double), ("ideal_rosenbluth", C.c_double), ("tail_insert", C.c_double),
+                ("seed", C.c_uint64), ("stream", C.c_uint32), ("pad2_", C.c_uint32)]
+
+
+class GcmcStats(C.Structure):
+    _fields_ = [("attempts", C.c_int64 * 4), ("accepted", C.c_int64 * 4), ("n_molecules", C.c_int64),
+                ("capacity_hits", C.c_int64), ("energy", C.c_double * 4), ("sum_n", C.c_double)]
+
 # every symbol include/grx.h declares
 EXPORTS = [
     "grx_status_string", "grx_last_error", "grx_device_count", "grx_box_create", "grx_box_destroy",
@@ -95,7 +109,7 @@ EXPORTS = [
     "grx_box_get_exclusion", "grx_trial_energies", "grx_single_body_energy", "grx_ewald_sizes",
     "grx_ewald_total", "grx_ewald_set_structure_factors", "grx_ewald_get_structure_factors",
     "grx_ewald_delta", "grx_ewald_commit", "grx_total_energy", "grx_cbmc_select",
-    "grx_widom_insertions", "grx_widom_insertions_async", "grx_launch_count", "grx_trial_energies_noalloc",
+    "grx_widom_insertions", "grx_widom_insertions_async", "grx_launch_count", "grx_trial_energies_noalloc", "grx_gcmc_run",
 ]
 
 _lib = None
@@ -146,6 +160,8 @@ def load(path=LIB_PATH):
     L.grx_launch_count.restype = C.c_uint64
     L.grx_trial_energies_noalloc.argtypes = [C.c_void_p, P(Trials), C.c_int32, C.c_int64, C.c_int64, C.c_int32,
                                              P(TrialEnergy), _u8p]
+    L.grx_gcmc_run.argtypes = [P(C.c_void_p), C.c_int32, P(GcmcDesc), C.c_uint64, C.c_int64, C.c_int32,
+                               P(GcmcStats)]
     _lib = L
     return L
 
@@ -290,6 +306,18 @@ class Box:
             rigid = 1 if c >= self.nhost else 0
         check(self.L.grx_box_set_component(self.h, c, C.byref(a), int(rigid)), "grx_box_set_component")
 
+    def component_size(self, c):
+        n = C.c_size_t()
+        check(self.L.grx_box_get_component_size(self.h, c, C.byref(n)), "grx_box_get_component_size")
+        return n.value
+
+    def positions(self, c, n=None):
+        """Atom positions of component c in storage order (caller order for hosts)."""
+        n = self.component_size(c) if n is None else n
+        out = np.zeros(3 * n)
+        check(self.L.grx_box_get_positions(self.h, c, _d(out), n), "grx_box_get_positions")
+        return out.reshape(-1, 3)
+
     # --- Ewald ---------------------------------------------------------
     def ewald_sizes(self):
         nv, na = C.c_int64(), C.c_int64()
@@ -425,6 +453,37 @@ def widom_desc(system, component, ntrials=10, norient=10, temperature=None, seed
     d.seed = seed
     d.stream = stream
     return d
+
+
+def gcmc_desc(component, ntrials=10, norient=10, p_translation=0.25, p_rotation=0.5, p_swap=1.0,
+              max_translation=1.0, max_rotation=0.5, temperature=300.0, pressure_pa=1e5, fugacity_coeff=1.0,
+              mol_fraction=1.0, ideal_rosenbluth=1.0, tail_insert=0.0, seed=42, stream=0):
+    """GCMC move mix of one box; probabilities are cumulative as in Move_Statistics,
+    pressure in Pa converted to internal units (fxn_main.h:120)."""
+    d = GcmcDesc()
+    d.component, d.ntrials, d.norient = component, ntrials, norient
+    d.p_translation, d.p_rotation, d.p_swap = p_translation, p_rotation, p_swap
+    for k in range(3):
+        d.max_translation[k] = max_translation
+        d.max_rotation[k] = max_rotation
+    d.beta = beta_from_temperature(temperature)
+    d.pressure = pressure_pa / 1.6605402e7
+    d.fugacity_coeff, d.mol_fraction, d.ideal_rosenbluth = fugacity_coeff, mol_fraction, ideal_rosenbluth
+    d.tail_insert = tail_insert
+    d.seed, d.stream = seed, stream
+    return d
+
+
+def gcmc_run(boxes, descs, first_step, nsteps, prec=GRX_MIXED):
+    """Run nsteps GCMC moves on every box in one persistent launch; returns one
+    GcmcStats per box."""
+    L = load()
+    n = len(boxes)
+    hs = (C.c_void_p * n)(*[b.h for b in boxes])
+    ds = (GcmcDesc * n)(*descs)
+    st = (GcmcStats * n)()
+    check(L.grx_gcmc_run(hs, n, ds, first_step, nsteps, prec, st), "grx_gcmc_run")
+    return list(st)
 
 
 def cbmc_select(logw, seed, stream, move, word):

@@ -50,11 +50,15 @@ typedef int32_t grx_status;
 
 /* Arithmetic of the pair and Ewald evaluation.
  *   GRX_FP64  : every operation in FP64 (the reference's arithmetic).
- *   GRX_MIXED : FP32 cutoff screening on split hi/lo coordinates; pairs inside
- *               the cutoff re-evaluated from an FP64 displacement; LJ in FP32
- *               (FP64 inside 1.1 sigma), real-space Coulomb and all sums in
- *               FP64; Ewald delta in FP64. Boltzmann weights agree with FP64
- *               to beta*|dE| <= 1e-6.
+ *   GRX_MIXED : FP32 cutoff screening on split hi/lo coordinates (hi on a
+ *               2^-12 A grid, so hi differences are exact); pairs inside the
+ *               cutoff are compacted per warp and evaluated in double-float
+ *               arithmetic on the FP32 pipe (LJ and the tabulated erfc(alpha r)/r
+ *               of real-space Coulomb); per-trial sums in double-float, then
+ *               FP64. The Ewald delta runs in double-float against temp*S(k)
+ *               tables and S(k) is updated in FP64 (compensated). FP64 is kept
+ *               for self / exclusion terms and exp(-beta dE). Boltzmann weights
+ *               agree with FP64 to beta*|dE| <= 1e-6.
  *   GRX_FP32  : FP32 pair math with FP64 sums; fastest, error reported, not
  *               within 1e-6 for charged systems. */
 typedef enum { GRX_FP64 = 0, GRX_MIXED = 1, GRX_FP32 = 2 } grx_precision;
@@ -274,6 +278,52 @@ grx_status grx_widom_insertions(grx_box* box, const grx_widom_desc* desc,
 grx_status grx_widom_insertions_async(grx_box* box, const grx_widom_desc* desc,
                                       uint64_t first_move, size_t n, grx_precision prec,
                                       grx_widom_result* results);
+
+/* ---- GCMC ----------------------------------------------------------------- */
+/* Move mix and thermodynamic state of one box's GCMC run: the translation /
+ * rotation / CBMC swap branches of RunMoves (axpy.cu:102-298) with the move
+ * probabilities of Move_Statistics (cumulative, as the reference stores them),
+ * get_new_position (mc_utilities.h:485-606) and GetPrefactor (mc_utilities.h:315-351). */
+typedef struct {
+  int32_t component;          /* the adsorbate component moved / exchanged */
+  int32_t ntrials;            /* NumberOfTrialPositions */
+  int32_t norient;            /* NumberOfTrialOrientations */
+  int32_t pad_;
+  double p_translation;       /* TranslationProb (cumulative) */
+  double p_rotation;          /* RotationProb (cumulative) */
+  double p_swap;              /* SwapProb (cumulative); insertion / deletion 50:50 */
+  double max_translation[3];  /* MaxTranslation, A */
+  double max_rotation[3];     /* MaxRotation, rad */
+  double beta;
+  double pressure;            /* internal units (Pa / 1.6605402e7) */
+  double fugacity_coeff;
+  double mol_fraction;
+  double ideal_rosenbluth;    /* IdealGasRosenbluthWeight */
+  double tail_insert;         /* TailCorrectionDifference of one insertion; a
+                                 deletion uses its negative (exact for the
+                                 host-guest tail, which is linear in N) */
+  uint64_t seed;              /* Philox key */
+  uint32_t stream;            /* Philox counter word 3 (chain id) */
+  uint32_t pad2_;
+} grx_gcmc_desc;
+
+typedef struct {
+  int64_t attempts[4];        /* translation, rotation, insertion, deletion */
+  int64_t accepted[4];
+  int64_t n_molecules;        /* after the run */
+  int64_t capacity_hits;      /* insertions refused for lack of component capacity */
+  double energy[4];           /* sum of accepted dE: VDW, real Coulomb, Ewald Fourier, total */
+  double sum_n;               /* sum over steps of N (loading average = sum_n / steps) */
+} grx_gcmc_stats;
+
+/* nsteps GCMC moves on each of nboxes independent boxes (Markov chains), all on the
+ * device in one persistent launch: one block per box, positions and S(k) resident.
+ * Step s of a box uses Philox move index first_step + s on the box's stream.
+ * stats[i] receives box i's counts for this call. Requires current structure
+ * factors (grx_ewald_total or grx_ewald_set_structure_factors). */
+grx_status grx_gcmc_run(grx_box* const* boxes, int32_t nboxes, const grx_gcmc_desc* descs,
+                        uint64_t first_step, int64_t nsteps, grx_precision prec,
+                        grx_gcmc_stats* stats);
 
 /* ---- allocation-free trial energies ------------------------------------- */
 /* grx_trial_energies without any device allocation at call time. No counterpart

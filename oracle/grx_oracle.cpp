@@ -792,3 +792,370 @@ void ora_widom_insertions(const ora_box* box, const ora_ff* ff, const ora_atoms*
 }
 
 }  // extern "C"
+
+// ----------------------------------------------------------------------------
+// GCMC (test oracle): translation, rotation, CBMC insertion and CBMC deletion of
+// one adsorbate component, sequential FP64, the same Philox stream layout as the
+// device driver: slot 4096 = {molecule pick, move choice, insertion-vs-deletion,
+// acceptance}, slot 4097 = {three uniforms of the displacement / rotation angles},
+// CBMC trials in slots 0..2047 and the selection uniforms in slot 2048.
+namespace {
+
+struct GState {
+  std::vector<double> pos, scale, charge, scc;
+  std::vector<int64_t> type, molid;
+  std::vector<int64_t> comp_start;
+  int64_t ncomp = 0, nhost = 0;
+  ora_atoms view() {
+    ora_atoms a;
+    a.ncomp = ncomp;
+    a.nhost = nhost;
+    a.comp_start = comp_start.data();
+    a.pos = pos.data();
+    a.scale = scale.data();
+    a.charge = charge.data();
+    a.scale_coul = scc.data();
+    a.type = type.data();
+    a.molid = molid.data();
+    return a;
+  }
+};
+
+struct Grow {
+  bool ok = false;
+  double rosen = 0.0;  // product of the averaged step weights
+  double e1[4] = {0, 0, 0, 0}, e2[4] = {0, 0, 0, 0};
+  std::vector<double> pos, qs;  // chosen (insertion) or existing (deletion) molecule
+};
+
+// RotationAroundAxis, mc_utilities.h:459-481, for a coordinate axis.
+void rotate_axis(double* v, double theta, int axis) {
+  const double c = std::cos(theta), w = 1.0 - c, s = std::sin(theta);
+  double ax[3] = {0, 0, 0};
+  ax[axis] = 1.0;
+  double rot[9];
+  rot[0] = ax[0] * ax[0] * w + c;
+  rot[1] = ax[0] * ax[1] * w + ax[2] * s;
+  rot[2] = ax[0] * ax[2] * w - ax[1] * s;
+  rot[3] = ax[0] * ax[1] * w - ax[2] * s;
+  rot[4] = ax[1] * ax[1] * w + c;
+  rot[5] = ax[1] * ax[2] * w + ax[0] * s;
+  rot[6] = ax[0] * ax[2] * w + ax[1] * s;
+  rot[7] = ax[1] * ax[2] * w - ax[0] * s;
+  rot[8] = ax[2] * ax[2] * w + c;
+  const double x = v[0] * rot[0] + v[1] * rot[1] + v[2] * rot[2];
+  const double y = v[0] * rot[3] + v[1] * rot[4] + v[2] * rot[5];
+  const double z = v[0] * rot[6] + v[1] * rot[7] + v[2] * rot[8];
+  v[0] = x; v[1] = y; v[2] = z;
+}
+
+// CBMC growth of one molecule (insertion) or retrace of an existing one (deletion):
+// Widom_Move_FirstBead_PARTIAL + Widom_Move_Chain_PARTIAL (mc_widom.h:385-614) with
+// CBMC_FirstBead_Finish (:305-383), insertion and deletion branches.
+Grow cbmc_grow(const ora_box* box, const ora_ff* ff, const ora_atoms* at, int64_t comp, int64_t ms,
+               const double* tmpl_pos, const double* tmpl_q, const int64_t* tmpl_t, int64_t nt, int64_t no,
+               double beta, uint64_t seed, uint32_t stream, uint64_t move, int64_t newmol, bool deletion,
+               const double* oldpos) {
+  Grow g;
+  const int64_t chain = ms - 1;
+  uint32_t sel_words[4];
+  ora_draw(seed, stream, move, 2048u, sel_words);
+  std::vector<double> tp(3 * nt), ones(std::max<int64_t>(nt, 1), 1.0), tq(nt, tmpl_q[0]);
+  std::vector<int64_t> tty(nt, tmpl_t[0]);
+  for (int64_t t = 0; t < nt; ++t) {
+    if (deletion && t == 0) {
+      for (int d = 0; d < 3; ++d) tp[d] = oldpos[d];
+      continue;
+    }
+    uint32_t r[4];
+    ora_draw(seed, stream, move, (uint32_t)t, r);
+    tp[3 * t] = box->cell[0] * u01(r[0]);
+    tp[3 * t + 1] = box->cell[4] * u01(r[1]);
+    tp[3 * t + 2] = box->cell[8] * u01(r[2]);
+  }
+  ora_trials tr1 = {nt, 1, tp.data(), ones.data(), tq.data(), ones.data(), tty.data(), newmol};
+  std::vector<double> e1(4 * nt);
+  std::vector<uint8_t> f1(nt);
+  ora_trial_energies(box, ff, at, &tr1, comp, -1, -1, e1.data(), f1.data());
+  // log-weights of the trials without overlap (Host_sum_Widom_HGGG_SEPARATE)
+  auto logw_of = [&](const std::vector<double>& e, const std::vector<uint8_t>& f, int64_t n,
+                     std::vector<double>& lw, std::vector<int64_t>& idx) {
+    for (int64_t t = 0; t < n; ++t) {
+      if (f[t]) continue;
+      double tot = e[4 * t] + e[4 * t + 2];
+      if (ff->vdw_real_bias) tot += e[4 * t + 1] + e[4 * t + 3];
+      lw.push_back(-beta * tot);
+      idx.push_back(t);
+    }
+  };
+  std::vector<double> lw1;
+  std::vector<int64_t> idx1;
+  logw_of(e1, f1, nt, lw1, idx1);
+  if (idx1.empty()) return g;
+  int64_t s1 = 0;
+  if (!deletion) s1 = ora_select_trial(lw1.data(), (int64_t)lw1.size(), u01(sel_words[0]));
+  double w1 = 0.0;
+  for (double l : lw1) w1 += std::exp(l);
+  if (!deletion && w1 < 1e-150) return g;
+  const int64_t real1 = idx1[(size_t)s1];
+  double avg1 = w1 / (double)nt;
+  if (!ff->vdw_real_bias) avg1 *= std::exp(-beta * (e1[4 * real1 + 1] + e1[4 * real1 + 3]));
+  if (avg1 <= 1e-150) return g;
+  for (int k = 0; k < 4; ++k) g.e1[k] = e1[4 * real1 + k];
+  g.pos.assign(3 * ms, 0.0);
+  g.qs.assign(ms, 0.0);
+  const double* fb = &tp[3 * real1];
+  for (int d = 0; d < 3; ++d) g.pos[d] = fb[d];
+  g.qs[0] = tmpl_q[0];
+  double rosen = avg1;
+  if (chain > 0) {
+    std::vector<double> op(3 * no * chain), oones(no * chain, 1.0), oq(no * chain);
+    std::vector<int64_t> oty(no * chain);
+    for (int64_t o = 0; o < no; ++o) {
+      uint32_t r[4];
+      ora_draw(seed, stream, move, 1024u + (uint32_t)o, r);
+      for (int64_t a = 0; a < chain; ++a) {
+        const int64_t j = o * chain + a;
+        if (deletion && o == 0) {
+          for (int d = 0; d < 3; ++d) op[3 * j + d] = oldpos[3 * (1 + a) + d];
+        } else {
+          double v[3] = {tmpl_pos[3 * (1 + a)] - tmpl_pos[0], tmpl_pos[3 * (1 + a) + 1] - tmpl_pos[1],
+                         tmpl_pos[3 * (1 + a) + 2] - tmpl_pos[2]};
+          ora_rotate_quaternion(v, u01(r[0]), u01(r[1]), u01(r[2]));
+          for (int d = 0; d < 3; ++d) op[3 * j + d] = fb[d] + v[d];
+        }
+        oq[j] = tmpl_q[1 + a];
+        oty[j] = tmpl_t[1 + a];
+      }
+    }
+    ora_trials tr2 = {no, chain, op.data(), oones.data(), oq.data(), oones.data(), oty.data(), newmol};
+    std::vector<double> e2(4 * no);
+    std::vector<uint8_t> f2(no);
+    ora_trial_energies(box, ff, at, &tr2, comp, -1, -1, e2.data(), f2.data());
+    std::vector<double> lw2;
+    std::vector<int64_t> idx2;
+    logw_of(e2, f2, no, lw2, idx2);
+    if (idx2.empty()) return g;
+    int64_t s2 = 0;
+    if (!deletion) s2 = ora_select_trial(lw2.data(), (int64_t)lw2.size(), u01(sel_words[1]));
+    double w2 = 0.0;
+    for (double l : lw2) w2 += std::exp(l);
+    if (!deletion && w2 < 1e-150) return g;
+    const int64_t real2 = idx2[(size_t)s2];
+    double avg2 = w2 / (double)no;
+    if (!ff->vdw_real_bias) avg2 *= std::exp(-beta * (e2[4 * real2 + 1] + e2[4 * real2 + 3]));
+    for (int k = 0; k < 4; ++k) g.e2[k] = e2[4 * real2 + k];
+    rosen *= avg2;
+    if (rosen <= 1e-150) return g;
+    for (int64_t a = 0; a < chain; ++a) {
+      for (int d = 0; d < 3; ++d) g.pos[3 * (1 + a) + d] = op[3 * (real2 * chain + a) + d];
+      g.qs[1 + a] = tmpl_q[1 + a];
+    }
+  }
+  g.ok = true;
+  g.rosen = rosen;
+  return g;
+}
+
+}  // namespace
+
+extern "C" void ora_gcmc_run(const ora_box* box, const ora_ff* ff, double* pos, double* charge, int64_t* type,
+                             int64_t* molid, int64_t ncomp, int64_t nhost, int64_t* comp_size,
+                             const int64_t* comp_off, const int64_t* molsize, const double* mol_pos,
+                             const double* mol_charge, const int64_t* mol_type, double excl_intra,
+                             double excl_self, double* s_fw, double* s_ads, const ora_gcmc* g,
+                             uint64_t first_step, int64_t nsteps, ora_gcmc_stats* st) {
+  // compact working copy: every host component, then the (single, last) adsorbate component
+  const int64_t comp = g->component;
+  const int64_t ms = molsize[comp];
+  GState S;
+  S.ncomp = ncomp;
+  S.nhost = nhost;
+  S.comp_start.assign(ncomp + 1, 0);
+  for (int64_t c = 0; c < ncomp; ++c) {
+    for (int64_t i = 0; i < comp_size[c]; ++i) {
+      const int64_t k = comp_off[c] + i;
+      for (int d = 0; d < 3; ++d) S.pos.push_back(pos[3 * k + d]);
+      S.charge.push_back(charge[k]);
+      S.type.push_back(type[k]);
+      S.molid.push_back(molid[k]);
+    }
+    S.comp_start[c + 1] = S.comp_start[c] + comp_size[c];
+  }
+  S.scale.assign(S.charge.size(), 1.0);
+  S.scc.assign(S.charge.size(), 1.0);
+  const int64_t nvec = ora_ewald_nvec(box);
+  std::vector<double> s_new(2 * nvec);
+  const bool charged = !ff->no_charges;
+  // Orientation trials grow from the coordinates stored in the component's first
+  // molecule slot (AllData.pos[1+a] - AllData.pos[0], mc_widom.h:262): they follow
+  // every write to slot 0 and survive the deletion of its molecule.
+  std::vector<double> slot0(mol_pos, mol_pos + 3 * ms);
+  const double bigP = g->mol_fraction * g->pressure * g->fugacity_coeff * box->volume;
+  for (int64_t step = 0; step < nsteps; ++step) {
+    const uint64_t move = first_step + (uint64_t)step;
+    uint32_t w[4], w2[4];
+    ora_draw(g->seed, g->stream, move, 4096u, w);
+    ora_draw(g->seed, g->stream, move, 4097u, w2);
+    const int64_t a0 = S.comp_start[comp];
+    const int64_t n_atoms = S.comp_start[comp + 1] - a0;
+    const int64_t N = n_atoms / ms;
+    const int64_t mol = (int64_t)(u01(w[0]) * (double)N);
+    const double r = u01(w[1]);
+    int kind = -1;
+    if (r < g->p_translation) kind = 0;
+    else if (r < g->p_rotation) kind = 1;
+    else if (r < g->p_swap) kind = (u01(w[2]) < 0.5) ? 2 : 3;
+    const double uacc = u01(w[3]);
+    if (kind == 0 || kind == 1) {
+      if (N > 0) {
+        st->attempts[kind]++;
+        const int64_t m0 = a0 + mol * ms;
+        std::vector<double> oldp(S.pos.begin() + 3 * m0, S.pos.begin() + 3 * (m0 + ms)), newp(3 * ms);
+        if (kind == 0) {  // get_new_position TRANSLATION (mc_utilities.h:500-515)
+          double dd[3];
+          for (int d = 0; d < 3; ++d) dd[d] = g->max_translation[d] * 2.0 * (u01(w2[d]) - 0.5);
+          for (int64_t a = 0; a < ms; ++a)
+            for (int d = 0; d < 3; ++d) newp[3 * a + d] = oldp[3 * a + d] + dd[d];
+        } else {  // ROTATION (mc_utilities.h:516-540)
+          double ang[3];
+          for (int d = 0; d < 3; ++d) ang[d] = g->max_rotation[d] * 2.0 * (u01(w2[d]) - 0.5);
+          for (int64_t a = 0; a < ms; ++a) {
+            double v[3] = {oldp[3 * a] - oldp[0], oldp[3 * a + 1] - oldp[1], oldp[3 * a + 2] - oldp[2]};
+            rotate_axis(v, ang[0], 0);
+            rotate_axis(v, ang[1], 1);
+            rotate_axis(v, ang[2], 2);
+            for (int d = 0; d < 3; ++d) newp[3 * a + d] = v[d] + oldp[d];
+          }
+        }
+        std::vector<double> q(S.charge.begin() + m0, S.charge.begin() + m0 + ms), ones(ms, 1.0);
+        std::vector<int64_t> ty(S.type.begin() + m0, S.type.begin() + m0 + ms);
+        ora_atoms at = S.view();
+        ora_trials to = {1, ms, oldp.data(), ones.data(), q.data(), ones.data(), ty.data(), mol};
+        ora_trials tn = {1, ms, newp.data(), ones.data(), q.data(), ones.data(), ty.data(), mol};
+        double e6[6];
+        uint8_t fl = 0;
+        ora_single_body(box, ff, &at, &to, &tn, comp, 1, 1, e6, &fl);
+        if (!fl) {
+          double ew = 0.0;
+          if (charged) {
+            double d2[2];
+            ora_ewald_delta(box, s_ads, s_fw, 0, nullptr, ms, oldp.data(), q.data(), ms, newp.data(), q.data(),
+                            s_new.data(), d2);
+            ew = d2[0] + 2.0 * d2[1];
+          }
+          const double tot = e6[0] + e6[1] + e6[2] + e6[3] + e6[4] + e6[5] + ew;
+          const double pacc = std::exp(-g->beta * tot);
+          if (uacc < pacc) {
+            st->accepted[kind]++;
+            for (int64_t k = 0; k < 3 * ms; ++k) S.pos[3 * m0 + k] = newp[k];
+            if (mol == 0) std::copy(newp.begin(), newp.end(), slot0.begin());
+            if (charged) std::copy(s_new.begin(), s_new.end(), s_ads);
+            st->energy[0] += e6[0] + e6[2] + e6[4];
+            st->energy[1] += e6[1] + e6[3] + e6[5];
+            st->energy[2] += ew;
+            st->energy[3] += tot;
+          }
+        }
+      }
+    } else if (kind == 2) {  // CBMC insertion (InsertionMove::Run, move_struct.h:71-89)
+      st->attempts[2]++;
+      ora_atoms at = S.view();
+      Grow gr = cbmc_grow(box, ff, &at, comp, ms, slot0.data(), mol_charge, mol_type, g->ntrials, g->norient,
+                          g->beta, g->seed, g->stream, move, N, false, nullptr);
+      if (gr.ok) {
+        double ew = 0.0, rosen = gr.rosen;
+        if (charged) {
+          double d2[2];
+          ora_ewald_delta(box, s_ads, s_fw, 0, nullptr, 0, nullptr, nullptr, ms, gr.pos.data(), gr.qs.data(),
+                          s_new.data(), d2);
+          const double same = d2[0] - (excl_intra + excl_self) * (1.0 - 0.0);
+          ew = same + 2.0 * d2[1];
+          rosen *= std::exp(-g->beta * ew);
+        }
+        const double pre = g->beta * bigP / (1.0 + (double)N);  // GetPrefactor INSERTION
+        const double pacc = pre * rosen / g->ideal_rosenbluth;
+        if (rosen > 1e-150 && uacc < pacc) {
+          st->accepted[2]++;
+          const int64_t at0 = S.comp_start[comp + 1];
+          for (int64_t a = 0; a < ms; ++a) {
+            for (int d = 0; d < 3; ++d) S.pos.insert(S.pos.begin() + 3 * (at0 + a) + d, gr.pos[3 * a + d]);
+            S.charge.insert(S.charge.begin() + at0 + a, mol_charge[a]);
+            S.type.insert(S.type.begin() + at0 + a, mol_type[a]);
+            S.molid.insert(S.molid.begin() + at0 + a, N);
+            S.scale.insert(S.scale.begin() + at0 + a, 1.0);
+            S.scc.insert(S.scc.begin() + at0 + a, 1.0);
+          }
+          for (int64_t c = comp + 1; c <= ncomp; ++c) S.comp_start[c] += ms;
+          if (N == 0) std::copy(gr.pos.begin(), gr.pos.end(), slot0.begin());
+          if (charged) std::copy(s_new.begin(), s_new.end(), s_ads);
+          const double ev = gr.e1[0] + gr.e1[2] + gr.e2[0] + gr.e2[2];
+          const double er = gr.e1[1] + gr.e1[3] + gr.e2[1] + gr.e2[3];
+          st->energy[0] += ev;
+          st->energy[1] += er;
+          st->energy[2] += ew;
+          st->energy[3] += ev + er + ew;
+        }
+      }
+    } else if (kind == 3 && N > 0) {  // CBMC deletion (DeletionMove::Run, move_struct.h:148-167)
+      st->attempts[3]++;
+      const int64_t m0 = a0 + mol * ms;
+      std::vector<double> oldp(S.pos.begin() + 3 * m0, S.pos.begin() + 3 * (m0 + ms));
+      ora_atoms at = S.view();
+      Grow gr = cbmc_grow(box, ff, &at, comp, ms, slot0.data(), mol_charge, mol_type, g->ntrials, g->norient,
+                          g->beta, g->seed, g->stream, move, mol, true, oldp.data());
+      if (gr.ok) {
+        double rosen = gr.rosen, ew = 0.0;
+        std::vector<double> q(S.charge.begin() + m0, S.charge.begin() + m0 + ms);
+        if (charged) {
+          double d2[2];
+          ora_ewald_delta(box, s_ads, s_fw, 0, nullptr, ms, oldp.data(), q.data(), 0, nullptr, nullptr,
+                          s_new.data(), d2);
+          const double same = d2[0] - (excl_intra + excl_self) * (0.0 - 1.0);
+          ew = same + 2.0 * d2[1];
+          rosen /= std::exp(-g->beta * ew);
+        }
+        const double pre = (double)N / (g->beta * bigP);  // GetPrefactor DELETION
+        const double pacc = pre * g->ideal_rosenbluth / rosen;
+        if (uacc < pacc) {
+          st->accepted[3]++;
+          const int64_t last = a0 + (N - 1) * ms;
+          if (mol == 0 && N > 1)
+            for (int64_t k = 0; k < 3 * ms; ++k) slot0[k] = S.pos[3 * last + k];
+          for (int64_t a = 0; a < ms; ++a) {  // Update_deletion_data_Parallel: last molecule into the slot
+            for (int d = 0; d < 3; ++d) S.pos[3 * (m0 + a) + d] = S.pos[3 * (last + a) + d];
+            S.charge[m0 + a] = S.charge[last + a];
+            S.type[m0 + a] = S.type[last + a];
+          }
+          S.pos.erase(S.pos.begin() + 3 * last, S.pos.begin() + 3 * (last + ms));
+          S.charge.erase(S.charge.begin() + last, S.charge.begin() + last + ms);
+          S.type.erase(S.type.begin() + last, S.type.begin() + last + ms);
+          S.molid.erase(S.molid.begin() + last, S.molid.begin() + last + ms);
+          S.scale.erase(S.scale.begin() + last, S.scale.begin() + last + ms);
+          S.scc.erase(S.scc.begin() + last, S.scc.begin() + last + ms);
+          for (int64_t c = comp + 1; c <= ncomp; ++c) S.comp_start[c] -= ms;
+          if (charged) std::copy(s_new.begin(), s_new.end(), s_ads);
+          const double ev = gr.e1[0] + gr.e1[2] + gr.e2[0] + gr.e2[2];
+          const double er = gr.e1[1] + gr.e1[3] + gr.e2[1] + gr.e2[3];
+          st->energy[0] -= ev;
+          st->energy[1] -= er;
+          st->energy[2] += ew;
+          st->energy[3] += -ev - er + ew;
+        }
+      }
+    }
+    st->sum_n += (double)((S.comp_start[comp + 1] - S.comp_start[comp]) / ms);
+  }
+  // write the state back (component regions from comp_off)
+  for (int64_t c = 0; c < ncomp; ++c) {
+    comp_size[c] = S.comp_start[c + 1] - S.comp_start[c];
+    for (int64_t i = 0; i < comp_size[c]; ++i) {
+      const int64_t k = comp_off[c] + i, j = S.comp_start[c] + i;
+      for (int d = 0; d < 3; ++d) pos[3 * k + d] = S.pos[3 * j + d];
+      charge[k] = S.charge[j];
+      type[k] = S.type[j];
+      molid[k] = S.molid[j];
+    }
+  }
+  st->n_molecules = comp_size[comp] / ms;
+}

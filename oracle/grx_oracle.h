@@ -166,6 +166,46 @@ void ora_widom_insertions(const ora_box* box, const ora_ff* ff, const ora_atoms*
                           ora_widom_result* results);
 int32_t ora_max_threads(void);
 
+
+/* GCMC of one adsorbate component (RunMoves, axpy.cu:102-298, restricted to the
+ * translation / rotation / CBMC insertion / CBMC deletion branches). */
+typedef struct {
+  int64_t component;
+  int64_t ntrials;
+  int64_t norient;
+  double p_translation;   /* cumulative move probabilities (Move_Statistics) */
+  double p_rotation;
+  double p_swap;
+  double max_translation[3];
+  double max_rotation[3];
+  double beta;
+  double pressure;        /* internal units */
+  double fugacity_coeff;
+  double mol_fraction;
+  double ideal_rosenbluth;
+  uint64_t seed;
+  uint32_t stream;
+  uint32_t pad_;
+} ora_gcmc;
+
+typedef struct {
+  int64_t attempts[4];    /* translation, rotation, insertion, deletion */
+  int64_t accepted[4];
+  int64_t n_molecules;
+  int64_t pad_;
+  double energy[4];       /* running sums of accepted dE: vdw, real, ewald, total */
+  double sum_n;           /* sum of N after every step (loading average) */
+} ora_gcmc_stats;
+
+/* Runs nsteps moves on one box. atoms/s_ads are updated in place (guest component
+ * region must have room for the growth: capacity atoms from comp_start). */
+void ora_gcmc_run(const ora_box* box, const ora_ff* ff, double* pos, double* charge, int64_t* type,
+                  int64_t* molid, int64_t ncomp, int64_t nhost, int64_t* comp_size,
+                  const int64_t* comp_off, const int64_t* molsize, const double* mol_pos,
+                  const double* mol_charge, const int64_t* mol_type, double excl_intra, double excl_self,
+                  double* s_fw, double* s_ads, const ora_gcmc* g, uint64_t first_step,
+                  int64_t nsteps, ora_gcmc_stats* stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -58,6 +58,19 @@ class OraWidomResult(C.Structure):
                 ("n_ok_orient", C.c_int64), ("success", C.c_int32), ("pad_", C.c_int32)]
 
 
+class OraGcmc(C.Structure):
+    _fields_ = [("component", C.c_int64), ("ntrials", C.c_int64), ("norient", C.c_int64),
+                ("p_translation", C.c_double), ("p_rotation", C.c_double), ("p_swap", C.c_double),
+                ("max_translation", C.c_double * 3), ("max_rotation", C.c_double * 3), ("beta", C.c_double),
+                ("pressure", C.c_double), ("fugacity_coeff", C.c_double), ("mol_fraction", C.c_double),
+                ("ideal_rosenbluth", C.c_double), ("seed", C.c_uint64), ("stream", C.c_uint32), ("pad_", C.c_uint32)]
+
+
+class OraGcmcStats(C.Structure):
+    _fields_ = [("attempts", C.c_int64 * 4), ("accepted", C.c_int64 * 4), ("n_molecules", C.c_int64),
+                ("pad_", C.c_int64), ("energy", C.c_double * 4), ("sum_n", C.c_double)]
+
+
 def build(force=False):
     if force or not os.path.exists(LIB_PATH):
         subprocess.run(["make", "-C", HERE], check=True, stdout=subprocess.DEVNULL)
@@ -98,6 +111,9 @@ def lib():
         L.ora_widom_insertions.argtypes = [P(OraBox), P(OraFF), P(OraAtoms), _dp, _dp, P(OraWidom),
                                            C.c_uint64, C.c_int64, C.c_int32, P(OraWidomResult)]
         L.ora_max_threads.restype = C.c_int32
+        L.ora_gcmc_run.argtypes = [P(OraBox), P(OraFF), _dp, _dp, _i64p, _i64p, C.c_int64, C.c_int64, _i64p, _i64p,
+                                   _i64p, _dp, _dp, _i64p, C.c_double, C.c_double, _dp, _dp, P(OraGcmc), C.c_uint64,
+                                   C.c_int64, P(OraGcmcStats)]
         _lib = L
     return _lib
 
@@ -220,6 +236,61 @@ class OracleSystem:
         lib().ora_rigid_exclusion(C.byref(self.box), len(charge), _d(pos), _d(charge), _d(scale_coul),
                                   C.byref(a), C.byref(b))
         return a.value, b.value
+
+    def gcmc(self, params, capacity, first_step, nsteps):
+        """Run nsteps GCMC moves (oracle). Returns (stats, system_after, s_ads_after)."""
+        sysd = self.s
+        comp = params.component
+        cs = list(sysd["comp_start"])
+        ncomp = len(cs) - 1
+        sizes = np.array([cs[c + 1] - cs[c] for c in range(ncomp)], dtype=np.int64)
+        offs = np.zeros(ncomp, dtype=np.int64)
+        caps = [max(sizes[c], capacity[c]) for c in range(ncomp)]
+        for c in range(1, ncomp):
+            offs[c] = offs[c - 1] + caps[c - 1]
+        tot = int(offs[-1] + caps[-1])
+        pos = np.zeros(3 * tot)
+        q = np.zeros(tot)
+        ty = np.zeros(tot, dtype=np.int64)
+        mol = np.zeros(tot, dtype=np.int64)
+        P_ = np.asarray(sysd["pos"], dtype=np.float64).reshape(-1, 3)
+        for c in range(ncomp):
+            a, b = cs[c], cs[c + 1]
+            o = offs[c]
+            pos[3 * o:3 * (o + b - a)] = P_[a:b].reshape(-1)
+            q[o:o + b - a] = np.asarray(sysd["charge"])[a:b]
+            ty[o:o + b - a] = np.asarray(sysd["type"])[a:b]
+            mol[o:o + b - a] = np.asarray(sysd["molid"])[a:b]
+        ms = np.array(sysd["molsize"], dtype=np.int64)
+        tm = sysd["templates"][comp]
+        a, b = cs[comp], cs[comp + 1]
+        mp = np.ascontiguousarray((P_[a:a + ms[comp]] if b > a else tm["pos"]).reshape(-1), dtype=np.float64)
+        mq = np.ascontiguousarray(tm["charge"], dtype=np.float64)
+        mt = np.ascontiguousarray(tm["type"], dtype=np.int64)
+        intra, self_ = self.rigid_exclusion(mp, mq, np.ones(len(mq)))
+        _, s_fw, s_ads = self.ewald_total(list(ms))
+        st = OraGcmcStats()
+        lib().ora_gcmc_run(C.byref(self.box), C.byref(self.ff), _d(pos), _d(q), _i(ty), _i(mol), ncomp,
+                           sysd["nhost"], _i(sizes), _i(offs), _i(ms), _d(mp), _d(mq), _i(mt), intra, self_,
+                           _d(s_fw), _d(s_ads), C.byref(params), first_step, nsteps, C.byref(st))
+        after = dict(sysd)
+        newpos, newq, newt, newm = [], [], [], []
+        starts = [0]
+        for c in range(ncomp):
+            o, n = offs[c], sizes[c]
+            newpos.append(pos[3 * o:3 * (o + n)].reshape(-1, 3))
+            newq.append(q[o:o + n])
+            newt.append(ty[o:o + n])
+            newm.append(mol[o:o + n])
+            starts.append(starts[-1] + n)
+        after["pos"] = np.concatenate(newpos)
+        after["charge"] = np.concatenate(newq)
+        after["type"] = np.concatenate(newt)
+        after["molid"] = np.concatenate(newm)
+        after["scale"] = np.ones(starts[-1])
+        after["scale_coul"] = np.ones(starts[-1])
+        after["comp_start"] = starts
+        return st, after, s_ads
 
     def widom(self, params, s_fw, s_ads, first_move, n, nthreads=0):
         res = (OraWidomResult * n)()

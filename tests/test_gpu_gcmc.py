@@ -1,0 +1,145 @@
+"""GPU parity of the device GCMC run (grx_gcmc_run) against the FP64 oracle.
+
+The oracle (ora_gcmc_run) restates RunMoves (axpy.cu:102-298) for translation,
+rotation and CBMC insertion / deletion of one component; both sides draw the same
+Philox counters, so in FP64 the two Markov chains must take identical decisions.
+
+Tolerances:
+  FP64 : identical move counts and molecule numbers; positions within 1e-9 A
+         (they are produced by the same FP64 expressions); accepted-energy sums
+         within 1e-9 relative.
+  MIXED: identical decisions on this seeded chain (the acceptance probabilities
+         agree to 1e-6 relative, see the pair-energy tests); accepted-energy sums
+         within beta*|dE| <= 1e-5 over the run.
+  Drift: the device's recomputed FP64 total after a run equals the initial total
+         plus the accepted move energies (gRASPA's ENERGY DRIFT check,
+         fxn_main.h:454-542) to 1e-8 relative.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.systems import co2_system
+
+pytestmark = pytest.mark.gpu
+
+CAP = 3 * 64
+
+
+def params(grx, **kw):
+    return grx.gcmc_desc(1, **kw)
+
+
+def ora_params(d):
+    g = O.OraGcmc()
+    g.component, g.ntrials, g.norient = d.component, d.ntrials, d.norient
+    g.p_translation, g.p_rotation, g.p_swap = d.p_translation, d.p_rotation, d.p_swap
+    for k in range(3):
+        g.max_translation[k] = d.max_translation[k]
+        g.max_rotation[k] = d.max_rotation[k]
+    g.beta, g.pressure = d.beta, d.pressure
+    g.fugacity_coeff, g.mol_fraction, g.ideal_rosenbluth = d.fugacity_coeff, d.mol_fraction, d.ideal_rosenbluth
+    g.seed, g.stream = d.seed, d.stream
+    return g
+
+
+def total(box):
+    t = box.total_energy()
+    return sum(t[k] for k in ("hh_vdw", "hh_real", "hg_vdw", "hg_real", "gg_vdw", "gg_real", "hh_ewald",
+                              "hg_ewald", "gg_ewald"))
+
+
+def make_box(grx, s):
+    box = grx.Box(s, capacity=[s["comp_start"][1], CAP])
+    box.ewald_total()
+    return box
+
+
+def run_pair(grx, s, d, nsteps, prec, first=0):
+    box = make_box(grx, s)
+    st = grx.gcmc_run([box], [d], first, nsteps, prec)[0]
+    ost, after, _ = O.OracleSystem(s).gcmc(ora_params(d), [s["comp_start"][1], CAP], first, nsteps)
+    return box, st, ost, after
+
+
+@pytest.mark.parametrize("n_co2", [0, 5])
+def test_gcmc_fp64_matches_oracle(grx_lib, n_co2):
+    s = co2_system(n_co2=n_co2)
+    d = params(grx_lib, pressure_pa=1e6)
+    box, st, ost, after = run_pair(grx_lib, s, d, 400, grx_lib.GRX_FP64)
+    assert list(st.attempts) == list(ost.attempts)
+    assert list(st.accepted) == list(ost.accepted)
+    assert st.n_molecules == ost.n_molecules and st.capacity_hits == 0
+    assert st.sum_n == ost.sum_n
+    assert sum(st.accepted) > 40
+    nfw = s["comp_start"][1]
+    got = box.positions(1)
+    ref = after["pos"][nfw:]
+    assert got.shape == ref.shape
+    assert np.max(np.abs(got - ref)) <= 1e-9
+    for k in range(4):
+        assert abs(st.energy[k] - ost.energy[k]) <= 1e-9 * max(1.0, abs(ost.energy[k]))
+
+
+def test_gcmc_mixed_matches_oracle(grx_lib):
+    s = co2_system(n_co2=5)
+    d = params(grx_lib, pressure_pa=1e6)
+    box, st, ost, after = run_pair(grx_lib, s, d, 400, grx_lib.GRX_MIXED)
+    assert list(st.accepted) == list(ost.accepted) and st.n_molecules == ost.n_molecules
+    nfw = s["comp_start"][1]
+    assert np.max(np.abs(box.positions(1) - after["pos"][nfw:])) <= 1e-9
+    for k in range(4):
+        assert d.beta * abs(st.energy[k] - ost.energy[k]) <= 1e-5
+
+
+@pytest.mark.parametrize("prec", ["GRX_FP64", "GRX_MIXED"])
+def test_gcmc_energy_drift(grx_lib, prec):
+    s = co2_system(n_co2=5)
+    box = make_box(grx_lib, s)
+    e0 = total(box)
+    box.ewald_total()
+    st = grx_lib.gcmc_run([box], [params(grx_lib, pressure_pa=1e6)], 0, 500, getattr(grx_lib, prec))[0]
+    e1 = total(box)
+    assert sum(st.accepted) > 50
+    assert abs((e1 - e0) - st.energy[3]) <= 1e-8 * max(abs(e1), abs(e0))
+
+
+def test_gcmc_multibox_independent_and_resumable(grx_lib):
+    s = co2_system(n_co2=3)
+    descs = [params(grx_lib, stream=k, pressure_pa=1e6) for k in range(4)]
+    boxes = [make_box(grx_lib, s) for _ in range(4)]
+    multi = grx_lib.gcmc_run(boxes, descs, 0, 200, grx_lib.GRX_FP64)
+    for k in (0, 3):  # each box of the batched launch equals its own single-box run
+        b = make_box(grx_lib, s)
+        one = grx_lib.gcmc_run([b], [descs[k]], 0, 200, grx_lib.GRX_FP64)[0]
+        assert list(one.accepted) == list(multi[k].accepted) and one.n_molecules == multi[k].n_molecules
+        assert np.array_equal(b.positions(1), boxes[k].positions(1))
+    assert len({tuple(m.accepted) for m in multi}) > 1  # different streams, different chains
+    # steps 0..99 then 100..199 equal one run of 200 steps
+    b = make_box(grx_lib, s)
+    grx_lib.gcmc_run([b], [descs[1]], 0, 100, grx_lib.GRX_FP64)
+    grx_lib.gcmc_run([b], [descs[1]], 100, 100, grx_lib.GRX_FP64)
+    assert np.array_equal(b.positions(1), boxes[1].positions(1))
+
+
+def test_gcmc_capacity_and_edges(grx_lib):
+    s = co2_system(n_co2=0)
+    box = grx_lib.Box(s, capacity=[s["comp_start"][1], 3 * 2])  # room for two molecules
+    box.ewald_total()
+    d = params(grx_lib, p_translation=0.0, p_rotation=0.0, pressure_pa=1e9)
+    st = grx_lib.gcmc_run([box], [d], 0, 300, grx_lib.GRX_FP64)[0]
+    assert st.n_molecules <= 2 and st.capacity_hits > 0
+    assert box.component_size(1) == 3 * st.n_molecules
+    # zero steps: nothing moves, counts are zero
+    st0 = grx_lib.gcmc_run([box], [d], 300, 0, grx_lib.GRX_FP64)[0]
+    assert sum(st0.attempts) == 0 and st0.n_molecules == st.n_molecules
+    # argument errors
+    bad = params(grx_lib)
+    bad.component = 0
+    with pytest.raises(grx_lib.GrxError):
+        grx_lib.gcmc_run([box], [bad], 0, 1, grx_lib.GRX_FP64)
+    bad = params(grx_lib, ntrials=65)
+    with pytest.raises(grx_lib.GrxError):
+        grx_lib.gcmc_run([box], [bad], 0, 1, grx_lib.GRX_FP64)
+    with pytest.raises(grx_lib.GrxError):
+        grx_lib.gcmc_run([box, box], [d, d], 0, 1, grx_lib.GRX_FP64)
