@@ -17,6 +17,9 @@ LIB = os.path.join(OUT, "libgrx.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["grx_box.cu", "grx_pair.cu", "grx_ewald.cu", "grx_widom.cu", "grx_noalloc.cu", "grx_gcmc.cu"]
 HEADERS = ["grx_internal.cuh", "grx_host.h", "grx_warp.cuh", "grx_df.cuh", "grx_cbmc.cuh"]
+HOST = os.path.join(HERE, "host")
+HOST_SOURCES = ["graspa_host.cpp", "gcmc_driver.cpp"]
+DRIVER = os.path.join(OUT, "gcmc_driver")
 
 
 def nvcc():
@@ -73,7 +76,25 @@ def build(force=False, verbose=False):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    build_host()
     return LIB
+
+
+def build_host():
+    """The C++ host layer (graspa_gb300/host) and its example driver, linked
+    against libgrx.so with g++ (no CUDA headers needed on this side)."""
+    inc = os.path.join(HERE, "..", "include")
+    srcs = [os.path.join(HOST, s) for s in HOST_SOURCES]
+    deps = srcs + [LIB, os.path.join(HOST, "graspa_host.hpp"), os.path.join(inc, "grx.h"),
+                   os.path.join(inc, "grx_philox.h")]
+    if not _stale(DRIVER, deps):
+        return DRIVER
+    cmd = ["g++", "-O2", "-std=c++17", "-Wall", "-I", inc, "-I", HOST] + srcs + \
+        ["-L", OUT, "-lgrx", "-Wl,-rpath,$ORIGIN", "-o", DRIVER]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"host layer build failed:\n{r.stdout}\n{r.stderr}")
+    return DRIVER
 
 
 if __name__ == "__main__":

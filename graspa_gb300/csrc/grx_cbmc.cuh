@@ -39,6 +39,7 @@ struct CbmcWork {
   int sel;      // chosen (or retraced) trial index
   int nok;      // trials without overlap
   double w;     // averaged weight of the step
+  double wraw;  // unaveraged weight sum of the step (reinsertion StoredR)
 };
 
 // ---------------------------------------------------------------- trials
@@ -90,7 +91,8 @@ __device__ __forceinline__ void rotate_quaternion(double& x, double& y, double& 
 __device__ __forceinline__ void gen_orientations(const BoxDev& b, CbmcWork& W, uint64_t seed, uint32_t stream,
                                                  uint64_t move, int no, int chain, int off, double scale_coul,
                                                  double scale, double fx, double fy, double fz, bool retrace,
-                                                 const double* ox, const double* oy, const double* oz) {
+                                                 const double* ox, const double* oy, const double* oz,
+                                                 uint32_t slot_base = SLOT_ORIENT) {
   const int tid = threadIdx.x;
   if (tid < no * chain) {
     const int o = tid / chain, at = tid % chain;
@@ -100,7 +102,7 @@ __device__ __forceinline__ void gen_orientations(const BoxDev& b, CbmcWork& W, u
       make_bead(W.beads[tid], ox[at], oy[at], oz[at], q, scale, type, b.prefactor);
     } else {
       uint32_t r[4];
-      draw4(seed, stream, move, SLOT_ORIENT + o, r);
+      draw4(seed, stream, move, slot_base + o, r);
       const double4 t0 = b.pos64[off];
       const double4 pa = b.pos64[off + 1 + at];
       double vx = pa.x - t0.x, vy = pa.y - t0.y, vz = pa.z - t0.z;
@@ -124,13 +126,14 @@ __device__ __forceinline__ void trial_pass(const BoxDev& b, CbmcWork& W, int nb,
   __syncthreads();
 }
 
-// CBMC weight of one growth step (warp 0 computes, results in W.ok/sel/w/nok).
+// CBMC weight of one growth step (warp 0 computes, results in W.ok/sel/w/nok/wraw).
 // Insertion: log-sum-exp selection with the uniform u (SelectTrialPosition) and the
 // 1e-150 failure test. Retrace (deletion): the first trial without overlap is the
-// existing configuration and no selection is drawn. Exponentials are evaluated one
+// existing configuration and no selection is drawn. `stored` is added to the sum
+// before averaging (the reinsertion retrace's StoredR, mc_widom.h:363-366). Exponentials are evaluated one
 // trial per lane; sums and the cumulative search stay sequential in trial order.
 __device__ __forceinline__ void step_weight(CbmcWork& W, int nt, double beta, int bias, double u, double navg,
-                                            bool retrace) {
+                                            bool retrace, double stored = 0.0) {
   if (threadIdx.x < 32) {
     const int lane = threadIdx.x;
     double lw[2];
@@ -187,8 +190,9 @@ __device__ __forceinline__ void step_weight(CbmcWork& W, int nt, double beta, in
         double w = 0.0;
         for (int t = 0; t < nt; ++t)
           if (!W.tflag[t]) w += W.sel_wa[t];
+        W.wraw = w;
         if (retrace || !(w < 1e-150)) {
-          double avg = w / navg;
+          double avg = (w + stored) / navg;
           if (!bias) avg *= exp(-beta * (W.te[4 * s + 1] + W.te[4 * s + 3]));
           W.ok = 1;
           W.sel = s;

@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(GRX_THREADS, 2) gcmc_kernel(const BoxDev* boxe
   __shared__ CbmcWork W;
   __shared__ grx_gcmc_stats st;
   __shared__ int s_accept;
-  __shared__ double s_e1[4], s_w1, s_dE[3];
+  __shared__ double s_e1[4], s_w1, s_dE[3], s_stored, s_r1[4], s_wr;
   extern __shared__ double2 eik[];
   const int tid = threadIdx.x;
   if (tid == 0) {
@@ -110,6 +110,7 @@ __global__ void __launch_bounds__(GRX_THREADS, 2) gcmc_kernel(const BoxDev* boxe
     int kind = -1;
     if (r < d.p_translation) kind = 0;
     else if (r < d.p_rotation) kind = 1;
+    else if (r < d.p_reinsertion) kind = 4;
     else if (r < d.p_swap) kind = (u01(w[2]) < 0.5) ? 2 : 3;
     const double uacc = u01(w[3]);
     if (tid == 0) s_accept = 0;
@@ -160,6 +161,103 @@ __global__ void __launch_bounds__(GRX_THREADS, 2) gcmc_kernel(const BoxDev* boxe
         if (a.charged) commit_sk(b, b.s_tmp);
         if (tid == 0) {
           st.accepted[kind]++;
+          st.energy[0] += s_dE[0]; st.energy[1] += s_dE[1]; st.energy[2] += s_dE[2];
+          st.energy[3] += s_dE[0] + s_dE[1] + s_dE[2];
+        }
+      }
+    } else if (kind == 4 && N > 0) {
+      // ---------------------------------------------- reinsertion (move_struct.h:170-406)
+      const int m0 = off + mol * ms;
+      if (tid == 0) st.attempts[4]++;
+      if (tid < ms) {  // [0, ms): the molecule now (charge negated); [ms, 2ms): its regrowth
+        const double4 p = b.pos64[m0 + tid];
+        W.mx[tid] = p.x; W.my[tid] = p.y; W.mz[tid] = p.z; W.mq[tid] = -p.w;
+        W.mq[ms + tid] = p.w;
+      }
+      __syncthreads();
+      // insertion half: every trial new, the molecule itself excluded
+      gen_first_trials(b, W, d.seed, d.stream, move, d.ntrials, b.charge[off], 1.0, b.meta[off].x, false, 0.0, 0.0,
+                       0.0);
+      trial_pass<PREC>(b, W, d.ntrials, 1, comp, mol);
+      step_weight(W, d.ntrials, d.beta, a.bias, u01(ws[0]), (double)d.ntrials, false);
+      bool ok = W.ok && W.w > 1e-150;
+      double fx = 0, fy = 0, fz = 0;
+      if (ok) {
+        const Bead& fb = W.beads[W.sel];
+        fx = fb.x; fy = fb.y; fz = fb.z;
+        if (tid == 0) {
+          for (int k = 0; k < 4; ++k) s_e1[k] = W.te[4 * W.sel + k];
+          s_w1 = W.w;
+          s_stored = W.wraw - W.sel_wa[W.sel];  // StoredR (mc_widom.h:363)
+          W.mx[ms] = fx; W.my[ms] = fy; W.mz[ms] = fz;
+        }
+      }
+      __syncthreads();
+      double rosen = ok ? s_w1 : 0.0;
+      double e2[4] = {0, 0, 0, 0};
+      if (ok && chain > 0) {
+        gen_orientations(b, W, d.seed, d.stream, move, d.norient, chain, off, 1.0, 1.0, fx, fy, fz, false, nullptr,
+                         nullptr, nullptr);
+        trial_pass<PREC>(b, W, d.norient * chain, chain, comp, mol);
+        step_weight(W, d.norient, d.beta, a.bias, u01(ws[1]), (double)d.norient, false);
+        ok = W.ok;
+        if (ok) {
+          rosen *= W.w;
+          for (int k = 0; k < 4; ++k) e2[k] = W.te[4 * W.sel + k];
+          if (rosen <= 1e-150) ok = false;
+          if (tid < chain) {
+            const Bead& bd = W.beads[W.sel * chain + tid];
+            W.mx[ms + 1 + tid] = bd.x; W.my[ms + 1 + tid] = bd.y; W.mz[ms + 1 + tid] = bd.z;
+          }
+        }
+        __syncthreads();
+      }
+      if (ok) {
+        // retrace half: the first bead's single trial is the molecule's own, plus StoredR
+        gen_first_trials(b, W, d.seed, d.stream, move, 1, b.charge[off], 1.0, b.meta[off].x, true, W.mx[0], W.my[0],
+                         W.mz[0]);
+        trial_pass<PREC>(b, W, 1, 1, comp, mol);
+        step_weight(W, 1, d.beta, a.bias, 0.0, (double)d.ntrials, true, s_stored);
+        bool ok2 = W.ok;
+        if (ok2 && tid == 0) {
+          for (int k = 0; k < 4; ++k) s_r1[k] = W.te[k];
+          s_wr = W.w;
+        }
+        __syncthreads();
+        double rosen_old = ok2 ? s_wr : 0.0;
+        double r2[4] = {0, 0, 0, 0};
+        if (ok2 && chain > 0) {
+          gen_orientations(b, W, d.seed, d.stream, move, d.norient, chain, off, 1.0, 1.0, W.mx[0], W.my[0], W.mz[0],
+                           true, W.mx + 1, W.my + 1, W.mz + 1, SLOT_RETRACE);
+          trial_pass<PREC>(b, W, d.norient * chain, chain, comp, mol);
+          step_weight(W, d.norient, d.beta, a.bias, 0.0, (double)d.norient, true);
+          ok2 = W.ok;
+          if (ok2) {
+            rosen_old *= W.w;
+            for (int k = 0; k < 4; ++k) r2[k] = W.te[4 * W.sel + k];
+          }
+          __syncthreads();
+        }
+        if (ok2) {
+          double same = 0.0, cross = 0.0;
+          if (a.charged) ewald_move<PREC>(b, W, 2 * ms, eik, b.s_tmp, same, cross);
+          if (tid == 0) {
+            const double ew = a.charged ? same + 2.0 * cross : 0.0;
+            rosen *= exp(-d.beta * ew);
+            const double pacc = rosen / rosen_old;
+            s_accept = uacc < pacc;
+            s_dE[0] = s_e1[0] + s_e1[2] + e2[0] + e2[2] - (s_r1[0] + s_r1[2] + r2[0] + r2[2]);
+            s_dE[1] = s_e1[1] + s_e1[3] + e2[1] + e2[3] - (s_r1[1] + s_r1[3] + r2[1] + r2[3]);
+            s_dE[2] = ew;
+          }
+        }
+      }
+      __syncthreads();
+      if (s_accept) {
+        if (tid < ms) store_position(b, m0 + tid, W.mx[ms + tid], W.my[ms + tid], W.mz[ms + tid]);
+        if (a.charged) commit_sk(b, b.s_tmp);
+        if (tid == 0) {
+          st.accepted[4]++;
           st.energy[0] += s_dE[0]; st.energy[1] += s_dE[1]; st.energy[2] += s_dE[2];
           st.energy[3] += s_dE[0] + s_dE[1] + s_dE[2];
         }
@@ -385,5 +483,87 @@ extern "C" grx_status grx_gcmc_run(grx_box* const* boxes, int32_t nboxes, const 
     b->stored[c] = std::max(b->stored[c], (size_t)b->size[c]);
     if (nsteps == 0) stats[i].n_molecules = b->size[descs[i].component] / (int)b->molsize[descs[i].component];
   }
+  return GRX_OK;
+}
+
+// ---------------------------------------------------------------- molecule updates
+namespace grx {
+
+struct MolWrite {
+  double x[kMolWork], y[kMolWork], z[kMolWork], q[kMolWork];
+  int type[kMolWork];
+};
+
+// Update_insertion_data_Parallel / update_translation_position (mc_utilities.h:191-234,
+// 285-292): one thread per atom writes every stored representation.
+__global__ void write_molecule_kernel(BoxDev b, int comp, int first, int ms, int mol, int grow, MolWrite m) {
+  const int a = threadIdx.x;
+  if (a < ms) store_atom(b, first + a, m.x[a], m.y[a], m.z[a], m.q[a], 1.0, 1.0, m.type[a], mol);
+  if (grow && a == 0) const_cast<int*>(b.comp_size)[comp] += ms;
+}
+
+// Update_deletion_data_Parallel (mc_utilities.h:163-189): the last molecule moves
+// into the removed slot, which keeps its molecule index.
+__global__ void remove_molecule_kernel(BoxDev b, int comp, int dst, int src, int ms, int mol) {
+  const int a = threadIdx.x;
+  if (a < ms && dst != src) copy_atom(b, dst + a, src + a, mol);
+  if (a == 0) const_cast<int*>(b.comp_size)[comp] -= ms;
+}
+
+}  // namespace grx
+
+extern "C" grx_status grx_box_write_molecule(grx_box* b, int32_t comp, size_t mol, const double* pos,
+                                             const double* charge, const size_t* type) {
+  GRX_REQUIRE(b && pos && charge && type, "grx_box_write_molecule: null argument");
+  GRX_REQUIRE(comp >= b->nhost && comp < b->ncomp, "grx_box_write_molecule: not an adsorbate component");
+  const size_t ms = b->molsize[comp];
+  GRX_REQUIRE(ms >= 1 && ms <= (size_t)kMolWork, "grx_box_write_molecule: molecule size must be 1..32");
+  GRX_CHECK_CUDA(cudaStreamSynchronize(b->stream), "write_molecule sync");
+  GRX_CHECK_CUDA(cudaMemcpy(b->size, b->d_size, GRX_MAX_COMPONENTS * sizeof(int), cudaMemcpyDeviceToHost),
+                 "read sizes");
+  const size_t n = (size_t)b->size[comp] / ms;
+  GRX_REQUIRE(mol <= n, "grx_box_write_molecule: molecule index beyond the count");
+  if ((mol + 1) * ms > b->cap[comp]) {
+    set_error("grx_box_write_molecule: component %d capacity %zu exhausted", comp, b->cap[comp]);
+    return GRX_ERR_CAPACITY;
+  }
+  MolWrite m{};
+  for (size_t a = 0; a < ms; ++a) {
+    m.x[a] = pos[3 * a];
+    m.y[a] = pos[3 * a + 1];
+    m.z[a] = pos[3 * a + 2];
+    m.q[a] = charge[a];
+    GRX_REQUIRE(type[a] < (size_t)b->dev.ntypes, "grx_box_write_molecule: atom type out of range");
+    m.type[a] = (int)type[a];
+    if (charge[a] != 0.0) b->has_charge[comp] = 1;
+  }
+  refresh_dev(b);
+  const int grow = mol == n ? 1 : 0;
+  write_molecule_kernel<<<1, 32, 0, b->stream>>>(b->dev, comp, (int)(b->off[comp] + mol * ms), (int)ms, (int)mol,
+                                                 grow, m);
+  count_launch();
+  GRX_CHECK_CUDA(cudaGetLastError(), "write_molecule launch");
+  if (grow) b->size[comp] += (int)ms;
+  b->stored[comp] = std::max(b->stored[comp], (mol + 1) * ms);
+  GRX_CHECK_CUDA(cudaStreamSynchronize(b->stream), "write_molecule");
+  return GRX_OK;
+}
+
+extern "C" grx_status grx_box_remove_molecule(grx_box* b, int32_t comp, size_t mol) {
+  GRX_REQUIRE(b, "grx_box_remove_molecule: null box");
+  GRX_REQUIRE(comp >= b->nhost && comp < b->ncomp, "grx_box_remove_molecule: not an adsorbate component");
+  const size_t ms = b->molsize[comp];
+  GRX_CHECK_CUDA(cudaStreamSynchronize(b->stream), "remove_molecule sync");
+  GRX_CHECK_CUDA(cudaMemcpy(b->size, b->d_size, GRX_MAX_COMPONENTS * sizeof(int), cudaMemcpyDeviceToHost),
+                 "read sizes");
+  const size_t n = (size_t)b->size[comp] / ms;
+  GRX_REQUIRE(mol < n, "grx_box_remove_molecule: molecule index beyond the count");
+  refresh_dev(b);
+  remove_molecule_kernel<<<1, 32, 0, b->stream>>>(b->dev, comp, (int)(b->off[comp] + mol * ms),
+                                                  (int)(b->off[comp] + (n - 1) * ms), (int)ms, (int)mol);
+  count_launch();
+  GRX_CHECK_CUDA(cudaGetLastError(), "remove_molecule launch");
+  b->size[comp] -= (int)ms;
+  GRX_CHECK_CUDA(cudaStreamSynchronize(b->stream), "remove_molecule");
   return GRX_OK;
 }

@@ -134,7 +134,7 @@ __host__ __device__ inline void draw4(uint64_t seed, uint32_t stream, uint64_t m
 
 __host__ __device__ inline double u01(uint32_t w) { return (double)w * 2.3283064365386963e-10; }
 
-enum : uint32_t { SLOT_FIRST = 0u, SLOT_ORIENT = 1024u, SLOT_SELECT = 2048u };
+enum : uint32_t { SLOT_FIRST = 0u, SLOT_ORIENT = 1024u, SLOT_SELECT = 2048u, SLOT_RETRACE = 3072u };
 
 // ---------------------------------------------------------------- geometry
 // Minimum image of the reference, PBC() maths.cuh:427-450 (int-cast rounding).

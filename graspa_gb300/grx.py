@@ -92,14 +92,14 @@ assert WIDOM_RESULT_DTYPE.itemsize == C.sizeof(WidomResult)
 class GcmcDesc(C.Structure):
     _fields_ = [("component", C.c_int32), ("ntrials", C.c_int32), ("norient", C.c_int32),
                 ("pad_", C.c_int32), ("p_translation", C.c_double), ("p_rotation", C.c_double),
-                ("p_swap", C.c_double), ("max_translation", C.c_double * 3), ("max_rotation", C.c_double * 3),
+                ("p_reinsertion", C.c_double), ("p_swap", C.c_double), ("max_translation", C.c_double * 3), ("max_rotation", C.c_double * 3),
                 ("beta", C.c_double), ("pressure", C.c_double), ("fugacity_coeff", C.c_double),
                 ("mol_fraction", C.c_double), ("ideal_rosenbluth", C.c_double), ("tail_insert", C.c_double),
                 ("seed", C.c_uint64), ("stream", C.c_uint32), ("pad2_", C.c_uint32)]
 
 
 class GcmcStats(C.Structure):
-    _fields_ = [("attempts", C.c_int64 * 4), ("accepted", C.c_int64 * 4), ("n_molecules", C.c_int64),
+    _fields_ = [("attempts", C.c_int64 * 5), ("accepted", C.c_int64 * 5), ("n_molecules", C.c_int64),
                 ("capacity_hits", C.c_int64), ("energy", C.c_double * 4), ("sum_n", C.c_double)]
 
 # every symbol include/grx.h declares
@@ -110,6 +110,7 @@ EXPORTS = [
     "grx_ewald_total", "grx_ewald_set_structure_factors", "grx_ewald_get_structure_factors",
     "grx_ewald_delta", "grx_ewald_commit", "grx_total_energy", "grx_cbmc_select",
     "grx_widom_insertions", "grx_widom_insertions_async", "grx_launch_count", "grx_trial_energies_noalloc", "grx_gcmc_run",
+    "grx_box_write_molecule", "grx_box_remove_molecule",
 ]
 
 _lib = None
@@ -160,6 +161,8 @@ def load(path=LIB_PATH):
     L.grx_launch_count.restype = C.c_uint64
     L.grx_trial_energies_noalloc.argtypes = [C.c_void_p, P(Trials), C.c_int32, C.c_int64, C.c_int64, C.c_int32,
                                              P(TrialEnergy), _u8p]
+    L.grx_box_write_molecule.argtypes = [C.c_void_p, C.c_int32, C.c_size_t, _dp, _dp, P(C.c_size_t)]
+    L.grx_box_remove_molecule.argtypes = [C.c_void_p, C.c_int32, C.c_size_t]
     L.grx_gcmc_run.argtypes = [P(C.c_void_p), C.c_int32, P(GcmcDesc), C.c_uint64, C.c_int64, C.c_int32,
                                P(GcmcStats)]
     _lib = L
@@ -318,6 +321,17 @@ class Box:
         check(self.L.grx_box_get_positions(self.h, c, _d(out), n), "grx_box_get_positions")
         return out.reshape(-1, 3)
 
+    def write_molecule(self, c, mol, pos, charge, types):
+        """Write adsorbate molecule `mol` of component c (mol == count appends)."""
+        p = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1)
+        q = np.ascontiguousarray(charge, dtype=np.float64)
+        t = np.ascontiguousarray(types, dtype=np.uint64)
+        check(self.L.grx_box_write_molecule(self.h, c, mol, _d(p), _d(q), _sz(t)), "grx_box_write_molecule")
+
+    def remove_molecule(self, c, mol):
+        """Remove adsorbate molecule `mol`; the last molecule takes its slot."""
+        check(self.L.grx_box_remove_molecule(self.h, c, mol), "grx_box_remove_molecule")
+
     # --- Ewald ---------------------------------------------------------
     def ewald_sizes(self):
         nv, na = C.c_int64(), C.c_int64()
@@ -455,7 +469,7 @@ def widom_desc(system, component, ntrials=10, norient=10, temperature=None, seed
     return d
 
 
-def gcmc_desc(component, ntrials=10, norient=10, p_translation=0.25, p_rotation=0.5, p_swap=1.0,
+def gcmc_desc(component, ntrials=10, norient=10, p_translation=0.25, p_rotation=0.5, p_reinsertion=None, p_swap=1.0,
               max_translation=1.0, max_rotation=0.5, temperature=300.0, pressure_pa=1e5, fugacity_coeff=1.0,
               mol_fraction=1.0, ideal_rosenbluth=1.0, tail_insert=0.0, seed=42, stream=0):
     """GCMC move mix of one box; probabilities are cumulative as in Move_Statistics,
@@ -463,6 +477,7 @@ def gcmc_desc(component, ntrials=10, norient=10, p_translation=0.25, p_rotation=
     d = GcmcDesc()
     d.component, d.ntrials, d.norient = component, ntrials, norient
     d.p_translation, d.p_rotation, d.p_swap = p_translation, p_rotation, p_swap
+    d.p_reinsertion = p_rotation if p_reinsertion is None else p_reinsertion
     for k in range(3):
         d.max_translation[k] = max_translation
         d.max_rotation[k] = max_rotation

@@ -1,0 +1,969 @@
+// graspa_host.cpp -- the reference-shaped move drivers over the libgrx C ABI.
+// Each function cites the gRASPA code it restates; the energy work of every call
+// runs in libgrx on the GPU.
+#include "graspa_host.hpp"
+
+#include <algorithm>
+#include <cstdio>
+#include <numeric>
+
+namespace graspa {
+
+// ------------------------------------------------------------------ small types
+void MoveEnergy::take_negative() {
+  HHVDW = -HHVDW; HGVDW = -HGVDW; GGVDW = -GGVDW;
+  HHReal = -HHReal; HGReal = -HGReal; GGReal = -GGReal;
+  HHEwaldE = -HHEwaldE; HGEwaldE = -HGEwaldE; GGEwaldE = -GGEwaldE;
+  TailE = -TailE;
+}
+MoveEnergy& MoveEnergy::operator+=(const MoveEnergy& o) {
+  HHVDW += o.HHVDW; HGVDW += o.HGVDW; GGVDW += o.GGVDW;
+  HHReal += o.HHReal; HGReal += o.HGReal; GGReal += o.GGReal;
+  HHEwaldE += o.HHEwaldE; HGEwaldE += o.HGEwaldE; GGEwaldE += o.GGEwaldE;
+  TailE += o.TailE;
+  return *this;
+}
+MoveEnergy& MoveEnergy::operator-=(const MoveEnergy& o) {
+  MoveEnergy n = o;
+  n.take_negative();
+  return *this += n;
+}
+MoveEnergy operator+(MoveEnergy a, const MoveEnergy& b) { return a += b; }
+
+void HostAtoms::allocate(size_t n) {
+  pos.assign(n, double3{});
+  scale.assign(n, 1.0);
+  charge.assign(n, 0.0);
+  scaleCoul.assign(n, 1.0);
+  Type.assign(n, 0);
+  MolID.assign(n, 0);
+}
+
+Atoms HostAtoms::view(size_t molsize, size_t size) {
+  Atoms a;
+  a.pos = pos.data();
+  a.scale = scale.data();
+  a.charge = charge.data();
+  a.scaleCoul = scaleCoul.data();
+  a.Type = Type.data();
+  a.MolID = MolID.data();
+  a.Molsize = molsize;
+  a.size = size;
+  a.Allocate_size = pos.size();
+  return a;
+}
+
+void Move_Statistics::Record_Move_Total(int move) {
+  switch (move) {
+    case TRANSLATION: ++TranslationTotal; break;
+    case ROTATION: ++RotationTotal; break;
+    case INSERTION: ++InsertionTotal; break;
+    case DELETION: ++DeletionTotal; break;
+    case REINSERTION: ++ReinsertionTotal; break;
+    default: break;
+  }
+}
+void Move_Statistics::Record_Move_Accept(int move) {
+  switch (move) {
+    case TRANSLATION: ++TranslationAccepted; break;
+    case ROTATION: ++RotationAccepted; break;
+    case INSERTION: ++InsertionAccepted; break;
+    case DELETION: ++DeletionAccepted; break;
+    case REINSERTION: ++ReinsertionAccepted; break;
+    default: break;
+  }
+}
+void Move_Statistics::NormalizeProbabilities() {
+  const double tot = TranslationProb + RotationProb + ReinsertionProb + SwapProb;
+  if (tot > 1e-10) {
+    TranslationProb /= tot; RotationProb /= tot; ReinsertionProb /= tot; SwapProb /= tot;
+  }
+  RotationProb += TranslationProb;
+  ReinsertionProb += RotationProb;
+  SwapProb += ReinsertionProb;
+}
+
+void check(grx_status st, const char* what) {
+  if (st != GRX_OK) {
+    throw std::runtime_error(std::string(what) + ": " + grx_status_string(st) + " (" + grx_last_error() + ")");
+  }
+}
+
+static void trial_buffers(Simulations& Sims) {
+  Sims.OldStore.allocate(1024);
+  Sims.NewStore.allocate(1024);
+  Sims.Old = Sims.OldStore.view(0, 0);
+  Sims.New = Sims.NewStore.view(0, 0);
+}
+
+// ------------------------------------------------------------------ set-up
+void Setup_Box(Variables& Vars, size_t systemId, const std::vector<size_t>& n_stored) {
+  Simulations& Sims = Vars.Sims[systemId];
+  Components& SC = Vars.SystemComponents[systemId];
+  ForceField& FF = Vars.device_FF;
+  Boxsize& B = Sims.Box;
+  grx_box_desc d{};
+  for (int k = 0; k < 9; ++k) {
+    d.geometry.cell[k] = B.Cell[k];
+    d.geometry.inverse_cell[k] = B.InverseCell[k];
+  }
+  d.geometry.volume = B.Volume;
+  d.geometry.cubic = B.Cubic;
+  d.geometry.use_lammps_ewald = B.UseLAMMPSEwald;
+  d.geometry.kmax[0] = B.kmax.x;
+  d.geometry.kmax[1] = B.kmax.y;
+  d.geometry.kmax[2] = B.kmax.z;
+  d.geometry.alpha = B.Alpha;
+  d.geometry.prefactor = B.Prefactor;
+  d.geometry.reciprocal_cutoff = B.ReciprocalCutOff;
+  d.forcefield.ntypes = (int32_t)FF.size;
+  d.forcefield.use_1264 = FF.Use1264;
+  d.forcefield.epsilon = FF.epsilon.data();
+  d.forcefield.sigma = FF.sigma.data();
+  d.forcefield.z = FF.z.empty() ? nullptr : FF.z.data();
+  d.forcefield.shift = FF.shift.data();
+  d.forcefield.c10 = FF.C10.empty() ? nullptr : FF.C10.data();
+  d.forcefield.no_charges = FF.noCharges;
+  d.forcefield.vdw_real_bias = FF.VDWRealBias;
+  d.forcefield.overlap_criteria = FF.OverlapCriteria;
+  d.forcefield.cutoff_vdw_sq = FF.CutOffVDW;
+  d.forcefield.cutoff_coul_sq = FF.CutOffCoul;
+  d.ncomponents = SC.NComponents.x;
+  d.nhost_components = SC.NComponents.y;
+  for (int c = 0; c < SC.NComponents.x; ++c) {
+    d.capacity[c] = SC.Allocate_size[c];
+    d.molsize[c] = SC.Moleculesize[c];
+  }
+  check(grx_box_create(&d, &B.handle), "grx_box_create");
+  SC.ExclusionIntra.assign(SC.NComponents.x, 0.0);
+  SC.ExclusionAtom.assign(SC.NComponents.x, 0.0);
+  SC.hasPartialCharge.assign(SC.NComponents.x, false);
+  for (int c = 0; c < SC.NComponents.x; ++c) {
+    Atoms& A = Sims.d_a[c];
+    grx_atoms ga{};
+    ga.pos = reinterpret_cast<const double*>(A.pos);
+    ga.scale = A.scale;
+    ga.charge = A.charge;
+    ga.scale_coul = A.scaleCoul;
+    ga.type = A.Type;
+    ga.molid = A.MolID;
+    ga.size = A.size;
+    ga.n_stored = std::max(A.size, n_stored[c]);
+    check(grx_box_set_component(B.handle, c, &ga, c >= SC.NComponents.y && SC.rigid[c]), "grx_box_set_component");
+    check(grx_box_get_exclusion(B.handle, c, &SC.ExclusionIntra[c], &SC.ExclusionAtom[c]), "grx_box_get_exclusion");
+    for (size_t i = 0; i < ga.n_stored; ++i)
+      if (A.charge[i] != 0.0) SC.hasPartialCharge[c] = true;
+    if (c >= SC.NComponents.y) SC.NumberOfMolecule_for_Component[c] = A.size / SC.Moleculesize[c];
+  }
+  double out8[8];
+  check(grx_ewald_total(B.handle, out8), "grx_ewald_total");
+  SC.Beta = SC.Beta > 0 ? SC.Beta : 1.0 / (1.380649e-23 / (1.6605402e-27 * 1e-20 / 1e-24) * SC.Temperature);
+  trial_buffers(Sims);
+}
+
+void Destroy_Box(Variables& Vars, size_t systemId) {
+  Boxsize& B = Vars.Sims[systemId].Box;
+  if (B.handle) grx_box_destroy(B.handle);
+  B.handle = nullptr;
+}
+
+// ------------------------------------------------------------------ energy calls
+void CBMC_PairwiseInteractions(Variables& Vars, size_t systemId, Components& SC, Simulations& Sims, size_t NTrials,
+                               size_t chainsize) {
+  (void)systemId;
+  const size_t nb = NTrials * chainsize;
+  std::vector<grx_trial_energy> e(NTrials);
+  std::vector<uint8_t> flag(NTrials);
+  grx_trials t{};
+  t.pos = reinterpret_cast<const double*>(Sims.New.pos);
+  t.scale = Sims.New.scale;
+  t.charge = Sims.New.charge;
+  t.scale_coul = Sims.New.scaleCoul;
+  t.type = Sims.New.Type;
+  t.molid = Sims.New.MolID[0];
+  t.ntrials = NTrials;
+  t.chainsize = chainsize;
+  (void)nb;
+  check(grx_trial_energies(Sims.Box.handle, &t, (int32_t)SC.TempVal.component, Sims.ExcludeComponent,
+                           Sims.ExcludeMolecule, Vars.Precision, e.data(), flag.data()),
+        "grx_trial_energies");
+  // Host_sum_Widom_HGGG_SEPARATE: keep the trials without overlap
+  SC.Rosen.clear();
+  SC.TrialEnergies.clear();
+  SC.Trialindex.clear();
+  for (size_t i = 0; i < NTrials; ++i) {
+    if (flag[i]) continue;
+    MoveEnergy m;
+    m.HGVDW = e[i].hg_vdw;
+    m.HGReal = e[i].hg_real;
+    m.GGVDW = e[i].gg_vdw;
+    m.GGReal = e[i].gg_real;
+    double tot = m.HGVDW + m.GGVDW;
+    if (Vars.device_FF.VDWRealBias) tot += m.HGReal + m.GGReal;
+    SC.Rosen.push_back(-SC.Beta * tot);
+    SC.TrialEnergies.push_back(m);
+    SC.Trialindex.push_back(i);
+  }
+}
+
+size_t SelectTrialPosition(std::vector<double>& LogBoltzmannFactors, const Variables& Vars, size_t systemId,
+                           int word) {
+  int32_t sel = 0;
+  double sum = 0.0;
+  check(grx_cbmc_select(LogBoltzmannFactors.data(), (int32_t)LogBoltzmannFactors.size(), Vars.Random.Seed,
+                        Vars.Random.Stream, Vars.SystemComponents[systemId].Step, word, &sel, &sum),
+        "grx_cbmc_select");
+  return (size_t)sel;
+}
+
+// The moved molecule's atoms for the Ewald delta, per move type.
+static void molecule_atoms(Simulations& Sims, Components& SC, size_t comp, size_t first_atom,
+                           std::vector<double>& pos, std::vector<double>& qs) {
+  const size_t ms = SC.Moleculesize[comp];
+  const Atoms& A = Sims.d_a[comp];
+  pos.resize(3 * ms);
+  qs.resize(ms);
+  for (size_t a = 0; a < ms; ++a) {
+    pos[3 * a] = A.pos[first_atom + a].x;
+    pos[3 * a + 1] = A.pos[first_atom + a].y;
+    pos[3 * a + 2] = A.pos[first_atom + a].z;
+    qs[a] = A.charge[first_atom + a] * A.scaleCoul[first_atom + a];
+  }
+}
+
+// The grown configuration: first bead in Old.pos[0], chain from New at orientation `orient`.
+static void grown_atoms(Simulations& Sims, Components& SC, size_t comp, size_t orient, std::vector<double>& pos,
+                        std::vector<double>& qs) {
+  const size_t ms = SC.Moleculesize[comp], chain = ms - 1;
+  const Atoms& T = Sims.d_a[comp];  // template charges (slot 0)
+  pos.resize(3 * ms);
+  qs.resize(ms);
+  pos[0] = Sims.Old.pos[0].x; pos[1] = Sims.Old.pos[0].y; pos[2] = Sims.Old.pos[0].z;
+  qs[0] = T.charge[0];
+  for (size_t a = 0; a < chain; ++a) {
+    const double3& p = Sims.New.pos[orient * chain + a];
+    pos[3 * (1 + a)] = p.x; pos[3 * (1 + a) + 1] = p.y; pos[3 * (1 + a) + 2] = p.z;
+    qs[1 + a] = T.charge[1 + a];
+  }
+}
+
+double2 GPU_EwaldDifference_General(Simulations& Sims, ForceField& FF, Components& SC, size_t comp, int MoveType,
+                                    size_t Location, double2 Scale) {
+  (void)FF;
+  std::vector<double> op, oq, np, nq;
+  switch (MoveType) {
+    case TRANSLATION: case ROTATION: {
+      molecule_atoms(Sims, SC, comp, Location, op, oq);
+      const size_t ms = SC.Moleculesize[comp];
+      np.resize(3 * ms);
+      for (size_t a = 0; a < ms; ++a) {
+        np[3 * a] = Sims.New.pos[a].x; np[3 * a + 1] = Sims.New.pos[a].y; np[3 * a + 2] = Sims.New.pos[a].z;
+      }
+      nq = oq;
+      break;
+    }
+    case INSERTION:
+      grown_atoms(Sims, SC, comp, Location, np, nq);
+      break;
+    case DELETION:
+      molecule_atoms(Sims, SC, comp, Location, op, oq);
+      break;
+    case REINSERTION: {
+      molecule_atoms(Sims, SC, comp, Location, op, oq);
+      const size_t ms = SC.Moleculesize[comp];
+      np.resize(3 * ms);
+      for (size_t a = 0; a < ms; ++a) {  // tempMolStorage, staged in Old[1..ms]
+        np[3 * a] = Sims.Old.pos[1 + a].x; np[3 * a + 1] = Sims.Old.pos[1 + a].y;
+        np[3 * a + 2] = Sims.Old.pos[1 + a].z;
+      }
+      nq = oq;
+      break;
+    }
+    default:
+      throw std::runtime_error("GPU_EwaldDifference_General: move type not on this path");
+  }
+  double out2[2];
+  check(grx_ewald_delta(Sims.Box.handle, (int32_t)comp, MoveType, op.data(), oq.data(), oq.size(), np.data(),
+                        nq.data(), nq.size(), Scale.y, out2),
+        "grx_ewald_delta");
+  return double2{out2[0], out2[1]};
+}
+
+void Update_Vector_Ewald(Boxsize& Box, bool UseTempVector, Components& SC, size_t comp) {
+  (void)UseTempVector;
+  (void)SC;
+  check(grx_ewald_commit(Box.handle, (int32_t)comp), "grx_ewald_commit");
+}
+
+MoveEnergy Total_Energy(Simulations& Sims) {
+  grx_energy e{};
+  check(grx_total_energy(Sims.Box.handle, &e), "grx_total_energy");
+  MoveEnergy m;
+  m.HHVDW = e.hh_vdw; m.HHReal = e.hh_real; m.HGVDW = e.hg_vdw; m.HGReal = e.hg_real;
+  m.GGVDW = e.gg_vdw; m.GGReal = e.gg_real;
+  m.HHEwaldE = e.hh_ewald; m.HGEwaldE = e.hg_ewald; m.GGEwaldE = e.gg_ewald;
+  return m;
+}
+
+double GetPrefactor(Components& SC, Simulations& Sims, size_t comp, int MoveType) {
+  const double bigP = SC.MolFraction[comp] * SC.Pressure * SC.FugacityCoeff[comp] * Sims.Box.Volume;
+  const double N = (double)SC.NumberOfMolecule_for_Component[comp];
+  if (MoveType == INSERTION) return SC.Beta * bigP / (N + 1.0);
+  if (MoveType == DELETION) return N / (SC.Beta * bigP);
+  return 0.0;
+}
+
+// ------------------------------------------------------------------ CBMC steps
+// Rotate_Quaternions (mc_utilities.h:423-457).
+static void rotate_quaternion(double3& v, double u, double w1, double w2) {
+  const double pi = 3.14159265358979323846;
+  const double s1 = std::sin(2 * pi * w1), c1 = std::cos(2 * pi * w1);
+  const double s2 = std::sin(2 * pi * w2), c2 = std::cos(2 * pi * w2);
+  const double q0 = std::sqrt(1 - u) * s1, q1 = std::sqrt(1 - u) * c1;
+  const double q2 = std::sqrt(u) * s2, q3 = std::sqrt(u) * c2;
+  const double a01 = q0 * q1, a02 = q0 * q2, a03 = q0 * q3;
+  const double a11 = q1 * q1, a12 = q1 * q2, a13 = q1 * q3;
+  const double a22 = q2 * q2, a23 = q2 * q3, a33 = q3 * q3;
+  const double r0 = 1.0 - 2.0 * (a22 + a33), r1 = 2.0 * (a12 - a03), r2 = 2.0 * (a13 + a02);
+  const double r3 = 2.0 * (a12 + a03), r4 = 1.0 - 2.0 * (a11 + a33), r5 = 2.0 * (a23 - a01);
+  const double r6 = 2.0 * (a13 - a02), r7 = 2.0 * (a23 + a01), r8 = 1.0 - 2.0 * (a11 + a22);
+  const double x = v.x * r0 + v.y * r1 + v.z * r2;
+  const double y = v.x * r3 + v.y * r4 + v.z * r5;
+  const double z = v.x * r6 + v.y * r7 + v.z * r8;
+  v = double3{x, y, z};
+}
+
+void CBMC_FirstBead_Finish(Variables& Vars, size_t systemId, CBMC_Variables& CBMC) {
+  Components& SC = Vars.SystemComponents[systemId];
+  std::vector<double>& Rosen = SC.Rosen;
+  bool good = false;
+  size_t sel = 0;
+  double W = 0.0;
+  switch (CBMC.MoveType) {
+    case CBMC_INSERTION: case REINSERTION_INSERTION: {
+      if (Rosen.empty()) break;
+      sel = SelectTrialPosition(Rosen, Vars, systemId, 0);
+      for (double& r : Rosen) r = std::exp(r);
+      W = std::accumulate(Rosen.begin(), Rosen.end(), 0.0);
+      if (W < 1e-150) break;
+      good = true;
+      break;
+    }
+    default: {  // CBMC_DELETION, REINSERTION_RETRACE: the existing bead, no selection
+      if (Rosen.empty()) break;
+      for (double& r : Rosen) r = std::exp(r);
+      W = std::accumulate(Rosen.begin(), Rosen.end(), 0.0);
+      good = true;
+      break;
+    }
+  }
+  if (!good) return;
+  if (CBMC.MoveType == REINSERTION_INSERTION) CBMC.StoredR = W - Rosen[sel];
+  if (CBMC.MoveType == REINSERTION_RETRACE) W += CBMC.StoredR;
+  double avg = W / (double)Vars.Widom[systemId].NumberWidomTrials;
+  if (!Vars.device_FF.VDWRealBias) avg *= std::exp(-SC.Beta * (SC.TrialEnergies[sel].HGReal + SC.TrialEnergies[sel].GGReal));
+  CBMC.selectedTrial = SC.Trialindex[sel];
+  CBMC.SuccessConstruction = true;
+  CBMC.FirstBeadEnergy = SC.TrialEnergies[sel];
+  CBMC.Rosenbluth = avg;
+}
+
+// mc_widom.h:385-507: trial positions (get_random_trial_position, :122-213), energies, finish.
+void Widom_Move_FirstBead_PARTIAL(Variables& Vars, size_t systemId, CBMC_Variables& CBMC) {
+  Components& SC = Vars.SystemComponents[systemId];
+  Simulations& Sims = Vars.Sims[systemId];
+  const size_t comp = SC.TempVal.component;
+  const size_t ms = SC.Moleculesize[comp];
+  const Atoms& A = Sims.d_a[comp];
+  size_t ntrials = Vars.Widom[systemId].NumberWidomTrials;
+  size_t molid = SC.TempVal.molecule;
+  const bool retrace = CBMC.MoveType == CBMC_DELETION || CBMC.MoveType == REINSERTION_RETRACE;
+  if (CBMC.MoveType == CBMC_INSERTION) molid = SC.NumberOfMolecule_for_Component[comp];
+  if (CBMC.MoveType == REINSERTION_RETRACE) ntrials = 1;
+  const size_t start = SC.TempVal.molecule * ms;
+  for (size_t t = 0; t < ntrials; ++t) {
+    if (retrace && t == 0) {
+      Sims.New.pos[0] = A.pos[start];
+    } else {
+      uint32_t r[4];
+      grx_draw(Vars.Random.Seed, Vars.Random.Stream, SC.Step, GRX_SLOT_FIRST + (uint32_t)t, r);
+      Sims.New.pos[t] = double3{Sims.Box.Cell[0] * grx_u01(r[0]), Sims.Box.Cell[4] * grx_u01(r[1]),
+                                Sims.Box.Cell[8] * grx_u01(r[2])};
+    }
+    Sims.New.scale[t] = SC.TempVal.Scale.x;
+    Sims.New.scaleCoul[t] = SC.TempVal.Scale.y;
+    Sims.New.charge[t] = A.charge[0];
+    Sims.New.Type[t] = A.Type[0];
+    Sims.New.MolID[t] = molid;
+  }
+  CBMC_PairwiseInteractions(Vars, systemId, SC, Sims, ntrials, 1);
+  CBMC_FirstBead_Finish(Vars, systemId, CBMC);
+  if (CBMC.SuccessConstruction) Sims.Old.pos[0] = Sims.New.pos[CBMC.selectedTrial];
+}
+
+// mc_widom.h:509-614 with get_random_trial_orientation (:215-303).
+void Widom_Move_Chain_PARTIAL(Variables& Vars, size_t systemId, CBMC_Variables& CBMC) {
+  Components& SC = Vars.SystemComponents[systemId];
+  Simulations& Sims = Vars.Sims[systemId];
+  const size_t comp = SC.TempVal.component;
+  const size_t ms = SC.Moleculesize[comp], chain = ms - 1;
+  const size_t no = Vars.Widom[systemId].NumberWidomTrialsOrientations;
+  const Atoms& A = Sims.d_a[comp];
+  const bool retrace = CBMC.MoveType == CBMC_DELETION || CBMC.MoveType == REINSERTION_RETRACE;
+  const size_t molid = CBMC.MoveType == CBMC_INSERTION ? SC.NumberOfMolecule_for_Component[comp] : SC.TempVal.molecule;
+  const size_t start = SC.TempVal.molecule * ms + 1;
+  const uint32_t slot = CBMC.MoveType == REINSERTION_RETRACE ? GRX_SLOT_RETRACE : GRX_SLOT_ORIENT;
+  const double3 fb = Sims.Old.pos[0];
+  for (size_t o = 0; o < no; ++o) {
+    uint32_t r[4];
+    grx_draw(Vars.Random.Seed, Vars.Random.Stream, SC.Step, slot + (uint32_t)o, r);
+    for (size_t a = 0; a < chain; ++a) {
+      const size_t i = o * chain + a;
+      if (retrace && o == 0) {
+        Sims.New.pos[i] = A.pos[start + a];
+      } else {
+        double3 v{A.pos[1 + a].x - A.pos[0].x, A.pos[1 + a].y - A.pos[0].y, A.pos[1 + a].z - A.pos[0].z};
+        rotate_quaternion(v, grx_u01(r[0]), grx_u01(r[1]), grx_u01(r[2]));
+        Sims.New.pos[i] = double3{fb.x + v.x, fb.y + v.y, fb.z + v.z};
+      }
+      Sims.New.scale[i] = SC.TempVal.Scale.x;
+      Sims.New.scaleCoul[i] = SC.TempVal.Scale.y;
+      Sims.New.charge[i] = A.charge[1 + a];
+      Sims.New.Type[i] = A.Type[1 + a];
+      Sims.New.MolID[i] = molid;
+    }
+  }
+  CBMC_PairwiseInteractions(Vars, systemId, SC, Sims, no, chain);
+  std::vector<double>& Rosen = SC.Rosen;
+  bool good = false;
+  size_t sel = 0;
+  double W = 0.0;
+  if (!Rosen.empty()) {
+    if (!retrace) sel = SelectTrialPosition(Rosen, Vars, systemId, 1);
+    for (double& x : Rosen) x = std::exp(x);
+    W = std::accumulate(Rosen.begin(), Rosen.end(), 0.0);
+    good = retrace || !(W < 1e-150);
+  }
+  if (!good) {
+    CBMC.Rosenbluth = 0.0;
+    CBMC.SuccessConstruction = false;
+    return;
+  }
+  double avg = W / (double)no;
+  if (!Vars.device_FF.VDWRealBias) avg *= std::exp(-SC.Beta * (SC.TrialEnergies[sel].HGReal + SC.TrialEnergies[sel].GGReal));
+  CBMC.selectedTrialOrientation = SC.Trialindex[sel];
+  CBMC.SuccessConstruction = true;
+  CBMC.ChainEnergy = SC.TrialEnergies[sel];
+  CBMC.Rosenbluth *= avg;
+}
+
+// ------------------------------------------------------------------ host mirror updates
+static void write_molecule(Variables& Vars, size_t systemId, size_t comp, size_t mol, const std::vector<double>& pos) {
+  Simulations& Sims = Vars.Sims[systemId];
+  Components& SC = Vars.SystemComponents[systemId];
+  const size_t ms = SC.Moleculesize[comp];
+  Atoms& A = Sims.d_a[comp];
+  std::vector<double> q(ms);
+  std::vector<size_t> ty(ms);
+  for (size_t a = 0; a < ms; ++a) {  // a molecule's charges and types follow the component's template
+    q[a] = A.charge[a];
+    ty[a] = A.Type[a];
+  }
+  check(grx_box_write_molecule(Sims.Box.handle, (int32_t)comp, mol, pos.data(), q.data(), ty.data()),
+        "grx_box_write_molecule");
+  for (size_t a = 0; a < ms; ++a) {
+    const size_t i = mol * ms + a;
+    A.pos[i] = double3{pos[3 * a], pos[3 * a + 1], pos[3 * a + 2]};
+    A.charge[i] = q[a];
+    A.Type[i] = ty[a];
+    A.MolID[i] = mol;
+    A.scale[i] = 1.0;
+    A.scaleCoul[i] = 1.0;
+  }
+  if (mol == SC.NumberOfMolecule_for_Component[comp]) {
+    SC.NumberOfMolecule_for_Component[comp]++;
+    A.size += ms;
+  }
+}
+
+static void remove_molecule(Variables& Vars, size_t systemId, size_t comp, size_t mol) {
+  Simulations& Sims = Vars.Sims[systemId];
+  Components& SC = Vars.SystemComponents[systemId];
+  const size_t ms = SC.Moleculesize[comp];
+  Atoms& A = Sims.d_a[comp];
+  check(grx_box_remove_molecule(Sims.Box.handle, (int32_t)comp, mol), "grx_box_remove_molecule");
+  const size_t last = SC.NumberOfMolecule_for_Component[comp] - 1;
+  if (last != mol)
+    for (size_t a = 0; a < ms; ++a) {
+      const size_t d = mol * ms + a, s = last * ms + a;
+      A.pos[d] = A.pos[s]; A.charge[d] = A.charge[s]; A.Type[d] = A.Type[s];
+      A.scale[d] = A.scale[s]; A.scaleCoul[d] = A.scaleCoul[s]; A.MolID[d] = mol;
+    }
+  SC.NumberOfMolecule_for_Component[comp]--;
+  A.size -= ms;
+}
+
+// ------------------------------------------------------------------ moves
+// RotationAroundAxis (mc_utilities.h:459-481) for a coordinate axis.
+static void rotate_axis(double3& v, double theta, int axis) {
+  const double c = std::cos(theta), w = 1.0 - c, s = std::sin(theta);
+  const double ax = axis == 0, ay = axis == 1, az = axis == 2;
+  const double r0 = ax * ax * w + c, r1 = ax * ay * w + az * s, r2 = ax * az * w - ay * s;
+  const double r3 = ax * ay * w - az * s, r4 = ay * ay * w + c, r5 = ay * az * w + ax * s;
+  const double r6 = ax * az * w + ay * s, r7 = ay * az * w - ax * s, r8 = az * az * w + c;
+  v = double3{v.x * r0 + v.y * r1 + v.z * r2, v.x * r3 + v.y * r4 + v.z * r5, v.x * r6 + v.y * r7 + v.z * r8};
+}
+
+MoveEnergy SingleBodyMove(Variables& Vars, size_t systemId, int MoveType, double RANDOM) {
+  Components& SC = Vars.SystemComponents[systemId];
+  Simulations& Sims = Vars.Sims[systemId];
+  const size_t comp = SC.TempVal.component, mol = SC.TempVal.molecule;
+  const size_t ms = SC.Moleculesize[comp], m0 = mol * ms;
+  Move_Statistics& MS = SC.Moves[comp];
+  MS.Record_Move_Total(MoveType);
+  Atoms& A = Sims.d_a[comp];
+  uint32_t w2[4];
+  grx_draw(Vars.Random.Seed, Vars.Random.Stream, SC.Step, GRX_SLOT_DISP, w2);
+  // get_new_position (mc_utilities.h:485-540)
+  if (MoveType == TRANSLATION) {
+    const double dx = MS.MaxTranslation.x * 2.0 * (grx_u01(w2[0]) - 0.5);
+    const double dy = MS.MaxTranslation.y * 2.0 * (grx_u01(w2[1]) - 0.5);
+    const double dz = MS.MaxTranslation.z * 2.0 * (grx_u01(w2[2]) - 0.5);
+    for (size_t a = 0; a < ms; ++a)
+      Sims.New.pos[a] = double3{A.pos[m0 + a].x + dx, A.pos[m0 + a].y + dy, A.pos[m0 + a].z + dz};
+  } else {
+    const double ang[3] = {MS.MaxRotation.x * 2.0 * (grx_u01(w2[0]) - 0.5),
+                           MS.MaxRotation.y * 2.0 * (grx_u01(w2[1]) - 0.5),
+                           MS.MaxRotation.z * 2.0 * (grx_u01(w2[2]) - 0.5)};
+    const double3 p0 = A.pos[m0];
+    for (size_t a = 0; a < ms; ++a) {
+      double3 v{A.pos[m0 + a].x - p0.x, A.pos[m0 + a].y - p0.y, A.pos[m0 + a].z - p0.z};
+      rotate_axis(v, ang[0], 0);
+      rotate_axis(v, ang[1], 1);
+      rotate_axis(v, ang[2], 2);
+      Sims.New.pos[a] = double3{v.x + p0.x, v.y + p0.y, v.z + p0.z};
+    }
+  }
+  // Calculate_Single_Body_Energy_VDWReal (VDW_Coulomb.cu:626-841) through the ABI
+  std::vector<double> q(ms), ones(ms, 1.0);
+  std::vector<size_t> ty(ms);
+  for (size_t a = 0; a < ms; ++a) {
+    q[a] = A.charge[m0 + a];
+    ty[a] = A.Type[m0 + a];
+  }
+  grx_trials to{}, tn{};
+  to.pos = reinterpret_cast<const double*>(A.pos + m0);
+  tn.pos = reinterpret_cast<const double*>(Sims.New.pos);
+  to.scale = tn.scale = ones.data();
+  to.charge = tn.charge = q.data();
+  to.scale_coul = tn.scale_coul = ones.data();
+  to.type = tn.type = ty.data();
+  to.molid = tn.molid = mol;
+  to.ntrials = tn.ntrials = 1;
+  to.chainsize = tn.chainsize = ms;
+  double e6[6];
+  uint8_t flag = 0;
+  check(grx_single_body_energy(Sims.Box.handle, &to, &tn, (int32_t)comp, 1, 1, Vars.Precision, e6, &flag),
+        "grx_single_body_energy");
+  MoveEnergy energy;
+  if (flag) return energy;
+  energy.HHVDW = e6[0]; energy.HHReal = e6[1]; energy.HGVDW = e6[2];
+  energy.HGReal = e6[3]; energy.GGVDW = e6[4]; energy.GGReal = e6[5];
+  const bool charged = !Vars.device_FF.noCharges && SC.hasPartialCharge[comp];
+  double ew = 0.0;
+  if (charged) {
+    const double2 E = GPU_EwaldDifference_General(Sims, Vars.device_FF, SC, comp, MoveType, m0, SC.TempVal.Scale);
+    energy.GGEwaldE = E.x;
+    energy.HGEwaldE = E.y;
+    ew = E.x + E.y;
+  }
+  const double tot = e6[0] + e6[1] + e6[2] + e6[3] + e6[4] + e6[5] + ew;
+  // SingleBody_Acceptance (mc_single_particle.h:234-293)
+  if (RANDOM < std::exp(-SC.Beta * tot)) {
+    std::vector<double> np(3 * ms);
+    for (size_t a = 0; a < ms; ++a) {
+      np[3 * a] = Sims.New.pos[a].x; np[3 * a + 1] = Sims.New.pos[a].y; np[3 * a + 2] = Sims.New.pos[a].z;
+    }
+    write_molecule(Vars, systemId, comp, mol, np);
+    if (charged) Update_Vector_Ewald(Sims.Box, false, SC, comp);
+    MS.Record_Move_Accept(MoveType);
+    return energy;
+  }
+  return MoveEnergy();
+}
+
+// Insertion_Body (mc_swap_utilities.h:3-132)
+static MoveEnergy Insertion_Body(Variables& Vars, size_t systemId, CBMC_Variables& CBMC) {
+  Components& SC = Vars.SystemComponents[systemId];
+  Simulations& Sims = Vars.Sims[systemId];
+  const size_t comp = SC.TempVal.component;
+  CBMC.MoveType = CBMC_INSERTION;
+  MoveEnergy energy;
+  Widom_Move_FirstBead_PARTIAL(Vars, systemId, CBMC);
+  if (!CBMC.SuccessConstruction || CBMC.Rosenbluth <= 1e-150) {
+    CBMC.SuccessConstruction = false;
+    return energy;
+  }
+  if (SC.Moleculesize[comp] > 1) {
+    Widom_Move_Chain_PARTIAL(Vars, systemId, CBMC);
+    if (!CBMC.SuccessConstruction || CBMC.Rosenbluth <= 1e-150) {
+      CBMC.SuccessConstruction = false;
+      return energy;
+    }
+  }
+  energy = CBMC.FirstBeadEnergy + CBMC.ChainEnergy;
+  if (!Vars.device_FF.noCharges && SC.hasPartialCharge[comp]) {
+    const double2 E = GPU_EwaldDifference_General(Sims, Vars.device_FF, SC, comp, INSERTION,
+                                                  CBMC.selectedTrialOrientation, SC.TempVal.Scale);
+    energy.GGEwaldE = E.x;
+    energy.HGEwaldE = E.y;
+    CBMC.Rosenbluth *= std::exp(-SC.Beta * (E.x + E.y));
+  }
+  energy.TailE = SC.TailCorrectionInsert.empty() ? 0.0 : SC.TailCorrectionInsert[comp];
+  CBMC.Rosenbluth *= std::exp(-SC.Beta * energy.TailE);
+  return energy;
+}
+
+void InsertionMove::Initialize() {
+  InsertionVariables.clear();
+  energy.zero();
+  preFactor = Pacc = 0.0;
+  Accept = false;
+}
+
+void InsertionMove::Calculate(Variables& Vars, size_t systemId) {
+  Components& SC = Vars.SystemComponents[systemId];
+  const size_t comp = SC.TempVal.component;
+  energy = Insertion_Body(Vars, systemId, InsertionVariables);
+  if (!InsertionVariables.SuccessConstruction) {
+    Pacc = preFactor = 0.0;
+    return;
+  }
+  preFactor = GetPrefactor(SC, Vars.Sims[systemId], comp, INSERTION);
+  Pacc = preFactor * InsertionVariables.Rosenbluth / SC.IdealRosenbluthWeight[comp];
+  if (InsertionVariables.Rosenbluth <= 1e-150) Pacc = 0.0;
+}
+
+void InsertionMove::Acceptance(Variables& Vars, size_t systemId, double RANDOM) {
+  Components& SC = Vars.SystemComponents[systemId];
+  Simulations& Sims = Vars.Sims[systemId];
+  const size_t comp = SC.TempVal.component;
+  if (!InsertionVariables.SuccessConstruction || !(RANDOM < Pacc)) {
+    energy.zero();
+    return;
+  }
+  const size_t N = SC.NumberOfMolecule_for_Component[comp];
+  if ((N + 1) * SC.Moleculesize[comp] > SC.Allocate_size[comp]) {  // no room: refuse, as the device driver does
+    energy.zero();
+    return;
+  }
+  Accept = true;
+  std::vector<double> pos, qs;  // AcceptInsertion (mc_swap_utilities.h:94-132)
+  if (SC.Moleculesize[comp] > 1) {
+    grown_atoms(Sims, SC, comp, InsertionVariables.selectedTrialOrientation, pos, qs);
+  } else {
+    pos = {Sims.Old.pos[0].x, Sims.Old.pos[0].y, Sims.Old.pos[0].z};
+  }
+  write_molecule(Vars, systemId, comp, N, pos);
+  if (!Vars.device_FF.noCharges && SC.hasPartialCharge[comp]) Update_Vector_Ewald(Sims.Box, false, SC, comp);
+}
+
+MoveEnergy InsertionMove::Run(Variables& Vars, size_t systemId, double RANDOM) {
+  Components& SC = Vars.SystemComponents[systemId];
+  const size_t comp = SC.TempVal.component;
+  Initialize();
+  SC.Moves[comp].Record_Move_Total(INSERTION);
+  Calculate(Vars, systemId);
+  if (!InsertionVariables.SuccessConstruction) return energy;
+  Acceptance(Vars, systemId, RANDOM);
+  if (Accept) SC.Moves[comp].Record_Move_Accept(INSERTION);
+  return energy;
+}
+
+double InsertionMove::WidomMove(Variables& Vars, size_t systemId) {
+  Initialize();
+  Calculate(Vars, systemId);
+  return InsertionVariables.SuccessConstruction ? InsertionVariables.Rosenbluth : 0.0;
+}
+
+void DeletionMove::Initialize() {
+  DeletionVariables.clear();
+  energy.zero();
+  preFactor = Pacc = 0.0;
+  Accept = false;
+}
+
+// Deletion_Body (mc_swap_utilities.h:135-225) + DeletionMove::Calculate (move_struct.h:122-132)
+void DeletionMove::Calculate(Variables& Vars, size_t systemId) {
+  Components& SC = Vars.SystemComponents[systemId];
+  Simulations& Sims = Vars.Sims[systemId];
+  const size_t comp = SC.TempVal.component;
+  CBMC_Variables& C = DeletionVariables;
+  C.MoveType = CBMC_DELETION;
+  Widom_Move_FirstBead_PARTIAL(Vars, systemId, C);
+  if (!C.SuccessConstruction || C.Rosenbluth <= 1e-150) {
+    C.SuccessConstruction = false;
+    return;
+  }
+  if (SC.Moleculesize[comp] > 1) {
+    Widom_Move_Chain_PARTIAL(Vars, systemId, C);
+    if (!C.SuccessConstruction || C.Rosenbluth <= 1e-150) {
+      C.SuccessConstruction = false;
+      return;
+    }
+  }
+  energy = C.FirstBeadEnergy + C.ChainEnergy;
+  energy.take_negative();
+  if (!Vars.device_FF.noCharges && SC.hasPartialCharge[comp]) {
+    const double2 E = GPU_EwaldDifference_General(Sims, Vars.device_FF, SC, comp, DELETION,
+                                                  SC.TempVal.molecule * SC.Moleculesize[comp], SC.TempVal.Scale);
+    energy.GGEwaldE = E.x;
+    energy.HGEwaldE = E.y;
+    C.Rosenbluth /= std::exp(-SC.Beta * (E.x + E.y));
+  }
+  energy.TailE = SC.TailCorrectionInsert.empty() ? 0.0 : -SC.TailCorrectionInsert[comp];
+  C.Rosenbluth /= std::exp(SC.Beta * energy.TailE);
+  preFactor = GetPrefactor(SC, Sims, comp, DELETION);
+  Pacc = preFactor * SC.IdealRosenbluthWeight[comp] / C.Rosenbluth;
+}
+
+void DeletionMove::Acceptance(Variables& Vars, size_t systemId, double RANDOM) {
+  Components& SC = Vars.SystemComponents[systemId];
+  Simulations& Sims = Vars.Sims[systemId];
+  const size_t comp = SC.TempVal.component;
+  if (!DeletionVariables.SuccessConstruction || !(RANDOM < Pacc)) {
+    energy.zero();
+    return;
+  }
+  Accept = true;
+  remove_molecule(Vars, systemId, comp, SC.TempVal.molecule);
+  if (!Vars.device_FF.noCharges && SC.hasPartialCharge[comp]) Update_Vector_Ewald(Sims.Box, false, SC, comp);
+}
+
+MoveEnergy DeletionMove::Run(Variables& Vars, size_t systemId, double RANDOM) {
+  Components& SC = Vars.SystemComponents[systemId];
+  const size_t comp = SC.TempVal.component;
+  Initialize();
+  SC.Moves[comp].Record_Move_Total(DELETION);
+  Calculate(Vars, systemId);
+  if (!DeletionVariables.SuccessConstruction) return energy;
+  Acceptance(Vars, systemId, RANDOM);
+  if (Accept) SC.Moves[comp].Record_Move_Accept(DELETION);
+  return energy;
+}
+
+void ReinsertionMove::Initialize() {
+  InsertionVariables.clear();
+  DeletionVariables.clear();
+  energy.zero();
+  old_energy.zero();
+  Pacc = 0.0;
+  Accept = false;
+}
+
+// move_struct.h:184-274
+void ReinsertionMove::Calculate_Insertion(Variables& Vars, size_t systemId) {
+  Components& SC = Vars.SystemComponents[systemId];
+  Simulations& Sims = Vars.Sims[systemId];
+  const size_t comp = SC.TempVal.component;
+  const size_t ms = SC.Moleculesize[comp];
+  CBMC_Variables& C = InsertionVariables;
+  C.MoveType = REINSERTION_INSERTION;
+  Widom_Move_FirstBead_PARTIAL(Vars, systemId, C);
+  if (C.Rosenbluth <= 1e-150) C.SuccessConstruction = false;
+  if (!C.SuccessConstruction) return;
+  if (ms > 1) {
+    Widom_Move_Chain_PARTIAL(Vars, systemId, C);
+    if (C.Rosenbluth <= 1e-150) C.SuccessConstruction = false;
+    if (!C.SuccessConstruction) return;
+  }
+  // StoreNewLocation_Reinsertion: the grown molecule, kept while the retrace reuses New
+  NewPositions.assign(ms, double3{});
+  NewPositions[0] = Sims.Old.pos[0];
+  for (size_t a = 1; a < ms; ++a) NewPositions[a] = Sims.New.pos[C.selectedTrialOrientation * (ms - 1) + (a - 1)];
+  energy = C.FirstBeadEnergy + C.ChainEnergy;
+}
+
+// move_struct.h:276-290
+void ReinsertionMove::Calculate_Deletion(Variables& Vars, size_t systemId) {
+  Components& SC = Vars.SystemComponents[systemId];
+  const size_t comp = SC.TempVal.component;
+  CBMC_Variables& C = DeletionVariables;
+  C.MoveType = REINSERTION_RETRACE;
+  C.StoredR = InsertionVariables.StoredR;
+  Widom_Move_FirstBead_PARTIAL(Vars, systemId, C);
+  if (!C.SuccessConstruction) return;
+  if (SC.Moleculesize[comp] > 1) Widom_Move_Chain_PARTIAL(Vars, systemId, C);
+  old_energy = C.FirstBeadEnergy + C.ChainEnergy;
+}
+
+// move_struct.h:292-336
+void ReinsertionMove::Calculate_AdjustRosenbluth(Variables& Vars, size_t systemId) {
+  Components& SC = Vars.SystemComponents[systemId];
+  Simulations& Sims = Vars.Sims[systemId];
+  const size_t comp = SC.TempVal.component;
+  const size_t ms = SC.Moleculesize[comp];
+  if (!Vars.device_FF.noCharges && SC.hasPartialCharge[comp]) {
+    for (size_t a = 0; a < ms; ++a) Sims.Old.pos[1 + a] = NewPositions[a];
+    const double2 E = GPU_EwaldDifference_General(Sims, Vars.device_FF, SC, comp, REINSERTION,
+                                                  SC.TempVal.molecule * ms, SC.TempVal.Scale);
+    energy.GGEwaldE = E.x;
+    energy.HGEwaldE = E.y;
+    InsertionVariables.Rosenbluth *= std::exp(-SC.Beta * (E.x + E.y));
+  }
+}
+
+// move_struct.h:338-376
+void ReinsertionMove::Acceptance(Variables& Vars, size_t systemId, double RANDOM) {
+  Components& SC = Vars.SystemComponents[systemId];
+  Simulations& Sims = Vars.Sims[systemId];
+  const size_t comp = SC.TempVal.component;
+  const size_t ms = SC.Moleculesize[comp];
+  Pacc = InsertionVariables.Rosenbluth / DeletionVariables.Rosenbluth;
+  if (!InsertionVariables.SuccessConstruction || InsertionVariables.Rosenbluth <= 1e-150 || !(RANDOM < Pacc)) {
+    energy.zero();
+    return;
+  }
+  Accept = true;
+  std::vector<double> pos(3 * ms);
+  for (size_t a = 0; a < ms; ++a) {
+    pos[3 * a] = NewPositions[a].x; pos[3 * a + 1] = NewPositions[a].y; pos[3 * a + 2] = NewPositions[a].z;
+  }
+  write_molecule(Vars, systemId, comp, SC.TempVal.molecule, pos);  // Update_Reinsertion_data
+  if (!Vars.device_FF.noCharges && SC.hasPartialCharge[comp]) Update_Vector_Ewald(Sims.Box, false, SC, comp);
+}
+
+MoveEnergy ReinsertionMove::Run(Variables& Vars, size_t systemId, double RANDOM) {
+  Components& SC = Vars.SystemComponents[systemId];
+  const size_t comp = SC.TempVal.component;
+  Initialize();
+  SC.Moves[comp].Record_Move_Total(REINSERTION);
+  Calculate_Insertion(Vars, systemId);
+  if (!InsertionVariables.SuccessConstruction) return MoveEnergy();
+  Calculate_Deletion(Vars, systemId);
+  if (!DeletionVariables.SuccessConstruction) return MoveEnergy();
+  energy -= old_energy;
+  Calculate_AdjustRosenbluth(Vars, systemId);
+  Acceptance(Vars, systemId, RANDOM);
+  if (Accept) SC.Moves[comp].Record_Move_Accept(REINSERTION);
+  return energy;
+}
+
+// RunMoves (axpy.cu:102-298) for the moves of this path.
+MoveEnergy RunMoves(Variables& Vars, size_t systemId, size_t comp) {
+  Components& SC = Vars.SystemComponents[systemId];
+  Move_Statistics& MS = SC.Moves[comp];
+  uint32_t w[4];
+  grx_draw(Vars.Random.Seed, Vars.Random.Stream, SC.Step, GRX_SLOT_MOVE, w);
+  const size_t N = SC.NumberOfMolecule_for_Component[comp];
+  SC.TempVal.component = comp;
+  SC.TempVal.molecule = (size_t)(grx_u01(w[0]) * (double)N);
+  SC.TempVal.Scale = double2{1.0, 1.0};
+  const double r = grx_u01(w[1]);
+  const double uacc = grx_u01(w[3]);
+  MoveEnergy dE;
+  if (r < MS.TranslationProb) {
+    if (N > 0) dE = SingleBodyMove(Vars, systemId, TRANSLATION, uacc);
+  } else if (r < MS.RotationProb) {
+    if (N > 0) dE = SingleBodyMove(Vars, systemId, ROTATION, uacc);
+  } else if (r < MS.ReinsertionProb) {
+    if (N > 0) {
+      ReinsertionMove m;
+      dE = m.Run(Vars, systemId, uacc);
+    }
+  } else if (r < MS.SwapProb) {
+    if (grx_u01(w[2]) < 0.5) {
+      InsertionMove m;
+      dE = m.Run(Vars, systemId, uacc);
+    } else if (N > 0) {
+      DeletionMove m;
+      dE = m.Run(Vars, systemId, uacc);
+    }
+  }
+  SC.deltaE += dE;
+  SC.Step++;
+  return dE;
+}
+
+// ------------------------------------------------------------------ Widom statistics
+void RecordRosen(Components& SC, size_t comp, size_t block, double W) {
+  if (SC.Rosen_Widom.size() <= comp) SC.Rosen_Widom.resize(comp + 1);
+  std::vector<double3>& B = SC.Rosen_Widom[comp].Blocks;
+  if (B.size() < SC.Nblock) B.resize(SC.Nblock);
+  if (block >= SC.Nblock) block = SC.Nblock - 1;
+  B[block].x += W;
+  B[block].y += W * W;
+  B[block].z += 1.0;
+}
+
+double WidomAverageRosenbluth(const Components& SC, size_t comp) {
+  const std::vector<double3>& B = SC.Rosen_Widom[comp].Blocks;
+  double s = 0.0;
+  size_t n = 0;
+  for (const double3& b : B) {
+    if (b.z <= 0) continue;
+    s += b.x / b.z;
+    ++n;
+  }
+  return n ? s / (double)n : 0.0;
+}
+
+// ComputeFugacity (print_statistics.cuh:100-110): mu_ex = -kT ln<W>, reported in K.
+double WidomChemicalPotential(const Components& SC, size_t comp) {
+  return -SC.Temperature * std::log(WidomAverageRosenbluth(SC, comp));
+}
+
+// ------------------------------------------------------------------ device-resident moves
+grx_gcmc_stats RunMoves_Device(Variables& Vars, size_t systemId, size_t comp, int64_t nsteps) {
+  Components& SC = Vars.SystemComponents[systemId];
+  Simulations& Sims = Vars.Sims[systemId];
+  const Move_Statistics& MS = SC.Moves[comp];
+  grx_gcmc_desc d{};
+  d.component = (int32_t)comp;
+  d.ntrials = (int32_t)Vars.Widom[systemId].NumberWidomTrials;
+  d.norient = (int32_t)Vars.Widom[systemId].NumberWidomTrialsOrientations;
+  d.p_translation = MS.TranslationProb;
+  d.p_rotation = MS.RotationProb;
+  d.p_reinsertion = MS.ReinsertionProb;
+  d.p_swap = MS.SwapProb;
+  d.max_translation[0] = MS.MaxTranslation.x; d.max_translation[1] = MS.MaxTranslation.y;
+  d.max_translation[2] = MS.MaxTranslation.z;
+  d.max_rotation[0] = MS.MaxRotation.x; d.max_rotation[1] = MS.MaxRotation.y; d.max_rotation[2] = MS.MaxRotation.z;
+  d.beta = SC.Beta;
+  d.pressure = SC.Pressure;
+  d.fugacity_coeff = SC.FugacityCoeff[comp];
+  d.mol_fraction = SC.MolFraction[comp];
+  d.ideal_rosenbluth = SC.IdealRosenbluthWeight[comp];
+  d.tail_insert = SC.TailCorrectionInsert.empty() ? 0.0 : SC.TailCorrectionInsert[comp];
+  d.seed = Vars.Random.Seed;
+  d.stream = Vars.Random.Stream;
+  grx_gcmc_stats st{};
+  grx_box* b = Sims.Box.handle;
+  check(grx_gcmc_run(&b, 1, &d, SC.Step, nsteps, Vars.Precision, &st), "grx_gcmc_run");
+  SC.Step += (uint64_t)nsteps;
+  Sync_Host_Mirror(Vars, systemId, comp);
+  return st;
+}
+
+void Sync_Host_Mirror(Variables& Vars, size_t systemId, size_t comp) {
+  Components& SC = Vars.SystemComponents[systemId];
+  Simulations& Sims = Vars.Sims[systemId];
+  const size_t ms = SC.Moleculesize[comp];
+  size_t n = 0;
+  check(grx_box_get_component_size(Sims.Box.handle, (int32_t)comp, &n), "grx_box_get_component_size");
+  Atoms& A = Sims.d_a[comp];
+  std::vector<double> pos(3 * n);
+  if (n) check(grx_box_get_positions(Sims.Box.handle, (int32_t)comp, pos.data(), n), "grx_box_get_positions");
+  for (size_t i = 0; i < n; ++i) {
+    A.pos[i] = double3{pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
+    A.charge[i] = A.charge[i % ms];
+    A.Type[i] = A.Type[i % ms];
+    A.MolID[i] = i / ms;
+    A.scale[i] = 1.0;
+    A.scaleCoul[i] = 1.0;
+  }
+  A.size = n;
+  SC.NumberOfMolecule_for_Component[comp] = n / ms;
+}
+
+}  // namespace graspa

@@ -205,6 +205,15 @@ grx_status grx_box_set_component(grx_box* box, int32_t comp, const grx_atoms* at
 grx_status grx_box_get_component_size(grx_box* box, int32_t comp, size_t* size);
 grx_status grx_box_get_positions(grx_box* box, int32_t comp, double* pos_out, size_t n);
 grx_status grx_box_get_exclusion(grx_box* box, int32_t comp, double* intra, double* self);
+/* Write the atoms of adsorbate molecule `mol` (positions 3*molsize, charges, types;
+ * every atom gets MolID = mol). mol equal to the current molecule count appends a
+ * molecule: Update_insertion_data_Parallel (mc_utilities.h:191-234); a smaller mol
+ * overwrites it in place: update_translation_position (mc_utilities.h:285-292). */
+grx_status grx_box_write_molecule(grx_box* box, int32_t comp, size_t mol, const double* pos,
+                                  const double* charge, const size_t* type);
+/* Remove adsorbate molecule `mol`; the component's last molecule moves into its
+ * slot and takes its MolID: Update_deletion_data_Parallel (mc_utilities.h:163-189). */
+grx_status grx_box_remove_molecule(grx_box* box, int32_t comp, size_t mol);
 
 /* ---- pair energies ------------------------------------------------------ */
 /* Per-trial host-guest and guest-guest VDW + real Coulomb energies and overlap
@@ -281,7 +290,7 @@ grx_status grx_widom_insertions_async(grx_box* box, const grx_widom_desc* desc,
 
 /* ---- GCMC ----------------------------------------------------------------- */
 /* Move mix and thermodynamic state of one box's GCMC run: the translation /
- * rotation / CBMC swap branches of RunMoves (axpy.cu:102-298) with the move
+ * rotation / reinsertion / CBMC swap branches of RunMoves (axpy.cu:102-298) with the move
  * probabilities of Move_Statistics (cumulative, as the reference stores them),
  * get_new_position (mc_utilities.h:485-606) and GetPrefactor (mc_utilities.h:315-351). */
 typedef struct {
@@ -291,6 +300,7 @@ typedef struct {
   int32_t pad_;
   double p_translation;       /* TranslationProb (cumulative) */
   double p_rotation;          /* RotationProb (cumulative) */
+  double p_reinsertion;       /* ReinsertionProb (cumulative) */
   double p_swap;              /* SwapProb (cumulative); insertion / deletion 50:50 */
   double max_translation[3];  /* MaxTranslation, A */
   double max_rotation[3];     /* MaxRotation, rad */
@@ -308,8 +318,8 @@ typedef struct {
 } grx_gcmc_desc;
 
 typedef struct {
-  int64_t attempts[4];        /* translation, rotation, insertion, deletion */
-  int64_t accepted[4];
+  int64_t attempts[5];        /* translation, rotation, insertion, deletion, reinsertion */
+  int64_t accepted[5];
   int64_t n_molecules;        /* after the run */
   int64_t capacity_hits;      /* insertions refused for lack of component capacity */
   double energy[4];           /* sum of accepted dE: VDW, real Coulomb, Ewald Fourier, total */

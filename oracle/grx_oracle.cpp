@@ -824,6 +824,7 @@ struct GState {
 struct Grow {
   bool ok = false;
   double rosen = 0.0;  // product of the averaged step weights
+  double stored = 0.0; // reinsertion: first-bead weight sum minus the selected trial
   double e1[4] = {0, 0, 0, 0}, e2[4] = {0, 0, 0, 0};
   std::vector<double> pos, qs;  // chosen (insertion) or existing (deletion) molecule
 };
@@ -852,11 +853,20 @@ void rotate_axis(double* v, double theta, int axis) {
 // CBMC growth of one molecule (insertion) or retrace of an existing one (deletion):
 // Widom_Move_FirstBead_PARTIAL + Widom_Move_Chain_PARTIAL (mc_widom.h:385-614) with
 // CBMC_FirstBead_Finish (:305-383), insertion and deletion branches.
+// mode: CBMC_INSERTION, CBMC_DELETION, REINSERTION_INSERTION (all trials new,
+// StoredR = W1 - w_selected returned in g.stored) or REINSERTION_RETRACE (one
+// first-bead trial at the old position, W1 += stored; orientations from the
+// retrace slots).
+enum { G_INSERT = 0, G_DELETE = 1, G_REINS = 2, G_RETRACE = 3 };
 Grow cbmc_grow(const ora_box* box, const ora_ff* ff, const ora_atoms* at, int64_t comp, int64_t ms,
                const double* tmpl_pos, const double* tmpl_q, const int64_t* tmpl_t, int64_t nt, int64_t no,
-               double beta, uint64_t seed, uint32_t stream, uint64_t move, int64_t newmol, bool deletion,
-               const double* oldpos) {
+               double beta, uint64_t seed, uint32_t stream, uint64_t move, int64_t newmol, int mode,
+               const double* oldpos, double stored = 0.0) {
   Grow g;
+  const bool deletion = mode == G_DELETE || mode == G_RETRACE;
+  const int64_t navg1 = nt;
+  if (mode == G_RETRACE) nt = 1;
+  const uint32_t oslot = mode == G_RETRACE ? 3072u : 1024u;
   const int64_t chain = ms - 1;
   uint32_t sel_words[4];
   ora_draw(seed, stream, move, 2048u, sel_words);
@@ -898,7 +908,9 @@ Grow cbmc_grow(const ora_box* box, const ora_ff* ff, const ora_atoms* at, int64_
   for (double l : lw1) w1 += std::exp(l);
   if (!deletion && w1 < 1e-150) return g;
   const int64_t real1 = idx1[(size_t)s1];
-  double avg1 = w1 / (double)nt;
+  if (mode == G_REINS) g.stored = w1 - std::exp(lw1[(size_t)s1]);
+  if (mode == G_RETRACE) w1 += stored;
+  double avg1 = w1 / (double)navg1;
   if (!ff->vdw_real_bias) avg1 *= std::exp(-beta * (e1[4 * real1 + 1] + e1[4 * real1 + 3]));
   if (avg1 <= 1e-150) return g;
   for (int k = 0; k < 4; ++k) g.e1[k] = e1[4 * real1 + k];
@@ -913,7 +925,7 @@ Grow cbmc_grow(const ora_box* box, const ora_ff* ff, const ora_atoms* at, int64_
     std::vector<int64_t> oty(no * chain);
     for (int64_t o = 0; o < no; ++o) {
       uint32_t r[4];
-      ora_draw(seed, stream, move, 1024u + (uint32_t)o, r);
+      ora_draw(seed, stream, move, oslot + (uint32_t)o, r);
       for (int64_t a = 0; a < chain; ++a) {
         const int64_t j = o * chain + a;
         if (deletion && o == 0) {
@@ -1005,6 +1017,7 @@ extern "C" void ora_gcmc_run(const ora_box* box, const ora_ff* ff, double* pos, 
     int kind = -1;
     if (r < g->p_translation) kind = 0;
     else if (r < g->p_rotation) kind = 1;
+    else if (r < g->p_reinsertion) kind = 4;
     else if (r < g->p_swap) kind = (u01(w[2]) < 0.5) ? 2 : 3;
     const double uacc = u01(w[3]);
     if (kind == 0 || kind == 1) {
@@ -1058,11 +1071,46 @@ extern "C" void ora_gcmc_run(const ora_box* box, const ora_ff* ff, double* pos, 
           }
         }
       }
+    } else if (kind == 4 && N > 0) {  // ReinsertionMove::Run (move_struct.h:377-406)
+      st->attempts[4]++;
+      const int64_t m0 = a0 + mol * ms;
+      std::vector<double> oldp(S.pos.begin() + 3 * m0, S.pos.begin() + 3 * (m0 + ms));
+      std::vector<double> q(S.charge.begin() + m0, S.charge.begin() + m0 + ms);
+      ora_atoms at = S.view();
+      Grow gi = cbmc_grow(box, ff, &at, comp, ms, slot0.data(), mol_charge, mol_type, g->ntrials, g->norient,
+                          g->beta, g->seed, g->stream, move, mol, G_REINS, nullptr);
+      if (gi.ok) {
+        Grow gr = cbmc_grow(box, ff, &at, comp, ms, slot0.data(), mol_charge, mol_type, g->ntrials, g->norient,
+                            g->beta, g->seed, g->stream, move, mol, G_RETRACE, oldp.data(), gi.stored);
+        if (gr.ok) {
+          double rosen = gi.rosen, ew = 0.0;
+          if (charged) {  // Calculate_AdjustRosenbluth: old molecule out, new in, no exclusion change
+            double d2[2];
+            ora_ewald_delta(box, s_ads, s_fw, 0, nullptr, ms, oldp.data(), q.data(), ms, gi.pos.data(), q.data(),
+                            s_new.data(), d2);
+            ew = d2[0] + 2.0 * d2[1];
+            rosen *= std::exp(-g->beta * ew);
+          }
+          const double pacc = rosen / gr.rosen;
+          if (uacc < pacc) {
+            st->accepted[4]++;
+            for (int64_t k = 0; k < 3 * ms; ++k) S.pos[3 * m0 + k] = gi.pos[k];
+            if (mol == 0) std::copy(gi.pos.begin(), gi.pos.end(), slot0.begin());
+            if (charged) std::copy(s_new.begin(), s_new.end(), s_ads);
+            const double ev = gi.e1[0] + gi.e1[2] + gi.e2[0] + gi.e2[2] - (gr.e1[0] + gr.e1[2] + gr.e2[0] + gr.e2[2]);
+            const double er = gi.e1[1] + gi.e1[3] + gi.e2[1] + gi.e2[3] - (gr.e1[1] + gr.e1[3] + gr.e2[1] + gr.e2[3]);
+            st->energy[0] += ev;
+            st->energy[1] += er;
+            st->energy[2] += ew;
+            st->energy[3] += ev + er + ew;
+          }
+        }
+      }
     } else if (kind == 2) {  // CBMC insertion (InsertionMove::Run, move_struct.h:71-89)
       st->attempts[2]++;
       ora_atoms at = S.view();
       Grow gr = cbmc_grow(box, ff, &at, comp, ms, slot0.data(), mol_charge, mol_type, g->ntrials, g->norient,
-                          g->beta, g->seed, g->stream, move, N, false, nullptr);
+                          g->beta, g->seed, g->stream, move, N, G_INSERT, nullptr);
       if (gr.ok) {
         double ew = 0.0, rosen = gr.rosen;
         if (charged) {
@@ -1103,7 +1151,7 @@ extern "C" void ora_gcmc_run(const ora_box* box, const ora_ff* ff, double* pos, 
       std::vector<double> oldp(S.pos.begin() + 3 * m0, S.pos.begin() + 3 * (m0 + ms));
       ora_atoms at = S.view();
       Grow gr = cbmc_grow(box, ff, &at, comp, ms, slot0.data(), mol_charge, mol_type, g->ntrials, g->norient,
-                          g->beta, g->seed, g->stream, move, mol, true, oldp.data());
+                          g->beta, g->seed, g->stream, move, mol, G_DELETE, oldp.data());
       if (gr.ok) {
         double rosen = gr.rosen, ew = 0.0;
         std::vector<double> q(S.charge.begin() + m0, S.charge.begin() + m0 + ms);

@@ -168,13 +168,14 @@ int32_t ora_max_threads(void);
 
 
 /* GCMC of one adsorbate component (RunMoves, axpy.cu:102-298, restricted to the
- * translation / rotation / CBMC insertion / CBMC deletion branches). */
+ * translation / rotation / reinsertion / CBMC insertion / CBMC deletion branches). */
 typedef struct {
   int64_t component;
   int64_t ntrials;
   int64_t norient;
   double p_translation;   /* cumulative move probabilities (Move_Statistics) */
   double p_rotation;
+  double p_reinsertion;
   double p_swap;
   double max_translation[3];
   double max_rotation[3];
@@ -189,10 +190,9 @@ typedef struct {
 } ora_gcmc;
 
 typedef struct {
-  int64_t attempts[4];    /* translation, rotation, insertion, deletion */
-  int64_t accepted[4];
+  int64_t attempts[5];    /* translation, rotation, insertion, deletion, reinsertion */
+  int64_t accepted[5];
   int64_t n_molecules;
-  int64_t pad_;
   double energy[4];       /* running sums of accepted dE: vdw, real, ewald, total */
   double sum_n;           /* sum of N after every step (loading average) */
 } ora_gcmc_stats;

@@ -60,15 +60,16 @@ class OraWidomResult(C.Structure):
 
 class OraGcmc(C.Structure):
     _fields_ = [("component", C.c_int64), ("ntrials", C.c_int64), ("norient", C.c_int64),
-                ("p_translation", C.c_double), ("p_rotation", C.c_double), ("p_swap", C.c_double),
-                ("max_translation", C.c_double * 3), ("max_rotation", C.c_double * 3), ("beta", C.c_double),
+                ("p_translation", C.c_double), ("p_rotation", C.c_double), ("p_reinsertion", C.c_double),
+                ("p_swap", C.c_double), ("max_translation", C.c_double * 3), ("max_rotation", C.c_double * 3),
+                ("beta", C.c_double),
                 ("pressure", C.c_double), ("fugacity_coeff", C.c_double), ("mol_fraction", C.c_double),
                 ("ideal_rosenbluth", C.c_double), ("seed", C.c_uint64), ("stream", C.c_uint32), ("pad_", C.c_uint32)]
 
 
 class OraGcmcStats(C.Structure):
-    _fields_ = [("attempts", C.c_int64 * 4), ("accepted", C.c_int64 * 4), ("n_molecules", C.c_int64),
-                ("pad_", C.c_int64), ("energy", C.c_double * 4), ("sum_n", C.c_double)]
+    _fields_ = [("attempts", C.c_int64 * 5), ("accepted", C.c_int64 * 5), ("n_molecules", C.c_int64),
+                ("energy", C.c_double * 4), ("sum_n", C.c_double)]
 
 
 def build(force=False):

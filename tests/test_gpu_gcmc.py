@@ -3,6 +3,7 @@
 The oracle (ora_gcmc_run) restates RunMoves (axpy.cu:102-298) for translation,
 rotation and CBMC insertion / deletion of one component; both sides draw the same
 Philox counters, so in FP64 the two Markov chains must take identical decisions.
+The move mix is translation : rotation : reinsertion : swap = 1 : 1 : 1 : 2.
 
 Tolerances:
   FP64 : identical move counts and molecule numbers; positions within 1e-9 A
@@ -27,13 +28,16 @@ CAP = 3 * 64
 
 
 def params(grx, **kw):
-    return grx.gcmc_desc(1, **kw)
+    mix = dict(p_translation=0.2, p_rotation=0.4, p_reinsertion=0.6, p_swap=1.0)
+    mix.update(kw)
+    return grx.gcmc_desc(1, **mix)
 
 
 def ora_params(d):
     g = O.OraGcmc()
     g.component, g.ntrials, g.norient = d.component, d.ntrials, d.norient
     g.p_translation, g.p_rotation, g.p_swap = d.p_translation, d.p_rotation, d.p_swap
+    g.p_reinsertion = d.p_reinsertion
     for k in range(3):
         g.max_translation[k] = d.max_translation[k]
         g.max_rotation[k] = d.max_rotation[k]
@@ -126,7 +130,7 @@ def test_gcmc_capacity_and_edges(grx_lib):
     s = co2_system(n_co2=0)
     box = grx_lib.Box(s, capacity=[s["comp_start"][1], 3 * 2])  # room for two molecules
     box.ewald_total()
-    d = params(grx_lib, p_translation=0.0, p_rotation=0.0, pressure_pa=1e9)
+    d = params(grx_lib, p_translation=0.0, p_rotation=0.0, p_reinsertion=0.0, pressure_pa=1e9)
     st = grx_lib.gcmc_run([box], [d], 0, 300, grx_lib.GRX_FP64)[0]
     assert st.n_molecules <= 2 and st.capacity_hits > 0
     assert box.component_size(1) == 3 * st.n_molecules

@@ -1,0 +1,92 @@
+"""The C++ host layer (graspa_gb300/host: gRASPA's structs and move drivers over
+the C ABI) on the GPU. Its example driver is run as a separate process on a system
+file, in three modes:
+  host   : RunMoves one move at a time (every energy call a libgrx call)
+  device : the same moves in one grx_gcmc_run
+  widom  : InsertionMove::WidomMove + the Widom statistics
+FP64 host-driven moves take the same decisions as the FP64 oracle (identical move
+counts, positions within 1e-9 A); the accepted-energy sum matches the drift check
+of the recomputed FP64 totals to 1e-8 relative; Widom Rosenbluth weights match the
+device Widom kernel to 1e-10 relative (same Philox draws, different summation order).
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from graspa_gb300 import build as B
+from graspa_gb300 import grx, system_file
+from oracle import oracle as O
+from tests.systems import co2_system
+from tests.test_gpu_gcmc import ora_params, params
+
+pytestmark = pytest.mark.gpu
+
+CAP = 3 * 64
+
+
+def run_driver(tmp_path, s, d, mode, n, prec=grx.GRX_FP64):
+    f = os.path.join(tmp_path, "system.txt")
+    system_file.write_system(f, s, [s["comp_start"][1], CAP], d, precision=prec)
+    r = subprocess.run([B.DRIVER, f, mode, str(n)], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    return system_file.parse_driver_output(r.stdout)
+
+
+@pytest.mark.parametrize("mode", ["host", "device"])
+def test_host_layer_gcmc_matches_oracle(grx_lib, tmp_path, mode):
+    s = co2_system(n_co2=4)
+    d = params(grx_lib, pressure_pa=1e6)
+    out = run_driver(str(tmp_path), s, d, mode, 150)
+    ost, after, _ = O.OracleSystem(s).gcmc(ora_params(d), [s["comp_start"][1], CAP], 0, 150)
+    assert out["attempts"] == list(ost.attempts)
+    assert out["accepted"] == list(ost.accepted)
+    assert int(out["n_molecules"]) == ost.n_molecules
+    nfw = s["comp_start"][1]
+    assert np.max(np.abs(out["positions"] - after["pos"][nfw:])) <= 1e-9
+    assert abs(out["energy_sum"] - ost.energy[3]) <= 1e-9 * max(1.0, abs(ost.energy[3]))
+    assert abs(out["drift"]) <= 1e-8 * max(1.0, abs(out["energy_sum"])) + 1e-6
+
+
+def test_host_layer_widom_matches_device_kernel(grx_lib, tmp_path):
+    s = co2_system(n_co2=0)
+    d = params(grx_lib)
+    out = run_driver(str(tmp_path), s, d, "widom", 40)
+    box = grx_lib.Box(s, capacity=[s["comp_start"][1], CAP])
+    box.ewald_total()
+    wd = grx_lib.widom_desc(s, 1, ntrials=d.ntrials, norient=d.norient, seed=d.seed, stream=d.stream)
+    res = box.widom(wd, 0, 40, grx_lib.GRX_FP64)
+    W = np.array(out["W"])
+    ref = res["rosenbluth"] * (res["success"] != 0)
+    assert np.all(np.abs(W - ref) <= 1e-10 * np.maximum(np.abs(ref), 1e-300))
+    # ComputeFugacity: mu_ex = -T ln<W> (block averages of equal blocks = plain mean)
+    assert abs(out["widom_average_rosenbluth"] - W.mean()) <= 1e-12 * W.mean()
+    assert abs(out["widom_mu_ex_K"] + 300.0 * np.log(W.mean())) <= 1e-9
+
+
+def test_write_and_remove_molecule(grx_lib):
+    """grx_box_write_molecule / grx_box_remove_molecule keep the device box equal
+    to the same edit of the system dict (FP64 totals against the oracle)."""
+    s = co2_system(n_co2=3)
+    nfw = s["comp_start"][1]
+    box = grx_lib.Box(s, capacity=[nfw, CAP])
+    P = s["pos"].reshape(-1, 3)
+    mols = [P[nfw + 3 * m: nfw + 3 * m + 3].copy() for m in range(3)]
+    tm = s["templates"][1]
+    box.remove_molecule(1, 0)          # the last molecule moves into slot 0
+    new = mols[1] + np.array([0.5, -0.3, 0.2])
+    box.write_molecule(1, 1, new, tm["charge"], tm["type"])          # overwrite in place
+    box.write_molecule(1, 2, mols[0], tm["charge"], tm["type"])      # append
+    expect = np.concatenate([mols[2], new, mols[0]])
+    assert np.array_equal(box.positions(1), expect)
+    s2 = dict(s)
+    s2["pos"] = np.concatenate([P[:nfw], expect])
+    t = box.total_energy()
+    ref = O.OracleSystem(s2).vdw_real_total()
+    got = [t[k] for k in ("hh_vdw", "hh_real", "hg_vdw", "hg_real", "gg_vdw", "gg_real")]
+    assert np.all(np.abs(np.array(got) - ref) <= 1e-10 * np.maximum(np.abs(ref), 1.0))
+    with pytest.raises(grx_lib.GrxError):
+        box.write_molecule(1, 5, new, tm["charge"], tm["type"])   # beyond the count
+    with pytest.raises(grx_lib.GrxError):
+        box.remove_molecule(1, 3)

@@ -11,7 +11,7 @@ from oracle import oracle as O
 def gcmc_params(seed=42, stream=0, T=300.0, pressure_pa=1e5):
     g = O.OraGcmc()
     g.component, g.ntrials, g.norient = 1, 10, 10
-    g.p_translation, g.p_rotation, g.p_swap = 0.25, 0.5, 1.0
+    g.p_translation, g.p_rotation, g.p_reinsertion, g.p_swap = 0.2, 0.4, 0.6, 1.0
     for d in range(3):
         g.max_translation[d] = 1.0
         g.max_rotation[d] = 0.5
