@@ -452,8 +452,32 @@ grx_status grx_box_create(const grx_box_desc* desc, grx_box** out) {
   d.cut_coul2f = (float)ff.cutoff_coul_sq;
   for (int k = 0; k < 3; ++k) d.kmax[k] = g.kmax[k];
   for (int k = 0; k < 9; ++k) d.cellf[k] = (float)g.cell[k];
-  d.cull = g.cubic ? 1 : 0;  // single-image rounding is the true minimum image only here
+  // Tile culling needs a lower bound of the periodic distance from a bead to a tile
+  // centre. Orthorhombic: the rounded image is the nearest one. General cells: the
+  // rounded image e is the nearest one when |e| <= w_min/2 (any other image is at
+  // least w_min - |e| away); otherwise max_k |s_k| w_k (s = fractional remainder,
+  // w_k = distance between lattice planes) bounds it from below.
+  d.cull = 1;
+  d.chunk_mult = 4;
   d.cull_r = (float)(std::sqrt((double)d.screen2) + 0.01);
+  {
+    const double* C = g.cell;
+    const double a[3] = {C[0], C[1], C[2]}, bb[3] = {C[3], C[4], C[5]}, c[3] = {C[6], C[7], C[8]};
+    auto cross_norm = [](const double* u, const double* v) {
+      const double x = u[1] * v[2] - u[2] * v[1], y = u[2] * v[0] - u[0] * v[2], z = u[0] * v[1] - u[1] * v[0];
+      return std::sqrt(x * x + y * y + z * z);
+    };
+    const double V = std::fabs(a[0] * (bb[1] * c[2] - bb[2] * c[1]) - a[1] * (bb[0] * c[2] - bb[2] * c[0]) +
+                               a[2] * (bb[0] * c[1] - bb[1] * c[0]));
+    const double w[3] = {V / cross_norm(bb, c), V / cross_norm(c, a), V / cross_norm(a, bb)};
+    double wmin = w[0];
+    for (int k = 0; k < 3; ++k) {
+      d.wperp[k] = (float)(w[k] * (1.0 - 1e-5));
+      wmin = std::min(wmin, w[k]);
+    }
+    const double h = 0.5 * wmin * (1.0 - 1e-4);
+    d.half_wmin2 = (float)(h * h);
+  }
 
   const int nt2 = ff.ntypes * ff.ntypes;
   std::vector<FFPair64> f64(nt2);

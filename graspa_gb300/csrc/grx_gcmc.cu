@@ -22,6 +22,7 @@
 namespace grx {
 
 enum : uint32_t { SLOT_MOVE = 4096u, SLOT_DISP = 4097u };
+constexpr int kMaxMoved = 4;  // moved components per box in one GCMC run
 
 struct GcmcArgs {
   grx_gcmc_desc d;
@@ -78,32 +79,41 @@ __device__ __forceinline__ void copy_atom(const BoxDev& b, int dst, int src, int
 }
 
 template <int PREC>
+// One block per box. The box's moved components are entries [first[box],
+// first[box + 1]) of args / stats; every step picks one of them uniformly with word 3
+// of the displacement slot (Select_Box_Component_Molecule, axpy.cu:74-100). All
+// entries of a box share its seed and stream.
 __global__ void __launch_bounds__(GRX_THREADS, 2) gcmc_kernel(const BoxDev* boxes, const GcmcArgs* args,
-                                                              uint64_t first_step, int64_t nsteps,
-                                                              grx_gcmc_stats* stats) {
+                                                              const int* first, const uint64_t* step0,
+                                                              int64_t nsteps, grx_gcmc_stats* stats) {
+  const uint64_t first_step = *step0;
   __shared__ BoxDev b;
-  __shared__ GcmcArgs a;
+  __shared__ GcmcArgs A[kMaxMoved];
   __shared__ CbmcWork W;
-  __shared__ grx_gcmc_stats st;
+  __shared__ grx_gcmc_stats ST[kMaxMoved];
   __shared__ int s_accept;
   __shared__ double s_e1[4], s_w1, s_dE[3], s_stored, s_r1[4], s_wr;
   extern __shared__ double2 eik[];
   const int tid = threadIdx.x;
-  if (tid == 0) {
-    b = boxes[blockIdx.x];
-    a = args[blockIdx.x];
-    st = grx_gcmc_stats{};
+  const int e0 = first[blockIdx.x], nm = first[blockIdx.x + 1] - e0;
+  if (tid == 0) b = boxes[blockIdx.x];
+  if (tid < nm) {
+    A[tid] = args[e0 + tid];
+    ST[tid] = grx_gcmc_stats{};
   }
   __syncthreads();
-  const int comp = a.comp, ms = a.ms, chain = ms - 1, off = a.off;
-  const grx_gcmc_desc& d = a.d;
   int* comp_size = const_cast<int*>(b.comp_size);
   for (int64_t step = 0; step < nsteps; ++step) {
     const uint64_t move = first_step + (uint64_t)step;
     uint32_t w[4], w2[4], ws[4];
-    draw4(d.seed, d.stream, move, SLOT_MOVE, w);
-    draw4(d.seed, d.stream, move, SLOT_DISP, w2);
-    draw4(d.seed, d.stream, move, SLOT_SELECT, ws);
+    draw4(A[0].d.seed, A[0].d.stream, move, SLOT_MOVE, w);
+    draw4(A[0].d.seed, A[0].d.stream, move, SLOT_DISP, w2);
+    draw4(A[0].d.seed, A[0].d.stream, move, SLOT_SELECT, ws);
+    const int sel = nm > 1 ? min(nm - 1, (int)(u01(w2[3]) * (double)nm)) : 0;
+    const GcmcArgs& a = A[sel];
+    const grx_gcmc_desc& d = a.d;
+    grx_gcmc_stats& st = ST[sel];
+    const int comp = a.comp, ms = a.ms, chain = ms - 1, off = a.off;
     const int N = comp_size[comp] / ms;
     const int mol = (int)(u01(w[0]) * (double)N);
     const double r = u01(w[1]);
@@ -363,14 +373,23 @@ __global__ void __launch_bounds__(GRX_THREADS, 2) gcmc_kernel(const BoxDev* boxe
       }
     }
     __syncthreads();
-    if (tid == 0) st.sum_n += (double)(comp_size[comp] / ms);
+    if (tid < nm) ST[tid].sum_n += (double)(comp_size[A[tid].comp] / A[tid].ms);
     __syncthreads();
   }
-  if (tid == 0) {
-    st.n_molecules = comp_size[comp] / ms;
-    stats[blockIdx.x] = st;
+  if (tid < nm) {  // accumulate into the caller's running statistics
+    grx_gcmc_stats& o = stats[e0 + tid];
+    for (int k = 0; k < 5; ++k) {
+      o.attempts[k] += ST[tid].attempts[k];
+      o.accepted[k] += ST[tid].accepted[k];
+    }
+    for (int k = 0; k < 4; ++k) o.energy[k] += ST[tid].energy[k];
+    o.capacity_hits += ST[tid].capacity_hits;
+    o.sum_n += ST[tid].sum_n;
+    o.n_molecules = comp_size[A[tid].comp] / A[tid].ms;
   }
 }
+
+__global__ void advance_step_kernel(uint64_t* step, int64_t nsteps) { *step += (uint64_t)nsteps; }
 
 __global__ void ewald_df_refresh_gcmc(BoxDev b) {
   float4* ewA = const_cast<float4*>(b.ewA);
@@ -388,101 +407,367 @@ __global__ void ewald_df_refresh_gcmc(BoxDev b) {
   }
 }
 
-template <int PREC>
-static grx_status launch_gcmc(grx_box* b0, int nboxes, const BoxDev* dboxes, const GcmcArgs* dargs,
-                              uint64_t first_step, int64_t nsteps, grx_gcmc_stats* dstats, size_t smem) {
-  GRX_CHECK_CUDA(cudaFuncSetAttribute(gcmc_kernel<PREC>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024),
+}  // namespace grx
+
+using namespace grx;
+
+// A prepared persistent GCMC launch over a set of boxes (see grx.h). The per-box
+// state descriptors, the move sets, the step counter and the running statistics
+// live in one device allocation owned by the batch.
+struct grx_gcmc_batch {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  grx_precision prec = GRX_MIXED;
+  std::vector<grx_box*> boxes;
+  std::vector<grx_gcmc_desc> descs;
+  std::vector<int> first;
+  int nentries = 0;
+  size_t smem = 0;
+  int chunk_mult = 4;
+  void* mem = nullptr;
+  BoxDev* d_boxes = nullptr;
+  GcmcArgs* d_args = nullptr;
+  int* d_first = nullptr;
+  grx_gcmc_stats* d_stats = nullptr;
+  uint64_t* d_step = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int64_t graph_nsteps = 0;
+  int graph_nlaunch = 0;
+  cudaStream_t graph_stream = nullptr;
+};
+
+namespace grx {
+
+// Validates the boxes and move sets and fills the per-box state and per-entry args.
+static grx_status prepare_gcmc(grx_box* const* boxes, int32_t nboxes, const grx_gcmc_desc* descs,
+                               const int32_t* ncomp_moved, std::vector<BoxDev>& hb, std::vector<GcmcArgs>& ha,
+                               std::vector<int>& first, size_t& smem, int chunk_mult) {
+  GRX_REQUIRE(boxes && descs && nboxes >= 1, "grx_gcmc: bad argument");
+  hb.assign(nboxes, BoxDev{});
+  ha.clear();
+  first.assign(nboxes + 1, 0);
+  smem = 0;
+  int e = 0;
+  for (int i = 0; i < nboxes; ++i) {
+    grx_box* b = boxes[i];
+    GRX_REQUIRE(b, "grx_gcmc: null box");
+    GRX_REQUIRE(b->device == boxes[0]->device, "grx_gcmc: boxes live on different devices");
+    for (int j = 0; j < i; ++j) GRX_REQUIRE(boxes[j] != b, "grx_gcmc: a box appears twice");
+    const int nm = ncomp_moved ? ncomp_moved[i] : 1;
+    GRX_REQUIRE(nm >= 1 && nm <= kMaxMoved, "grx_gcmc: 1..4 moved components per box");
+    first[i] = e;
+    refresh_dev(b);
+    b->dev.chunk_mult = chunk_mult;
+    for (int k = 0; k < nm; ++k, ++e) {
+      const grx_gcmc_desc& d = descs[e];
+      GRX_REQUIRE(d.component >= b->nhost && d.component < b->ncomp,
+                  "grx_gcmc: component must be an adsorbate component");
+      for (int j = first[i]; j < e; ++j)
+        GRX_REQUIRE(descs[j].component != d.component, "grx_gcmc: a component is listed twice for one box");
+      GRX_REQUIRE(d.seed == descs[first[i]].seed && d.stream == descs[first[i]].stream,
+                  "grx_gcmc: the entries of one box must share seed and stream");
+      const int ms = (int)b->molsize[d.component];
+      GRX_REQUIRE(ms >= 1 && ms <= kMolWork, "grx_gcmc: molecule size must be 1..32");
+      GRX_REQUIRE(b->stored[d.component] >= (size_t)ms,
+                  "grx_gcmc: the component stores no molecule template (set it with n_stored >= molsize)");
+      GRX_REQUIRE(d.ntrials >= 1 && d.ntrials <= kMaxTrials, "grx_gcmc: ntrials out of range (1..64)");
+      GRX_REQUIRE(ms == 1 || (d.norient >= 1 && d.norient <= kMaxTrials &&
+                              d.norient * (ms - 1) <= GRX_MAX_TRIAL_BEADS),
+                  "grx_gcmc: norient out of range");
+      GRX_REQUIRE(d.beta > 0 && d.pressure > 0 && d.ideal_rosenbluth > 0, "grx_gcmc: bad thermodynamic state");
+      GcmcArgs a{};
+      a.d = d;
+      a.comp = d.component;
+      a.ms = ms;
+      a.off = (int)b->off[d.component];
+      a.cap = (int)b->cap[d.component];
+      a.rigid = b->rigid[d.component];
+      a.charged = (!b->dev.no_charges && b->has_charge[d.component] && b->nact > 0) ? 1 : 0;
+      a.bias = b->dev.vdw_real_bias;
+      a.excl = b->excl_intra[d.component] + b->excl_self[d.component];
+      a.big_p = d.mol_fraction * d.pressure * d.fugacity_coeff * b->dev.volume;
+      ha.push_back(a);
+      const size_t need = (size_t)(b->dev.kmax[0] + b->dev.kmax[1] + b->dev.kmax[2] + 3) * 2 * ms *
+                          (sizeof(double2) + sizeof(float4));
+      smem = std::max(smem, need);
+    }
+    if (!b->ewdf_valid && b->nact > 0) {
+      ewald_df_refresh_gcmc<<<std::max(1, std::min((b->nact + 255) / 256, sm_count(b))), 256, 0,
+                              boxes[0]->stream>>>(b->dev);
+      count_launch();
+      b->ewdf_valid = true;
+    }
+    hb[i] = b->dev;
+  }
+  first[nboxes] = e;
+  GRX_REQUIRE(smem <= 64 * 1024, "grx_gcmc: Ewald tables exceed the shared-memory budget");
+  return GRX_OK;
+}
+
+static grx_status set_gcmc_smem() {
+  GRX_CHECK_CUDA(cudaFuncSetAttribute(gcmc_kernel<GRX_FP64>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024),
                  "gcmc shared memory attribute");
-  gcmc_kernel<PREC><<<nboxes, GRX_THREADS, smem, b0->stream>>>(dboxes, dargs, first_step, nsteps, dstats);
+  GRX_CHECK_CUDA(cudaFuncSetAttribute(gcmc_kernel<GRX_MIXED>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024),
+                 "gcmc shared memory attribute");
+  GRX_CHECK_CUDA(cudaFuncSetAttribute(gcmc_kernel<GRX_FP32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024),
+                 "gcmc shared memory attribute");
+  return GRX_OK;
+}
+
+// Enqueues one persistent launch and the step-counter advance (no host sync).
+static grx_status enqueue_gcmc(grx_precision prec, int nboxes, const BoxDev* dboxes, const GcmcArgs* dargs,
+                               const int* dfirst, uint64_t* dstep, int64_t nsteps, grx_gcmc_stats* dstats,
+                               size_t smem, cudaStream_t stream) {
+  if (prec == GRX_FP64)
+    gcmc_kernel<GRX_FP64><<<nboxes, GRX_THREADS, smem, stream>>>(dboxes, dargs, dfirst, dstep, nsteps, dstats);
+  else if (prec == GRX_MIXED)
+    gcmc_kernel<GRX_MIXED><<<nboxes, GRX_THREADS, smem, stream>>>(dboxes, dargs, dfirst, dstep, nsteps, dstats);
+  else
+    gcmc_kernel<GRX_FP32><<<nboxes, GRX_THREADS, smem, stream>>>(dboxes, dargs, dfirst, dstep, nsteps, dstats);
+  advance_step_kernel<<<1, 1, 0, stream>>>(dstep, nsteps);
+  count_launch();
   count_launch();
   GRX_CHECK_CUDA(cudaGetLastError(), "gcmc launch");
   return GRX_OK;
 }
 
-}  // namespace grx
-
-using namespace grx;
-
-extern "C" grx_status grx_gcmc_run(grx_box* const* boxes, int32_t nboxes, const grx_gcmc_desc* descs,
-                                   uint64_t first_step, int64_t nsteps, grx_precision prec,
-                                   grx_gcmc_stats* stats) {
-  GRX_REQUIRE(boxes && descs && stats && nboxes >= 1, "grx_gcmc_run: bad argument");
-  GRX_REQUIRE(prec == GRX_FP64 || prec == GRX_MIXED || prec == GRX_FP32, "grx_gcmc_run: bad precision");
-  GRX_REQUIRE(nsteps >= 0, "grx_gcmc_run: negative step count");
-  std::vector<BoxDev> hb(nboxes);
-  std::vector<GcmcArgs> ha(nboxes);
-  size_t smem = 0;
-  for (int i = 0; i < nboxes; ++i) {
-    grx_box* b = boxes[i];
-    const grx_gcmc_desc& d = descs[i];
-    GRX_REQUIRE(b, "grx_gcmc_run: null box");
-    GRX_REQUIRE(b->device == boxes[0]->device, "grx_gcmc_run: boxes live on different devices");
-    for (int j = 0; j < i; ++j) GRX_REQUIRE(boxes[j] != b, "grx_gcmc_run: a box appears twice");
-    GRX_REQUIRE(d.component >= b->nhost && d.component < b->ncomp,
-                "grx_gcmc_run: component must be an adsorbate component");
-    const int ms = (int)b->molsize[d.component];
-    GRX_REQUIRE(ms >= 1 && ms <= kMolWork, "grx_gcmc_run: molecule size must be 1..32");
-    GRX_REQUIRE(b->stored[d.component] >= (size_t)ms,
-                "grx_gcmc_run: the component stores no molecule template (set it with n_stored >= molsize)");
-    GRX_REQUIRE(d.ntrials >= 1 && d.ntrials <= kMaxTrials, "grx_gcmc_run: ntrials out of range (1..64)");
-    GRX_REQUIRE(ms == 1 || (d.norient >= 1 && d.norient <= kMaxTrials && d.norient * (ms - 1) <= GRX_MAX_TRIAL_BEADS),
-                "grx_gcmc_run: norient out of range");
-    GRX_REQUIRE(d.beta > 0 && d.pressure > 0 && d.ideal_rosenbluth > 0, "grx_gcmc_run: bad thermodynamic state");
-    refresh_dev(b);
-    if (!b->ewdf_valid && b->nact > 0) {
-      ewald_df_refresh_gcmc<<<std::max(1, std::min((b->nact + 255) / 256, sm_count(b))), 256, 0, boxes[0]->stream>>>(
-          b->dev);
-      count_launch();
-      b->ewdf_valid = true;
-    }
-    hb[i] = b->dev;
-    GcmcArgs& a = ha[i];
-    a.d = d;
-    a.comp = d.component;
-    a.ms = ms;
-    a.off = (int)b->off[d.component];
-    a.cap = (int)b->cap[d.component];
-    a.rigid = b->rigid[d.component];
-    a.charged = (!b->dev.no_charges && b->has_charge[d.component] && b->nact > 0) ? 1 : 0;
-    a.bias = b->dev.vdw_real_bias;
-    a.excl = b->excl_intra[d.component] + b->excl_self[d.component];
-    a.big_p = d.mol_fraction * d.pressure * d.fugacity_coeff * b->dev.volume;
-    const size_t need = (size_t)(b->dev.kmax[0] + b->dev.kmax[1] + b->dev.kmax[2] + 3) * 2 * ms *
-                        (sizeof(double2) + sizeof(float4));
-    smem = std::max(smem, need);
-  }
-  GRX_REQUIRE(smem <= 64 * 1024, "grx_gcmc_run: Ewald tables exceed the shared-memory budget");
-  grx_box* b0 = boxes[0];
-  const size_t bbytes = (nboxes * sizeof(BoxDev) + 255) / 256 * 256;
-  const size_t abytes = (nboxes * sizeof(GcmcArgs) + 255) / 256 * 256;
-  grx_status st = ensure_scratch(b0, bbytes + abytes + nboxes * sizeof(grx_gcmc_stats));
-  if (st) return st;
-  BoxDev* dboxes = (BoxDev*)b0->scratch;
-  GcmcArgs* dargs = (GcmcArgs*)((char*)b0->scratch + bbytes);
-  grx_gcmc_stats* dstats = (grx_gcmc_stats*)((char*)b0->scratch + bbytes + abytes);
-  GRX_CHECK_CUDA(cudaMemcpyAsync(dboxes, hb.data(), nboxes * sizeof(BoxDev), cudaMemcpyHostToDevice, b0->stream),
-                 "upload boxes");
-  GRX_CHECK_CUDA(cudaMemcpyAsync(dargs, ha.data(), nboxes * sizeof(GcmcArgs), cudaMemcpyHostToDevice, b0->stream),
-                 "upload gcmc args");
-  if (nsteps > 0) {
-    if (prec == GRX_FP64) st = launch_gcmc<GRX_FP64>(b0, nboxes, dboxes, dargs, first_step, nsteps, dstats, smem);
-    else if (prec == GRX_MIXED) st = launch_gcmc<GRX_MIXED>(b0, nboxes, dboxes, dargs, first_step, nsteps, dstats, smem);
-    else st = launch_gcmc<GRX_FP32>(b0, nboxes, dboxes, dargs, first_step, nsteps, dstats, smem);
-    if (st) return st;
-    GRX_CHECK_CUDA(cudaMemcpyAsync(stats, dstats, nboxes * sizeof(grx_gcmc_stats), cudaMemcpyDefault, b0->stream),
-                   "read gcmc stats");
-  } else {
-    for (int i = 0; i < nboxes; ++i) stats[i] = grx_gcmc_stats{};
-  }
-  GRX_CHECK_CUDA(cudaStreamSynchronize(b0->stream), "gcmc run");
+static grx_status sync_sizes(grx_box* const* boxes, int nboxes, const grx_gcmc_desc* descs, const int* first) {
   for (int i = 0; i < nboxes; ++i) {
     grx_box* b = boxes[i];
     GRX_CHECK_CUDA(cudaMemcpy(b->size, b->d_size, GRX_MAX_COMPONENTS * sizeof(int), cudaMemcpyDeviceToHost),
                    "read sizes");
-    const int c = descs[i].component;
-    b->stored[c] = std::max(b->stored[c], (size_t)b->size[c]);
-    if (nsteps == 0) stats[i].n_molecules = b->size[descs[i].component] / (int)b->molsize[descs[i].component];
+    for (int e = first[i]; e < first[i + 1]; ++e) {
+      const int c = descs[e].component;
+      b->stored[c] = std::max(b->stored[c], (size_t)b->size[c]);
+    }
   }
+  return GRX_OK;
+}
+
+}  // namespace grx
+
+extern "C" grx_status grx_gcmc_run(grx_box* const* boxes, int32_t nboxes, const grx_gcmc_desc* descs,
+                                   const int32_t* ncomp_moved, uint64_t first_step, int64_t nsteps,
+                                   grx_precision prec, grx_gcmc_stats* stats) {
+  GRX_REQUIRE(boxes && descs && stats && nboxes >= 1, "grx_gcmc_run: bad argument");
+  GRX_REQUIRE(prec == GRX_FP64 || prec == GRX_MIXED || prec == GRX_FP32, "grx_gcmc_run: bad precision");
+  GRX_REQUIRE(nsteps >= 0, "grx_gcmc_run: negative step count");
+  std::vector<BoxDev> hb;
+  std::vector<GcmcArgs> ha;
+  std::vector<int> first;
+  size_t smem = 0;
+  grx_status st = prepare_gcmc(boxes, nboxes, descs, ncomp_moved, hb, ha, first, smem, boxes[0]->dev.chunk_mult);
+  if (st) return st;
+  const int ne = first[nboxes];
+  grx_box* b0 = boxes[0];
+  auto al = [](size_t n) { return (n + 255) / 256 * 256; };
+  const size_t ob = 0, oa = al(nboxes * sizeof(BoxDev)), of = oa + al(ne * sizeof(GcmcArgs)),
+               os = of + al((nboxes + 1) * sizeof(int)), ot = os + al(ne * sizeof(grx_gcmc_stats));
+  st = ensure_scratch(b0, ot + 256);
+  if (st) return st;
+  char* base = (char*)b0->scratch;
+  BoxDev* dboxes = (BoxDev*)(base + ob);
+  GcmcArgs* dargs = (GcmcArgs*)(base + oa);
+  int* dfirst = (int*)(base + of);
+  grx_gcmc_stats* dstats = (grx_gcmc_stats*)(base + os);
+  uint64_t* dstep = (uint64_t*)(base + ot);
+  GRX_CHECK_CUDA(cudaMemcpyAsync(dboxes, hb.data(), nboxes * sizeof(BoxDev), cudaMemcpyHostToDevice, b0->stream),
+                 "upload boxes");
+  GRX_CHECK_CUDA(cudaMemcpyAsync(dargs, ha.data(), ne * sizeof(GcmcArgs), cudaMemcpyHostToDevice, b0->stream),
+                 "upload gcmc args");
+  GRX_CHECK_CUDA(cudaMemcpyAsync(dfirst, first.data(), (nboxes + 1) * sizeof(int), cudaMemcpyHostToDevice,
+                                 b0->stream),
+                 "upload entry offsets");
+  GRX_CHECK_CUDA(cudaMemcpyAsync(dstep, &first_step, sizeof(uint64_t), cudaMemcpyHostToDevice, b0->stream),
+                 "upload step");
+  GRX_CHECK_CUDA(cudaMemsetAsync(dstats, 0, ne * sizeof(grx_gcmc_stats), b0->stream), "clear stats");
+  if (nsteps > 0) {
+    st = set_gcmc_smem();
+    if (st) return st;
+    st = enqueue_gcmc(prec, nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem, b0->stream);
+    if (st) return st;
+  }
+  GRX_CHECK_CUDA(cudaMemcpyAsync(stats, dstats, ne * sizeof(grx_gcmc_stats), cudaMemcpyDefault, b0->stream),
+                 "read gcmc stats");
+  GRX_CHECK_CUDA(cudaStreamSynchronize(b0->stream), "gcmc run");
+  st = sync_sizes(boxes, nboxes, descs, first.data());
+  if (st) return st;
+  if (nsteps == 0)
+    for (int i = 0; i < nboxes; ++i)
+      for (int e = first[i]; e < first[i + 1]; ++e)
+        stats[e].n_molecules = boxes[i]->size[descs[e].component] / (int)boxes[i]->molsize[descs[e].component];
+  return GRX_OK;
+}
+
+extern "C" grx_status grx_gcmc_batch_create(grx_box* const* boxes, int32_t nboxes, const grx_gcmc_desc* descs,
+                                            const int32_t* ncomp_moved, grx_precision prec,
+                                            grx_gcmc_batch** out) {
+  GRX_REQUIRE(out, "grx_gcmc_batch_create: null output");
+  GRX_REQUIRE(prec == GRX_FP64 || prec == GRX_MIXED || prec == GRX_FP32, "grx_gcmc_batch_create: bad precision");
+  *out = nullptr;
+  auto* B = new grx_gcmc_batch();
+  B->prec = prec;
+  std::vector<BoxDev> hb;
+  std::vector<GcmcArgs> ha;
+  grx_status st = prepare_gcmc(boxes, nboxes, descs, ncomp_moved, hb, ha, B->first, B->smem, B->chunk_mult);
+  if (st) { delete B; return st; }
+  B->nentries = B->first[nboxes];
+  B->boxes.assign(boxes, boxes + nboxes);
+  B->descs.assign(descs, descs + B->nentries);
+  B->device = boxes[0]->device;
+  B->stream = boxes[0]->stream;
+  auto al = [](size_t n) { return (n + 255) / 256 * 256; };
+  const size_t oa = al(nboxes * sizeof(BoxDev)), of = oa + al(B->nentries * sizeof(GcmcArgs)),
+               os = of + al((nboxes + 1) * sizeof(int)), ot = os + al(B->nentries * sizeof(grx_gcmc_stats));
+  if (cudaMalloc(&B->mem, ot + 256) != cudaSuccess) {
+    delete B;
+    set_error("grx_gcmc_batch_create: out of device memory");
+    return GRX_ERR_OUT_OF_MEMORY;
+  }
+  char* base = (char*)B->mem;
+  B->d_boxes = (BoxDev*)base;
+  B->d_args = (GcmcArgs*)(base + oa);
+  B->d_first = (int*)(base + of);
+  B->d_stats = (grx_gcmc_stats*)(base + os);
+  B->d_step = (uint64_t*)(base + ot);
+  const uint64_t zero = 0;
+  bool ok = cudaMemcpy(B->d_boxes, hb.data(), nboxes * sizeof(BoxDev), cudaMemcpyHostToDevice) == cudaSuccess &&
+            cudaMemcpy(B->d_args, ha.data(), B->nentries * sizeof(GcmcArgs), cudaMemcpyHostToDevice) == cudaSuccess &&
+            cudaMemcpy(B->d_first, B->first.data(), (nboxes + 1) * sizeof(int), cudaMemcpyHostToDevice) ==
+                cudaSuccess &&
+            cudaMemset(B->d_stats, 0, B->nentries * sizeof(grx_gcmc_stats)) == cudaSuccess &&
+            cudaMemcpy(B->d_step, &zero, sizeof(uint64_t), cudaMemcpyHostToDevice) == cudaSuccess;
+  st = set_gcmc_smem();
+  if (!ok || st) {
+    cudaFree(B->mem);
+    delete B;
+    set_error("grx_gcmc_batch_create: device set-up failed");
+    return GRX_ERR_CUDA;
+  }
+  *out = B;
+  return GRX_OK;
+}
+
+static void drop_graph(grx_gcmc_batch* B) {
+  if (B->exec) cudaGraphExecDestroy(B->exec);
+  if (B->graph) cudaGraphDestroy(B->graph);
+  B->exec = nullptr;
+  B->graph = nullptr;
+}
+
+extern "C" grx_status grx_gcmc_batch_destroy(grx_gcmc_batch* B) {
+  if (!B) return GRX_OK;
+  drop_graph(B);
+  if (B->mem) cudaFree(B->mem);
+  delete B;
+  return GRX_OK;
+}
+
+extern "C" grx_status grx_gcmc_batch_set_step(grx_gcmc_batch* B, uint64_t step) {
+  GRX_REQUIRE(B, "grx_gcmc_batch_set_step: null batch");
+  GRX_CHECK_CUDA(cudaMemcpyAsync(B->d_step, &step, sizeof(uint64_t), cudaMemcpyHostToDevice, B->stream),
+                 "set step");
+  GRX_CHECK_CUDA(cudaStreamSynchronize(B->stream), "set step");
+  return GRX_OK;
+}
+
+extern "C" grx_status grx_gcmc_batch_launch(grx_gcmc_batch* B, int64_t nsteps, void* stream) {
+  GRX_REQUIRE(B && nsteps >= 0, "grx_gcmc_batch_launch: bad argument");
+  cudaStream_t s = stream ? (cudaStream_t)stream : B->stream;
+  if (nsteps == 0) return GRX_OK;
+  return enqueue_gcmc(B->prec, (int)B->boxes.size(), B->d_boxes, B->d_args, B->d_first, B->d_step, nsteps,
+                      B->d_stats, B->smem, s);
+}
+
+extern "C" grx_status grx_gcmc_batch_run_graph(grx_gcmc_batch* B, int64_t nsteps, int32_t nlaunch, void* stream) {
+  GRX_REQUIRE(B && nsteps >= 1 && nlaunch >= 1, "grx_gcmc_batch_run_graph: bad argument");
+  cudaStream_t s = stream ? (cudaStream_t)stream : B->stream;
+  if (!B->exec || B->graph_nsteps != nsteps || B->graph_nlaunch != nlaunch) {
+    drop_graph(B);
+    cudaStream_t cap = nullptr;
+    GRX_CHECK_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), "capture stream");
+    GRX_CHECK_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal), "begin capture");
+    grx_status st = GRX_OK;
+    for (int k = 0; k < nlaunch && st == GRX_OK; ++k)
+      st = enqueue_gcmc(B->prec, (int)B->boxes.size(), B->d_boxes, B->d_args, B->d_first, B->d_step, nsteps,
+                        B->d_stats, B->smem, cap);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(cap, &g);
+    cudaStreamDestroy(cap);
+    if (st) {
+      if (g) cudaGraphDestroy(g);
+      return st;
+    }
+    GRX_CHECK_CUDA(ec, "end capture");
+    B->graph = g;
+    GRX_CHECK_CUDA(cudaGraphInstantiate(&B->exec, g, 0), "instantiate graph");
+    B->graph_nsteps = nsteps;
+    B->graph_nlaunch = nlaunch;
+  }
+  GRX_CHECK_CUDA(cudaGraphLaunch(B->exec, s), "graph launch");
+  return GRX_OK;
+}
+
+extern "C" grx_status grx_gcmc_batch_stats(grx_gcmc_batch* B, grx_gcmc_stats* stats, uint64_t* next_step) {
+  GRX_REQUIRE(B, "grx_gcmc_batch_stats: null batch");
+  GRX_CHECK_CUDA(cudaDeviceSynchronize(), "gcmc batch sync");
+  if (stats)
+    GRX_CHECK_CUDA(cudaMemcpy(stats, B->d_stats, B->nentries * sizeof(grx_gcmc_stats), cudaMemcpyDeviceToHost),
+                   "read stats");
+  if (next_step)
+    GRX_CHECK_CUDA(cudaMemcpy(next_step, B->d_step, sizeof(uint64_t), cudaMemcpyDeviceToHost), "read step");
+  return sync_sizes(B->boxes.data(), (int)B->boxes.size(), B->descs.data(), B->first.data());
+}
+
+extern "C" grx_status grx_gcmc_batch_reset_stats(grx_gcmc_batch* B) {
+  GRX_REQUIRE(B, "grx_gcmc_batch_reset_stats: null batch");
+  GRX_CHECK_CUDA(cudaMemsetAsync(B->d_stats, 0, B->nentries * sizeof(grx_gcmc_stats), B->stream), "clear stats");
+  GRX_CHECK_CUDA(cudaStreamSynchronize(B->stream), "clear stats");
+  return GRX_OK;
+}
+
+// Autotuner: times nsteps real steps of every box for each candidate work split
+// (items per warp per bead pass) with CUDA events and keeps the fastest. The probe
+// steps are ordinary Monte Carlo steps: the chains advance by ncand * nsteps.
+extern "C" grx_status grx_gcmc_batch_autotune(grx_gcmc_batch* B, int64_t nsteps, int32_t* chosen,
+                                              float* ms_per_candidate) {
+  GRX_REQUIRE(B && nsteps >= 1, "grx_gcmc_batch_autotune: bad argument");
+  static const int cand[4] = {1, 2, 4, 8};
+  const int nb = (int)B->boxes.size();
+  std::vector<BoxDev> hb(nb);
+  cudaEvent_t e0, e1;
+  GRX_CHECK_CUDA(cudaEventCreate(&e0), "event");
+  GRX_CHECK_CUDA(cudaEventCreate(&e1), "event");
+  float best = 1e30f;
+  int best_m = B->chunk_mult;
+  for (int c = 0; c < 4; ++c) {
+    for (int i = 0; i < nb; ++i) {
+      hb[i] = B->boxes[i]->dev;
+      hb[i].chunk_mult = cand[c];
+    }
+    GRX_CHECK_CUDA(cudaMemcpy(B->d_boxes, hb.data(), nb * sizeof(BoxDev), cudaMemcpyHostToDevice), "tune upload");
+    GRX_CHECK_CUDA(cudaEventRecord(e0, B->stream), "event");
+    grx_status st = enqueue_gcmc(B->prec, nb, B->d_boxes, B->d_args, B->d_first, B->d_step, nsteps, B->d_stats,
+                                 B->smem, B->stream);
+    if (st) return st;
+    GRX_CHECK_CUDA(cudaEventRecord(e1, B->stream), "event");
+    GRX_CHECK_CUDA(cudaEventSynchronize(e1), "event");
+    float ms = 0.f;
+    GRX_CHECK_CUDA(cudaEventElapsedTime(&ms, e0, e1), "event");
+    if (ms_per_candidate) ms_per_candidate[c] = ms;
+    if (ms < best) { best = ms; best_m = cand[c]; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  B->chunk_mult = best_m;
+  for (int i = 0; i < nb; ++i) {
+    B->boxes[i]->dev.chunk_mult = best_m;
+    hb[i] = B->boxes[i]->dev;
+  }
+  GRX_CHECK_CUDA(cudaMemcpy(B->d_boxes, hb.data(), nb * sizeof(BoxDev), cudaMemcpyHostToDevice), "tune upload");
+  drop_graph(B);
+  if (chosen) *chosen = best_m;
   return GRX_OK;
 }
 

@@ -68,9 +68,12 @@ struct BoxDev {
   const float4* tile_c;  // bounding sphere {x, y, z, radius}
   const int4* tile_r;    // {first atom, end atom, component, 0}
   int ntiles;
-  int cull;              // tile culling on (orthorhombic cells only)
+  int cull;              // tile culling on
   float cull_r;          // screening radius used by the tile test
   float cellf[9];
+  int chunk_mult;        // work items per warp and bead pass (tile-range chunking; autotuned)
+  float wperp[3];        // perpendicular widths of the cell (distances between lattice planes)
+  float half_wmin2;      // (min width / 2)^2, shrunk for FP32 rounding
   // real-space Coulomb table: g(s) = erfc(alpha sqrt s)/sqrt s, piecewise quintic in
   // s = r^2, 64 pieces per octave indexed by the FP32 bit pattern of s
   const double* ctab;    // per piece {s0, 1/width, c0..c5}

@@ -207,25 +207,47 @@ __device__ __forceinline__ void warp_item(const BoxDev& b, const Bead& bd, int t
   LaneAcc<PREC>& la = hacc;
   // Tiles are tested 32 at a time, one per lane; survivors are then screened one
   // tile at a time by the whole warp. When a tile lies inside one periodic image of
-  // the bead (orthorhombic cells, stored positions unwrapped-compact), the image shift
-  // is applied once to the bead instead of once per atom.
+  // the bead (stored positions compact, the tile sphere clear of the rounding
+  // boundaries), the image shift is applied once to the bead instead of per atom.
   for (int base = t0; base < t1; base += 32) {
     const int tl = base + lane;
     bool pass = tl < t1;
-    float nx = 0.f, ny = 0.f, nz = 0.f;
+    float sx = 0.f, sy = 0.f, sz = 0.f;  // image shift of the bead for this tile
     bool one_image = false;
     if (pass && b.cull) {
       const float4 tc = b.tile_c[tl];
       float dx = tc.x - bx, dy = tc.y - by, dz = tc.z - bz;
-      nx = rnd(dx * b.invf[0]); ny = rnd(dy * b.invf[4]); nz = rnd(dz * b.invf[8]);
-      dx = __fmaf_rn(-nx, b.cellf[0], dx);
-      dy = __fmaf_rn(-ny, b.cellf[4], dy);
-      dz = __fmaf_rn(-nz, b.cellf[8], dz);
       const float lim = b.cull_r + tc.w;
-      pass = dx * dx + dy * dy + dz * dz <= lim * lim;
       const float m = tc.w + 1e-2f;
-      one_image = b.tile_r[tl].w != 0 && fabsf(dx) + m < 0.5f * b.cellf[0] &&
-                  fabsf(dy) + m < 0.5f * b.cellf[4] && fabsf(dz) + m < 0.5f * b.cellf[8];
+      if (b.cubic) {
+        const float nx = rnd(dx * b.invf[0]), ny = rnd(dy * b.invf[4]), nz = rnd(dz * b.invf[8]);
+        dx = __fmaf_rn(-nx, b.cellf[0], dx);
+        dy = __fmaf_rn(-ny, b.cellf[4], dy);
+        dz = __fmaf_rn(-nz, b.cellf[8], dz);
+        pass = dx * dx + dy * dy + dz * dz <= lim * lim;
+        one_image = b.tile_r[tl].w != 0 && fabsf(dx) + m < 0.5f * b.cellf[0] &&
+                    fabsf(dy) + m < 0.5f * b.cellf[4] && fabsf(dz) + m < 0.5f * b.cellf[8];
+        sx = nx * b.cell_hi[0]; sy = ny * b.cell_hi[4]; sz = nz * b.cell_hi[8];
+      } else {
+        const float fx = b.invf[0] * dx + b.invf[3] * dy + b.invf[6] * dz;
+        const float fy = b.invf[1] * dx + b.invf[4] * dy + b.invf[7] * dz;
+        const float fz = b.invf[2] * dx + b.invf[5] * dy + b.invf[8] * dz;
+        const float nx = rnd(fx), ny = rnd(fy), nz = rnd(fz);
+        sx = nx * b.cellf[0] + ny * b.cellf[3] + nz * b.cellf[6];
+        sy = nx * b.cellf[1] + ny * b.cellf[4] + nz * b.cellf[7];
+        sz = nx * b.cellf[2] + ny * b.cellf[5] + nz * b.cellf[8];
+        dx -= sx; dy -= sy; dz -= sz;
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        const float rx = fabsf(fx - nx), ry = fabsf(fy - ny), rz = fabsf(fz - nz);
+        if (d2 <= b.half_wmin2) {
+          pass = d2 <= lim * lim;
+        } else {
+          const float lb = fmaxf(fmaxf(rx * b.wperp[0], ry * b.wperp[1]), rz * b.wperp[2]);
+          pass = lb - 1e-3f <= lim;
+        }
+        one_image = b.tile_r[tl].w != 0 && rx + m / b.wperp[0] < 0.5f - 1e-4f &&
+                    ry + m / b.wperp[1] < 0.5f - 1e-4f && rz + m / b.wperp[2] < 0.5f - 1e-4f;
+      }
     }
     unsigned mask = __ballot_sync(kFull, pass);
     while (mask) {
@@ -233,8 +255,8 @@ __device__ __forceinline__ void warp_item(const BoxDev& b, const Bead& bd, int t
       mask &= mask - 1;
       const int t = base + src;
       const bool oi = __shfl_sync(kFull, one_image, src);
-      const float tnx = __shfl_sync(kFull, nx, src), tny = __shfl_sync(kFull, ny, src),
-                  tnz = __shfl_sync(kFull, nz, src);
+      const float tsx = __shfl_sync(kFull, sx, src), tsy = __shfl_sync(kFull, sy, src),
+                  tsz = __shfl_sync(kFull, sz, src);
       const int4 tr = b.tile_r[t];
       const int i = tr.x + lane;
       bool in = false;
@@ -247,9 +269,9 @@ __device__ __forceinline__ void warp_item(const BoxDev& b, const Bead& bd, int t
         if (!skip) {
           if (PREC != GRX_FP64 && oi) {
             const float4 ah = b.hi[i];
-            const float x = ah.x - __fmaf_rn(tnx, b.cell_hi[0], bd.h.x);
-            const float y = ah.y - __fmaf_rn(tny, b.cell_hi[4], bd.h.y);
-            const float z = ah.z - __fmaf_rn(tnz, b.cell_hi[8], bd.h.z);
+            const float x = ah.x - (bd.h.x + tsx);
+            const float y = ah.y - (bd.h.y + tsy);
+            const float z = ah.z - (bd.h.z + tsz);
             in = x * x + y * y + z * z < b.screen2;
           } else {
             in = pair_screen<PREC>(b, i, bd);
@@ -345,8 +367,8 @@ __device__ __forceinline__ void warp_store(const LaneAcc<PREC>& h, const LaneAcc
 }
 
 // Host-tile chunks per bead so that a pass has at least ~4 items per warp.
-__host__ __device__ __forceinline__ int chunks_for(int nb, int ntiles, int nwarps) {
-  int c = (4 * nwarps + nb - 1) / nb;
+__host__ __device__ __forceinline__ int chunks_for(int nb, int ntiles, int nwarps, int mult = 4) {
+  int c = (mult * nwarps + nb - 1) / nb;
   if (c > ntiles) c = ntiles;
   if (c < 1) c = 1;
   return c;

@@ -110,7 +110,9 @@ EXPORTS = [
     "grx_ewald_total", "grx_ewald_set_structure_factors", "grx_ewald_get_structure_factors",
     "grx_ewald_delta", "grx_ewald_commit", "grx_total_energy", "grx_cbmc_select",
     "grx_widom_insertions", "grx_widom_insertions_async", "grx_launch_count", "grx_trial_energies_noalloc", "grx_gcmc_run",
-    "grx_box_write_molecule", "grx_box_remove_molecule",
+    "grx_box_write_molecule", "grx_box_remove_molecule", "grx_gcmc_batch_create", "grx_gcmc_batch_destroy",
+    "grx_gcmc_batch_set_step", "grx_gcmc_batch_launch", "grx_gcmc_batch_run_graph", "grx_gcmc_batch_stats",
+    "grx_gcmc_batch_reset_stats", "grx_gcmc_batch_autotune",
 ]
 
 _lib = None
@@ -163,8 +165,17 @@ def load(path=LIB_PATH):
                                              P(TrialEnergy), _u8p]
     L.grx_box_write_molecule.argtypes = [C.c_void_p, C.c_int32, C.c_size_t, _dp, _dp, P(C.c_size_t)]
     L.grx_box_remove_molecule.argtypes = [C.c_void_p, C.c_int32, C.c_size_t]
-    L.grx_gcmc_run.argtypes = [P(C.c_void_p), C.c_int32, P(GcmcDesc), C.c_uint64, C.c_int64, C.c_int32,
-                               P(GcmcStats)]
+    L.grx_gcmc_run.argtypes = [P(C.c_void_p), C.c_int32, P(GcmcDesc), P(C.c_int32), C.c_uint64, C.c_int64,
+                               C.c_int32, P(GcmcStats)]
+    L.grx_gcmc_batch_create.argtypes = [P(C.c_void_p), C.c_int32, P(GcmcDesc), P(C.c_int32), C.c_int32,
+                                        P(C.c_void_p)]
+    L.grx_gcmc_batch_destroy.argtypes = [C.c_void_p]
+    L.grx_gcmc_batch_set_step.argtypes = [C.c_void_p, C.c_uint64]
+    L.grx_gcmc_batch_launch.argtypes = [C.c_void_p, C.c_int64, C.c_void_p]
+    L.grx_gcmc_batch_run_graph.argtypes = [C.c_void_p, C.c_int64, C.c_int32, C.c_void_p]
+    L.grx_gcmc_batch_stats.argtypes = [C.c_void_p, P(GcmcStats), P(C.c_uint64)]
+    L.grx_gcmc_batch_reset_stats.argtypes = [C.c_void_p]
+    L.grx_gcmc_batch_autotune.argtypes = [C.c_void_p, C.c_int64, P(C.c_int32), P(C.c_float)]
     _lib = L
     return L
 
@@ -489,16 +500,79 @@ def gcmc_desc(component, ntrials=10, norient=10, p_translation=0.25, p_rotation=
     return d
 
 
-def gcmc_run(boxes, descs, first_step, nsteps, prec=GRX_MIXED):
-    """Run nsteps GCMC moves on every box in one persistent launch; returns one
-    GcmcStats per box."""
+def _moved(descs, ncomp_moved, nboxes):
+    flat = [d for group in descs for d in (group if isinstance(group, (list, tuple)) else [group])]
+    if ncomp_moved is None:
+        ncomp_moved = [len(g) if isinstance(g, (list, tuple)) else 1 for g in descs]
+    assert len(ncomp_moved) == nboxes and sum(ncomp_moved) == len(flat)
+    return flat, (C.c_int32 * nboxes)(*ncomp_moved)
+
+
+def gcmc_run(boxes, descs, first_step, nsteps, prec=GRX_MIXED, ncomp_moved=None):
+    """Run nsteps GCMC moves on every box in one persistent launch. descs: one GcmcDesc
+    per box, or a list of them for a box that moves several components. Returns one
+    GcmcStats per entry (flat, box-major)."""
     L = load()
     n = len(boxes)
+    flat, nm = _moved(descs, ncomp_moved, n)
     hs = (C.c_void_p * n)(*[b.h for b in boxes])
-    ds = (GcmcDesc * n)(*descs)
-    st = (GcmcStats * n)()
-    check(L.grx_gcmc_run(hs, n, ds, first_step, nsteps, prec, st), "grx_gcmc_run")
+    ds = (GcmcDesc * len(flat))(*flat)
+    st = (GcmcStats * len(flat))()
+    check(L.grx_gcmc_run(hs, n, ds, nm, first_step, nsteps, prec, st), "grx_gcmc_run")
     return list(st)
+
+
+class GcmcBatch:
+    """grx_gcmc_batch: a prepared persistent GCMC launch (device step counter,
+    accumulated statistics, CUDA-graph replay, autotuner)."""
+
+    def __init__(self, boxes, descs, prec=GRX_MIXED, ncomp_moved=None):
+        self.L = load()
+        n = len(boxes)
+        self.boxes = boxes
+        flat, nm = _moved(descs, ncomp_moved, n)
+        self.nentries = len(flat)
+        hs = (C.c_void_p * n)(*[b.h for b in boxes])
+        ds = (GcmcDesc * len(flat))(*flat)
+        h = C.c_void_p()
+        check(self.L.grx_gcmc_batch_create(hs, n, ds, nm, prec, C.byref(h)), "grx_gcmc_batch_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.grx_gcmc_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_step(self, step):
+        check(self.L.grx_gcmc_batch_set_step(self.h, step), "grx_gcmc_batch_set_step")
+
+    def launch(self, nsteps, stream=None):
+        check(self.L.grx_gcmc_batch_launch(self.h, nsteps, C.c_void_p(stream or 0)), "grx_gcmc_batch_launch")
+
+    def run_graph(self, nsteps, nlaunch, stream=None):
+        check(self.L.grx_gcmc_batch_run_graph(self.h, nsteps, nlaunch, C.c_void_p(stream or 0)),
+              "grx_gcmc_batch_run_graph")
+
+    def stats(self):
+        st = (GcmcStats * self.nentries)()
+        nxt = C.c_uint64()
+        check(self.L.grx_gcmc_batch_stats(self.h, st, C.byref(nxt)), "grx_gcmc_batch_stats")
+        return list(st), nxt.value
+
+    def reset_stats(self):
+        check(self.L.grx_gcmc_batch_reset_stats(self.h), "grx_gcmc_batch_reset_stats")
+
+    def autotune(self, nsteps):
+        ch = C.c_int32()
+        ms = (C.c_float * 4)()
+        check(self.L.grx_gcmc_batch_autotune(self.h, nsteps, C.byref(ch), ms), "grx_gcmc_batch_autotune")
+        return ch.value, list(ms)
 
 
 def cbmc_select(logw, seed, stream, move, word):

@@ -939,7 +939,7 @@ grx_gcmc_stats RunMoves_Device(Variables& Vars, size_t systemId, size_t comp, in
   d.stream = Vars.Random.Stream;
   grx_gcmc_stats st{};
   grx_box* b = Sims.Box.handle;
-  check(grx_gcmc_run(&b, 1, &d, SC.Step, nsteps, Vars.Precision, &st), "grx_gcmc_run");
+  check(grx_gcmc_run(&b, 1, &d, nullptr, SC.Step, nsteps, Vars.Precision, &st), "grx_gcmc_run");
   SC.Step += (uint64_t)nsteps;
   Sync_Host_Mirror(Vars, systemId, comp);
   return st;

@@ -217,3 +217,83 @@ def place_molecules(system, comp, n, g, min_dist=2.6, max_tries=200000):
     fw_q = system["charge"][: len(fw)]
     _set_atoms(system, fw, fw_type, fw_q, guests)
     return len(new)
+
+
+# ------------------------------------------------------------------ batched CH4 / Xe
+CH4_EPS_K, CH4_SIGMA = 148.0, 3.73
+XE_EPS_K, XE_SIGMA = 221.0, 4.10
+
+
+def _random_cell(g, edge=(10.0, 40.0), angle=(60.0, 120.0)):
+    """Cell edges U[edge], angles U[angle] degrees; redrawn until the metric is valid
+    (positive volume, no near-degenerate cell)."""
+    while True:
+        a, b, c = g.uniform(*edge, 3)
+        al, be, ga = g.uniform(*angle, 3)
+        ca, cb, cg = (math.cos(math.radians(x)) for x in (al, be, ga))
+        v2 = 1 - ca * ca - cb * cb - cg * cg + 2 * ca * cb * cg
+        if v2 > 0.15:
+            return triclinic_cell(a, b, c, al, be, ga)
+
+
+def lj_framework(seed, cutoff=12.0, n_atoms=None, n_types=3, rho_max=0.03):
+    """Seeded LJ-only framework of the batched benchmark: a triclinic cell (edges
+    10-40 A, angles 60-120 deg), N atoms log-uniform in [500, 8000]. The cell is
+    replicated until every perpendicular width exceeds 2 x cutoff (and the density
+    is at most rho_max atoms/A^3). The base cell holds N / replicas atoms on a
+    jittered fractional lattice (random vacancies, +/-0.15 lattice spacing), with
+    n_types types of eps/k U[20, 90] K and sigma U[2.5, 3.5] A.
+    Returns (cell, positions, types, eps_K, sigma)."""
+    g = _rng(seed)
+    base = np.array(_random_cell(g)).reshape(3, 3).T
+    n_target = int(round(math.exp(g.uniform(math.log(500), math.log(8000))))) if n_atoms is None else n_atoms
+    w = perpendicular_widths(base.T.reshape(-1))
+    reps = np.maximum(1, np.ceil(2.0 * cutoff * 1.0001 / w)).astype(int)
+    vol = abs(np.linalg.det(base))
+    while n_target / (vol * reps.prod()) > rho_max:
+        reps[np.argmin(w * reps)] += 1
+    n_base = max(1, int(round(n_target / reps.prod())))
+    # lattice with >= n_base sites, spacing roughly equal along the three widths
+    f = (n_base / (w[0] * w[1] * w[2])) ** (1.0 / 3.0)
+    grid = np.maximum(1, np.ceil(w * f)).astype(int)
+    while grid.prod() < n_base:
+        grid[np.argmin(grid / w)] += 1
+    idx = np.stack(np.meshgrid(*[np.arange(k) for k in grid], indexing="ij"), -1).reshape(-1, 3)
+    idx = idx[g.choice(len(idx), n_base, replace=False)]
+    frac = (idx + 0.5 + g.uniform(-0.15, 0.15, (n_base, 3))) / grid
+    pts = frac @ base.T
+    types = g.integers(0, n_types, n_base)
+    eps_K = g.uniform(20.0, 90.0, n_types)
+    sig = g.uniform(2.5, 3.5, n_types)
+    shifts = np.stack(np.meshgrid(*[np.arange(k) for k in reps], indexing="ij"), -1).reshape(-1, 3)
+    allp = (pts[None, :, :] + (shifts @ base.T)[:, None, :]).reshape(-1, 3)
+    allt = np.tile(types, len(shifts))
+    cell = base * reps[None, :]
+    return cell.T.reshape(-1).tolist(), allp, allt, list(eps_K), list(sig)
+
+
+def ch4_xe_system(seed, cutoff=12.0, n_atoms=None, n_ch4=0, n_xe=0):
+    """One box of the batched CH4 / Xe benchmark on lj_framework(seed): united-atom
+    CH4 (148 K, 3.73 A) and Xe (221 K, 4.10 A), no charges, Lorentz-Berthelot mixing
+    shifted at the cutoff. Components: 0 framework, 1 CH4, 2 Xe (one bead each)."""
+    cell, fw, ft, eps_fw, sig_fw = lj_framework(seed, cutoff=cutoff, n_atoms=n_atoms)
+    nt = len(eps_fw)
+    eps_K = eps_fw + [CH4_EPS_K, XE_EPS_K]
+    sig = sig_fw + [CH4_SIGMA, XE_SIGMA]
+    eps, sg, shift = mix_lorentz_berthelot(eps_K, sig, [1] * (nt + 2), cutoff)
+    h = np.array(cell).reshape(3, 3).T
+    off = abs(h[0, 1]) + abs(h[0, 2]) + abs(h[1, 2]) + abs(h[1, 0]) + abs(h[2, 0]) + abs(h[2, 1])
+    templates = {1: dict(pos=np.zeros((1, 3)), charge=np.zeros(1), type=np.array([nt])),
+                 2: dict(pos=np.zeros((1, 3)), charge=np.zeros(1), type=np.array([nt + 1]))}
+    system = dict(
+        name=f"ch4_xe_{seed}", cell=cell, kmax=[1, 1, 1], alpha=0.265, use_lammps_ewald=int(off == 0.0),
+        prefactor=COULOMB_PREFACTOR, ntypes=nt + 2, epsilon=eps, sigma=sg, shift=shift, cutoff_vdw=cutoff,
+        cutoff_coul=cutoff, overlap_criteria=1e6, no_charges=1, vdw_real_bias=1, temperature=300.0, nhost=1,
+        molsize=[len(fw), 1, 1], templates=templates)
+    _set_atoms(system, fw, ft, np.zeros(len(fw)), [np.zeros((0, 3)), np.zeros((0, 3))])
+    gg = _rng(seed + 1000003)
+    if n_ch4:
+        place_molecules(system, 1, n_ch4, gg, min_dist=2.8)
+    if n_xe:
+        place_molecules(system, 2, n_xe, gg, min_dist=2.8)
+    return system

@@ -328,12 +328,42 @@ typedef struct {
 
 /* nsteps GCMC moves on each of nboxes independent boxes (Markov chains), all on the
  * device in one persistent launch: one block per box, positions and S(k) resident.
- * Step s of a box uses Philox move index first_step + s on the box's stream.
- * stats[i] receives box i's counts for this call. Requires current structure
- * factors (grx_ewald_total or grx_ewald_set_structure_factors). */
+ * Box i moves ncomp_moved[i] components (1..4; NULL: one each): its entries of descs
+ * (and of stats) are consecutive, box-major, and share one seed and stream; every step
+ * picks one of them uniformly (Select_Box_Component_Molecule, axpy.cu:74-100). Step s
+ * of a box uses Philox move index first_step + s. stats[e] receives entry e's counts
+ * for this call. Requires current structure factors (grx_ewald_total or
+ * grx_ewald_set_structure_factors). */
 grx_status grx_gcmc_run(grx_box* const* boxes, int32_t nboxes, const grx_gcmc_desc* descs,
-                        uint64_t first_step, int64_t nsteps, grx_precision prec,
-                        grx_gcmc_stats* stats);
+                        const int32_t* ncomp_moved, uint64_t first_step, int64_t nsteps,
+                        grx_precision prec, grx_gcmc_stats* stats);
+
+/* A prepared GCMC launch over a fixed set of boxes, for long runs and CUDA graphs:
+ * the per-box state, move sets, the Philox step counter (starting at 0) and running
+ * statistics stay in device memory owned by the batch. Re-create the batch after
+ * changing a box with any other call. */
+typedef struct grx_gcmc_batch grx_gcmc_batch;
+grx_status grx_gcmc_batch_create(grx_box* const* boxes, int32_t nboxes, const grx_gcmc_desc* descs,
+                                 const int32_t* ncomp_moved, grx_precision prec, grx_gcmc_batch** out);
+grx_status grx_gcmc_batch_destroy(grx_gcmc_batch* batch);
+grx_status grx_gcmc_batch_set_step(grx_gcmc_batch* batch, uint64_t step);
+/* Enqueues nsteps steps of every box on `stream` (NULL: the first box's stream) and
+ * advances the device step counter; no host synchronization, so it can be captured
+ * into a CUDA graph. Statistics accumulate on the device. */
+grx_status grx_gcmc_batch_launch(grx_gcmc_batch* batch, int64_t nsteps, void* stream);
+/* nlaunch launches of nsteps steps each, captured once into a CUDA graph (re-captured
+ * when nsteps or nlaunch change) and replayed on `stream`. */
+grx_status grx_gcmc_batch_run_graph(grx_gcmc_batch* batch, int64_t nsteps, int32_t nlaunch, void* stream);
+/* Waits for the device, then copies the accumulated statistics (one per entry) and
+ * the next step index, and refreshes the boxes' molecule counts. */
+grx_status grx_gcmc_batch_stats(grx_gcmc_batch* batch, grx_gcmc_stats* stats, uint64_t* next_step);
+grx_status grx_gcmc_batch_reset_stats(grx_gcmc_batch* batch);
+/* Autotuner of the bead-pass work split (work items per warp: 1, 2, 4, 8): times
+ * nsteps real steps per candidate with CUDA events, keeps the fastest for this batch
+ * and returns it (ms_per_candidate: 4 floats or NULL). The probe steps are ordinary
+ * Monte Carlo steps and advance the chains. */
+grx_status grx_gcmc_batch_autotune(grx_gcmc_batch* batch, int64_t nsteps, int32_t* chosen,
+                                   float* ms_per_candidate);
 
 /* ---- allocation-free trial energies ------------------------------------- */
 /* grx_trial_energies without any device allocation at call time. No counterpart

@@ -971,15 +971,14 @@ Grow cbmc_grow(const ora_box* box, const ora_ff* ff, const ora_atoms* at, int64_
 
 }  // namespace
 
-extern "C" void ora_gcmc_run(const ora_box* box, const ora_ff* ff, double* pos, double* charge, int64_t* type,
-                             int64_t* molid, int64_t ncomp, int64_t nhost, int64_t* comp_size,
-                             const int64_t* comp_off, const int64_t* molsize, const double* mol_pos,
-                             const double* mol_charge, const int64_t* mol_type, double excl_intra,
-                             double excl_self, double* s_fw, double* s_ads, const ora_gcmc* g,
-                             uint64_t first_step, int64_t nsteps, ora_gcmc_stats* st) {
-  // compact working copy: every host component, then the (single, last) adsorbate component
-  const int64_t comp = g->component;
-  const int64_t ms = molsize[comp];
+extern "C" void ora_gcmc_run_mix(const ora_box* box, const ora_ff* ff, double* pos, double* charge,
+                                 int64_t* type, int64_t* molid, int64_t ncomp, int64_t nhost, int64_t* comp_size,
+                                 const int64_t* comp_off, const int64_t* molsize, const double* const* mol_pos_k,
+                                 const double* const* mol_charge_k, const int64_t* const* mol_type_k,
+                                 const double* excl_intra_k, const double* excl_self_k, double* s_fw, double* s_ads,
+                                 const ora_gcmc* gk, int64_t ng, uint64_t first_step, int64_t nsteps,
+                                 ora_gcmc_stats* stk) {
+  // compact working copy of every component
   GState S;
   S.ncomp = ncomp;
   S.nhost = nhost;
@@ -1002,13 +1001,27 @@ extern "C" void ora_gcmc_run(const ora_box* box, const ora_ff* ff, double* pos, 
   // Orientation trials grow from the coordinates stored in the component's first
   // molecule slot (AllData.pos[1+a] - AllData.pos[0], mc_widom.h:262): they follow
   // every write to slot 0 and survive the deletion of its molecule.
-  std::vector<double> slot0(mol_pos, mol_pos + 3 * ms);
-  const double bigP = g->mol_fraction * g->pressure * g->fugacity_coeff * box->volume;
+  std::vector<std::vector<double>> slot0s(ng);
+  for (int64_t k = 0; k < ng; ++k)
+    slot0s[k].assign(mol_pos_k[k], mol_pos_k[k] + 3 * molsize[gk[k].component]);
+  const uint64_t seed = gk[0].seed;
+  const uint32_t stream = gk[0].stream;
   for (int64_t step = 0; step < nsteps; ++step) {
     const uint64_t move = first_step + (uint64_t)step;
     uint32_t w[4], w2[4];
-    ora_draw(g->seed, g->stream, move, 4096u, w);
-    ora_draw(g->seed, g->stream, move, 4097u, w2);
+    ora_draw(seed, stream, move, 4096u, w);
+    ora_draw(seed, stream, move, 4097u, w2);
+    // Select_Box_Component_Molecule (axpy.cu:74-100): one moved component, uniformly
+    const int64_t sel = ng > 1 ? std::min<int64_t>(ng - 1, (int64_t)(u01(w2[3]) * (double)ng)) : 0;
+    const ora_gcmc* g = &gk[sel];
+    ora_gcmc_stats* st = &stk[sel];
+    const int64_t comp = g->component;
+    const int64_t ms = molsize[comp];
+    std::vector<double>& slot0 = slot0s[sel];
+    const double* mol_charge = mol_charge_k[sel];
+    const int64_t* mol_type = mol_type_k[sel];
+    const double excl_intra = excl_intra_k[sel], excl_self = excl_self_k[sel];
+    const double bigP = g->mol_fraction * g->pressure * g->fugacity_coeff * box->volume;
     const int64_t a0 = S.comp_start[comp];
     const int64_t n_atoms = S.comp_start[comp + 1] - a0;
     const int64_t N = n_atoms / ms;
@@ -1192,7 +1205,10 @@ extern "C" void ora_gcmc_run(const ora_box* box, const ora_ff* ff, double* pos, 
         }
       }
     }
-    st->sum_n += (double)((S.comp_start[comp + 1] - S.comp_start[comp]) / ms);
+    for (int64_t k = 0; k < ng; ++k) {
+      const int64_t ck = gk[k].component;
+      stk[k].sum_n += (double)((S.comp_start[ck + 1] - S.comp_start[ck]) / molsize[ck]);
+    }
   }
   // write the state back (component regions from comp_off)
   for (int64_t c = 0; c < ncomp; ++c) {
@@ -1205,5 +1221,15 @@ extern "C" void ora_gcmc_run(const ora_box* box, const ora_ff* ff, double* pos, 
       molid[k] = S.molid[j];
     }
   }
-  st->n_molecules = comp_size[comp] / ms;
+  for (int64_t k = 0; k < ng; ++k) stk[k].n_molecules = comp_size[gk[k].component] / molsize[gk[k].component];
+}
+
+extern "C" void ora_gcmc_run(const ora_box* box, const ora_ff* ff, double* pos, double* charge, int64_t* type,
+                             int64_t* molid, int64_t ncomp, int64_t nhost, int64_t* comp_size,
+                             const int64_t* comp_off, const int64_t* molsize, const double* mol_pos,
+                             const double* mol_charge, const int64_t* mol_type, double excl_intra,
+                             double excl_self, double* s_fw, double* s_ads, const ora_gcmc* g,
+                             uint64_t first_step, int64_t nsteps, ora_gcmc_stats* st) {
+  ora_gcmc_run_mix(box, ff, pos, charge, type, molid, ncomp, nhost, comp_size, comp_off, molsize, &mol_pos,
+                   &mol_charge, &mol_type, &excl_intra, &excl_self, s_fw, s_ads, g, 1, first_step, nsteps, st);
 }

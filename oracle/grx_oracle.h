@@ -206,6 +206,17 @@ void ora_gcmc_run(const ora_box* box, const ora_ff* ff, double* pos, double* cha
                   double* s_fw, double* s_ads, const ora_gcmc* g, uint64_t first_step,
                   int64_t nsteps, ora_gcmc_stats* stats);
 
+/* Mixture form: ng moved components (gk[k], one template / exclusion pair each;
+ * seed and stream from gk[0]); every step picks entry floor(u * ng) with word 3 of
+ * the displacement slot (Select_Box_Component_Molecule, axpy.cu:74-100). stk[k]
+ * receives entry k's counts. */
+void ora_gcmc_run_mix(const ora_box* box, const ora_ff* ff, double* pos, double* charge, int64_t* type,
+                      int64_t* molid, int64_t ncomp, int64_t nhost, int64_t* comp_size, const int64_t* comp_off,
+                      const int64_t* molsize, const double* const* mol_pos_k, const double* const* mol_charge_k,
+                      const int64_t* const* mol_type_k, const double* excl_intra_k, const double* excl_self_k,
+                      double* s_fw, double* s_ads, const ora_gcmc* gk, int64_t ng, uint64_t first_step,
+                      int64_t nsteps, ora_gcmc_stats* stk);
+
 #ifdef __cplusplus
 }
 #endif

@@ -115,6 +115,9 @@ def lib():
         L.ora_gcmc_run.argtypes = [P(OraBox), P(OraFF), _dp, _dp, _i64p, _i64p, C.c_int64, C.c_int64, _i64p, _i64p,
                                    _i64p, _dp, _dp, _i64p, C.c_double, C.c_double, _dp, _dp, P(OraGcmc), C.c_uint64,
                                    C.c_int64, P(OraGcmcStats)]
+        L.ora_gcmc_run_mix.argtypes = [P(OraBox), P(OraFF), _dp, _dp, _i64p, _i64p, C.c_int64, C.c_int64, _i64p,
+                                       _i64p, _i64p, P(_dp), P(_dp), P(_i64p), _dp, _dp, _dp, _dp, P(OraGcmc),
+                                       C.c_int64, C.c_uint64, C.c_int64, P(OraGcmcStats)]
         _lib = L
     return _lib
 
@@ -239,9 +242,11 @@ class OracleSystem:
         return a.value, b.value
 
     def gcmc(self, params, capacity, first_step, nsteps):
-        """Run nsteps GCMC moves (oracle). Returns (stats, system_after, s_ads_after)."""
+        """Run nsteps GCMC moves (oracle). params: one OraGcmc, or a list of them for a
+        mixture (one per moved component). Returns (stats, system_after, s_ads_after),
+        stats a list when params is a list."""
+        plist = list(params) if isinstance(params, (list, tuple)) else [params]
         sysd = self.s
-        comp = params.component
         cs = list(sysd["comp_start"])
         ncomp = len(cs) - 1
         sizes = np.array([cs[c + 1] - cs[c] for c in range(ncomp)], dtype=np.int64)
@@ -263,17 +268,30 @@ class OracleSystem:
             ty[o:o + b - a] = np.asarray(sysd["type"])[a:b]
             mol[o:o + b - a] = np.asarray(sysd["molid"])[a:b]
         ms = np.array(sysd["molsize"], dtype=np.int64)
-        tm = sysd["templates"][comp]
-        a, b = cs[comp], cs[comp + 1]
-        mp = np.ascontiguousarray((P_[a:a + ms[comp]] if b > a else tm["pos"]).reshape(-1), dtype=np.float64)
-        mq = np.ascontiguousarray(tm["charge"], dtype=np.float64)
-        mt = np.ascontiguousarray(tm["type"], dtype=np.int64)
-        intra, self_ = self.rigid_exclusion(mp, mq, np.ones(len(mq)))
+        keep = []
+        mps, mqs, mts, ein, esf = [], [], [], [], []
+        for pr in plist:
+            comp = pr.component
+            tm = sysd["templates"][comp]
+            a, b = cs[comp], cs[comp + 1]
+            mp = np.ascontiguousarray((P_[a:a + ms[comp]] if b > a else tm["pos"]).reshape(-1), dtype=np.float64)
+            mq = np.ascontiguousarray(tm["charge"], dtype=np.float64)
+            mt = np.ascontiguousarray(tm["type"], dtype=np.int64)
+            intra, self_ = self.rigid_exclusion(mp, mq, np.ones(len(mq)))
+            keep += [mp, mq, mt]
+            mps.append(_d(mp))
+            mqs.append(_d(mq))
+            mts.append(_i(mt))
+            ein.append(intra)
+            esf.append(self_)
+        ng = len(plist)
         _, s_fw, s_ads = self.ewald_total(list(ms))
-        st = OraGcmcStats()
-        lib().ora_gcmc_run(C.byref(self.box), C.byref(self.ff), _d(pos), _d(q), _i(ty), _i(mol), ncomp,
-                           sysd["nhost"], _i(sizes), _i(offs), _i(ms), _d(mp), _d(mq), _i(mt), intra, self_,
-                           _d(s_fw), _d(s_ads), C.byref(params), first_step, nsteps, C.byref(st))
+        st = (OraGcmcStats * ng)()
+        gk = (OraGcmc * ng)(*plist)
+        lib().ora_gcmc_run_mix(C.byref(self.box), C.byref(self.ff), _d(pos), _d(q), _i(ty), _i(mol), ncomp,
+                               sysd["nhost"], _i(sizes), _i(offs), _i(ms), (_dp * ng)(*mps), (_dp * ng)(*mqs),
+                               (_i64p * ng)(*mts), (C.c_double * ng)(*ein), (C.c_double * ng)(*esf), _d(s_fw),
+                               _d(s_ads), gk, ng, first_step, nsteps, st)
         after = dict(sysd)
         newpos, newq, newt, newm = [], [], [], []
         starts = [0]
@@ -291,7 +309,8 @@ class OracleSystem:
         after["scale"] = np.ones(starts[-1])
         after["scale_coul"] = np.ones(starts[-1])
         after["comp_start"] = starts
-        return st, after, s_ads
+        stats = list(st) if isinstance(params, (list, tuple)) else st[0]
+        return stats, after, s_ads
 
     def widom(self, params, s_fw, s_ads, first_move, n, nthreads=0):
         res = (OraWidomResult * n)()

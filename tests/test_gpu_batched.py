@@ -1,0 +1,127 @@
+"""Batched CBMC of the CH4 / Xe benchmark: triclinic LJ frameworks, mixture GCMC,
+the prepared batch (device step counter, CUDA-graph replay) and the autotuner.
+
+Tolerances as in test_gpu_parity: FP64 1e-12 relative (energies) and identical
+decisions against the FP64 oracle; mixed beta*|dE| <= 1e-6 per trial.
+"""
+import numpy as np
+import pytest
+
+from graspa_gb300 import synth
+from oracle import oracle as O
+from tests.test_gpu_gcmc import ora_params
+from tests.test_gpu_parity import beta, fp64_close, mixed_close
+
+pytestmark = pytest.mark.gpu
+
+CAP = 256
+
+
+def mix_descs(grx, stream=0, pressure_pa=2e6, ntrials=16):
+    kw = dict(p_translation=0.3, p_rotation=0.3, p_reinsertion=0.5, p_swap=1.0, pressure_pa=pressure_pa,
+              ntrials=ntrials, norient=1, stream=stream, max_translation=0.7)
+    return [grx.gcmc_desc(1, **kw), grx.gcmc_desc(2, **kw)]
+
+
+def make_box(grx, s):
+    box = grx.Box(s, capacity=[s["comp_start"][1], CAP, CAP])
+    box.ewald_total()
+    return box
+
+
+@pytest.mark.parametrize("seed", [0, 2, 6])
+def test_triclinic_trial_energies(grx_lib, seed):
+    """Tile culling in general (triclinic) cells: per-trial energies of random beads
+    against framework + guests equal the oracle in FP64 and within tolerance mixed."""
+    s = synth.ch4_xe_system(seed, n_ch4=6, n_xe=4)
+    box = make_box(grx_lib, s)
+    S = O.OracleSystem(s)
+    rng = np.random.default_rng(seed)
+    cell = np.array(s["cell"]).reshape(3, 3).T
+    ntr = 32
+    pos = (cell @ rng.uniform(-0.2, 1.2, (3, ntr))).T   # also outside the stored cell
+    q = np.zeros(ntr)
+    ty = np.full(ntr, s["templates"][1]["type"][0])
+    ref, rf = S.trial_energies(pos, np.ones(ntr), q, np.ones(ntr), ty, 6, ntr, 1, 1)
+    e, f = box.trial_energies(pos, q, ty, 6, ntr, 1, 1, prec=grx_lib.GRX_FP64)
+    assert np.array_equal(f, rf) and fp64_close(e, ref), np.max(np.abs(e - ref))
+    em, fm = box.trial_energies(pos, q, ty, 6, ntr, 1, 1, prec=grx_lib.GRX_MIXED)
+    ok = rf == 0
+    assert np.array_equal(fm, rf) and mixed_close(em[ok].sum(1), ref[ok].sum(1))
+
+
+def test_mixture_gcmc_matches_oracle(grx_lib):
+    s = synth.ch4_xe_system(3, n_ch4=5, n_xe=5)
+    descs = mix_descs(grx_lib)
+    box = make_box(grx_lib, s)
+    st = grx_lib.gcmc_run([box], [descs], 0, 400, grx_lib.GRX_FP64)
+    ost, after, _ = O.OracleSystem(s).gcmc([ora_params(d) for d in descs], [s["comp_start"][1], CAP, CAP], 0, 400)
+    for k in range(2):
+        assert list(st[k].attempts) == list(ost[k].attempts)
+        assert list(st[k].accepted) == list(ost[k].accepted)
+        assert st[k].n_molecules == ost[k].n_molecules and st[k].sum_n == ost[k].sum_n
+    assert sum(st[0].accepted) > 20 and sum(st[1].accepted) > 20
+    for c in (1, 2):
+        a, b = after["comp_start"][c], after["comp_start"][c + 1]
+        assert np.max(np.abs(box.positions(c) - after["pos"][a:b]), initial=0.0) <= 1e-9
+
+
+def test_batch_launch_graph_and_resume(grx_lib):
+    seeds = [0, 3, 5, 7]
+    systems = [synth.ch4_xe_system(k) for k in seeds]
+    descs = [mix_descs(grx_lib, stream=k) for k in range(4)]
+    ref_boxes = [make_box(grx_lib, s) for s in systems]
+    ref = grx_lib.gcmc_run(ref_boxes, descs, 0, 200, grx_lib.GRX_FP64)
+    # two plain launches of 100 steps
+    boxes = [make_box(grx_lib, s) for s in systems]
+    batch = grx_lib.GcmcBatch(boxes, descs, grx_lib.GRX_FP64)
+    batch.launch(100)
+    batch.launch(100)
+    st, nxt = batch.stats()
+    assert nxt == 200
+    for a, b in zip(st, ref):
+        assert list(a.attempts) == list(b.attempts) and list(a.accepted) == list(b.accepted)
+        assert a.n_molecules == b.n_molecules
+    for bx, rb in zip(boxes, ref_boxes):
+        for c in (1, 2):
+            assert np.array_equal(bx.positions(c), rb.positions(c))
+    batch.close()
+    # the same 200 steps as one CUDA graph of 4 launches x 50 steps
+    boxes = [make_box(grx_lib, s) for s in systems]
+    batch = grx_lib.GcmcBatch(boxes, descs, grx_lib.GRX_FP64)
+    batch.run_graph(50, 4)
+    st, nxt = batch.stats()
+    assert nxt == 200
+    for a, b in zip(st, ref):
+        assert list(a.accepted) == list(b.accepted) and a.n_molecules == b.n_molecules
+    for bx, rb in zip(boxes, ref_boxes):
+        for c in (1, 2):
+            assert np.array_equal(bx.positions(c), rb.positions(c))
+    # replaying the graph continues the chains from step 200
+    batch.reset_stats()
+    batch.run_graph(50, 4)
+    st2, nxt = batch.stats()
+    assert nxt == 400 and sum(sum(x.attempts) for x in st2) > 0
+    batch.close()
+
+
+def test_autotune_keeps_chains_valid(grx_lib):
+    systems = [synth.ch4_xe_system(k) for k in (2, 4)]
+    boxes = [make_box(grx_lib, s) for s in systems]
+    descs = [mix_descs(grx_lib, stream=k) for k in range(2)]
+    totals0 = [sum(b.total_energy().values()) for b in boxes]
+    for b in boxes:
+        b.ewald_total()
+    batch = grx_lib.GcmcBatch(boxes, descs, grx_lib.GRX_MIXED)
+    chosen, ms = batch.autotune(50)
+    assert chosen in (1, 2, 4, 8) and all(m > 0 for m in ms)
+    batch.launch(100)
+    st, nxt = batch.stats()
+    assert nxt == 300
+    batch.close()
+    for i, b in enumerate(boxes):
+        esum = st[2 * i].energy[3] + st[2 * i + 1].energy[3]
+        nacc = sum(st[2 * i].accepted) + sum(st[2 * i + 1].accepted)
+        e1 = sum(b.total_energy().values())
+        # mixed precision: each accepted move's dE within 1e-6 kT of FP64
+        assert beta() * abs((e1 - totals0[i]) - esum) <= 1e-6 * (nacc + 1)
