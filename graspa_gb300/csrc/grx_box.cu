@@ -40,13 +40,27 @@ int sm_count(grx_box* b) {
   return b->num_sms;
 }
 
+cudaError_t dev_alloc(grx_box* b, void** p, size_t bytes) {
+  if (b->arena) {
+    *p = arena_alloc(b->arena, bytes);
+    return *p ? cudaSuccess : cudaErrorMemoryAllocation;
+  }
+  return cudaMalloc(p, bytes);
+}
+
+void dev_free(grx_box* b, void* p) {
+  if (!p) return;
+  if (b->arena) arena_free(b->arena, p);
+  else cudaFree(p);
+}
+
 grx_status ensure_scratch(grx_box* b, size_t bytes) {
   if (bytes <= b->scratch_bytes) return GRX_OK;
-  if (b->scratch) cudaFree(b->scratch);
+  dev_free(b, b->scratch);
   b->scratch = nullptr;
   b->scratch_bytes = 0;
   size_t want = std::max(bytes, (size_t)1 << 20);
-  GRX_CHECK_CUDA(cudaMalloc(&b->scratch, want), "scratch allocation");
+  GRX_CHECK_CUDA(dev_alloc(b, (void**)&b->scratch, want), "scratch allocation");
   b->scratch_bytes = want;
   return GRX_OK;
 }
@@ -64,11 +78,11 @@ grx_status ensure_pinned(grx_box* b, size_t bytes) {
 
 grx_status ensure_results(grx_box* b, size_t n) {
   if (n <= b->results_cap) return GRX_OK;
-  if (b->d_results) cudaFree(b->d_results);
+  dev_free(b, b->d_results);
   b->d_results = nullptr;
   b->results_cap = 0;
   size_t want = std::max(n, (size_t)1024);
-  GRX_CHECK_CUDA(cudaMalloc(&b->d_results, want * sizeof(grx_widom_result)), "result buffer");
+  GRX_CHECK_CUDA(dev_alloc(b, (void**)&b->d_results, want * sizeof(grx_widom_result)), "result buffer");
   b->results_cap = want;
   return GRX_OK;
 }
@@ -208,10 +222,10 @@ static grx_status build_coulomb_table(grx_box* b, double alpha, double cut2) {
     tf[4 * k + 2] = make_float4(c[3].x, c[3].y, c[4].x, c[4].y);
     tf[4 * k + 3] = make_float4(c[5].x, c[5].y, 0.0f, 0.0f);
   }
-  GRX_CHECK_CUDA(cudaMalloc(&b->ctab, tab.size() * sizeof(double)), "alloc Coulomb table");
+  GRX_CHECK_CUDA(dev_alloc(b, (void**)&b->ctab, tab.size() * sizeof(double)), "alloc Coulomb table");
   GRX_CHECK_CUDA(cudaMemcpy(b->ctab, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice),
                  "upload Coulomb table");
-  GRX_CHECK_CUDA(cudaMalloc(&b->ctabf, tf.size() * sizeof(float4)), "alloc Coulomb table (float pairs)");
+  GRX_CHECK_CUDA(dev_alloc(b, (void**)&b->ctabf, tf.size() * sizeof(float4)), "alloc Coulomb table (float pairs)");
   GRX_CHECK_CUDA(cudaMemcpy(b->ctabf, tf.data(), tf.size() * sizeof(float4), cudaMemcpyHostToDevice),
                  "upload Coulomb table (float pairs)");
   return GRX_OK;
@@ -282,13 +296,13 @@ static grx_status build_tiles(grx_box* b) {
   }
   b->ntiles = (int)b->h_tile_c.size();
   if ((size_t)b->ntiles > b->tile_cap) {
-    if (b->tile_c) cudaFree(b->tile_c);
-    if (b->tile_r) cudaFree(b->tile_r);
+    dev_free(b, b->tile_c);
+    dev_free(b, b->tile_r);
     b->tile_c = nullptr;
     b->tile_r = nullptr;
     b->tile_cap = 0;
-    GRX_CHECK_CUDA(cudaMalloc(&b->tile_c, b->ntiles * sizeof(float4)), "alloc tiles");
-    GRX_CHECK_CUDA(cudaMalloc(&b->tile_r, b->ntiles * sizeof(int4)), "alloc tile ranges");
+    GRX_CHECK_CUDA(dev_alloc(b, (void**)&b->tile_c, b->ntiles * sizeof(float4)), "alloc tiles");
+    GRX_CHECK_CUDA(dev_alloc(b, (void**)&b->tile_r, b->ntiles * sizeof(int4)), "alloc tile ranges");
     b->tile_cap = b->ntiles;
   }
   if (b->ntiles) {
@@ -379,7 +393,16 @@ grx_status grx_device_count(int32_t* n) {
   return GRX_OK;
 }
 
-grx_status grx_box_create(const grx_box_desc* desc, grx_box** out) {
+static grx_status box_create(const grx_box_desc* desc, grx_arena* arena, grx_box** out);
+
+grx_status grx_box_create(const grx_box_desc* desc, grx_box** out) { return box_create(desc, nullptr, out); }
+
+grx_status grx_box_create_in(const grx_box_desc* desc, grx_arena* arena, grx_box** out) {
+  GRX_REQUIRE(arena, "grx_box_create_in: null arena");
+  return box_create(desc, arena, out);
+}
+
+static grx_status box_create(const grx_box_desc* desc, grx_arena* arena, grx_box** out) {
   GRX_REQUIRE(desc && out, "grx_box_create: null argument");
   *out = nullptr;
   const grx_forcefield& ff = desc->forcefield;
@@ -400,6 +423,7 @@ grx_status grx_box_create(const grx_box_desc* desc, grx_box** out) {
     return GRX_ERR_NO_DEVICE;
   }
   grx_box* b = new grx_box();
+  b->arena = arena;
   cudaGetDevice(&b->device);
   b->ncomp = desc->ncomponents;
   b->nhost = desc->nhost_components;
@@ -511,28 +535,28 @@ grx_status grx_box_create(const grx_box_desc* desc, grx_box** out) {
   };
   cudaError_t e;
   const size_t n = b->total_cap;
-  if ((e = cudaMalloc(&b->pos64, n * sizeof(double4))) != cudaSuccess) return fail(e, "alloc pos64");
-  if ((e = cudaMalloc(&b->hi, n * sizeof(float4))) != cudaSuccess) return fail(e, "alloc hi");
-  if ((e = cudaMalloc(&b->lo, n * sizeof(float4))) != cudaSuccess) return fail(e, "alloc lo");
-  if ((e = cudaMalloc(&b->meta, n * sizeof(int2))) != cudaSuccess) return fail(e, "alloc meta");
-  if ((e = cudaMalloc(&b->scale, n * sizeof(double))) != cudaSuccess) return fail(e, "alloc scale");
-  if ((e = cudaMalloc(&b->charge, n * sizeof(double))) != cudaSuccess) return fail(e, "alloc charge");
-  if ((e = cudaMalloc(&b->d_size, GRX_MAX_COMPONENTS * sizeof(int))) != cudaSuccess) return fail(e, "alloc sizes");
-  if ((e = cudaMalloc(&b->ff64, nt2 * sizeof(FFPair64))) != cudaSuccess) return fail(e, "alloc ff64");
-  if ((e = cudaMalloc(&b->ffc10, nt2 * sizeof(double))) != cudaSuccess) return fail(e, "alloc ffc10");
-  if ((e = cudaMalloc(&b->ff32, nt2 * sizeof(float4))) != cudaSuccess) return fail(e, "alloc ff32");
-  if ((e = cudaMalloc(&b->ffdf, nt2 * sizeof(float4))) != cudaSuccess) return fail(e, "alloc ffdf");
-  if ((e = cudaMalloc(&b->ffdf2, nt2 * sizeof(float2))) != cudaSuccess) return fail(e, "alloc ffdf2");
-  if ((e = cudaMalloc(&b->qdf, n * sizeof(float2))) != cudaSuccess) return fail(e, "alloc qdf");
+  if ((e = dev_alloc(b, (void**)&b->pos64, n * sizeof(double4))) != cudaSuccess) return fail(e, "alloc pos64");
+  if ((e = dev_alloc(b, (void**)&b->hi, n * sizeof(float4))) != cudaSuccess) return fail(e, "alloc hi");
+  if ((e = dev_alloc(b, (void**)&b->lo, n * sizeof(float4))) != cudaSuccess) return fail(e, "alloc lo");
+  if ((e = dev_alloc(b, (void**)&b->meta, n * sizeof(int2))) != cudaSuccess) return fail(e, "alloc meta");
+  if ((e = dev_alloc(b, (void**)&b->scale, n * sizeof(double))) != cudaSuccess) return fail(e, "alloc scale");
+  if ((e = dev_alloc(b, (void**)&b->charge, n * sizeof(double))) != cudaSuccess) return fail(e, "alloc charge");
+  if ((e = dev_alloc(b, (void**)&b->d_size, GRX_MAX_COMPONENTS * sizeof(int))) != cudaSuccess) return fail(e, "alloc sizes");
+  if ((e = dev_alloc(b, (void**)&b->ff64, nt2 * sizeof(FFPair64))) != cudaSuccess) return fail(e, "alloc ff64");
+  if ((e = dev_alloc(b, (void**)&b->ffc10, nt2 * sizeof(double))) != cudaSuccess) return fail(e, "alloc ffc10");
+  if ((e = dev_alloc(b, (void**)&b->ff32, nt2 * sizeof(float4))) != cudaSuccess) return fail(e, "alloc ff32");
+  if ((e = dev_alloc(b, (void**)&b->ffdf, nt2 * sizeof(float4))) != cudaSuccess) return fail(e, "alloc ffdf");
+  if ((e = dev_alloc(b, (void**)&b->ffdf2, nt2 * sizeof(float2))) != cudaSuccess) return fail(e, "alloc ffdf2");
+  if ((e = dev_alloc(b, (void**)&b->qdf, n * sizeof(float2))) != cudaSuccess) return fail(e, "alloc qdf");
   const size_t nv = std::max(b->nvec, 1), na = std::max(b->nact, 1);
-  if ((e = cudaMalloc(&b->kact, na * sizeof(int4))) != cudaSuccess) return fail(e, "alloc kact");
-  if ((e = cudaMalloc(&b->ktemp, na * sizeof(double))) != cudaSuccess) return fail(e, "alloc ktemp");
-  if ((e = cudaMalloc(&b->s_fw, nv * sizeof(double2))) != cudaSuccess) return fail(e, "alloc s_fw");
-  if ((e = cudaMalloc(&b->s_ads, nv * sizeof(double2))) != cudaSuccess) return fail(e, "alloc s_ads");
-  if ((e = cudaMalloc(&b->s_tmp, nv * sizeof(double2))) != cudaSuccess) return fail(e, "alloc s_tmp");
-  if ((e = cudaMalloc(&b->ewA, na * sizeof(float4))) != cudaSuccess) return fail(e, "alloc ewA");
-  if ((e = cudaMalloc(&b->ewF, na * sizeof(float4))) != cudaSuccess) return fail(e, "alloc ewF");
-  if ((e = cudaMalloc(&b->ewT, na * sizeof(float2))) != cudaSuccess) return fail(e, "alloc ewT");
+  if ((e = dev_alloc(b, (void**)&b->kact, na * sizeof(int4))) != cudaSuccess) return fail(e, "alloc kact");
+  if ((e = dev_alloc(b, (void**)&b->ktemp, na * sizeof(double))) != cudaSuccess) return fail(e, "alloc ktemp");
+  if ((e = dev_alloc(b, (void**)&b->s_fw, nv * sizeof(double2))) != cudaSuccess) return fail(e, "alloc s_fw");
+  if ((e = dev_alloc(b, (void**)&b->s_ads, nv * sizeof(double2))) != cudaSuccess) return fail(e, "alloc s_ads");
+  if ((e = dev_alloc(b, (void**)&b->s_tmp, nv * sizeof(double2))) != cudaSuccess) return fail(e, "alloc s_tmp");
+  if ((e = dev_alloc(b, (void**)&b->ewA, na * sizeof(float4))) != cudaSuccess) return fail(e, "alloc ewA");
+  if ((e = dev_alloc(b, (void**)&b->ewF, na * sizeof(float4))) != cudaSuccess) return fail(e, "alloc ewF");
+  if ((e = dev_alloc(b, (void**)&b->ewT, na * sizeof(float2))) != cudaSuccess) return fail(e, "alloc ewT");
   cudaMemset(b->pos64, 0, n * sizeof(double4));
   cudaMemset(b->hi, 0, n * sizeof(float4));
   cudaMemset(b->lo, 0, n * sizeof(float4));
@@ -553,7 +577,7 @@ grx_status grx_box_create(const grx_box_desc* desc, grx_box** out) {
     cudaMemcpy(b->kact, b->h_kact.data(), b->nact * sizeof(int4), cudaMemcpyHostToDevice);
     cudaMemcpy(b->ktemp, b->h_ktemp.data(), b->nact * sizeof(double), cudaMemcpyHostToDevice);
   }
-  if ((e = cudaDeviceSynchronize()) != cudaSuccess) return fail(e, "box upload");
+  if ((e = cudaStreamSynchronize(nullptr)) != cudaSuccess) return fail(e, "box upload");
   if (!ff.no_charges) {
     grx_status st = build_coulomb_table(b, g.alpha, ff.cutoff_coul_sq);
     if (st) {
@@ -566,14 +590,46 @@ grx_status grx_box_create(const grx_box_desc* desc, grx_box** out) {
   return GRX_OK;
 }
 
+grx_status grx_box_footprint(const grx_box_desc* desc, size_t* bytes) {
+  GRX_REQUIRE(desc && bytes, "grx_box_footprint: null argument");
+  GRX_REQUIRE(desc->ncomponents >= 1 && desc->ncomponents <= GRX_MAX_COMPONENTS, "grx_box_footprint: bad components");
+  auto al = [](size_t n) { return (n + 255) / 256 * 256; };
+  size_t acc = 0, ntiles = 0;
+  for (int c = 0; c < desc->ncomponents; ++c) {
+    acc += (desc->capacity[c] + 31) / 32 * 32;
+    if (c < desc->nhost_components) ntiles += (desc->capacity[c] + 31) / 32;
+  }
+  const size_t n = std::max<size_t>(acc, 32);
+  const size_t nt2 = (size_t)desc->forcefield.ntypes * desc->forcefield.ntypes;
+  grx_box tmp;
+  build_kvectors(&tmp, desc->geometry);
+  const size_t nv = std::max(tmp.nvec, 1), na = std::max(tmp.nact, 1);
+  size_t t = al(n * sizeof(double4)) + 2 * al(n * sizeof(float4)) + al(n * sizeof(int2)) + 2 * al(n * sizeof(double)) +
+             al(n * sizeof(float2)) + al(GRX_MAX_COMPONENTS * sizeof(int));
+  t += al(nt2 * sizeof(FFPair64)) + al(nt2 * sizeof(double)) + 2 * al(nt2 * sizeof(float4)) + al(nt2 * sizeof(float2));
+  t += al(na * sizeof(int4)) + al(na * sizeof(double)) + 3 * al(nv * sizeof(double2)) + 2 * al(na * sizeof(float4)) +
+       al(na * sizeof(float2));
+  t += al(ntiles * sizeof(float4)) + al(ntiles * sizeof(int4));
+  if (!desc->forcefield.no_charges) {
+    const float s_lo = 0.25f, s_hi = (float)(desc->forcefield.cutoff_coul_sq * (1.0 + 1e-4) + 1e-2);
+    uint32_t lb, hb;
+    std::memcpy(&lb, &s_lo, 4);
+    std::memcpy(&hb, &s_hi, 4);
+    const size_t np = (size_t)((int)(hb >> 17) - (int)(lb >> 17) + 2);
+    t += al(8 * np * sizeof(double)) + al(4 * np * sizeof(float4));
+  }
+  t += al((size_t)1 << 20) + al(1024 * sizeof(grx_widom_result));  // first scratch and result buffers
+  *bytes = t;
+  return GRX_OK;
+}
+
 grx_status grx_box_destroy(grx_box* b) {
   if (!b) return GRX_OK;
   void* ptrs[] = {b->pos64, b->hi, b->lo, b->meta, b->scale, b->charge, b->d_size, b->ff64,
                   b->ffc10, b->ff32, b->kact, b->ktemp, b->s_fw, b->s_ads, b->s_tmp,
                   b->scratch, b->d_results, b->tile_c, b->tile_r, b->ctab, b->ctabf, b->qdf,
                   b->ffdf, b->ffdf2, b->ewA, b->ewF, b->ewT};
-  for (void* p : ptrs)
-    if (p) cudaFree(p);
+  for (void* p : ptrs) dev_free(b, p);
   if (b->pinned) cudaFreeHost(b->pinned);
   delete b;
   return GRX_OK;

@@ -425,6 +425,7 @@ struct grx_gcmc_batch {
   size_t smem = 0;
   int chunk_mult = 4;
   void* mem = nullptr;
+  grx_arena* arena = nullptr;
   BoxDev* d_boxes = nullptr;
   GcmcArgs* d_args = nullptr;
   int* d_first = nullptr;
@@ -435,6 +436,7 @@ struct grx_gcmc_batch {
   int64_t graph_nsteps = 0;
   int graph_nlaunch = 0;
   cudaStream_t graph_stream = nullptr;
+  cudaStream_t last_stream = nullptr;  // stream of the latest launch
 };
 
 namespace grx {
@@ -620,7 +622,11 @@ extern "C" grx_status grx_gcmc_batch_create(grx_box* const* boxes, int32_t nboxe
   auto al = [](size_t n) { return (n + 255) / 256 * 256; };
   const size_t oa = al(nboxes * sizeof(BoxDev)), of = oa + al(B->nentries * sizeof(GcmcArgs)),
                os = of + al((nboxes + 1) * sizeof(int)), ot = os + al(B->nentries * sizeof(grx_gcmc_stats));
-  if (cudaMalloc(&B->mem, ot + 256) != cudaSuccess) {
+  B->arena = boxes[0]->arena;  // a batch of arena boxes lives in the same arena
+  if (B->arena) B->mem = arena_alloc(B->arena, ot + 256);
+  else if (cudaMalloc(&B->mem, ot + 256) != cudaSuccess) B->mem = nullptr;
+  if (!B->mem) {
+    cudaGetLastError();
     delete B;
     set_error("grx_gcmc_batch_create: out of device memory");
     return GRX_ERR_OUT_OF_MEMORY;
@@ -632,15 +638,20 @@ extern "C" grx_status grx_gcmc_batch_create(grx_box* const* boxes, int32_t nboxe
   B->d_stats = (grx_gcmc_stats*)(base + os);
   B->d_step = (uint64_t*)(base + ot);
   const uint64_t zero = 0;
-  bool ok = cudaMemcpy(B->d_boxes, hb.data(), nboxes * sizeof(BoxDev), cudaMemcpyHostToDevice) == cudaSuccess &&
-            cudaMemcpy(B->d_args, ha.data(), B->nentries * sizeof(GcmcArgs), cudaMemcpyHostToDevice) == cudaSuccess &&
-            cudaMemcpy(B->d_first, B->first.data(), (nboxes + 1) * sizeof(int), cudaMemcpyHostToDevice) ==
-                cudaSuccess &&
-            cudaMemset(B->d_stats, 0, B->nentries * sizeof(grx_gcmc_stats)) == cudaSuccess &&
-            cudaMemcpy(B->d_step, &zero, sizeof(uint64_t), cudaMemcpyHostToDevice) == cudaSuccess;
+  cudaStream_t s0 = B->stream;
+  bool ok =
+      cudaMemcpyAsync(B->d_boxes, hb.data(), nboxes * sizeof(BoxDev), cudaMemcpyHostToDevice, s0) == cudaSuccess &&
+      cudaMemcpyAsync(B->d_args, ha.data(), B->nentries * sizeof(GcmcArgs), cudaMemcpyHostToDevice, s0) ==
+          cudaSuccess &&
+      cudaMemcpyAsync(B->d_first, B->first.data(), (nboxes + 1) * sizeof(int), cudaMemcpyHostToDevice, s0) ==
+          cudaSuccess &&
+      cudaMemsetAsync(B->d_stats, 0, B->nentries * sizeof(grx_gcmc_stats), s0) == cudaSuccess &&
+      cudaMemcpyAsync(B->d_step, &zero, sizeof(uint64_t), cudaMemcpyHostToDevice, s0) == cudaSuccess &&
+      cudaStreamSynchronize(s0) == cudaSuccess;
   st = set_gcmc_smem();
   if (!ok || st) {
-    cudaFree(B->mem);
+    if (B->arena) arena_free(B->arena, B->mem);
+    else cudaFree(B->mem);
     delete B;
     set_error("grx_gcmc_batch_create: device set-up failed");
     return GRX_ERR_CUDA;
@@ -659,7 +670,8 @@ static void drop_graph(grx_gcmc_batch* B) {
 extern "C" grx_status grx_gcmc_batch_destroy(grx_gcmc_batch* B) {
   if (!B) return GRX_OK;
   drop_graph(B);
-  if (B->mem) cudaFree(B->mem);
+  if (B->arena) arena_free(B->arena, B->mem);
+  else if (B->mem) cudaFree(B->mem);
   delete B;
   return GRX_OK;
 }
@@ -676,6 +688,7 @@ extern "C" grx_status grx_gcmc_batch_launch(grx_gcmc_batch* B, int64_t nsteps, v
   GRX_REQUIRE(B && nsteps >= 0, "grx_gcmc_batch_launch: bad argument");
   cudaStream_t s = stream ? (cudaStream_t)stream : B->stream;
   if (nsteps == 0) return GRX_OK;
+  B->last_stream = s;
   return enqueue_gcmc(B->prec, (int)B->boxes.size(), B->d_boxes, B->d_args, B->d_first, B->d_step, nsteps,
                       B->d_stats, B->smem, s);
 }
@@ -706,12 +719,15 @@ extern "C" grx_status grx_gcmc_batch_run_graph(grx_gcmc_batch* B, int64_t nsteps
     B->graph_nlaunch = nlaunch;
   }
   GRX_CHECK_CUDA(cudaGraphLaunch(B->exec, s), "graph launch");
+  B->last_stream = s;
   return GRX_OK;
 }
 
 extern "C" grx_status grx_gcmc_batch_stats(grx_gcmc_batch* B, grx_gcmc_stats* stats, uint64_t* next_step) {
   GRX_REQUIRE(B, "grx_gcmc_batch_stats: null batch");
-  GRX_CHECK_CUDA(cudaDeviceSynchronize(), "gcmc batch sync");
+  GRX_CHECK_CUDA(cudaStreamSynchronize(B->stream), "gcmc batch sync");
+  if (B->last_stream && B->last_stream != B->stream)
+    GRX_CHECK_CUDA(cudaStreamSynchronize(B->last_stream), "gcmc batch sync");
   if (stats)
     GRX_CHECK_CUDA(cudaMemcpy(stats, B->d_stats, B->nentries * sizeof(grx_gcmc_stats), cudaMemcpyDeviceToHost),
                    "read stats");

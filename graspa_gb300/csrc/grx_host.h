@@ -8,6 +8,7 @@
 
 struct grx_box {
   grx::BoxDev dev{};
+  grx_arena* arena = nullptr;  // device memory comes from here when set (else cudaMalloc)
   cudaStream_t stream = nullptr;
   int device = 0;
   int num_sms = 0;
@@ -86,6 +87,11 @@ grx_status ensure_pinned(grx_box* b, size_t bytes);
 grx_status ensure_results(grx_box* b, size_t n);
 void refresh_dev(grx_box* b);
 int sm_count(grx_box* b);
+void* arena_alloc(grx_arena* a, size_t bytes);
+void arena_free(grx_arena* a, void* p);
+// Device allocation of a box: from its arena when it has one, else cudaMalloc.
+cudaError_t dev_alloc(grx_box* b, void** p, size_t bytes);
+void dev_free(grx_box* b, void* p);
 }  // namespace grx
 
 #define GRX_CHECK_CUDA(call, what)                                    \

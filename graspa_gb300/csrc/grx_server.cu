@@ -1,0 +1,363 @@
+// grx_server.cu -- continuous-batching job server for Widom and GCMC jobs.
+//
+// Jobs (a box plus its work) are queued by grx_server_submit. grx_server_progress,
+// called in the caller's loop, does one non-blocking scheduling round:
+//   retire  jobs whose last slice finished: reduce the results, destroy the box
+//           (its memory returns to the arena without a device-wide wait);
+//   admit   queued jobs in arrival order while a slot is free and the job's box fits
+//           in the arena (admission by HBM footprint);
+//   launch  the next slice of every resident job without a slice in flight, each job
+//           on its own non-blocking stream, so slices of different jobs overlap.
+// A job's arithmetic is independent of the other resident jobs: it sees only its own
+// box, and its Philox stream is fixed by its own seed, so its result is the same alone
+// and in any mix.
+#include <chrono>
+#include <deque>
+#include <mutex>
+#include <vector>
+
+#include "grx_host.h"
+
+namespace grx {
+
+struct ServerJob {
+  uint64_t id = 0, tag = 0;
+  int32_t kind = GRX_JOB_WIDOM;
+  // owned copies of the inputs
+  grx_box_desc desc{};
+  std::vector<double> eps, sig, z, shift, c10;
+  std::vector<std::vector<double>> pos, scale, charge, scc;
+  std::vector<std::vector<size_t>> type, molid;
+  std::vector<size_t> size, n_stored;
+  std::vector<int32_t> rigid;
+  grx_widom_desc widom{};
+  int64_t total = 0;  // insertions or steps
+  std::vector<grx_gcmc_desc> gcmc;
+  // resident state
+  grx_box* box = nullptr;
+  grx_gcmc_batch* batch = nullptr;
+  grx_widom_result* d_results = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev = nullptr;
+  bool inflight = false;
+  int64_t issued = 0;
+  size_t footprint = 0;
+  double t_submit = 0, t_admit = 0, t_done = 0;
+  grx_status status = GRX_OK;
+};
+
+}  // namespace grx
+
+using namespace grx;
+
+struct grx_server {
+  grx_server_config cfg{};
+  grx_arena* arena = nullptr;
+  bool own_arena = false;
+  std::deque<ServerJob*> pending;
+  std::vector<ServerJob*> resident;
+  std::vector<grx_job_result> done;
+  std::vector<cudaStream_t> streams;  // idle streams for reuse
+  std::chrono::steady_clock::time_point t0;
+  uint64_t next_id = 1;
+  uint64_t launches = 0;
+  std::mutex m;
+  double now() const {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+};
+
+namespace {
+
+grx_status release_job(grx_server* S, ServerJob* j) {
+  if (j->batch) grx_gcmc_batch_destroy(j->batch);
+  j->batch = nullptr;
+  if (j->d_results) arena_free(S->arena, j->d_results);
+  j->d_results = nullptr;
+  if (j->box) grx_box_destroy(j->box);
+  j->box = nullptr;
+  if (j->ev) cudaEventDestroy(j->ev);
+  j->ev = nullptr;
+  if (j->stream) S->streams.push_back(j->stream);
+  j->stream = nullptr;
+  return GRX_OK;
+}
+
+// Creates the job's box in the arena and uploads its state. GRX_ERR_OUT_OF_MEMORY
+// means "does not fit now" (nothing is left allocated).
+grx_status admit_job(grx_server* S, ServerJob* j) {
+  size_t before = 0;
+  grx_arena_usage(S->arena, &before, nullptr, nullptr);
+  grx_status st = grx_box_create_in(&j->desc, S->arena, &j->box);
+  if (st) return st;
+  if (!S->streams.empty()) {
+    j->stream = S->streams.back();
+    S->streams.pop_back();
+  } else {
+    GRX_CHECK_CUDA(cudaStreamCreateWithFlags(&j->stream, cudaStreamNonBlocking), "job stream");
+  }
+  GRX_CHECK_CUDA(cudaEventCreateWithFlags(&j->ev, cudaEventDisableTiming), "job event");
+  for (int c = 0; c < j->desc.ncomponents && st == GRX_OK; ++c) {
+    grx_atoms a{};
+    a.pos = j->pos[c].data();
+    a.scale = j->scale[c].data();
+    a.charge = j->charge[c].data();
+    a.scale_coul = j->scc[c].data();
+    a.type = j->type[c].data();
+    a.molid = j->molid[c].data();
+    a.size = j->size[c];
+    a.n_stored = j->n_stored[c];
+    st = grx_box_set_component(j->box, c, &a, j->rigid[c]);
+  }
+  if (st == GRX_OK) {
+    double out8[8];
+    st = grx_ewald_total(j->box, out8);
+  }
+  if (st == GRX_OK) st = grx_box_set_stream(j->box, j->stream);
+  if (st == GRX_OK && j->kind == GRX_JOB_GCMC) {
+    const int32_t nm = (int32_t)j->gcmc.size();
+    st = grx_gcmc_batch_create(&j->box, 1, j->gcmc.data(), &nm, S->cfg.precision, &j->batch);
+  }
+  if (st == GRX_OK && j->kind == GRX_JOB_WIDOM) {
+    j->d_results = (grx_widom_result*)arena_alloc(S->arena, std::max<int64_t>(j->total, 1) * sizeof(grx_widom_result));
+    if (!j->d_results) st = GRX_ERR_OUT_OF_MEMORY;
+  }
+  if (st) {
+    release_job(S, j);
+    if (st == GRX_ERR_OUT_OF_MEMORY) cudaGetLastError();
+    return st;
+  }
+  size_t after = 0;
+  grx_arena_usage(S->arena, &after, nullptr, nullptr);
+  j->footprint = after - before;
+  return GRX_OK;
+}
+
+grx_status launch_slice(grx_server* S, ServerJob* j) {
+  const int64_t left = j->total - j->issued;
+  grx_status st = GRX_OK;
+  if (j->kind == GRX_JOB_WIDOM) {
+    const int64_t n = std::min<int64_t>(left, std::max<int64_t>(S->cfg.widom_slice, 1));
+    st = grx_widom_insertions_async(j->box, &j->widom, (uint64_t)j->issued, (size_t)n, S->cfg.precision,
+                                    j->d_results + j->issued);
+    j->issued += n;
+  } else {
+    const int64_t n = std::min<int64_t>(left, std::max<int64_t>(S->cfg.gcmc_slice, 1));
+    st = grx_gcmc_batch_launch(j->batch, n, j->stream);
+    j->issued += n;
+  }
+  if (st) return st;
+  GRX_CHECK_CUDA(cudaEventRecord(j->ev, j->stream), "job event");
+  j->inflight = true;
+  S->launches++;
+  return GRX_OK;
+}
+
+grx_status collect(grx_server* S, ServerJob* j, grx_job_result& r) {
+  r = grx_job_result{};
+  r.tag = j->tag;
+  r.job_id = j->id;
+  r.kind = j->kind;
+  r.status = j->status;
+  r.t_submit = j->t_submit;
+  r.t_admit = j->t_admit;
+  r.footprint_bytes = j->footprint;
+  if (j->status == GRX_OK && j->kind == GRX_JOB_WIDOM) {
+    std::vector<grx_widom_result> h((size_t)j->total);
+    if (j->total)
+      GRX_CHECK_CUDA(cudaMemcpyAsync(h.data(), j->d_results, j->total * sizeof(grx_widom_result),
+                                     cudaMemcpyDeviceToHost, j->stream),
+                     "widom results");
+    GRX_CHECK_CUDA(cudaStreamSynchronize(j->stream), "widom results");
+    double s = 0.0, s2 = 0.0;
+    for (const grx_widom_result& x : h) {
+      const double w = x.success ? x.rosenbluth : 0.0;
+      s += w;
+      s2 += w * w;
+    }
+    r.widom_n = j->total;
+    r.widom_mean_w = j->total ? s / (double)j->total : 0.0;
+    r.widom_mean_w2 = j->total ? s2 / (double)j->total : 0.0;
+  } else if (j->status == GRX_OK) {
+    std::vector<grx_gcmc_stats> st(j->gcmc.size());
+    grx_status e = grx_gcmc_batch_stats(j->batch, st.data(), nullptr);
+    if (e) return e;
+    r.ncomp_moved = (int32_t)st.size();
+    for (size_t k = 0; k < st.size() && k < 4; ++k) r.gcmc[k] = st[k];
+    r.gcmc_steps = j->total;
+  }
+  r.t_done = S->now();
+  return GRX_OK;
+}
+
+}  // namespace
+
+extern "C" grx_status grx_server_create(const grx_server_config* cfg, grx_arena* arena, grx_server** out) {
+  GRX_REQUIRE(cfg && out, "grx_server_create: null argument");
+  GRX_REQUIRE(cfg->max_resident >= 1, "grx_server_create: max_resident must be >= 1");
+  GRX_REQUIRE(cfg->precision == GRX_FP64 || cfg->precision == GRX_MIXED || cfg->precision == GRX_FP32,
+              "grx_server_create: bad precision");
+  auto* S = new grx_server();
+  S->cfg = *cfg;
+  if (S->cfg.widom_slice <= 0) S->cfg.widom_slice = 1 << 30;
+  if (S->cfg.gcmc_slice <= 0) S->cfg.gcmc_slice = 1 << 30;
+  if (arena) {
+    S->arena = arena;
+  } else {
+    grx_status st = grx_arena_create(cfg->hbm_budget_bytes, &S->arena);
+    if (st) {
+      delete S;
+      return st;
+    }
+    S->own_arena = true;
+  }
+  S->t0 = std::chrono::steady_clock::now();
+  *out = S;
+  return GRX_OK;
+}
+
+extern "C" grx_status grx_server_destroy(grx_server* S) {
+  if (!S) return GRX_OK;
+  for (ServerJob* j : S->resident) {
+    if (j->stream) cudaStreamSynchronize(j->stream);
+    release_job(S, j);
+    delete j;
+  }
+  for (ServerJob* j : S->pending) delete j;
+  for (cudaStream_t s : S->streams) cudaStreamDestroy(s);
+  if (S->own_arena) grx_arena_destroy(S->arena);
+  delete S;
+  return GRX_OK;
+}
+
+extern "C" grx_status grx_server_submit(grx_server* S, const grx_job_desc* jd, uint64_t* job_id) {
+  GRX_REQUIRE(S && jd && jd->box && jd->atoms, "grx_server_submit: null argument");
+  GRX_REQUIRE(jd->kind == GRX_JOB_WIDOM || jd->kind == GRX_JOB_GCMC, "grx_server_submit: bad job kind");
+  const grx_box_desc& d = *jd->box;
+  GRX_REQUIRE(d.ncomponents >= 1 && d.ncomponents <= GRX_MAX_COMPONENTS, "grx_server_submit: bad components");
+  auto* j = new ServerJob();
+  j->kind = jd->kind;
+  j->tag = jd->tag;
+  j->desc = d;
+  const grx_forcefield& ff = d.forcefield;
+  const size_t nt2 = (size_t)ff.ntypes * ff.ntypes;
+  auto cp = [&](const double* p, std::vector<double>& v) {
+    if (p) v.assign(p, p + nt2);
+  };
+  cp(ff.epsilon, j->eps);
+  cp(ff.sigma, j->sig);
+  cp(ff.z, j->z);
+  cp(ff.shift, j->shift);
+  cp(ff.c10, j->c10);
+  j->desc.forcefield.epsilon = j->eps.empty() ? nullptr : j->eps.data();
+  j->desc.forcefield.sigma = j->sig.empty() ? nullptr : j->sig.data();
+  j->desc.forcefield.z = j->z.empty() ? nullptr : j->z.data();
+  j->desc.forcefield.shift = j->shift.empty() ? nullptr : j->shift.data();
+  j->desc.forcefield.c10 = j->c10.empty() ? nullptr : j->c10.data();
+  const int nc = d.ncomponents;
+  j->pos.resize(nc); j->scale.resize(nc); j->charge.resize(nc); j->scc.resize(nc);
+  j->type.resize(nc); j->molid.resize(nc); j->size.resize(nc); j->n_stored.resize(nc); j->rigid.resize(nc);
+  for (int c = 0; c < nc; ++c) {
+    const grx_atoms& a = jd->atoms[c];
+    const size_t n = std::max(a.size, a.n_stored);
+    j->size[c] = a.size;
+    j->n_stored[c] = n;
+    j->pos[c].assign(a.pos, a.pos + 3 * n);
+    j->charge[c].assign(a.charge, a.charge + n);
+    j->type[c].assign(a.type, a.type + n);
+    j->molid[c].assign(a.molid, a.molid + n);
+    j->scale[c] = a.scale ? std::vector<double>(a.scale, a.scale + n) : std::vector<double>(n, 1.0);
+    j->scc[c] = a.scale_coul ? std::vector<double>(a.scale_coul, a.scale_coul + n) : std::vector<double>(n, 1.0);
+    j->rigid[c] = jd->rigid ? jd->rigid[c] : (c >= d.nhost_components ? 1 : 0);
+  }
+  if (jd->kind == GRX_JOB_WIDOM) {
+    GRX_REQUIRE(jd->widom_insertions >= 0, "grx_server_submit: negative insertion count");
+    j->widom = jd->widom;
+    j->total = jd->widom_insertions;
+  } else {
+    GRX_REQUIRE(jd->gcmc && jd->ncomp_moved >= 1 && jd->ncomp_moved <= 4 && jd->gcmc_steps >= 0,
+                "grx_server_submit: GCMC job needs 1..4 move sets and a step count");
+    j->gcmc.assign(jd->gcmc, jd->gcmc + jd->ncomp_moved);
+    j->total = jd->gcmc_steps;
+  }
+  std::lock_guard<std::mutex> g(S->m);
+  j->id = S->next_id++;
+  j->t_submit = S->now();
+  S->pending.push_back(j);
+  if (job_id) *job_id = j->id;
+  return GRX_OK;
+}
+
+extern "C" grx_status grx_server_progress(grx_server* S, int32_t* n_resident, int32_t* n_pending) {
+  GRX_REQUIRE(S, "grx_server_progress: null server");
+  std::lock_guard<std::mutex> g(S->m);
+  // retire / advance resident jobs
+  for (size_t i = 0; i < S->resident.size();) {
+    ServerJob* j = S->resident[i];
+    if (j->inflight) {
+      const cudaError_t e = cudaEventQuery(j->ev);
+      if (e == cudaErrorNotReady) { ++i; continue; }
+      j->inflight = false;
+      if (e != cudaSuccess) j->status = cuda_status(e, "job slice");
+    }
+    if (j->status == GRX_OK && j->issued < j->total) {
+      j->status = launch_slice(S, j);
+      if (j->status == GRX_OK) { ++i; continue; }
+    }
+    grx_job_result r;
+    grx_status st = collect(S, j, r);
+    if (st && r.status == GRX_OK) r.status = st;
+    release_job(S, j);
+    S->done.push_back(r);
+    delete j;
+    S->resident.erase(S->resident.begin() + i);
+  }
+  // admit in arrival order while slots and memory allow
+  while (!S->pending.empty() && (int)S->resident.size() < S->cfg.max_resident) {
+    ServerJob* j = S->pending.front();
+    const grx_status st = admit_job(S, j);
+    if (st == GRX_ERR_OUT_OF_MEMORY && !S->resident.empty()) break;  // wait for memory to free up
+    S->pending.pop_front();
+    if (st) {  // does not fit even alone, or invalid: report and drop
+      j->status = st;
+      grx_job_result r{};
+      r.tag = j->tag;
+      r.job_id = j->id;
+      r.kind = j->kind;
+      r.status = st;
+      r.t_submit = j->t_submit;
+      r.t_done = S->now();
+      S->done.push_back(r);
+      delete j;
+      continue;
+    }
+    j->t_admit = S->now();
+    S->resident.push_back(j);
+    j->status = j->total > 0 ? launch_slice(S, j) : GRX_OK;
+  }
+  if (n_resident) *n_resident = (int32_t)S->resident.size();
+  if (n_pending) *n_pending = (int32_t)S->pending.size();
+  return GRX_OK;
+}
+
+extern "C" grx_status grx_server_poll(grx_server* S, grx_job_result* out, int32_t max, int32_t* n) {
+  GRX_REQUIRE(S && n && (out || max == 0), "grx_server_poll: bad argument");
+  std::lock_guard<std::mutex> g(S->m);
+  const int32_t k = std::min<int32_t>(max, (int32_t)S->done.size());
+  for (int32_t i = 0; i < k; ++i) out[i] = S->done[i];
+  S->done.erase(S->done.begin(), S->done.begin() + k);
+  *n = k;
+  return GRX_OK;
+}
+
+extern "C" grx_status grx_server_time(grx_server* S, double* seconds) {
+  GRX_REQUIRE(S && seconds, "grx_server_time: bad argument");
+  *seconds = S->now();
+  return GRX_OK;
+}
+
+extern "C" grx_status grx_server_launch_count(grx_server* S, uint64_t* launches) {
+  GRX_REQUIRE(S && launches, "grx_server_launch_count: bad argument");
+  *launches = S->launches;
+  return GRX_OK;
+}

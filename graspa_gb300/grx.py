@@ -102,6 +102,29 @@ class GcmcStats(C.Structure):
     _fields_ = [("attempts", C.c_int64 * 5), ("accepted", C.c_int64 * 5), ("n_molecules", C.c_int64),
                 ("capacity_hits", C.c_int64), ("energy", C.c_double * 4), ("sum_n", C.c_double)]
 
+JOB_WIDOM, JOB_GCMC = 0, 1
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_resident", C.c_int32), ("precision", C.c_int32),
+                ("widom_slice", C.c_int64), ("gcmc_slice", C.c_int64)]
+
+
+class JobDesc(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("ncomp_moved", C.c_int32), ("box", C.POINTER(BoxDesc)),
+                ("atoms", C.POINTER(Atoms)), ("rigid", C.POINTER(C.c_int32)), ("widom", WidomDesc),
+                ("widom_insertions", C.c_int64), ("gcmc", C.POINTER(GcmcDesc)), ("gcmc_steps", C.c_int64),
+                ("tag", C.c_uint64)]
+
+
+class JobResult(C.Structure):
+    _fields_ = [("tag", C.c_uint64), ("job_id", C.c_uint64), ("kind", C.c_int32), ("status", C.c_int32),
+                ("t_submit", C.c_double), ("t_admit", C.c_double), ("t_done", C.c_double),
+                ("footprint_bytes", C.c_size_t), ("widom_n", C.c_int64), ("widom_mean_w", C.c_double),
+                ("widom_mean_w2", C.c_double), ("gcmc_steps", C.c_int64), ("ncomp_moved", C.c_int32),
+                ("pad_", C.c_int32), ("gcmc", GcmcStats * 4)]
+
+
 # every symbol include/grx.h declares
 EXPORTS = [
     "grx_status_string", "grx_last_error", "grx_device_count", "grx_box_create", "grx_box_destroy",
@@ -112,7 +135,9 @@ EXPORTS = [
     "grx_widom_insertions", "grx_widom_insertions_async", "grx_launch_count", "grx_trial_energies_noalloc", "grx_gcmc_run",
     "grx_box_write_molecule", "grx_box_remove_molecule", "grx_gcmc_batch_create", "grx_gcmc_batch_destroy",
     "grx_gcmc_batch_set_step", "grx_gcmc_batch_launch", "grx_gcmc_batch_run_graph", "grx_gcmc_batch_stats",
-    "grx_gcmc_batch_reset_stats", "grx_gcmc_batch_autotune",
+    "grx_gcmc_batch_reset_stats", "grx_gcmc_batch_autotune", "grx_arena_create", "grx_arena_destroy",
+    "grx_arena_usage", "grx_box_create_in", "grx_box_footprint", "grx_server_create", "grx_server_destroy",
+    "grx_server_submit", "grx_server_progress", "grx_server_poll", "grx_server_time", "grx_server_launch_count",
 ]
 
 _lib = None
@@ -176,6 +201,18 @@ def load(path=LIB_PATH):
     L.grx_gcmc_batch_stats.argtypes = [C.c_void_p, P(GcmcStats), P(C.c_uint64)]
     L.grx_gcmc_batch_reset_stats.argtypes = [C.c_void_p]
     L.grx_gcmc_batch_autotune.argtypes = [C.c_void_p, C.c_int64, P(C.c_int32), P(C.c_float)]
+    L.grx_arena_create.argtypes = [C.c_size_t, P(C.c_void_p)]
+    L.grx_arena_destroy.argtypes = [C.c_void_p]
+    L.grx_arena_usage.argtypes = [C.c_void_p, P(C.c_size_t), P(C.c_size_t), P(C.c_size_t)]
+    L.grx_box_create_in.argtypes = [P(BoxDesc), C.c_void_p, P(C.c_void_p)]
+    L.grx_box_footprint.argtypes = [P(BoxDesc), P(C.c_size_t)]
+    L.grx_server_create.argtypes = [P(ServerConfig), C.c_void_p, P(C.c_void_p)]
+    L.grx_server_destroy.argtypes = [C.c_void_p]
+    L.grx_server_submit.argtypes = [C.c_void_p, P(JobDesc), P(C.c_uint64)]
+    L.grx_server_progress.argtypes = [C.c_void_p, P(C.c_int32), P(C.c_int32)]
+    L.grx_server_poll.argtypes = [C.c_void_p, P(JobResult), C.c_int32, P(C.c_int32)]
+    L.grx_server_time.argtypes = [C.c_void_p, P(C.c_double)]
+    L.grx_server_launch_count.argtypes = [C.c_void_p, P(C.c_uint64)]
     _lib = L
     return L
 
@@ -237,48 +274,85 @@ def geometry_from_system(system):
     return g
 
 
+def box_desc(system, capacity=None):
+    """grx_box_desc of a system dict; returns (desc, keep) with `keep` owning the
+    force-field arrays the descriptor points to."""
+    nt = int(system["ntypes"])
+    eps = np.ascontiguousarray(system["epsilon"], dtype=np.float64)
+    sig = np.ascontiguousarray(system["sigma"], dtype=np.float64)
+    shift = np.ascontiguousarray(system["shift"], dtype=np.float64)
+    d = BoxDesc()
+    d.geometry = geometry_from_system(system)
+    ff = ForceField()
+    ff.ntypes = nt
+    ff.use_1264 = 0
+    ff.epsilon, ff.sigma, ff.shift = _d(eps), _d(sig), _d(shift)
+    ff.z = _dp()
+    ff.c10 = _dp()
+    ff.no_charges = int(system.get("no_charges", 0))
+    ff.vdw_real_bias = int(system.get("vdw_real_bias", 1))
+    ff.overlap_criteria = float(system.get("overlap_criteria", 1e6))
+    ff.cutoff_vdw_sq = float(system["cutoff_vdw"]) ** 2
+    ff.cutoff_coul_sq = float(system["cutoff_coul"]) ** 2
+    d.forcefield = ff
+    cs = system["comp_start"]
+    ncomp = len(cs) - 1
+    d.ncomponents = ncomp
+    d.nhost_components = int(system["nhost"])
+    for c in range(ncomp):
+        n = cs[c + 1] - cs[c]
+        ms = int(system["molsize"][c])
+        cap = capacity[c] if capacity is not None else max(n, ms)
+        d.capacity[c] = max(cap, ms)
+        d.molsize[c] = ms
+    return d, (eps, sig, shift)
+
+
+def component_atoms(system, c):
+    """grx_atoms of component c; returns (atoms, keep). An empty adsorbate component
+    stores its molecule template."""
+    s = system
+    a0, a1 = s["comp_start"][c], s["comp_start"][c + 1]
+    n = a1 - a0
+    ms = int(s["molsize"][c])
+    pos = np.ascontiguousarray(np.asarray(s["pos"], dtype=np.float64)[a0:a1]).reshape(-1, 3)
+    q = np.ascontiguousarray(np.asarray(s["charge"], dtype=np.float64)[a0:a1])
+    ty = np.ascontiguousarray(np.asarray(s["type"])[a0:a1], dtype=np.uint64)
+    mol = np.ascontiguousarray(np.asarray(s["molid"])[a0:a1], dtype=np.uint64)
+    sc = np.ascontiguousarray(np.asarray(s["scale"], dtype=np.float64)[a0:a1])
+    scc = np.ascontiguousarray(np.asarray(s["scale_coul"], dtype=np.float64)[a0:a1])
+    stored = n
+    if n == 0 and c >= int(s["nhost"]) and c in s.get("templates", {}):
+        tm = s["templates"][c]
+        pos = np.ascontiguousarray(tm["pos"], dtype=np.float64)
+        q = np.ascontiguousarray(tm["charge"], dtype=np.float64)
+        ty = np.ascontiguousarray(tm["type"], dtype=np.uint64)
+        mol = np.zeros(ms, dtype=np.uint64)
+        sc = np.ones(ms)
+        scc = np.ones(ms)
+        stored = ms
+    pos = np.ascontiguousarray(pos.reshape(-1))
+    return Atoms(_d(pos), _d(sc), _d(q), _d(scc), _sz(ty), _sz(mol), n, stored), (pos, q, ty, mol, sc, scc)
+
+
 class Box:
     """Device-resident box (one grx_box)."""
 
-    def __init__(self, system, capacity=None):
+    def __init__(self, system, capacity=None, arena=None):
         L = load()
         self.L = L
         self.system = system
-        nt = int(system["ntypes"])
-        self._eps = np.ascontiguousarray(system["epsilon"], dtype=np.float64)
-        self._sig = np.ascontiguousarray(system["sigma"], dtype=np.float64)
-        self._shift = np.ascontiguousarray(system["shift"], dtype=np.float64)
-        d = BoxDesc()
-        d.geometry = geometry_from_system(system)
-        ff = ForceField()
-        ff.ntypes = nt
-        ff.use_1264 = 0
-        ff.epsilon, ff.sigma, ff.shift = _d(self._eps), _d(self._sig), _d(self._shift)
-        ff.z = _dp()
-        ff.c10 = _dp()
-        ff.no_charges = int(system.get("no_charges", 0))
-        ff.vdw_real_bias = int(system.get("vdw_real_bias", 1))
-        ff.overlap_criteria = float(system.get("overlap_criteria", 1e6))
-        ff.cutoff_vdw_sq = float(system["cutoff_vdw"]) ** 2
-        ff.cutoff_coul_sq = float(system["cutoff_coul"]) ** 2
-        d.forcefield = ff
-        cs = system["comp_start"]
-        ncomp = len(cs) - 1
-        d.ncomponents = ncomp
-        d.nhost_components = int(system["nhost"])
-        for c in range(ncomp):
-            n = cs[c + 1] - cs[c]
-            ms = int(system["molsize"][c])
-            cap = capacity[c] if capacity is not None else max(n, ms)
-            d.capacity[c] = max(cap, ms)
-            d.molsize[c] = ms
+        d, self._keep = box_desc(system, capacity)
         self.desc = d
-        self.ncomp = ncomp
+        self.ncomp = d.ncomponents
         self.nhost = int(system["nhost"])
         h = C.c_void_p()
-        check(L.grx_box_create(C.byref(d), C.byref(h)), "grx_box_create")
+        if arena is None:
+            check(L.grx_box_create(C.byref(d), C.byref(h)), "grx_box_create")
+        else:
+            check(L.grx_box_create_in(C.byref(d), arena.h, C.byref(h)), "grx_box_create_in")
         self.h = h
-        for c in range(ncomp):
+        for c in range(self.ncomp):
             self.set_component(c)
 
     def close(self):
@@ -293,29 +367,7 @@ class Box:
             pass
 
     def set_component(self, c, rigid=None):
-        s = self.system
-        a0, a1 = s["comp_start"][c], s["comp_start"][c + 1]
-        n = a1 - a0
-        ms = int(s["molsize"][c])
-        pos = np.ascontiguousarray(np.asarray(s["pos"], dtype=np.float64)[a0:a1]).reshape(-1, 3)
-        q = np.ascontiguousarray(np.asarray(s["charge"], dtype=np.float64)[a0:a1])
-        ty = np.ascontiguousarray(np.asarray(s["type"])[a0:a1], dtype=np.uint64)
-        mol = np.ascontiguousarray(np.asarray(s["molid"])[a0:a1], dtype=np.uint64)
-        sc = np.ascontiguousarray(np.asarray(s["scale"], dtype=np.float64)[a0:a1])
-        scc = np.ascontiguousarray(np.asarray(s["scale_coul"], dtype=np.float64)[a0:a1])
-        stored = n
-        if n == 0 and c >= self.nhost and c in s.get("templates", {}):
-            # an empty adsorbate component still stores its molecule template
-            tm = s["templates"][c]
-            pos = np.ascontiguousarray(tm["pos"], dtype=np.float64)
-            q = np.ascontiguousarray(tm["charge"], dtype=np.float64)
-            ty = np.ascontiguousarray(tm["type"], dtype=np.uint64)
-            mol = np.zeros(ms, dtype=np.uint64)
-            sc = np.ones(ms)
-            scc = np.ones(ms)
-            stored = ms
-        pos = np.ascontiguousarray(pos.reshape(-1))
-        a = Atoms(_d(pos), _d(sc), _d(q), _d(scc), _sz(ty), _sz(mol), n, stored)
+        a, keep = component_atoms(self.system, c)
         if rigid is None:
             rigid = 1 if c >= self.nhost else 0
         check(self.L.grx_box_set_component(self.h, c, C.byref(a), int(rigid)), "grx_box_set_component")
@@ -455,6 +507,106 @@ class Box:
 
     def set_stream(self, stream_ptr):
         check(self.L.grx_box_set_stream(self.h, C.c_void_p(stream_ptr)), "grx_box_set_stream")
+
+
+class Arena:
+    """grx_arena: one reserved region of device memory that boxes are carved from."""
+
+    def __init__(self, nbytes):
+        self.L = load()
+        h = C.c_void_p()
+        check(self.L.grx_arena_create(int(nbytes), C.byref(h)), "grx_arena_create")
+        self.h = h
+
+    def usage(self):
+        u, lf, pk = C.c_size_t(), C.c_size_t(), C.c_size_t()
+        check(self.L.grx_arena_usage(self.h, C.byref(u), C.byref(lf), C.byref(pk)), "grx_arena_usage")
+        return u.value, lf.value, pk.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            check(self.L.grx_arena_destroy(self.h), "grx_arena_destroy")
+            self.h = None
+
+
+def box_footprint(system, capacity=None):
+    d, keep = box_desc(system, capacity)
+    n = C.c_size_t()
+    check(load().grx_box_footprint(C.byref(d), C.byref(n)), "grx_box_footprint")
+    return n.value
+
+
+class Server:
+    """grx_server: continuous-batching Widom / GCMC job server."""
+
+    def __init__(self, hbm_budget_bytes, max_resident, prec=GRX_MIXED, widom_slice=0, gcmc_slice=0):
+        self.L = load()
+        cfg = ServerConfig(int(hbm_budget_bytes), int(max_resident), int(prec), int(widom_slice), int(gcmc_slice))
+        h = C.c_void_p()
+        check(self.L.grx_server_create(C.byref(cfg), None, C.byref(h)), "grx_server_create")
+        self.h = h
+
+    def submit(self, system, capacity, kind, widom=None, insertions=0, gcmc=None, steps=0, tag=0):
+        """Copy one job (box + work) into the server's queue; returns its id."""
+        d, keep_d = box_desc(system, capacity)
+        ncomp = d.ncomponents
+        atoms = (Atoms * ncomp)()
+        keep = [keep_d]
+        for c in range(ncomp):
+            a, k = component_atoms(system, c)
+            atoms[c] = a
+            keep.append(k)
+        jd = JobDesc()
+        jd.kind = kind
+        jd.box = C.pointer(d)
+        jd.atoms = atoms
+        jd.rigid = C.POINTER(C.c_int32)()
+        if kind == JOB_WIDOM:
+            jd.widom = widom
+            jd.widom_insertions = int(insertions)
+        else:
+            gl = list(gcmc) if isinstance(gcmc, (list, tuple)) else [gcmc]
+            arr = (GcmcDesc * len(gl))(*gl)
+            keep.append(arr)
+            jd.gcmc = arr
+            jd.ncomp_moved = len(gl)
+            jd.gcmc_steps = int(steps)
+        jd.tag = int(tag)
+        jid = C.c_uint64()
+        check(self.L.grx_server_submit(self.h, C.byref(jd), C.byref(jid)), "grx_server_submit")
+        return jid.value
+
+    def progress(self):
+        r, p = C.c_int32(), C.c_int32()
+        check(self.L.grx_server_progress(self.h, C.byref(r), C.byref(p)), "grx_server_progress")
+        return r.value, p.value
+
+    def poll(self, max_results=256):
+        out = (JobResult * max_results)()
+        n = C.c_int32()
+        check(self.L.grx_server_poll(self.h, out, max_results, C.byref(n)), "grx_server_poll")
+        return [out[i] for i in range(n.value)]
+
+    def time(self):
+        t = C.c_double()
+        check(self.L.grx_server_time(self.h, C.byref(t)), "grx_server_time")
+        return t.value
+
+    def launches(self):
+        n = C.c_uint64()
+        check(self.L.grx_server_launch_count(self.h, C.byref(n)), "grx_server_launch_count")
+        return n.value
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.grx_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def beta_from_temperature(T):

@@ -43,7 +43,7 @@ def mix_lorentz_berthelot(eps_K, sigma, shifted, cutoff):
             sg = 0.5 * (sigma[i] + sigma[j])
             eps[i * n + j] = ep
             sig[i * n + j] = sg
-            if shifted[i] and shifted[j]:
+            if shifted[i] and shifted[j] and ep > 0.0 and sg > 0.0:
                 t = rc2 / (sg * sg)
                 rri3 = 1.0 / (t * t * t)
                 shift[i * n + j] = 4.0 * ep * (rri3 * (rri3 - 1.0))
@@ -297,3 +297,82 @@ def ch4_xe_system(seed, cutoff=12.0, n_atoms=None, n_ch4=0, n_xe=0):
     if n_xe:
         place_molecules(system, 2, n_xe, gg, min_dist=2.8)
     return system
+
+
+# ------------------------------------------------------------------ serving jobs
+KR_EPS_K, KR_SIGMA = 166.0, 3.64
+
+SPECIES = {
+    # name: list of (site, eps_K, sigma, charge, position); the first site is the CBMC first bead
+    "CH4": [("CH4", CH4_EPS_K, CH4_SIGMA, 0.0, (0.0, 0.0, 0.0))],
+    "Xe": [("Xe", XE_EPS_K, XE_SIGMA, 0.0, (0.0, 0.0, 0.0))],
+    "Kr": [("Kr", KR_EPS_K, KR_SIGMA, 0.0, (0.0, 0.0, 0.0))],
+    "CO2": [("C_co2", 27.0, 2.80, 0.70, (0.0, 0.0, 0.0)), ("O_co2", 79.0, 3.05, -0.35, (0.0, 0.0, 1.16)),
+            ("O_co2", 79.0, 3.05, -0.35, (0.0, 0.0, -1.16))],
+    "N2": [("N_n2", 36.0, 3.31, -0.482, (0.0, 0.0, -0.55)), ("N_n2", 36.0, 3.31, -0.482, (0.0, 0.0, 0.55)),
+           ("N_com", 0.0, 1.0, 0.964, (0.0, 0.0, 0.0))],   # charge site only (eps 0)
+}
+
+
+def raspa_ewald(cell, cutoff, precision=1e-6):
+    """Alpha, kmax and reciprocal cutoff from the Ewald precision, the automatic
+    set-up of read_Ewald_Parameters_from_input (read_data.cpp:689-700)."""
+    tol = math.sqrt(abs(math.log(precision * cutoff)))
+    alpha = math.sqrt(abs(math.log(precision * cutoff * tol))) / cutoff
+    tol1 = math.sqrt(-math.log(precision * cutoff * (2.0 * tol * alpha) ** 2))
+    kmax = [int(round(0.25 + cell[k] * alpha * tol1 / math.pi)) for k in (0, 4, 8)]
+    return alpha, kmax, (1.05 * max(kmax)) ** 2
+
+
+def adsorbate_system(species, seed, n_atoms=None, cutoff=12.0, n_guest=0):
+    """One box of `species` (a key of SPECIES) on lj_framework(seed, n_atoms). Charged
+    species get framework charges U[-1.2, +1.4] e, neutralised, and the automatic Ewald
+    set-up at precision 1e-6; the others run with charges off."""
+    cell, fw, ft, eps_fw, sig_fw = lj_framework(seed, cutoff=cutoff, n_atoms=n_atoms)
+    sites = SPECIES[species]
+    charged = any(q != 0.0 for (_, _, _, q, _) in sites)
+    g = _rng(seed + 7919)
+    nt_fw = len(eps_fw)
+    names, eps_K, sig, idx = [], list(eps_fw), list(sig_fw), []
+    for name, e, s_, _, _ in sites:
+        if name not in names:
+            names.append(name)
+            eps_K.append(e)
+            sig.append(s_)
+        idx.append(nt_fw + names.index(name))
+    eps, sg, shift = mix_lorentz_berthelot(eps_K, sig, [1] * len(eps_K), cutoff)
+    if charged:
+        q = g.uniform(-1.2, 1.4, len(fw))
+        q -= q.mean()
+        alpha, kmax, rc = raspa_ewald(cell, cutoff)
+    else:
+        q = np.zeros(len(fw))
+        alpha, kmax, rc = 0.265, [1, 1, 1], None
+    tmpl = dict(pos=np.array([p for (_, _, _, _, p) in sites]), charge=np.array([c for (_, _, _, c, _) in sites]),
+                type=np.array(idx))
+    system = dict(
+        name=f"{species}_{seed}", cell=cell, kmax=kmax, alpha=alpha, use_lammps_ewald=0, reciprocal_cutoff=rc,
+        prefactor=COULOMB_PREFACTOR, ntypes=len(eps_K), epsilon=eps, sigma=sg, shift=shift, cutoff_vdw=cutoff,
+        cutoff_coul=cutoff, overlap_criteria=1e6, no_charges=0 if charged else 1, vdw_real_bias=1,
+        temperature=300.0, nhost=1, molsize=[len(fw), len(sites)], templates={1: tmpl})
+    _set_atoms(system, fw, ft, q, [np.zeros((0, 3))])
+    if n_guest:
+        place_molecules(system, 1, n_guest, g, min_dist=2.8)
+    return system
+
+
+def serving_job(seed, widom_insertions=5000, gcmc_cycles=2000, steps_per_cycle=20, n_atoms_range=(200, 20000)):
+    """One job of the serving stream: species uniform over CH4, CO2, N2, Xe, Kr; Widom
+    (widom_insertions) or GCMC (gcmc_cycles x steps_per_cycle steps) with equal odds;
+    framework atoms log-uniform in n_atoms_range. Returns a dict with the system,
+    capacities and the work."""
+    g = _rng(10_000_019 + seed)
+    species = ["CH4", "CO2", "N2", "Xe", "Kr"][int(g.integers(0, 5))]
+    kind = "widom" if g.uniform() < 0.5 else "gcmc"
+    lo, hi = n_atoms_range
+    n_atoms = int(round(math.exp(g.uniform(math.log(lo), math.log(hi)))))
+    system = adsorbate_system(species, seed, n_atoms=n_atoms)
+    ms = int(system["molsize"][1])
+    return dict(seed=seed, species=species, kind=kind, n_atoms=len(system["pos"]), system=system,
+                capacity=[system["comp_start"][1], ms * 256], widom_insertions=widom_insertions,
+                gcmc_steps=gcmc_cycles * steps_per_cycle)

@@ -193,6 +193,23 @@ grx_status grx_device_count(int32_t* n);
  * fxn_main.h:46-113,163-280 / main.cpp:243-300). */
 grx_status grx_box_create(const grx_box_desc* desc, grx_box** out);
 grx_status grx_box_destroy(grx_box* box);
+
+/* ---- device memory arena -------------------------------------------------- */
+/* One reserved region of device memory that boxes are carved from by a host-side
+ * first-fit allocator (256-byte granules). A box created in an arena takes every
+ * device allocation from it and returns them at grx_box_destroy without cudaFree,
+ * so retiring a box does not wait on the device; a box that does not fit fails with
+ * GRX_ERR_OUT_OF_MEMORY and nothing allocated. No counterpart in the reference (it
+ * sizes one simulation per process); it is the admission resource of the serving
+ * loop. */
+typedef struct grx_arena grx_arena;
+grx_status grx_arena_create(size_t bytes, grx_arena** out);
+grx_status grx_arena_destroy(grx_arena* arena);      /* every box in it destroyed first */
+grx_status grx_arena_usage(grx_arena* arena, size_t* in_use, size_t* largest_free, size_t* peak);
+grx_status grx_box_create_in(const grx_box_desc* desc, grx_arena* arena, grx_box** out);
+/* Upper estimate of the device bytes a box of this description takes, including its
+ * first scratch and Widom result buffers. */
+grx_status grx_box_footprint(const grx_box_desc* desc, size_t* bytes);
 /* All later work of the box goes to this stream (cudaStream_t, NULL = default). */
 grx_status grx_box_set_stream(grx_box* box, void* cuda_stream);
 
@@ -364,6 +381,66 @@ grx_status grx_gcmc_batch_reset_stats(grx_gcmc_batch* batch);
  * Monte Carlo steps and advance the chains. */
 grx_status grx_gcmc_batch_autotune(grx_gcmc_batch* batch, int64_t nsteps, int32_t* chosen,
                                    float* ms_per_candidate);
+
+/* ---- serving ----------------------------------------------------------------- */
+/* A continuous-batching job server. Each job is one box (its description and atoms,
+ * copied at submission) with Widom insertions or GCMC steps to run. The caller's loop
+ * calls grx_server_progress, which in one non-blocking round retires finished jobs,
+ * admits queued jobs in arrival order while a slot is free and the job's box fits in
+ * the server's device memory arena (admission by HBM footprint), and launches the next
+ * slice of every resident job on the job's own stream, so the work of different jobs
+ * overlaps on the device. A job's result does not depend on the other jobs. No
+ * counterpart in the reference (one simulation per process). */
+#define GRX_JOB_WIDOM 0
+#define GRX_JOB_GCMC 1
+
+typedef struct {
+  size_t hbm_budget_bytes;      /* arena size when the server makes its own arena */
+  int32_t max_resident;         /* job slots */
+  grx_precision precision;
+  int64_t widom_slice;          /* insertions per launch (<= 0: whole job) */
+  int64_t gcmc_slice;           /* steps per launch (<= 0: whole job) */
+} grx_server_config;
+
+typedef struct {
+  int32_t kind;                 /* GRX_JOB_WIDOM or GRX_JOB_GCMC */
+  int32_t ncomp_moved;          /* GCMC: entries of gcmc (1..4) */
+  const grx_box_desc* box;
+  const grx_atoms* atoms;       /* box->ncomponents entries (empty adsorbates store their template) */
+  const int32_t* rigid;         /* per component, NULL: adsorbate components rigid */
+  grx_widom_desc widom;
+  int64_t widom_insertions;
+  const grx_gcmc_desc* gcmc;
+  int64_t gcmc_steps;
+  uint64_t tag;                 /* returned with the result */
+} grx_job_desc;
+
+typedef struct {
+  uint64_t tag;
+  uint64_t job_id;
+  int32_t kind;
+  int32_t status;               /* grx_status of the job */
+  double t_submit, t_admit, t_done;   /* seconds on the server clock */
+  size_t footprint_bytes;       /* arena bytes the job held */
+  int64_t widom_n;
+  double widom_mean_w;          /* <W> over the insertions (failed constructions count as 0) */
+  double widom_mean_w2;         /* <W^2> */
+  int64_t gcmc_steps;
+  int32_t ncomp_moved;
+  int32_t pad_;
+  grx_gcmc_stats gcmc[4];
+} grx_job_result;
+
+typedef struct grx_server grx_server;
+/* arena: NULL to make one of cfg->hbm_budget_bytes owned by the server. */
+grx_status grx_server_create(const grx_server_config* cfg, grx_arena* arena, grx_server** out);
+grx_status grx_server_destroy(grx_server* server);
+grx_status grx_server_submit(grx_server* server, const grx_job_desc* job, uint64_t* job_id);
+grx_status grx_server_progress(grx_server* server, int32_t* n_resident, int32_t* n_pending);
+/* Moves up to max finished jobs' results into out; *n = how many. */
+grx_status grx_server_poll(grx_server* server, grx_job_result* out, int32_t max, int32_t* n);
+grx_status grx_server_time(grx_server* server, double* seconds);
+grx_status grx_server_launch_count(grx_server* server, uint64_t* launches);
 
 /* ---- allocation-free trial energies ------------------------------------- */
 /* grx_trial_energies without any device allocation at call time. No counterpart
