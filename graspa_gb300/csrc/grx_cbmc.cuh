@@ -119,7 +119,7 @@ template <int PREC>
 __device__ __forceinline__ void trial_pass(const BoxDev& b, CbmcWork& W, int nb, int chain, int comp, int newmol) {
   if (threadIdx.x == 0) W.counter = 0;
   __syncthreads();
-  const int nch = chunks_for(nb, b.ntiles, GRX_THREADS / 32, b.chunk_mult);
+  const int nch = chunks_for(nb, work_tiles(b), GRX_THREADS / 32, b.chunk_mult);
   block_bead_pass<PREC>(b, W.beads, nb, comp, newmol, -1, -1, W.qbuf, W.ipart, W.iflag, &W.counter, nch);
   __syncthreads();
   reduce_items<PREC>(W.ipart, W.iflag, nb / chain, chain, nch, W.te, W.tflag);

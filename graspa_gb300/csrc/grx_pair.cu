@@ -21,7 +21,7 @@ __global__ void __launch_bounds__(GRX_THREADS) trial_bead_kernel(BoxDev b, const
   __shared__ int counter;
   if (threadIdx.x == 0) counter = 0;
   __syncthreads();
-  const int nch = chunks_for(1, b.ntiles, GRX_THREADS / 32);
+  const int nch = chunks_for(1, work_tiles(b), GRX_THREADS / 32);
   block_bead_pass<PREC>(b, beads + blockIdx.x, 1, component, newmol, excl_comp, excl_mol, qbuf, ipart, iflag,
                         &counter, nch);
   __syncthreads();

@@ -196,7 +196,7 @@ __device__ __forceinline__ void pair_dense(const BoxDev& b, int i, const Bead& b
 // guest atom. acc = {hg_vdw, hg_real, gg_vdw, gg_real} (valid on every lane, summed
 // later); flag is per lane.
 template <int PREC>
-__device__ __forceinline__ void warp_item(const BoxDev& b, const Bead& bd, int t0, int t1, bool guests,
+__device__ __forceinline__ void warp_item(const BoxDev& b, const Bead& bd, int t0, int t1, int g0, int g1,
                                           int component, int newmol, int excl_comp, int excl_mol, int* q,
                                           LaneAcc<PREC>& hacc, LaneAcc<PREC>& gacc, int& flag) {
   const int lane = threadIdx.x & 31;
@@ -293,16 +293,20 @@ __device__ __forceinline__ void warp_item(const BoxDev& b, const Bead& bd, int t
   __syncwarp();
   if (lane < (int)(tail - head)) pair_dense<PREC>(b, q[(head + lane) & (kQueue - 1)], bd, pq, la, flag);
   __syncwarp();
-  if (!guests) return;
+  if (g1 <= g0) return;
   head = tail = 0;
-  for (int c = b.nhost; c < b.ncomp; ++c) {
+  // guest atoms [g0, g1) of the concatenated adsorbate components
+  for (int c = b.nhost, base = 0; c < b.ncomp && base < g1; ++c) {
     const int n = b.comp_size[c];
     const int off = b.comp_off[c];
+    const int lo = max(g0 - base, 0), hi = min(g1 - base, n);
+    base += n;
+    if (hi <= lo) continue;
     const bool check = (c == component) || (c == excl_comp);
-    for (int i0 = 0; i0 < n; i0 += 32) {
+    for (int i0 = lo; i0 < hi; i0 += 32) {
       const int i = off + i0 + lane;
       bool in = false;
-      if (i0 + lane < n) {
+      if (i0 + lane < hi) {
         bool skip = false;
         if (check) {
           const int mol = b.meta[i].y;
@@ -366,7 +370,16 @@ __device__ __forceinline__ void warp_store(const LaneAcc<PREC>& h, const LaneAcc
   }
 }
 
-// Host-tile chunks per bead so that a pass has at least ~4 items per warp.
+// Live adsorbate atoms of the box, and the 32-atom work units a bead pass covers
+// (host tiles plus guest atoms in groups of 32).
+__device__ __forceinline__ int guest_atoms(const BoxDev& b) {
+  int g = 0;
+  for (int c = b.nhost; c < b.ncomp; ++c) g += b.comp_size[c];
+  return g;
+}
+__device__ __forceinline__ int work_tiles(const BoxDev& b) { return b.ntiles + (guest_atoms(b) + 31) / 32; }
+
+// Chunks per bead so that a pass has at least ~4 items per warp.
 __host__ __device__ __forceinline__ int chunks_for(int nb, int ntiles, int nwarps, int mult = 4) {
   int c = (mult * nwarps + nb - 1) / nb;
   if (c > ntiles) c = ntiles;
@@ -387,6 +400,7 @@ __device__ __forceinline__ void block_bead_pass(const BoxDev& b, const Bead* bea
   int* q = qbuf + warp * kQueue;
   const int items = nb * nchunk;
   const int nt = b.ntiles;
+  const int ng = guest_atoms(b);
   for (;;) {
     int item = 0;
     if (lane == 0) item = atomicAdd(counter, 1);
@@ -394,14 +408,13 @@ __device__ __forceinline__ void block_bead_pass(const BoxDev& b, const Bead* bea
     if (item >= items) break;
     const int bead = item / nchunk, chunk = item - bead * nchunk;
     const int t0 = (int)((long long)nt * chunk / nchunk), t1 = (int)((long long)nt * (chunk + 1) / nchunk);
+    const int g0 = (int)((long long)ng * chunk / nchunk), g1 = (int)((long long)ng * (chunk + 1) / nchunk);
     const Bead bd = beads[bead];
     LaneAcc<PREC> hacc, gacc;
     int flag = 0;
-    warp_item<PREC>(b, bd, t0, t1, chunk == nchunk - 1, component, newmol, excl_comp, excl_mol, q, hacc, gacc,
-                    flag);
+    warp_item<PREC>(b, bd, t0, t1, g0, g1, component, newmol, excl_comp, excl_mol, q, hacc, gacc, flag);
     const unsigned fm = __ballot_sync(kFull, flag != 0);
-    warp_store<PREC>(hacc, gacc, ipart + item * 4, df{bd.pq.x, bd.pq.y},
-                     chunk == nchunk - 1 && b.comp_off[b.ncomp] > b.host_end);
+    warp_store<PREC>(hacc, gacc, ipart + item * 4, df{bd.pq.x, bd.pq.y}, g1 > g0);
     if (lane == 0) iflag[item] = fm ? 1 : 0;
   }
 }

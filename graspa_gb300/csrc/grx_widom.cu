@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(GRX_THREADS, 3) widom_kernel(BoxDev b, WidomAr
     __syncthreads();
     // 2. pair energies of the first-bead trials
     {
-      const int nch = chunks_for(nt, b.ntiles, GRX_THREADS / 32);
+      const int nch = chunks_for(nt, work_tiles(b), GRX_THREADS / 32);
       block_bead_pass<PREC>(b, beads, nt, a.comp, a.newmol, -1, -1, qbuf, ipart, iflag, &counter, nch);
       __syncthreads();
       reduce_items<PREC>(ipart, iflag, nt, 1, nch, te, tflag);
@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(GRX_THREADS, 3) widom_kernel(BoxDev b, WidomAr
       if (tid == 0) counter = 0;
       __syncthreads();
       // 5. pair energies of the orientations
-      const int nch = chunks_for(nb, b.ntiles, GRX_THREADS / 32);
+      const int nch = chunks_for(nb, work_tiles(b), GRX_THREADS / 32);
       block_bead_pass<PREC>(b, beads, nb, a.comp, a.newmol, -1, -1, qbuf, ipart, iflag, &counter, nch);
       __syncthreads();
       reduce_items<PREC>(ipart, iflag, no, chain, nch, te, tflag);

@@ -376,3 +376,59 @@ def serving_job(seed, widom_insertions=5000, gcmc_cycles=2000, steps_per_cycle=2
     return dict(seed=seed, species=species, kind=kind, n_atoms=len(system["pos"]), system=system,
                 capacity=[system["comp_start"][1], ms * 256], widom_insertions=widom_insertions,
                 gcmc_steps=gcmc_cycles * steps_per_cycle)
+
+
+# ------------------------------------------------------------------ TIP4P-Ew water
+def tip4p_ew_template():
+    """TIP4P-Ew: O (81.899 K, 3.16435 A, no charge) first, then H, H (+0.52422) and the
+    massless M site (-1.04844) 0.125 A from O on the bisector; O-H 0.9572 A, HOH 104.52
+    deg."""
+    th = math.radians(104.52 / 2.0)
+    h = 0.9572
+    pos = np.array([[0.0, 0.0, 0.0], [h * math.sin(th), 0.0, h * math.cos(th)],
+                    [-h * math.sin(th), 0.0, h * math.cos(th)], [0.0, 0.0, 0.125]])
+    return dict(pos=pos, charge=np.array([0.0, 0.52422, 0.52422, -1.04844]), names=["Ow", "Hw", "Hw", "Mw"])
+
+
+def tip4p_hex_system(seed=42, n_water=0, cutoff=11.0, alpha=0.30, kmax=(10, 10, 8), cells=(1, 1, 4),
+                     n_per_cell=216, n_types=4, channel_r=6.0):
+    """Charge-dominated Ewald benchmark: TIP4P-Ew water in a synthetic hexagonal
+    framework, a = b = 25.9 A, c = 6.9 A, gamma = 120 deg, 1 x 1 x 4 cells (864 atoms)
+    on a jittered fractional lattice with random vacancies around one open channel
+    (radius channel_r) along c. Framework charges
+    U[-1.2, +1.4] e neutralised; LJ eps/k U[20, 100] K, sigma U[2.5, 3.5] A. The
+    perpendicular width of this cell is 22.4 A, so the cutoff is 11 A (< width / 2);
+    Ewald alpha 0.30 A^-1 with kmax 10/10/8 (explicit set-up)."""
+    g = _rng(seed)
+    base = np.array(triclinic_cell(25.9, 25.9, 6.9, 90.0, 90.0, 120.0)).reshape(3, 3).T
+    grid = np.array([9, 9, 4])
+    idx = np.stack(np.meshgrid(*[np.arange(k) for k in grid], indexing="ij"), -1).reshape(-1, 3)
+    frac = (idx + 0.5) / grid
+    # one open channel along c through the cell corner (radius channel_r): the
+    # framework atoms fill the rest, as the walls of a hexagonal channel framework
+    d = frac[:, :2] - np.round(frac[:, :2])
+    r_xy = np.linalg.norm(np.c_[d, np.zeros(len(d))] @ base.T, axis=1)
+    keep = np.where(r_xy > channel_r)[0]
+    sel = keep[g.choice(len(keep), n_per_cell, replace=False)]
+    frac = (idx[sel] + 0.5 + g.uniform(-0.15, 0.15, (n_per_cell, 3))) / grid
+    pts = frac @ base.T
+    shifts = np.stack(np.meshgrid(*[np.arange(k) for k in cells], indexing="ij"), -1).reshape(-1, 3)
+    fw = (pts[None, :, :] + (shifts @ base.T)[:, None, :]).reshape(-1, 3)
+    ft = np.tile(g.integers(0, n_types, n_per_cell), len(shifts))
+    q = g.uniform(-1.2, 1.4, len(fw))
+    q -= q.mean()
+    cell = (base * np.array(cells)[None, :]).T.reshape(-1).tolist()
+    eps_K = list(g.uniform(20.0, 100.0, n_types)) + [81.899, 0.0, 0.0]
+    sig = list(g.uniform(2.5, 3.5, n_types)) + [3.16435, 1.0, 1.0]
+    eps, sg, shift = mix_lorentz_berthelot(eps_K, sig, [1] * len(eps_K), cutoff)
+    tm = tip4p_ew_template()
+    tm["type"] = np.array([n_types, n_types + 1, n_types + 1, n_types + 2])
+    system = dict(
+        name="tip4p_hex", cell=cell, kmax=list(kmax), alpha=alpha, use_lammps_ewald=1, prefactor=COULOMB_PREFACTOR,
+        ntypes=len(eps_K), epsilon=eps, sigma=sg, shift=shift, cutoff_vdw=cutoff, cutoff_coul=cutoff,
+        overlap_criteria=1e6, no_charges=0, vdw_real_bias=1, temperature=300.0, nhost=1, molsize=[len(fw), 4],
+        templates={1: tm})
+    _set_atoms(system, fw, ft, q, [np.zeros((0, 3))])
+    if n_water:
+        place_molecules(system, 1, n_water, g, min_dist=2.5)
+    return system
