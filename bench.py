@@ -1,27 +1,37 @@
-"""Benchmark: CBMC trial energies/s on one GB300 (batched mixed precision vs plain FP64).
+"""Benchmark: CBMC trial energies/s on one GB300, mixed precision vs plain FP64,
+with the p50 / p99 job latency of the serving form.
 
-Workload (one "step"): 20,000 CBMC Widom insertions of rigid CO2 into the
+Headline workload (`--workload gcmc`, the default): GCMC of rigid CO2 in the
 synthetic all-silica framework (2x2x3 cells of 20.09 x 19.74 x 13.14 A, 3456
-atoms), 10 first-bead trial positions + 10 trial orientations per insertion,
-shifted LJ + real-space Coulomb at 12 A, Ewald alpha 0.265 with kmax 9/9/6,
-T = 300 K, Philox seed 42. One step evaluates 400,000 trial energies
-(2.07e9 pair evaluations) plus 20,000 Ewald deltas.
+atoms; shifted LJ + real Coulomb at 12 A; Ewald alpha 0.265, kmax 9/9/6) at 300 K
+and 1e5 Pa (fugacity coefficient 1): translation : rotation : CBMC insertion :
+CBMC deletion = 1:1:1:1, 10 trial positions and 10 orientations, boxes starting
+empty (0-120 molecules). Independent Markov chains (three per SM, different Philox
+streams) run in one persistent launch replayed as a CUDA graph; one benchmark
+"step" is S Monte Carlo steps of every chain. A trial energy is one trial
+configuration against every atom (2 per translation / rotation, 20 per CBMC
+insertion or deletion of CO2).
 
-`value`  : trial energies/s of the batched mixed-precision form, inputs resident.
-`e2e`    : the same metric through the C ABI with host buffers (framework upload
-           from pinned host memory, results read back), per step.
-`fp64`   : the plain FP64 single-box form of the same workload (the denominator
-           of the >= 5x target).
-Reference arm (--impl reference): the FP64 CPU implementation of the same
-routines (the test oracle, OpenMP on all host cores) on a bounded sample.
+  value      trial energies/s of the batched mixed-precision form, state resident
+  fp64       the same batch in FP64, and the plain FP64 single-box form
+  e2e        the same metric through the public C ABI (grx_gcmc_run) per step: move
+             descriptors uploaded, statistics read back, host synchronised
+  accuracy   energy drift (FP64 recomputed totals vs accepted energies), loading,
+             and mixed-vs-FP64 decisions and energies per move
+  widom      the configs[0]-style Widom workload (20,000 CO2 insertions per step)
+  serving    a bounded Poisson job stream through grx_server: jobs/s, p50 / p99
+             latency, next to the one-job-at-a-time FP64 form
+Reference arm (--impl reference): the FP64 C++ oracle of the same moves, one chain
+per host thread on all host cores, on a bounded sample.
 """
 import argparse
+import concurrent.futures
 import json
+import math
 import os
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 import numpy as np
@@ -29,11 +39,12 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-N_INSERT = 20000
 NTRIALS = 10
 NORIENT = 10
-FLOP_PER_PAIR_CHARGED = 70.0   # FP32-equivalent work model per pair (LJ + real Coulomb)
+FLOP_PER_PAIR_CHARGED = 70.0   # FP32-equivalent work per pair (LJ + real Coulomb), the frozen work model
+FLOP_PER_PAIR_LJ = 40.0
 L2_FLUSH_BYTES = 256 << 20
+PEAK_FP32_NOMINAL = 152 * 128 * 2 * 2070e6 / 1e12   # TFLOP/s; no measured FP32 figure exists
 
 
 def dist_env():
@@ -94,18 +105,237 @@ class ClockSampler:
         return out
 
 
-def make_workload():
+# ------------------------------------------------------------------ workloads
+def co2_system():
     from graspa_gb300 import synth
     return synth.silica_co2(seed=42)
 
 
-def pairs_per_insertion(system):
-    n_atoms = system["comp_start"][-1]
-    chain = system["molsize"][1] - 1
-    return (NTRIALS + NORIENT * chain) * n_atoms
+def gcmc_descs(grx, n, seed=42):
+    """configs[1] move set: translation : rotation : insertion : deletion = 1:1:1:1."""
+    return [grx.gcmc_desc(1, ntrials=NTRIALS, norient=NORIENT, p_translation=0.25, p_rotation=0.5,
+                          p_reinsertion=0.5, p_swap=1.0, pressure_pa=1e5, seed=seed, stream=k) for k in range(n)]
 
 
-def oracle_setup(system):
+def work_of(stats, ms, nfw):
+    """(trial energies, pair evaluations) of a list of GCMC statistics. Pairs are
+    beads x (framework atoms + guest atoms at the run's mean loading)."""
+    chain = ms - 1
+    g_te = NTRIALS + (NORIENT if chain else 0)
+    g_beads = NTRIALS + NORIENT * chain
+    te = pairs = 0.0
+    for st in stats:
+        a = list(st.attempts)
+        te += 2 * (a[0] + a[1]) + g_te * (a[2] + a[3]) + (g_te + 1 + (NORIENT if chain else 0)) * a[4]
+        beads = 2 * ms * (a[0] + a[1]) + g_beads * (a[2] + a[3]) + (g_beads + 1 + NORIENT * chain) * a[4]
+        steps = max(1, sum(a))
+        guests = ms * st.sum_n / max(steps, 1)
+        pairs += beads * (nfw + guests)
+    return te, pairs
+
+
+def make_boxes(grx, system, n, stream_ptr, cap_molecules=160):
+    nfw = system["comp_start"][1]
+    ms = int(system["molsize"][1])
+    boxes = []
+    for _ in range(n):
+        b = grx.Box(system, capacity=[nfw, ms * cap_molecules])
+        b.set_stream(stream_ptr)
+        b.ewald_total()
+        boxes.append(b)
+    return boxes
+
+
+def total_energy(box):
+    return sum(box.total_energy().values())
+
+
+# ------------------------------------------------------------------ GPU arm
+def timed_graph(torch, batch, stream, S, steps, warmup, flush, dist=None):
+    """CUDA-event time of `steps` graph replays of S Monte Carlo steps each (L2
+    flushed before each), after `warmup` replays."""
+    for _ in range(warmup):
+        batch.run_graph(S, 1, stream.cuda_stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    warm_stats, _ = batch.stats()
+    batch.reset_stats()
+    times = []
+    for _ in range(steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        batch.run_graph(S, 1, stream.cuda_stream)
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) / 1000.0)
+    torch.cuda.synchronize()
+    stats, _ = batch.stats()
+    timed_graph.warm_stats = warm_stats
+    return times, stats
+
+
+def bench_gcmc(args, grx, torch, stream, flush, rank, world, dist):
+    system = co2_system()
+    nfw = system["comp_start"][1]
+    ms = int(system["molsize"][1])
+    R = args.chains or 3 * torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    S = args.mc_steps
+    descs = gcmc_descs(grx, R, seed=42 + 1000 * rank)
+    out = {"chains": R, "mc_steps_per_step": S}
+
+    # mixed, batched: the headline
+    boxes = make_boxes(grx, system, R, stream.cuda_stream)
+    n_drift = min(8, R)
+    e0 = [total_energy(b) for b in boxes[:n_drift]]
+    for b in boxes[:n_drift]:
+        b.ewald_total()
+    batch = grx.GcmcBatch(boxes, descs, grx.GRX_MIXED)
+    chunk, cand = batch.autotune(10)   # real steps; picks the bead-pass work split for this batch
+    out["autotune"] = {"chunk_mult": chunk, "ms_per_candidate": cand}
+    l0 = grx.launch_count()
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    times, stats = timed_graph(torch, batch, stream, S, args.steps, args.warmup, flush, dist)
+    clk = clocks.stop()
+    launches = grx.launch_count() - l0
+    tot = sum(times)
+    if dist:
+        t = torch.tensor([tot], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        tot = float(t.item())
+    te, pairs = work_of(stats, ms, nfw)
+    out.update(value=te * world / tot, seconds=tot, times=times, trial_energies=te, pairs=pairs, clocks=clk,
+               launches=launches)
+    warm = timed_graph.warm_stats
+    acc_stats, nxt = batch.stats()
+    batch.close()
+    if args.profile:
+        for b in boxes:
+            b.close()
+        return out
+    # drift and loading of the timed chains (all steps since creation)
+    drift = []
+    beta = grx.beta_from_temperature(300.0)
+    for i, b in enumerate(boxes[:n_drift]):
+        e1 = total_energy(b)
+        drift.append(abs((e1 - e0[i]) - (warm[i].energy[3] + acc_stats[i].energy[3])))
+    loading = float(np.mean([st.n_molecules for st in acc_stats]))
+    out["accuracy"] = {
+        "drift_max_beta_abs": float(beta * max(drift)), "drift_max_abs_internal": float(max(drift)),
+        "drift_chains": n_drift, "drift_steps": int(nxt),
+        "loading_mean_molecules": loading,
+        "acceptance": [float(sum(st.accepted[k] for st in acc_stats) / max(1, sum(st.attempts[k] for st in acc_stats)))
+                       for k in range(4)],
+    }
+    for b in boxes:
+        b.close()
+
+    # the same batch in FP64
+    boxes = make_boxes(grx, system, R, stream.cuda_stream)
+    batch = grx.GcmcBatch(boxes, descs, grx.GRX_FP64)
+    k64 = max(1, min(args.steps, 3))
+    t64, st64 = timed_graph(torch, batch, stream, S, k64, 1, flush)
+    te64, _ = work_of(st64, ms, nfw)
+    batch.close()
+    for b in boxes:
+        b.close()
+    # the plain FP64 single-box form
+    box1 = make_boxes(grx, system, 1, stream.cuda_stream)
+    batch = grx.GcmcBatch(box1, descs[:1], grx.GRX_FP64)
+    t1, st1 = timed_graph(torch, batch, stream, S, 3, 1, flush)
+    te1, _ = work_of(st1, ms, nfw)
+    batch.close()
+    box1[0].close()
+    out["fp64"] = {"batched_value": te64 / sum(t64), "single_box_value": te1 / sum(t1),
+                   "single_box_mc_steps_per_s": 3 * S / sum(t1),
+                   "speedup_mixed_over_fp64_batched": out["value"] / (te64 / sum(t64)),
+                   "speedup_batched_mixed_over_fp64_single_box": out["value"] / (te1 / sum(t1))}
+
+    # per-move agreement: the same 8 chains from the same state, FP64 vs mixed
+    n_cmp = min(8, R)
+    res = {}
+    for name, p in (("fp64", grx.GRX_FP64), ("mixed", grx.GRX_MIXED)):
+        bx = make_boxes(grx, system, n_cmp, stream.cuda_stream)
+        res[name] = grx.gcmc_run(bx, descs[:n_cmp], 0, 300, p)
+        for b in bx:
+            b.close()
+    same = [list(a.accepted) == list(b.accepted) and a.n_molecules == b.n_molecules
+            for a, b in zip(res["fp64"], res["mixed"])]
+    rel = [abs(a.energy[3] - b.energy[3]) / max(abs(b.energy[3]), 1.0 / beta)
+           for a, b in zip(res["mixed"], res["fp64"]) if list(a.accepted) == list(b.accepted)]
+    out["accuracy"].update(chains_identical_decisions_300_steps=f"{sum(same)}/{n_cmp}",
+                           max_rel_energy_sum_vs_fp64=float(max(rel)) if rel else None)
+
+    # end to end through the public C ABI (synchronous grx_gcmc_run per step)
+    boxes = make_boxes(grx, system, R, stream.cuda_stream)
+    e2e = []
+    step0 = 0
+    te_e2e = 0.0
+    for i in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        st = grx.gcmc_run(boxes, descs, step0, S, grx.GRX_MIXED)
+        dt = time.perf_counter() - t0
+        step0 += S
+        if i >= args.warmup:
+            e2e.append(dt)
+            te_e2e += work_of(st, ms, nfw)[0]
+    for b in boxes:
+        b.close()
+    desc_bytes = R * 160 + 8
+    out["e2e"] = {"value": te_e2e * world / sum(e2e), "unit": "trial_energies/s",
+                  "h2d_bytes_per_step": desc_bytes, "d2h_bytes_per_step": R * 136}
+    return out
+
+
+def bench_widom(args, grx, torch, stream, flush, n_insert):
+    system = co2_system()
+    nfw = system["comp_start"][1]
+    box = grx.Box(system, capacity=[nfw, 3 * 64])
+    box.set_stream(stream.cuda_stream)
+    box.ewald_total()
+    d = grx.widom_desc(system, 1, NTRIALS, NORIENT, seed=42)
+    res_dev = torch.empty(n_insert * grx.WIDOM_RESULT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
+    te_step = (NTRIALS + NORIENT) * n_insert
+    pairs_step = (NTRIALS + 2 * NORIENT) * system["comp_start"][-1] * n_insert
+
+    def run(p, steps, warmup, move):
+        for _ in range(warmup):
+            box.widom_async(d, move, n_insert, p, res_dev.data_ptr())
+            move += n_insert
+        torch.cuda.synchronize()
+        times = []
+        for _ in range(steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            box.widom_async(d, move, n_insert, p, res_dev.data_ptr())
+            e1.record(stream)
+            move += n_insert
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1) / 1000.0)
+        return times
+
+    tm = run(grx.GRX_MIXED, args.widom_steps, 2, 0)
+    t64 = run(grx.GRX_FP64, 2, 1, 10 ** 8)
+    acc = widom_accuracy(box, grx, system)
+    box.close()
+    t_launch = float(np.mean(tm))
+    achieved = FLOP_PER_PAIR_CHARGED * pairs_step / t_launch / 1e12
+    return {"workload": f"widom_co2_silica_3456, {n_insert} insertions per launch",
+            "value": te_step * len(tm) / sum(tm), "unit": "trial_energies/s",
+            "fp64_value": te_step * len(t64) / sum(t64),
+            "speedup_mixed_over_fp64": (te_step * len(tm) / sum(tm)) / (te_step * len(t64) / sum(t64)),
+            "kernel_ms": 1000 * t_launch, "achieved_tflops": achieved, "frac_of_nominal_fp32": achieved / PEAK_FP32_NOMINAL,
+            "accuracy_vs_fp64_oracle": acc}
+
+
+def widom_accuracy(box, grx, system, n=200):
+    """Mixed / FP32 vs the FP64 oracle on the first n insertions of the stream."""
     from oracle import oracle as O
     S = O.OracleSystem(system)
     _, s_fw, s_ads = S.ewald_total(list(system["molsize"]))
@@ -114,7 +344,6 @@ def oracle_setup(system):
     mq = np.ascontiguousarray(tm["charge"], dtype=np.float64)
     mt = np.ascontiguousarray(tm["type"], dtype=np.int64)
     intra, self_ = S.rigid_exclusion(mp, mq, np.ones(3))
-    from graspa_gb300 import grx
     w = O.OraWidom()
     w.component, w.molsize = 1, 3
     w.mol_pos, w.mol_charge, w.mol_type = O._d(mp), O._d(mq), O._i(mt)
@@ -124,68 +353,6 @@ def oracle_setup(system):
     w.excl_intra, w.excl_self = intra, self_
     w.rigid, w.has_charge = 1, 1
     w.seed, w.stream = 42, 0
-    return S, s_fw, s_ads, w, (mp, mq, mt)
-
-
-def cpu_rate(system, seconds, first_move=10 ** 9):
-    """Time the FP64 OpenMP oracle on a bounded sample; returns (trial energies/s, sample, cores)."""
-    from oracle import oracle as O
-    S, s_fw, s_ads, w, keep = oracle_setup(system)
-    cores = int(O.lib().ora_max_threads())
-    n = max(cores, 16)
-    t0 = time.perf_counter()
-    S.widom(w, s_fw, s_ads, first_move, n)
-    dt = time.perf_counter() - t0
-    n2 = int(max(n, min(200000, n * seconds / max(dt, 1e-6))))
-    t0 = time.perf_counter()
-    S.widom(w, s_fw, s_ads, first_move + n, n2)
-    dt2 = time.perf_counter() - t0
-    return (NTRIALS + NORIENT) * n2 / dt2, n2, cores, dt2
-
-
-def run_reference(args):
-    rank, world, _ = dist_env()
-    if rank != 0:
-        return
-    system = make_workload()
-    from oracle import oracle as O
-    S, s_fw, s_ads, w, keep = oracle_setup(system)
-    cores = int(O.lib().ora_max_threads())
-    # calibrate a per-step sample of about 4 s of CPU work
-    t0 = time.perf_counter()
-    S.widom(w, s_fw, s_ads, 0, max(cores, 16))
-    per = (time.perf_counter() - t0) / max(cores, 16)
-    n_step = int(max(cores, min(N_INSERT, 4.0 / max(per, 1e-9))))
-    move = 1000
-    for _ in range(args.warmup):
-        S.widom(w, s_fw, s_ads, move, n_step)
-        move += n_step
-    times = []
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        S.widom(w, s_fw, s_ads, move, n_step)
-        times.append(time.perf_counter() - t0)
-        move += n_step
-    tot = sum(times)
-    value = (NTRIALS + NORIENT) * n_step * args.steps / tot
-    line = {
-        "metric": "CBMC trial energies/s", "value": value, "unit": "trial_energies/s", "impl": "reference",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1000 * tot / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Philox)",
-        "config": {"workload": "widom_co2_silica_3456", "insertions_per_step": n_step,
-                   "full_step_insertions": N_INSERT, "trials": NTRIALS, "orientations": NORIENT},
-        "cpu_baseline": {"value": value, "unit": "trial_energies/s", "cores": cores, "kind": "port",
-                         "sample": f"{n_step} insertions per step (of {N_INSERT}), FP64 C++ OpenMP oracle"},
-        "e2e": {"value": value, "unit": "trial_energies/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-    }
-    print(json.dumps(line), flush=True)
-
-
-def accuracy_check(box, grx, system, n=200):
-    """Mixed / FP32 vs the FP64 oracle on the first n insertions of the stream."""
-    from oracle import oracle as O
-    S, s_fw, s_ads, w, keep = oracle_setup(system)
     ref = S.widom(w, s_fw, s_ads, 0, n)
     R = np.array([r.rosenbluth for r in ref])
     sf = np.array([r.sel_first for r in ref])
@@ -199,21 +366,47 @@ def accuracy_check(box, grx, system, n=200):
         same = (g["sel_first"] == sf) & (g["sel_orient"] == so)
         r = same & (R > 0)
         Eg = np.concatenate([g["e_first"], g["e_chain"]], axis=1)
-        tot_g = Eg[r].reshape(-1, 2, 4).sum(2)
-        tot_r = E[r].reshape(-1, 2, 4).sum(2)
-        dE = np.abs(tot_g - tot_r)
-        out[name] = {
-            "selection_agreement": float(same.mean()),
-            "max_rel_rosenbluth": float(np.max(np.abs(g["rosenbluth"][r] - R[r]) / R[r])) if r.any() else 0.0,
-            "max_beta_dE": float(beta * dE.max()) if dE.size else 0.0,
-            "max_rel_energy_vs_max_E_kT": float(np.max(dE / np.maximum(np.abs(tot_r), 1.0 / beta))) if dE.size else 0.0,
-        }
+        dE = np.abs(Eg[r].reshape(-1, 2, 4).sum(2) - E[r].reshape(-1, 2, 4).sum(2))
+        out[name] = {"selection_agreement": float(same.mean()),
+                     "max_rel_rosenbluth": float(np.max(np.abs(g["rosenbluth"][r] - R[r]) / R[r])) if r.any() else 0.0,
+                     "max_beta_dE": float(beta * dE.max()) if dE.size else 0.0}
     return out
 
 
+def bench_serving(args, grx):
+    from graspa_gb300 import serving, synth
+    n = args.serve_jobs
+    jobs = [synth.serving_job(j, widom_insertions=5000, gcmc_cycles=args.serve_gcmc_cycles)
+            for j in range(n)]
+    rate = args.serve_rate
+    g = np.random.default_rng(7)
+    arrivals = np.cumsum(g.exponential(1.0 / rate, n))
+    srv = grx.Server(args.serve_hbm_gb * (1 << 30), max_resident=args.serve_slots, prec=grx.GRX_MIXED,
+                     widom_slice=0, gcmc_slice=args.serve_gcmc_slice)
+    out = serving.run_stream(srv, jobs, arrivals, timeout=600.0)
+    srv.close()
+    summ = serving.summarize(out)
+    te = sum(serving.trial_energies_of(jobs[i], r) for i, (r, _) in out.items())
+    summ["trial_energies_per_s"] = te / summ["makespan_s"]
+    # the plain one-job-at-a-time FP64 form on a subsample: service times, no overlap
+    sub = jobs[: args.serve_fp64_jobs]
+    plain = grx.Server(args.serve_hbm_gb * (1 << 30), max_resident=1, prec=grx.GRX_FP64)
+    t0 = time.perf_counter()
+    out64 = serving.run_stream(plain, sub, None, timeout=600.0)
+    dt = time.perf_counter() - t0
+    plain.close()
+    svc = np.array([r.t_done - r.t_admit for (r, _) in out64.values()])
+    te64 = sum(serving.trial_energies_of(sub[i], r) for i, (r, _) in out64.items())
+    return {"jobs": n, "arrival_rate_per_s": rate, "slots": args.serve_slots, "gcmc_cycles": args.serve_gcmc_cycles,
+            "widom_insertions": 5000, "species": "CH4 CO2 N2 Xe Kr uniform", "framework_atoms": "200-20000 log-uniform",
+            **summ,
+            "plain_fp64_one_at_a_time": {"jobs": len(sub), "jobs_per_s": len(sub) / dt,
+                                         "service_p50_s": float(np.percentile(svc, 50)),
+                                         "service_p99_s": float(np.percentile(svc, 99)),
+                                         "trial_energies_per_s": te64 / dt}}
+
+
 def run_grx(args):
-    global N_INSERT
-    N_INSERT = args.insertions
     rank, world, local = dist_env()
     import torch
     torch.cuda.set_device(local)
@@ -223,126 +416,243 @@ def run_grx(args):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from graspa_gb300 import grx
     grx.build()
-    system = make_workload()
-    nfw = system["comp_start"][1]
-    box = grx.Box(system, capacity=[nfw, 3 * 64])
     stream = torch.cuda.current_stream()
-    box.set_stream(stream.cuda_stream)
-    box.ewald_total()
-    prec = grx.PRECISIONS[args.precision]
-    d = grx.widom_desc(system, 1, NTRIALS, NORIENT, seed=42, stream=rank)
-    res_dev = torch.empty(N_INSERT * grx.WIDOM_RESULT_DTYPE.itemsize, dtype=torch.uint8, device="cuda")
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
-    pairs = pairs_per_insertion(system) * N_INSERT
-    te_per_step = (NTRIALS + NORIENT) * N_INSERT
-
-    def timed_steps(p, steps, warmup, first_move):
-        move = first_move
-        for _ in range(warmup):
-            box.widom_async(d, move, N_INSERT, p, res_dev.data_ptr())
-            move += N_INSERT
-        torch.cuda.synchronize()
-        if dist:
-            dist.barrier()
-        torch.cuda.synchronize()
-        times = []
-        launches0 = grx.launch_count()
-        for _ in range(steps):
-            flush.zero_()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            box.widom_async(d, move, N_INSERT, p, res_dev.data_ptr())
-            e1.record(stream)
-            move += N_INSERT
-            e1.synchronize()
-            times.append(e0.elapsed_time(e1) / 1000.0)
-        torch.cuda.synchronize()
-        launches = grx.launch_count() - launches0
-        tot = sum(times)
-        if dist:
-            t = torch.tensor([tot], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            tot = float(t.item())
-            dist.barrier()
-        return tot, times, launches
-
-    clocks = ClockSampler(local)
-    clocks.start()
-    tot, times, launches = timed_steps(prec, args.steps, args.warmup, 0)
-    clk = clocks.stop()
-    value = te_per_step * args.steps * world / tot
-    t_launch = float(np.mean(times))
-    if args.profile:
+    if args.workload == "widom":
+        w = bench_widom(args, grx, torch, stream, flush, args.insertions)
         if rank == 0:
-            print(json.dumps({"profile_run": True, "value": value, "ms_per_step": 1000 * tot / args.steps,
-                              "insertions": N_INSERT, "launches": int(launches)}), flush=True)
-        box.close()
+            print(json.dumps({"metric": "CBMC trial energies/s", "value": w["value"], "unit": "trial_energies/s",
+                              "n_gpus": world, "workload": "widom", **w}), flush=True)
+        return
+    if args.workload in ("batched", "water"):
+        line = bench_other(args, grx, torch, stream, flush, args.workload)
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        return
+    if args.workload == "serving":
+        s = bench_serving(args, grx)
+        if rank == 0:
+            print(json.dumps({"metric": "serving jobs/s and p99 job latency", "n_gpus": world, **s}), flush=True)
         return
 
-    # plain FP64 single-box form of the same workload (fewer steps: it is slower)
-    fp64_steps = max(1, min(args.steps, 3))
-    tot64, _, _ = timed_steps(grx.GRX_FP64, fp64_steps, 1, 10 ** 8)
-    fp64_value = te_per_step * fp64_steps * world / tot64
+    g = bench_gcmc(args, grx, torch, stream, flush, rank, world, dist)
+    if args.profile:
+        if rank == 0:
+            print(json.dumps({"profile_run": True, "value": g["value"], "seconds": g["seconds"],
+                              "launches": int(g["launches"])}), flush=True)
+        return
+    line = None
+    if rank == 0:
+        widom = bench_widom(args, grx, torch, stream, flush, args.insertions)
+        serve = bench_serving(args, grx) if args.serve_jobs > 0 else None
+        cpu_val, cpu_te, cpu_dt, cores, chains, steps = cpu_gcmc_rate(args.cpu_seconds)
+        t_launch = float(np.mean(g["times"]))
+        achieved = FLOP_PER_PAIR_CHARGED * g["pairs"] / args.steps / t_launch / 1e12
+        clk = g["clocks"]
+        line = {
+            "metric": "CBMC trial energies/s", "value": g["value"], "unit": "trial_energies/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000 * g["seconds"] / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "fp32+fp64",
+            "data": "synthetic (seeded Philox framework, Philox move stream)",
+            "config": {"workload": "gcmc_co2_silica_3456 (1:1:1:1 translation/rotation/insertion/deletion, "
+                                   "k=10, 300 K, 1e5 Pa, boxes start empty)",
+                       "chains": g["chains"], "mc_steps_per_step": g["mc_steps_per_step"],
+                       "autotune": g.get("autotune"),
+                       "trial_energies_per_step": g["trial_energies"] / args.steps,
+                       "framework_atoms": 3456, "precision": "mixed",
+                       "launch": "one persistent kernel per step, replayed as a CUDA graph",
+                       "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
+            "fp64": g["fp64"],
+            "accuracy": g["accuracy"],
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": PEAK_FP32_NOMINAL, "unit": "TFLOP/s",
+                         "frac": achieved / PEAK_FP32_NOMINAL, "traffic": None,
+                         "peak_kind": "nominal FP32 CUDA-core peak at 2070 MHz (no measured FP32 figure; "
+                                      "MEASURED_PEAKS.json has HBM and bf16 only)",
+                         "kernel": "gcmc_kernel<mixed>",
+                         "model": f"{FLOP_PER_PAIR_CHARGED:.0f} FLOP/pair x {g['pairs'] / args.steps:.4g} pairs "
+                                  "per launch (beads x (framework + guest atoms))"},
+            "cpu_baseline": {"value": cpu_val, "unit": "trial_energies/s", "cores": cores, "kind": "port",
+                             "sample": f"{chains} chains x {steps} GCMC steps ({cpu_te:.0f} trial energies, "
+                                       f"{cpu_dt:.1f} s), FP64 C++ oracle, one chain per thread"},
+            "e2e": g["e2e"],
+            "gpu_launches": int(g["launches"]),
+            "clocks": {"sm_mhz": clk["sm_mhz"], "sm_max_mhz": clk["sm_max_mhz"], "reasons": clk["reasons"]},
+            "widom": widom,
+            "serving": serve,
+        }
+        if serve:
+            line["p99_job_latency_s"] = serve["p99_s"]
+            line["p50_job_latency_s"] = serve["p50_s"]
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    if line:
+        print(json.dumps(line), flush=True)
 
-    # end to end through the C ABI with host buffers
-    pinned = torch.empty(nfw * 8 * 8, dtype=torch.uint8, pin_memory=True)
-    host_sys = dict(system)
-    pn = pinned.numpy().view(np.float64)
-    pn[: 3 * nfw] = np.asarray(system["pos"][:nfw]).reshape(-1)
-    host_sys["pos"] = pn[: 3 * nfw].reshape(-1, 3)
-    host_res = torch.empty(N_INSERT * grx.WIDOM_RESULT_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True)
-    res_view = host_res.numpy().view(grx.WIDOM_RESULT_DTYPE)
-    box.system = host_sys
-    e2e_times = []
-    move = 2 * 10 ** 8
+
+def bench_other(args, grx, torch, stream, flush, which):
+    """configs[2] (64 batched CH4/Xe boxes, triclinic, LJ only, autotuned) or
+    configs[3] (TIP4P-Ew water in the hexagonal framework) as their own lines."""
+    from graspa_gb300 import synth
+    if which == "batched":
+        systems = [synth.ch4_xe_system(k) for k in range(64)]
+        descs = []
+        g = np.random.default_rng(3)
+        for k in range(64):
+            nt = int(g.integers(8, 33))
+            kw = dict(ntrials=nt, norient=1, p_translation=0.3, p_rotation=0.3, p_reinsertion=0.5, p_swap=1.0,
+                      pressure_pa=1e6, max_translation=0.7, seed=42, stream=k)
+            descs.append([grx.gcmc_desc(1, **kw), grx.gcmc_desc(2, **kw)])
+        boxes = []
+        for s in systems:
+            b = grx.Box(s, capacity=[s["comp_start"][1], 256, 256])
+            b.set_stream(stream.cuda_stream)
+            b.ewald_total()
+            boxes.append(b)
+        prec = grx.GRX_MIXED
+        batch = grx.GcmcBatch(boxes, descs, prec)
+        chosen, cand_ms = batch.autotune(20)
+        times, stats = timed_graph(torch, batch, stream, args.mc_steps, args.steps, args.warmup, flush)
+        batch.close()
+        te = 0.0
+        pairs = 0.0
+        for k, s in enumerate(systems):
+            for e in range(2):
+                st = stats[2 * k + e]
+                a = list(st.attempts)
+                nt = descs[k][e].ntrials
+                te += 2 * (a[0] + a[1]) + nt * (a[2] + a[3]) + (nt + 1) * a[4]
+                beads = 2 * (a[0] + a[1]) + nt * (a[2] + a[3]) + (nt + 1) * a[4]
+                pairs += beads * (s["comp_start"][1] + st.sum_n / max(1, sum(a)))
+        t = sum(times)
+        for b in boxes:
+            b.close()
+        achieved = FLOP_PER_PAIR_LJ * pairs / t / 1e12
+        return {"metric": "CBMC trial energies/s", "value": te / t, "unit": "trial_energies/s", "n_gpus": 1,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * t / args.steps,
+                "workload": "batched_ch4_xe_64_triclinic (mixture GCMC, 8-32 trials, LJ only)",
+                "mc_steps_per_step": args.mc_steps, "autotune": {"chunk_mult": chosen, "ms_per_candidate": cand_ms},
+                "roofline": {"bound": "fp32", "achieved": achieved, "peak": PEAK_FP32_NOMINAL, "unit": "TFLOP/s",
+                             "frac": achieved / PEAK_FP32_NOMINAL, "model": "40 FLOP/pair (LJ only)"},
+                "framework_atoms": [int(s["comp_start"][1]) for s in systems[:8]]}
+    system = synth.tip4p_hex_system(n_water=0)
+    nfw = system["comp_start"][1]
+    R = 3 * torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    descs = [grx.gcmc_desc(1, p_translation=0.25, p_rotation=0.5, p_reinsertion=0.75, p_swap=1.0, pressure_pa=3.5e3,
+                           max_translation=0.5, max_rotation=0.4, seed=42, stream=k) for k in range(R)]
+    out = {}
+    for name, p in (("mixed", grx.GRX_MIXED), ("fp64", grx.GRX_FP64)):
+        boxes = []
+        for _ in range(R):
+            b = grx.Box(system, capacity=[nfw, 4 * 400])
+            b.set_stream(stream.cuda_stream)
+            b.ewald_total()
+            boxes.append(b)
+        e0 = [total_energy(b) for b in boxes[:4]]
+        for b in boxes[:4]:
+            b.ewald_total()
+        batch = grx.GcmcBatch(boxes, descs, p)
+        steps = args.steps if name == "mixed" else max(1, min(args.steps, 3))
+        times, stats = timed_graph(torch, batch, stream, args.mc_steps, steps, args.warmup, flush)
+        warm = timed_graph.warm_stats
+        acc, _ = batch.stats()
+        batch.close()
+        te, _ = work_of(stats, 4, nfw)
+        beta = grx.beta_from_temperature(300.0)
+        drift = [beta * abs((total_energy(b) - e0[i]) - (warm[i].energy[3] + acc[i].energy[3]))
+                 for i, b in enumerate(boxes[:4])]
+        out[name] = {"value": te / sum(times), "loading": float(np.mean([s.n_molecules for s in acc])),
+                     "drift_max_beta_abs": float(max(drift))}
+        for b in boxes:
+            b.close()
+    return {"metric": "CBMC trial energies/s", "value": out["mixed"]["value"], "unit": "trial_energies/s",
+            "n_gpus": 1, "workload": "gcmc_tip4p_ew_hexagonal_864 (alpha 0.30, kmax 10/10/8, cutoff 11 A)",
+            "chains": R, "mc_steps_per_step": args.mc_steps, "mixed": out["mixed"], "fp64": out["fp64"],
+            "speedup_mixed_over_fp64": out["mixed"]["value"] / out["fp64"]["value"]}
+
+
+# ------------------------------------------------------------------ reference arm
+def _oracle_chain(system, desc, first, nsteps):
+    from graspa_gb300 import grx
+    from oracle import oracle as O
+    g = O.OraGcmc()
+    g.component, g.ntrials, g.norient = 1, desc.ntrials, desc.norient
+    g.p_translation, g.p_rotation, g.p_reinsertion, g.p_swap = (desc.p_translation, desc.p_rotation,
+                                                                desc.p_reinsertion, desc.p_swap)
+    for k in range(3):
+        g.max_translation[k] = desc.max_translation[k]
+        g.max_rotation[k] = desc.max_rotation[k]
+    g.beta, g.pressure = desc.beta, desc.pressure
+    g.fugacity_coeff, g.mol_fraction, g.ideal_rosenbluth = desc.fugacity_coeff, desc.mol_fraction, 1.0
+    g.seed, g.stream = desc.seed, desc.stream
+    st, after, _ = O.OracleSystem(system).gcmc(g, [system["comp_start"][1], 3 * 160], first, nsteps)
+    return st, after
+
+
+def cpu_gcmc_rate(seconds, threads=None):
+    """The FP64 oracle on the same GCMC workload, one chain per host thread, for about
+    `seconds`. Returns (trial energies/s, trial energies, seconds, threads, chains, steps)."""
+    from graspa_gb300 import grx
+    from oracle import oracle as O
+    O.lib()
+    system = co2_system()
+    threads = threads or os.cpu_count() or 1
+    descs = gcmc_descs(grx, threads)
+    t0 = time.perf_counter()
+    _oracle_chain(system, descs[0], 0, 20)
+    per_step = (time.perf_counter() - t0) / 20
+    steps = int(max(20, min(5000, seconds / max(per_step, 1e-6))))
+    t0 = time.perf_counter()
+    with concurrent.futures.ThreadPoolExecutor(threads) as ex:
+        res = list(ex.map(lambda d: _oracle_chain(system, d, 0, steps)[0], descs))
+    dt = time.perf_counter() - t0
+    te, _ = work_of(res, 3, system["comp_start"][1])
+    return te / dt, te, dt, threads, threads, steps
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from graspa_gb300 import grx
+    from oracle import oracle as O
+    O.lib()
+    system = co2_system()
+    threads = os.cpu_count() or 1
+    descs = gcmc_descs(grx, threads)
+    t0 = time.perf_counter()
+    _oracle_chain(system, descs[0], 0, 20)
+    per_step = (time.perf_counter() - t0) / 20
+    n_step = int(max(10, min(args.mc_steps, 4.0 / max(per_step, 1e-9))))
+    state = [system] * threads
+    first = 0
+    times, te_tot = [], 0.0
     for i in range(args.warmup + args.steps):
         t0 = time.perf_counter()
-        box.set_component(0)
-        box.widom(d, move, N_INSERT, prec=prec, out=res_view)
+        with concurrent.futures.ThreadPoolExecutor(threads) as ex:
+            res = list(ex.map(lambda k: _oracle_chain(state[k], descs[k], first, n_step), range(threads)))
         dt = time.perf_counter() - t0
-        move += N_INSERT
+        state = [r[1] for r in res]
+        first += n_step
         if i >= args.warmup:
-            e2e_times.append(dt)
-    box.system = system
-    e2e_value = te_per_step * world / float(np.mean(e2e_times))
-    h2d = nfw * (3 * 8 + 8 + 8 + 8 + 8 + 8)
-    d2h = N_INSERT * grx.WIDOM_RESULT_DTYPE.itemsize
-
-    if rank == 0:
-        acc = accuracy_check(box, grx, system)
-        cpu_val, cpu_n, cores, cpu_dt = cpu_rate(system, args.cpu_seconds)
-        sm_mhz = clk["sm_mhz"] or 2070.0
-        peak_fp32 = 152 * 128 * 2 * 2070e6 / 1e12
-        achieved = FLOP_PER_PAIR_CHARGED * pairs / t_launch / 1e12
-        line = {
-            "metric": "CBMC trial energies/s", "value": value, "unit": "trial_energies/s",
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * tot / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "fp32+fp64" if args.precision == "mixed" else args.precision,
-            "data": "synthetic (seeded Philox framework, Philox trial stream)",
-            "config": {"workload": "widom_co2_silica_3456", "insertions_per_step": N_INSERT, "trials": NTRIALS,
-                       "orientations": NORIENT, "framework_atoms": nfw, "precision": args.precision,
-                       "pairs_per_step": pairs, "l2": "flushed between steps (256 MB write)",
-                       "parallelism": f"replicas x{world}"},
-            "fp64": {"value": fp64_value, "unit": "trial_energies/s", "steps": fp64_steps,
-                     "speedup_mixed_over_fp64": value / fp64_value},
-            "accuracy_vs_fp64_oracle": acc,
-            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_fp32, "unit": "TFLOP/s",
-                         "frac": achieved / peak_fp32, "traffic": None,
-                         "peak_kind": "nominal FP32 CUDA-core peak at 2070 MHz (no measured FP32 peak exists)",
-                         "model": f"{FLOP_PER_PAIR_CHARGED:.0f} FLOP/pair x {pairs} pairs per launch"},
-            "cpu_baseline": {"value": cpu_val, "unit": "trial_energies/s", "cores": cores, "kind": "port",
-                             "sample": f"{cpu_n} insertions ({cpu_dt:.1f} s), FP64 C++ OpenMP oracle"},
-            "e2e": {"value": e2e_value, "unit": "trial_energies/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
-            "gpu_launches": int(launches),
-            "clocks": {"sm_mhz": clk["sm_mhz"], "sm_max_mhz": clk["sm_max_mhz"], "reasons": clk["reasons"]},
-        }
-        print(json.dumps(line), flush=True)
-    box.close()
-    if dist:
-        dist.destroy_process_group()
+            times.append(dt)
+            te_tot += work_of([r[0] for r in res], 3, system["comp_start"][1])[0]
+    tot = sum(times)
+    value = te_tot / tot
+    line = {
+        "metric": "CBMC trial energies/s", "value": value, "unit": "trial_energies/s", "impl": "reference",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000 * tot / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Philox)",
+        "config": {"workload": "gcmc_co2_silica_3456 (1:1:1:1 translation/rotation/insertion/deletion, k=10)",
+                   "chains": threads, "mc_steps_per_step": n_step},
+        "cpu_baseline": {"value": value, "unit": "trial_energies/s", "cores": threads, "kind": "port",
+                         "sample": f"{threads} chains x {n_step} GCMC steps per step, FP64 C++ oracle, "
+                                   "one chain per thread"},
+        "e2e": {"value": value, "unit": "trial_energies/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
 
 
 def main():
@@ -351,12 +661,20 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="grx", choices=["grx", "reference"])
-    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64", "fp32"])
+    ap.add_argument("--workload", default="gcmc", choices=["gcmc", "widom", "batched", "water", "serving"])
+    ap.add_argument("--chains", type=int, default=0, help="GCMC chains (default: three per SM)")
+    ap.add_argument("--mc-steps", type=int, default=100, help="Monte Carlo steps of every chain per step")
+    ap.add_argument("--insertions", type=int, default=20000, help="Widom insertions per launch")
+    ap.add_argument("--widom-steps", type=int, default=5)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--insertions", type=int, default=N_INSERT,
-                    help="insertions per step (the benchmark workload is 20000)")
-    ap.add_argument("--profile", action="store_true",
-                    help="only the timed mixed-precision steps (for profiler launch lists)")
+    ap.add_argument("--serve-jobs", type=int, default=48)
+    ap.add_argument("--serve-rate", type=float, default=40.0, help="Poisson arrival rate, jobs/s")
+    ap.add_argument("--serve-slots", type=int, default=152)
+    ap.add_argument("--serve-hbm-gb", type=float, default=8.0)
+    ap.add_argument("--serve-gcmc-cycles", type=int, default=100, help="GCMC cycles of 20 steps per serving job")
+    ap.add_argument("--serve-gcmc-slice", type=int, default=500)
+    ap.add_argument("--serve-fp64-jobs", type=int, default=6)
+    ap.add_argument("--profile", action="store_true", help="only the timed mixed GCMC steps (launch lists)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -8,6 +8,8 @@
 
 namespace grx {
 
+constexpr int kBigMolecule = 64;  // molecules above this size get the pair-parallel exclusion
+
 struct CompRanges {  // live atoms of every component, compact numbering
   int n;                                // total live atoms
   int ncomp, nhost;
@@ -107,7 +109,7 @@ __global__ void __launch_bounds__(GRX_THREADS) self_excl_kernel(BoxDev b, CompRa
     if (c < r.nhost) sh = v;
     const int ms = r.molsize[c];
     const int mol0 = (local / ms) * ms;
-    const int lend = min(mol0 + ms, r.base[c + 1] - r.base[c]);
+    const int lend = ms > kBigMolecule ? local + 1 : min(mol0 + ms, r.base[c + 1] - r.base[c]);
     for (int l2 = local + 1; l2 < lend; ++l2) {
       const double4 q = b.pos64[r.off[c] + l2];
       double x = p.x - q.x, y = p.y - q.y, z = p.z - q.z;
@@ -127,6 +129,38 @@ __global__ void __launch_bounds__(GRX_THREADS) self_excl_kernel(BoxDev b, CompRa
     part[4 * blockIdx.x + 1] = sh;
     part[4 * blockIdx.x + 2] = ea;
     part[4 * blockIdx.x + 3] = eh;
+  }
+}
+
+// Intramolecular erf exclusion of the molecules of one component with more than
+// kBigMolecule atoms (a framework is one such molecule): the pairs i < j of each
+// molecule spread over the whole grid instead of one thread per atom.
+// part per block: [excl_all, excl_host].
+__global__ void __launch_bounds__(GRX_THREADS) big_excl_kernel(BoxDev b, CompRanges r, int c, double* part) {
+  __shared__ double sbuf[32];
+  const int ms = r.molsize[c];
+  const int n = r.base[c + 1] - r.base[c];
+  const long long nmol = (n + ms - 1) / ms;
+  const long long npair = nmol * (long long)ms * ms;
+  double ea = 0.0;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npair;
+       p += (long long)gridDim.x * blockDim.x) {
+    const long long m = p / ((long long)ms * ms);
+    const int rem = (int)(p - m * (long long)ms * ms);
+    const int i = rem / ms, j = rem - i * ms;
+    const int li = (int)(m * ms) + i, lj = (int)(m * ms) + j;
+    if (j <= i || lj >= n) continue;
+    const double4 a = b.pos64[r.off[c] + li];
+    const double4 q = b.pos64[r.off[c] + lj];
+    double x = a.x - q.x, y = a.y - q.y, z = a.z - q.z;
+    pbc64(b, x, y, z);
+    const double rr = sqrt(x * x + y * y + z * z);
+    ea += b.prefactor * a.w * q.w * erf(b.alpha * rr) / rr;
+  }
+  ea = block_sum(ea, sbuf);
+  if (threadIdx.x == 0) {
+    part[2 * blockIdx.x + 0] = ea;
+    part[2 * blockIdx.x + 1] = c < r.nhost ? ea : 0.0;
   }
 }
 
@@ -280,7 +314,8 @@ grx_status grx_ewald_total(grx_box* b, double* out8) {
   const size_t n = std::max(r.n, 1);
   const size_t ntab = (size_t)(b->dev.kmax[0] + b->dev.kmax[1] + b->dev.kmax[2] + 3) * n;
   const int nblk_atoms = (r.n + GRX_THREADS - 1) / GRX_THREADS;
-  const size_t part_doubles = 4 * (size_t)std::max(nblk_atoms, 1);
+  const int nblk_big = 4 * sm_count(b);
+  const size_t part_doubles = 4 * (size_t)std::max(nblk_atoms, 1) + 2 * (size_t)nblk_big * GRX_MAX_COMPONENTS;
   st = ensure_scratch(b, ntab * sizeof(double2) + part_doubles * sizeof(double));
   if (st) return st;
   double2* ex = (double2*)b->scratch;
@@ -299,11 +334,19 @@ grx_status grx_ewald_total(grx_box* b, double* out8) {
     count_launch();
   }
   std::vector<double> parts(part_doubles, 0.0);
+  std::vector<int> big;
   if (r.n > 0) {
     self_excl_kernel<<<nblk_atoms, GRX_THREADS, 0, b->stream>>>(b->dev, r, part);
     count_launch();
-    GRX_CHECK_CUDA(cudaMemcpyAsync(parts.data(), part, 4 * nblk_atoms * sizeof(double),
-                                   cudaMemcpyDeviceToHost, b->stream), "read self/exclusion");
+    double* pbig = part + 4 * (size_t)std::max(nblk_atoms, 1);
+    for (int c = 0; c < r.ncomp; ++c) {
+      if (r.molsize[c] <= kBigMolecule || r.base[c + 1] - r.base[c] < 2) continue;
+      big_excl_kernel<<<nblk_big, GRX_THREADS, 0, b->stream>>>(b->dev, r, c, pbig + 2 * (size_t)nblk_big * big.size());
+      count_launch();
+      big.push_back(c);
+    }
+    GRX_CHECK_CUDA(cudaMemcpyAsync(parts.data(), part, part_doubles * sizeof(double), cudaMemcpyDeviceToHost,
+                                   b->stream), "read self/exclusion");
   }
   std::vector<double2> sfw(b->nvec), sads(b->nvec);
   GRX_CHECK_CUDA(cudaMemcpyAsync(sfw.data(), b->s_fw, b->nvec * sizeof(double2), cudaMemcpyDeviceToHost, b->stream), "read S_fw");
@@ -323,6 +366,12 @@ grx_status grx_ewald_total(grx_box* b, double* out8) {
   for (int k = 0; k < nblk_atoms; ++k) {
     sa += parts[4 * k]; sh += parts[4 * k + 1]; ea += parts[4 * k + 2]; eh += parts[4 * k + 3];
   }
+  const double* pb = parts.data() + 4 * (size_t)std::max(nblk_atoms, 1);
+  for (size_t g = 0; g < big.size(); ++g)
+    for (int k = 0; k < nblk_big; ++k) {
+      ea += pb[2 * (nblk_big * g + k)];
+      eh += pb[2 * (nblk_big * g + k) + 1];
+    }
   out8[0] = gg; out8[1] = hh; out8[2] = hg;
   out8[3] = sa; out8[4] = sh; out8[5] = -ea; out8[6] = -eh;
   out8[7] = (double)b->nact;

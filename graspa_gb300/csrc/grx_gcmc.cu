@@ -83,7 +83,7 @@ template <int PREC>
 // first[box + 1]) of args / stats; every step picks one of them uniformly with word 3
 // of the displacement slot (Select_Box_Component_Molecule, axpy.cu:74-100). All
 // entries of a box share its seed and stream.
-__global__ void __launch_bounds__(GRX_THREADS, 2) gcmc_kernel(const BoxDev* boxes, const GcmcArgs* args,
+__global__ void __launch_bounds__(GRX_THREADS, 3) gcmc_kernel(const BoxDev* boxes, const GcmcArgs* args,
                                                               const int* first, const uint64_t* step0,
                                                               int64_t nsteps, grx_gcmc_stats* stats) {
   const uint64_t first_step = *step0;
@@ -702,9 +702,11 @@ extern "C" grx_status grx_gcmc_batch_run_graph(grx_gcmc_batch* B, int64_t nsteps
     GRX_CHECK_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), "capture stream");
     GRX_CHECK_CUDA(cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal), "begin capture");
     grx_status st = GRX_OK;
+    const uint64_t before = grx_launch_count();
     for (int k = 0; k < nlaunch && st == GRX_OK; ++k)
       st = enqueue_gcmc(B->prec, (int)B->boxes.size(), B->d_boxes, B->d_args, B->d_first, B->d_step, nsteps,
                         B->d_stats, B->smem, cap);
+    count_launch(0 - (grx_launch_count() - before));  // capture records the kernels, it launches nothing
     cudaGraph_t g = nullptr;
     const cudaError_t ec = cudaStreamEndCapture(cap, &g);
     cudaStreamDestroy(cap);
@@ -719,6 +721,7 @@ extern "C" grx_status grx_gcmc_batch_run_graph(grx_gcmc_batch* B, int64_t nsteps
     B->graph_nlaunch = nlaunch;
   }
   GRX_CHECK_CUDA(cudaGraphLaunch(B->exec, s), "graph launch");
+  count_launch(2 * (uint64_t)nlaunch);  // the graph's kernels: one GCMC launch + one step advance each
   B->last_stream = s;
   return GRX_OK;
 }
