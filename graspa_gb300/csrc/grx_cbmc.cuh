@@ -45,7 +45,7 @@ struct CbmcWork {
 // ---------------------------------------------------------------- trials
 // First-bead trial positions: Cell diagonal x Philox uniforms (mc_widom.h:133-139);
 // with `retrace`, trial 0 is the existing bead (deletion, mc_widom.h:141-156).
-__device__ __forceinline__ void gen_first_trials(const BoxDev& b, CbmcWork& W, uint64_t seed, uint32_t stream,
+__device__ __noinline__ void gen_first_trials(const BoxDev& b, CbmcWork& W, uint64_t seed, uint32_t stream,
                                                  uint64_t move, int nt, double q, double scale, int type,
                                                  bool retrace, double ox, double oy, double oz) {
   const int t = threadIdx.x;
@@ -88,7 +88,7 @@ __device__ __forceinline__ void rotate_quaternion(double& x, double& y, double& 
 // Trial orientations about the chosen first bead (fx, fy, fz): the vectors from the
 // component's slot-0 atom to its chain atoms, rotated by Philox quaternions. With
 // `retrace`, orientation 0 is the existing chain (ox/oy/oz arrays, chain atoms).
-__device__ __forceinline__ void gen_orientations(const BoxDev& b, CbmcWork& W, uint64_t seed, uint32_t stream,
+__device__ __noinline__ void gen_orientations(const BoxDev& b, CbmcWork& W, uint64_t seed, uint32_t stream,
                                                  uint64_t move, int no, int chain, int off, double scale_coul,
                                                  double scale, double fx, double fy, double fz, bool retrace,
                                                  const double* ox, const double* oy, const double* oz,
@@ -116,7 +116,7 @@ __device__ __forceinline__ void gen_orientations(const BoxDev& b, CbmcWork& W, u
 // Energies of ntr = nb / chain trials of `chain` beads each (W.beads) against every
 // atom, with the atoms of (comp, newmol) excluded: W.te[4 t + k], W.tflag[t].
 template <int PREC>
-__device__ __forceinline__ void trial_pass(const BoxDev& b, CbmcWork& W, int nb, int chain, int comp, int newmol) {
+__device__ __noinline__ void trial_pass(const BoxDev& b, CbmcWork& W, int nb, int chain, int comp, int newmol) {
   if (threadIdx.x == 0) W.counter = 0;
   __syncthreads();
   const int nch = chunks_for(nb, work_tiles(b), GRX_THREADS / 32, b.chunk_mult);
@@ -132,7 +132,7 @@ __device__ __forceinline__ void trial_pass(const BoxDev& b, CbmcWork& W, int nb,
 // existing configuration and no selection is drawn. `stored` is added to the sum
 // before averaging (the reinsertion retrace's StoredR, mc_widom.h:363-366). Exponentials are evaluated one
 // trial per lane; sums and the cumulative search stay sequential in trial order.
-__device__ __forceinline__ void step_weight(CbmcWork& W, int nt, double beta, int bias, double u, double navg,
+__device__ __noinline__ void step_weight(CbmcWork& W, int nt, double beta, int bias, double u, double navg,
                                             bool retrace, double stored = 0.0) {
   if (threadIdx.x < 32) {
     const int lane = threadIdx.x;
@@ -212,7 +212,7 @@ __device__ __forceinline__ void step_weight(CbmcWork& W, int nt, double beta, in
 // double-float on the FP32 pipe against temp*S tables (ewA, ewF). When s_out is
 // given, S_same + dS is staged there (FP64) for a later commit. Results on thread 0.
 template <int PREC>
-__device__ __forceinline__ void ewald_move(const BoxDev& b, CbmcWork& W, int na, double2* eik, double2* s_out,
+__device__ __noinline__ void ewald_move(const BoxDev& b, CbmcWork& W, int na, double2* eik, double2* s_out,
                                            double& same, double& cross) {
   const int tid = threadIdx.x;
   const int kx1 = b.kmax[0] + 1, ky1 = b.kmax[1] + 1;

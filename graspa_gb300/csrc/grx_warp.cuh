@@ -393,7 +393,7 @@ constexpr int kMaxItems = 320;
 // taken dynamically by warps; per-item partials land in ipart[item*4 + q] and
 // iflag[item] (item = bead * nchunk + chunk). Caller syncs before reading them.
 template <int PREC>
-__device__ __forceinline__ void block_bead_pass(const BoxDev& b, const Bead* beads, int nb, int component,
+__device__ __noinline__ void block_bead_pass(const BoxDev& b, const Bead* beads, int nb, int component,
                                                 int newmol, int excl_comp, int excl_mol, int* qbuf,
                                                 double* ipart, int* iflag, int* counter, int nchunk) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
