@@ -18,8 +18,10 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["grx_box.cu", "grx_pair.cu", "grx_ewald.cu", "grx_widom.cu", "grx_noalloc.cu", "grx_gcmc.cu", "grx_arena.cu", "grx_server.cu"]
 HEADERS = ["grx_internal.cuh", "grx_host.h", "grx_warp.cuh", "grx_df.cuh", "grx_cbmc.cuh"]
 HOST = os.path.join(HERE, "host")
-HOST_SOURCES = ["graspa_host.cpp", "gcmc_driver.cpp"]
+HOST_SOURCES = ["graspa_host.cpp", "graspa_input.cpp"]
+HOST_PROGRAMS = {"gcmc_driver": "gcmc_driver.cpp", "graspa_run": "graspa_run.cpp"}
 DRIVER = os.path.join(OUT, "gcmc_driver")
+RUNNER = os.path.join(OUT, "graspa_run")
 
 
 def nvcc():
@@ -81,19 +83,22 @@ def build(force=False, verbose=False):
 
 
 def build_host():
-    """The C++ host layer (graspa_gb300/host) and its example driver, linked
-    against libgrx.so with g++ (no CUDA headers needed on this side)."""
+    """The C++ host layer (graspa_gb300/host) and its programs, linked against
+    libgrx.so with g++ (no CUDA headers needed on this side)."""
     inc = os.path.join(HERE, "..", "include")
-    srcs = [os.path.join(HOST, s) for s in HOST_SOURCES]
-    deps = srcs + [LIB, os.path.join(HOST, "graspa_host.hpp"), os.path.join(inc, "grx.h"),
-                   os.path.join(inc, "grx_philox.h")]
-    if not _stale(DRIVER, deps):
-        return DRIVER
-    cmd = ["g++", "-O2", "-std=c++17", "-Wall", "-I", inc, "-I", HOST] + srcs + \
-        ["-L", OUT, "-lgrx", "-Wl,-rpath,$ORIGIN", "-o", DRIVER]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError(f"host layer build failed:\n{r.stdout}\n{r.stderr}")
+    common = [os.path.join(HOST, s) for s in HOST_SOURCES]
+    headers = [os.path.join(HOST, h) for h in ("graspa_host.hpp", "graspa_input.hpp")] + \
+        [os.path.join(inc, "grx.h"), os.path.join(inc, "grx_philox.h")]
+    for exe, src in HOST_PROGRAMS.items():
+        target = os.path.join(OUT, exe)
+        srcs = common + [os.path.join(HOST, src)]
+        if not _stale(target, srcs + headers + [LIB]):
+            continue
+        cmd = ["g++", "-O2", "-std=c++17", "-Wall", "-I", inc, "-I", HOST] + srcs + \
+            ["-L", OUT, "-lgrx", "-Wl,-rpath,$ORIGIN", "-o", target]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"host layer build failed for {exe}:\n{r.stdout}\n{r.stderr}")
     return DRIVER
 
 

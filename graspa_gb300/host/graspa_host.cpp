@@ -914,6 +914,53 @@ double WidomChemicalPotential(const Components& SC, size_t comp) {
 }
 
 // ------------------------------------------------------------------ device-resident moves
+static grx_gcmc_desc device_desc(Variables& Vars, size_t systemId, size_t comp) {
+  Components& SC = Vars.SystemComponents[systemId];
+  const Move_Statistics& MS = SC.Moves[comp];
+  grx_gcmc_desc d{};
+  d.component = (int32_t)comp;
+  d.ntrials = (int32_t)Vars.Widom[systemId].NumberWidomTrials;
+  d.norient = (int32_t)Vars.Widom[systemId].NumberWidomTrialsOrientations;
+  d.p_translation = MS.TranslationProb;
+  d.p_rotation = MS.RotationProb;
+  d.p_reinsertion = MS.ReinsertionProb;
+  d.p_swap = MS.SwapProb;
+  d.max_translation[0] = MS.MaxTranslation.x; d.max_translation[1] = MS.MaxTranslation.y;
+  d.max_translation[2] = MS.MaxTranslation.z;
+  d.max_rotation[0] = MS.MaxRotation.x; d.max_rotation[1] = MS.MaxRotation.y; d.max_rotation[2] = MS.MaxRotation.z;
+  d.beta = SC.Beta;
+  d.pressure = SC.Pressure;
+  d.fugacity_coeff = SC.FugacityCoeff[comp];
+  d.mol_fraction = SC.MolFraction[comp];
+  d.ideal_rosenbluth = SC.IdealRosenbluthWeight[comp];
+  d.tail_insert = SC.TailCorrectionInsert.empty() ? 0.0 : SC.TailCorrectionInsert[comp];
+  d.seed = Vars.Random.Seed;
+  d.stream = Vars.Random.Stream;
+  return d;
+}
+
+std::vector<grx_gcmc_stats> RunMoves_Device_All(Variables& Vars, size_t systemId, int64_t nsteps,
+                                                std::vector<size_t>* moved) {
+  Components& SC = Vars.SystemComponents[systemId];
+  Simulations& Sims = Vars.Sims[systemId];
+  std::vector<grx_gcmc_desc> descs;
+  std::vector<size_t> comps;
+  for (int c = SC.NComponents.y; c < SC.NComponents.x; ++c)
+    if (SC.Moves[c].SwapProb > 1e-10) {  // cumulative: the total of this component's moves
+      descs.push_back(device_desc(Vars, systemId, (size_t)c));
+      comps.push_back((size_t)c);
+    }
+  if (descs.empty()) throw std::runtime_error("RunMoves_Device_All: no component has moves");
+  std::vector<grx_gcmc_stats> st(descs.size());
+  grx_box* b = Sims.Box.handle;
+  const int32_t nm = (int32_t)descs.size();
+  check(grx_gcmc_run(&b, 1, descs.data(), &nm, SC.Step, nsteps, Vars.Precision, st.data()), "grx_gcmc_run");
+  SC.Step += (uint64_t)nsteps;
+  for (size_t c : comps) Sync_Host_Mirror(Vars, systemId, c);
+  if (moved) *moved = comps;
+  return st;
+}
+
 grx_gcmc_stats RunMoves_Device(Variables& Vars, size_t systemId, size_t comp, int64_t nsteps) {
   Components& SC = Vars.SystemComponents[systemId];
   Simulations& Sims = Vars.Sims[systemId];

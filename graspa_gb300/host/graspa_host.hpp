@@ -285,6 +285,12 @@ double WidomAverageRosenbluth(const Components& SystemComponents, size_t comp);
 // The same moves fully on the device: nsteps steps of grx_gcmc_run for one box.
 grx_gcmc_stats RunMoves_Device(Variables& Vars, size_t systemId, size_t comp, int64_t nsteps);
 
+// Every adsorbate component with a move probability, picked uniformly per step
+// (Select_Box_Component_Molecule, axpy.cu:74-100): nsteps steps of grx_gcmc_run, one
+// statistics entry per moved component (in `moved`).
+std::vector<grx_gcmc_stats> RunMoves_Device_All(Variables& Vars, size_t systemId, int64_t nsteps,
+                                                std::vector<size_t>* moved = nullptr);
+
 // Copies the device atoms of adsorbate component comp back into the host mirror.
 void Sync_Host_Mirror(Variables& Vars, size_t systemId, size_t comp);
 
