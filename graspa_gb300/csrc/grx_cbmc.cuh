@@ -1,6 +1,6 @@
 // grx_cbmc.cuh -- block-level CBMC stages shared by the Widom and GCMC kernels.
 //
-// Every function here is called by all threads of a block (GRX_THREADS) with the
+// Every function here is called by all threads of a block (kCbmcThreads) with the
 // same arguments; each ends with the block synchronised and its results in the
 // shared-memory workspace CbmcWork. The stages restate gRASPA's CBMC move pieces:
 //   gen_first_trials  get_random_trial_position      mc_widom.h:122-213
@@ -18,13 +18,17 @@
 namespace grx {
 
 constexpr int kMaxTrials = 64;
-constexpr int kMolWork = 32;  // atoms of one molecule held in shared memory
+constexpr int kMolWork = 32;      // atoms of one molecule held in shared memory
+constexpr int kCbmcThreads = 256; // threads of a block running the CBMC stages (8 warps)
+constexpr int kCbmcBeads = 128;   // trial beads of one pass
+// work items of one pass: nb * chunks <= mult * warps + nb with mult <= 8
+constexpr int kCbmcItems = kCbmcBeads + 8 * (kCbmcThreads / 32);
 
 struct CbmcWork {
-  Bead beads[GRX_MAX_TRIAL_BEADS];
-  double ipart[kMaxItems * 4];
-  int iflag[kMaxItems];
-  int qbuf[(GRX_THREADS / 32) * kQueue];
+  Bead beads[kCbmcBeads];
+  double ipart[kCbmcItems * 4];
+  int iflag[kCbmcItems];
+  int qbuf[(kCbmcThreads / 32) * kQueue];
   double te[kMaxTrials * 4];
   int tflag[kMaxTrials];
   double sel_ws[kMaxTrials], sel_wa[kMaxTrials];
@@ -32,7 +36,7 @@ struct CbmcWork {
   // [n_old, n_old + n_new) arrive
   double mx[2 * kMolWork], my[2 * kMolWork], mz[2 * kMolWork], mq[2 * kMolWork];
   double sbuf[32];
-  double wsum[2][GRX_THREADS / 32];
+  double wsum[2][kCbmcThreads / 32];
   float2 qd[2 * kMolWork];
   int counter;
   int ok;       // step constructed
@@ -48,8 +52,7 @@ struct CbmcWork {
 __device__ __noinline__ void gen_first_trials(const BoxDev& b, CbmcWork& W, uint64_t seed, uint32_t stream,
                                                  uint64_t move, int nt, double q, double scale, int type,
                                                  bool retrace, double ox, double oy, double oz) {
-  const int t = threadIdx.x;
-  if (t < nt) {
+  for (int t = threadIdx.x; t < nt; t += blockDim.x) {
     if (retrace && t == 0) {
       make_bead(W.beads[0], ox, oy, oz, q, scale, type, b.prefactor);
     } else {
@@ -93,8 +96,7 @@ __device__ __noinline__ void gen_orientations(const BoxDev& b, CbmcWork& W, uint
                                                  double scale, double fx, double fy, double fz, bool retrace,
                                                  const double* ox, const double* oy, const double* oz,
                                                  uint32_t slot_base = SLOT_ORIENT) {
-  const int tid = threadIdx.x;
-  if (tid < no * chain) {
+  for (int tid = threadIdx.x; tid < no * chain; tid += blockDim.x) {
     const int o = tid / chain, at = tid % chain;
     const double q = b.charge[off + 1 + at] * scale_coul;
     const int type = b.meta[off + 1 + at].x;
@@ -119,7 +121,7 @@ template <int PREC>
 __device__ __noinline__ void trial_pass(const BoxDev& b, CbmcWork& W, int nb, int chain, int comp, int newmol) {
   if (threadIdx.x == 0) W.counter = 0;
   __syncthreads();
-  const int nch = chunks_for(nb, work_tiles(b), GRX_THREADS / 32, b.chunk_mult);
+  const int nch = chunks_for(nb, work_tiles(b), (int)(blockDim.x >> 5), b.chunk_mult);
   block_bead_pass<PREC>(b, W.beads, nb, comp, newmol, -1, -1, W.qbuf, W.ipart, W.iflag, &W.counter, nch);
   __syncthreads();
   reduce_items<PREC>(W.ipart, W.iflag, nb / chain, chain, nch, W.te, W.tflag);
@@ -311,7 +313,7 @@ __device__ __noinline__ void ewald_move(const BoxDev& b, CbmcWork& W, int na, do
     if ((tid & 31) == 0) { W.wsum[0][tid >> 5] = df_to(sm); W.wsum[1][tid >> 5] = df_to(cr); }
     __syncthreads();
     if (tid == 0)
-      for (int w = 0; w < GRX_THREADS / 32; ++w) { same += W.wsum[0][w]; cross += W.wsum[1][w]; }
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { same += W.wsum[0][w]; cross += W.wsum[1][w]; }
   }
   __syncthreads();
 }

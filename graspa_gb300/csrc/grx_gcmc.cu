@@ -83,7 +83,7 @@ template <int PREC>
 // first[box + 1]) of args / stats; every step picks one of them uniformly with word 3
 // of the displacement slot (Select_Box_Component_Molecule, axpy.cu:74-100). All
 // entries of a box share its seed and stream.
-__global__ void __launch_bounds__(GRX_THREADS, 3) gcmc_kernel(const BoxDev* boxes, const GcmcArgs* args,
+__global__ void __launch_bounds__(kCbmcThreads, 3) gcmc_kernel(const BoxDev* boxes, const GcmcArgs* args,
                                                               const int* first, const uint64_t* step0,
                                                               int64_t nsteps, grx_gcmc_stats* stats) {
   const uint64_t first_step = *step0;
@@ -474,9 +474,9 @@ static grx_status prepare_gcmc(grx_box* const* boxes, int32_t nboxes, const grx_
       GRX_REQUIRE(b->stored[d.component] >= (size_t)ms,
                   "grx_gcmc: the component stores no molecule template (set it with n_stored >= molsize)");
       GRX_REQUIRE(d.ntrials >= 1 && d.ntrials <= kMaxTrials, "grx_gcmc: ntrials out of range (1..64)");
-      GRX_REQUIRE(ms == 1 || (d.norient >= 1 && d.norient <= kMaxTrials &&
-                              d.norient * (ms - 1) <= GRX_MAX_TRIAL_BEADS),
-                  "grx_gcmc: norient out of range");
+      GRX_REQUIRE(ms == 1 || (d.norient >= 1 && d.norient <= kMaxTrials && d.norient * (ms - 1) <= kCbmcBeads),
+                  "grx_gcmc: norient * (molecule size - 1) must be <= 128");
+      GRX_REQUIRE(2 * ms <= kCbmcBeads, "grx_gcmc: molecule too large");
       GRX_REQUIRE(d.beta > 0 && d.pressure > 0 && d.ideal_rosenbluth > 0, "grx_gcmc: bad thermodynamic state");
       GcmcArgs a{};
       a.d = d;
@@ -522,11 +522,11 @@ static grx_status enqueue_gcmc(grx_precision prec, int nboxes, const BoxDev* dbo
                                const int* dfirst, uint64_t* dstep, int64_t nsteps, grx_gcmc_stats* dstats,
                                size_t smem, cudaStream_t stream) {
   if (prec == GRX_FP64)
-    gcmc_kernel<GRX_FP64><<<nboxes, GRX_THREADS, smem, stream>>>(dboxes, dargs, dfirst, dstep, nsteps, dstats);
+    gcmc_kernel<GRX_FP64><<<nboxes, kCbmcThreads, smem, stream>>>(dboxes, dargs, dfirst, dstep, nsteps, dstats);
   else if (prec == GRX_MIXED)
-    gcmc_kernel<GRX_MIXED><<<nboxes, GRX_THREADS, smem, stream>>>(dboxes, dargs, dfirst, dstep, nsteps, dstats);
+    gcmc_kernel<GRX_MIXED><<<nboxes, kCbmcThreads, smem, stream>>>(dboxes, dargs, dfirst, dstep, nsteps, dstats);
   else
-    gcmc_kernel<GRX_FP32><<<nboxes, GRX_THREADS, smem, stream>>>(dboxes, dargs, dfirst, dstep, nsteps, dstats);
+    gcmc_kernel<GRX_FP32><<<nboxes, kCbmcThreads, smem, stream>>>(dboxes, dargs, dfirst, dstep, nsteps, dstats);
   advance_step_kernel<<<1, 1, 0, stream>>>(dstep, nsteps);
   count_launch();
   count_launch();
