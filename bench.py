@@ -135,15 +135,24 @@ def work_of(stats, ms, nfw):
 
 
 def make_boxes(grx, system, n, stream_ptr, cap_molecules=160):
+    """n chains of one system: a box and n-1 replicas sharing its framework (one copy
+    of framework atoms, tiles and tables on the device for all chains)."""
     nfw = system["comp_start"][1]
     ms = int(system["molsize"][1])
-    boxes = []
-    for _ in range(n):
-        b = grx.Box(system, capacity=[nfw, ms * cap_molecules])
-        b.set_stream(stream_ptr)
-        b.ewald_total()
-        boxes.append(b)
+    parent = grx.Box(system, capacity=[nfw, ms * cap_molecules])
+    parent.set_stream(stream_ptr)
+    parent.ewald_total()
+    boxes = [parent]
+    for _ in range(n - 1):
+        r = parent.replica()
+        r.set_stream(stream_ptr)
+        boxes.append(r)
     return boxes
+
+
+def close_boxes(boxes):
+    for b in reversed(boxes):   # replicas before their parent
+        b.close()
 
 
 def total_energy(box):
@@ -214,8 +223,7 @@ def bench_gcmc(args, grx, torch, stream, flush, rank, world, dist):
     acc_stats, nxt = batch.stats()
     batch.close()
     if args.profile:
-        for b in boxes:
-            b.close()
+        close_boxes(boxes)
         return out
     # drift and loading of the timed chains (all steps since creation)
     drift = []
@@ -231,8 +239,7 @@ def bench_gcmc(args, grx, torch, stream, flush, rank, world, dist):
         "acceptance": [float(sum(st.accepted[k] for st in acc_stats) / max(1, sum(st.attempts[k] for st in acc_stats)))
                        for k in range(4)],
     }
-    for b in boxes:
-        b.close()
+    close_boxes(boxes)
 
     # the same batch in FP64
     boxes = make_boxes(grx, system, R, stream.cuda_stream)
@@ -241,8 +248,7 @@ def bench_gcmc(args, grx, torch, stream, flush, rank, world, dist):
     t64, st64 = timed_graph(torch, batch, stream, S, k64, 1, flush)
     te64, _ = work_of(st64, ms, nfw)
     batch.close()
-    for b in boxes:
-        b.close()
+    close_boxes(boxes)
     # the plain FP64 single-box form
     box1 = make_boxes(grx, system, 1, stream.cuda_stream)
     batch = grx.GcmcBatch(box1, descs[:1], grx.GRX_FP64)
@@ -261,8 +267,7 @@ def bench_gcmc(args, grx, torch, stream, flush, rank, world, dist):
     for name, p in (("fp64", grx.GRX_FP64), ("mixed", grx.GRX_MIXED)):
         bx = make_boxes(grx, system, n_cmp, stream.cuda_stream)
         res[name] = grx.gcmc_run(bx, descs[:n_cmp], 0, 300, p)
-        for b in bx:
-            b.close()
+        close_boxes(bx)
     same = [list(a.accepted) == list(b.accepted) and a.n_molecules == b.n_molecules
             for a, b in zip(res["fp64"], res["mixed"])]
     rel = [abs(a.energy[3] - b.energy[3]) / max(abs(b.energy[3]), 1.0 / beta)
@@ -283,8 +288,7 @@ def bench_gcmc(args, grx, torch, stream, flush, rank, world, dist):
         if i >= args.warmup:
             e2e.append(dt)
             te_e2e += work_of(st, ms, nfw)[0]
-    for b in boxes:
-        b.close()
+    close_boxes(boxes)
     desc_bytes = R * 160 + 8
     out["e2e"] = {"value": te_e2e * world / sum(e2e), "unit": "trial_energies/s",
                   "h2d_bytes_per_step": desc_bytes, "d2h_bytes_per_step": R * 136}
@@ -456,7 +460,8 @@ def run_grx(args):
             "vs_baseline": None, "dtype": "fp32+fp64",
             "data": "synthetic (seeded Philox framework, Philox move stream)",
             "config": {"workload": "gcmc_co2_silica_3456 (1:1:1:1 translation/rotation/insertion/deletion, "
-                                   "k=10, 300 K, 1e5 Pa, boxes start empty)",
+                                   "k=10, 300 K, 1e5 Pa, boxes start empty; chains are replicas sharing one "
+                                   "framework copy)",
                        "chains": g["chains"], "mc_steps_per_step": g["mc_steps_per_step"],
                        "autotune": g.get("autotune"),
                        "trial_energies_per_step": g["trial_energies"] / args.steps,
@@ -543,12 +548,7 @@ def bench_other(args, grx, torch, stream, flush, which):
                            max_translation=0.5, max_rotation=0.4, seed=42, stream=k) for k in range(R)]
     out = {}
     for name, p in (("mixed", grx.GRX_MIXED), ("fp64", grx.GRX_FP64)):
-        boxes = []
-        for _ in range(R):
-            b = grx.Box(system, capacity=[nfw, 4 * 400])
-            b.set_stream(stream.cuda_stream)
-            b.ewald_total()
-            boxes.append(b)
+        boxes = make_boxes(grx, system, R, stream.cuda_stream, cap_molecules=400)
         e0 = [total_energy(b) for b in boxes[:4]]
         for b in boxes[:4]:
             b.ewald_total()
@@ -564,8 +564,7 @@ def bench_other(args, grx, torch, stream, flush, which):
                  for i, b in enumerate(boxes[:4])]
         out[name] = {"value": te / sum(times), "loading": float(np.mean([s.n_molecules for s in acc])),
                      "drift_max_beta_abs": float(max(drift))}
-        for b in boxes:
-            b.close()
+        close_boxes(boxes)
     return {"metric": "CBMC trial energies/s", "value": out["mixed"]["value"], "unit": "trial_energies/s",
             "n_gpus": 1, "workload": "gcmc_tip4p_ew_hexagonal_864 (alpha 0.30, kmax 10/10/8, cutoff 11 A)",
             "chains": R, "mc_steps_per_step": args.mc_steps, "mixed": out["mixed"], "fp64": out["fp64"],

@@ -123,6 +123,14 @@ void refresh_dev(grx_box* b) {
   d.ewA = b->ewA;
   d.ewF = b->ewF;
   d.ewT = b->ewT;
+  const grx_box* h = b->parent ? b->parent : b;
+  d.hpos64 = h->pos64;
+  d.hhi = h->hi;
+  d.hlo = h->lo;
+  d.hmeta = h->meta;
+  d.hscale = h->scale;
+  d.hqdf = h->qdf;
+  d.shared_host = b->parent ? 1 : 0;
 }
 
 static float2 split_df(double x) {
@@ -623,8 +631,83 @@ grx_status grx_box_footprint(const grx_box_desc* desc, size_t* bytes) {
   return GRX_OK;
 }
 
+grx_status grx_box_create_replica(grx_box* parent, grx_box** out) {
+  GRX_REQUIRE(parent && out, "grx_box_create_replica: null argument");
+  GRX_REQUIRE(!parent->parent, "grx_box_create_replica: the parent is itself a replica");
+  GRX_REQUIRE(parent->sk_valid, "grx_box_create_replica: the parent needs current structure factors");
+  *out = nullptr;
+  if (!parent->ewdf_valid && parent->nact > 0) {
+    grx_status st = ewald_df_refresh(parent);
+    if (st) return st;
+  }
+  GRX_CHECK_CUDA(cudaStreamSynchronize(parent->stream), "replica: parent ready");
+  grx_box* r = new grx_box(*parent);
+  r->parent = parent;
+  r->replicas = 0;
+  r->pos64 = nullptr; r->hi = nullptr; r->lo = nullptr; r->meta = nullptr; r->scale = nullptr;
+  r->charge = nullptr; r->qdf = nullptr; r->d_size = nullptr;
+  r->s_ads = nullptr; r->s_tmp = nullptr; r->ewA = nullptr;
+  r->scratch = nullptr; r->scratch_bytes = 0; r->d_results = nullptr; r->results_cap = 0;
+  r->pinned = nullptr; r->pinned_bytes = 0; r->tile_cap = 0;
+  parent->replicas++;
+  const size_t n = r->total_cap, nv = std::max(r->nvec, 1), na = std::max(r->nact, 1);
+  cudaError_t e = cudaSuccess;
+  auto al = [&](void** p, size_t bytes) { if (e == cudaSuccess) e = dev_alloc(r, p, bytes); };
+  al((void**)&r->pos64, n * sizeof(double4));
+  al((void**)&r->hi, n * sizeof(float4));
+  al((void**)&r->lo, n * sizeof(float4));
+  al((void**)&r->meta, n * sizeof(int2));
+  al((void**)&r->scale, n * sizeof(double));
+  al((void**)&r->charge, n * sizeof(double));
+  al((void**)&r->qdf, n * sizeof(float2));
+  al((void**)&r->d_size, GRX_MAX_COMPONENTS * sizeof(int));
+  al((void**)&r->s_ads, nv * sizeof(double2));
+  al((void**)&r->s_tmp, nv * sizeof(double2));
+  al((void**)&r->ewA, na * sizeof(float4));
+  if (e != cudaSuccess) {
+    grx_status st = cuda_status(e, "replica allocation");
+    grx_box_destroy(r);
+    return st;
+  }
+  // guests (and their templates), sizes and S_ads from the parent
+  const size_t g0 = r->off[r->nhost], gn = n - g0;
+  auto cp = [&](void* dst, const void* src, size_t bytes) {
+    if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, r->stream);
+  };
+  cp(r->pos64 + g0, parent->pos64 + g0, gn * sizeof(double4));
+  cp(r->hi + g0, parent->hi + g0, gn * sizeof(float4));
+  cp(r->lo + g0, parent->lo + g0, gn * sizeof(float4));
+  cp(r->meta + g0, parent->meta + g0, gn * sizeof(int2));
+  cp(r->scale + g0, parent->scale + g0, gn * sizeof(double));
+  cp(r->charge + g0, parent->charge + g0, gn * sizeof(double));
+  cp(r->qdf + g0, parent->qdf + g0, gn * sizeof(float2));
+  cp(r->d_size, parent->d_size, GRX_MAX_COMPONENTS * sizeof(int));
+  cp(r->s_ads, parent->s_ads, nv * sizeof(double2));
+  cp(r->s_tmp, parent->s_tmp, nv * sizeof(double2));
+  if (e == cudaSuccess) e = cudaStreamSynchronize(r->stream);
+  if (e != cudaSuccess) {
+    grx_status st = cuda_status(e, "replica copy");
+    grx_box_destroy(r);
+    return st;
+  }
+  r->ewdf_valid = false;  // its S_ads table; the framework tables are the parent's
+  refresh_dev(r);
+  *out = r;
+  return GRX_OK;
+}
+
 grx_status grx_box_destroy(grx_box* b) {
   if (!b) return GRX_OK;
+  GRX_REQUIRE(b->replicas == 0, "grx_box_destroy: the box still has live replicas");
+  if (b->parent) {  // free only what the replica owns
+    void* own[] = {b->pos64, b->hi, b->lo, b->meta, b->scale, b->charge, b->d_size, b->qdf,
+                   b->s_ads, b->s_tmp, b->ewA, b->scratch, b->d_results};
+    for (void* p : own) dev_free(b, p);
+    if (b->pinned) cudaFreeHost(b->pinned);
+    b->parent->replicas--;
+    delete b;
+    return GRX_OK;
+  }
   void* ptrs[] = {b->pos64, b->hi, b->lo, b->meta, b->scale, b->charge, b->d_size, b->ff64,
                   b->ffc10, b->ff32, b->kact, b->ktemp, b->s_fw, b->s_ads, b->s_tmp,
                   b->scratch, b->d_results, b->tile_c, b->tile_r, b->ctab, b->ctabf, b->qdf,
@@ -644,6 +727,8 @@ grx_status grx_box_set_stream(grx_box* b, void* s) {
 grx_status grx_box_set_component(grx_box* b, int32_t comp, const grx_atoms* a, int32_t rigid) {
   GRX_REQUIRE(b && a, "grx_box_set_component: null argument");
   GRX_REQUIRE(comp >= 0 && comp < b->ncomp, "grx_box_set_component: component out of range");
+  GRX_REQUIRE(comp >= b->nhost || (!b->parent && b->replicas == 0),
+              "grx_box_set_component: framework atoms are shared with replicas (set them on a box without any)");
   const size_t nst = std::max(a->n_stored, a->size);
   if (nst > b->cap[comp] || a->size > b->cap[comp]) {
     set_error("grx_box_set_component: %zu atoms exceed capacity %zu of component %d", nst,
@@ -766,8 +851,9 @@ grx_status grx_box_get_positions(grx_box* b, int32_t comp, double* out, size_t n
   GRX_REQUIRE(b && out && comp >= 0 && comp < b->ncomp, "grx_box_get_positions: bad argument");
   GRX_REQUIRE(n <= b->cap[comp], "grx_box_get_positions: n exceeds capacity");
   std::vector<double4> p(n);
+  const double4* src = (comp < b->nhost && b->parent) ? b->parent->pos64 : b->pos64;
   if (n)
-    GRX_CHECK_CUDA(cudaMemcpy(p.data(), b->pos64 + b->off[comp], n * sizeof(double4), cudaMemcpyDeviceToHost),
+    GRX_CHECK_CUDA(cudaMemcpy(p.data(), src + b->off[comp], n * sizeof(double4), cudaMemcpyDeviceToHost),
                    "read positions");
   std::vector<double> flat(3 * n);
   const std::vector<int>& perm = b->perm[comp];
@@ -796,6 +882,7 @@ grx_status grx_ewald_sizes(grx_box* b, int64_t* nvec, int64_t* nactive) {
 
 grx_status grx_ewald_set_structure_factors(grx_box* b, const double* s_fw, const double* s_ads) {
   GRX_REQUIRE(b && s_fw && s_ads, "grx_ewald_set_structure_factors: null argument");
+  GRX_REQUIRE(!b->parent, "grx_ewald_set_structure_factors: a replica's framework structure factor is its parent's");
   GRX_CHECK_CUDA(cudaMemcpy(b->s_fw, s_fw, b->nvec * sizeof(double2), cudaMemcpyDefault), "set S_fw");
   GRX_CHECK_CUDA(cudaMemcpy(b->s_ads, s_ads, b->nvec * sizeof(double2), cudaMemcpyDefault), "set S_ads");
   GRX_CHECK_CUDA(cudaMemcpy(b->s_tmp, s_ads, b->nvec * sizeof(double2), cudaMemcpyDefault), "set S_tmp");

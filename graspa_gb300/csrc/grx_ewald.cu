@@ -32,7 +32,7 @@ __global__ void eik_tables_kernel(BoxDev b, CompRanges r, double2* ex, double2* 
   if (j >= r.n) return;
   int local;
   const int c = comp_of(r, j, local);
-  const double4 p = b.pos64[r.off[c] + local];
+  const double4 p = atom_pos64(b, r.off[c] + local);
   const double PI2 = 2.0 * 3.14159265358979323846;
   double s[3];
   s[0] = (b.inv[0] * p.x + b.inv[3] * p.y + b.inv[6] * p.z) * PI2;
@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(GRX_THREADS) sk_kernel(BoxDev b, CompRanges r,
   for (int j = threadIdx.x; j < r.n; j += blockDim.x) {
     int local;
     const int c = comp_of(r, j, local);
-    const double q = b.pos64[r.off[c] + local].w;
+    const double q = atom_pos64(b, r.off[c] + local).w;
     const double2 t = eik_term(ex, ey, ez, r.n, j, k.x, k.y, k.z);
     if (j < nhost_atoms) { fr += q * t.x; fi += q * t.y; }
     else { ar += q * t.x; ai += q * t.y; }
@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(GRX_THREADS) sk_kernel(BoxDev b, CompRanges r,
   ar = block_sum(ar, sbuf);
   ai = block_sum(ai, sbuf);
   if (threadIdx.x == 0) {
-    b.s_fw[k.w] = make_double2(fr, fi);
+    if (!b.shared_host) b.s_fw[k.w] = make_double2(fr, fi);  // a replica reads its parent's
     b.s_ads[k.w] = make_double2(ar, ai);
     b.s_tmp[k.w] = make_double2(ar, ai);
   }
@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(GRX_THREADS) self_excl_kernel(BoxDev b, CompRa
   if (j < r.n) {
     int local;
     const int c = comp_of(r, j, local);
-    const double4 p = b.pos64[r.off[c] + local];
+    const double4 p = atom_pos64(b, r.off[c] + local);
     const double pself = b.prefactor * b.alpha / sqrt(3.14159265358979323846);
     const double v = pself * p.w * p.w;
     sa = v;
@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(GRX_THREADS) self_excl_kernel(BoxDev b, CompRa
     const int mol0 = (local / ms) * ms;
     const int lend = ms > kBigMolecule ? local + 1 : min(mol0 + ms, r.base[c + 1] - r.base[c]);
     for (int l2 = local + 1; l2 < lend; ++l2) {
-      const double4 q = b.pos64[r.off[c] + l2];
+      const double4 q = atom_pos64(b, r.off[c] + l2);
       double x = p.x - q.x, y = p.y - q.y, z = p.z - q.z;
       pbc64(b, x, y, z);
       const double rr = sqrt(x * x + y * y + z * z);
@@ -150,8 +150,8 @@ __global__ void __launch_bounds__(GRX_THREADS) big_excl_kernel(BoxDev b, CompRan
     const int i = rem / ms, j = rem - i * ms;
     const int li = (int)(m * ms) + i, lj = (int)(m * ms) + j;
     if (j <= i || lj >= n) continue;
-    const double4 a = b.pos64[r.off[c] + li];
-    const double4 q = b.pos64[r.off[c] + lj];
+    const double4 a = atom_pos64(b, r.off[c] + li);
+    const double4 q = atom_pos64(b, r.off[c] + lj);
     double x = a.x - q.x, y = a.y - q.y, z = a.z - q.z;
     pbc64(b, x, y, z);
     const double rr = sqrt(x * x + y * y + z * z);
@@ -175,9 +175,9 @@ __global__ void __launch_bounds__(GRX_THREADS) vdw_real_total_kernel(BoxDev b, C
     int li;
     const int ci = comp_of(r, j, li);
     const int ii = r.off[ci] + li;
-    const double4 p = b.pos64[ii];
-    const int2 mi = b.meta[ii];
-    const double si = b.scale[ii];
+    const double4 p = atom_pos64(b, ii);
+    const int2 mi = atom_meta(b, ii);
+    const double si = atom_scale(b, ii);
     for (int cj = 0; cj < r.ncomp; ++cj) {
       int it;
       if (ci < r.nhost || cj < r.nhost) it = (!(ci < r.nhost) || !(cj < r.nhost)) ? 1 : 0;
@@ -185,13 +185,13 @@ __global__ void __launch_bounds__(GRX_THREADS) vdw_real_total_kernel(BoxDev b, C
       const int nj = r.base[cj + 1] - r.base[cj];
       for (int lj = 0; lj < nj; ++lj) {
         const int jj = r.off[cj] + lj;
-        const int2 mj = b.meta[jj];
+        const int2 mj = atom_meta(b, jj);
         if (mi.y == mj.y && ci == cj) continue;
-        const double4 q = b.pos64[jj];
+        const double4 q = atom_pos64(b, jj);
         double x = p.x - q.x, y = p.y - q.y, z = p.z - q.z;
         pbc64(b, x, y, z);
         const double rr = x * x + y * y + z * z;
-        if (rr < b.cut_vdw2) e[2 * it] += 0.5 * vdw64(b, mi.x * b.ntypes + mj.x, rr, si * b.scale[jj]);
+        if (rr < b.cut_vdw2) e[2 * it] += 0.5 * vdw64(b, mi.x * b.ntypes + mj.x, rr, si * atom_scale(b, jj));
         if (!b.no_charges && rr < b.cut_coul2) e[2 * it + 1] += 0.5 * coul64(b, p.w * q.w, rr);
       }
     }
@@ -326,7 +326,8 @@ grx_status grx_ewald_total(grx_box* b, double* out8) {
     eik_tables_kernel<<<nblk_atoms, GRX_THREADS, 0, b->stream>>>(b->dev, r, ex, ey, ez);
     count_launch();
   }
-  GRX_CHECK_CUDA(cudaMemsetAsync(b->s_fw, 0, b->nvec * sizeof(double2), b->stream), "clear S_fw");
+  if (!b->parent)  // a replica's framework structure factor is its parent's, shared by every replica
+    GRX_CHECK_CUDA(cudaMemsetAsync(b->s_fw, 0, b->nvec * sizeof(double2), b->stream), "clear S_fw");
   GRX_CHECK_CUDA(cudaMemsetAsync(b->s_ads, 0, b->nvec * sizeof(double2), b->stream), "clear S_ads");
   GRX_CHECK_CUDA(cudaMemsetAsync(b->s_tmp, 0, b->nvec * sizeof(double2), b->stream), "clear S_tmp");
   if (b->nact > 0 && r.n > 0) {
@@ -478,6 +479,7 @@ grx_status grx_ewald_commit(grx_box* b, int32_t comp) {
   GRX_REQUIRE(b && comp >= 0 && comp < b->ncomp, "grx_ewald_commit: bad argument");
   if (b->nact == 0) return GRX_OK;
   refresh_dev(b);
+  GRX_REQUIRE(comp >= b->nhost || !b->parent, "grx_ewald_commit: a replica cannot move its shared framework");
   double2* dst = comp < b->nhost ? b->s_fw : b->s_ads;
   commit_kernel<<<std::max(1, std::min((b->nact + 255) / 256, sm_count(b))), 256, 0, b->stream>>>(b->dev, dst, b->s_tmp);
   count_launch();

@@ -401,10 +401,20 @@ __global__ void ewald_df_refresh_gcmc(BoxDev b) {
     const double2 sa = b.s_ads[slot], sf = b.s_fw[slot];
     const df ar = df_from(t * sa.x), ai = df_from(t * sa.y), fr = df_from(t * sf.x), fi = df_from(t * sf.y);
     ewA[j] = make_float4(ar.hi, ar.lo, ai.hi, ai.lo);
+    if (b.shared_host) continue;  // a replica's framework tables are its parent's
     ewF[j] = make_float4(fr.hi, fr.lo, fi.hi, fi.lo);
     const df tt = df_from(t);
     ewT[j] = make_float2(tt.hi, tt.lo);
   }
+}
+
+grx_status ewald_df_refresh(grx_box* b) {
+  refresh_dev(b);
+  ewald_df_refresh_gcmc<<<std::max(1, std::min((b->nact + 255) / 256, sm_count(b))), 256, 0, b->stream>>>(b->dev);
+  count_launch();
+  GRX_CHECK_CUDA(cudaGetLastError(), "ewald table refresh");
+  b->ewdf_valid = true;
+  return GRX_OK;
 }
 
 }  // namespace grx
@@ -495,10 +505,8 @@ static grx_status prepare_gcmc(grx_box* const* boxes, int32_t nboxes, const grx_
       smem = std::max(smem, need);
     }
     if (!b->ewdf_valid && b->nact > 0) {
-      ewald_df_refresh_gcmc<<<std::max(1, std::min((b->nact + 255) / 256, sm_count(b))), 256, 0,
-                              boxes[0]->stream>>>(b->dev);
-      count_launch();
-      b->ewdf_valid = true;
+      grx_status st = ewald_df_refresh(b);
+      if (st) return st;
     }
     hb[i] = b->dev;
   }

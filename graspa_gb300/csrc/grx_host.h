@@ -9,6 +9,8 @@
 struct grx_box {
   grx::BoxDev dev{};
   grx_arena* arena = nullptr;  // device memory comes from here when set (else cudaMalloc)
+  grx_box* parent = nullptr;   // a replica shares its parent's framework atoms, tiles and tables
+  int replicas = 0;            // live replicas of this box
   cudaStream_t stream = nullptr;
   int device = 0;
   int num_sms = 0;
@@ -91,6 +93,9 @@ void* arena_alloc(grx_arena* a, size_t bytes);
 void arena_free(grx_arena* a, void* p);
 // Device allocation of a box: from its arena when it has one, else cudaMalloc.
 cudaError_t dev_alloc(grx_box* b, void** p, size_t bytes);
+// Builds the double-float S(k) tables of a box on its stream (framework tables skipped
+// for replicas) and marks them valid.
+grx_status ewald_df_refresh(grx_box* b);
 void dev_free(grx_box* b, void* p);
 }  // namespace grx
 

@@ -64,6 +64,15 @@ struct BoxDev {
   const double* scale;
   const double* charge;  // bare charge (Atoms.charge), templates for trial beads
   int host_end;          // storage index where guest components begin
+  // host (framework) atoms, index < host_end: the box's own arrays, or a parent box's
+  // when the box is a replica sharing its framework (guests are always the box's own)
+  const double4* hpos64;
+  const float4* hhi;
+  const float4* hlo;
+  const int2* hmeta;
+  const double* hscale;
+  const float2* hqdf;
+  int shared_host;       // 1: host atoms, tiles, tables and framework S(k) belong to a parent
   // spatial tiles of host atoms (32 atoms each, Morton order)
   const float4* tile_c;  // bounding sphere {x, y, z, radius}
   const int4* tile_r;    // {first atom, end atom, component, 0}
@@ -260,32 +269,43 @@ __device__ __forceinline__ void make_bead(Bead& bd, double x, double y, double z
 
 // Energy of one (atom, bead) pair. Returns true when the pair is inside a cutoff;
 // adds to vdw / real and sets `flag` on overlap (VDW_Coulomb.cu:1290-1322).
+// Atom arrays by storage index: host atoms may live in a parent box (replicas).
+__device__ __forceinline__ double4 atom_pos64(const BoxDev& b, int i) { return i < b.host_end ? b.hpos64[i] : b.pos64[i]; }
+__device__ __forceinline__ int2 atom_meta(const BoxDev& b, int i) { return i < b.host_end ? b.hmeta[i] : b.meta[i]; }
+__device__ __forceinline__ double atom_scale(const BoxDev& b, int i) { return i < b.host_end ? b.hscale[i] : b.scale[i]; }
+
 template <int PREC>
 __device__ __forceinline__ void pair_energy(const BoxDev& b, int i, const Bead& bd, int rowbase,
                                             double& vdw, double& real, int& flag) {
+  const bool host = i < b.host_end;
+  const double4* P64 = host ? b.hpos64 : b.pos64;
+  const float4* HI = host ? b.hhi : b.hi;
+  const float4* LO = host ? b.hlo : b.lo;
+  const int2* META = host ? b.hmeta : b.meta;
+  const double* SC = host ? b.hscale : b.scale;
   if (PREC == GRX_FP64) {
-    const double4 p = b.pos64[i];
+    const double4 p = P64[i];
     double x = p.x - bd.x, y = p.y - bd.y, z = p.z - bd.z;
     pbc64(b, x, y, z);
     const double rr = x * x + y * y + z * z;
-    const int2 mt = b.meta[i];
+    const int2 mt = META[i];
     if (rr < b.cut_vdw2) {
-      const double e = vdw64(b, mt.x * b.ntypes + bd.type, rr, b.scale[i] * bd.scale);
+      const double e = vdw64(b, mt.x * b.ntypes + bd.type, rr, SC[i] * bd.scale);
       if (e > b.overlap) flag = 1;
       if (rr < 0.01) flag = 1;
       vdw += e;
     }
     if (!b.no_charges && rr < b.cut_coul2) real += coul64(b, p.w * bd.q, rr);
   } else {
-    const float4 ah = b.hi[i];
-    const float4 al = b.lo[i];
+    const float4 ah = HI[i];
+    const float4 al = LO[i];
     float3 dh = make_float3(ah.x - bd.h.x, ah.y - bd.h.y, ah.z - bd.h.z);
     float3 dl = make_float3(al.x - bd.l.x, al.y - bd.l.y, al.z - bd.l.z);
     pbc_split(b, dh, dl);
     const float fx = dh.x + dl.x, fy = dh.y + dl.y, fz = dh.z + dl.z;
     const float rr32 = fx * fx + fy * fy + fz * fz;
     if (rr32 >= b.screen2) return;
-    const int2 mt = b.meta[i];
+    const int2 mt = META[i];
     const int row = mt.x * b.ntypes + bd.type;
     if (PREC == GRX_MIXED) {
       const double x = (double)dh.x + (double)dl.x;
@@ -297,12 +317,12 @@ __device__ __forceinline__ void pair_energy(const BoxDev& b, int i, const Bead& 
         const bool unit = (al.w == 1.0f) && (bd.scale == 1.0) && !b.use_1264;
         double e;
         if (unit && (float)rr > f.w) e = (double)vdw32(f, (float)rr);
-        else e = vdw64(b, row, rr, b.scale[i] * bd.scale);
+        else e = vdw64(b, row, rr, SC[i] * bd.scale);
         if (e > b.overlap) flag = 1;
         if (rr < 0.01) flag = 1;
         vdw += e;
       }
-      if (!b.no_charges && rr < b.cut_coul2) real += coul64(b, b.pos64[i].w * bd.q, rr);
+      if (!b.no_charges && rr < b.cut_coul2) real += coul64(b, P64[i].w * bd.q, rr);
     } else {  // GRX_FP32
       const float sc = al.w * (float)bd.scale;
       if (rr32 < b.cut_vdw2f) {
@@ -336,7 +356,7 @@ __device__ __forceinline__ void bead_pass(const BoxDev& b, const Bead& bd, int l
 #pragma unroll 2
     for (int i = lane; i < n; i += lane_stride) {
       if (check_mol) {
-        const int mol = b.meta[off + i].y;
+        const int mol = atom_meta(b, off + i).y;
         if ((c == excl_comp && mol == excl_mol) || (c == component && mol == newmol)) continue;
       }
       pair_energy<PREC>(b, off + i, bd, 0, v, r, flag);

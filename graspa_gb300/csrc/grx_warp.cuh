@@ -65,16 +65,16 @@ __device__ __forceinline__ void image_split(const BoxDev& b, float3& dh, float3&
 // Screening test of one pair (true when it may lie inside a cutoff). FP64 form: the
 // exact FP64 test. Mixed / FP32 forms: FP32 on the hi parts alone (16 bytes per
 // atom), against a radius padded for the hi rounding.
-template <int PREC>
+template <int PREC, bool HOST>
 __device__ __forceinline__ bool pair_screen(const BoxDev& b, int i, const Bead& bd) {
   if (PREC == GRX_FP64) {
-    const double4 p = b.pos64[i];
+    const double4 p = (HOST ? b.hpos64 : b.pos64)[i];
     double x = p.x - bd.x, y = p.y - bd.y, z = p.z - bd.z;
     pbc64(b, x, y, z);
     const double rr = x * x + y * y + z * z;
     return rr < b.cut_vdw2 || (!b.no_charges && rr < b.cut_coul2);
   } else {
-    const float4 ah = b.hi[i];
+    const float4 ah = (HOST ? b.hhi : b.hi)[i];
     float x = ah.x - bd.h.x, y = ah.y - bd.h.y, z = ah.z - bd.h.z;
     if (b.cubic) {
       x = __fmaf_rn(-rnd(x * b.invf[0]), b.cellf[0], x);
@@ -131,26 +131,31 @@ template <int PREC> __device__ __forceinline__ double acc_value(const LaneAcc<PR
 // Dense evaluation of one screened pair: exact cutoff tests, LJ, real Coulomb,
 // overlap flag (VDW_Coulomb.cu:1287-1322). pq = prefactor * q_bead (double-float
 // in the mixed form).
-template <int PREC>
+template <int PREC, bool HOST>
 __device__ __forceinline__ void pair_dense(const BoxDev& b, int i, const Bead& bd, df pq,
                                            LaneAcc<PREC>& acc, int& flag) {
-  const int2 mt = b.meta[i];
+  const double4* P64 = HOST ? b.hpos64 : b.pos64;
+  const float4* HI = HOST ? b.hhi : b.hi;
+  const float4* LO = HOST ? b.hlo : b.lo;
+  const double* SC = HOST ? b.hscale : b.scale;
+  const float2* QDF = HOST ? b.hqdf : b.qdf;
+  const int2 mt = (HOST ? b.hmeta : b.meta)[i];
   const int row = mt.x * b.ntypes + bd.type;
   if constexpr (PREC == GRX_FP64) {
-    const double4 p = b.pos64[i];
+    const double4 p = P64[i];
     double x = p.x - bd.x, y = p.y - bd.y, z = p.z - bd.z;
     pbc64(b, x, y, z);
     const double rr = x * x + y * y + z * z;
     if (rr < b.cut_vdw2) {
-      const double e = vdw64(b, row, rr, b.scale[i] * bd.scale);
+      const double e = vdw64(b, row, rr, SC[i] * bd.scale);
       if (e > b.overlap) flag = 1;
       if (rr < 0.01) flag = 1;
       acc.v += e;
     }
     if (!b.no_charges && rr < b.cut_coul2) acc.r += coul64(b, p.w * bd.q, rr);
   } else {
-    const float4 ah = b.hi[i];
-    const float4 al = b.lo[i];
+    const float4 ah = HI[i];
+    const float4 al = LO[i];
     float3 dh = make_float3(ah.x - bd.h.x, ah.y - bd.h.y, ah.z - bd.h.z);
     float3 dl = make_float3(al.x - bd.l.x, al.y - bd.l.y, al.z - bd.l.z);
     image_split(b, dh, dl);
@@ -162,7 +167,7 @@ __device__ __forceinline__ void pair_dense(const BoxDev& b, int i, const Bead& b
         df e;
         if (unit && s.hi > f.w) e = df{vdw32(f, s.hi), 0.0f};
         else if (unit) e = lj_df(b, row, s);
-        else e = df_from(vdw64(b, row, df_to(s), b.scale[i] * bd.scale));
+        else e = df_from(vdw64(b, row, df_to(s), SC[i] * bd.scale));
         if (e.hi > b.overlapf) flag = 1;
         if (s.hi < 0.01f) flag = 1;
         acc.v = df_add(acc.v, e);
@@ -172,7 +177,7 @@ __device__ __forceinline__ void pair_dense(const BoxDev& b, int i, const Bead& b
         const int k = (__float_as_int(s.hi) >> 17) - b.ctab_base;
         if (k >= 0 && k < b.ctab_n) g = coul_table_df(b, s);
         else { const double rr = df_to(s), r = sqrt(rr); g = df_from(erfc(b.alpha * r) / r); }
-        const float2 qa = b.qdf[i];
+        const float2 qa = QDF[i];
         acc.r = df_add(acc.r, df_mul(g, df{qa.x, qa.y}));  // prefactor * q_bead applied once per item
       }
     } else {  // GRX_FP32
@@ -263,18 +268,18 @@ __device__ __forceinline__ void warp_item(const BoxDev& b, const Bead& bd, int t
       if (i < tr.y) {
         bool skip = false;
         if (tr.z == component || tr.z == excl_comp) {
-          const int mol = b.meta[i].y;
+          const int mol = b.hmeta[i].y;
           skip = (tr.z == excl_comp && mol == excl_mol) || (tr.z == component && mol == newmol);
         }
         if (!skip) {
           if (PREC != GRX_FP64 && oi) {
-            const float4 ah = b.hi[i];
+            const float4 ah = b.hhi[i];
             const float x = ah.x - (bd.h.x + tsx);
             const float y = ah.y - (bd.h.y + tsy);
             const float z = ah.z - (bd.h.z + tsz);
             in = x * x + y * y + z * z < b.screen2;
           } else {
-            in = pair_screen<PREC>(b, i, bd);
+            in = pair_screen<PREC, true>(b, i, bd);
           }
         }
       }
@@ -285,13 +290,13 @@ __device__ __forceinline__ void warp_item(const BoxDev& b, const Bead& bd, int t
         __syncwarp();
         const int j = q[(head + lane) & (kQueue - 1)];
         __syncwarp();
-        pair_dense<PREC>(b, j, bd, pq, la, flag);
+        pair_dense<PREC, true>(b, j, bd, pq, la, flag);
         head += 32;
       }
     }
   }
   __syncwarp();
-  if (lane < (int)(tail - head)) pair_dense<PREC>(b, q[(head + lane) & (kQueue - 1)], bd, pq, la, flag);
+  if (lane < (int)(tail - head)) pair_dense<PREC, true>(b, q[(head + lane) & (kQueue - 1)], bd, pq, la, flag);
   __syncwarp();
   if (g1 <= g0) return;
   head = tail = 0;
@@ -312,7 +317,7 @@ __device__ __forceinline__ void warp_item(const BoxDev& b, const Bead& bd, int t
           const int mol = b.meta[i].y;
           skip = (c == excl_comp && mol == excl_mol) || (c == component && mol == newmol);
         }
-        if (!skip) in = pair_screen<PREC>(b, i, bd);
+        if (!skip) in = pair_screen<PREC, false>(b, i, bd);
       }
       const unsigned m = __ballot_sync(kFull, in);
       if (in) q[(tail + __popc(m & lt)) & (kQueue - 1)] = i;
@@ -321,13 +326,13 @@ __device__ __forceinline__ void warp_item(const BoxDev& b, const Bead& bd, int t
         __syncwarp();
         const int j = q[(head + lane) & (kQueue - 1)];
         __syncwarp();
-        pair_dense<PREC>(b, j, bd, pq, gacc, flag);
+        pair_dense<PREC, false>(b, j, bd, pq, gacc, flag);
         head += 32;
       }
     }
   }
   __syncwarp();
-  if (lane < (int)(tail - head)) pair_dense<PREC>(b, q[(head + lane) & (kQueue - 1)], bd, pq, gacc, flag);
+  if (lane < (int)(tail - head)) pair_dense<PREC, false>(b, q[(head + lane) & (kQueue - 1)], bd, pq, gacc, flag);
   __syncwarp();
 }
 

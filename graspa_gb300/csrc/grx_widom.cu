@@ -413,6 +413,7 @@ __global__ void ewald_df_refresh_kernel(BoxDev b, float4* ewA, float4* ewF, floa
     const double2 sa = b.s_ads[slot], sf = b.s_fw[slot];
     const df ar = df_from(t * sa.x), ai = df_from(t * sa.y), fr = df_from(t * sf.x), fi = df_from(t * sf.y);
     ewA[j] = make_float4(ar.hi, ar.lo, ai.hi, ai.lo);
+    if (b.shared_host) continue;  // a replica's framework tables are its parent's
     ewF[j] = make_float4(fr.hi, fr.lo, fi.hi, fi.lo);
     const df tt = df_from(t);
     ewT[j] = make_float2(tt.hi, tt.lo);

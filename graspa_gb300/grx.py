@@ -138,6 +138,7 @@ EXPORTS = [
     "grx_gcmc_batch_reset_stats", "grx_gcmc_batch_autotune", "grx_arena_create", "grx_arena_destroy",
     "grx_arena_usage", "grx_box_create_in", "grx_box_footprint", "grx_server_create", "grx_server_destroy",
     "grx_server_submit", "grx_server_progress", "grx_server_poll", "grx_server_time", "grx_server_launch_count",
+    "grx_box_create_replica",
 ]
 
 _lib = None
@@ -206,6 +207,7 @@ def load(path=LIB_PATH):
     L.grx_arena_usage.argtypes = [C.c_void_p, P(C.c_size_t), P(C.c_size_t), P(C.c_size_t)]
     L.grx_box_create_in.argtypes = [P(BoxDesc), C.c_void_p, P(C.c_void_p)]
     L.grx_box_footprint.argtypes = [P(BoxDesc), P(C.c_size_t)]
+    L.grx_box_create_replica.argtypes = [C.c_void_p, P(C.c_void_p)]
     L.grx_server_create.argtypes = [P(ServerConfig), C.c_void_p, P(C.c_void_p)]
     L.grx_server_destroy.argtypes = [C.c_void_p]
     L.grx_server_submit.argtypes = [C.c_void_p, P(JobDesc), P(C.c_uint64)]
@@ -354,6 +356,17 @@ class Box:
         self.h = h
         for c in range(self.ncomp):
             self.set_component(c)
+
+    def replica(self):
+        """A new box sharing this box's framework (grx_box_create_replica)."""
+        r = Box.__new__(Box)
+        r.L, r.system, r.desc, r._keep = self.L, self.system, self.desc, self._keep
+        r.ncomp, r.nhost = self.ncomp, self.nhost
+        h = C.c_void_p()
+        check(self.L.grx_box_create_replica(self.h, C.byref(h)), "grx_box_create_replica")
+        r.h = h
+        r.parent = self
+        return r
 
     def close(self):
         if getattr(self, "h", None):

@@ -192,7 +192,15 @@ grx_status grx_device_count(int32_t* n);
 /* Allocates the device state of one box (replaces the per-box allocations of
  * fxn_main.h:46-113,163-280 / main.cpp:243-300). */
 grx_status grx_box_create(const grx_box_desc* desc, grx_box** out);
-grx_status grx_box_destroy(grx_box* box);
+grx_status grx_box_destroy(grx_box* box);   /* refused while the box has live replicas */
+/* A replica: a second Markov chain of the same system that shares the parent's
+ * framework atoms, tiles, Coulomb table, force-field tables, k vectors and framework
+ * structure factor (read-only), and owns its adsorbates, S_ads and their tables. It
+ * starts as a copy of the parent's adsorbates. Many replicas keep one copy of the
+ * framework in L1/L2 instead of one per chain. The parent must have current structure
+ * factors, and its framework components cannot change while replicas live. No
+ * counterpart in the reference (one box per simulation). */
+grx_status grx_box_create_replica(grx_box* parent, grx_box** out);
 
 /* ---- device memory arena -------------------------------------------------- */
 /* One reserved region of device memory that boxes are carved from by a host-side
