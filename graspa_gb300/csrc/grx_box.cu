@@ -239,34 +239,47 @@ static grx_status build_coulomb_table(grx_box* b, double alpha, double cut2) {
   return GRX_OK;
 }
 
-static uint64_t spread3(uint32_t v) {  // 10-bit value -> every third bit
-  uint64_t x = v & 0x3ff;
-  x = (x | (x << 16)) & 0x30000ff;
-  x = (x | (x << 8)) & 0x300f00f;
-  x = (x | (x << 4)) & 0x30c30c3;
-  x = (x | (x << 2)) & 0x9249249;
-  return x;
-}
-
-// Morton order of atoms by wrapped fractional coordinates (storage slot -> caller index).
-static void morton_order(const BoxDev& d, const double* pos, size_t n, std::vector<int>& order) {
-  std::vector<uint64_t> code(n);
+// Storage order of host atoms: recursive bisection of the wrapped Cartesian positions
+// along the longest extent, into leaves of 32 consecutive atoms (storage slot -> caller
+// index). Leaves are compact boxes, tighter than runs of a space-filling curve where a
+// framework has pores.
+static void kd_order(const BoxDev& d, const double* pos, size_t n, std::vector<int>& order) {
+  std::vector<double> X(3 * n);
   for (size_t i = 0; i < n; ++i) {
-    uint32_t q[3];
+    double s[3];
     for (int k = 0; k < 3; ++k) {
-      double sk = d.inv[k] * pos[3 * i] + d.inv[3 + k] * pos[3 * i + 1] + d.inv[6 + k] * pos[3 * i + 2];
-      sk -= std::floor(sk);
-      q[k] = (uint32_t)std::min(1023.0, std::max(0.0, sk * 1024.0));
+      s[k] = d.inv[k] * pos[3 * i] + d.inv[3 + k] * pos[3 * i + 1] + d.inv[6 + k] * pos[3 * i + 2];
+      s[k] -= std::floor(s[k]);
     }
-    code[i] = spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
+    for (int j = 0; j < 3; ++j) X[3 * i + j] = s[0] * d.cell[j] + s[1] * d.cell[3 + j] + s[2] * d.cell[6 + j];
   }
   order.resize(n);
   for (size_t i = 0; i < n; ++i) order[i] = (int)i;
-  std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return code[a] < code[c]; });
+  std::vector<std::pair<size_t, size_t>> todo = {{0, n}};
+  while (!todo.empty()) {
+    const auto [lo, hi] = todo.back();
+    todo.pop_back();
+    if (hi - lo <= 32) continue;
+    double mn[3] = {1e300, 1e300, 1e300}, mx[3] = {-1e300, -1e300, -1e300};
+    for (size_t j = lo; j < hi; ++j)
+      for (int k = 0; k < 3; ++k) {
+        mn[k] = std::min(mn[k], X[3 * order[j] + k]);
+        mx[k] = std::max(mx[k], X[3 * order[j] + k]);
+      }
+    int ax = 0;
+    for (int k = 1; k < 3; ++k)
+      if (mx[k] - mn[k] > mx[ax] - mn[ax]) ax = k;
+    std::stable_sort(order.begin() + lo, order.begin() + hi,
+                     [&](int a, int c) { return X[3 * a + ax] < X[3 * c + ax]; });
+    const size_t nl = (((hi - lo) / 32 + 1) / 2) * 32;  // left half: whole leaves
+    todo.push_back({lo + nl, hi});
+    todo.push_back({lo, lo + nl});
+  }
 }
 
-// Tiles of 32 consecutive host atoms with a bounding sphere (centre from minimum
-// images relative to the tile's first atom, radius rounded up).
+// Tiles of 32 consecutive host atoms: two records per tile, {centre, bounding-sphere
+// radius} and {half extents of the bounding box, 0}, from minimum images relative to the
+// tile's first atom, rounded up.
 static grx_status build_tiles(grx_box* b) {
   b->h_tile_c.clear();
   b->h_tile_r.clear();
@@ -299,22 +312,25 @@ static grx_status build_tiles(grx_box* b) {
       }
       const float rad = (float)(std::sqrt(r2) * (1.0 + 1e-6) + 1e-4);
       b->h_tile_c.push_back(make_float4((float)cx, (float)cy, (float)cz, rad));
+      float hw[3];
+      for (int k = 0; k < 3; ++k) hw[k] = (float)(0.5 * (hi[k] - lo[k]) * (1.0 + 1e-6) + 1e-4);
+      b->h_tile_c.push_back(make_float4(hw[0], hw[1], hw[2], 0.0f));
       b->h_tile_r.push_back(make_int4((int)(o + t0), (int)(o + t1), c, compact));
     }
   }
-  b->ntiles = (int)b->h_tile_c.size();
+  b->ntiles = (int)b->h_tile_r.size();
   if ((size_t)b->ntiles > b->tile_cap) {
     dev_free(b, b->tile_c);
     dev_free(b, b->tile_r);
     b->tile_c = nullptr;
     b->tile_r = nullptr;
     b->tile_cap = 0;
-    GRX_CHECK_CUDA(dev_alloc(b, (void**)&b->tile_c, b->ntiles * sizeof(float4)), "alloc tiles");
+    GRX_CHECK_CUDA(dev_alloc(b, (void**)&b->tile_c, 2 * b->ntiles * sizeof(float4)), "alloc tiles");
     GRX_CHECK_CUDA(dev_alloc(b, (void**)&b->tile_r, b->ntiles * sizeof(int4)), "alloc tile ranges");
     b->tile_cap = b->ntiles;
   }
   if (b->ntiles) {
-    GRX_CHECK_CUDA(cudaMemcpy(b->tile_c, b->h_tile_c.data(), b->ntiles * sizeof(float4), cudaMemcpyHostToDevice),
+    GRX_CHECK_CUDA(cudaMemcpy(b->tile_c, b->h_tile_c.data(), 2 * b->ntiles * sizeof(float4), cudaMemcpyHostToDevice),
                    "upload tiles");
     GRX_CHECK_CUDA(cudaMemcpy(b->tile_r, b->h_tile_r.data(), b->ntiles * sizeof(int4), cudaMemcpyHostToDevice),
                    "upload tile ranges");
@@ -775,11 +791,11 @@ grx_status grx_box_set_component(grx_box* b, int32_t comp, const grx_atoms* a, i
     b->excl_intra[comp] = e;
     b->excl_self[comp] = sv;
   }
-  // host (framework) atoms are stored in Morton order so that 32-atom tiles are compact
+  // host (framework) atoms are stored in k-d order so that 32-atom tiles are compact
   b->perm[comp].clear();
   if (comp < b->nhost && a->size > 1) {
     std::vector<int> order;
-    morton_order(b->dev, pos.data(), a->size, order);
+    kd_order(b->dev, pos.data(), a->size, order);
     b->perm[comp] = order;
     std::vector<double> pos2(pos), sc2(sc), q2(q), scc2(scc);
     std::vector<size_t> ty2(ty), mol2(mol);

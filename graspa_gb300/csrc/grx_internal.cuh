@@ -73,8 +73,8 @@ struct BoxDev {
   const double* hscale;
   const float2* hqdf;
   int shared_host;       // 1: host atoms, tiles, tables and framework S(k) belong to a parent
-  // spatial tiles of host atoms (32 atoms each, Morton order)
-  const float4* tile_c;  // bounding sphere {x, y, z, radius}
+  // spatial tiles of host atoms (32 atoms each, k-d order)
+  const float4* tile_c;  // per tile: {x, y, z, bounding radius}, {box half extents, 0}
   const int4* tile_r;    // {first atom, end atom, component, 0}
   int ntiles;
   int cull;              // tile culling on

@@ -65,6 +65,23 @@ __device__ __forceinline__ void image_split(const BoxDev& b, float3& dh, float3&
 // Screening test of one pair (true when it may lie inside a cutoff). FP64 form: the
 // exact FP64 test. Mixed / FP32 forms: FP32 on the hi parts alone (16 bytes per
 // atom), against a radius padded for the hi rounding.
+__device__ __forceinline__ bool screen_hi(const BoxDev& b, float4 ah, const Bead& bd) {
+  float x = ah.x - bd.h.x, y = ah.y - bd.h.y, z = ah.z - bd.h.z;
+  if (b.cubic) {
+    x = __fmaf_rn(-rnd(x * b.invf[0]), b.cellf[0], x);
+    y = __fmaf_rn(-rnd(y * b.invf[4]), b.cellf[4], y);
+    z = __fmaf_rn(-rnd(z * b.invf[8]), b.cellf[8], z);
+  } else {
+    const float nx = rnd(b.invf[0] * x + b.invf[3] * y + b.invf[6] * z);
+    const float ny = rnd(b.invf[1] * x + b.invf[4] * y + b.invf[7] * z);
+    const float nz = rnd(b.invf[2] * x + b.invf[5] * y + b.invf[8] * z);
+    x -= nx * b.cellf[0] + ny * b.cellf[3] + nz * b.cellf[6];
+    y -= nx * b.cellf[1] + ny * b.cellf[4] + nz * b.cellf[7];
+    z -= nx * b.cellf[2] + ny * b.cellf[5] + nz * b.cellf[8];
+  }
+  return x * x + y * y + z * z < b.screen2;
+}
+
 template <int PREC, bool HOST>
 __device__ __forceinline__ bool pair_screen(const BoxDev& b, int i, const Bead& bd) {
   if (PREC == GRX_FP64) {
@@ -74,21 +91,7 @@ __device__ __forceinline__ bool pair_screen(const BoxDev& b, int i, const Bead& 
     const double rr = x * x + y * y + z * z;
     return rr < b.cut_vdw2 || (!b.no_charges && rr < b.cut_coul2);
   } else {
-    const float4 ah = (HOST ? b.hhi : b.hi)[i];
-    float x = ah.x - bd.h.x, y = ah.y - bd.h.y, z = ah.z - bd.h.z;
-    if (b.cubic) {
-      x = __fmaf_rn(-rnd(x * b.invf[0]), b.cellf[0], x);
-      y = __fmaf_rn(-rnd(y * b.invf[4]), b.cellf[4], y);
-      z = __fmaf_rn(-rnd(z * b.invf[8]), b.cellf[8], z);
-    } else {
-      const float nx = rnd(b.invf[0] * x + b.invf[3] * y + b.invf[6] * z);
-      const float ny = rnd(b.invf[1] * x + b.invf[4] * y + b.invf[7] * z);
-      const float nz = rnd(b.invf[2] * x + b.invf[5] * y + b.invf[8] * z);
-      x -= nx * b.cellf[0] + ny * b.cellf[3] + nz * b.cellf[6];
-      y -= nx * b.cellf[1] + ny * b.cellf[4] + nz * b.cellf[7];
-      z -= nx * b.cellf[2] + ny * b.cellf[5] + nz * b.cellf[8];
-    }
-    return x * x + y * y + z * z < b.screen2;
+    return screen_hi(b, (HOST ? b.hhi : b.hi)[i], bd);
   }
 }
 
@@ -219,19 +222,28 @@ __device__ __forceinline__ void warp_item(const BoxDev& b, const Bead& bd, int t
     bool pass = tl < t1;
     float sx = 0.f, sy = 0.f, sz = 0.f;  // image shift of the bead for this tile
     bool one_image = false;
+    int4 trl = make_int4(0, 0, -1, 0);   // this lane's tile range, shuffled to the warp below
+    if (pass) trl = b.tile_r[tl];
     if (pass && b.cull) {
-      const float4 tc = b.tile_c[tl];
+      const float4 tc = b.tile_c[2 * tl];
       float dx = tc.x - bx, dy = tc.y - by, dz = tc.z - bz;
       const float lim = b.cull_r + tc.w;
       const float m = tc.w + 1e-2f;
       if (b.cubic) {
+        // Bounding box of the tile at the centre's rounded image. Per axis the distance to
+        // the box bounds every atom's rounded-image distance from below: an atom whose
+        // rounding differs from the centre's lies at least half a cell minus the half
+        // extent away on that axis.
+        const float4 th = b.tile_c[2 * tl + 1];
         const float nx = rnd(dx * b.invf[0]), ny = rnd(dy * b.invf[4]), nz = rnd(dz * b.invf[8]);
         dx = __fmaf_rn(-nx, b.cellf[0], dx);
         dy = __fmaf_rn(-ny, b.cellf[4], dy);
         dz = __fmaf_rn(-nz, b.cellf[8], dz);
-        pass = dx * dx + dy * dy + dz * dz <= lim * lim;
-        one_image = b.tile_r[tl].w != 0 && fabsf(dx) + m < 0.5f * b.cellf[0] &&
-                    fabsf(dy) + m < 0.5f * b.cellf[4] && fabsf(dz) + m < 0.5f * b.cellf[8];
+        const float qx = fmaxf(fabsf(dx) - th.x, 0.f), qy = fmaxf(fabsf(dy) - th.y, 0.f),
+                    qz = fmaxf(fabsf(dz) - th.z, 0.f);
+        pass = qx * qx + qy * qy + qz * qz <= b.cull_r * b.cull_r;
+        one_image = trl.w != 0 && fabsf(dx) + th.x + 1e-2f < 0.5f * b.cellf[0] &&
+                    fabsf(dy) + th.y + 1e-2f < 0.5f * b.cellf[4] && fabsf(dz) + th.z + 1e-2f < 0.5f * b.cellf[8];
         sx = nx * b.cell_hi[0]; sy = ny * b.cell_hi[4]; sz = nz * b.cell_hi[8];
       } else {
         const float fx = b.invf[0] * dx + b.invf[3] * dy + b.invf[6] * dz;
@@ -250,7 +262,7 @@ __device__ __forceinline__ void warp_item(const BoxDev& b, const Bead& bd, int t
           const float lb = fmaxf(fmaxf(rx * b.wperp[0], ry * b.wperp[1]), rz * b.wperp[2]);
           pass = lb - 1e-3f <= lim;
         }
-        one_image = b.tile_r[tl].w != 0 && rx + m / b.wperp[0] < 0.5f - 1e-4f &&
+        one_image = trl.w != 0 && rx + m / b.wperp[0] < 0.5f - 1e-4f &&
                     ry + m / b.wperp[1] < 0.5f - 1e-4f && rz + m / b.wperp[2] < 0.5f - 1e-4f;
       }
     }
@@ -258,18 +270,16 @@ __device__ __forceinline__ void warp_item(const BoxDev& b, const Bead& bd, int t
     while (mask) {
       const int src = __ffs(mask) - 1;
       mask &= mask - 1;
-      const int t = base + src;
+      const int i = __shfl_sync(kFull, trl.x, src) + lane, tz = __shfl_sync(kFull, trl.z, src);
       const bool oi = __shfl_sync(kFull, one_image, src);
       const float tsx = __shfl_sync(kFull, sx, src), tsy = __shfl_sync(kFull, sy, src),
                   tsz = __shfl_sync(kFull, sz, src);
-      const int4 tr = b.tile_r[t];
-      const int i = tr.x + lane;
       bool in = false;
-      if (i < tr.y) {
+      if (i < __shfl_sync(kFull, trl.y, src)) {
         bool skip = false;
-        if (tr.z == component || tr.z == excl_comp) {
+        if (tz == component || tz == excl_comp) {
           const int mol = b.hmeta[i].y;
-          skip = (tr.z == excl_comp && mol == excl_mol) || (tr.z == component && mol == newmol);
+          skip = (tz == excl_comp && mol == excl_mol) || (tz == component && mol == newmol);
         }
         if (!skip) {
           if (PREC != GRX_FP64 && oi) {
@@ -406,14 +416,18 @@ __device__ __noinline__ void block_bead_pass(const BoxDev& b, const Bead* beads,
   const int items = nb * nchunk;
   const int nt = b.ntiles;
   const int ng = guest_atoms(b);
+  const int nu = nt + (ng + 31) / 32;  // work units: host tiles, then guest atoms in groups of 32
   for (;;) {
     int item = 0;
     if (lane == 0) item = atomicAdd(counter, 1);
     item = __shfl_sync(kFull, item, 0);
     if (item >= items) break;
     const int bead = item / nchunk, chunk = item - bead * nchunk;
-    const int t0 = (int)((long long)nt * chunk / nchunk), t1 = (int)((long long)nt * (chunk + 1) / nchunk);
-    const int g0 = (int)((long long)ng * chunk / nchunk), g1 = (int)((long long)ng * (chunk + 1) / nchunk);
+    // a chunk is a contiguous range of units, so only the chunks reaching past the host
+    // tiles touch guest atoms
+    const int u0 = (int)((long long)nu * chunk / nchunk), u1 = (int)((long long)nu * (chunk + 1) / nchunk);
+    const int t0 = min(u0, nt), t1 = min(u1, nt);
+    const int g0 = min(32 * max(u0 - nt, 0), ng), g1 = min(32 * max(u1 - nt, 0), ng);
     const Bead bd = beads[bead];
     LaneAcc<PREC> hacc, gacc;
     int flag = 0;
