@@ -121,10 +121,10 @@ template <int PREC>
 __device__ __noinline__ void trial_pass(const BoxDev& b, CbmcWork& W, int nb, int chain, int comp, int newmol) {
   if (threadIdx.x == 0) W.counter = 0;
   __syncthreads();
-  const int nch = chunks_for(nb, work_tiles(b), (int)(blockDim.x >> 5), b.chunk_mult);
-  block_bead_pass<PREC>(b, W.beads, nb, comp, newmol, -1, -1, W.qbuf, W.ipart, W.iflag, &W.counter, nch);
+  const PassSplit sp = pass_split(b, nb, (int)(blockDim.x >> 5), b.chunk_mult);
+  block_bead_pass<PREC>(b, W.beads, nb, comp, newmol, -1, -1, W.qbuf, W.ipart, W.iflag, &W.counter, sp);
   __syncthreads();
-  reduce_items<PREC>(W.ipart, W.iflag, nb / chain, chain, nch, W.te, W.tflag);
+  reduce_items<PREC>(W.ipart, W.iflag, nb / chain, chain, sp, W.te, W.tflag);
   __syncthreads();
 }
 

@@ -99,9 +99,10 @@ __global__ void __launch_bounds__(GRX_THREADS) noalloc_bead_pass_kernel(BoxDev b
   __shared__ int counter;
   if (threadIdx.x == 0) counter = 0;
   __syncthreads();
-  const int nch = chunks_for(1, work_tiles(b), GRX_THREADS / 32);
+  const PassSplit sp = pass_split(b, 1, GRX_THREADS / 32, 4);
+  const int nch = (int)sp.items;  // one bead: slot = item
   block_bead_pass<PREC>(b, beads + blockIdx.x, 1, component, newmol, excl_comp, excl_mol, qbuf, ipart, iflag,
-                        &counter, nch);
+                        &counter, sp);
   __syncthreads();
   if (threadIdx.x < 4) {
     double s = 0.0;

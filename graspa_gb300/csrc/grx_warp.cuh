@@ -394,47 +394,76 @@ __device__ __forceinline__ int guest_atoms(const BoxDev& b) {
 }
 __device__ __forceinline__ int work_tiles(const BoxDev& b) { return b.ntiles + (guest_atoms(b) + 31) / 32; }
 
-// Chunks per bead so that a pass has at least ~4 items per warp.
-__host__ __device__ __forceinline__ int chunks_for(int nb, int ntiles, int nwarps, int mult = 4) {
-  int c = (mult * nwarps + nb - 1) / nb;
-  if (c > ntiles) c = ntiles;
-  if (c < 1) c = 1;
-  return c;
+// Work split of one bead pass. The flattened space of nb beads x nu work units (host
+// tiles, then guest atoms in groups of 32) is cut into `items` contiguous ranges of equal
+// size, so every warp gets the same share whatever nb is. An item that crosses a bead
+// boundary stores one partial per bead it touches, in slot item + bead; these slots are
+// distinct (a later item cannot reach an earlier bead), so a pass uses at most
+// items + nb - 1 slots.
+struct PassSplit {
+  unsigned nu, items, q, r;  // units per bead, items, and T = items * q + r with T = nb * nu
+  __device__ __forceinline__ void range(unsigned item, unsigned& lo, unsigned& hi) const {
+    lo = item * q + min(item, r);
+    hi = lo + q + (item < r ? 1u : 0u);
+  }
+  __device__ __forceinline__ unsigned item_of(unsigned p) const {  // the item holding unit p
+    const unsigned big = r * (q + 1);
+    return p < big ? p / (q + 1) : r + (p - big) / q;
+  }
+};
+
+// Items of a pass: mult per warp, never more than the units of the pass (at least 1).
+__device__ __forceinline__ PassSplit pass_split(const BoxDev& b, int nb, int nwarps, int mult) {
+  PassSplit s;
+  s.nu = (unsigned)work_tiles(b);
+  const unsigned T = (unsigned)nb * s.nu;
+  s.items = max(1u, min((unsigned)(mult * nwarps), T));
+  s.q = T / s.items;
+  s.r = T - s.q * s.items;
+  return s;
 }
 
 constexpr int kMaxItems = 320;
 
 // One pass of `nb` beads (shared memory) over every atom by a whole block. Items are
-// taken dynamically by warps; per-item partials land in ipart[item*4 + q] and
-// iflag[item] (item = bead * nchunk + chunk). Caller syncs before reading them.
+// taken dynamically by warps; the partial of bead `bead` within item `item` lands in
+// ipart[(item + bead)*4 + q] and iflag[item + bead]. Caller syncs before reading them.
 template <int PREC>
 __device__ __noinline__ void block_bead_pass(const BoxDev& b, const Bead* beads, int nb, int component,
                                                 int newmol, int excl_comp, int excl_mol, int* qbuf,
-                                                double* ipart, int* iflag, int* counter, int nchunk) {
+                                                double* ipart, int* iflag, int* counter, PassSplit sp) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int* q = qbuf + warp * kQueue;
-  const int items = nb * nchunk;
   const int nt = b.ntiles;
   const int ng = guest_atoms(b);
-  const int nu = nt + (ng + 31) / 32;  // work units: host tiles, then guest atoms in groups of 32
+  if (sp.nu == 0) {  // nothing to interact with: zero partials, one item per bead slot
+    for (int k = threadIdx.x; k < nb * 4; k += blockDim.x) ipart[k] = 0.0;
+    for (int k = threadIdx.x; k < nb; k += blockDim.x) iflag[k] = 0;
+    return;
+  }
   for (;;) {
     int item = 0;
     if (lane == 0) item = atomicAdd(counter, 1);
     item = __shfl_sync(kFull, item, 0);
-    if (item >= items) break;
-    const int bead = item / nchunk, chunk = item - bead * nchunk;
-    // a chunk is a contiguous range of units, so only the chunks reaching past the host
-    // tiles touch guest atoms
-    const int u0 = (int)((long long)nu * chunk / nchunk), u1 = (int)((long long)nu * (chunk + 1) / nchunk);
-    const int t0 = min(u0, nt), t1 = min(u1, nt);
-    const int g0 = min(32 * max(u0 - nt, 0), ng), g1 = min(32 * max(u1 - nt, 0), ng);
-    const Bead bd = beads[bead];
-    LaneAcc<PREC> hacc, gacc;
-    int flag = 0;
-    warp_item<PREC>(b, bd, t0, t1, g0, g1, component, newmol, excl_comp, excl_mol, q, hacc, gacc, flag);
-    const unsigned fm = __ballot_sync(kFull, flag != 0);
-    warp_store<PREC>(hacc, gacc, ipart + item * 4, df{bd.pq.x, bd.pq.y}, g1 > g0);
-    if (lane == 0) iflag[item] = fm ? 1 : 0;
+    if (item >= (int)sp.items) break;
+    unsigned lo, hi;
+    sp.range((unsigned)item, lo, hi);
+    while (lo < hi) {
+      const int bead = (int)(lo / sp.nu);
+      const int u0 = (int)(lo - (unsigned)bead * sp.nu);
+      const int u1 = (int)min(sp.nu, (unsigned)u0 + (hi - lo));
+      // only the ranges reaching past the host tiles touch guest atoms
+      const int t0 = min(u0, nt), t1 = min(u1, nt);
+      const int g0 = min(32 * max(u0 - nt, 0), ng), g1 = min(32 * max(u1 - nt, 0), ng);
+      const Bead bd = beads[bead];
+      LaneAcc<PREC> hacc, gacc;
+      int flag = 0;
+      warp_item<PREC>(b, bd, t0, t1, g0, g1, component, newmol, excl_comp, excl_mol, q, hacc, gacc, flag);
+      const unsigned fm = __ballot_sync(kFull, flag != 0);
+      warp_store<PREC>(hacc, gacc, ipart + (item + bead) * 4, df{bd.pq.x, bd.pq.y}, g1 > g0);
+      if (lane == 0) iflag[item + bead] = fm ? 1 : 0;
+      lo += (unsigned)(u1 - u0);
+    }
   }
 }
 
@@ -449,31 +478,43 @@ __device__ __forceinline__ double item_get(const double* ipart, int idx) {
   }
 }
 
-// Per-trial sums of one pass: trial t = beads [t*chain, (t+1)*chain), chunks in order.
+// Slots of bead `bead`: [first, last] (slot = item + bead), in unit order.
+__device__ __forceinline__ void bead_slots(const PassSplit& sp, int bead, int& first, int& last) {
+  if (sp.nu == 0) { first = last = bead; return; }
+  const unsigned p0 = (unsigned)bead * sp.nu;
+  first = (int)sp.item_of(p0) + bead;
+  last = (int)sp.item_of(p0 + sp.nu - 1) + bead;
+}
+
+// Per-trial sums of one pass: trial t = beads [t*chain, (t+1)*chain), partials in order.
 template <int PREC>
 __device__ __forceinline__ void reduce_items(const double* ipart, const int* iflag, int ntr, int chain,
-                                             int nchunk, double* te, int* tflag) {
+                                             const PassSplit& sp, double* te, int* tflag) {
   for (int w = threadIdx.x; w < ntr * 4; w += blockDim.x) {
     const int t = w >> 2, k = w & 3;
     int f = 0;
     if constexpr (PREC == GRX_MIXED) {
       df s = {0.f, 0.f};
-      for (int a = 0; a < chain; ++a)
-        for (int c = 0; c < nchunk; ++c) {
-          const int item = (t * chain + a) * nchunk + c;
-          const float2 v = reinterpret_cast<const float2*>(ipart)[item * 4 + k];
+      for (int a = 0; a < chain; ++a) {
+        int s0, s1;
+        bead_slots(sp, t * chain + a, s0, s1);
+        for (int c = s0; c <= s1; ++c) {
+          const float2 v = reinterpret_cast<const float2*>(ipart)[c * 4 + k];
           s = df_add(s, df{v.x, v.y});
-          f |= iflag[item];
+          f |= iflag[c];
         }
+      }
       te[4 * t + k] = df_to(s);
     } else {
       double s = 0.0;
-      for (int a = 0; a < chain; ++a)
-        for (int c = 0; c < nchunk; ++c) {
-          const int item = (t * chain + a) * nchunk + c;
-          s += ipart[item * 4 + k];
-          f |= iflag[item];
+      for (int a = 0; a < chain; ++a) {
+        int s0, s1;
+        bead_slots(sp, t * chain + a, s0, s1);
+        for (int c = s0; c <= s1; ++c) {
+          s += ipart[c * 4 + k];
+          f |= iflag[c];
         }
+      }
       te[4 * t + k] = s;
     }
     if (k == 0) tflag[t] = f;

@@ -19,6 +19,7 @@
 namespace grx {
 
 constexpr int kMaxTrials = 64;
+constexpr int kWidomItemsPerWarp = 1;  // work split of a bead pass (items per warp)
 
 struct WidomArgs {
   int comp;
@@ -214,10 +215,10 @@ __global__ void __launch_bounds__(GRX_THREADS, 3) widom_kernel(BoxDev b, WidomAr
     __syncthreads();
     // 2. pair energies of the first-bead trials
     {
-      const int nch = chunks_for(nt, work_tiles(b), GRX_THREADS / 32);
-      block_bead_pass<PREC>(b, beads, nt, a.comp, a.newmol, -1, -1, qbuf, ipart, iflag, &counter, nch);
+      const PassSplit sp = pass_split(b, nt, GRX_THREADS / 32, kWidomItemsPerWarp);
+      block_bead_pass<PREC>(b, beads, nt, a.comp, a.newmol, -1, -1, qbuf, ipart, iflag, &counter, sp);
       __syncthreads();
-      reduce_items<PREC>(ipart, iflag, nt, 1, nch, te, tflag);
+      reduce_items<PREC>(ipart, iflag, nt, 1, sp, te, tflag);
       __syncthreads();
     }
     // 3. select the first bead
@@ -255,10 +256,10 @@ __global__ void __launch_bounds__(GRX_THREADS, 3) widom_kernel(BoxDev b, WidomAr
       if (tid == 0) counter = 0;
       __syncthreads();
       // 5. pair energies of the orientations
-      const int nch = chunks_for(nb, work_tiles(b), GRX_THREADS / 32);
-      block_bead_pass<PREC>(b, beads, nb, a.comp, a.newmol, -1, -1, qbuf, ipart, iflag, &counter, nch);
+      const PassSplit sp = pass_split(b, nb, GRX_THREADS / 32, kWidomItemsPerWarp);
+      block_bead_pass<PREC>(b, beads, nb, a.comp, a.newmol, -1, -1, qbuf, ipart, iflag, &counter, sp);
       __syncthreads();
-      reduce_items<PREC>(ipart, iflag, no, chain, nch, te, tflag);
+      reduce_items<PREC>(ipart, iflag, no, chain, sp, te, tflag);
       __syncthreads();
       if (tid < 32) {
         int sel = -1, nok = 0;
