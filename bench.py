@@ -203,8 +203,8 @@ def bench_gcmc(args, grx, torch, stream, flush, rank, world, dist):
     for b in boxes[:n_drift]:
         b.ewald_total()
     batch = grx.GcmcBatch(boxes, descs, grx.GRX_MIXED)
-    chunk, cand = batch.autotune(10)   # real steps; picks the bead-pass work split for this batch
-    out["autotune"] = {"chunk_mult": chunk, "ms_per_candidate": cand}
+    shape, cand = batch.autotune(S)   # real steps at the timed launch length; picks the launch shape
+    out["autotune"] = {"warps_per_box": shape[0], "chunk_mult": shape[1], "ms_per_candidate": cand}
     l0 = grx.launch_count()
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     clocks.start()
@@ -517,7 +517,7 @@ def bench_other(args, grx, torch, stream, flush, which):
             boxes.append(b)
         prec = grx.GRX_MIXED
         batch = grx.GcmcBatch(boxes, descs, prec)
-        chosen, cand_ms = batch.autotune(20)
+        chosen, cand_ms = batch.autotune(args.mc_steps)
         times, stats = timed_graph(torch, batch, stream, args.mc_steps, args.steps, args.warmup, flush)
         batch.close()
         te = 0.0
@@ -537,7 +537,8 @@ def bench_other(args, grx, torch, stream, flush, which):
         return {"metric": "CBMC trial energies/s", "value": te / t, "unit": "trial_energies/s", "n_gpus": 1,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * t / args.steps,
                 "workload": "batched_ch4_xe_64_triclinic (mixture GCMC, 8-32 trials, LJ only)",
-                "mc_steps_per_step": args.mc_steps, "autotune": {"chunk_mult": chosen, "ms_per_candidate": cand_ms},
+                "mc_steps_per_step": args.mc_steps,
+                "autotune": {"warps_per_box": chosen[0], "chunk_mult": chosen[1], "ms_per_candidate": cand_ms},
                 "roofline": {"bound": "fp32", "achieved": achieved, "peak": PEAK_FP32_NOMINAL, "unit": "TFLOP/s",
                              "frac": achieved / PEAK_FP32_NOMINAL, "model": "40 FLOP/pair (LJ only)"},
                 "framework_atoms": [int(s["comp_start"][1]) for s in systems[:8]]}
@@ -553,6 +554,11 @@ def bench_other(args, grx, torch, stream, flush, which):
         for b in boxes[:4]:
             b.ewald_total()
         batch = grx.GcmcBatch(boxes, descs, p)
+        if name == "mixed":
+            shape, _ = batch.autotune(args.mc_steps)
+            out["autotune"] = {"warps_per_box": shape[0], "chunk_mult": shape[1]}
+        else:
+            batch.set_shape(*shape)
         steps = args.steps if name == "mixed" else max(1, min(args.steps, 3))
         times, stats = timed_graph(torch, batch, stream, args.mc_steps, steps, args.warmup, flush)
         warm = timed_graph.warm_stats
@@ -567,7 +573,8 @@ def bench_other(args, grx, torch, stream, flush, which):
         close_boxes(boxes)
     return {"metric": "CBMC trial energies/s", "value": out["mixed"]["value"], "unit": "trial_energies/s",
             "n_gpus": 1, "workload": "gcmc_tip4p_ew_hexagonal_864 (alpha 0.30, kmax 10/10/8, cutoff 11 A)",
-            "chains": R, "mc_steps_per_step": args.mc_steps, "mixed": out["mixed"], "fp64": out["fp64"],
+            "chains": R, "mc_steps_per_step": args.mc_steps, "autotune": out["autotune"],
+            "mixed": out["mixed"], "fp64": out["fp64"],
             "speedup_mixed_over_fp64": out["mixed"]["value"] / out["fp64"]["value"]}
 
 

@@ -506,7 +506,7 @@ static grx_status box_create(const grx_box_desc* desc, grx_arena* arena, grx_box
   // least w_min - |e| away); otherwise max_k |s_k| w_k (s = fractional remainder,
   // w_k = distance between lattice planes) bounds it from below.
   d.cull = 1;
-  d.chunk_mult = 4;
+  d.chunk_mult = 1;
   d.cull_r = (float)(std::sqrt((double)d.screen2) + 0.01);
   {
     const double* C = g.cell;

@@ -1,8 +1,8 @@
 // grx_cbmc.cuh -- block-level CBMC stages shared by the Widom and GCMC kernels.
 //
-// Every function here is called by all threads of a block (kCbmcThreads) with the
-// same arguments; each ends with the block synchronised and its results in the
-// shared-memory workspace CbmcWork. The stages restate gRASPA's CBMC move pieces:
+// Every function here is called by all threads of a block (NW warps) with the same
+// arguments; each ends with the block synchronised and its results in the
+// shared-memory workspace CbmcWork<NW>. The stages restate gRASPA's CBMC move pieces:
 //   gen_first_trials  get_random_trial_position      mc_widom.h:122-213
 //   gen_orientations  get_random_trial_orientation   mc_widom.h:215-303
 //   trial_pass        Calculate_Multiple_Trial_Energy_VDWReal + host sums
@@ -19,16 +19,18 @@ namespace grx {
 
 constexpr int kMaxTrials = 64;
 constexpr int kMolWork = 32;      // atoms of one molecule held in shared memory
-constexpr int kCbmcThreads = 256; // threads of a block running the CBMC stages (8 warps)
 constexpr int kCbmcBeads = 128;   // trial beads of one pass
-// work items of one pass: nb * chunks <= mult * warps + nb with mult <= 8
-constexpr int kCbmcItems = kCbmcBeads + 8 * (kCbmcThreads / 32);
+constexpr int kCbmcMaxMult = 8;   // items per warp of a bead pass, at most
 
+// Workspace of a block of NW warps. A pass uses at most items + beads - 1 partial
+// slots, items = mult * NW.
+template <int NW>
 struct CbmcWork {
+  static constexpr int kItems = kCbmcBeads + kCbmcMaxMult * NW;
   Bead beads[kCbmcBeads];
-  double ipart[kCbmcItems * 4];
-  int iflag[kCbmcItems];
-  int qbuf[(kCbmcThreads / 32) * kQueue];
+  double ipart[kItems * 4];
+  int iflag[kItems];
+  int qbuf[NW * kQueue];
   double te[kMaxTrials * 4];
   int tflag[kMaxTrials];
   double sel_ws[kMaxTrials], sel_wa[kMaxTrials];
@@ -36,7 +38,7 @@ struct CbmcWork {
   // [n_old, n_old + n_new) arrive
   double mx[2 * kMolWork], my[2 * kMolWork], mz[2 * kMolWork], mq[2 * kMolWork];
   double sbuf[32];
-  double wsum[2][kCbmcThreads / 32];
+  double wsum[2][NW];
   float2 qd[2 * kMolWork];
   int counter;
   int ok;       // step constructed
@@ -49,7 +51,8 @@ struct CbmcWork {
 // ---------------------------------------------------------------- trials
 // First-bead trial positions: Cell diagonal x Philox uniforms (mc_widom.h:133-139);
 // with `retrace`, trial 0 is the existing bead (deletion, mc_widom.h:141-156).
-__device__ __noinline__ void gen_first_trials(const BoxDev& b, CbmcWork& W, uint64_t seed, uint32_t stream,
+template <class WK>
+__device__ __noinline__ void gen_first_trials(const BoxDev& b, WK& W, uint64_t seed, uint32_t stream,
                                                  uint64_t move, int nt, double q, double scale, int type,
                                                  bool retrace, double ox, double oy, double oz) {
   for (int t = threadIdx.x; t < nt; t += blockDim.x) {
@@ -91,7 +94,8 @@ __device__ __forceinline__ void rotate_quaternion(double& x, double& y, double& 
 // Trial orientations about the chosen first bead (fx, fy, fz): the vectors from the
 // component's slot-0 atom to its chain atoms, rotated by Philox quaternions. With
 // `retrace`, orientation 0 is the existing chain (ox/oy/oz arrays, chain atoms).
-__device__ __noinline__ void gen_orientations(const BoxDev& b, CbmcWork& W, uint64_t seed, uint32_t stream,
+template <class WK>
+__device__ __noinline__ void gen_orientations(const BoxDev& b, WK& W, uint64_t seed, uint32_t stream,
                                                  uint64_t move, int no, int chain, int off, double scale_coul,
                                                  double scale, double fx, double fy, double fz, bool retrace,
                                                  const double* ox, const double* oy, const double* oz,
@@ -117,8 +121,8 @@ __device__ __noinline__ void gen_orientations(const BoxDev& b, CbmcWork& W, uint
 
 // Energies of ntr = nb / chain trials of `chain` beads each (W.beads) against every
 // atom, with the atoms of (comp, newmol) excluded: W.te[4 t + k], W.tflag[t].
-template <int PREC>
-__device__ __noinline__ void trial_pass(const BoxDev& b, CbmcWork& W, int nb, int chain, int comp, int newmol) {
+template <int PREC, class WK>
+__device__ __noinline__ void trial_pass(const BoxDev& b, WK& W, int nb, int chain, int comp, int newmol) {
   if (threadIdx.x == 0) W.counter = 0;
   __syncthreads();
   const PassSplit sp = pass_split(b, nb, (int)(blockDim.x >> 5), b.chunk_mult);
@@ -134,7 +138,8 @@ __device__ __noinline__ void trial_pass(const BoxDev& b, CbmcWork& W, int nb, in
 // existing configuration and no selection is drawn. `stored` is added to the sum
 // before averaging (the reinsertion retrace's StoredR, mc_widom.h:363-366). Exponentials are evaluated one
 // trial per lane; sums and the cumulative search stay sequential in trial order.
-__device__ __noinline__ void step_weight(CbmcWork& W, int nt, double beta, int bias, double u, double navg,
+template <class WK>
+__device__ __noinline__ void step_weight(WK& W, int nt, double beta, int bias, double u, double navg,
                                             bool retrace, double stored = 0.0) {
   if (threadIdx.x < 32) {
     const int lane = threadIdx.x;
@@ -213,8 +218,8 @@ __device__ __noinline__ void step_weight(CbmcWork& W, int nt, double beta, int b
 // the reference arithmetic; the other forms evaluate dS and both sums in
 // double-float on the FP32 pipe against temp*S tables (ewA, ewF). When s_out is
 // given, S_same + dS is staged there (FP64) for a later commit. Results on thread 0.
-template <int PREC>
-__device__ __noinline__ void ewald_move(const BoxDev& b, CbmcWork& W, int na, double2* eik, double2* s_out,
+template <int PREC, class WK>
+__device__ __noinline__ void ewald_move(const BoxDev& b, WK& W, int na, double2* eik, double2* s_out,
                                            double& same, double& cross) {
   const int tid = threadIdx.x;
   const int kx1 = b.kmax[0] + 1, ky1 = b.kmax[1] + 1;

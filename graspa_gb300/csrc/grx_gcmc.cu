@@ -78,18 +78,19 @@ __device__ __forceinline__ void copy_atom(const BoxDev& b, int dst, int src, int
   const_cast<float2*>(b.qdf)[dst] = b.qdf[src];
 }
 
-template <int PREC>
-// One block per box. The box's moved components are entries [first[box],
-// first[box + 1]) of args / stats; every step picks one of them uniformly with word 3
-// of the displacement slot (Select_Box_Component_Molecule, axpy.cu:74-100). All
-// entries of a box share its seed and stream.
-__global__ void __launch_bounds__(kCbmcThreads, 3) gcmc_kernel(const BoxDev* boxes, const GcmcArgs* args,
+// One block of NW warps per box (NW = 8, 12 or 24: 24 warps per SM in every shape).
+// The box's moved components are entries [first[box], first[box + 1]) of args /
+// stats; every step picks one of them uniformly with word 3 of the displacement slot
+// (Select_Box_Component_Molecule, axpy.cu:74-100). All entries of a box share its seed
+// and stream.
+template <int PREC, int NW>
+__global__ void __launch_bounds__(NW * 32, 24 / NW) gcmc_kernel(const BoxDev* boxes, const GcmcArgs* args,
                                                               const int* first, const uint64_t* step0,
                                                               int64_t nsteps, grx_gcmc_stats* stats) {
   const uint64_t first_step = *step0;
   __shared__ BoxDev b;
   __shared__ GcmcArgs A[kMaxMoved];
-  __shared__ CbmcWork W;
+  __shared__ CbmcWork<NW> W;
   __shared__ grx_gcmc_stats ST[kMaxMoved];
   __shared__ int s_accept;
   __shared__ double s_e1[4], s_w1, s_dE[3], s_stored, s_r1[4], s_wr;
@@ -433,7 +434,8 @@ struct grx_gcmc_batch {
   std::vector<int> first;
   int nentries = 0;
   size_t smem = 0;
-  int chunk_mult = 4;
+  int chunk_mult = 1;
+  int nwarps = 8;  // warps per box (block size / 32): 8, 12 or 24
   void* mem = nullptr;
   grx_arena* arena = nullptr;
   BoxDev* d_boxes = nullptr;
@@ -515,26 +517,55 @@ static grx_status prepare_gcmc(grx_box* const* boxes, int32_t nboxes, const grx_
   return GRX_OK;
 }
 
-static grx_status set_gcmc_smem() {
-  GRX_CHECK_CUDA(cudaFuncSetAttribute(gcmc_kernel<GRX_FP64>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024),
-                 "gcmc shared memory attribute");
-  GRX_CHECK_CUDA(cudaFuncSetAttribute(gcmc_kernel<GRX_MIXED>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024),
-                 "gcmc shared memory attribute");
-  GRX_CHECK_CUDA(cudaFuncSetAttribute(gcmc_kernel<GRX_FP32>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024),
+template <int PREC, int NW>
+static grx_status set_smem_one() {
+  GRX_CHECK_CUDA(cudaFuncSetAttribute(gcmc_kernel<PREC, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024),
                  "gcmc shared memory attribute");
   return GRX_OK;
 }
 
-// Enqueues one persistent launch and the step-counter advance (no host sync).
-static grx_status enqueue_gcmc(grx_precision prec, int nboxes, const BoxDev* dboxes, const GcmcArgs* dargs,
+static grx_status set_gcmc_smem() {
+  grx_status st = GRX_OK;
+  for (grx_status r : {set_smem_one<GRX_FP64, 8>(), set_smem_one<GRX_FP64, 12>(), set_smem_one<GRX_FP64, 24>(),
+                       set_smem_one<GRX_MIXED, 8>(), set_smem_one<GRX_MIXED, 12>(), set_smem_one<GRX_MIXED, 24>(),
+                       set_smem_one<GRX_FP32, 8>(), set_smem_one<GRX_FP32, 12>(), set_smem_one<GRX_FP32, 24>()})
+    if (r && !st) st = r;
+  return st;
+}
+
+// Warps per box when no shape was chosen: fill the SMs with one wave of blocks.
+static int default_warps(int nboxes) {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                  cudaSuccess)
+      sms = 1;
+  }
+  if (nboxes <= sms) return 24;
+  if (nboxes <= 2 * sms) return 12;
+  return 8;
+}
+
+template <int NW>
+static void launch_shape(grx_precision prec, int nboxes, const BoxDev* dboxes, const GcmcArgs* dargs,
+                         const int* dfirst, uint64_t* dstep, int64_t nsteps, grx_gcmc_stats* dstats, size_t smem,
+                         cudaStream_t stream) {
+  if (prec == GRX_FP64)
+    gcmc_kernel<GRX_FP64, NW><<<nboxes, NW * 32, smem, stream>>>(dboxes, dargs, dfirst, dstep, nsteps, dstats);
+  else if (prec == GRX_MIXED)
+    gcmc_kernel<GRX_MIXED, NW><<<nboxes, NW * 32, smem, stream>>>(dboxes, dargs, dfirst, dstep, nsteps, dstats);
+  else
+    gcmc_kernel<GRX_FP32, NW><<<nboxes, NW * 32, smem, stream>>>(dboxes, dargs, dfirst, dstep, nsteps, dstats);
+}
+
+// Enqueues one persistent launch of nw warps per box and the step-counter advance (no host sync).
+static grx_status enqueue_gcmc(grx_precision prec, int nw, int nboxes, const BoxDev* dboxes, const GcmcArgs* dargs,
                                const int* dfirst, uint64_t* dstep, int64_t nsteps, grx_gcmc_stats* dstats,
                                size_t smem, cudaStream_t stream) {
-  if (prec == GRX_FP64)
-    gcmc_kernel<GRX_FP64><<<nboxes, kCbmcThreads, smem, stream>>>(dboxes, dargs, dfirst, dstep, nsteps, dstats);
-  else if (prec == GRX_MIXED)
-    gcmc_kernel<GRX_MIXED><<<nboxes, kCbmcThreads, smem, stream>>>(dboxes, dargs, dfirst, dstep, nsteps, dstats);
-  else
-    gcmc_kernel<GRX_FP32><<<nboxes, kCbmcThreads, smem, stream>>>(dboxes, dargs, dfirst, dstep, nsteps, dstats);
+  if (nw == 24) launch_shape<24>(prec, nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem, stream);
+  else if (nw == 12) launch_shape<12>(prec, nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem, stream);
+  else launch_shape<8>(prec, nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem, stream);
   advance_step_kernel<<<1, 1, 0, stream>>>(dstep, nsteps);
   count_launch();
   count_launch();
@@ -595,7 +626,8 @@ extern "C" grx_status grx_gcmc_run(grx_box* const* boxes, int32_t nboxes, const 
   if (nsteps > 0) {
     st = set_gcmc_smem();
     if (st) return st;
-    st = enqueue_gcmc(prec, nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem, b0->stream);
+    st = enqueue_gcmc(prec, default_warps(nboxes), nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem,
+                      b0->stream);
     if (st) return st;
   }
   GRX_CHECK_CUDA(cudaMemcpyAsync(stats, dstats, ne * sizeof(grx_gcmc_stats), cudaMemcpyDefault, b0->stream),
@@ -623,6 +655,7 @@ extern "C" grx_status grx_gcmc_batch_create(grx_box* const* boxes, int32_t nboxe
   grx_status st = prepare_gcmc(boxes, nboxes, descs, ncomp_moved, hb, ha, B->first, B->smem, B->chunk_mult);
   if (st) { delete B; return st; }
   B->nentries = B->first[nboxes];
+  B->nwarps = default_warps(nboxes);
   B->boxes.assign(boxes, boxes + nboxes);
   B->descs.assign(descs, descs + B->nentries);
   B->device = boxes[0]->device;
@@ -697,7 +730,7 @@ extern "C" grx_status grx_gcmc_batch_launch(grx_gcmc_batch* B, int64_t nsteps, v
   cudaStream_t s = stream ? (cudaStream_t)stream : B->stream;
   if (nsteps == 0) return GRX_OK;
   B->last_stream = s;
-  return enqueue_gcmc(B->prec, (int)B->boxes.size(), B->d_boxes, B->d_args, B->d_first, B->d_step, nsteps,
+  return enqueue_gcmc(B->prec, B->nwarps, (int)B->boxes.size(), B->d_boxes, B->d_args, B->d_first, B->d_step, nsteps,
                       B->d_stats, B->smem, s);
 }
 
@@ -712,7 +745,7 @@ extern "C" grx_status grx_gcmc_batch_run_graph(grx_gcmc_batch* B, int64_t nsteps
     grx_status st = GRX_OK;
     const uint64_t before = grx_launch_count();
     for (int k = 0; k < nlaunch && st == GRX_OK; ++k)
-      st = enqueue_gcmc(B->prec, (int)B->boxes.size(), B->d_boxes, B->d_args, B->d_first, B->d_step, nsteps,
+      st = enqueue_gcmc(B->prec, B->nwarps, (int)B->boxes.size(), B->d_boxes, B->d_args, B->d_first, B->d_step, nsteps,
                         B->d_stats, B->smem, cap);
     count_launch(0 - (grx_launch_count() - before));  // capture records the kernels, it launches nothing
     cudaGraph_t g = nullptr;
@@ -754,47 +787,109 @@ extern "C" grx_status grx_gcmc_batch_reset_stats(grx_gcmc_batch* B) {
   return GRX_OK;
 }
 
-// Autotuner: times nsteps real steps of every box for each candidate work split
-// (items per warp per bead pass) with CUDA events and keeps the fastest. The probe
-// steps are ordinary Monte Carlo steps: the chains advance by ncand * nsteps.
+static grx_status upload_mult(grx_gcmc_batch* B, int mult) {
+  const int nb = (int)B->boxes.size();
+  std::vector<BoxDev> hb(nb);
+  for (int i = 0; i < nb; ++i) {
+    B->boxes[i]->dev.chunk_mult = mult;
+    hb[i] = B->boxes[i]->dev;
+  }
+  GRX_CHECK_CUDA(cudaMemcpy(B->d_boxes, hb.data(), nb * sizeof(BoxDev), cudaMemcpyHostToDevice), "shape upload");
+  return GRX_OK;
+}
+
+extern "C" grx_status grx_gcmc_batch_set_shape(grx_gcmc_batch* B, int32_t nwarps, int32_t chunk_mult) {
+  GRX_REQUIRE(B, "grx_gcmc_batch_set_shape: null batch");
+  GRX_REQUIRE(nwarps == 8 || nwarps == 12 || nwarps == 24, "grx_gcmc_batch_set_shape: nwarps must be 8, 12 or 24");
+  GRX_REQUIRE(chunk_mult >= 1 && chunk_mult <= kCbmcMaxMult, "grx_gcmc_batch_set_shape: chunk_mult must be 1..8");
+  GRX_CHECK_CUDA(cudaStreamSynchronize(B->stream), "set shape");
+  grx_status st = upload_mult(B, chunk_mult);
+  if (st) return st;
+  B->nwarps = nwarps;
+  B->chunk_mult = chunk_mult;
+  drop_graph(B);
+  return GRX_OK;
+}
+
+extern "C" grx_status grx_gcmc_batch_get_shape(grx_gcmc_batch* B, int32_t* nwarps, int32_t* chunk_mult) {
+  GRX_REQUIRE(B, "grx_gcmc_batch_get_shape: null batch");
+  if (nwarps) *nwarps = B->nwarps;
+  if (chunk_mult) *chunk_mult = B->chunk_mult;
+  return GRX_OK;
+}
+
+// Trial energies behind a set of statistics (one trial configuration against every
+// atom: 2 per translation / rotation, trials + orientations per CBMC insertion or
+// deletion, the same plus the retrace per reinsertion).
+static double trial_energies(const grx_gcmc_batch* B, const std::vector<grx_gcmc_stats>& st) {
+  double te = 0.0;
+  for (size_t i = 0; i < B->boxes.size(); ++i)
+    for (int e = B->first[i]; e < B->first[i + 1]; ++e) {
+      const grx_gcmc_desc& d = B->descs[e];
+      const bool chain = B->boxes[i]->molsize[d.component] > 1;
+      const double grow = d.ntrials + (chain ? d.norient : 0);
+      const int64_t* a = st[e].attempts;
+      te += 2.0 * (a[0] + a[1]) + grow * (a[2] + a[3]) + (grow + 1 + (chain ? d.norient : 0)) * a[4];
+    }
+  return te;
+}
+
+// Autotuner: runs nsteps real steps of every box for each candidate launch shape
+// (warps per box 8 / 12 / 24, times items per warp of a bead pass 1 / 2 / 4), timed
+// with CUDA events, and keeps the shape with the most trial energies per second. The
+// chains change while they are probed (boxes fill up from empty), so each candidate
+// is timed twice, in a forward and a reverse sweep, and ranked by work per time.
+// ms_per_candidate reports the mean time of one probe. The probe steps are ordinary
+// Monte Carlo steps: the chains advance by 2 * GRX_GCMC_TUNE_CANDIDATES * nsteps.
 extern "C" grx_status grx_gcmc_batch_autotune(grx_gcmc_batch* B, int64_t nsteps, int32_t* chosen,
                                               float* ms_per_candidate) {
   GRX_REQUIRE(B && nsteps >= 1, "grx_gcmc_batch_autotune: bad argument");
-  static const int cand[4] = {1, 2, 4, 8};
+  static const int warps[3] = {8, 12, 24}, mults[3] = {1, 2, 4};
+  static_assert(GRX_GCMC_TUNE_CANDIDATES == 9, "candidate table");
   const int nb = (int)B->boxes.size();
-  std::vector<BoxDev> hb(nb);
   cudaEvent_t e0, e1;
   GRX_CHECK_CUDA(cudaEventCreate(&e0), "event");
   GRX_CHECK_CUDA(cudaEventCreate(&e1), "event");
-  float best = 1e30f;
-  int best_m = B->chunk_mult;
-  for (int c = 0; c < 4; ++c) {
-    for (int i = 0; i < nb; ++i) {
-      hb[i] = B->boxes[i]->dev;
-      hb[i].chunk_mult = cand[c];
-    }
-    GRX_CHECK_CUDA(cudaMemcpy(B->d_boxes, hb.data(), nb * sizeof(BoxDev), cudaMemcpyHostToDevice), "tune upload");
+  double ms_sum[GRX_GCMC_TUNE_CANDIDATES] = {}, te_sum[GRX_GCMC_TUNE_CANDIDATES] = {};
+  std::vector<grx_gcmc_stats> before(B->nentries), after(B->nentries);
+  auto read = [&](std::vector<grx_gcmc_stats>& v) {
+    return cudaMemcpy(v.data(), B->d_stats, B->nentries * sizeof(grx_gcmc_stats), cudaMemcpyDeviceToHost);
+  };
+  GRX_CHECK_CUDA(cudaStreamSynchronize(B->stream), "tune sync");
+  for (int k = 0; k < 2 * GRX_GCMC_TUNE_CANDIDATES; ++k) {
+    const int c = k < GRX_GCMC_TUNE_CANDIDATES ? k : 2 * GRX_GCMC_TUNE_CANDIDATES - 1 - k;
+    const int nw = warps[c / 3], mult = mults[c % 3];
+    grx_status st = upload_mult(B, mult);
+    if (st) return st;
+    GRX_CHECK_CUDA(read(before), "tune stats");
     GRX_CHECK_CUDA(cudaEventRecord(e0, B->stream), "event");
-    grx_status st = enqueue_gcmc(B->prec, nb, B->d_boxes, B->d_args, B->d_first, B->d_step, nsteps, B->d_stats,
-                                 B->smem, B->stream);
+    st = enqueue_gcmc(B->prec, nw, nb, B->d_boxes, B->d_args, B->d_first, B->d_step, nsteps, B->d_stats, B->smem,
+                      B->stream);
     if (st) return st;
     GRX_CHECK_CUDA(cudaEventRecord(e1, B->stream), "event");
     GRX_CHECK_CUDA(cudaEventSynchronize(e1), "event");
     float ms = 0.f;
     GRX_CHECK_CUDA(cudaEventElapsedTime(&ms, e0, e1), "event");
-    if (ms_per_candidate) ms_per_candidate[c] = ms;
-    if (ms < best) { best = ms; best_m = cand[c]; }
+    GRX_CHECK_CUDA(read(after), "tune stats");
+    ms_sum[c] += ms;
+    te_sum[c] += trial_energies(B, after) - trial_energies(B, before);
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  B->chunk_mult = best_m;
-  for (int i = 0; i < nb; ++i) {
-    B->boxes[i]->dev.chunk_mult = best_m;
-    hb[i] = B->boxes[i]->dev;
+  int best = 0;
+  double best_rate = -1.0;
+  for (int c = 0; c < GRX_GCMC_TUNE_CANDIDATES; ++c) {
+    const double rate = te_sum[c] > 0.0 ? te_sum[c] / ms_sum[c] : 1.0 / ms_sum[c];
+    if (ms_per_candidate) ms_per_candidate[c] = (float)(ms_sum[c] / 2.0);
+    if (rate > best_rate) { best_rate = rate; best = c; }
   }
-  GRX_CHECK_CUDA(cudaMemcpy(B->d_boxes, hb.data(), nb * sizeof(BoxDev), cudaMemcpyHostToDevice), "tune upload");
+  const int best_w = warps[best / 3], best_m = mults[best % 3];
+  grx_status st = upload_mult(B, best_m);
+  if (st) return st;
+  B->nwarps = best_w;
+  B->chunk_mult = best_m;
   drop_graph(B);
-  if (chosen) *chosen = best_m;
+  if (chosen) *chosen = best_w * 100 + best_m;
   return GRX_OK;
 }
 

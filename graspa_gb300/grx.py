@@ -103,6 +103,7 @@ class GcmcStats(C.Structure):
                 ("capacity_hits", C.c_int64), ("energy", C.c_double * 4), ("sum_n", C.c_double)]
 
 JOB_WIDOM, JOB_GCMC = 0, 1
+GCMC_TUNE_CANDIDATES = 9  # GRX_GCMC_TUNE_CANDIDATES: warps per box 8/12/24 x items per warp 1/2/4
 
 
 class ServerConfig(C.Structure):
@@ -135,7 +136,7 @@ EXPORTS = [
     "grx_widom_insertions", "grx_widom_insertions_async", "grx_launch_count", "grx_trial_energies_noalloc", "grx_gcmc_run",
     "grx_box_write_molecule", "grx_box_remove_molecule", "grx_gcmc_batch_create", "grx_gcmc_batch_destroy",
     "grx_gcmc_batch_set_step", "grx_gcmc_batch_launch", "grx_gcmc_batch_run_graph", "grx_gcmc_batch_stats",
-    "grx_gcmc_batch_reset_stats", "grx_gcmc_batch_autotune", "grx_arena_create", "grx_arena_destroy",
+    "grx_gcmc_batch_reset_stats", "grx_gcmc_batch_autotune", "grx_gcmc_batch_set_shape", "grx_gcmc_batch_get_shape", "grx_arena_create", "grx_arena_destroy",
     "grx_arena_usage", "grx_box_create_in", "grx_box_footprint", "grx_server_create", "grx_server_destroy",
     "grx_server_submit", "grx_server_progress", "grx_server_poll", "grx_server_time", "grx_server_launch_count",
     "grx_box_create_replica",
@@ -202,6 +203,8 @@ def load(path=LIB_PATH):
     L.grx_gcmc_batch_stats.argtypes = [C.c_void_p, P(GcmcStats), P(C.c_uint64)]
     L.grx_gcmc_batch_reset_stats.argtypes = [C.c_void_p]
     L.grx_gcmc_batch_autotune.argtypes = [C.c_void_p, C.c_int64, P(C.c_int32), P(C.c_float)]
+    L.grx_gcmc_batch_set_shape.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
+    L.grx_gcmc_batch_get_shape.argtypes = [C.c_void_p, P(C.c_int32), P(C.c_int32)]
     L.grx_arena_create.argtypes = [C.c_size_t, P(C.c_void_p)]
     L.grx_arena_destroy.argtypes = [C.c_void_p]
     L.grx_arena_usage.argtypes = [C.c_void_p, P(C.c_size_t), P(C.c_size_t), P(C.c_size_t)]
@@ -733,11 +736,23 @@ class GcmcBatch:
     def reset_stats(self):
         check(self.L.grx_gcmc_batch_reset_stats(self.h), "grx_gcmc_batch_reset_stats")
 
+    def set_shape(self, nwarps, chunk_mult):
+        check(self.L.grx_gcmc_batch_set_shape(self.h, nwarps, chunk_mult), "grx_gcmc_batch_set_shape")
+
+    def shape(self):
+        """(warps per box, work items per warp of a bead pass)."""
+        w, m = C.c_int32(), C.c_int32()
+        check(self.L.grx_gcmc_batch_get_shape(self.h, C.byref(w), C.byref(m)), "grx_gcmc_batch_get_shape")
+        return w.value, m.value
+
     def autotune(self, nsteps):
+        """Times the GCMC_TUNE_CANDIDATES launch shapes on real steps (forward and
+        reverse sweep, ranked by trial energies per second) and keeps the best:
+        returns ((nwarps, chunk_mult), mean ms per candidate probe)."""
         ch = C.c_int32()
-        ms = (C.c_float * 4)()
+        ms = (C.c_float * GCMC_TUNE_CANDIDATES)()
         check(self.L.grx_gcmc_batch_autotune(self.h, nsteps, C.byref(ch), ms), "grx_gcmc_batch_autotune")
-        return ch.value, list(ms)
+        return (ch.value // 100, ch.value % 100), list(ms)
 
 
 def cbmc_select(logw, seed, stream, move, word):

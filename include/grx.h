@@ -383,10 +383,20 @@ grx_status grx_gcmc_batch_run_graph(grx_gcmc_batch* batch, int64_t nsteps, int32
  * the next step index, and refreshes the boxes' molecule counts. */
 grx_status grx_gcmc_batch_stats(grx_gcmc_batch* batch, grx_gcmc_stats* stats, uint64_t* next_step);
 grx_status grx_gcmc_batch_reset_stats(grx_gcmc_batch* batch);
-/* Autotuner of the bead-pass work split (work items per warp: 1, 2, 4, 8): times
- * nsteps real steps per candidate with CUDA events, keeps the fastest for this batch
- * and returns it (ms_per_candidate: 4 floats or NULL). The probe steps are ordinary
- * Monte Carlo steps and advance the chains. */
+/* Launch shape of a batch: nwarps warps per box (8, 12 or 24; every shape keeps 24
+ * warps per SM) and chunk_mult work items per warp in a bead pass (1..8). A new batch
+ * takes 24 warps when its boxes fit one per SM, 12 when they fit two per SM, else 8,
+ * with chunk_mult 1. */
+grx_status grx_gcmc_batch_set_shape(grx_gcmc_batch* batch, int32_t nwarps, int32_t chunk_mult);
+grx_status grx_gcmc_batch_get_shape(grx_gcmc_batch* batch, int32_t* nwarps, int32_t* chunk_mult);
+/* Autotuner of the launch shape: runs nsteps real steps for each of the
+ * GRX_GCMC_TUNE_CANDIDATES shapes (nwarps 8, 12, 24 x chunk_mult 1, 2, 4, in that
+ * order), in a forward and a reverse sweep timed with CUDA events, and keeps the shape
+ * with the most trial energies per second for this batch. chosen receives
+ * nwarps * 100 + chunk_mult; ms_per_candidate receives GRX_GCMC_TUNE_CANDIDATES mean
+ * probe times (or NULL). The probe steps are ordinary Monte Carlo steps: the chains
+ * advance by 2 * GRX_GCMC_TUNE_CANDIDATES * nsteps. */
+#define GRX_GCMC_TUNE_CANDIDATES 9
 grx_status grx_gcmc_batch_autotune(grx_gcmc_batch* batch, int64_t nsteps, int32_t* chosen,
                                    float* ms_per_candidate);
 

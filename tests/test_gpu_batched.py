@@ -113,11 +113,12 @@ def test_autotune_keeps_chains_valid(grx_lib):
     for b in boxes:
         b.ewald_total()
     batch = grx_lib.GcmcBatch(boxes, descs, grx_lib.GRX_MIXED)
-    chosen, ms = batch.autotune(50)
-    assert chosen in (1, 2, 4, 8) and all(m > 0 for m in ms)
+    chosen, ms = batch.autotune(20)
+    assert chosen[0] in (8, 12, 24) and chosen[1] in (1, 2, 4) and batch.shape() == chosen
+    assert len(ms) == grx_lib.GCMC_TUNE_CANDIDATES and all(m > 0 for m in ms)
     batch.launch(100)
     st, nxt = batch.stats()
-    assert nxt == 300
+    assert nxt == 2 * 20 * grx_lib.GCMC_TUNE_CANDIDATES + 100
     batch.close()
     for i, b in enumerate(boxes):
         esum = st[2 * i].energy[3] + st[2 * i + 1].energy[3]

@@ -147,3 +147,27 @@ def test_gcmc_capacity_and_edges(grx_lib):
         grx_lib.gcmc_run([box], [bad], 0, 1, grx_lib.GRX_FP64)
     with pytest.raises(grx_lib.GrxError):
         grx_lib.gcmc_run([box, box], [d, d], 0, 1, grx_lib.GRX_FP64)
+
+
+@pytest.mark.parametrize("shape", [(8, 1), (8, 8), (12, 2), (24, 1), (24, 4)])
+def test_gcmc_launch_shapes_match_oracle(grx_lib, shape):
+    """Every launch shape (warps per box x items per warp of a bead pass) only changes
+    how a pass is split over warps: the FP64 chain still takes the oracle's decisions."""
+    s = co2_system(n_co2=5)
+    d = params(grx_lib, pressure_pa=1e6)
+    box = make_box(grx_lib, s)
+    batch = grx_lib.GcmcBatch([box], [d], grx_lib.GRX_FP64)
+    batch.set_shape(*shape)
+    assert batch.shape() == shape
+    batch.launch(300)
+    st, nxt = batch.stats()
+    batch.close()
+    ost, after, _ = O.OracleSystem(s).gcmc(ora_params(d), [s["comp_start"][1], CAP], 0, 300)
+    assert nxt == 300
+    assert list(st[0].accepted) == list(ost.accepted) and st[0].n_molecules == ost.n_molecules
+    nfw = s["comp_start"][1]
+    assert np.max(np.abs(box.positions(1) - after["pos"][nfw:])) <= 1e-9
+    for k in range(4):
+        assert abs(st[0].energy[k] - ost.energy[k]) <= 1e-9 * max(1.0, abs(ost.energy[k]))
+    with pytest.raises(grx_lib.GrxError):
+        grx_lib.GcmcBatch([box], [d], grx_lib.GRX_FP64).set_shape(16, 1)
