@@ -44,7 +44,31 @@ NORIENT = 10
 FLOP_PER_PAIR_CHARGED = 70.0   # FP32-equivalent work per pair (LJ + real Coulomb), the frozen work model
 FLOP_PER_PAIR_LJ = 40.0
 L2_FLUSH_BYTES = 256 << 20
-PEAK_FP32_NOMINAL = 152 * 128 * 2 * 2070e6 / 1e12   # TFLOP/s; no measured FP32 figure exists
+PEAK_FP32_NOMINAL = 152 * 128 * 2 * 2070e6 / 1e12   # TFLOP/s, 128 FMA lanes per SM at the maximum clock
+# DRAM bytes (read + write) of gcmc_kernel<mixed> per chain and Monte Carlo step: ncu
+# dram__bytes_read.sum + dram__bytes_write.sum = 28.7 + 55.8 MB for one launch of 456
+# chains x 20 steps (bench.py --profile --chains 456 --mc-steps 20, ncu --set full -k
+# regex:gcmc_kernel -s 6 -c 1), scaled by chains x steps to the timed launch.
+DRAM_BYTES_PER_CHAIN_STEP = (28.697e6 + 55.824e6) / (456 * 20)
+_FP32_PEAK = []
+
+
+def _hbm_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"])
+    except (OSError, KeyError, ValueError):
+        return 6800.0
+
+
+HBM_PEAK_GBS = _hbm_peak()
+
+
+def fp32_peak(grx):
+    """Measured FP32 FMA peak of this device (TFLOP/s), once per process."""
+    if not _FP32_PEAK:
+        _FP32_PEAK.append(grx.probe_fp32_fma())
+    return _FP32_PEAK[0]
 
 
 def dist_env():
@@ -330,11 +354,12 @@ def bench_widom(args, grx, torch, stream, flush, n_insert):
     box.close()
     t_launch = float(np.mean(tm))
     achieved = FLOP_PER_PAIR_CHARGED * pairs_step / t_launch / 1e12
+    peak = fp32_peak(grx)
     return {"workload": f"widom_co2_silica_3456, {n_insert} insertions per launch",
             "value": te_step * len(tm) / sum(tm), "unit": "trial_energies/s",
             "fp64_value": te_step * len(t64) / sum(t64),
             "speedup_mixed_over_fp64": (te_step * len(tm) / sum(tm)) / (te_step * len(t64) / sum(t64)),
-            "kernel_ms": 1000 * t_launch, "achieved_tflops": achieved, "frac_of_nominal_fp32": achieved / PEAK_FP32_NOMINAL,
+            "kernel_ms": 1000 * t_launch, "achieved_tflops": achieved, "frac_of_measured_fp32": achieved / peak,
             "accuracy_vs_fp64_oracle": acc}
 
 
@@ -452,6 +477,7 @@ def run_grx(args):
         cpu_val, cpu_te, cpu_dt, cores, chains, steps = cpu_gcmc_rate(args.cpu_seconds)
         t_launch = float(np.mean(g["times"]))
         achieved = FLOP_PER_PAIR_CHARGED * g["pairs"] / args.steps / t_launch / 1e12
+        peak = fp32_peak(grx)
         clk = g["clocks"]
         line = {
             "metric": "CBMC trial energies/s", "value": g["value"], "unit": "trial_energies/s",
@@ -470,10 +496,15 @@ def run_grx(args):
                        "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}"},
             "fp64": g["fp64"],
             "accuracy": g["accuracy"],
-            "roofline": {"bound": "fp32", "achieved": achieved, "peak": PEAK_FP32_NOMINAL, "unit": "TFLOP/s",
-                         "frac": achieved / PEAK_FP32_NOMINAL, "traffic": None,
-                         "peak_kind": "nominal FP32 CUDA-core peak at 2070 MHz (no measured FP32 figure; "
-                                      "MEASURED_PEAKS.json has HBM and bf16 only)",
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak,
+                         "traffic": DRAM_BYTES_PER_CHAIN_STEP * g["chains"] * g["mc_steps_per_step"],
+                         "traffic_unit": "bytes per launch (ncu DRAM read + write, 20-step capture scaled)",
+                         "hbm_gbs_achieved": DRAM_BYTES_PER_CHAIN_STEP * g["chains"] * g["mc_steps_per_step"]
+                                             / t_launch / 1e9,
+                         "hbm_peak_gbs": HBM_PEAK_GBS,
+                         "peak_kind": "measured FP32 FMA throughput of this GPU in this run (grx_probe_fp32_fma); "
+                                      f"nominal {PEAK_FP32_NOMINAL:.1f}",
                          "kernel": "gcmc_kernel<mixed>",
                          "model": f"{FLOP_PER_PAIR_CHARGED:.0f} FLOP/pair x {g['pairs'] / args.steps:.4g} pairs "
                                   "per launch (beads x (framework + guest atoms))"},
@@ -539,8 +570,8 @@ def bench_other(args, grx, torch, stream, flush, which):
                 "workload": "batched_ch4_xe_64_triclinic (mixture GCMC, 8-32 trials, LJ only)",
                 "mc_steps_per_step": args.mc_steps,
                 "autotune": {"warps_per_box": chosen[0], "chunk_mult": chosen[1], "ms_per_candidate": cand_ms},
-                "roofline": {"bound": "fp32", "achieved": achieved, "peak": PEAK_FP32_NOMINAL, "unit": "TFLOP/s",
-                             "frac": achieved / PEAK_FP32_NOMINAL, "model": "40 FLOP/pair (LJ only)"},
+                "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak(grx), "unit": "TFLOP/s",
+                             "frac": achieved / fp32_peak(grx), "model": "40 FLOP/pair (LJ only)"},
                 "framework_atoms": [int(s["comp_start"][1]) for s in systems[:8]]}
     system = synth.tip4p_hex_system(n_water=0)
     nfw = system["comp_start"][1]

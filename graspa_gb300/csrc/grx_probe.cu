@@ -1,0 +1,60 @@
+// grx_probe.cu -- FP32 FMA throughput of the device, the denominator of the pair
+// kernels' roofline (no measured FP32 figure is supplied with the device peaks).
+//
+// Every thread runs kChains independent FMA chains (enough instruction-level
+// parallelism to cover the FMA latency); the grid fills every SM with 1024 threads.
+#include "grx_host.h"
+
+namespace grx {
+
+constexpr int kChains = 8;
+
+__global__ void __launch_bounds__(256) fma_probe_kernel(float* out, int iters, float b, float c) {
+  float a[kChains];
+#pragma unroll
+  for (int k = 0; k < kChains; ++k) a[k] = 1e-3f * (float)(threadIdx.x + k);
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int u = 0; u < 16; ++u)
+#pragma unroll
+      for (int k = 0; k < kChains; ++k) a[k] = __fmaf_rn(a[k], b, c);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int k = 0; k < kChains; ++k) s += a[k];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+}  // namespace grx
+
+using namespace grx;
+
+extern "C" grx_status grx_probe_fp32_fma(int32_t iters, double* tflops, float* ms) {
+  GRX_REQUIRE(tflops && iters >= 1, "grx_probe_fp32_fma: bad argument");
+  int dev = 0, sms = 0;
+  GRX_CHECK_CUDA(cudaGetDevice(&dev), "device");
+  GRX_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev), "SM count");
+  const int blocks = 4 * sms, threads = 256;
+  float* out = nullptr;
+  GRX_CHECK_CUDA(cudaMalloc(&out, (size_t)blocks * threads * sizeof(float)), "probe buffer");
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  fma_probe_kernel<<<blocks, threads>>>(out, 16, 0.999f, 1e-6f);  // warm-up
+  count_launch();
+  cudaEventRecord(e0);
+  fma_probe_kernel<<<blocks, threads>>>(out, iters, 0.999f, 1e-6f);
+  count_launch();
+  cudaEventRecord(e1);
+  const cudaError_t e = cudaEventSynchronize(e1);
+  float t = 0.f;
+  cudaEventElapsedTime(&t, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  GRX_CHECK_CUDA(e, "probe run");
+  const double flop = 2.0 * kChains * 16.0 * (double)iters * blocks * threads;
+  *tflops = flop / (t * 1e-3) / 1e12;
+  if (ms) *ms = t;
+  return GRX_OK;
+}

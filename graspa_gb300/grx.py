@@ -133,7 +133,7 @@ EXPORTS = [
     "grx_box_get_exclusion", "grx_trial_energies", "grx_single_body_energy", "grx_ewald_sizes",
     "grx_ewald_total", "grx_ewald_set_structure_factors", "grx_ewald_get_structure_factors",
     "grx_ewald_delta", "grx_ewald_commit", "grx_total_energy", "grx_cbmc_select",
-    "grx_widom_insertions", "grx_widom_insertions_async", "grx_launch_count", "grx_trial_energies_noalloc", "grx_gcmc_run",
+    "grx_widom_insertions", "grx_widom_insertions_async", "grx_launch_count", "grx_probe_fp32_fma", "grx_trial_energies_noalloc", "grx_gcmc_run",
     "grx_box_write_molecule", "grx_box_remove_molecule", "grx_gcmc_batch_create", "grx_gcmc_batch_destroy",
     "grx_gcmc_batch_set_step", "grx_gcmc_batch_launch", "grx_gcmc_batch_run_graph", "grx_gcmc_batch_stats",
     "grx_gcmc_batch_reset_stats", "grx_gcmc_batch_autotune", "grx_gcmc_batch_set_shape", "grx_gcmc_batch_get_shape", "grx_arena_create", "grx_arena_destroy",
@@ -188,6 +188,7 @@ def load(path=LIB_PATH):
     L.grx_widom_insertions_async.argtypes = [C.c_void_p, P(WidomDesc), C.c_uint64, C.c_size_t, C.c_int32,
                                              C.c_void_p]
     L.grx_launch_count.restype = C.c_uint64
+    L.grx_probe_fp32_fma.argtypes = [C.c_int32, P(C.c_double), P(C.c_float)]
     L.grx_trial_energies_noalloc.argtypes = [C.c_void_p, P(Trials), C.c_int32, C.c_int64, C.c_int64, C.c_int32,
                                              P(TrialEnergy), _u8p]
     L.grx_box_write_molecule.argtypes = [C.c_void_p, C.c_int32, C.c_size_t, _dp, _dp, P(C.c_size_t)]
@@ -766,3 +767,10 @@ def cbmc_select(logw, seed, stream, move, word):
 
 def launch_count():
     return load().grx_launch_count()
+
+
+def probe_fp32_fma(iters=20000):
+    """Measured FP32 FMA throughput of the device in TFLOP/s (grx_probe_fp32_fma)."""
+    t, ms = C.c_double(), C.c_float()
+    check(load().grx_probe_fp32_fma(iters, C.byref(t), C.byref(ms)), "grx_probe_fp32_fma")
+    return t.value

@@ -400,6 +400,12 @@ grx_status grx_gcmc_batch_get_shape(grx_gcmc_batch* batch, int32_t* nwarps, int3
 grx_status grx_gcmc_batch_autotune(grx_gcmc_batch* batch, int64_t nsteps, int32_t* chosen,
                                    float* ms_per_candidate);
 
+/* ---- measurement ------------------------------------------------------------ */
+/* FP32 FMA throughput of the current device (TFLOP/s, 2 FLOP per FMA): independent
+ * FMA chains on every SM, timed with CUDA events over `iters` x 128 FMAs per thread.
+ * The roofline denominator of the pair kernels (no gRASPA counterpart). */
+grx_status grx_probe_fp32_fma(int32_t iters, double* tflops, float* ms);
+
 /* ---- serving ----------------------------------------------------------------- */
 /* A continuous-batching job server. Each job is one box (its description and atoms,
  * copied at submission) with Widom insertions or GCMC steps to run. The caller's loop
