@@ -412,17 +412,16 @@ grx_status grx_total_energy(grx_box* b, grx_energy* out) {
   return GRX_OK;
 }
 
-grx_status grx_ewald_delta(grx_box* b, int32_t comp, int32_t move_type, const double* old_pos,
-                           const double* old_qs, size_t n_old, const double* new_pos,
-                           const double* new_qs, size_t n_new, double scale_coul_new,
-                           double* out2) {
-  GRX_REQUIRE(b && out2, "grx_ewald_delta: null argument");
-  GRX_REQUIRE(comp >= 0 && comp < b->ncomp, "grx_ewald_delta: component out of range");
-  GRX_REQUIRE(n_old <= GRX_MAX_MOLSIZE && n_new <= GRX_MAX_MOLSIZE, "grx_ewald_delta: too many atoms");
-  GRX_REQUIRE((n_old == 0 || (old_pos && old_qs)) && (n_new == 0 || (new_pos && new_qs)),
-              "grx_ewald_delta: atom arrays missing");
-  out2[0] = out2[1] = 0.0;
-  if (b->dev.no_charges && !b->has_charge[comp]) return GRX_OK;
+}  // extern "C"
+
+namespace grx {
+
+// Runs the Fourier delta of the staged old / new atoms (ewald_delta_kernel) against
+// `same` (its S + dS staged into s_tmp) and `cross`; returns the two sums.
+static grx_status ewald_delta_run(grx_box* b, const double* old_pos, const double* old_qs, size_t n_old,
+                                  const double* new_pos, const double* new_qs, size_t n_new, const double2* same,
+                                  const double2* cross, double& s_same, double& s_cross) {
+  s_same = s_cross = 0.0;
   MoveAtoms mv{};
   mv.n_old = (int)n_old;
   mv.n_new = (int)n_new;
@@ -446,9 +445,6 @@ grx_status grx_ewald_delta(grx_box* b, int32_t comp, int32_t move_type, const do
   double* part = (double*)((char*)b->scratch + (sizeof(MoveAtoms) + 255) / 256 * 256);
   GRX_CHECK_CUDA(cudaMemcpyAsync(d_mv, &mv, sizeof(MoveAtoms), cudaMemcpyHostToDevice, b->stream), "upload move");
   refresh_dev(b);
-  const bool host_comp = comp < b->nhost;
-  const double2* same = host_comp ? b->s_fw : b->s_ads;
-  const double2* cross = host_comp ? b->s_ads : b->s_fw;
   const int na = (int)(n_old + n_new);
   const size_t smem = (size_t)(b->dev.kmax[0] + b->dev.kmax[1] + b->dev.kmax[2] + 3) * std::max(na, 1) * sizeof(double2);
   std::vector<double> parts(2 * nblk, 0.0);
@@ -460,8 +456,30 @@ grx_status grx_ewald_delta(grx_box* b, int32_t comp, int32_t move_type, const do
                    "read ewald partials");
   }
   GRX_CHECK_CUDA(cudaStreamSynchronize(b->stream), "ewald delta");
-  double s_same = 0, s_cross = 0;
   for (int k = 0; k < nblk; ++k) { s_same += parts[2 * k]; s_cross += parts[2 * k + 1]; }
+  return GRX_OK;
+}
+
+}  // namespace grx
+
+extern "C" {
+
+grx_status grx_ewald_delta(grx_box* b, int32_t comp, int32_t move_type, const double* old_pos,
+                           const double* old_qs, size_t n_old, const double* new_pos,
+                           const double* new_qs, size_t n_new, double scale_coul_new,
+                           double* out2) {
+  GRX_REQUIRE(b && out2, "grx_ewald_delta: null argument");
+  GRX_REQUIRE(comp >= 0 && comp < b->ncomp, "grx_ewald_delta: component out of range");
+  GRX_REQUIRE(n_old <= GRX_MAX_MOLSIZE && n_new <= GRX_MAX_MOLSIZE, "grx_ewald_delta: too many atoms");
+  GRX_REQUIRE((n_old == 0 || (old_pos && old_qs)) && (n_new == 0 || (new_pos && new_qs)),
+              "grx_ewald_delta: atom arrays missing");
+  out2[0] = out2[1] = 0.0;
+  if (b->dev.no_charges && !b->has_charge[comp]) return GRX_OK;
+  const bool host_comp = comp < b->nhost;
+  double s_same = 0, s_cross = 0;
+  grx_status st = ewald_delta_run(b, old_pos, old_qs, n_old, new_pos, new_qs, n_new, host_comp ? b->s_fw : b->s_ads,
+                                  host_comp ? b->s_ads : b->s_fw, s_same, s_cross);
+  if (st) return st;
   // rigid exclusion correction of GPU_EwaldDifference_General (:548-574)
   if (b->rigid[comp]) {
     const double ex = b->excl_intra[comp] + b->excl_self[comp];
@@ -470,6 +488,56 @@ grx_status grx_ewald_delta(grx_box* b, int32_t comp, int32_t move_type, const do
     else if (move_type == GRX_MOVE_DELETION || move_type == GRX_MOVE_SINGLE_DELETION)
       s_same -= ex * (0.0 - 1.0);
   }
+  out2[0] = s_same;
+  out2[1] = 2.0 * s_cross;
+  return GRX_OK;
+}
+
+grx_status grx_ewald_delta_lambda(grx_box* b, int32_t comp, const double* pos, const double* charge, size_t n,
+                                  double scale_coul_old, double scale_coul_new, int32_t use_staged, double* out2) {
+  GRX_REQUIRE(b && out2, "grx_ewald_delta_lambda: null argument");
+  GRX_REQUIRE(comp >= b->nhost && comp < b->ncomp, "grx_ewald_delta_lambda: component must be an adsorbate");
+  GRX_REQUIRE(n >= 1 && n <= GRX_MAX_MOLSIZE && pos && charge, "grx_ewald_delta_lambda: bad atom arrays");
+  out2[0] = out2[1] = 0.0;
+  if (b->dev.no_charges && !b->has_charge[comp]) return GRX_OK;
+  std::vector<double> hq(n), qo(n), qn(n);
+  GRX_CHECK_CUDA(cudaMemcpy(hq.data(), charge, n * sizeof(double), cudaMemcpyDefault), "read charges");
+  for (size_t a = 0; a < n; ++a) {  // Fourier_Ewald_Diff_LambdaChange: the same atoms, old and new scaleCoul
+    qo[a] = hq[a] * scale_coul_old;
+    qn[a] = hq[a] * scale_coul_new;
+  }
+  double s_same = 0, s_cross = 0;
+  grx_status st = ewald_delta_run(b, pos, qo.data(), n, pos, qn.data(), n, use_staged ? b->s_tmp : b->s_ads, b->s_fw,
+                                  s_same, s_cross);
+  if (st) return st;
+  // GPU_EwaldDifference_LambdaChange (:782-785): exclusion times the change of scaleCoul^2
+  s_same -= (b->excl_intra[comp] + b->excl_self[comp]) *
+            (scale_coul_new * scale_coul_new - scale_coul_old * scale_coul_old);
+  out2[0] = s_same;
+  out2[1] = 2.0 * s_cross;
+  return GRX_OK;
+}
+
+grx_status grx_ewald_delta_identity_swap(grx_box* b, int32_t old_comp, int32_t new_comp, const double* old_pos,
+                                         const double* old_qs, size_t n_old, const double* new_pos,
+                                         const double* new_qs, size_t n_new, double* out2) {
+  GRX_REQUIRE(b && out2, "grx_ewald_delta_identity_swap: null argument");
+  GRX_REQUIRE(old_comp >= b->nhost && old_comp < b->ncomp && new_comp >= b->nhost && new_comp < b->ncomp,
+              "grx_ewald_delta_identity_swap: both components must be adsorbates");
+  GRX_REQUIRE(n_old <= GRX_MAX_MOLSIZE && n_new <= GRX_MAX_MOLSIZE, "grx_ewald_delta_identity_swap: too many atoms");
+  GRX_REQUIRE((n_old == 0 || (old_pos && old_qs)) && (n_new == 0 || (new_pos && new_qs)),
+              "grx_ewald_delta_identity_swap: atom arrays missing");
+  out2[0] = out2[1] = 0.0;
+  const bool q_old = b->has_charge[old_comp] != 0, q_new = b->has_charge[new_comp] != 0;
+  if (b->dev.no_charges && !q_old && !q_new) return GRX_OK;
+  // atoms of an uncharged side do not enter (Ewald_Energy_Functions.h:588-597)
+  const size_t no = q_old ? n_old : 0, nn = q_new ? n_new : 0;
+  if (no + nn == 0) return GRX_OK;
+  double s_same = 0, s_cross = 0;
+  grx_status st = ewald_delta_run(b, old_pos, old_qs, no, new_pos, new_qs, nn, b->s_ads, b->s_fw, s_same, s_cross);
+  if (st) return st;
+  if (b->rigid[new_comp] && q_new) s_same -= (b->excl_intra[new_comp] + b->excl_self[new_comp]) * 1.0;
+  if (b->rigid[old_comp] && q_old) s_same -= (b->excl_intra[old_comp] + b->excl_self[old_comp]) * -1.0;
   out2[0] = s_same;
   out2[1] = 2.0 * s_cross;
   return GRX_OK;

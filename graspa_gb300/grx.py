@@ -17,6 +17,7 @@ GRX_FP64, GRX_MIXED, GRX_FP32 = 0, 1, 2
 PRECISIONS = {"fp64": GRX_FP64, "mixed": GRX_MIXED, "fp32": GRX_FP32}
 MOVE_TRANSLATION, MOVE_ROTATION, MOVE_SINGLE_INSERTION, MOVE_SINGLE_DELETION = 0, 1, 2, 3
 MOVE_INSERTION, MOVE_DELETION, MOVE_REINSERTION = 5, 6, 7
+MOVE_CBCF_LAMBDACHANGE, MOVE_CBCF_INSERTION, MOVE_CBCF_DELETION, MOVE_IDENTITY_SWAP = 8, 9, 10, 11
 MAX_COMPONENTS = 8
 
 _dp = C.POINTER(C.c_double)
@@ -132,7 +133,7 @@ EXPORTS = [
     "grx_box_set_stream", "grx_box_set_component", "grx_box_get_component_size", "grx_box_get_positions",
     "grx_box_get_exclusion", "grx_trial_energies", "grx_single_body_energy", "grx_ewald_sizes",
     "grx_ewald_total", "grx_ewald_set_structure_factors", "grx_ewald_get_structure_factors",
-    "grx_ewald_delta", "grx_ewald_commit", "grx_total_energy", "grx_cbmc_select",
+    "grx_ewald_delta", "grx_ewald_delta_lambda", "grx_ewald_delta_identity_swap", "grx_ewald_commit", "grx_total_energy", "grx_cbmc_select",
     "grx_widom_insertions", "grx_widom_insertions_async", "grx_launch_count", "grx_probe_fp32_fma", "grx_trial_energies_noalloc", "grx_gcmc_run",
     "grx_box_write_molecule", "grx_box_remove_molecule", "grx_gcmc_batch_create", "grx_gcmc_batch_destroy",
     "grx_gcmc_batch_set_step", "grx_gcmc_batch_launch", "grx_gcmc_batch_run_graph", "grx_gcmc_batch_stats",
@@ -180,6 +181,10 @@ def load(path=LIB_PATH):
     L.grx_ewald_get_structure_factors.argtypes = [C.c_void_p, _dp, _dp, _dp]
     L.grx_ewald_delta.argtypes = [C.c_void_p, C.c_int32, C.c_int32, _dp, _dp, C.c_size_t, _dp, _dp,
                                   C.c_size_t, C.c_double, _dp]
+    L.grx_ewald_delta_lambda.argtypes = [C.c_void_p, C.c_int32, _dp, _dp, C.c_size_t, C.c_double, C.c_double,
+                                         C.c_int32, _dp]
+    L.grx_ewald_delta_identity_swap.argtypes = [C.c_void_p, C.c_int32, C.c_int32, _dp, _dp, C.c_size_t, _dp, _dp,
+                                                C.c_size_t, _dp]
     L.grx_ewald_commit.argtypes = [C.c_void_p, C.c_int32]
     L.grx_total_energy.argtypes = [C.c_void_p, P(Energy)]
     L.grx_cbmc_select.argtypes = [_dp, C.c_int32, C.c_uint64, C.c_uint32, C.c_uint64, C.c_int32,
@@ -442,6 +447,26 @@ class Box:
         out = np.zeros(2)
         check(self.L.grx_ewald_delta(self.h, comp, move_type, _d(op), _d(oq), len(oq), _d(npos), _d(nq), len(nq),
                                      scale_coul_new, _d(out)), "grx_ewald_delta")
+        return out
+
+    def ewald_delta_lambda(self, comp, pos, charge, scale_coul_old, scale_coul_new, use_staged=False):
+        """Fourier delta of a lambda change at fixed positions (CB/CFC)."""
+        p = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1)
+        q = np.ascontiguousarray(charge, dtype=np.float64)
+        out = np.zeros(2)
+        check(self.L.grx_ewald_delta_lambda(self.h, comp, _d(p), _d(q), len(q), scale_coul_old, scale_coul_new,
+                                            int(bool(use_staged)), _d(out)), "grx_ewald_delta_lambda")
+        return out
+
+    def ewald_delta_identity_swap(self, old_comp, new_comp, old_pos, old_qs, new_pos, new_qs):
+        """Fourier delta of an identity swap (old_comp molecule out, new_comp molecule in)."""
+        op = np.ascontiguousarray(old_pos, dtype=np.float64).reshape(-1)
+        oq = np.ascontiguousarray(old_qs, dtype=np.float64)
+        npos = np.ascontiguousarray(new_pos, dtype=np.float64).reshape(-1)
+        nq = np.ascontiguousarray(new_qs, dtype=np.float64)
+        out = np.zeros(2)
+        check(self.L.grx_ewald_delta_identity_swap(self.h, old_comp, new_comp, _d(op), _d(oq), len(oq), _d(npos),
+                                                   _d(nq), len(nq), _d(out)), "grx_ewald_delta_identity_swap")
         return out
 
     def ewald_commit(self, comp):

@@ -138,6 +138,25 @@ int main(int argc, char** argv) {
       }
       std::printf("widom_average_rosenbluth %.17g\n", WidomAverageRosenbluth(C, comp));
       std::printf("widom_mu_ex_K %.17g\n", WidomChemicalPotential(C, comp));
+    } else if (mode == "lambda") {
+      // CB/CFC lambda steps of molecule 0: 1 -> 0.4 as a lambda change, the caller's update
+      // of the molecule's scales, then 0.4 -> 0.1 as the second step of a CB/CFC deletion
+      // (Fourier part from the staged vector)
+      const double steps[2][2] = {{1.0, 0.4}, {0.4, 0.1}};
+      const int types[2] = {CBCF_LAMBDACHANGE, CBCF_DELETION};
+      Atoms& A = V.Sims[0].d_a[comp];
+      for (int k = 0; k < 2; ++k) {
+        size_t start = 0;
+        bool ok = false;
+        const MoveEnergy e = CBCF_LambdaChange(V, 0, 0, comp, double2{steps[k][0], steps[k][0]},
+                                               double2{steps[k][1], steps[k][1]}, start, types[k], ok);
+        std::printf("lambda %d %d %.17g %.17g %.17g %.17g %.17g %.17g %.17g %.17g\n", k, ok ? 1 : 0, e.HGVDW,
+                    e.HGReal, e.GGVDW, e.GGReal, e.GGEwaldE, e.HGEwaldE, e.TailE, e.total());
+        for (size_t a = 0; a < C.Moleculesize[comp]; ++a) {
+          A.scale[start + a] = steps[k][1];
+          A.scaleCoul[start + a] = steps[k][1];
+        }
+      }
     } else {
       long long att[5] = {0, 0, 0, 0, 0}, acc[5] = {0, 0, 0, 0, 0};
       double esum = 0.0;

@@ -514,6 +514,100 @@ static void rotate_axis(double3& v, double theta, int axis) {
   v = double3{v.x * r0 + v.y * r1 + v.z * r2, v.x * r3 + v.y * r4 + v.z * r5, v.x * r6 + v.y * r7 + v.z * r8};
 }
 
+double2 GPU_EwaldDifference_LambdaChange(Simulations& Sims, ForceField& FF, Components& SC, size_t comp,
+                                         size_t start_position, double2 oldScale, double2 newScale, int MoveType) {
+  if (FF.noCharges && !SC.hasPartialCharge[comp]) return double2{};
+  const size_t ms = SC.Moleculesize[comp];
+  const Atoms& A = Sims.d_a[comp];
+  std::vector<double> pos(3 * ms), q(ms);
+  for (size_t a = 0; a < ms; ++a) {
+    pos[3 * a] = A.pos[start_position + a].x;
+    pos[3 * a + 1] = A.pos[start_position + a].y;
+    pos[3 * a + 2] = A.pos[start_position + a].z;
+    q[a] = A.charge[start_position + a];
+  }
+  // the second step of a CB/CFC deletion starts from the staged vector (:775-778)
+  const int use_staged = MoveType == CBCF_DELETION ? 1 : 0;
+  double out2[2];
+  check(grx_ewald_delta_lambda(Sims.Box.handle, (int32_t)comp, pos.data(), q.data(), ms, oldScale.y, newScale.y,
+                               use_staged, out2),
+        "grx_ewald_delta_lambda");
+  return double2{out2[0], out2[1]};
+}
+
+double2 GPU_EwaldDifference_IdentitySwap(Simulations& Sims, ForceField& FF, Components& SC, size_t OLDComponent,
+                                         size_t NEWComponent, size_t UpdateLocation,
+                                         const std::vector<double3>& NewPositions) {
+  if (FF.noCharges && !SC.hasPartialCharge[NEWComponent] && !SC.hasPartialCharge[OLDComponent]) return double2{};
+  std::vector<double> op, oq;
+  molecule_atoms(Sims, SC, OLDComponent, UpdateLocation, op, oq);
+  const size_t mn = SC.Moleculesize[NEWComponent];
+  const Atoms& T = Sims.d_a[NEWComponent];  // charges of the new species: its slot-0 storage
+  std::vector<double> np(3 * mn), nq(mn);
+  for (size_t a = 0; a < mn; ++a) {
+    np[3 * a] = NewPositions[a].x; np[3 * a + 1] = NewPositions[a].y; np[3 * a + 2] = NewPositions[a].z;
+    nq[a] = T.charge[a];
+  }
+  double out2[2];
+  check(grx_ewald_delta_identity_swap(Sims.Box.handle, (int32_t)OLDComponent, (int32_t)NEWComponent, op.data(),
+                                      oq.data(), oq.size(), np.data(), nq.data(), mn, out2),
+        "grx_ewald_delta_identity_swap");
+  return double2{out2[0], out2[1]};
+}
+
+MoveEnergy CBCF_LambdaChange(Variables& Vars, size_t systemId, size_t SelectedMolInComponent,
+                             size_t SelectedComponent, double2 oldScale, double2 newScale, size_t& start_position,
+                             int MoveType, bool& SuccessConstruction) {
+  Components& SC = Vars.SystemComponents[systemId];
+  Simulations& Sims = Vars.Sims[systemId];
+  const size_t comp = SelectedComponent, ms = SC.Moleculesize[comp];
+  start_position = SelectedMolInComponent * ms;
+  const Atoms& A = Sims.d_a[comp];
+  // Calculate_Single_Body_Energy_VDWReal_LambdaChange (VDW_Coulomb.cu:843-1009): the same
+  // positions with the stored (old) scales and with newScale
+  std::vector<double> q(ms), sco(ms), scco(ms), scn(ms, newScale.x), sccn(ms, newScale.y);
+  std::vector<size_t> ty(ms);
+  for (size_t a = 0; a < ms; ++a) {
+    q[a] = A.charge[start_position + a];
+    sco[a] = A.scale[start_position + a];
+    scco[a] = A.scaleCoul[start_position + a];
+    ty[a] = A.Type[start_position + a];
+  }
+  grx_trials to{}, tn{};
+  to.pos = tn.pos = reinterpret_cast<const double*>(A.pos + start_position);
+  to.scale = sco.data();
+  to.scale_coul = scco.data();
+  tn.scale = scn.data();
+  tn.scale_coul = sccn.data();
+  to.charge = tn.charge = q.data();
+  to.type = tn.type = ty.data();
+  to.molid = tn.molid = SelectedMolInComponent;
+  to.ntrials = tn.ntrials = 1;
+  to.chainsize = tn.chainsize = ms;
+  double e6[6];
+  uint8_t flag = 0;
+  check(grx_single_body_energy(Sims.Box.handle, &to, &tn, (int32_t)comp, 1, 1, Vars.Precision, e6, &flag),
+        "grx_single_body_energy");
+  MoveEnergy tot;
+  SuccessConstruction = flag == 0;
+  if (!SuccessConstruction) return tot;
+  tot.HHVDW = e6[0]; tot.HHReal = e6[1]; tot.HGVDW = e6[2];
+  tot.HGReal = e6[3]; tot.GGVDW = e6[4]; tot.GGReal = e6[5];
+  if (!Vars.device_FF.noCharges && SC.hasPartialCharge[comp]) {
+    const double2 E = GPU_EwaldDifference_LambdaChange(Sims, Vars.device_FF, SC, comp, start_position, oldScale,
+                                                       newScale, MoveType);
+    if (comp >= (size_t)SC.NComponents.y) { tot.GGEwaldE = E.x; tot.HGEwaldE = E.y; }
+    else { tot.HHEwaldE = E.x; tot.HGEwaldE = E.y; }
+  }
+  // TailCorrectionDifference (TailCorrection_Energy_Functions.h:35-84): CB/CFC insertion and
+  // deletion refuse tail corrections; a plain lambda change takes the insertion sign.
+  const double tail = SC.TailCorrectionInsert.empty() ? 0.0 : SC.TailCorrectionInsert[comp];
+  if (tail != 0.0 && (MoveType == CBCF_INSERTION || MoveType == CBCF_DELETION))
+    throw std::runtime_error("TAIL CORRECTIONS NOT READY FOR CBCF MOVES!");
+  tot.TailE = tail;
+  return tot;
+}
+
 MoveEnergy SingleBodyMove(Variables& Vars, size_t systemId, int MoveType, double RANDOM) {
   Components& SC = Vars.SystemComponents[systemId];
   Simulations& Sims = Vars.Sims[systemId];

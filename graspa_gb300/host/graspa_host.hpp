@@ -220,6 +220,20 @@ double2 GPU_EwaldDifference_General(Simulations& Sims, ForceField& FF, Component
                                     size_t SelectedComponent, int MoveType, size_t Location, double2 Scale);
 // Ewald_Energy_Functions.h:423-433.
 void Update_Vector_Ewald(Boxsize& Box, bool UseTempVector, Components& SystemComponents, size_t SelectedComponent);
+// CB/CFC and identity-swap variants of the Fourier delta (Ewald_Energy_Functions.h:582-634,764-789):
+// the molecule starting at start_position changes (scale, scaleCoul) from oldScale to newScale,
+// or the molecule of OLDComponent at UpdateLocation becomes one of NEWComponent at NewPositions.
+double2 GPU_EwaldDifference_LambdaChange(Simulations& Sims, ForceField& FF, Components& SystemComponents,
+                                         size_t SelectedComponent, size_t start_position, double2 oldScale,
+                                         double2 newScale, int MoveType);
+double2 GPU_EwaldDifference_IdentitySwap(Simulations& Sims, ForceField& FF, Components& SystemComponents,
+                                         size_t OLDComponent, size_t NEWComponent, size_t UpdateLocation,
+                                         const std::vector<double3>& NewPositions);
+// Energy of a lambda change of one molecule (mc_cbcfc.h:20-124): pair part over every other
+// atom at fixed positions, Fourier part and tail; SuccessConstruction is false on overlap.
+MoveEnergy CBCF_LambdaChange(Variables& Vars, size_t systemId, size_t SelectedMolInComponent,
+                             size_t SelectedComponent, double2 oldScale, double2 newScale, size_t& start_position,
+                             int MoveType, bool& SuccessConstruction);
 // VDW_Coulomb.cu:1580 + Ewald_Energy_Functions.h:1272 (FP64 drift-check totals).
 MoveEnergy Total_Energy(Simulations& Sims);
 // GetPrefactor (mc_utilities.h:315-351).

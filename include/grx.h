@@ -72,7 +72,11 @@ enum {
   GRX_MOVE_SPECIAL_ROTATION = 4,
   GRX_MOVE_INSERTION = 5,
   GRX_MOVE_DELETION = 6,
-  GRX_MOVE_REINSERTION = 7
+  GRX_MOVE_REINSERTION = 7,
+  GRX_MOVE_CBCF_LAMBDACHANGE = 8,
+  GRX_MOVE_CBCF_INSERTION = 9,
+  GRX_MOVE_CBCF_DELETION = 10,
+  GRX_MOVE_IDENTITY_SWAP = 11
 };
 
 typedef struct grx_box grx_box; /* opaque, device-resident state of one box */
@@ -282,6 +286,29 @@ grx_status grx_ewald_delta(grx_box* box, int32_t component, int32_t move_type,
                            const double* old_pos, const double* old_qs, size_t n_old,
                            const double* new_pos, const double* new_qs, size_t n_new,
                            double scale_coul_new, double* out2);
+/* Fourier delta of a lambda change of one fractional molecule of an adsorbate
+ * component at fixed positions: GPU_EwaldDifference_LambdaChange
+ * (Ewald_Energy_Functions.h:764-789) with Fourier_Ewald_Diff_LambdaChange (:636-762).
+ * charge holds the atoms' charges without lambda; the old atoms carry
+ * scale_coul_old, the new ones scale_coul_new. use_staged != 0 starts from the staged
+ * vector instead of the adsorbate S(k) (the second step of a CB/CFC deletion, :775-778).
+ * Stages S + dS. out2 = {same-type delta - (ExclusionIntra + ExclusionAtom) *
+ * (scale_coul_new^2 - scale_coul_old^2), 2 * cross-type delta}. The pair part of the
+ * lambda change (Calculate_Single_Body_Energy_VDWReal_LambdaChange, VDW_Coulomb.cu:843-1009)
+ * is grx_single_body_energy with the same positions and the old / new scales. */
+grx_status grx_ewald_delta_lambda(grx_box* box, int32_t component, const double* pos, const double* charge,
+                                  size_t n, double scale_coul_old, double scale_coul_new, int32_t use_staged,
+                                  double* out2);
+/* Fourier delta of an identity swap (GPU_EwaldDifference_IdentitySwap,
+ * Ewald_Energy_Functions.h:582-634): the molecule of old_component (positions,
+ * charge*scaleCoul) leaves, the molecule of new_component arrives; atoms of an uncharged
+ * side do not enter. Stages S + dS. out2 = {same-type delta - ExclusionNew +
+ * ExclusionOld (rigid, charged components), 2 * cross-type delta}. The pair part of the
+ * new molecule is grx_trial_energies with the old molecule excluded (ExcludeList). */
+grx_status grx_ewald_delta_identity_swap(grx_box* box, int32_t old_component, int32_t new_component,
+                                         const double* old_pos, const double* old_qs, size_t n_old,
+                                         const double* new_pos, const double* new_qs, size_t n_new,
+                                         double* out2);
 /* Accept: make the staged structure factor current (Update_Vector_Ewald,
  * Ewald_Energy_Functions.h:423-433). */
 grx_status grx_ewald_commit(grx_box* box, int32_t component);

@@ -551,6 +551,35 @@ void ora_ewald_delta(const ora_box* box, const double* s_same, const double* s_c
   out2[1] = cross;
 }
 
+// Lambda change of one fractional molecule at fixed positions: Fourier_Ewald_Diff_LambdaChange
+// (Ewald_Energy_Functions.h:636-762) driven by GPU_EwaldDifference_LambdaChange (:764-789).
+// q are the atoms' charges; dS = sum q (scale_new - scale_old) e^{ik.r}; use_temp starts
+// from s_temp (the CB/CFC deletion's second step). out2 = {same - excl * (new^2 - old^2),
+// 2 * cross}, excl = ExclusionIntra + ExclusionAtom of the component.
+void ora_ewald_delta_lambda(const ora_box* box, const double* s_same, const double* s_cross, int32_t use_temp,
+                            const double* s_temp, int64_t n, const double* pos, const double* q, double scale_old,
+                            double scale_new, double excl, double* s_new, double* out2) {
+  std::vector<double> qo((size_t)n), qn((size_t)n);
+  for (int64_t i = 0; i < n; ++i) { qo[i] = q[i] * scale_old; qn[i] = q[i] * scale_new; }
+  double o2[2];
+  ora_ewald_delta(box, s_same, s_cross, use_temp, s_temp, n, pos, qo.data(), n, pos, qn.data(), s_new, o2);
+  out2[0] = o2[0] - excl * (scale_new * scale_new - scale_old * scale_old);
+  out2[1] = 2.0 * o2[1];
+}
+
+// Identity swap: GPU_EwaldDifference_IdentitySwap (Ewald_Energy_Functions.h:582-634). The old
+// molecule leaves, the new one arrives (n_old / n_new already zero for an uncharged side);
+// excl_new / excl_old are ExclusionIntra + ExclusionAtom of rigid charged components, else 0.
+void ora_ewald_delta_identity_swap(const ora_box* box, const double* s_same, const double* s_cross,
+                                   int64_t n_old, const double* old_pos, const double* old_qs, int64_t n_new,
+                                   const double* new_pos, const double* new_qs, double excl_new, double excl_old,
+                                   double* s_new, double* out2) {
+  double o2[2];
+  ora_ewald_delta(box, s_same, s_cross, 0, nullptr, n_old, old_pos, old_qs, n_new, new_pos, new_qs, s_new, o2);
+  out2[0] = o2[0] - excl_new * 1.0 - excl_old * -1.0;
+  out2[1] = 2.0 * o2[1];
+}
+
 // Rigid-molecule exclusion constants: Calculate_Intra_Molecule_Exclusion and
 // Calculate_Self_Exclusion, ewald_preparation.h:261-298.
 void ora_rigid_exclusion(const ora_box* box, int64_t ms, const double* pos, const double* q,

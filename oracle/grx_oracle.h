@@ -149,6 +149,13 @@ void ora_ewald_delta(const ora_box* box, const double* s_same, const double* s_c
                      int64_t n_old, const double* old_pos, const double* old_qs,
                      int64_t n_new, const double* new_pos, const double* new_qs,
                      double* s_new, double* out2);
+void ora_ewald_delta_lambda(const ora_box* box, const double* s_same, const double* s_cross, int32_t use_temp,
+                            const double* s_temp, int64_t n, const double* pos, const double* q, double scale_old,
+                            double scale_new, double excl, double* s_new, double* out2);
+void ora_ewald_delta_identity_swap(const ora_box* box, const double* s_same, const double* s_cross,
+                                   int64_t n_old, const double* old_pos, const double* old_qs, int64_t n_new,
+                                   const double* new_pos, const double* new_qs, double excl_new, double excl_old,
+                                   double* s_new, double* out2);
 void ora_rigid_exclusion(const ora_box* box, int64_t molsize, const double* pos,
                          const double* charge, const double* scale_coul,
                          double* intra, double* self);

@@ -103,6 +103,10 @@ def lib():
         L.ora_ewald_total.argtypes = [P(OraBox), P(OraAtoms), _i64p, _dp, _dp, _dp]
         L.ora_ewald_delta.argtypes = [P(OraBox), _dp, _dp, C.c_int32, _dp, C.c_int64, _dp, _dp,
                                       C.c_int64, _dp, _dp, _dp, _dp]
+        L.ora_ewald_delta_lambda.argtypes = [P(OraBox), _dp, _dp, C.c_int32, _dp, C.c_int64, _dp, _dp, C.c_double,
+                                             C.c_double, C.c_double, _dp, _dp]
+        L.ora_ewald_delta_identity_swap.argtypes = [P(OraBox), _dp, _dp, C.c_int64, _dp, _dp, C.c_int64, _dp, _dp,
+                                                    C.c_double, C.c_double, _dp, _dp]
         L.ora_rigid_exclusion.argtypes = [P(OraBox), C.c_int64, _dp, _dp, _dp, _dp, _dp]
         L.ora_philox4x32_10.argtypes = [P(C.c_uint32), P(C.c_uint32), P(C.c_uint32)]
         L.ora_draw.argtypes = [C.c_uint64, C.c_uint32, C.c_uint64, C.c_uint32, P(C.c_uint32)]
@@ -230,6 +234,32 @@ class OracleSystem:
         lib().ora_ewald_delta(C.byref(self.box), _d(s_same), _d(s_cross), 0, _d(s_same),
                               len(old_qs), _d(old_pos), _d(old_qs), len(new_qs), _d(new_pos), _d(new_qs),
                               _d(s_new), _d(out))
+        return out, s_new
+
+    def ewald_delta_lambda(self, s_same, s_cross, pos, charge, scale_old, scale_new, excl, s_temp=None):
+        """GPU_EwaldDifference_LambdaChange: (out2 with exclusion and the doubled cross term, S staged)."""
+        nv = self.nvec()
+        pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1)
+        q = np.ascontiguousarray(charge, dtype=np.float64)
+        st = np.ascontiguousarray(s_temp if s_temp is not None else s_same, dtype=np.float64)
+        s_new = np.zeros(2 * nv)
+        out = np.zeros(2)
+        lib().ora_ewald_delta_lambda(C.byref(self.box), _d(s_same), _d(s_cross), int(s_temp is not None), _d(st),
+                                     len(q), _d(pos), _d(q), scale_old, scale_new, excl, _d(s_new), _d(out))
+        return out, s_new
+
+    def ewald_delta_identity_swap(self, s_same, s_cross, old_pos, old_qs, new_pos, new_qs, excl_new, excl_old):
+        """GPU_EwaldDifference_IdentitySwap: (out2, S staged)."""
+        nv = self.nvec()
+        old_pos = np.ascontiguousarray(old_pos, dtype=np.float64).reshape(-1)
+        new_pos = np.ascontiguousarray(new_pos, dtype=np.float64).reshape(-1)
+        old_qs = np.ascontiguousarray(old_qs, dtype=np.float64)
+        new_qs = np.ascontiguousarray(new_qs, dtype=np.float64)
+        s_new = np.zeros(2 * nv)
+        out = np.zeros(2)
+        lib().ora_ewald_delta_identity_swap(C.byref(self.box), _d(s_same), _d(s_cross), len(old_qs), _d(old_pos),
+                                            _d(old_qs), len(new_qs), _d(new_pos), _d(new_qs), excl_new, excl_old,
+                                            _d(s_new), _d(out))
         return out, s_new
 
     def rigid_exclusion(self, pos, charge, scale_coul):

@@ -90,3 +90,35 @@ def test_write_and_remove_molecule(grx_lib):
         box.write_molecule(1, 5, new, tm["charge"], tm["type"])   # beyond the count
     with pytest.raises(grx_lib.GrxError):
         box.remove_molecule(1, 3)
+
+
+def test_host_layer_cbcf_lambda_change(grx_lib, tmp_path):
+    """CBCF_LambdaChange (mc_cbcfc.h:20-124) through the host layer: molecule 0 goes
+    1 -> 0.4 (lambda change), then 0.4 -> 0.1 as a CB/CFC deletion's second step whose
+    Fourier part starts from the staged vector; pair and Fourier parts against the
+    oracle (FP64, 1e-10 relative)."""
+    import ctypes
+    s = co2_system(n_co2=4)
+    d = params(grx_lib, pressure_pa=1e6)
+    out = run_driver(str(tmp_path), s, d, "lambda", 0)
+    nfw = s["comp_start"][1]
+    S = O.OracleSystem(s)
+    _, s_fw, s_ads = S.ewald_total([nfw, 3])
+    oi, os_ = S.rigid_exclusion(s["templates"][1]["pos"], s["templates"][1]["charge"], np.ones(3))
+    pos, q, ty = s["pos"][nfw:nfw + 3], s["charge"][nfw:nfw + 3], s["type"][nfw:nfw + 3]
+    staged = None
+    for k, (lo, ln) in enumerate(((1.0, 0.4), (0.4, 0.1))):
+        row = out["lambda"][k]
+        assert row[0] == 1.0
+        keep = [np.ascontiguousarray(pos.reshape(-1)), np.full(3, lo), np.ascontiguousarray(q), np.full(3, ln),
+                np.ascontiguousarray(ty, dtype=np.int64)]
+        to = O.OraTrials(1, 3, O._d(keep[0]), O._d(keep[1]), O._d(keep[2]), O._d(keep[1]), O._i(keep[4]), 0)
+        tn = O.OraTrials(1, 3, O._d(keep[0]), O._d(keep[3]), O._d(keep[2]), O._d(keep[3]), O._i(keep[4]), 0)
+        ref = np.zeros(6)
+        rf = np.zeros(1, dtype=np.uint8)
+        O.lib().ora_single_body(ctypes.byref(S.box), ctypes.byref(S.ff), ctypes.byref(S.atoms), ctypes.byref(to),
+                                ctypes.byref(tn), 1, 1, 1, O._d(ref), rf.ctypes.data_as(O._u8p))
+        got_pair = np.array(row[1:5])
+        assert np.all(np.abs(got_pair - ref[2:6]) <= 1e-10 * np.maximum(np.abs(ref[2:6]), 1.0))
+        ew, staged = S.ewald_delta_lambda(s_ads, s_fw, pos, q, lo, ln, oi + os_, s_temp=staged)
+        assert abs(row[5] - ew[0]) <= 1e-10 * max(abs(ew[0]), 1.0) and abs(row[6] - ew[1]) <= 1e-10 * max(abs(ew[1]), 1.0)
