@@ -166,11 +166,14 @@ __global__ void __launch_bounds__(GRX_THREADS) big_excl_kernel(BoxDev b, CompRan
 
 // Total VDW + real Coulomb over ordered pairs with factor 0.5 (VDWReal_Total_CPU,
 // VDW_Coulomb.cu:34-226; device form Total_VDW_Coulomb_Energy :1580-1665).
-// part per block: hh_v hh_r hg_v hg_r gg_v gg_r.
+// part per block: hh_v hh_r hg_v hg_r gg_v gg_r, then per block an overlap flag (a pair
+// with an adsorbate atom above the overlap criterion or closer than 0.1 A,
+// VDWCoulEnergy_Total :1385-1386).
 __global__ void __launch_bounds__(GRX_THREADS) vdw_real_total_kernel(BoxDev b, CompRanges r, double* part) {
   __shared__ double sbuf[32];
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   double e[6] = {0, 0, 0, 0, 0, 0};
+  int ovl = 0;
   if (j < r.n) {
     int li;
     const int ci = comp_of(r, j, li);
@@ -191,7 +194,11 @@ __global__ void __launch_bounds__(GRX_THREADS) vdw_real_total_kernel(BoxDev b, C
         double x = p.x - q.x, y = p.y - q.y, z = p.z - q.z;
         pbc64(b, x, y, z);
         const double rr = x * x + y * y + z * z;
-        if (rr < b.cut_vdw2) e[2 * it] += 0.5 * vdw64(b, mi.x * b.ntypes + mj.x, rr, si * atom_scale(b, jj));
+        if (rr < b.cut_vdw2) {
+          const double ev = vdw64(b, mi.x * b.ntypes + mj.x, rr, si * atom_scale(b, jj));
+          e[2 * it] += 0.5 * ev;
+          if (it > 0 && (ev > b.overlap || rr < 0.01)) ovl = 1;
+        }
         if (!b.no_charges && rr < b.cut_coul2) e[2 * it + 1] += 0.5 * coul64(b, p.w * q.w, rr);
       }
     }
@@ -200,6 +207,8 @@ __global__ void __launch_bounds__(GRX_THREADS) vdw_real_total_kernel(BoxDev b, C
     const double v = block_sum(e[k], sbuf);
     if (threadIdx.x == 0) part[6 * blockIdx.x + k] = v;
   }
+  ovl = __syncthreads_or(ovl);
+  if (threadIdx.x == 0) part[6 * gridDim.x + blockIdx.x] = ovl ? 1.0 : 0.0;
 }
 
 // Fourier delta of one move (Fourier_Ewald_Diff, Ewald_Energy_Functions.h:280-397):
@@ -381,17 +390,19 @@ grx_status grx_ewald_total(grx_box* b, double* out8) {
   return GRX_OK;
 }
 
-grx_status grx_total_energy(grx_box* b, grx_energy* out) {
+grx_status grx_total_energy(grx_box* b, grx_energy* out) { return grx_total_energy_overlap(b, out, nullptr); }
+
+grx_status grx_total_energy_overlap(grx_box* b, grx_energy* out, uint8_t* overlap) {
   GRX_REQUIRE(b && out, "grx_total_energy: null argument");
   double ew[8];
   grx_status st = grx_ewald_total(b, ew);
   if (st) return st;
   CompRanges r = ranges(b);
   const int nblk = std::max((r.n + GRX_THREADS - 1) / GRX_THREADS, 1);
-  st = ensure_scratch(b, 6 * (size_t)nblk * sizeof(double));
+  st = ensure_scratch(b, 7 * (size_t)nblk * sizeof(double));
   if (st) return st;
   double* part = b->scratch;
-  std::vector<double> parts(6 * (size_t)nblk, 0.0);
+  std::vector<double> parts(7 * (size_t)nblk, 0.0);
   if (r.n > 0) {
     vdw_real_total_kernel<<<nblk, GRX_THREADS, 0, b->stream>>>(b->dev, r, part);
     count_launch();
@@ -402,6 +413,11 @@ grx_status grx_total_energy(grx_box* b, grx_energy* out) {
   double e[6] = {0, 0, 0, 0, 0, 0};
   for (int k = 0; k < nblk; ++k)
     for (int q = 0; q < 6; ++q) e[q] += parts[6 * k + q];
+  if (overlap) {
+    *overlap = 0;
+    for (int k = 0; k < nblk; ++k)
+      if (parts[6 * (size_t)nblk + k] != 0.0) *overlap = 1;
+  }
   out->hh_vdw = e[0]; out->hh_real = e[1];
   out->hg_vdw = e[2]; out->hg_real = e[3];
   out->gg_vdw = e[4]; out->gg_real = e[5];

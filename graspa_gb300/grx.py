@@ -133,7 +133,7 @@ EXPORTS = [
     "grx_box_set_stream", "grx_box_set_component", "grx_box_get_component_size", "grx_box_get_positions",
     "grx_box_get_exclusion", "grx_trial_energies", "grx_single_body_energy", "grx_ewald_sizes",
     "grx_ewald_total", "grx_ewald_set_structure_factors", "grx_ewald_get_structure_factors",
-    "grx_ewald_delta", "grx_ewald_delta_lambda", "grx_ewald_delta_identity_swap", "grx_ewald_commit", "grx_total_energy", "grx_cbmc_select",
+    "grx_total_energy_overlap", "grx_ewald_delta", "grx_ewald_delta_lambda", "grx_ewald_delta_identity_swap", "grx_ewald_commit", "grx_total_energy", "grx_cbmc_select",
     "grx_widom_insertions", "grx_widom_insertions_async", "grx_launch_count", "grx_probe_fp32_fma", "grx_trial_energies_noalloc", "grx_gcmc_run",
     "grx_box_write_molecule", "grx_box_remove_molecule", "grx_gcmc_batch_create", "grx_gcmc_batch_destroy",
     "grx_gcmc_batch_set_step", "grx_gcmc_batch_launch", "grx_gcmc_batch_run_graph", "grx_gcmc_batch_stats",
@@ -187,6 +187,7 @@ def load(path=LIB_PATH):
                                                 C.c_size_t, _dp]
     L.grx_ewald_commit.argtypes = [C.c_void_p, C.c_int32]
     L.grx_total_energy.argtypes = [C.c_void_p, P(Energy)]
+    L.grx_total_energy_overlap.argtypes = [C.c_void_p, P(Energy), _u8p]
     L.grx_cbmc_select.argtypes = [_dp, C.c_int32, C.c_uint64, C.c_uint32, C.c_uint64, C.c_int32,
                                   P(C.c_int32), _dp]
     L.grx_widom_insertions.argtypes = [C.c_void_p, P(WidomDesc), C.c_uint64, C.c_size_t, C.c_int32, C.c_void_p]
@@ -477,8 +478,13 @@ class Box:
         check(self.L.grx_box_get_exclusion(self.h, comp, C.byref(a), C.byref(b)), "exclusion")
         return a.value, b.value
 
-    def total_energy(self):
+    def total_energy(self, with_overlap=False):
         e = Energy()
+        if with_overlap:
+            f = np.zeros(1, dtype=np.uint8)
+            check(self.L.grx_total_energy_overlap(self.h, C.byref(e), f.ctypes.data_as(_u8p)),
+                  "grx_total_energy_overlap")
+            return {n: getattr(e, n) for n, _ in Energy._fields_}, int(f[0])
         check(self.L.grx_total_energy(self.h, C.byref(e)), "grx_total_energy")
         return {n: getattr(e, n) for n, _ in Energy._fields_}
 

@@ -5,6 +5,8 @@
 //                    call (CBMC_PairwiseInteractions, GPU_EwaldDifference_General, ...)
 //   device <nsteps>  runs the same moves with RunMoves_Device (one grx_gcmc_run)
 //   widom  <n>       runs n InsertionMove::WidomMove calls and the Widom statistics
+//   volume <n>       runs n NPT VolumeMove calls (trial volume, trial energy, acceptance)
+//   lambda 0         two CB/CFC lambda steps of molecule 0 (CBCF_LambdaChange)
 // and prints the move statistics, the accepted-energy sum and the drift check,
 // then the adsorbate positions, as plain text.
 #include <cstdio>
@@ -113,7 +115,7 @@ void read_system(const char* path, Variables& V, std::vector<size_t>& n_stored, 
 
 int main(int argc, char** argv) {
   if (argc < 4) {
-    std::fprintf(stderr, "usage: %s <system file> host|device|widom <nsteps>\n", argv[0]);
+    std::fprintf(stderr, "usage: %s <system file> host|device|widom|volume|lambda <nsteps>\n", argv[0]);
     return 2;
   }
   try {
@@ -138,6 +140,24 @@ int main(int argc, char** argv) {
       }
       std::printf("widom_average_rosenbluth %.17g\n", WidomAverageRosenbluth(C, comp));
       std::printf("widom_mu_ex_K %.17g\n", WidomChemicalPotential(C, comp));
+    } else if (mode == "volume") {
+      // NPT volume moves of the box (max change of ln V 0.05): per move the trial volume,
+      // the trial box's FP64 total, its overlap flag, the energy before the move, acceptance
+      C.VolumeMoveMaxChange = 0.05;
+      for (long long k = 0; k < nsteps; ++k) {
+        const double e_before = Total_Energy(V.Sims[0]).total();
+        const size_t acc0 = C.VolumeMoveAccepted;
+        VolumeMove(V, 0);
+        std::printf("volume %lld %d %.17g %.17g %d %.17g\n", k, C.VolumeMoveAccepted > acc0 ? 1 : 0,
+                    C.VolumeMoveLastV, C.VolumeMoveLastE.total(), C.VolumeMoveLastOverlap ? 1 : 0, e_before);
+      }
+      const MoveEnergy e1 = Total_Energy(V.Sims[0]);
+      std::printf("energy_sum %.17g\n", C.deltaE.total());
+      std::printf("drift %.17g\n", (e1.total() - e0.total()) - C.deltaE.total());
+      std::printf("final_volume %.17g\n", V.Sims[0].Box.Volume);
+      const Atoms& A = V.Sims[0].d_a[comp];
+      std::printf("positions %zu\n", A.size);
+      for (size_t i = 0; i < A.size; ++i) std::printf("%.17g %.17g %.17g\n", A.pos[i].x, A.pos[i].y, A.pos[i].z);
     } else if (mode == "lambda") {
       // CB/CFC lambda steps of molecule 0: 1 -> 0.4 as a lambda change, the caller's update
       // of the molecule's scales, then 0.4 -> 0.1 as the second step of a CB/CFC deletion

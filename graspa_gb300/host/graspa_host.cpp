@@ -97,11 +97,10 @@ static void trial_buffers(Simulations& Sims) {
 }
 
 // ------------------------------------------------------------------ set-up
-void Setup_Box(Variables& Vars, size_t systemId, const std::vector<size_t>& n_stored) {
-  Simulations& Sims = Vars.Sims[systemId];
-  Components& SC = Vars.SystemComponents[systemId];
-  ForceField& FF = Vars.device_FF;
-  Boxsize& B = Sims.Box;
+// A device box of geometry B holding `atoms` (host arrays per component, n_stored[c] atoms
+// stored), with its structure factors computed (fxn_main.h:46-113 / main.cpp:243-300).
+static grx_box* create_box(const Boxsize& B, const ForceField& FF, const Components& SC, const std::vector<Atoms>& atoms,
+                           const std::vector<size_t>& n_stored) {
   grx_box_desc d{};
   for (int k = 0; k < 9; ++k) {
     d.geometry.cell[k] = B.Cell[k];
@@ -134,12 +133,10 @@ void Setup_Box(Variables& Vars, size_t systemId, const std::vector<size_t>& n_st
     d.capacity[c] = SC.Allocate_size[c];
     d.molsize[c] = SC.Moleculesize[c];
   }
-  check(grx_box_create(&d, &B.handle), "grx_box_create");
-  SC.ExclusionIntra.assign(SC.NComponents.x, 0.0);
-  SC.ExclusionAtom.assign(SC.NComponents.x, 0.0);
-  SC.hasPartialCharge.assign(SC.NComponents.x, false);
+  grx_box* box = nullptr;
+  check(grx_box_create(&d, &box), "grx_box_create");
   for (int c = 0; c < SC.NComponents.x; ++c) {
-    Atoms& A = Sims.d_a[c];
+    const Atoms& A = atoms[c];
     grx_atoms ga{};
     ga.pos = reinterpret_cast<const double*>(A.pos);
     ga.scale = A.scale;
@@ -149,14 +146,38 @@ void Setup_Box(Variables& Vars, size_t systemId, const std::vector<size_t>& n_st
     ga.molid = A.MolID;
     ga.size = A.size;
     ga.n_stored = std::max(A.size, n_stored[c]);
-    check(grx_box_set_component(B.handle, c, &ga, c >= SC.NComponents.y && SC.rigid[c]), "grx_box_set_component");
+    const grx_status st = grx_box_set_component(box, c, &ga, c >= SC.NComponents.y && SC.rigid[c]);
+    if (st) {
+      grx_box_destroy(box);
+      check(st, "grx_box_set_component");
+    }
+  }
+  double out8[8];
+  const grx_status st = grx_ewald_total(box, out8);
+  if (st) {
+    grx_box_destroy(box);
+    check(st, "grx_ewald_total");
+  }
+  return box;
+}
+
+void Setup_Box(Variables& Vars, size_t systemId, const std::vector<size_t>& n_stored) {
+  Simulations& Sims = Vars.Sims[systemId];
+  Components& SC = Vars.SystemComponents[systemId];
+  Boxsize& B = Sims.Box;
+  SC.StoredAtoms.assign(SC.NComponents.x, 0);
+  for (int c = 0; c < SC.NComponents.x; ++c) SC.StoredAtoms[c] = std::max(Sims.d_a[c].size, n_stored[c]);
+  B.handle = create_box(B, Vars.device_FF, SC, Sims.d_a, SC.StoredAtoms);
+  SC.ExclusionIntra.assign(SC.NComponents.x, 0.0);
+  SC.ExclusionAtom.assign(SC.NComponents.x, 0.0);
+  SC.hasPartialCharge.assign(SC.NComponents.x, false);
+  for (int c = 0; c < SC.NComponents.x; ++c) {
+    const Atoms& A = Sims.d_a[c];
     check(grx_box_get_exclusion(B.handle, c, &SC.ExclusionIntra[c], &SC.ExclusionAtom[c]), "grx_box_get_exclusion");
-    for (size_t i = 0; i < ga.n_stored; ++i)
+    for (size_t i = 0; i < SC.StoredAtoms[c]; ++i)
       if (A.charge[i] != 0.0) SC.hasPartialCharge[c] = true;
     if (c >= SC.NComponents.y) SC.NumberOfMolecule_for_Component[c] = A.size / SC.Moleculesize[c];
   }
-  double out8[8];
-  check(grx_ewald_total(B.handle, out8), "grx_ewald_total");
   SC.Beta = SC.Beta > 0 ? SC.Beta : 1.0 / (1.380649e-23 / (1.6605402e-27 * 1e-20 / 1e-24) * SC.Temperature);
   trial_buffers(Sims);
 }
@@ -303,6 +324,219 @@ MoveEnergy Total_Energy(Simulations& Sims) {
   m.GGVDW = e.gg_vdw; m.GGReal = e.gg_real;
   m.HHEwaldE = e.hh_ewald; m.HGEwaldE = e.hg_ewald; m.GGEwaldE = e.gg_ewald;
   return m;
+}
+
+// ------------------------------------------------------------------ volume moves
+// Single-image rounding of PBC (maths.cuh:427-450): cast of x +- 0.5, half away from zero.
+static double round_away(double x) { return (double)(long long)(x + (x >= 0 ? 0.5 : -0.5)); }
+
+static void pbc_host(const Boxsize& B, double3& v) {
+  if (B.Cubic) {
+    v.x -= round_away(v.x * B.InverseCell[0]) * B.Cell[0];
+    v.y -= round_away(v.y * B.InverseCell[4]) * B.Cell[4];
+    v.z -= round_away(v.z * B.InverseCell[8]) * B.Cell[8];
+    return;
+  }
+  const double* I = B.InverseCell;
+  const double* C = B.Cell;
+  double s[3] = {I[0] * v.x + I[3] * v.y + I[6] * v.z, I[1] * v.x + I[4] * v.y + I[7] * v.z,
+                 I[2] * v.x + I[5] * v.y + I[8] * v.z};
+  for (double& x : s) x -= round_away(x);
+  v = double3{C[0] * s[0] + C[3] * s[1] + C[6] * s[2], C[1] * s[0] + C[4] * s[1] + C[7] * s[2],
+              C[2] * s[0] + C[5] * s[1] + C[8] * s[2]};
+}
+
+// The box geometry with every length scaled by s (ScalePositions :71-84): kmax from the
+// precision factor tol1, or, with explicit k vectors (tol1 = 0), the same kmax and the
+// LAMMPS reciprocal cutoff of the scaled cell (read_data.cpp:664-687).
+static Boxsize scaled_geometry(const Boxsize& B, double s, double newV, bool charges) {
+  Boxsize T = B;
+  T.handle = nullptr;
+  for (int k = 0; k < 9; ++k) {
+    T.Cell[k] *= s;
+    T.InverseCell[k] /= s;
+  }
+  T.Volume = newV;
+  if (charges) {
+    const double pi = 3.14159265358979323846;
+    if (B.tol1 > 0.0) {
+      T.kmax = int3{(int)std::round(0.25 + T.Cell[0] * T.Alpha * T.tol1 / pi),
+                    (int)std::round(0.25 + T.Cell[4] * T.Alpha * T.tol1 / pi),
+                    (int)std::round(0.25 + T.Cell[8] * T.Alpha * T.tol1 / pi)};
+      T.ReciprocalCutOff = std::pow(1.05 * (double)std::max(T.kmax.x, std::max(T.kmax.y, T.kmax.z)), 2);
+    } else {
+      const double kvx = T.kmax.x * (2 * pi / T.Cell[0]), kvy = T.kmax.y * (2 * pi / T.Cell[4]),
+                   kvz = T.kmax.z * (2 * pi / T.Cell[8]);
+      T.ReciprocalCutOff = std::max(kvx * kvx, std::max(kvy * kvy, kvz * kvz)) * 1.00001;
+    }
+  }
+  return T;
+}
+
+// One box at a scaled volume: its geometry, the scaled atoms, the device box and its totals.
+struct ScaledBox {
+  Boxsize Box;
+  std::vector<HostAtoms> host;
+  std::vector<Atoms> atoms;
+  MoveEnergy E;
+  bool overlap = false;
+};
+
+// ScalePositions / ScaleCopyPositions (mc_box.h:19-86): adsorbate molecules only (the
+// framework is not scaled); the first bead moves to s * its position, the other atoms keep
+// their minimum-image offsets from it. Then the FP64 totals of the scaled box.
+static void build_scaled(Variables& Vars, size_t systemId, double s, double newV, ScaledBox& out) {
+  Simulations& Sims = Vars.Sims[systemId];
+  Components& SC = Vars.SystemComponents[systemId];
+  const ForceField& FF = Vars.device_FF;
+  for (size_t c = 0; c < SC.TailCorrectionInsert.size(); ++c)
+    if (SC.TailCorrectionInsert[c] != 0.0)
+      throw std::runtime_error("volume moves: tail corrections are not supported on this path");
+  out.Box = scaled_geometry(Sims.Box, s, newV, !FF.noCharges);
+  const int nc = SC.NComponents.x;
+  out.host.assign(nc, HostAtoms());
+  out.atoms.resize(nc);
+  for (int c = 0; c < nc; ++c) {
+    const Atoms& A = Sims.d_a[c];
+    HostAtoms& H = out.host[c];
+    const size_t n = SC.StoredAtoms[c];
+    H.allocate(std::max(n, (size_t)1));
+    for (size_t i = 0; i < n; ++i) {
+      H.pos[i] = A.pos[i];
+      H.scale[i] = A.scale[i];
+      H.charge[i] = A.charge[i];
+      H.scaleCoul[i] = A.scaleCoul[i];
+      H.Type[i] = A.Type[i];
+      H.MolID[i] = A.MolID[i];
+    }
+    if (c >= SC.NComponents.y) {
+      const size_t ms = SC.Moleculesize[c];
+      for (size_t m = 0; m + 1 <= A.size / ms; ++m) {
+        const double3 p0 = A.pos[m * ms];
+        const double3 c0{p0.x * s, p0.y * s, p0.z * s};
+        for (size_t a = 0; a < ms; ++a) {
+          double3 v{A.pos[m * ms + a].x - p0.x, A.pos[m * ms + a].y - p0.y, A.pos[m * ms + a].z - p0.z};
+          pbc_host(Sims.Box, v);
+          H.pos[m * ms + a] = double3{c0.x + v.x, c0.y + v.y, c0.z + v.z};
+        }
+      }
+    }
+    out.atoms[c] = H.view(A.Molsize, A.size);
+  }
+  out.Box.handle = create_box(out.Box, FF, SC, out.atoms, SC.StoredAtoms);
+  grx_energy e{};
+  uint8_t ovl = 0;
+  const grx_status st = grx_total_energy_overlap(out.Box.handle, &e, &ovl);
+  if (st) {
+    grx_box_destroy(out.Box.handle);
+    check(st, "grx_total_energy_overlap");
+  }
+  out.overlap = ovl != 0;
+  out.E.HHVDW = e.hh_vdw; out.E.HHReal = e.hh_real; out.E.HGVDW = e.hg_vdw; out.E.HGReal = e.hg_real;
+  out.E.GGVDW = e.gg_vdw; out.E.GGReal = e.gg_real;
+  out.E.HHEwaldE = e.hh_ewald; out.E.HGEwaldE = e.hg_ewald; out.E.GGEwaldE = e.gg_ewald;
+}
+
+// Make a scaled box current: its device box replaces the old one, its atoms the mirror's.
+static void adopt_scaled(Variables& Vars, size_t systemId, ScaledBox& t) {
+  Simulations& Sims = Vars.Sims[systemId];
+  Components& SC = Vars.SystemComponents[systemId];
+  grx_box_destroy(Sims.Box.handle);
+  Sims.Box = t.Box;
+  t.Box.handle = nullptr;
+  for (int c = SC.NComponents.y; c < SC.NComponents.x; ++c)
+    for (size_t i = 0; i < SC.StoredAtoms[c]; ++i) Sims.d_a[c].pos[i] = t.host[c].pos[i];
+}
+
+// Adsorbate molecules of a box (Get_TotalNumberOfMolecule_In_Box, mc_box.h:177-189; no
+// fractional molecules on this path).
+static double molecules_in_box(const Components& SC) {
+  double n = 0.0;
+  for (int c = SC.NComponents.y; c < SC.NComponents.x; ++c) n += (double)SC.NumberOfMolecule_for_Component[c];
+  return n;
+}
+
+// VolumeMove (mc_box.h:191-291). The current energy is the box's FP64 total (the reference
+// uses its running sum CreateMol_Energy + deltaE, equal to it within the drift).
+void VolumeMove(Variables& Vars, size_t systemId) {
+  Components& SC = Vars.SystemComponents[systemId];
+  Simulations& Sims = Vars.Sims[systemId];
+  SC.VolumeMoveAttempts++;
+  uint32_t w[4];
+  grx_draw(Vars.Random.Seed, Vars.Random.Stream, SC.Step, GRX_SLOT_VOLUME, w);
+  const double OldV = Sims.Box.Volume;
+  const double newV = std::exp(std::log(OldV) + SC.VolumeMoveMaxChange * 2.0 * (grx_u01(w[0]) - 0.5));
+  const double scale = std::cbrt(newV / OldV);
+  ScaledBox t;
+  build_scaled(Vars, systemId, scale, newV, t);
+  SC.VolumeMoveLastV = newV;
+  SC.VolumeMoveLastE = t.E;
+  SC.VolumeMoveLastOverlap = t.overlap;
+  bool accept = false;
+  MoveEnergy dE;
+  if (!t.overlap) {
+    const MoveEnergy cur = Total_Energy(Sims);
+    dE = t.E;
+    dE -= cur;
+    const double pacc = std::exp((molecules_in_box(SC) + 1.0) * std::log(newV / OldV) -
+                                 (dE.total() + SC.Pressure * (newV - OldV)) * SC.Beta);
+    accept = grx_u01(w[1]) < pacc;
+  }
+  if (accept) {
+    adopt_scaled(Vars, systemId, t);
+    SC.VolumeMoveAccepted++;
+    SC.deltaE += dE;
+  } else {
+    grx_box_destroy(t.Box.handle);
+  }
+  SC.Step++;
+}
+
+// NVTGibbsMove (mc_box.h:319-430): volume passes between boxes 0 and 1 at fixed total; the
+// random numbers come from box 0's stream (box choice, ln(VA/VB) change, acceptance).
+void NVTGibbsMove(Variables& Vars, Gibbs& G) {
+  if (Vars.SystemComponents.size() < 2) throw std::runtime_error("NVTGibbsMove: two boxes needed");
+  Components& C0 = Vars.SystemComponents[0];
+  uint32_t w[4];
+  grx_draw(Vars.Random.Seed, Vars.Random.Stream, C0.Step, GRX_SLOT_VOLUME, w);
+  const size_t sel = grx_u01(w[2]) > 0.5 ? 1 : 0, oth = 1 - sel;
+  G.GibbsBoxStats[0] += 1.0;
+  const double VA = Vars.Sims[sel].Box.Volume, VB = Vars.Sims[oth].Box.Volume, TotalV = VA + VB;
+  const double expdV = std::exp(std::log(VA / VB) + G.MaxGibbsBoxChange * 2.0 * (grx_u01(w[0]) - 0.5));
+  const double newVA = expdV * TotalV / (1.0 + expdV), newVB = TotalV - newVA;
+  const ForceField& FF = Vars.device_FF;
+  const double la = std::pow(std::cbrt(newVA), 2), lb = std::pow(std::cbrt(newVB), 2);
+  for (size_t b : {(size_t)0, (size_t)1}) Vars.SystemComponents[b].Step++;
+  if (la < 4.0 * FF.CutOffVDW || la < 4.0 * FF.CutOffCoul || lb < 4.0 * FF.CutOffVDW || lb < 4.0 * FF.CutOffCoul)
+    return;  // a box would be narrower than twice the cutoff
+  const double newV[2] = {sel == 0 ? newVA : newVB, sel == 0 ? newVB : newVA};
+  const double oldV[2] = {sel == 0 ? VA : VB, sel == 0 ? VB : VA};
+  ScaledBox t[2];
+  bool overlap = false;
+  MoveEnergy dE[2];
+  for (size_t b = 0; b < 2; ++b) {
+    build_scaled(Vars, b, std::cbrt(newV[b] / oldV[b]), newV[b], t[b]);
+    overlap = overlap || t[b].overlap;
+    dE[b] = t[b].E;
+    dE[b] -= Total_Energy(Vars.Sims[b]);
+  }
+  bool accept = false;
+  if (!overlap) {
+    const double beta = Vars.SystemComponents[sel].Beta;
+    const double pacc = std::exp(-beta * (dE[0].total() + dE[1].total()) +
+                                 (molecules_in_box(Vars.SystemComponents[sel]) + 1.0) * std::log(newV[sel] / oldV[sel]) +
+                                 (molecules_in_box(Vars.SystemComponents[oth]) + 1.0) * std::log(newV[oth] / oldV[oth]));
+    accept = grx_u01(w[1]) < pacc;
+  }
+  for (size_t b = 0; b < 2; ++b) {
+    if (accept) {
+      adopt_scaled(Vars, b, t[b]);
+      Vars.SystemComponents[b].deltaE += dE[b];
+    } else {
+      grx_box_destroy(t[b].Box.handle);
+    }
+  }
+  if (accept) G.GibbsBoxStats[1] += 1.0;
 }
 
 double GetPrefactor(Components& SC, Simulations& Sims, size_t comp, int MoveType) {

@@ -102,6 +102,7 @@ struct Boxsize {
   double Alpha = 0.265;
   bool Cubic = true;
   bool UseLAMMPSEwald = true;
+  double tol1 = 0.0;          // Ewald precision factor of the automatic set-up (0: explicit kmax)
   int3 kmax;
   grx_box* handle = nullptr;  // the device box: eik tables and S(k) live here
 };
@@ -167,6 +168,12 @@ struct Components {
   std::vector<double> Rosen;
   std::vector<MoveEnergy> TrialEnergies;
   TempVals TempVal;
+  std::vector<size_t> StoredAtoms;                   // atoms stored per component (templates included)
+  double VolumeMoveMaxChange = 0.0;                  // MaxVolumeChange of ln V
+  size_t VolumeMoveAttempts = 0, VolumeMoveAccepted = 0;
+  double VolumeMoveLastV = 0.0;                      // the last volume trial (reporting):
+  MoveEnergy VolumeMoveLastE;                        //   its volume, FP64 totals and overlap flag
+  bool VolumeMoveLastOverlap = false;
   MoveEnergy deltaE;                                 // running sum of accepted move energies
   uint64_t Step = 0;                                 // Philox move index of the next move
 };
@@ -229,6 +236,17 @@ double2 GPU_EwaldDifference_LambdaChange(Simulations& Sims, ForceField& FF, Comp
 double2 GPU_EwaldDifference_IdentitySwap(Simulations& Sims, ForceField& FF, Components& SystemComponents,
                                          size_t OLDComponent, size_t NEWComponent, size_t UpdateLocation,
                                          const std::vector<double3>& NewPositions);
+// Volume moves (mc_box.h:197-430) on the FP64 totals: the cell and the adsorbate
+// molecules (first bead scaled, the others kept at their minimum-image offsets) are scaled,
+// the totals of the scaled box decide. VolumeMove is the NPT move of one box; NVTGibbsMove
+// exchanges volume between boxes 0 and 1 at fixed total volume.
+struct Gibbs {
+  double MaxGibbsBoxChange = 0.1;
+  double GibbsBoxStats[2] = {0.0, 0.0};  // attempts, accepted
+};
+void VolumeMove(Variables& Vars, size_t systemId);
+void NVTGibbsMove(Variables& Vars, Gibbs& GibbsStatistics);
+
 // Energy of a lambda change of one molecule (mc_cbcfc.h:20-124): pair part over every other
 // atom at fixed positions, Fourier part and tail; SuccessConstruction is false on overlap.
 MoveEnergy CBCF_LambdaChange(Variables& Vars, size_t systemId, size_t SelectedMolInComponent,

@@ -290,6 +290,7 @@ void Setup_Box_Geometry(Boxsize& B, const SimulationInput& in) {
     const double tol = std::sqrt(std::fabs(std::log(p * rc)));
     B.Alpha = std::sqrt(std::fabs(std::log(p * rc * tol))) / rc;
     const double tol1 = std::sqrt(-std::log(p * rc * std::pow(2.0 * tol * B.Alpha, 2)));
+    B.tol1 = tol1;
     B.kmax = int3{(int)std::round(0.25 + x[0] * B.Alpha * tol1 / pi), (int)std::round(0.25 + x[4] * B.Alpha * tol1 / pi),
                   (int)std::round(0.25 + x[8] * B.Alpha * tol1 / pi)};
     B.ReciprocalCutOff = std::pow(1.05 * (double)std::max(B.kmax.x, std::max(B.kmax.y, B.kmax.z)), 2);

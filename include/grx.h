@@ -317,6 +317,10 @@ grx_status grx_ewald_commit(grx_box* box, int32_t component);
 /* FP64 totals for drift checks: Total_VDW_Coulomb_Energy (VDW_Coulomb.cu:1580)
  * + Ewald_TotalEnergy (Ewald_Energy_Functions.h:1272), split as MoveEnergy. */
 grx_status grx_total_energy(grx_box* box, grx_energy* out);
+/* The same totals and the overlap flag of TotalVDWRealCoulomb (VDW_Coulomb.cu:1385-1386):
+ * set when a pair with an adsorbate atom has an LJ energy above the overlap criterion or
+ * r^2 < 0.01 A^2 (the rejection test of VolumeMove, mc_box.h:247-252). */
+grx_status grx_total_energy_overlap(grx_box* box, grx_energy* out, uint8_t* overlap);
 
 /* ---- CBMC --------------------------------------------------------------- */
 /* Rosenbluth selection of SelectTrialPosition (mc_widom.h:14-39) with the

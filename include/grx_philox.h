@@ -18,6 +18,7 @@
  *   GRX_SLOT_RETRACE + o  reinsertion retrace orientation o
  *   GRX_SLOT_MOVE         {molecule pick, move choice, insertion-vs-deletion, acceptance}
  *   GRX_SLOT_DISP         {three displacement / rotation-angle uniforms}
+ *   GRX_SLOT_VOLUME       {volume change, acceptance, Gibbs box choice} of a volume move
  */
 #ifndef GRX_PHILOX_H
 #define GRX_PHILOX_H
@@ -29,6 +30,7 @@
 #define GRX_SLOT_RETRACE 3072u
 #define GRX_SLOT_MOVE 4096u
 #define GRX_SLOT_DISP 4097u
+#define GRX_SLOT_VOLUME 4098u
 
 static inline void grx_philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
   for (int r = 0; r < 10; ++r) {

@@ -357,6 +357,11 @@ def philox(ctr, key):
     return list(o)
 
 
+def u01(w):
+    """Uniform in [0, 1) from one Philox word (grx_u01: w * 2^-32)."""
+    return float(w) * 2.3283064365386963e-10
+
+
 def draw(seed, stream, move, slot):
     o = (C.c_uint32 * 4)()
     lib().ora_draw(seed, stream, move, slot, o)

@@ -122,3 +122,49 @@ def test_host_layer_cbcf_lambda_change(grx_lib, tmp_path):
         assert np.all(np.abs(got_pair - ref[2:6]) <= 1e-10 * np.maximum(np.abs(ref[2:6]), 1.0))
         ew, staged = S.ewald_delta_lambda(s_ads, s_fw, pos, q, lo, ln, oi + os_, s_temp=staged)
         assert abs(row[5] - ew[0]) <= 1e-10 * max(abs(ew[0]), 1.0) and abs(row[6] - ew[1]) <= 1e-10 * max(abs(ew[1]), 1.0)
+
+
+def _round_away(x):
+    return np.where(x >= 0, np.floor(x + 0.5), np.ceil(x - 0.5))
+
+
+def test_host_layer_volume_move(grx_lib, tmp_path):
+    """VolumeMove (mc_box.h:191-291) through the host layer: the first trial's volume is
+    the Philox draw, its FP64 total equals the oracle's totals of the scaled box (cell and
+    adsorbate molecules scaled, first bead by s, the other atoms at their minimum-image
+    offsets; the framework unscaled, as in the reference), and the acceptance follows
+    exp((N+1) ln(V'/V) - beta (dE + P dV)). Over several moves the accepted energies
+    match the recomputed totals (drift)."""
+    s = co2_system(n_co2=10)
+    d = params(grx_lib, pressure_pa=2e7)
+    out = run_driver(str(tmp_path), s, d, "volume", 8)
+    nfw = s["comp_start"][1]
+    cell = np.array(s["cell"], dtype=np.float64).reshape(3, 3)
+    V0 = abs(np.linalg.det(cell))
+    acc, newV, e_trial, overlap, e_before = out["volume"][0]
+    w = O.draw(d.seed, d.stream, 0, 4098)  # GRX_SLOT_VOLUME of move 0
+    V1 = np.exp(np.log(V0) + 0.05 * 2.0 * (O.u01(w[0]) - 0.5))
+    assert abs(newV - V1) <= 1e-12 * V1
+    sc = np.cbrt(V1 / V0)
+    s2 = dict(s)
+    s2["cell"] = list(np.array(s["cell"], dtype=np.float64) * sc)
+    pos = np.array(s["pos"], dtype=np.float64).copy()
+    Lx, Ly, Lz = s["cell"][0], s["cell"][4], s["cell"][8]
+    for m in range(10):
+        a0 = nfw + 3 * m
+        p0 = pos[a0].copy()
+        v = pos[a0:a0 + 3] - p0
+        v -= _round_away(v / np.array([Lx, Ly, Lz])) * np.array([Lx, Ly, Lz])
+        pos[a0:a0 + 3] = p0 * sc + v
+    s2["pos"] = pos
+    S2 = O.OracleSystem(s2)
+    vr = S2.vdw_real_total()
+    ew, _, _ = S2.ewald_total([nfw, 3])
+    total = vr.sum() + (ew[1] - ew[4] + ew[6]) + ew[2] + (ew[0] + ew[1] - ew[3] + ew[5])
+    assert abs(e_trial - total) <= 1e-9 * abs(total), (e_trial, total)
+    assert overlap == 0.0
+    lp = 11.0 * np.log(V1 / V0) - d.beta * (e_trial - e_before + d.pressure * (V1 - V0))
+    pacc = np.exp(min(lp, 700.0))
+    assert acc == float(O.u01(w[1]) < pacc)
+    assert sum(r[0] for r in out["volume"]) >= 1  # some moves accepted at this pressure
+    assert abs(out["drift"]) <= 1e-8 * max(1.0, abs(e_before)) + 1e-6
