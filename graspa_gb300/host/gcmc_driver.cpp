@@ -6,9 +6,11 @@
 //   device <nsteps>  runs the same moves with RunMoves_Device (one grx_gcmc_run)
 //   widom  <n>       runs n InsertionMove::WidomMove calls and the Widom statistics
 //   volume <n>       runs n NPT VolumeMove calls (trial volume, trial energy, acceptance)
+//   gibbs  <n>       runs n NVTGibbsMove calls between the box and an identical copy
 //   lambda 0         two CB/CFC lambda steps of molecule 0 (CBCF_LambdaChange)
 // and prints the move statistics, the accepted-energy sum and the drift check,
 // then the adsorbate positions, as plain text.
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
@@ -125,6 +127,15 @@ int main(int argc, char** argv) {
     read_system(argv[1], V, n_stored, comp);
     const std::string mode = argv[2];
     const long long nsteps = std::atoll(argv[3]);
+    if (mode == "gibbs") {  // a second, identical box (its arrays re-pointed at its own storage)
+      V.Sims.push_back(V.Sims[0]);
+      V.SystemComponents.push_back(V.SystemComponents[0]);
+      V.Widom.push_back(V.Widom[0]);
+      Simulations& S1 = V.Sims[1];
+      for (size_t c = 0; c < S1.host.size(); ++c)
+        S1.d_a[c] = S1.host[c].view(V.SystemComponents[1].Moleculesize[c], V.Sims[0].d_a[c].size);
+      Setup_Box(V, 1, n_stored);
+    }
     Setup_Box(V, 0, n_stored);
     Components& C = V.SystemComponents[0];
     const MoveEnergy e0 = Total_Energy(V.Sims[0]);
@@ -140,6 +151,22 @@ int main(int argc, char** argv) {
       }
       std::printf("widom_average_rosenbluth %.17g\n", WidomAverageRosenbluth(C, comp));
       std::printf("widom_mu_ex_K %.17g\n", WidomChemicalPotential(C, comp));
+    } else if (mode == "gibbs") {
+      // NVT Gibbs volume exchange between box 0 and its copy (max change of ln(VA/VB) 0.1)
+      Gibbs G;
+      G.MaxGibbsBoxChange = 0.1;
+      const MoveEnergy e0b = Total_Energy(V.Sims[1]);
+      for (long long k = 0; k < nsteps; ++k) {
+        NVTGibbsMove(V, G);
+        std::printf("gibbs %lld %.17g %.17g\n", k, V.Sims[0].Box.Volume, V.Sims[1].Box.Volume);
+      }
+      const MoveEnergy e1 = Total_Energy(V.Sims[0]), e1b = Total_Energy(V.Sims[1]);
+      std::printf("gibbs_attempts %.17g\n", G.GibbsBoxStats[0]);
+      std::printf("gibbs_accepted %.17g\n", G.GibbsBoxStats[1]);
+      std::printf("drift %.17g\n", (e1.total() - e0.total()) - C.deltaE.total());
+      std::printf("drift_b %.17g\n", (e1b.total() - e0b.total()) - V.SystemComponents[1].deltaE.total());
+      std::printf("energy_scale %.17g\n", std::fabs(e1.total()) + std::fabs(e1b.total()));
+      Destroy_Box(V, 1);
     } else if (mode == "volume") {
       // NPT volume moves of the box (max change of ln V 0.05): per move the trial volume,
       // the trial box's FP64 total, its overlap flag, the energy before the move, acceptance

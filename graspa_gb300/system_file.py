@@ -91,6 +91,8 @@ def parse_driver_output(text):
             out[k] = [int(x) for x in parts[1:]]
         elif k == "W":
             out["W"].append(float(parts[2]))
+        elif k == "gibbs":  # move, volume of box 0, volume of box 1
+            out.setdefault("gibbs", []).append([float(x) for x in parts[2:]])
         elif k == "volume":  # move, accepted, trial volume, trial total, overlap, total before
             out.setdefault("volume", []).append([float(x) for x in parts[2:]])
         elif k == "lambda":  # step, constructed, HGVDW HGReal GGVDW GGReal GGEwald HGEwald Tail total

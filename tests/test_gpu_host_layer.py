@@ -168,3 +168,18 @@ def test_host_layer_volume_move(grx_lib, tmp_path):
     assert acc == float(O.u01(w[1]) < pacc)
     assert sum(r[0] for r in out["volume"]) >= 1  # some moves accepted at this pressure
     assert abs(out["drift"]) <= 1e-8 * max(1.0, abs(e_before)) + 1e-6
+
+
+def test_host_layer_gibbs_volume_exchange(grx_lib, tmp_path):
+    """NVTGibbsMove (mc_box.h:319-430) between a box and an identical copy: the total
+    volume is conserved, both boxes' accepted energies match their recomputed totals."""
+    s = co2_system(n_co2=10)
+    d = params(grx_lib, pressure_pa=1e6)
+    out = run_driver(str(tmp_path), s, d, "gibbs", 6)
+    cell = np.array(s["cell"], dtype=np.float64).reshape(3, 3)
+    V0 = abs(np.linalg.det(cell))
+    for va, vb in out["gibbs"]:
+        assert abs((va + vb) - 2 * V0) <= 1e-9 * V0
+    assert out["gibbs_attempts"] == 6.0
+    tol = 1e-8 * out["energy_scale"] + 1e-6
+    assert abs(out["drift"]) <= tol and abs(out["drift_b"]) <= tol
