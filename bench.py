@@ -18,7 +18,7 @@ insertion or deletion of CO2).
              descriptors uploaded, statistics read back, host synchronised
   accuracy   energy drift (FP64 recomputed totals vs accepted energies), loading,
              and mixed-vs-FP64 decisions and energies per move
-  widom      the configs[0]-style Widom workload (20,000 CO2 insertions per step)
+  widom      the Widom workload of the same system (20,000 CO2 insertions per step)
   serving    a bounded Poisson job stream through grx_server: jobs/s, p50 / p99
              latency, next to the one-job-at-a-time FP64 form
 Reference arm (--impl reference): the FP64 C++ oracle of the same moves, one chain
@@ -136,7 +136,7 @@ def co2_system():
 
 
 def gcmc_descs(grx, n, seed=42):
-    """configs[1] move set: translation : rotation : insertion : deletion = 1:1:1:1."""
+    """The GCMC move set: translation : rotation : insertion : deletion = 1:1:1:1."""
     return [grx.gcmc_desc(1, ntrials=NTRIALS, norient=NORIENT, p_translation=0.25, p_rotation=0.5,
                           p_reinsertion=0.5, p_swap=1.0, pressure_pa=1e5, seed=seed, stream=k) for k in range(n)]
 
@@ -528,8 +528,8 @@ def run_grx(args):
 
 
 def bench_other(args, grx, torch, stream, flush, which):
-    """configs[2] (64 batched CH4/Xe boxes, triclinic, LJ only, autotuned) or
-    configs[3] (TIP4P-Ew water in the hexagonal framework) as their own lines."""
+    """The batched line (64 CH4/Xe boxes, triclinic, LJ only, autotuned) or the water
+    line (TIP4P-Ew water in the hexagonal framework) as their own JSON lines."""
     from graspa_gb300 import synth
     if which == "batched":
         systems = [synth.ch4_xe_system(k) for k in range(64)]

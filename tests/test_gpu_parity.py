@@ -1,7 +1,7 @@
 """GPU parity: every libgrx entry point against the FP64 oracle on the same inputs.
 
 Tolerances (written per test):
-  FP64   : |dE| <= 1e-12 * max(|E|, 1)          (the benchmark spec: FP64 path within 1e-12)
+  FP64   : |dE| <= 1e-12 * max(|E|, 1)          (the FP64 path's bar)
   MIXED  : beta*|dE| <= 1e-6 and |dE| <= 1e-6 * max(|E|, kT)   (Boltzmann weights
            exp(-beta E) agree to 1e-6 relative; energies smaller than kT are
            measured against kT)
