@@ -313,9 +313,9 @@ def bench_gcmc(args, grx, torch, stream, flush, rank, world, dist):
             e2e.append(dt)
             te_e2e += work_of(st, ms, nfw)[0]
     close_boxes(boxes)
-    desc_bytes = R * 160 + 8
+    h2d, d2h = grx.last_transfer()  # what one grx_gcmc_run copies (the same every step)
     out["e2e"] = {"value": te_e2e * world / sum(e2e), "unit": "trial_energies/s",
-                  "h2d_bytes_per_step": desc_bytes, "d2h_bytes_per_step": R * 136}
+                  "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
     return out
 
 

@@ -31,6 +31,9 @@ grx_status cuda_status(cudaError_t e, const char* what) {
 
 void count_launch(uint64_t n) { g_launches += n; }
 
+static thread_local size_t g_h2d = 0, g_d2h = 0;
+void note_transfer(size_t h2d, size_t d2h) { g_h2d = h2d; g_d2h = d2h; }
+
 int sm_count(grx_box* b) {
   if (!b->num_sms) {
     int v = 0;
@@ -405,6 +408,12 @@ const char* grx_status_string(grx_status s) {
 const char* grx_last_error(void) { return g_err; }
 
 uint64_t grx_launch_count(void) { return g_launches.load(); }
+
+grx_status grx_last_transfer(size_t* h2d, size_t* d2h) {
+  if (h2d) *h2d = g_h2d;
+  if (d2h) *d2h = g_d2h;
+  return GRX_OK;
+}
 
 grx_status grx_device_count(int32_t* n) {
   int v = 0;

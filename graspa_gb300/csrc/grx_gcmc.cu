@@ -443,6 +443,7 @@ struct grx_gcmc_batch {
   int* d_first = nullptr;
   grx_gcmc_stats* d_stats = nullptr;
   uint64_t* d_step = nullptr;
+  int* d_sizes = nullptr;  // molecule counts gathered after a launch
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   int64_t graph_nsteps = 0;
@@ -525,11 +526,15 @@ static grx_status set_smem_one() {
 }
 
 static grx_status set_gcmc_smem() {
+  static bool done[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64 && done[dev]) return GRX_OK;
   grx_status st = GRX_OK;
   for (grx_status r : {set_smem_one<GRX_FP64, 8>(), set_smem_one<GRX_FP64, 12>(), set_smem_one<GRX_FP64, 24>(),
                        set_smem_one<GRX_MIXED, 8>(), set_smem_one<GRX_MIXED, 12>(), set_smem_one<GRX_MIXED, 24>(),
                        set_smem_one<GRX_FP32, 8>(), set_smem_one<GRX_FP32, 12>(), set_smem_one<GRX_FP32, 24>()})
     if (r && !st) st = r;
+  if (!st && dev >= 0 && dev < 64) done[dev] = true;
   return st;
 }
 
@@ -573,11 +578,28 @@ static grx_status enqueue_gcmc(grx_precision prec, int nw, int nboxes, const Box
   return GRX_OK;
 }
 
-static grx_status sync_sizes(grx_box* const* boxes, int nboxes, const grx_gcmc_desc* descs, const int* first) {
+// Molecule counts of every box of a launch, gathered into one buffer.
+__global__ void gather_sizes_kernel(const BoxDev* boxes, int nboxes, int* out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nboxes * GRX_MAX_COMPONENTS) return;
+  const int i = t / GRX_MAX_COMPONENTS, c = t % GRX_MAX_COMPONENTS;
+  out[t] = c < boxes[i].ncomp ? boxes[i].comp_size[c] : 0;
+}
+
+// Refreshes the host copies of the boxes' molecule counts after a launch on `stream`:
+// one gather kernel and one copy (dout: nboxes * GRX_MAX_COMPONENTS ints on the device).
+static grx_status sync_sizes(grx_box* const* boxes, int nboxes, const grx_gcmc_desc* descs, const int* first,
+                             const BoxDev* dboxes, int* dout, cudaStream_t stream) {
+  std::vector<int> h((size_t)nboxes * GRX_MAX_COMPONENTS);
+  gather_sizes_kernel<<<(nboxes * GRX_MAX_COMPONENTS + 255) / 256, 256, 0, stream>>>(dboxes, nboxes, dout);
+  count_launch();
+  GRX_CHECK_CUDA(cudaGetLastError(), "gather sizes");
+  GRX_CHECK_CUDA(cudaMemcpyAsync(h.data(), dout, h.size() * sizeof(int), cudaMemcpyDeviceToHost, stream),
+                 "read sizes");
+  GRX_CHECK_CUDA(cudaStreamSynchronize(stream), "read sizes");
   for (int i = 0; i < nboxes; ++i) {
     grx_box* b = boxes[i];
-    GRX_CHECK_CUDA(cudaMemcpy(b->size, b->d_size, GRX_MAX_COMPONENTS * sizeof(int), cudaMemcpyDeviceToHost),
-                   "read sizes");
+    for (int c = 0; c < GRX_MAX_COMPONENTS; ++c) b->size[c] = h[(size_t)i * GRX_MAX_COMPONENTS + c];
     for (int e = first[i]; e < first[i + 1]; ++e) {
       const int c = descs[e].component;
       b->stored[c] = std::max(b->stored[c], (size_t)b->size[c]);
@@ -604,10 +626,12 @@ extern "C" grx_status grx_gcmc_run(grx_box* const* boxes, int32_t nboxes, const 
   grx_box* b0 = boxes[0];
   auto al = [](size_t n) { return (n + 255) / 256 * 256; };
   const size_t ob = 0, oa = al(nboxes * sizeof(BoxDev)), of = oa + al(ne * sizeof(GcmcArgs)),
-               os = of + al((nboxes + 1) * sizeof(int)), ot = os + al(ne * sizeof(grx_gcmc_stats));
-  st = ensure_scratch(b0, ot + 256);
+               os = of + al((nboxes + 1) * sizeof(int)), ot = os + al(ne * sizeof(grx_gcmc_stats)),
+               oz = ot + 256;
+  st = ensure_scratch(b0, oz + al((size_t)nboxes * GRX_MAX_COMPONENTS * sizeof(int)));
   if (st) return st;
   char* base = (char*)b0->scratch;
+  int* dsizes = (int*)(base + oz);
   BoxDev* dboxes = (BoxDev*)(base + ob);
   GcmcArgs* dargs = (GcmcArgs*)(base + oa);
   int* dfirst = (int*)(base + of);
@@ -632,9 +656,10 @@ extern "C" grx_status grx_gcmc_run(grx_box* const* boxes, int32_t nboxes, const 
   }
   GRX_CHECK_CUDA(cudaMemcpyAsync(stats, dstats, ne * sizeof(grx_gcmc_stats), cudaMemcpyDefault, b0->stream),
                  "read gcmc stats");
-  GRX_CHECK_CUDA(cudaStreamSynchronize(b0->stream), "gcmc run");
-  st = sync_sizes(boxes, nboxes, descs, first.data());
+  st = sync_sizes(boxes, nboxes, descs, first.data(), dboxes, dsizes, b0->stream);
   if (st) return st;
+  note_transfer(nboxes * sizeof(BoxDev) + ne * sizeof(GcmcArgs) + (nboxes + 1) * sizeof(int) + sizeof(uint64_t),
+                ne * sizeof(grx_gcmc_stats) + (size_t)nboxes * GRX_MAX_COMPONENTS * sizeof(int));
   if (nsteps == 0)
     for (int i = 0; i < nboxes; ++i)
       for (int e = first[i]; e < first[i + 1]; ++e)
@@ -662,10 +687,11 @@ extern "C" grx_status grx_gcmc_batch_create(grx_box* const* boxes, int32_t nboxe
   B->stream = boxes[0]->stream;
   auto al = [](size_t n) { return (n + 255) / 256 * 256; };
   const size_t oa = al(nboxes * sizeof(BoxDev)), of = oa + al(B->nentries * sizeof(GcmcArgs)),
-               os = of + al((nboxes + 1) * sizeof(int)), ot = os + al(B->nentries * sizeof(grx_gcmc_stats));
+               os = of + al((nboxes + 1) * sizeof(int)), ot = os + al(B->nentries * sizeof(grx_gcmc_stats)),
+               oz = ot + 256, total = oz + al((size_t)nboxes * GRX_MAX_COMPONENTS * sizeof(int));
   B->arena = boxes[0]->arena;  // a batch of arena boxes lives in the same arena
-  if (B->arena) B->mem = arena_alloc(B->arena, ot + 256);
-  else if (cudaMalloc(&B->mem, ot + 256) != cudaSuccess) B->mem = nullptr;
+  if (B->arena) B->mem = arena_alloc(B->arena, total);
+  else if (cudaMalloc(&B->mem, total) != cudaSuccess) B->mem = nullptr;
   if (!B->mem) {
     cudaGetLastError();
     delete B;
@@ -678,6 +704,7 @@ extern "C" grx_status grx_gcmc_batch_create(grx_box* const* boxes, int32_t nboxe
   B->d_first = (int*)(base + of);
   B->d_stats = (grx_gcmc_stats*)(base + os);
   B->d_step = (uint64_t*)(base + ot);
+  B->d_sizes = (int*)(base + oz);
   const uint64_t zero = 0;
   cudaStream_t s0 = B->stream;
   bool ok =
@@ -777,7 +804,8 @@ extern "C" grx_status grx_gcmc_batch_stats(grx_gcmc_batch* B, grx_gcmc_stats* st
                    "read stats");
   if (next_step)
     GRX_CHECK_CUDA(cudaMemcpy(next_step, B->d_step, sizeof(uint64_t), cudaMemcpyDeviceToHost), "read step");
-  return sync_sizes(B->boxes.data(), (int)B->boxes.size(), B->descs.data(), B->first.data());
+  return sync_sizes(B->boxes.data(), (int)B->boxes.size(), B->descs.data(), B->first.data(), B->d_boxes, B->d_sizes,
+                    B->stream);
 }
 
 extern "C" grx_status grx_gcmc_batch_reset_stats(grx_gcmc_batch* B) {

@@ -400,4 +400,5 @@ struct BoxHost;
 void set_error(const char* fmt, ...);
 grx_status cuda_status(cudaError_t e, const char* what);
 void count_launch(uint64_t n = 1);
+void note_transfer(size_t h2d, size_t d2h);  // bytes the calling thread's last grx_gcmc_run copied
 }  // namespace grx

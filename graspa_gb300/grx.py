@@ -134,7 +134,7 @@ EXPORTS = [
     "grx_box_get_exclusion", "grx_trial_energies", "grx_single_body_energy", "grx_ewald_sizes",
     "grx_ewald_total", "grx_ewald_set_structure_factors", "grx_ewald_get_structure_factors",
     "grx_total_energy_overlap", "grx_ewald_delta", "grx_ewald_delta_lambda", "grx_ewald_delta_identity_swap", "grx_ewald_commit", "grx_total_energy", "grx_cbmc_select",
-    "grx_widom_insertions", "grx_widom_insertions_async", "grx_launch_count", "grx_probe_fp32_fma", "grx_trial_energies_noalloc", "grx_gcmc_run",
+    "grx_widom_insertions", "grx_widom_insertions_async", "grx_launch_count", "grx_last_transfer", "grx_probe_fp32_fma", "grx_trial_energies_noalloc", "grx_gcmc_run",
     "grx_box_write_molecule", "grx_box_remove_molecule", "grx_gcmc_batch_create", "grx_gcmc_batch_destroy",
     "grx_gcmc_batch_set_step", "grx_gcmc_batch_launch", "grx_gcmc_batch_run_graph", "grx_gcmc_batch_stats",
     "grx_gcmc_batch_reset_stats", "grx_gcmc_batch_autotune", "grx_gcmc_batch_set_shape", "grx_gcmc_batch_get_shape", "grx_arena_create", "grx_arena_destroy",
@@ -195,6 +195,7 @@ def load(path=LIB_PATH):
                                              C.c_void_p]
     L.grx_launch_count.restype = C.c_uint64
     L.grx_probe_fp32_fma.argtypes = [C.c_int32, P(C.c_double), P(C.c_float)]
+    L.grx_last_transfer.argtypes = [P(C.c_size_t), P(C.c_size_t)]
     L.grx_trial_energies_noalloc.argtypes = [C.c_void_p, P(Trials), C.c_int32, C.c_int64, C.c_int64, C.c_int32,
                                              P(TrialEnergy), _u8p]
     L.grx_box_write_molecule.argtypes = [C.c_void_p, C.c_int32, C.c_size_t, _dp, _dp, P(C.c_size_t)]
@@ -798,6 +799,13 @@ def cbmc_select(logw, seed, stream, move, word):
 
 def launch_count():
     return load().grx_launch_count()
+
+
+def last_transfer():
+    """(h2d, d2h) bytes of this thread's last grx_gcmc_run."""
+    a, b = C.c_size_t(), C.c_size_t()
+    check(load().grx_last_transfer(C.byref(a), C.byref(b)), "grx_last_transfer")
+    return a.value, b.value
 
 
 def probe_fp32_fma(iters=20000):

@@ -518,6 +518,10 @@ grx_status grx_trial_energies_noalloc(grx_box* box, const grx_trials* trials, in
 
 /* Number of kernel launches this process issued through the library. */
 uint64_t grx_launch_count(void);
+/* Bytes copied host -> device and device -> host by the calling thread's last
+ * grx_gcmc_run (box state descriptors, move sets, offsets and step in; statistics and
+ * molecule counts out). */
+grx_status grx_last_transfer(size_t* h2d, size_t* d2h);
 
 #ifdef __cplusplus
 }
