@@ -78,6 +78,25 @@ def dist_env():
     return rank, world, local
 
 
+def rank_seed(rank, seed=42):
+    """Philox key of a rank's chains: every rank runs independent replicas (no exchange)."""
+    return seed + 1000 * rank
+
+
+def aggregate(torch, dist, work, seconds, device):
+    """Whole-job throughput over ranks: the work summed over ranks divided by the slowest
+    rank's time (max over ranks, as the timing contract asks). Without a process group the
+    rank is the job."""
+    if dist is None:
+        return work / seconds, work, seconds
+    t = torch.tensor([float(work), float(seconds)], dtype=torch.float64, device=device)
+    w = t[:1].clone()
+    s = t[1:].clone()
+    dist.all_reduce(w, op=dist.ReduceOp.SUM)
+    dist.all_reduce(s, op=dist.ReduceOp.MAX)
+    return float(w.item()) / float(s.item()), float(w.item()), float(s.item())
+
+
 class ClockSampler:
     """nvidia-smi clock / throttle sampling during the timed region."""
 
@@ -217,7 +236,7 @@ def bench_gcmc(args, grx, torch, stream, flush, rank, world, dist):
     ms = int(system["molsize"][1])
     R = args.chains or 3 * torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
     S = args.mc_steps
-    descs = gcmc_descs(grx, R, seed=42 + 1000 * rank)
+    descs = gcmc_descs(grx, R, seed=rank_seed(rank))
     out = {"chains": R, "mc_steps_per_step": S}
 
     # mixed, batched: the headline
@@ -235,13 +254,9 @@ def bench_gcmc(args, grx, torch, stream, flush, rank, world, dist):
     times, stats = timed_graph(torch, batch, stream, S, args.steps, args.warmup, flush, dist)
     clk = clocks.stop()
     launches = grx.launch_count() - l0
-    tot = sum(times)
-    if dist:
-        t = torch.tensor([tot], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        tot = float(t.item())
     te, pairs = work_of(stats, ms, nfw)
-    out.update(value=te * world / tot, seconds=tot, times=times, trial_energies=te, pairs=pairs, clocks=clk,
+    value, te_all, tot = aggregate(torch, dist, te, sum(times), "cuda")
+    out.update(value=value, seconds=tot, times=times, trial_energies=te, pairs=pairs, clocks=clk,
                launches=launches)
     warm = timed_graph.warm_stats
     acc_stats, nxt = batch.stats()
@@ -314,7 +329,7 @@ def bench_gcmc(args, grx, torch, stream, flush, rank, world, dist):
             te_e2e += work_of(st, ms, nfw)[0]
     close_boxes(boxes)
     h2d, d2h = grx.last_transfer()  # what one grx_gcmc_run copies (the same every step)
-    out["e2e"] = {"value": te_e2e * world / sum(e2e), "unit": "trial_energies/s",
+    out["e2e"] = {"value": aggregate(torch, dist, te_e2e, sum(e2e), "cuda")[0], "unit": "trial_energies/s",
                   "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
     return out
 
