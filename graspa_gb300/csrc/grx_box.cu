@@ -516,6 +516,7 @@ static grx_status box_create(const grx_box_desc* desc, grx_arena* arena, grx_box
   // w_k = distance between lattice planes) bounds it from below.
   d.cull = 1;
   d.chunk_mult = 1;
+  d.ew_rows = 0;
   d.cull_r = (float)(std::sqrt((double)d.screen2) + 0.01);
   {
     const double* C = g.cell;

@@ -21,6 +21,17 @@ constexpr int kMaxTrials = 64;
 constexpr int kMolWork = 32;      // atoms of one molecule held in shared memory
 constexpr int kCbmcBeads = 128;   // trial beads of one pass
 constexpr int kCbmcMaxMult = 8;   // items per warp of a bead pass, at most
+constexpr int kEwRowBytes = 96 * 1024;  // largest (kx, ky) row-product table of a move
+constexpr int kEwRowReuse = 16;         // active k per row at which the row products pay
+
+// Entries of the row-product table of the double-float Ewald delta: one per (kx, ky) row and
+// moved atom. The host enables it for a box (BoxDev::ew_rows) when the table for 2 * molsize
+// atoms (a translation) fits kEwRowBytes and the box has at least kEwRowReuse active k per
+// row, and sizes dynamic shared memory for it; the kernels read the flag.
+__host__ __device__ __forceinline__ int ew_rows(const int* kmax) { return (kmax[0] + 1) * (2 * kmax[1] + 1); }
+__host__ __device__ __forceinline__ bool ew_rows_worth(const int* kmax, int nact, int molsize) {
+  return (size_t)ew_rows(kmax) * 2 * molsize * 16 <= (size_t)kEwRowBytes && nact >= kEwRowReuse * ew_rows(kmax);
+}
 
 // Workspace of a block of NW warps. A pass uses at most items + beads - 1 partial
 // slots, items = mult * NW.
@@ -221,6 +232,7 @@ __device__ __noinline__ void step_weight(WK& W, int nt, double beta, int bias, d
 template <int PREC, class WK>
 __device__ __noinline__ void ewald_move(const BoxDev& b, WK& W, int na, double2* eik, double2* s_out,
                                            double& same, double& cross) {
+  const bool rows = b.ew_rows != 0;
   const int tid = threadIdx.x;
   const int kx1 = b.kmax[0] + 1, ky1 = b.kmax[1] + 1;
   double2* ex = eik;
@@ -284,33 +296,73 @@ __device__ __noinline__ void ewald_move(const BoxDev& b, WK& W, int na, double2*
     const float4* fy = fx + kx1 * na;
     const float4* fz = fy + ky1 * na;
     df sm = {0.f, 0.f}, cr = {0.f, 0.f};
-    for (int j = tid; j < b.nact; j += blockDim.x) {
-      const int4 k = b.kact[j];
-      df cre = {0.f, 0.f}, cim = {0.f, 0.f};
-      const int ay = abs(k.y), az = abs(k.z);
-      const float sy = k.y < 0 ? -1.f : 1.f, sz = k.z < 0 ? -1.f : 1.f;
-      for (int at = 0; at < na; ++at) {
-        const float4 X = fx[at + na * k.x], Y = fy[at + na * ay], Z = fz[at + na * az];
-        const df xr = {X.x, X.y}, xi = {X.z, X.w};
-        const df yr = {Y.x, Y.y}, yi = {sy * Y.z, sy * Y.w};
-        const df zr = {Z.x, Z.y}, zi = {sz * Z.z, sz * Z.w};
-        const df pr = df_add(df_mul(xr, yr), df_mul(df{-xi.hi, -xi.lo}, yi));
-        const df pi = df_add(df_mul(xr, yi), df_mul(xi, yr));
-        const df tr = df_add(df_mul(pr, zr), df_mul(df{-pi.hi, -pi.lo}, zi));
-        const df ti = df_add(df_mul(pr, zi), df_mul(pi, zr));
-        const df q = {W.qd[at].x, W.qd[at].y};
-        cre = df_add(cre, df_mul(q, tr));
-        cim = df_add(cim, df_mul(q, ti));
-      }
+    // energy terms of one k from its dS: sm += 2 Re(temp S* dS) + temp |dS|^2,
+    // cr += Re(temp S_fw* dS); optionally stage S + dS (FP64, compensated)
+    auto k_energy = [&](int j, int slot, const df& cre, const df& cim) {
       const float4 A = b.ewA[j], F = b.ewF[j];
       const float2 T = b.ewT[j];
       const df reA = df_add(df_mul(df{A.x, A.y}, cre), df_mul(df{A.z, A.w}, cim));
       const df n2 = df_add(df_mul(cre, cre), df_mul(cim, cim));
       sm = df_add(sm, df_add(df{2.f * reA.hi, 2.f * reA.lo}, df_mul(df{T.x, T.y}, n2)));
       cr = df_add(cr, df_add(df_mul(df{F.x, F.y}, cre), df_mul(df{F.z, F.w}, cim)));
-      if (s_out) {  // compensated update: FP64 S plus the double-float dS
-        const double2 ov = b.s_ads[k.w];
-        s_out[k.w] = make_double2(ov.x + df_to(cre), ov.y + df_to(cim));
+      if (s_out) {
+        const double2 ov = b.s_ads[slot];
+        s_out[slot] = make_double2(ov.x + df_to(cre), ov.y + df_to(cim));
+      }
+    };
+    if (rows) {
+      // q X(kx) Y(ky) per (kx, ky) row and atom, then one complex product with Z(kz) per
+      // (k, atom); threads keep one k each, as in the direct form
+      const int ny = 2 * b.kmax[1] + 1, nrow = ew_rows(b.kmax);
+      float4* rxy = fx + ntab;
+      for (int e = tid; e < nrow * na; e += blockDim.x) {
+        const int row = e / na, at = e - row * na;
+        const int kx = row / ny, ky = row - kx * ny - b.kmax[1];
+        const float s = ky < 0 ? -1.f : 1.f;
+        const float4 X = fx[at + na * kx], Y = fy[at + na * abs(ky)];
+        const df xr = {X.x, X.y}, xi = {X.z, X.w};
+        const df yr = {Y.x, Y.y}, yi = {s * Y.z, s * Y.w};
+        const df q = {W.qd[at].x, W.qd[at].y};
+        const df pr = df_mul(q, df_add(df_mul(xr, yr), df_mul(df{-xi.hi, -xi.lo}, yi)));
+        const df pi = df_mul(q, df_add(df_mul(xr, yi), df_mul(xi, yr)));
+        rxy[e] = make_float4(pr.hi, pr.lo, pi.hi, pi.lo);
+      }
+      __syncthreads();
+      for (int j = tid; j < b.nact; j += blockDim.x) {
+        const int4 k = b.kact[j];
+        const float4* P = rxy + (k.x * ny + k.y + b.kmax[1]) * na;
+        const int az = abs(k.z);
+        const float sz = k.z < 0 ? -1.f : 1.f;
+        df cre = {0.f, 0.f}, cim = {0.f, 0.f};
+        for (int at = 0; at < na; ++at) {
+          const float4 R = P[at], Z = fz[at + na * az];
+          const df pr = {R.x, R.y}, pi = {R.z, R.w};
+          const df zr = {Z.x, Z.y}, zi = {sz * Z.z, sz * Z.w};
+          cre = df_add(cre, df_add(df_mul(pr, zr), df_mul(df{-pi.hi, -pi.lo}, zi)));
+          cim = df_add(cim, df_add(df_mul(pr, zi), df_mul(pi, zr)));
+        }
+        k_energy(j, k.w, cre, cim);
+      }
+    } else {
+      for (int j = tid; j < b.nact; j += blockDim.x) {
+        const int4 k = b.kact[j];
+        df cre = {0.f, 0.f}, cim = {0.f, 0.f};
+        const int ay = abs(k.y), az = abs(k.z);
+        const float sy = k.y < 0 ? -1.f : 1.f, sz = k.z < 0 ? -1.f : 1.f;
+        for (int at = 0; at < na; ++at) {
+          const float4 X = fx[at + na * k.x], Y = fy[at + na * ay], Z = fz[at + na * az];
+          const df xr = {X.x, X.y}, xi = {X.z, X.w};
+          const df yr = {Y.x, Y.y}, yi = {sy * Y.z, sy * Y.w};
+          const df zr = {Z.x, Z.y}, zi = {sz * Z.z, sz * Z.w};
+          const df pr = df_add(df_mul(xr, yr), df_mul(df{-xi.hi, -xi.lo}, yi));
+          const df pi = df_add(df_mul(xr, yi), df_mul(xi, yr));
+          const df tr = df_add(df_mul(pr, zr), df_mul(df{-pi.hi, -pi.lo}, zi));
+          const df ti = df_add(df_mul(pr, zi), df_mul(pi, zr));
+          const df q = {W.qd[at].x, W.qd[at].y};
+          cre = df_add(cre, df_mul(q, tr));
+          cim = df_add(cim, df_mul(q, ti));
+        }
+        k_energy(j, k.w, cre, cim);
       }
     }
     sm = warp_sum_df(sm);

@@ -454,6 +454,11 @@ struct grx_gcmc_batch {
 
 namespace grx {
 
+// Dynamic shared memory of a GCMC block: eik tables of a move plus, when enabled, the
+// (kx, ky) row products (at most kEwRowBytes); with the largest static workspace (24 warps)
+// it stays within the 227 KB of one block.
+constexpr size_t kGcmcDynSmem = 160 * 1024;
+
 // Validates the boxes and move sets and fills the per-box state and per-entry args.
 static grx_status prepare_gcmc(grx_box* const* boxes, int32_t nboxes, const grx_gcmc_desc* descs,
                                const int32_t* ncomp_moved, std::vector<BoxDev>& hb, std::vector<GcmcArgs>& ha,
@@ -474,6 +479,10 @@ static grx_status prepare_gcmc(grx_box* const* boxes, int32_t nboxes, const grx_
     first[i] = e;
     refresh_dev(b);
     b->dev.chunk_mult = chunk_mult;
+    int msmax = 1;
+    for (int k = 0; k < nm; ++k) msmax = std::max(msmax, (int)b->molsize[descs[e + k].component]);
+    // row products of the Ewald delta for every move of the box, sized for its largest molecule
+    b->dev.ew_rows = ew_rows_worth(b->dev.kmax, b->nact, msmax) ? 1 : 0;
     for (int k = 0; k < nm; ++k, ++e) {
       const grx_gcmc_desc& d = descs[e];
       GRX_REQUIRE(d.component >= b->nhost && d.component < b->ncomp,
@@ -503,8 +512,9 @@ static grx_status prepare_gcmc(grx_box* const* boxes, int32_t nboxes, const grx_
       a.excl = b->excl_intra[d.component] + b->excl_self[d.component];
       a.big_p = d.mol_fraction * d.pressure * d.fugacity_coeff * b->dev.volume;
       ha.push_back(a);
-      const size_t need = (size_t)(b->dev.kmax[0] + b->dev.kmax[1] + b->dev.kmax[2] + 3) * 2 * ms *
-                          (sizeof(double2) + sizeof(float4));
+      size_t need = (size_t)(b->dev.kmax[0] + b->dev.kmax[1] + b->dev.kmax[2] + 3) * 2 * ms *
+                    (sizeof(double2) + sizeof(float4));
+      if (b->dev.ew_rows) need += (size_t)ew_rows(b->dev.kmax) * 2 * msmax * sizeof(float4);
       smem = std::max(smem, need);
     }
     if (!b->ewdf_valid && b->nact > 0) {
@@ -514,13 +524,13 @@ static grx_status prepare_gcmc(grx_box* const* boxes, int32_t nboxes, const grx_
     hb[i] = b->dev;
   }
   first[nboxes] = e;
-  GRX_REQUIRE(smem <= 64 * 1024, "grx_gcmc: Ewald tables exceed the shared-memory budget");
+  GRX_REQUIRE(smem <= kGcmcDynSmem, "grx_gcmc: Ewald tables exceed the shared-memory budget");
   return GRX_OK;
 }
 
 template <int PREC, int NW>
 static grx_status set_smem_one() {
-  GRX_CHECK_CUDA(cudaFuncSetAttribute(gcmc_kernel<PREC, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024),
+  GRX_CHECK_CUDA(cudaFuncSetAttribute(gcmc_kernel<PREC, NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, kGcmcDynSmem),
                  "gcmc shared memory attribute");
   return GRX_OK;
 }

@@ -81,6 +81,7 @@ struct BoxDev {
   float cull_r;          // screening radius used by the tile test
   float cellf[9];
   int chunk_mult;        // work items per warp and bead pass (tile-range chunking; autotuned)
+  int ew_rows;           // GCMC Ewald delta through (kx, ky) row products (shared memory sized for it)
   float wperp[3];        // perpendicular widths of the cell (distances between lattice planes)
   float half_wmin2;      // (min width / 2)^2, shrunk for FP32 rounding
   // real-space Coulomb table: g(s) = erfc(alpha sqrt s)/sqrt s, piecewise quintic in

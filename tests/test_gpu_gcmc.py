@@ -171,3 +171,27 @@ def test_gcmc_launch_shapes_match_oracle(grx_lib, shape):
         assert abs(st[0].energy[k] - ost.energy[k]) <= 1e-9 * max(1.0, abs(ost.energy[k]))
     with pytest.raises(grx_lib.GrxError):
         grx_lib.GcmcBatch([box], [d], grx_lib.GRX_FP64).set_shape(16, 1)
+
+
+def test_gcmc_mixed_ewald_row_products_match_oracle(grx_lib):
+    """A charged box with many k vectors per (kx, ky) row (automatic Ewald set-up of a
+    2,500-atom framework: kmax 10/16/15, 8,466 active k, 23 per row) takes the row-product
+    form of the double-float Ewald delta; the mixed chain still takes the oracle's exact
+    decisions and positions, with energies within beta*|dE| <= 1e-5 over the run."""
+    from graspa_gb300 import synth
+    s = synth.adsorbate_system("CO2", 12, n_atoms=2500)
+    S = O.OracleSystem(s)
+    _, act = S.ewald_active()
+    nrow = (s["kmax"][0] + 1) * (2 * s["kmax"][1] + 1)
+    assert int(np.sum(act)) >= 16 * nrow  # the box qualifies for the row products
+    d = params(grx_lib, pressure_pa=1e6)
+    nfw = s["comp_start"][1]
+    box = make_box(grx_lib, s)
+    st = grx_lib.gcmc_run([box], [d], 0, 250, grx_lib.GRX_MIXED)[0]
+    ost, after, _ = S.gcmc(ora_params(d), [nfw, CAP], 0, 250)
+    assert sum(st.accepted) > 20
+    assert list(st.accepted) == list(ost.accepted) and st.n_molecules == ost.n_molecules
+    assert np.max(np.abs(box.positions(1) - after["pos"][nfw:])) <= 1e-9
+    for k in range(4):
+        assert d.beta * abs(st.energy[k] - ost.energy[k]) <= 1e-5
+    box.close()
