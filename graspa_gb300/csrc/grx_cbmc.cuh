@@ -229,10 +229,9 @@ __device__ __noinline__ void step_weight(WK& W, int nt, double beta, int bias, d
 // the reference arithmetic; the other forms evaluate dS and both sums in
 // double-float on the FP32 pipe against temp*S tables (ewA, ewF). When s_out is
 // given, S_same + dS is staged there (FP64) for a later commit. Results on thread 0.
-template <int PREC, class WK>
+template <int PREC, class WK, bool ROWS = false>
 __device__ __noinline__ void ewald_move(const BoxDev& b, WK& W, int na, double2* eik, double2* s_out,
                                            double& same, double& cross) {
-  const bool rows = b.ew_rows != 0;
   const int tid = threadIdx.x;
   const int kx1 = b.kmax[0] + 1, ky1 = b.kmax[1] + 1;
   double2* ex = eik;
@@ -296,21 +295,22 @@ __device__ __noinline__ void ewald_move(const BoxDev& b, WK& W, int na, double2*
     const float4* fy = fx + kx1 * na;
     const float4* fz = fy + ky1 * na;
     df sm = {0.f, 0.f}, cr = {0.f, 0.f};
-    // energy terms of one k from its dS: sm += 2 Re(temp S* dS) + temp |dS|^2,
-    // cr += Re(temp S_fw* dS); optionally stage S + dS (FP64, compensated)
-    auto k_energy = [&](int j, int slot, const df& cre, const df& cim) {
-      const float4 A = b.ewA[j], F = b.ewF[j];
-      const float2 T = b.ewT[j];
-      const df reA = df_add(df_mul(df{A.x, A.y}, cre), df_mul(df{A.z, A.w}, cim));
-      const df n2 = df_add(df_mul(cre, cre), df_mul(cim, cim));
-      sm = df_add(sm, df_add(df{2.f * reA.hi, 2.f * reA.lo}, df_mul(df{T.x, T.y}, n2)));
-      cr = df_add(cr, df_add(df_mul(df{F.x, F.y}, cre), df_mul(df{F.z, F.w}, cim)));
-      if (s_out) {
-        const double2 ov = b.s_ads[slot];
-        s_out[slot] = make_double2(ov.x + df_to(cre), ov.y + df_to(cim));
-      }
-    };
-    if (rows) {
+    if constexpr (ROWS) {
+      // energy terms of one k from its dS: sm += 2 Re(temp S* dS) + temp |dS|^2,
+      // cr += Re(temp S_fw* dS); optionally stage S + dS (FP64, compensated)
+      auto k_energy = [&](int j, int slot, const df& cre, const df& cim) {
+        const float4 A = b.ewA[j], F = b.ewF[j];
+        const float2 T = b.ewT[j];
+        const df reA = df_add(df_mul(df{A.x, A.y}, cre), df_mul(df{A.z, A.w}, cim));
+        const df n2 = df_add(df_mul(cre, cre), df_mul(cim, cim));
+        sm = df_add(sm, df_add(df{2.f * reA.hi, 2.f * reA.lo}, df_mul(df{T.x, T.y}, n2)));
+        cr = df_add(cr, df_add(df_mul(df{F.x, F.y}, cre), df_mul(df{F.z, F.w}, cim)));
+        if (s_out) {
+          const double2 ov = b.s_ads[slot];
+          s_out[slot] = make_double2(ov.x + df_to(cre), ov.y + df_to(cim));
+        }
+      };
+
       // q X(kx) Y(ky) per (kx, ky) row and atom, then one complex product with Z(kz) per
       // (k, atom); threads keep one k each, as in the direct form
       const int ny = 2 * b.kmax[1] + 1, nrow = ew_rows(b.kmax);
@@ -362,7 +362,16 @@ __device__ __noinline__ void ewald_move(const BoxDev& b, WK& W, int na, double2*
           cre = df_add(cre, df_mul(q, tr));
           cim = df_add(cim, df_mul(q, ti));
         }
-        k_energy(j, k.w, cre, cim);
+        const float4 A = b.ewA[j], F = b.ewF[j];
+        const float2 T = b.ewT[j];
+        const df reA = df_add(df_mul(df{A.x, A.y}, cre), df_mul(df{A.z, A.w}, cim));
+        const df n2 = df_add(df_mul(cre, cre), df_mul(cim, cim));
+        sm = df_add(sm, df_add(df{2.f * reA.hi, 2.f * reA.lo}, df_mul(df{T.x, T.y}, n2)));
+        cr = df_add(cr, df_add(df_mul(df{F.x, F.y}, cre), df_mul(df{F.z, F.w}, cim)));
+        if (s_out) {  // compensated update: FP64 S plus the double-float dS
+          const double2 ov = b.s_ads[k.w];
+          s_out[k.w] = make_double2(ov.x + df_to(cre), ov.y + df_to(cim));
+        }
       }
     }
     sm = warp_sum_df(sm);

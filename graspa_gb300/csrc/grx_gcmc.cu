@@ -78,6 +78,16 @@ __device__ __forceinline__ void copy_atom(const BoxDev& b, int dst, int src, int
   const_cast<float2*>(b.qdf)[dst] = b.qdf[src];
 }
 
+// The Fourier delta of a GCMC move, staged for commit_sk: the row-product form for boxes
+// that enable it (BoxDev::ew_rows), the direct form otherwise; two instantiations, so each
+// form keeps its own register allocation.
+template <int PREC, class WK>
+__device__ __forceinline__ void ewald_delta_move(const BoxDev& b, WK& W, int na, double2* eik, double& same,
+                                                 double& cross) {
+  if (b.ew_rows) ewald_move<PREC, WK, true>(b, W, na, eik, b.s_tmp, same, cross);
+  else ewald_move<PREC, WK, false>(b, W, na, eik, b.s_tmp, same, cross);
+}
+
 // One block of NW warps per box (NW = 8, 12 or 24: 24 warps per SM in every shape).
 // The box's moved components are entries [first[box], first[box + 1]) of args /
 // stats; every step picks one of them uniformly with word 3 of the displacement slot
@@ -156,7 +166,7 @@ __global__ void __launch_bounds__(NW * 32, 24 / NW) gcmc_kernel(const BoxDev* bo
       trial_pass<PREC>(b, W, 2 * ms, ms, comp, mol);  // te[0..3] new, te[4..7] old
       if (!W.tflag[0]) {
         double same = 0.0, cross = 0.0;
-        if (a.charged) ewald_move<PREC>(b, W, 2 * ms, eik, b.s_tmp, same, cross);
+        if (a.charged) ewald_delta_move<PREC>(b, W, 2 * ms, eik, same, cross);
         if (tid == 0) {
           const double dv = (W.te[0] + W.te[2]) - (W.te[4] + W.te[6]);
           const double dr = (W.te[1] + W.te[3]) - (W.te[5] + W.te[7]);
@@ -251,7 +261,7 @@ __global__ void __launch_bounds__(NW * 32, 24 / NW) gcmc_kernel(const BoxDev* bo
         }
         if (ok2) {
           double same = 0.0, cross = 0.0;
-          if (a.charged) ewald_move<PREC>(b, W, 2 * ms, eik, b.s_tmp, same, cross);
+          if (a.charged) ewald_delta_move<PREC>(b, W, 2 * ms, eik, same, cross);
           if (tid == 0) {
             const double ew = a.charged ? same + 2.0 * cross : 0.0;
             rosen *= exp(-d.beta * ew);
@@ -322,7 +332,7 @@ __global__ void __launch_bounds__(NW * 32, 24 / NW) gcmc_kernel(const BoxDev* bo
       }
       if (ok) {
         double same = 0.0, cross = 0.0;
-        if (a.charged) ewald_move<PREC>(b, W, ms, eik, b.s_tmp, same, cross);
+        if (a.charged) ewald_delta_move<PREC>(b, W, ms, eik, same, cross);
         if (tid == 0) {
           double ew = 0.0;
           if (a.charged) {
