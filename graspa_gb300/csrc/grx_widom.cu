@@ -42,56 +42,10 @@ struct WidomArgs {
 };
 
 // Log-sum-exp selection and weight of one CBMC step (SelectTrialPosition,
-// mc_widom.h:14-39, and CBMC_FirstBead_Finish :330-376, insertion branch).
-__device__ bool select_trial(const double* te, const int* tflag, int nt, double beta, int bias,
-                             double u, double navg, int& sel, double& wavg, int& nok) {
-  double mx = -INFINITY;
-  nok = 0;
-  for (int t = 0; t < nt; ++t) {
-    if (tflag[t]) continue;
-    double tot = te[4 * t] + te[4 * t + 2];
-    if (bias) tot += te[4 * t + 1] + te[4 * t + 3];
-    mx = fmax(mx, __dmul_rn(-beta, tot));
-    ++nok;
-  }
-  if (nok == 0) return false;
-  double sum = 0.0;
-  for (int t = 0; t < nt; ++t) {
-    if (tflag[t]) continue;
-    double tot = te[4 * t] + te[4 * t + 2];
-    if (bias) tot += te[4 * t + 1] + te[4 * t + 3];
-    sum += exp(__dsub_rn(__dmul_rn(-beta, tot), mx));
-  }
-  const double ws = u * sum;
-  int s = -1, left = nok;
-  double cum = 0.0;
-  for (int t = 0; t < nt; ++t) {
-    if (tflag[t]) continue;
-    double tot = te[4 * t] + te[4 * t + 2];
-    if (bias) tot += te[4 * t + 1] + te[4 * t + 3];
-    cum += exp(__dsub_rn(__dmul_rn(-beta, tot), mx));
-    s = t;
-    --left;
-    if (!(cum < ws) || left == 0) break;
-  }
-  double w = 0.0;
-  for (int t = 0; t < nt; ++t) {
-    if (tflag[t]) continue;
-    double tot = te[4 * t] + te[4 * t + 2];
-    if (bias) tot += te[4 * t + 1] + te[4 * t + 3];
-    w += exp(__dmul_rn(-beta, tot));
-  }
-  if (w < 1e-150) return false;
-  sel = s;
-  double avg = w / navg;
-  if (!bias) avg *= exp(-beta * (te[4 * s + 1] + te[4 * s + 3]));
-  wavg = avg;
-  return true;
-}
-
-// The same selection computed by warp 0: the exponentials are evaluated one trial
-// per lane, the sums and the cumulative search stay sequential in trial order on
-// lane 0, so the result is identical to select_trial. Results are valid on lane 0.
+// mc_widom.h:14-39, and CBMC_FirstBead_Finish :330-376, insertion branch), computed by
+// warp 0: the exponentials are evaluated one trial per lane, the sums and the cumulative
+// search stay sequential in trial order on lane 0, as in the reference's host loop.
+// Results are valid on lane 0.
 __device__ bool select_trial_warp(const double* te, const int* tflag, int nt, double beta, int bias,
                                   double u, double navg, int& sel, double& wavg, int& nok, double* ws,
                                   double* wa) {
