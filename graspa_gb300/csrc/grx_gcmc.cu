@@ -351,7 +351,7 @@ __global__ void __launch_bounds__(NW * 32, 24 / NW) gcmc_kernel(const BoxDev* bo
             }
           } else {
             rosen /= exp(-d.beta * ew);
-            rosen /= exp(-d.beta * d.tail_insert);
+            rosen /= exp(d.beta * d.tail_insert);  // the deletion's tail difference is -tail_insert
             pacc = (double)N / (d.beta * a.big_p) * d.ideal_rosenbluth / rosen;
             s_accept = uacc < pacc;
           }

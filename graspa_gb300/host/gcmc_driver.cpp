@@ -7,6 +7,9 @@
 //   widom  <n>       runs n InsertionMove::WidomMove calls and the Widom statistics
 //   volume <n>       runs n NPT VolumeMove calls (trial volume, trial energy, acceptance)
 //   gibbs  <n>       runs n NVTGibbsMove calls between the box and an identical copy
+//   transfer <n>     runs n GibbsParticleTransfer calls of the moved component between the
+//                    box and an identical copy
+//   swap   <n>       runs n IdentitySwapMove calls (every adsorbate component takes part)
 //   lambda 0         two CB/CFC lambda steps of molecule 0 (CBCF_LambdaChange)
 // and prints the move statistics, the accepted-energy sum and the drift check,
 // then the adsorbate positions, as plain text.
@@ -100,6 +103,7 @@ void read_system(const char* path, Variables& V, std::vector<size_t>& n_stored, 
   R.key("fugacity_coeff"); C.FugacityCoeff[comp] = R.d();
   R.key("mol_fraction"); C.MolFraction[comp] = R.d();
   R.key("ideal_rosenbluth"); C.IdealRosenbluthWeight[comp] = R.d();
+  R.key("tail_insert"); C.TailCorrectionInsert[comp] = R.d();
   R.key("ntrials"); V.Widom[0].NumberWidomTrials = (size_t)R.i();
   R.key("norient"); V.Widom[0].NumberWidomTrialsOrientations = (size_t)R.i();
   Move_Statistics& M = C.Moves[comp];
@@ -117,7 +121,8 @@ void read_system(const char* path, Variables& V, std::vector<size_t>& n_stored, 
 
 int main(int argc, char** argv) {
   if (argc < 4) {
-    std::fprintf(stderr, "usage: %s <system file> host|device|widom|volume|lambda <nsteps>\n", argv[0]);
+    std::fprintf(stderr, "usage: %s <system file> host|device|widom|volume|gibbs|transfer|swap|lambda <nsteps>\n",
+                 argv[0]);
     return 2;
   }
   try {
@@ -127,7 +132,7 @@ int main(int argc, char** argv) {
     read_system(argv[1], V, n_stored, comp);
     const std::string mode = argv[2];
     const long long nsteps = std::atoll(argv[3]);
-    if (mode == "gibbs") {  // a second, identical box (its arrays re-pointed at its own storage)
+    if (mode == "gibbs" || mode == "transfer") {  // a second, identical box (arrays re-pointed at its own storage)
       V.Sims.push_back(V.Sims[0]);
       V.SystemComponents.push_back(V.SystemComponents[0]);
       V.Widom.push_back(V.Widom[0]);
@@ -167,6 +172,47 @@ int main(int argc, char** argv) {
       std::printf("drift_b %.17g\n", (e1b.total() - e0b.total()) - V.SystemComponents[1].deltaE.total());
       std::printf("energy_scale %.17g\n", std::fabs(e1.total()) + std::fabs(e1b.total()));
       Destroy_Box(V, 1);
+    } else if (mode == "transfer") {
+      // Gibbs particle transfers of the moved component between box 0 and its copy
+      Gibbs G;
+      Components& C1 = V.SystemComponents[1];
+      const MoveEnergy e0b = Total_Energy(V.Sims[1]);
+      for (long long k = 0; k < nsteps; ++k) {
+        GibbsParticleTransfer(V, comp, G);
+        const Gibbs::TransferRecord& r = G.LastTransfer;
+        std::printf("transfer %lld %zu %zu %d %.17g %.17g %.17g %zu %zu\n", k, r.InsertionBox, r.DeletedMolecule,
+                    r.Accepted ? 1 : 0, r.RosenbluthInsertion, r.RosenbluthDeletion, r.Pacc,
+                    C.NumberOfMolecule_for_Component[comp], C1.NumberOfMolecule_for_Component[comp]);
+      }
+      const MoveEnergy e1 = Total_Energy(V.Sims[0]), e1b = Total_Energy(V.Sims[1]);
+      std::printf("transfer_attempts %.17g\n", G.GibbsXferStats[0]);
+      std::printf("transfer_accepted %.17g\n", G.GibbsXferStats[1]);
+      std::printf("drift %.17g\n", (e1.total() - e0.total()) - (C.deltaE.total() - C.deltaE.TailE));
+      std::printf("drift_b %.17g\n", (e1b.total() - e0b.total()) - (C1.deltaE.total() - C1.deltaE.TailE));
+      std::printf("energy_scale %.17g\n", std::fabs(e1.total()) + std::fabs(e1b.total()));
+      Destroy_Box(V, 1);
+    } else if (mode == "swap") {
+      // identity swaps among the adsorbate components
+      for (long long k = 0; k < nsteps; ++k) {
+        const MoveEnergy dE = IdentitySwapMove(V, 0);
+        C.deltaE += dE;
+        C.Step++;
+        const Components::IdentitySwapRecord& r = C.LastIdentitySwap;
+        std::printf("swap %lld %zu %zu %zu %d %.17g %.17g %.17g %.17g %.17g\n", k, r.OldComponent, r.NewComponent,
+                    r.OldMolecule, r.Accepted ? 1 : 0, r.RosenbluthNew, r.RosenbluthOld, r.Pacc, r.Ewald.x,
+                    r.Ewald.y);
+      }
+      const MoveEnergy e1 = Total_Energy(V.Sims[0]);
+      std::printf("energy_sum %.17g\n", C.deltaE.total());
+      std::printf("drift %.17g\n", (e1.total() - e0.total()) - C.deltaE.total());
+      for (int c = C.NComponents.y; c < C.NComponents.x; ++c)
+        std::printf("count %d %zu %zu %zu\n", c, C.NumberOfMolecule_for_Component[c],
+                    C.Moves[c].IdentitySwapAddAccepted, C.Moves[c].IdentitySwapRemoveAccepted);
+      for (int c = C.NComponents.y; c < C.NComponents.x; ++c) {
+        const Atoms& A = V.Sims[0].d_a[c];
+        std::printf("positions %zu\n", A.size);
+        for (size_t i = 0; i < A.size; ++i) std::printf("%.17g %.17g %.17g\n", A.pos[i].x, A.pos[i].y, A.pos[i].z);
+      }
     } else if (mode == "volume") {
       // NPT volume moves of the box (max change of ln V 0.05): per move the trial volume,
       // the trial box's FP64 total, its overlap flag, the energy before the move, acceptance
@@ -214,7 +260,7 @@ int main(int argc, char** argv) {
         att[3] = M.DeletionTotal; att[4] = M.ReinsertionTotal;
         acc[0] = M.TranslationAccepted; acc[1] = M.RotationAccepted; acc[2] = M.InsertionAccepted;
         acc[3] = M.DeletionAccepted; acc[4] = M.ReinsertionAccepted;
-        esum = C.deltaE.total();
+        esum = C.deltaE.total() - C.deltaE.TailE;  // the FP64 totals below carry no tail term
       } else if (mode == "device") {
         const grx_gcmc_stats st = RunMoves_Device(V, 0, comp, nsteps);
         for (int k = 0; k < 5; ++k) { att[k] = st.attempts[k]; acc[k] = st.accepted[k]; }

@@ -74,13 +74,14 @@ void Move_Statistics::Record_Move_Accept(int move) {
   }
 }
 void Move_Statistics::NormalizeProbabilities() {
-  const double tot = TranslationProb + RotationProb + ReinsertionProb + SwapProb;
+  const double tot = TranslationProb + RotationProb + ReinsertionProb + IdentitySwapProb + SwapProb;
   if (tot > 1e-10) {
-    TranslationProb /= tot; RotationProb /= tot; ReinsertionProb /= tot; SwapProb /= tot;
+    TranslationProb /= tot; RotationProb /= tot; ReinsertionProb /= tot; IdentitySwapProb /= tot; SwapProb /= tot;
   }
   RotationProb += TranslationProb;
   ReinsertionProb += RotationProb;
-  SwapProb += ReinsertionProb;
+  IdentitySwapProb += ReinsertionProb;
+  SwapProb += IdentitySwapProb;
 }
 
 void check(grx_status st, const char* what) {
@@ -232,7 +233,7 @@ size_t SelectTrialPosition(std::vector<double>& LogBoltzmannFactors, const Varia
   int32_t sel = 0;
   double sum = 0.0;
   check(grx_cbmc_select(LogBoltzmannFactors.data(), (int32_t)LogBoltzmannFactors.size(), Vars.Random.Seed,
-                        Vars.Random.Stream, Vars.SystemComponents[systemId].Step, word, &sel, &sum),
+                        Vars.Random.BoxStream(systemId), Vars.SystemComponents[systemId].Step, word, &sel, &sum),
         "grx_cbmc_select");
   return (size_t)sel;
 }
@@ -463,7 +464,7 @@ void VolumeMove(Variables& Vars, size_t systemId) {
   Simulations& Sims = Vars.Sims[systemId];
   SC.VolumeMoveAttempts++;
   uint32_t w[4];
-  grx_draw(Vars.Random.Seed, Vars.Random.Stream, SC.Step, GRX_SLOT_VOLUME, w);
+  grx_draw(Vars.Random.Seed, Vars.Random.BoxStream(systemId), SC.Step, GRX_SLOT_VOLUME, w);
   const double OldV = Sims.Box.Volume;
   const double newV = std::exp(std::log(OldV) + SC.VolumeMoveMaxChange * 2.0 * (grx_u01(w[0]) - 0.5));
   const double scale = std::cbrt(newV / OldV);
@@ -498,7 +499,7 @@ void NVTGibbsMove(Variables& Vars, Gibbs& G) {
   if (Vars.SystemComponents.size() < 2) throw std::runtime_error("NVTGibbsMove: two boxes needed");
   Components& C0 = Vars.SystemComponents[0];
   uint32_t w[4];
-  grx_draw(Vars.Random.Seed, Vars.Random.Stream, C0.Step, GRX_SLOT_VOLUME, w);
+  grx_draw(Vars.Random.Seed, Vars.Random.BoxStream(0), C0.Step, GRX_SLOT_VOLUME, w);
   const size_t sel = grx_u01(w[2]) > 0.5 ? 1 : 0, oth = 1 - sel;
   G.GibbsBoxStats[0] += 1.0;
   const double VA = Vars.Sims[sel].Box.Volume, VB = Vars.Sims[oth].Box.Volume, TotalV = VA + VB;
@@ -583,7 +584,15 @@ void CBMC_FirstBead_Finish(Variables& Vars, size_t systemId, CBMC_Variables& CBM
       good = true;
       break;
     }
-    default: {  // CBMC_DELETION, REINSERTION_RETRACE: the existing bead, no selection
+    case IDENTITY_SWAP_NEW: {  // one trial, the swapped molecule's first bead
+      if (Rosen.empty()) break;
+      for (double& r : Rosen) r = std::exp(r);
+      W = std::accumulate(Rosen.begin(), Rosen.end(), 0.0);
+      if (W < 1e-150) break;
+      good = true;
+      break;
+    }
+    default: {  // CBMC_DELETION, REINSERTION_RETRACE, IDENTITY_SWAP_OLD: the existing bead, no selection
       if (Rosen.empty()) break;
       for (double& r : Rosen) r = std::exp(r);
       W = std::accumulate(Rosen.begin(), Rosen.end(), 0.0);
@@ -594,7 +603,9 @@ void CBMC_FirstBead_Finish(Variables& Vars, size_t systemId, CBMC_Variables& CBM
   if (!good) return;
   if (CBMC.MoveType == REINSERTION_INSERTION) CBMC.StoredR = W - Rosen[sel];
   if (CBMC.MoveType == REINSERTION_RETRACE) W += CBMC.StoredR;
-  double avg = W / (double)Vars.Widom[systemId].NumberWidomTrials;
+  // an identity swap's first bead is a single trial: not averaged (mc_widom.h:368-370)
+  const bool swap = CBMC.MoveType == IDENTITY_SWAP_NEW || CBMC.MoveType == IDENTITY_SWAP_OLD;
+  double avg = swap ? W : W / (double)Vars.Widom[systemId].NumberWidomTrials;
   if (!Vars.device_FF.VDWRealBias) avg *= std::exp(-SC.Beta * (SC.TrialEnergies[sel].HGReal + SC.TrialEnergies[sel].GGReal));
   CBMC.selectedTrial = SC.Trialindex[sel];
   CBMC.SuccessConstruction = true;
@@ -611,16 +622,20 @@ void Widom_Move_FirstBead_PARTIAL(Variables& Vars, size_t systemId, CBMC_Variabl
   const Atoms& A = Sims.d_a[comp];
   size_t ntrials = Vars.Widom[systemId].NumberWidomTrials;
   size_t molid = SC.TempVal.molecule;
-  const bool retrace = CBMC.MoveType == CBMC_DELETION || CBMC.MoveType == REINSERTION_RETRACE;
-  if (CBMC.MoveType == CBMC_INSERTION) molid = SC.NumberOfMolecule_for_Component[comp];
-  if (CBMC.MoveType == REINSERTION_RETRACE) ntrials = 1;
+  const bool retrace = CBMC.MoveType == CBMC_DELETION || CBMC.MoveType == REINSERTION_RETRACE ||
+                       CBMC.MoveType == IDENTITY_SWAP_OLD;
+  const bool swap_new = CBMC.MoveType == IDENTITY_SWAP_NEW;
+  if (CBMC.MoveType == CBMC_INSERTION || swap_new) molid = SC.NumberOfMolecule_for_Component[comp];
+  if (CBMC.MoveType == REINSERTION_RETRACE || CBMC.MoveType == IDENTITY_SWAP_OLD || swap_new) ntrials = 1;
   const size_t start = SC.TempVal.molecule * ms;
   for (size_t t = 0; t < ntrials; ++t) {
-    if (retrace && t == 0) {
+    if (swap_new) {
+      // the caller placed the swapped molecule's first bead in New.pos[0] (mc_swap_moves.h:267)
+    } else if (retrace && t == 0) {
       Sims.New.pos[0] = A.pos[start];
     } else {
       uint32_t r[4];
-      grx_draw(Vars.Random.Seed, Vars.Random.Stream, SC.Step, GRX_SLOT_FIRST + (uint32_t)t, r);
+      grx_draw(Vars.Random.Seed, Vars.Random.BoxStream(systemId), SC.Step, GRX_SLOT_FIRST + (uint32_t)t, r);
       Sims.New.pos[t] = double3{Sims.Box.Cell[0] * grx_u01(r[0]), Sims.Box.Cell[4] * grx_u01(r[1]),
                                 Sims.Box.Cell[8] * grx_u01(r[2])};
     }
@@ -643,14 +658,18 @@ void Widom_Move_Chain_PARTIAL(Variables& Vars, size_t systemId, CBMC_Variables& 
   const size_t ms = SC.Moleculesize[comp], chain = ms - 1;
   const size_t no = Vars.Widom[systemId].NumberWidomTrialsOrientations;
   const Atoms& A = Sims.d_a[comp];
-  const bool retrace = CBMC.MoveType == CBMC_DELETION || CBMC.MoveType == REINSERTION_RETRACE;
-  const size_t molid = CBMC.MoveType == CBMC_INSERTION ? SC.NumberOfMolecule_for_Component[comp] : SC.TempVal.molecule;
+  const bool retrace = CBMC.MoveType == CBMC_DELETION || CBMC.MoveType == REINSERTION_RETRACE ||
+                       CBMC.MoveType == IDENTITY_SWAP_OLD;
+  const bool grow_new = CBMC.MoveType == CBMC_INSERTION || CBMC.MoveType == IDENTITY_SWAP_NEW;
+  const size_t molid = grow_new ? SC.NumberOfMolecule_for_Component[comp] : SC.TempVal.molecule;
   const size_t start = SC.TempVal.molecule * ms + 1;
-  const uint32_t slot = CBMC.MoveType == REINSERTION_RETRACE ? GRX_SLOT_RETRACE : GRX_SLOT_ORIENT;
+  // a retrace that follows a growth in the same move draws its own orientations
+  const uint32_t slot = (CBMC.MoveType == REINSERTION_RETRACE || CBMC.MoveType == IDENTITY_SWAP_OLD)
+                            ? GRX_SLOT_RETRACE : GRX_SLOT_ORIENT;
   const double3 fb = Sims.Old.pos[0];
   for (size_t o = 0; o < no; ++o) {
     uint32_t r[4];
-    grx_draw(Vars.Random.Seed, Vars.Random.Stream, SC.Step, slot + (uint32_t)o, r);
+    grx_draw(Vars.Random.Seed, Vars.Random.BoxStream(systemId), SC.Step, slot + (uint32_t)o, r);
     for (size_t a = 0; a < chain; ++a) {
       const size_t i = o * chain + a;
       if (retrace && o == 0) {
@@ -851,7 +870,7 @@ MoveEnergy SingleBodyMove(Variables& Vars, size_t systemId, int MoveType, double
   MS.Record_Move_Total(MoveType);
   Atoms& A = Sims.d_a[comp];
   uint32_t w2[4];
-  grx_draw(Vars.Random.Seed, Vars.Random.Stream, SC.Step, GRX_SLOT_DISP, w2);
+  grx_draw(Vars.Random.Seed, Vars.Random.BoxStream(systemId), SC.Step, GRX_SLOT_DISP, w2);
   // get_new_position (mc_utilities.h:485-540)
   if (MoveType == TRANSLATION) {
     const double dx = MS.MaxTranslation.x * 2.0 * (grx_u01(w2[0]) - 0.5);
@@ -986,13 +1005,21 @@ void InsertionMove::Acceptance(Variables& Vars, size_t systemId, double RANDOM) 
     return;
   }
   Accept = true;
-  std::vector<double> pos, qs;  // AcceptInsertion (mc_swap_utilities.h:94-132)
+  Commit(Vars, systemId);
+}
+
+// AcceptInsertion (mc_utilities.h:357-385): the grown molecule stored, S(k) committed.
+void InsertionMove::Commit(Variables& Vars, size_t systemId) {
+  Components& SC = Vars.SystemComponents[systemId];
+  Simulations& Sims = Vars.Sims[systemId];
+  const size_t comp = SC.TempVal.component;
+  std::vector<double> pos, qs;
   if (SC.Moleculesize[comp] > 1) {
     grown_atoms(Sims, SC, comp, InsertionVariables.selectedTrialOrientation, pos, qs);
   } else {
     pos = {Sims.Old.pos[0].x, Sims.Old.pos[0].y, Sims.Old.pos[0].z};
   }
-  write_molecule(Vars, systemId, comp, N, pos);
+  write_molecule(Vars, systemId, comp, SC.NumberOfMolecule_for_Component[comp], pos);
   if (!Vars.device_FF.noCharges && SC.hasPartialCharge[comp]) Update_Vector_Ewald(Sims.Box, false, SC, comp);
 }
 
@@ -1050,7 +1077,7 @@ void DeletionMove::Calculate(Variables& Vars, size_t systemId) {
     C.Rosenbluth /= std::exp(-SC.Beta * (E.x + E.y));
   }
   energy.TailE = SC.TailCorrectionInsert.empty() ? 0.0 : -SC.TailCorrectionInsert[comp];
-  C.Rosenbluth /= std::exp(SC.Beta * energy.TailE);
+  C.Rosenbluth /= std::exp(-SC.Beta * energy.TailE);  // TailE: the deletion difference (mc_swap_utilities.h:197-200)
   preFactor = GetPrefactor(SC, Sims, comp, DELETION);
   Pacc = preFactor * SC.IdealRosenbluthWeight[comp] / C.Rosenbluth;
 }
@@ -1064,6 +1091,14 @@ void DeletionMove::Acceptance(Variables& Vars, size_t systemId, double RANDOM) {
     return;
   }
   Accept = true;
+  Commit(Vars, systemId);
+}
+
+// AcceptDeletion (mc_utilities.h:387-417): the last molecule moved into the slot, S(k) committed.
+void DeletionMove::Commit(Variables& Vars, size_t systemId) {
+  Components& SC = Vars.SystemComponents[systemId];
+  Simulations& Sims = Vars.Sims[systemId];
+  const size_t comp = SC.TempVal.component;
   remove_molecule(Vars, systemId, comp, SC.TempVal.molecule);
   if (!Vars.device_FF.noCharges && SC.hasPartialCharge[comp]) Update_Vector_Ewald(Sims.Box, false, SC, comp);
 }
@@ -1182,7 +1217,7 @@ MoveEnergy RunMoves(Variables& Vars, size_t systemId, size_t comp) {
   Components& SC = Vars.SystemComponents[systemId];
   Move_Statistics& MS = SC.Moves[comp];
   uint32_t w[4];
-  grx_draw(Vars.Random.Seed, Vars.Random.Stream, SC.Step, GRX_SLOT_MOVE, w);
+  grx_draw(Vars.Random.Seed, Vars.Random.BoxStream(systemId), SC.Step, GRX_SLOT_MOVE, w);
   const size_t N = SC.NumberOfMolecule_for_Component[comp];
   SC.TempVal.component = comp;
   SC.TempVal.molecule = (size_t)(grx_u01(w[0]) * (double)N);
@@ -1199,6 +1234,8 @@ MoveEnergy RunMoves(Variables& Vars, size_t systemId, size_t comp) {
       ReinsertionMove m;
       dE = m.Run(Vars, systemId, uacc);
     }
+  } else if (r < MS.IdentitySwapProb) {
+    dE = IdentitySwapMove(Vars, systemId);
   } else if (r < MS.SwapProb) {
     if (grx_u01(w[2]) < 0.5) {
       InsertionMove m;
@@ -1211,6 +1248,163 @@ MoveEnergy RunMoves(Variables& Vars, size_t systemId, size_t comp) {
   SC.deltaE += dE;
   SC.Step++;
   return dE;
+}
+
+// ------------------------------------------------------------------ identity swap, Gibbs transfer
+static std::vector<double> flat_positions(const std::vector<double3>& p) {
+  std::vector<double> f(3 * p.size());
+  for (size_t a = 0; a < p.size(); ++a) {
+    f[3 * a] = p[a].x; f[3 * a + 1] = p[a].y; f[3 * a + 2] = p[a].z;
+  }
+  return f;
+}
+
+// IdentitySwapMove (mc_swap_moves.h:199-420). The reference redraws the old and the new
+// component together until the old one holds a molecule, so the old component is uniform over
+// the adsorbate components that hold molecules and the new one uniform over all adsorbate
+// components; one Philox draw (GRX_SLOT_SWAP) gives both here.
+MoveEnergy IdentitySwapMove(Variables& Vars, size_t systemId) {
+  Components& SC = Vars.SystemComponents[systemId];
+  Simulations& Sims = Vars.Sims[systemId];
+  const size_t c0 = (size_t)SC.NComponents.y, nc = (size_t)SC.NComponents.x;
+  std::vector<size_t> have;
+  for (size_t c = c0; c < nc; ++c)
+    if (SC.NumberOfMolecule_for_Component[c] > 0) have.push_back(c);
+  if (have.empty()) return MoveEnergy();
+  uint32_t w[4];
+  grx_draw(Vars.Random.Seed, Vars.Random.BoxStream(systemId), SC.Step, GRX_SLOT_SWAP, w);
+  const size_t OLD = have[std::min(have.size() - 1, (size_t)(grx_u01(w[0]) * (double)have.size()))];
+  const size_t NEW = c0 + std::min(nc - c0 - 1, (size_t)(grx_u01(w[1]) * (double)(nc - c0)));
+  const size_t oldmol = (size_t)(grx_u01(w[2]) * (double)SC.NumberOfMolecule_for_Component[OLD]);
+  const size_t newmol = SC.NumberOfMolecule_for_Component[NEW];
+  const size_t ms_old = SC.Moleculesize[OLD], ms_new = SC.Moleculesize[NEW];
+  if (SC.TailCorrectionInsert[OLD] != 0.0 || SC.TailCorrectionInsert[NEW] != 0.0)
+    throw std::runtime_error("IdentitySwapMove: tail corrections are not supported on this path");
+  for (size_t c : {OLD, NEW}) {
+    SC.Moves[c].IdentitySwap_Total_TO.resize(nc, 0);
+    SC.Moves[c].IdentitySwap_Acc_TO.resize(nc, 0);
+  }
+  SC.Moves[OLD].IdentitySwapRemoveTotal++;
+  SC.Moves[NEW].IdentitySwapAddTotal++;
+  SC.Moves[OLD].IdentitySwap_Total_TO[NEW]++;
+  Components::IdentitySwapRecord& rec = SC.LastIdentitySwap;
+  rec = Components::IdentitySwapRecord{};
+  rec.OldComponent = OLD;
+  rec.NewComponent = NEW;
+  rec.OldMolecule = oldmol;
+
+  // the new species grown on the old molecule's first bead, the old molecule excluded
+  SC.TempVal.component = NEW;
+  SC.TempVal.molecule = newmol;
+  SC.TempVal.Scale = double2{1.0, 1.0};
+  CBMC_Variables ins;
+  ins.MoveType = IDENTITY_SWAP_NEW;
+  Sims.New.pos[0] = Sims.d_a[OLD].pos[oldmol * ms_old];
+  Sims.ExcludeComponent = (int)OLD;
+  Sims.ExcludeMolecule = (int64_t)oldmol;
+  Widom_Move_FirstBead_PARTIAL(Vars, systemId, ins);
+  if (ins.SuccessConstruction && ins.Rosenbluth > 1e-150 && ms_new > 1) Widom_Move_Chain_PARTIAL(Vars, systemId, ins);
+  Sims.ExcludeComponent = -1;
+  Sims.ExcludeMolecule = -1;
+  if (!ins.SuccessConstruction || ins.Rosenbluth <= 1e-150) return MoveEnergy();
+  MoveEnergy energy = ins.FirstBeadEnergy + ins.ChainEnergy;
+  std::vector<double3> grown(ms_new);
+  grown[0] = Sims.Old.pos[0];
+  for (size_t a = 1; a < ms_new; ++a) grown[a] = Sims.New.pos[ins.selectedTrialOrientation * (ms_new - 1) + (a - 1)];
+
+  // retrace of the old molecule (trial 0 of each stage is its current configuration)
+  SC.TempVal.component = OLD;
+  SC.TempVal.molecule = oldmol;
+  CBMC_Variables del;
+  del.MoveType = IDENTITY_SWAP_OLD;
+  Widom_Move_FirstBead_PARTIAL(Vars, systemId, del);
+  if (del.SuccessConstruction && ms_old > 1) Widom_Move_Chain_PARTIAL(Vars, systemId, del);
+  if (!del.SuccessConstruction) return MoveEnergy();
+  energy -= del.FirstBeadEnergy + del.ChainEnergy;
+
+  if (!Vars.device_FF.noCharges) {
+    const double2 E = GPU_EwaldDifference_IdentitySwap(Sims, Vars.device_FF, SC, OLD, NEW, oldmol * ms_old, grown);
+    energy.GGEwaldE = E.x;
+    energy.HGEwaldE = E.y;
+    rec.Ewald = E;
+    ins.Rosenbluth *= std::exp(-SC.Beta * (E.x + E.y));
+  }
+  const double pre = GetPrefactor(SC, Sims, NEW, INSERTION) * GetPrefactor(SC, Sims, OLD, DELETION);
+  const double pacc = pre * (ins.Rosenbluth / SC.IdealRosenbluthWeight[NEW]) /
+                      (del.Rosenbluth / SC.IdealRosenbluthWeight[OLD]);
+  rec.RosenbluthNew = ins.Rosenbluth;
+  rec.RosenbluthOld = del.Rosenbluth;
+  rec.Pacc = pacc;
+  if (!(grx_u01(w[3]) < pacc)) return MoveEnergy();
+  if (NEW != OLD && (newmol + 1) * ms_new > SC.Allocate_size[NEW]) return MoveEnergy();  // no room: refused
+  rec.Accepted = true;
+  if (NEW != OLD) {
+    remove_molecule(Vars, systemId, OLD, oldmol);
+    write_molecule(Vars, systemId, NEW, newmol, flat_positions(grown));
+  } else {
+    write_molecule(Vars, systemId, OLD, oldmol, flat_positions(grown));
+  }
+  if (!Vars.device_FF.noCharges && (SC.hasPartialCharge[NEW] || SC.hasPartialCharge[OLD]))
+    Update_Vector_Ewald(Sims.Box, false, SC, NEW);
+  SC.Moves[NEW].IdentitySwapAddAccepted++;
+  SC.Moves[OLD].IdentitySwapRemoveAccepted++;
+  SC.Moves[OLD].IdentitySwap_Acc_TO[NEW]++;
+  return energy;
+}
+
+// GibbsParticleTransfer (mc_swap_moves.h:51-176). The box choice, the molecule to delete and the
+// acceptance come from box 0's move counter (GRX_SLOT_GIBBS); each growth draws from its own
+// box's stream and counter, and both counters advance. Fractional (CB/CFC) molecules are not
+// transferred on this path.
+bool GibbsParticleTransfer(Variables& Vars, size_t comp, Gibbs& G) {
+  if (Vars.SystemComponents.size() < 2) throw std::runtime_error("GibbsParticleTransfer: two boxes needed");
+  uint32_t w[4];
+  grx_draw(Vars.Random.Seed, Vars.Random.BoxStream(0), Vars.SystemComponents[0].Step, GRX_SLOT_GIBBS, w);
+  G.GibbsXferStats[0] += 1.0;
+  const size_t A = grx_u01(w[0]) > 0.5 ? 1 : 0, B = 1 - A;  // insert into A, delete from B
+  Gibbs::TransferRecord& rec = G.LastTransfer;
+  rec = Gibbs::TransferRecord{};
+  rec.InsertionBox = A;
+  Components& SA = Vars.SystemComponents[A];
+  Components& SB = Vars.SystemComponents[B];
+  bool accept = false;
+  if (SB.NumberOfMolecule_for_Component[comp] >= 1) {
+    SA.TempVal.component = comp;
+    SA.TempVal.molecule = SA.NumberOfMolecule_for_Component[comp];
+    SA.TempVal.Scale = double2{1.0, 1.0};
+    InsertionMove ins;
+    ins.Initialize();
+    ins.Calculate(Vars, A);
+    if (ins.InsertionVariables.SuccessConstruction) {
+      SB.TempVal.component = comp;
+      SB.TempVal.molecule = (size_t)(grx_u01(w[1]) * (double)SB.NumberOfMolecule_for_Component[comp]);
+      SB.TempVal.Scale = double2{1.0, 1.0};
+      DeletionMove del;
+      del.Initialize();
+      del.Calculate(Vars, B);
+      if (del.DeletionVariables.SuccessConstruction) {
+        const double NA = molecules_in_box(SA), NB = molecules_in_box(SB);
+        const double pacc = (ins.InsertionVariables.Rosenbluth * NB * Vars.Sims[A].Box.Volume) /
+                            (del.DeletionVariables.Rosenbluth * (NA + 1.0) * Vars.Sims[B].Box.Volume);
+        const size_t N = SA.NumberOfMolecule_for_Component[comp];
+        accept = grx_u01(w[2]) < pacc && (N + 1) * SA.Moleculesize[comp] <= SA.Allocate_size[comp];
+        rec.DeletedMolecule = SB.TempVal.molecule;
+        rec.RosenbluthInsertion = ins.InsertionVariables.Rosenbluth;
+        rec.RosenbluthDeletion = del.DeletionVariables.Rosenbluth;
+        rec.Pacc = pacc;
+        rec.Accepted = accept;
+        if (accept) {
+          ins.Commit(Vars, A);
+          del.Commit(Vars, B);
+          SA.deltaE += ins.energy;
+          SB.deltaE += del.energy;
+          G.GibbsXferStats[1] += 1.0;
+        }
+      }
+    }
+  }
+  for (Components& C : Vars.SystemComponents) C.Step++;
+  return accept;
 }
 
 // ------------------------------------------------------------------ Widom statistics
@@ -1263,7 +1457,7 @@ static grx_gcmc_desc device_desc(Variables& Vars, size_t systemId, size_t comp) 
   d.ideal_rosenbluth = SC.IdealRosenbluthWeight[comp];
   d.tail_insert = SC.TailCorrectionInsert.empty() ? 0.0 : SC.TailCorrectionInsert[comp];
   d.seed = Vars.Random.Seed;
-  d.stream = Vars.Random.Stream;
+  d.stream = Vars.Random.BoxStream(systemId);
   return d;
 }
 
@@ -1311,7 +1505,7 @@ grx_gcmc_stats RunMoves_Device(Variables& Vars, size_t systemId, size_t comp, in
   d.ideal_rosenbluth = SC.IdealRosenbluthWeight[comp];
   d.tail_insert = SC.TailCorrectionInsert.empty() ? 0.0 : SC.TailCorrectionInsert[comp];
   d.seed = Vars.Random.Seed;
-  d.stream = Vars.Random.Stream;
+  d.stream = Vars.Random.BoxStream(systemId);
   grx_gcmc_stats st{};
   grx_box* b = Sims.Box.handle;
   check(grx_gcmc_run(&b, 1, &d, nullptr, SC.Step, nsteps, Vars.Precision, &st), "grx_gcmc_run");

@@ -122,12 +122,16 @@ struct CBMC_Variables {
 
 struct Move_Statistics {
   double TranslationProb = 0.0, RotationProb = 0.0, ReinsertionProb = 0.0, SwapProb = 0.0;
+  double IdentitySwapProb = 0.0;         // cumulative, between reinsertion and swap (0: none)
   size_t NumberOfTrials = 10;            // first-bead trials of the CBMC moves
   size_t TranslationTotal = 0, TranslationAccepted = 0;
   size_t RotationTotal = 0, RotationAccepted = 0;
   size_t InsertionTotal = 0, InsertionAccepted = 0;
   size_t DeletionTotal = 0, DeletionAccepted = 0;
   size_t ReinsertionTotal = 0, ReinsertionAccepted = 0;
+  size_t IdentitySwapRemoveTotal = 0, IdentitySwapRemoveAccepted = 0;  // this component swapped out
+  size_t IdentitySwapAddTotal = 0, IdentitySwapAddAccepted = 0;        // this component swapped in
+  std::vector<size_t> IdentitySwap_Total_TO, IdentitySwap_Acc_TO;      // per target component
   double3 MaxTranslation{1.0, 1.0, 1.0};
   double3 MaxRotation{0.5, 0.5, 0.5};
   void Record_Move_Total(int move);
@@ -174,6 +178,12 @@ struct Components {
   double VolumeMoveLastV = 0.0;                      // the last volume trial (reporting):
   MoveEnergy VolumeMoveLastE;                        //   its volume, FP64 totals and overlap flag
   bool VolumeMoveLastOverlap = false;
+  struct IdentitySwapRecord {                        // the last identity swap (reporting)
+    size_t OldComponent = 0, NewComponent = 0, OldMolecule = 0;
+    double RosenbluthNew = 0.0, RosenbluthOld = 0.0, Pacc = 0.0;  // 0 where the move stopped early
+    double2 Ewald;                                                // {GGEwaldE, HGEwaldE} of the trial
+    bool Accepted = false;
+  } LastIdentitySwap;
   MoveEnergy deltaE;                                 // running sum of accepted move energies
   uint64_t Step = 0;                                 // Philox move index of the next move
 };
@@ -196,6 +206,9 @@ struct WidomStruct {
 struct RandomNumber {
   uint64_t Seed = 42;
   uint32_t Stream = 0;
+  // Box b of a multi-box system draws from stream Stream + b * 2^24, so boxes at the same
+  // move index never share a random number (box 0 keeps Stream).
+  uint32_t BoxStream(size_t systemId) const { return Stream + ((uint32_t)systemId << 24); }
 };
 
 struct Variables {
@@ -242,10 +255,22 @@ double2 GPU_EwaldDifference_IdentitySwap(Simulations& Sims, ForceField& FF, Comp
 // exchanges volume between boxes 0 and 1 at fixed total volume.
 struct Gibbs {
   double MaxGibbsBoxChange = 0.1;
-  double GibbsBoxStats[2] = {0.0, 0.0};  // attempts, accepted
+  double GibbsBoxStats[2] = {0.0, 0.0};  // volume exchanges: attempts, accepted
+  double GibbsXferStats[2] = {0.0, 0.0};  // particle transfers: attempts, accepted
+  struct TransferRecord {                  // the last particle transfer (reporting)
+    size_t InsertionBox = 0, DeletedMolecule = 0;
+    double RosenbluthInsertion = 0.0, RosenbluthDeletion = 0.0, Pacc = 0.0;
+    bool Accepted = false;
+  } LastTransfer;
 };
 void VolumeMove(Variables& Vars, size_t systemId);
 void NVTGibbsMove(Variables& Vars, Gibbs& GibbsStatistics);
+// GibbsParticleTransfer (mc_swap_moves.h:51-176): a CBMC insertion of `comp` into one box
+// and a CBMC deletion from the other, accepted together. Returns true when accepted.
+bool GibbsParticleTransfer(Variables& Vars, size_t comp, Gibbs& GibbsStatistics);
+// IdentitySwapMove (mc_swap_moves.h:199-420): one adsorbate molecule replaced by a molecule
+// of another (or the same) adsorbate component grown on its first bead.
+MoveEnergy IdentitySwapMove(Variables& Vars, size_t systemId);
 
 // Energy of a lambda change of one molecule (mc_cbcfc.h:20-124): pair part over every other
 // atom at fixed positions, Fourier part and tail; SuccessConstruction is false on overlap.
@@ -275,6 +300,7 @@ struct InsertionMove {
   void Initialize();
   void Calculate(Variables& Vars, size_t systemId);
   void Acceptance(Variables& Vars, size_t systemId, double RANDOM);
+  void Commit(Variables& Vars, size_t systemId);   // store the grown molecule, commit S(k)
   MoveEnergy Run(Variables& Vars, size_t systemId, double RANDOM);
   double WidomMove(Variables& Vars, size_t systemId);
 };
@@ -287,6 +313,7 @@ struct DeletionMove {
   void Initialize();
   void Calculate(Variables& Vars, size_t systemId);
   void Acceptance(Variables& Vars, size_t systemId, double RANDOM);
+  void Commit(Variables& Vars, size_t systemId);   // remove the molecule, commit S(k)
   MoveEnergy Run(Variables& Vars, size_t systemId, double RANDOM);
 };
 

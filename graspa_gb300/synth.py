@@ -79,6 +79,9 @@ def co2_template():
                 charge=np.array([0.70, -0.35, -0.35]), names=["C_co2", "O_co2", "O_co2"])
 
 
+SILICA_CO2_TYPES = [("Si", 22.0, 2.30), ("O", 53.0, 3.30), ("C_co2", 27.0, 2.80), ("O_co2", 79.0, 3.05)]
+
+
 def silica_co2(seed=42, cells=(2, 2, 3), cutoff=12.0, alpha=0.265, kmax=(9, 9, 6), n_co2=0):
     """Widom / GCMC system of the CO2 + synthetic all-silica configuration.
 
@@ -122,10 +125,10 @@ def silica_co2(seed=42, cells=(2, 2, 3), cutoff=12.0, alpha=0.265, kmax=(9, 9, 6
     fw = np.concatenate([si, oxy])
     fw = fw - L * np.floor(fw / L)
     nsi, no = len(si), len(oxy)
-    names = ["Si", "O", "C_co2", "O_co2"]
-    eps_K = [22.0, 53.0, 27.0, 79.0]
-    sig = [2.30, 3.30, 2.80, 3.05]
-    eps, sg, shift = mix_lorentz_berthelot(eps_K, sig, [1, 1, 1, 1], cutoff)
+    names = [n for n, _, _ in SILICA_CO2_TYPES]
+    eps_K = [e for _, e, _ in SILICA_CO2_TYPES]
+    sig = [x for _, _, x in SILICA_CO2_TYPES]
+    eps, sg, shift = mix_lorentz_berthelot(eps_K, sig, [1] * len(eps_K), cutoff)
     fw_type = np.array([0] * nsi + [1] * no)
     fw_q = np.array([2.05] * nsi + [-1.025] * no)
     tmpl = co2_template()
@@ -140,6 +143,29 @@ def silica_co2(seed=42, cells=(2, 2, 3), cutoff=12.0, alpha=0.265, kmax=(9, 9, 6
     if n_co2:
         place_molecules(system, 1, n_co2, g)
     return system
+
+
+def silica_co2_n2(seed=42, n_co2=0, n_n2=0):
+    """The CO2 + silica system of silica_co2 with a second charged, rigid adsorbate: N2
+    (two N sites, 36 K / 3.31 A, q -0.482 at +/-0.55 A, and a charge-only centre +0.964;
+    the first N is the CBMC first bead). Components: 0 framework, 1 CO2, 2 N2."""
+    s = silica_co2(seed=seed)
+    nfw = s["comp_start"][1]
+    sites = SPECIES["N2"]
+    types = SILICA_CO2_TYPES + [("N_n2", 36.0, 3.31), ("N_com", 0.0, 1.0)]
+    eps, sg, shift = mix_lorentz_berthelot([e for _, e, _ in types], [x for _, _, x in types], [1] * len(types),
+                                           s["cutoff_vdw"])
+    s.update(name="co2_n2_silica", ntypes=len(types), type_names=[n for n, _, _ in types], epsilon=eps, sigma=sg,
+             shift=shift, molsize=[nfw, 3, 3])
+    s["templates"][2] = dict(pos=np.array([p for (_, _, _, _, p) in sites]),
+                             charge=np.array([q for (_, _, _, q, _) in sites]), type=np.array([4, 4, 5]))
+    _set_atoms(s, s["pos"][:nfw], s["type"][:nfw], s["charge"][:nfw], [np.zeros((0, 3)), np.zeros((0, 3))])
+    g = _rng(seed + 104729)
+    if n_co2:
+        place_molecules(s, 1, n_co2, g)
+    if n_n2:
+        place_molecules(s, 2, n_n2, g)
+    return s
 
 
 def _set_atoms(system, fw_pos, fw_type, fw_q, guest_pos_list):

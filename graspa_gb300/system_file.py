@@ -65,6 +65,7 @@ def write_system(path, system, capacity, desc, precision=grx.GRX_FP64, first_ste
     L.append(f"fugacity_coeff {desc.fugacity_coeff!r}")
     L.append(f"mol_fraction {desc.mol_fraction!r}")
     L.append(f"ideal_rosenbluth {desc.ideal_rosenbluth!r}")
+    L.append(f"tail_insert {desc.tail_insert!r}")
     L.append(f"ntrials {desc.ntrials}")
     L.append(f"norient {desc.norient}")
     L.append(f"cumulative_probabilities {desc.p_translation!r} {desc.p_rotation!r} {desc.p_reinsertion!r} "
@@ -97,10 +98,17 @@ def parse_driver_output(text):
             out.setdefault("volume", []).append([float(x) for x in parts[2:]])
         elif k == "lambda":  # step, constructed, HGVDW HGReal GGVDW GGReal GGEwald HGEwald Tail total
             out.setdefault("lambda", []).append([float(x) for x in parts[2:]])
-        elif k == "positions":
+        elif k == "transfer":  # move, insertion box, deleted molecule, accepted, W_ins, W_del, Pacc, N0, N1
+            out.setdefault("transfer", []).append([float(x) for x in parts[2:]])
+        elif k == "swap":  # move, old comp, new comp, old molecule, accepted, W_new, W_old, Pacc, GGEwald, HGEwald
+            out.setdefault("swap", []).append([float(x) for x in parts[2:]])
+        elif k == "count":  # component: molecules, identity swaps in, identity swaps out
+            out.setdefault("count", {})[int(parts[1])] = [int(x) for x in parts[2:]]
+        elif k == "positions":  # one block per printed component; "positions" is the first
             n = int(parts[1])
-            out["positions"] = np.array([[float(x) for x in lines[i + 1 + j].split()] for j in range(n)]
-                                        ).reshape(-1, 3)
+            p = np.array([[float(x) for x in lines[i + 1 + j].split()] for j in range(n)]).reshape(-1, 3)
+            out.setdefault("positions", p)
+            out.setdefault("positions_all", []).append(p)
             i += n
         elif k == "mode":
             out["mode"] = parts[1]

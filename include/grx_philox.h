@@ -19,6 +19,10 @@
  *   GRX_SLOT_MOVE         {molecule pick, move choice, insertion-vs-deletion, acceptance}
  *   GRX_SLOT_DISP         {three displacement / rotation-angle uniforms}
  *   GRX_SLOT_VOLUME       {volume change, acceptance, Gibbs box choice} of a volume move
+ *   GRX_SLOT_SWAP         {old component, new component, old molecule, acceptance} of an
+ *                         identity swap
+ *   GRX_SLOT_GIBBS        {box choice, deletion molecule, acceptance} of a Gibbs particle
+ *                         transfer
  */
 #ifndef GRX_PHILOX_H
 #define GRX_PHILOX_H
@@ -31,6 +35,8 @@
 #define GRX_SLOT_MOVE 4096u
 #define GRX_SLOT_DISP 4097u
 #define GRX_SLOT_VOLUME 4098u
+#define GRX_SLOT_SWAP 4099u
+#define GRX_SLOT_GIBBS 4100u
 
 static inline void grx_philox4x32_10(uint32_t c[4], uint32_t k0, uint32_t k1) {
   for (int r = 0; r < 10; ++r) {

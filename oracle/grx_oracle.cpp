@@ -1163,6 +1163,7 @@ extern "C" void ora_gcmc_run_mix(const ora_box* box, const ora_ff* ff, double* p
           ew = same + 2.0 * d2[1];
           rosen *= std::exp(-g->beta * ew);
         }
+        rosen *= std::exp(-g->beta * g->tail_insert);  // Insertion_Body (mc_swap_utilities.h:105-108)
         const double pre = g->beta * bigP / (1.0 + (double)N);  // GetPrefactor INSERTION
         const double pacc = pre * rosen / g->ideal_rosenbluth;
         if (rosen > 1e-150 && uacc < pacc) {
@@ -1205,6 +1206,9 @@ extern "C" void ora_gcmc_run_mix(const ora_box* box, const ora_ff* ff, double* p
           ew = same + 2.0 * d2[1];
           rosen /= std::exp(-g->beta * ew);
         }
+        // Deletion_Body (mc_swap_utilities.h:197-200): the weight is divided by
+        // exp(-beta TailE) with TailE the deletion difference, -tail_insert here
+        rosen /= std::exp(-g->beta * -g->tail_insert);
         const double pre = (double)N / (g->beta * bigP);  // GetPrefactor DELETION
         const double pacc = pre * g->ideal_rosenbluth / rosen;
         if (uacc < pacc) {

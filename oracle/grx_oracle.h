@@ -194,6 +194,8 @@ typedef struct {
   uint64_t seed;
   uint32_t stream;
   uint32_t pad_;
+  double tail_insert;     /* TailCorrectionDifference of one insertion; a deletion
+                             takes its negative (exact for a host-guest tail) */
 } ora_gcmc;
 
 typedef struct {

@@ -64,7 +64,8 @@ class OraGcmc(C.Structure):
                 ("p_swap", C.c_double), ("max_translation", C.c_double * 3), ("max_rotation", C.c_double * 3),
                 ("beta", C.c_double),
                 ("pressure", C.c_double), ("fugacity_coeff", C.c_double), ("mol_fraction", C.c_double),
-                ("ideal_rosenbluth", C.c_double), ("seed", C.c_uint64), ("stream", C.c_uint32), ("pad_", C.c_uint32)]
+                ("ideal_rosenbluth", C.c_double), ("seed", C.c_uint64), ("stream", C.c_uint32), ("pad_", C.c_uint32),
+                ("tail_insert", C.c_double)]
 
 
 class OraGcmcStats(C.Structure):

@@ -44,6 +44,7 @@ def ora_params(d):
     g.beta, g.pressure = d.beta, d.pressure
     g.fugacity_coeff, g.mol_fraction, g.ideal_rosenbluth = d.fugacity_coeff, d.mol_fraction, d.ideal_rosenbluth
     g.seed, g.stream = d.seed, d.stream
+    g.tail_insert = d.tail_insert
     return g
 
 
@@ -83,6 +84,21 @@ def test_gcmc_fp64_matches_oracle(grx_lib, n_co2):
     assert np.max(np.abs(got - ref)) <= 1e-9
     for k in range(4):
         assert abs(st.energy[k] - ost.energy[k]) <= 1e-9 * max(1.0, abs(ost.energy[k]))
+
+
+@pytest.mark.parametrize("prec", ["GRX_FP64", "GRX_MIXED"])
+def test_gcmc_tail_correction_matches_oracle(grx_lib, prec):
+    """A tail correction on insertion and deletion (the deletion takes the negative
+    difference, mc_swap_utilities.h:197-200): the same decisions as the oracle."""
+    s = co2_system(n_co2=5)
+    d = params(grx_lib, pressure_pa=1e6, tail_insert=-200.0)
+    box, st, ost, after = run_pair(grx_lib, s, d, 400, getattr(grx_lib, prec))
+    assert list(st.attempts) == list(ost.attempts) and list(st.accepted) == list(ost.accepted)
+    assert st.n_molecules == ost.n_molecules
+    nfw = s["comp_start"][1]
+    assert np.max(np.abs(box.positions(1) - after["pos"][nfw:])) <= 1e-9
+    free = run_pair(grx_lib, s, params(grx_lib, pressure_pa=1e6), 400, grx_lib.GRX_FP64)[1]
+    assert st.n_molecules > free.n_molecules
 
 
 def test_gcmc_mixed_matches_oracle(grx_lib):

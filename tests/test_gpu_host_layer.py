@@ -34,10 +34,10 @@ def run_driver(tmp_path, s, d, mode, n, prec=grx.GRX_FP64):
     return system_file.parse_driver_output(r.stdout)
 
 
-@pytest.mark.parametrize("mode", ["host", "device"])
-def test_host_layer_gcmc_matches_oracle(grx_lib, tmp_path, mode):
+@pytest.mark.parametrize("mode,tail", [("host", 0.0), ("device", 0.0), ("host", -200.0), ("device", -200.0)])
+def test_host_layer_gcmc_matches_oracle(grx_lib, tmp_path, mode, tail):
     s = co2_system(n_co2=4)
-    d = params(grx_lib, pressure_pa=1e6)
+    d = params(grx_lib, pressure_pa=1e6, tail_insert=tail)
     out = run_driver(str(tmp_path), s, d, mode, 150)
     ost, after, _ = O.OracleSystem(s).gcmc(ora_params(d), [s["comp_start"][1], CAP], 0, 150)
     assert out["attempts"] == list(ost.attempts)
@@ -181,5 +181,119 @@ def test_host_layer_gibbs_volume_exchange(grx_lib, tmp_path):
     for va, vb in out["gibbs"]:
         assert abs((va + vb) - 2 * V0) <= 1e-9 * V0
     assert out["gibbs_attempts"] == 6.0
+    tol = 1e-8 * out["energy_scale"] + 1e-6
+    assert abs(out["drift"]) <= tol and abs(out["drift_b"]) <= tol
+
+
+def _rotate(v, u, w1, w2):
+    import ctypes
+    a = np.ascontiguousarray(v, dtype=np.float64).copy()
+    O.lib().ora_rotate_quaternion(O._d(a), ctypes.c_double(u), ctypes.c_double(w1), ctypes.c_double(w2))
+    return a
+
+
+def _close(a, b, tol=1e-9):
+    return abs(a - b) <= tol * max(abs(b), 1e-300)
+
+
+def test_host_layer_identity_swap(grx_lib, tmp_path):
+    """IdentitySwapMove (mc_swap_moves.h:199-420) in a CO2 + N2 mixture through the host layer.
+    The first move is recomputed with the oracle: component and molecule picks from the Philox
+    draw; the new species' single first-bead trial on the old molecule's first bead with the old
+    molecule excluded (not averaged); its orientations (stored molecule 0 rotated by the
+    orientation draws) and their selection; the old molecule's retrace (trial 0 its current
+    configuration, the others from the retrace draws); the identity-swap Fourier delta; then
+    Pacc = N_old / (N_new + 1) * W_new / W_old. Weights, Pacc and the Fourier delta agree to
+    1e-9 and the decision is the same. Over the run the molecule count is conserved and the
+    accepted energies match the recomputed FP64 totals."""
+    from graspa_gb300 import synth
+    s = synth.silica_co2_n2(n_co2=4, n_n2=4)
+    d = params(grx_lib, pressure_pa=1e6)
+    f = os.path.join(str(tmp_path), "system.txt")
+    cs = s["comp_start"]
+    system_file.write_system(f, s, [cs[1], CAP, CAP], d, precision=grx.GRX_FP64)
+    r = subprocess.run([B.DRIVER, f, "swap", "60"], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    out = system_file.parse_driver_output(r.stdout)
+    beta = d.beta
+    P, Q, T = s["pos"], s["charge"], s["type"]
+    w = O.draw(d.seed, d.stream, 0, 4099)
+    old = [1, 2][min(1, int(O.u01(w[0]) * 2))]
+    new = 1 + min(1, int(O.u01(w[1]) * 2))
+    oldmol = int(O.u01(w[2]) * 4)
+    row = out["swap"][0]
+    assert (int(row[0]), int(row[1]), int(row[2])) == (old, new, oldmol)
+    S = O.OracleSystem(s)
+    o0 = cs[old] + 3 * oldmol
+    old_pos, old_q, old_t = P[o0:o0 + 3], Q[o0:o0 + 3], T[o0:o0 + 3]
+    new_q, new_t = Q[cs[new]:cs[new] + 3], T[cs[new]:cs[new] + 3]
+    fb = old_pos[0]
+    # growth of the new species: one first-bead trial, ten orientations, the old molecule excluded
+    e, fl = S.trial_energies(fb, [1.0], [new_q[0]], [1.0], [new_t[0]], 4, 1, 1, new, old, oldmol)
+    assert fl[0] == 0
+    W_new = np.exp(-beta * e[0].sum())
+    vec = P[cs[new] + 1:cs[new] + 3] - P[cs[new]]
+    tp = []
+    for o in range(10):
+        wo = O.draw(d.seed, d.stream, 0, 1024 + o)
+        tp += [fb + _rotate(vec[a], O.u01(wo[0]), O.u01(wo[1]), O.u01(wo[2])) for a in range(2)]
+    e, fl = S.trial_energies(np.array(tp), np.ones(20), np.tile(new_q[1:], 10), np.ones(20), np.tile(new_t[1:], 10),
+                             4, 10, 2, new, old, oldmol)
+    ok = np.flatnonzero(fl == 0)
+    lw = -beta * e[ok].sum(1)
+    orient = ok[O.select_trial(lw, O.u01(O.draw(d.seed, d.stream, 0, 2048)[1]))]
+    W_new *= np.exp(lw).sum() / 10
+    grown = np.array([fb, tp[2 * orient], tp[2 * orient + 1]])
+    # retrace of the old molecule
+    e, fl = S.trial_energies(fb, [1.0], [old_q[0]], [1.0], [old_t[0]], oldmol, 1, 1, old)
+    W_old = np.exp(-beta * e[0].sum())
+    vec = P[cs[old] + 1:cs[old] + 3] - P[cs[old]]
+    tp = [old_pos[1], old_pos[2]]
+    for o in range(1, 10):
+        wo = O.draw(d.seed, d.stream, 0, 3072 + o)
+        tp += [fb + _rotate(vec[a], O.u01(wo[0]), O.u01(wo[1]), O.u01(wo[2])) for a in range(2)]
+    e, fl = S.trial_energies(np.array(tp), np.ones(20), np.tile(old_q[1:], 10), np.ones(20), np.tile(old_t[1:], 10),
+                             oldmol, 10, 2, old)
+    W_old *= np.exp(-beta * e[fl == 0].sum(1)).sum() / 10
+    # Fourier delta: the old molecule out, the grown one in (rigid exclusions of both species)
+    _, s_fw, s_ads = S.ewald_total([cs[1], 3, 3])
+    ex = {c: sum(S.rigid_exclusion(P[cs[c]:cs[c] + 3], Q[cs[c]:cs[c] + 3], np.ones(3))) for c in (1, 2)}
+    ew, _ = S.ewald_delta_identity_swap(s_ads, s_fw, old_pos, old_q, grown, new_q, ex[new], ex[old])
+    W_new *= np.exp(-beta * (ew[0] + ew[1]))
+    pacc = 4.0 / 5.0 * W_new / W_old
+    assert _close(row[4], W_new) and _close(row[5], W_old) and _close(row[6], pacc)
+    assert _close(row[7], ew[0]) and _close(row[8], ew[1])
+    assert row[3] == float(O.u01(w[3]) < pacc)
+    # the run: counts conserved, swaps accepted both ways, drift
+    counts = out["count"]
+    assert counts[1][0] + counts[2][0] == 8
+    assert counts[1][1] + counts[2][1] >= 2 and counts[1][1] + counts[2][1] == counts[1][2] + counts[2][2]
+    assert abs(out["drift"]) <= 1e-8 * max(1.0, abs(out["energy_sum"])) + 1e-6
+
+
+def test_host_layer_gibbs_particle_transfer(grx_lib, tmp_path):
+    """GibbsParticleTransfer (mc_swap_moves.h:51-176) between a CO2 box and an identical copy.
+    First move: the box choice and the deleted molecule follow the Philox draw; the insertion
+    weight equals the device Widom kernel's weight for the inserting box's stream (box b draws
+    from stream + b * 2^24) and move index; Pacc = W_ins N_B V_A / (W_del (N_A + 1) V_B) and the
+    decision follows it. Over the run the total count is conserved, transfers are accepted and
+    both boxes' accepted energies match their recomputed totals."""
+    s = co2_system(n_co2=8)
+    d = params(grx_lib, pressure_pa=1e6)
+    out = run_driver(str(tmp_path), s, d, "transfer", 40)
+    w = O.draw(d.seed, d.stream, 0, 4100)
+    A = 1 if O.u01(w[0]) > 0.5 else 0
+    row = out["transfer"][0]
+    assert int(row[0]) == A and int(row[1]) == int(O.u01(w[1]) * 8)
+    box = grx_lib.Box(s, capacity=[s["comp_start"][1], CAP])
+    box.ewald_total()
+    wd = grx_lib.widom_desc(s, 1, ntrials=d.ntrials, norient=d.norient, seed=d.seed, stream=d.stream + (A << 24))
+    res = box.widom(wd, 0, 1, grx_lib.GRX_FP64)
+    assert res["success"][0] != 0 and _close(row[3], res["rosenbluth"][0], 1e-10)
+    pacc = row[3] * 8 / (row[4] * 9)
+    assert _close(row[5], pacc, 1e-12) and row[2] == float(O.u01(w[2]) < pacc)
+    for r in out["transfer"]:
+        assert r[6] + r[7] == 16
+    assert out["transfer_attempts"] == 40.0 and out["transfer_accepted"] >= 1
     tol = 1e-8 * out["energy_scale"] + 1e-6
     assert abs(out["drift"]) <= tol and abs(out["drift_b"]) <= tol

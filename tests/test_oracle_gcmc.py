@@ -53,3 +53,23 @@ def test_gcmc_deterministic_and_resumable():
     c2, end, _ = O.OracleSystem(mid).gcmc(gcmc_params(), cap, 60, 60)
     assert np.allclose(end["pos"], sa["pos"], rtol=0, atol=1e-9)
     assert c2.n_molecules == a.n_molecules
+
+
+def test_gcmc_tail_correction_sign():
+    """Insertion_Body multiplies the Rosenbluth weight by exp(-beta t) for the insertion
+    tail difference t, and Deletion_Body divides it by exp(-beta TailE) with TailE the
+    deletion difference -t (mc_swap_utilities.h:105-108, 197-200). Both acceptances
+    then carry the factor of a pressure scaled by exp(-beta t): a chain with the tail
+    equals the tail-free chain at that pressure, move for move."""
+    s = synth.silica_co2(n_co2=3)
+    cap = [s["comp_start"][1], 3 * 64]
+    g = gcmc_params(pressure_pa=1e6)
+    t = -200.0  # internal units; beta t ~ -0.8 at 300 K
+    g.tail_insert = t
+    a, sa, _ = O.OracleSystem(s).gcmc(g, cap, 0, 300)
+    p = gcmc_params(pressure_pa=1e6 * np.exp(-g.beta * t))
+    b, sb, _ = O.OracleSystem(s).gcmc(p, cap, 0, 300)
+    c, _, _ = O.OracleSystem(s).gcmc(gcmc_params(pressure_pa=1e6), cap, 0, 300)
+    assert list(a.accepted) == list(b.accepted) and a.n_molecules == b.n_molecules
+    assert np.allclose(sa["pos"], sb["pos"], rtol=0, atol=1e-9)
+    assert a.n_molecules > c.n_molecules  # an attractive tail raises the loading
