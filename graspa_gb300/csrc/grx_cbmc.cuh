@@ -49,6 +49,7 @@ struct CbmcWork {
   // [n_old, n_old + n_new) arrive
   double mx[2 * kMolWork], my[2 * kMolWork], mz[2 * kMolWork], mq[2 * kMolWork];
   double sbuf[32];
+  double ewx[8][2];  // per-CTA Fourier partials {same, cross} of a cluster
   double wsum[2][NW];
   float2 qd[2 * kMolWork];
   int counter;
@@ -132,15 +133,52 @@ __device__ __noinline__ void gen_orientations(const BoxDev& b, WK& W, uint64_t s
 
 // Energies of ntr = nb / chain trials of `chain` beads each (W.beads) against every
 // atom, with the atoms of (comp, newmol) excluded: W.te[4 t + k], W.tflag[t].
-template <int PREC, class WK>
+// With CL > 1 the block is one CTA of a cluster that shares the chain: the pass is split
+// over the cluster's warps (items per warp capped so the slots fit the workspace), each
+// CTA copies its slots into its peers' workspaces, and every CTA reduces all slots. The
+// second cluster barrier keeps a CTA from writing the next pass's slots into a peer that
+// is still reducing this one.
+template <int PREC, int CL = 1, class WK>
 __device__ __noinline__ void trial_pass(const BoxDev& b, WK& W, int nb, int chain, int comp, int newmol) {
   if (threadIdx.x == 0) W.counter = 0;
   __syncthreads();
-  const PassSplit sp = pass_split(b, nb, (int)(blockDim.x >> 5), b.chunk_mult);
-  block_bead_pass<PREC>(b, W.beads, nb, comp, newmol, -1, -1, W.qbuf, W.ipart, W.iflag, &W.counter, sp);
-  __syncthreads();
-  reduce_items<PREC>(W.ipart, W.iflag, nb / chain, chain, sp, W.te, W.tflag);
-  __syncthreads();
+  const int nw = (int)(blockDim.x >> 5);
+  if constexpr (CL == 1) {
+    const PassSplit sp = pass_split(b, nb, nw, b.chunk_mult);
+    block_bead_pass<PREC>(b, W.beads, nb, comp, newmol, -1, -1, W.qbuf, W.ipart, W.iflag, &W.counter, sp);
+    __syncthreads();
+    reduce_items<PREC>(W.ipart, W.iflag, nb / chain, chain, sp, W.te, W.tflag);
+    __syncthreads();
+  } else {
+    const PassSplit sp = pass_split(b, nb, nw * CL, max(1, min(b.chunk_mult, kCbmcMaxMult / CL)));
+    const unsigned rank = cluster_rank();
+    int i0, i1;
+    cluster_items(sp, CL, rank, i0, i1);
+    block_bead_pass<PREC>(b, W.beads, nb, comp, newmol, -1, -1, W.qbuf, W.ipart, W.iflag, &W.counter, sp, i0, i1);
+    __syncthreads();
+    if (sp.nu > 0 && i0 < i1) {  // this CTA's slots [s0, s0 + n): item + bead, increasing
+      unsigned lo, hi;
+      sp.range((unsigned)i0, lo, hi);
+      const int s0 = i0 + (int)(lo / sp.nu);
+      sp.range((unsigned)(i1 - 1), lo, hi);
+      const int n = (i1 - 1) + (int)((hi - 1u) / sp.nu) - s0 + 1;
+      const unsigned long long* src = reinterpret_cast<const unsigned long long*>(W.ipart);
+      for (int k = threadIdx.x; k < (CL - 1) * n * 5; k += blockDim.x) {
+        const int j = k / (n * 5), e = k - j * (n * 5);
+        const unsigned peer = (unsigned)j + ((unsigned)j >= rank ? 1u : 0u);
+        const int slot = s0 + e / 5, f = e % 5;
+        if (f < 4) {
+          cluster_map(reinterpret_cast<unsigned long long*>(W.ipart), peer)[slot * 4 + f] = src[slot * 4 + f];
+        } else {
+          cluster_map(W.iflag, peer)[slot] = W.iflag[slot];
+        }
+      }
+    }
+    cluster_sync_all();
+    reduce_items<PREC>(W.ipart, W.iflag, nb / chain, chain, sp, W.te, W.tflag);
+    __syncthreads();
+    cluster_sync_all();
+  }
 }
 
 // CBMC weight of one growth step (warp 0 computes, results in W.ok/sel/w/nok/wraw).
@@ -229,10 +267,15 @@ __device__ __noinline__ void step_weight(WK& W, int nt, double beta, int bias, d
 // the reference arithmetic; the other forms evaluate dS and both sums in
 // double-float on the FP32 pipe against temp*S tables (ewA, ewF). When s_out is
 // given, S_same + dS is staged there (FP64) for a later commit. Results on thread 0.
-template <int PREC, class WK, bool ROWS = false>
+// With CL > 1 each CTA of the cluster takes a contiguous range of the active k (its
+// range of S is staged, and later committed, by that CTA alone); the CTAs' partial sums
+// are exchanged through distributed shared memory and added in rank order by every CTA.
+template <int PREC, class WK, bool ROWS = false, int CL = 1>
 __device__ __noinline__ void ewald_move(const BoxDev& b, WK& W, int na, double2* eik, double2* s_out,
                                            double& same, double& cross) {
   const int tid = threadIdx.x;
+  int k0 = 0, k1 = b.nact;
+  if constexpr (CL > 1) cluster_k_range(b.nact, CL, cluster_rank(), k0, k1);
   const int kx1 = b.kmax[0] + 1, ky1 = b.kmax[1] + 1;
   double2* ex = eik;
   double2* ey = ex + kx1 * na;
@@ -260,7 +303,7 @@ __device__ __noinline__ void ewald_move(const BoxDev& b, WK& W, int na, double2*
   same = 0.0;
   cross = 0.0;
   if constexpr (PREC == GRX_FP64) {
-    for (int j = tid; j < b.nact; j += blockDim.x) {
+    for (int j = k0 + tid; j < k1; j += blockDim.x) {
       const int4 k = b.kact[j];
       double2 dsk = make_double2(0.0, 0.0);
       for (int at = 0; at < na; ++at) {
@@ -328,7 +371,7 @@ __device__ __noinline__ void ewald_move(const BoxDev& b, WK& W, int na, double2*
         rxy[e] = make_float4(pr.hi, pr.lo, pi.hi, pi.lo);
       }
       __syncthreads();
-      for (int j = tid; j < b.nact; j += blockDim.x) {
+      for (int j = k0 + tid; j < k1; j += blockDim.x) {
         const int4 k = b.kact[j];
         const float4* P = rxy + (k.x * ny + k.y + b.kmax[1]) * na;
         const int az = abs(k.z);
@@ -344,7 +387,7 @@ __device__ __noinline__ void ewald_move(const BoxDev& b, WK& W, int na, double2*
         k_energy(j, k.w, cre, cim);
       }
     } else {
-      for (int j = tid; j < b.nact; j += blockDim.x) {
+      for (int j = k0 + tid; j < k1; j += blockDim.x) {
         const int4 k = b.kact[j];
         df cre = {0.f, 0.f}, cim = {0.f, 0.f};
         const int ay = abs(k.y), az = abs(k.z);
@@ -381,13 +424,32 @@ __device__ __noinline__ void ewald_move(const BoxDev& b, WK& W, int na, double2*
     if (tid == 0)
       for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { same += W.wsum[0][w]; cross += W.wsum[1][w]; }
   }
+  if constexpr (CL > 1) {
+    const unsigned rank = cluster_rank();
+    if (tid == 0)
+      for (unsigned p = 0; p < (unsigned)CL; ++p) {
+        double* dst = cluster_map(&W.ewx[0][0], p);
+        dst[2 * rank] = same;
+        dst[2 * rank + 1] = cross;
+      }
+    cluster_sync_all();
+    if (tid == 0) {
+      same = 0.0;
+      cross = 0.0;
+      for (int p = 0; p < CL; ++p) { same += W.ewx[p][0]; cross += W.ewx[p][1]; }
+    }
+  }
   __syncthreads();
 }
 
-// Make the staged structure factor current and refresh its double-float table.
+// Make the staged structure factor current and refresh its double-float table (in a
+// cluster, the CTA's own range of k).
+template <int CL = 1>
 __device__ __forceinline__ void commit_sk(const BoxDev& b, const double2* s_tmp) {
   float4* ewA = const_cast<float4*>(b.ewA);
-  for (int j = threadIdx.x; j < b.nact; j += blockDim.x) {
+  int k0 = 0, k1 = b.nact;
+  if constexpr (CL > 1) cluster_k_range(b.nact, CL, cluster_rank(), k0, k1);
+  for (int j = k0 + threadIdx.x; j < k1; j += blockDim.x) {
     const int slot = b.kact[j].w;
     const double2 v = s_tmp[slot];
     b.s_ads[slot] = v;

@@ -1,404 +1,15 @@
-// grx_gcmc.cu -- GCMC moves fully on the device: one persistent block per box,
-// looping over the box's Markov chain. A step restates RunMoves (axpy.cu:102-298)
-// for one adsorbate component:
-//   translation / rotation  get_new_position (mc_utilities.h:485-540), single-body
-//                           energy (VDW_Coulomb.cu:626-841), Ewald delta,
-//                           exp(-beta dE) (mc_single_particle.h:123-293)
-//   CBMC insertion          Insertion_Body + InsertionMove (mc_swap_utilities.h:3-132,
-//                           move_struct.h:18-90), Update_insertion_data_Parallel
-//   CBMC deletion           Deletion_Body + DeletionMove (mc_swap_utilities.h:135-225,
-//                           move_struct.h:122-167), Update_deletion_data_Parallel
-// Random numbers: Philox, key = seed, counter = {slot, step lo, step hi, stream};
-// slot 4096 = {molecule pick, move choice, insertion-vs-deletion, acceptance},
-// slot 4097 = {three uniforms of the displacement / rotation angles}, CBMC trial
-// slots 0..2047 and selection slot 2048 as in the Widom kernel.
+// grx_gcmc.cu -- GCMC moves fully on the device: preparation of the boxes and move sets,
+// persistent launches of the kernel in grx_gcmc_kernel.cuh (one block per box, or one
+// thread-block cluster per box through grx_gcmc_cluster.cu), batches replayed as CUDA
+// graphs, the launch-shape autotuner, and the single-molecule updates of the host layer.
 #include <algorithm>
 #include <cmath>
 #include <vector>
 
-#include "grx_cbmc.cuh"
+#include "grx_gcmc_kernel.cuh"
 #include "grx_host.h"
 
 namespace grx {
-
-enum : uint32_t { SLOT_MOVE = 4096u, SLOT_DISP = 4097u };
-constexpr int kMaxMoved = 4;  // moved components per box in one GCMC run
-
-struct GcmcArgs {
-  grx_gcmc_desc d;
-  int comp;
-  int ms;
-  int off;
-  int cap;      // component capacity in atoms
-  int rigid;
-  int charged;
-  int bias;
-  int pad_;
-  double excl;  // ExclusionIntra + ExclusionAtom of the component
-  double big_p; // MolFraction * Pressure * FugacityCoefficient * Volume
-};
-
-// RotationAroundAxis (mc_utilities.h:459-481) for a coordinate axis.
-__device__ __forceinline__ void rotate_axis(double& x, double& y, double& z, double theta, int axis) {
-  double s, c;
-  sincos(theta, &s, &c);
-  const double w = 1.0 - c;
-  const double ax = axis == 0, ay = axis == 1, az = axis == 2;
-  const double r0 = ax * ax * w + c, r1 = ax * ay * w + az * s, r2 = ax * az * w - ay * s;
-  const double r3 = ax * ay * w - az * s, r4 = ay * ay * w + c, r5 = ay * az * w + ax * s;
-  const double r6 = ax * az * w + ay * s, r7 = ay * az * w - ax * s, r8 = az * az * w + c;
-  const double nx = x * r0 + y * r1 + z * r2;
-  const double ny = x * r3 + y * r4 + z * r5;
-  const double nz = x * r6 + y * r7 + z * r8;
-  x = nx; y = ny; z = nz;
-}
-
-__device__ __forceinline__ void store_position(const BoxDev& b, int idx, double x, double y, double z) {
-  double4* p64 = const_cast<double4*>(b.pos64);
-  const double w = p64[idx].w;
-  p64[idx] = make_double4(x, y, z, w);
-  float hx, lx, hy, ly, hz, lz;
-  split_coord(x, hx, lx);
-  split_coord(y, hy, ly);
-  split_coord(z, hz, lz);
-  float4* hi = const_cast<float4*>(b.hi);
-  float4* lo = const_cast<float4*>(b.lo);
-  const float hw = hi[idx].w, lw = lo[idx].w;
-  hi[idx] = make_float4(hx, hy, hz, hw);
-  lo[idx] = make_float4(lx, ly, lz, lw);
-}
-
-__device__ __forceinline__ void copy_atom(const BoxDev& b, int dst, int src, int molid) {
-  const_cast<double4*>(b.pos64)[dst] = b.pos64[src];
-  const_cast<float4*>(b.hi)[dst] = b.hi[src];
-  const_cast<float4*>(b.lo)[dst] = b.lo[src];
-  const_cast<int2*>(b.meta)[dst] = make_int2(b.meta[src].x, molid);
-  const_cast<double*>(b.scale)[dst] = b.scale[src];
-  const_cast<double*>(b.charge)[dst] = b.charge[src];
-  const_cast<float2*>(b.qdf)[dst] = b.qdf[src];
-}
-
-// The Fourier delta of a GCMC move, staged for commit_sk: the row-product form for boxes
-// that enable it (BoxDev::ew_rows), the direct form otherwise; two instantiations, so each
-// form keeps its own register allocation.
-template <int PREC, class WK>
-__device__ __forceinline__ void ewald_delta_move(const BoxDev& b, WK& W, int na, double2* eik, double& same,
-                                                 double& cross) {
-  if (b.ew_rows) ewald_move<PREC, WK, true>(b, W, na, eik, b.s_tmp, same, cross);
-  else ewald_move<PREC, WK, false>(b, W, na, eik, b.s_tmp, same, cross);
-}
-
-// One block of NW warps per box (NW = 8, 12 or 24: 24 warps per SM in every shape).
-// The box's moved components are entries [first[box], first[box + 1]) of args /
-// stats; every step picks one of them uniformly with word 3 of the displacement slot
-// (Select_Box_Component_Molecule, axpy.cu:74-100). All entries of a box share its seed
-// and stream.
-template <int PREC, int NW>
-__global__ void __launch_bounds__(NW * 32, 24 / NW) gcmc_kernel(const BoxDev* boxes, const GcmcArgs* args,
-                                                              const int* first, const uint64_t* step0,
-                                                              int64_t nsteps, grx_gcmc_stats* stats) {
-  const uint64_t first_step = *step0;
-  __shared__ BoxDev b;
-  __shared__ GcmcArgs A[kMaxMoved];
-  __shared__ CbmcWork<NW> W;
-  __shared__ grx_gcmc_stats ST[kMaxMoved];
-  __shared__ int s_accept;
-  __shared__ double s_e1[4], s_w1, s_dE[3], s_stored, s_r1[4], s_wr;
-  extern __shared__ double2 eik[];
-  const int tid = threadIdx.x;
-  const int e0 = first[blockIdx.x], nm = first[blockIdx.x + 1] - e0;
-  if (tid == 0) b = boxes[blockIdx.x];
-  if (tid < nm) {
-    A[tid] = args[e0 + tid];
-    ST[tid] = grx_gcmc_stats{};
-  }
-  __syncthreads();
-  int* comp_size = const_cast<int*>(b.comp_size);
-  for (int64_t step = 0; step < nsteps; ++step) {
-    const uint64_t move = first_step + (uint64_t)step;
-    uint32_t w[4], w2[4], ws[4];
-    draw4(A[0].d.seed, A[0].d.stream, move, SLOT_MOVE, w);
-    draw4(A[0].d.seed, A[0].d.stream, move, SLOT_DISP, w2);
-    draw4(A[0].d.seed, A[0].d.stream, move, SLOT_SELECT, ws);
-    const int sel = nm > 1 ? min(nm - 1, (int)(u01(w2[3]) * (double)nm)) : 0;
-    const GcmcArgs& a = A[sel];
-    const grx_gcmc_desc& d = a.d;
-    grx_gcmc_stats& st = ST[sel];
-    const int comp = a.comp, ms = a.ms, chain = ms - 1, off = a.off;
-    const int N = comp_size[comp] / ms;
-    const int mol = (int)(u01(w[0]) * (double)N);
-    const double r = u01(w[1]);
-    int kind = -1;
-    if (r < d.p_translation) kind = 0;
-    else if (r < d.p_rotation) kind = 1;
-    else if (r < d.p_reinsertion) kind = 4;
-    else if (r < d.p_swap) kind = (u01(w[2]) < 0.5) ? 2 : 3;
-    const double uacc = u01(w[3]);
-    if (tid == 0) s_accept = 0;
-
-    if ((kind == 0 || kind == 1) && N > 0) {
-      // ---------------------------------------------- translation / rotation
-      const int m0 = off + mol * ms;
-      if (tid == 0) st.attempts[kind]++;
-      if (tid < ms) {
-        const double4 p = b.pos64[m0 + tid];
-        const double4 p0 = b.pos64[m0];
-        double nx, ny, nz;
-        if (kind == 0) {
-          nx = p.x + d.max_translation[0] * 2.0 * (u01(w2[0]) - 0.5);
-          ny = p.y + d.max_translation[1] * 2.0 * (u01(w2[1]) - 0.5);
-          nz = p.z + d.max_translation[2] * 2.0 * (u01(w2[2]) - 0.5);
-        } else {
-          double vx = p.x - p0.x, vy = p.y - p0.y, vz = p.z - p0.z;
-          rotate_axis(vx, vy, vz, d.max_rotation[0] * 2.0 * (u01(w2[0]) - 0.5), 0);
-          rotate_axis(vx, vy, vz, d.max_rotation[1] * 2.0 * (u01(w2[1]) - 0.5), 1);
-          rotate_axis(vx, vy, vz, d.max_rotation[2] * 2.0 * (u01(w2[2]) - 0.5), 2);
-          nx = vx + p0.x; ny = vy + p0.y; nz = vz + p0.z;
-        }
-        W.mx[tid] = p.x; W.my[tid] = p.y; W.mz[tid] = p.z; W.mq[tid] = -p.w;
-        W.mx[ms + tid] = nx; W.my[ms + tid] = ny; W.mz[ms + tid] = nz; W.mq[ms + tid] = p.w;
-        const int type = b.meta[m0 + tid].x;
-        const double sc = b.scale[m0 + tid];
-        make_bead(W.beads[tid], nx, ny, nz, p.w, sc, type, b.prefactor);
-        make_bead(W.beads[ms + tid], p.x, p.y, p.z, p.w, sc, type, b.prefactor);
-      }
-      __syncthreads();
-      trial_pass<PREC>(b, W, 2 * ms, ms, comp, mol);  // te[0..3] new, te[4..7] old
-      if (!W.tflag[0]) {
-        double same = 0.0, cross = 0.0;
-        if (a.charged) ewald_delta_move<PREC>(b, W, 2 * ms, eik, same, cross);
-        if (tid == 0) {
-          const double dv = (W.te[0] + W.te[2]) - (W.te[4] + W.te[6]);
-          const double dr = (W.te[1] + W.te[3]) - (W.te[5] + W.te[7]);
-          const double ew = same + 2.0 * cross;
-          const double pacc = exp(-d.beta * (dv + dr + ew));
-          s_accept = uacc < pacc;
-          s_dE[0] = dv; s_dE[1] = dr; s_dE[2] = ew;
-        }
-      }
-      __syncthreads();
-      if (s_accept) {
-        if (tid < ms) store_position(b, m0 + tid, W.mx[ms + tid], W.my[ms + tid], W.mz[ms + tid]);
-        if (a.charged) commit_sk(b, b.s_tmp);
-        if (tid == 0) {
-          st.accepted[kind]++;
-          st.energy[0] += s_dE[0]; st.energy[1] += s_dE[1]; st.energy[2] += s_dE[2];
-          st.energy[3] += s_dE[0] + s_dE[1] + s_dE[2];
-        }
-      }
-    } else if (kind == 4 && N > 0) {
-      // ---------------------------------------------- reinsertion (move_struct.h:170-406)
-      const int m0 = off + mol * ms;
-      if (tid == 0) st.attempts[4]++;
-      if (tid < ms) {  // [0, ms): the molecule now (charge negated); [ms, 2ms): its regrowth
-        const double4 p = b.pos64[m0 + tid];
-        W.mx[tid] = p.x; W.my[tid] = p.y; W.mz[tid] = p.z; W.mq[tid] = -p.w;
-        W.mq[ms + tid] = p.w;
-      }
-      __syncthreads();
-      // insertion half: every trial new, the molecule itself excluded
-      gen_first_trials(b, W, d.seed, d.stream, move, d.ntrials, b.charge[off], 1.0, b.meta[off].x, false, 0.0, 0.0,
-                       0.0);
-      trial_pass<PREC>(b, W, d.ntrials, 1, comp, mol);
-      step_weight(W, d.ntrials, d.beta, a.bias, u01(ws[0]), (double)d.ntrials, false);
-      bool ok = W.ok && W.w > 1e-150;
-      double fx = 0, fy = 0, fz = 0;
-      if (ok) {
-        const Bead& fb = W.beads[W.sel];
-        fx = fb.x; fy = fb.y; fz = fb.z;
-        if (tid == 0) {
-          for (int k = 0; k < 4; ++k) s_e1[k] = W.te[4 * W.sel + k];
-          s_w1 = W.w;
-          s_stored = W.wraw - W.sel_wa[W.sel];  // StoredR (mc_widom.h:363)
-          W.mx[ms] = fx; W.my[ms] = fy; W.mz[ms] = fz;
-        }
-      }
-      __syncthreads();
-      double rosen = ok ? s_w1 : 0.0;
-      double e2[4] = {0, 0, 0, 0};
-      if (ok && chain > 0) {
-        gen_orientations(b, W, d.seed, d.stream, move, d.norient, chain, off, 1.0, 1.0, fx, fy, fz, false, nullptr,
-                         nullptr, nullptr);
-        trial_pass<PREC>(b, W, d.norient * chain, chain, comp, mol);
-        step_weight(W, d.norient, d.beta, a.bias, u01(ws[1]), (double)d.norient, false);
-        ok = W.ok;
-        if (ok) {
-          rosen *= W.w;
-          for (int k = 0; k < 4; ++k) e2[k] = W.te[4 * W.sel + k];
-          if (rosen <= 1e-150) ok = false;
-          if (tid < chain) {
-            const Bead& bd = W.beads[W.sel * chain + tid];
-            W.mx[ms + 1 + tid] = bd.x; W.my[ms + 1 + tid] = bd.y; W.mz[ms + 1 + tid] = bd.z;
-          }
-        }
-        __syncthreads();
-      }
-      if (ok) {
-        // retrace half: the first bead's single trial is the molecule's own, plus StoredR
-        gen_first_trials(b, W, d.seed, d.stream, move, 1, b.charge[off], 1.0, b.meta[off].x, true, W.mx[0], W.my[0],
-                         W.mz[0]);
-        trial_pass<PREC>(b, W, 1, 1, comp, mol);
-        step_weight(W, 1, d.beta, a.bias, 0.0, (double)d.ntrials, true, s_stored);
-        bool ok2 = W.ok;
-        if (ok2 && tid == 0) {
-          for (int k = 0; k < 4; ++k) s_r1[k] = W.te[k];
-          s_wr = W.w;
-        }
-        __syncthreads();
-        double rosen_old = ok2 ? s_wr : 0.0;
-        double r2[4] = {0, 0, 0, 0};
-        if (ok2 && chain > 0) {
-          gen_orientations(b, W, d.seed, d.stream, move, d.norient, chain, off, 1.0, 1.0, W.mx[0], W.my[0], W.mz[0],
-                           true, W.mx + 1, W.my + 1, W.mz + 1, SLOT_RETRACE);
-          trial_pass<PREC>(b, W, d.norient * chain, chain, comp, mol);
-          step_weight(W, d.norient, d.beta, a.bias, 0.0, (double)d.norient, true);
-          ok2 = W.ok;
-          if (ok2) {
-            rosen_old *= W.w;
-            for (int k = 0; k < 4; ++k) r2[k] = W.te[4 * W.sel + k];
-          }
-          __syncthreads();
-        }
-        if (ok2) {
-          double same = 0.0, cross = 0.0;
-          if (a.charged) ewald_delta_move<PREC>(b, W, 2 * ms, eik, same, cross);
-          if (tid == 0) {
-            const double ew = a.charged ? same + 2.0 * cross : 0.0;
-            rosen *= exp(-d.beta * ew);
-            const double pacc = rosen / rosen_old;
-            s_accept = uacc < pacc;
-            s_dE[0] = s_e1[0] + s_e1[2] + e2[0] + e2[2] - (s_r1[0] + s_r1[2] + r2[0] + r2[2]);
-            s_dE[1] = s_e1[1] + s_e1[3] + e2[1] + e2[3] - (s_r1[1] + s_r1[3] + r2[1] + r2[3]);
-            s_dE[2] = ew;
-          }
-        }
-      }
-      __syncthreads();
-      if (s_accept) {
-        if (tid < ms) store_position(b, m0 + tid, W.mx[ms + tid], W.my[ms + tid], W.mz[ms + tid]);
-        if (a.charged) commit_sk(b, b.s_tmp);
-        if (tid == 0) {
-          st.accepted[4]++;
-          st.energy[0] += s_dE[0]; st.energy[1] += s_dE[1]; st.energy[2] += s_dE[2];
-          st.energy[3] += s_dE[0] + s_dE[1] + s_dE[2];
-        }
-      }
-    } else if (kind == 2 || (kind == 3 && N > 0)) {
-      // ---------------------------------------------- CBMC insertion / deletion
-      const bool del = kind == 3;
-      const int m0 = off + mol * ms;
-      const int newmol = del ? mol : N;
-      if (tid == 0) st.attempts[kind]++;
-      if (del && tid < ms) {  // the molecule to retrace and remove
-        const double4 p = b.pos64[m0 + tid];
-        W.mx[tid] = p.x; W.my[tid] = p.y; W.mz[tid] = p.z; W.mq[tid] = -p.w;
-      }
-      __syncthreads();
-      gen_first_trials(b, W, d.seed, d.stream, move, d.ntrials, b.charge[off], 1.0, b.meta[off].x, del,
-                       W.mx[0], W.my[0], W.mz[0]);
-      trial_pass<PREC>(b, W, d.ntrials, 1, comp, newmol);
-      step_weight(W, d.ntrials, d.beta, a.bias, u01(ws[0]), (double)d.ntrials, del);
-      bool ok = W.ok && W.w > 1e-150;
-      double fx = 0, fy = 0, fz = 0;
-      if (ok) {
-        const Bead& fb = W.beads[W.sel];
-        fx = fb.x; fy = fb.y; fz = fb.z;
-        if (tid == 0) {
-          for (int k = 0; k < 4; ++k) s_e1[k] = W.te[4 * W.sel + k];
-          s_w1 = W.w;
-        }
-        if (!del && tid == 0) { W.mx[0] = fx; W.my[0] = fy; W.mz[0] = fz; W.mq[0] = b.charge[off]; }
-      }
-      __syncthreads();
-      double rosen = ok ? s_w1 : 0.0;
-      double e2[4] = {0, 0, 0, 0};
-      if (ok && chain > 0) {
-        gen_orientations(b, W, d.seed, d.stream, move, d.norient, chain, off, 1.0, 1.0, fx, fy, fz, del,
-                         W.mx + 1, W.my + 1, W.mz + 1);
-        trial_pass<PREC>(b, W, d.norient * chain, chain, comp, newmol);
-        step_weight(W, d.norient, d.beta, a.bias, u01(ws[1]), (double)d.norient, del);
-        ok = W.ok;
-        if (ok) {
-          rosen *= W.w;
-          for (int k = 0; k < 4; ++k) e2[k] = W.te[4 * W.sel + k];
-          if (rosen <= 1e-150) ok = false;
-          if (!del && tid < chain) {
-            const Bead& bd = W.beads[W.sel * chain + tid];
-            W.mx[1 + tid] = bd.x; W.my[1 + tid] = bd.y; W.mz[1 + tid] = bd.z;
-            W.mq[1 + tid] = b.charge[off + 1 + tid];
-          }
-        }
-        __syncthreads();
-      }
-      if (ok) {
-        double same = 0.0, cross = 0.0;
-        if (a.charged) ewald_delta_move<PREC>(b, W, ms, eik, same, cross);
-        if (tid == 0) {
-          double ew = 0.0;
-          if (a.charged) {
-            if (a.rigid) same -= a.excl * (del ? (0.0 - 1.0) : (1.0 - 0.0));
-            ew = same + 2.0 * cross;
-          }
-          double pacc;
-          if (!del) {
-            rosen *= exp(-d.beta * ew);
-            rosen *= exp(-d.beta * d.tail_insert);
-            pacc = d.beta * a.big_p / (1.0 + (double)N) * rosen / d.ideal_rosenbluth;
-            s_accept = rosen > 1e-150 && uacc < pacc;
-            if (s_accept && (N + 1) * ms > a.cap) {
-              s_accept = 0;
-              st.capacity_hits++;
-            }
-          } else {
-            rosen /= exp(-d.beta * ew);
-            rosen /= exp(d.beta * d.tail_insert);  // the deletion's tail difference is -tail_insert
-            pacc = (double)N / (d.beta * a.big_p) * d.ideal_rosenbluth / rosen;
-            s_accept = uacc < pacc;
-          }
-          const double ev = s_e1[0] + s_e1[2] + e2[0] + e2[2];
-          const double er = s_e1[1] + s_e1[3] + e2[1] + e2[3];
-          const double sg = del ? -1.0 : 1.0;
-          s_dE[0] = sg * ev; s_dE[1] = sg * er; s_dE[2] = ew;
-        }
-      }
-      __syncthreads();
-      if (s_accept) {
-        if (!del) {
-          if (tid < ms)
-            store_atom(b, off + N * ms + tid, W.mx[tid], W.my[tid], W.mz[tid], b.charge[off + tid], 1.0, 1.0,
-                       b.meta[off + tid].x, N);
-          __syncthreads();
-          if (tid == 0) comp_size[comp] += ms;
-        } else {
-          const int last = off + (N - 1) * ms;
-          if (m0 != last && tid < ms) copy_atom(b, m0 + tid, last + tid, mol);
-          __syncthreads();
-          if (tid == 0) comp_size[comp] -= ms;
-        }
-        if (a.charged) commit_sk(b, b.s_tmp);
-        if (tid == 0) {
-          st.accepted[kind]++;
-          st.energy[0] += s_dE[0]; st.energy[1] += s_dE[1]; st.energy[2] += s_dE[2];
-          st.energy[3] += s_dE[0] + s_dE[1] + s_dE[2];
-        }
-      }
-    }
-    __syncthreads();
-    if (tid < nm) ST[tid].sum_n += (double)(comp_size[A[tid].comp] / A[tid].ms);
-    __syncthreads();
-  }
-  if (tid < nm) {  // accumulate into the caller's running statistics
-    grx_gcmc_stats& o = stats[e0 + tid];
-    for (int k = 0; k < 5; ++k) {
-      o.attempts[k] += ST[tid].attempts[k];
-      o.accepted[k] += ST[tid].accepted[k];
-    }
-    for (int k = 0; k < 4; ++k) o.energy[k] += ST[tid].energy[k];
-    o.capacity_hits += ST[tid].capacity_hits;
-    o.sum_n += ST[tid].sum_n;
-    o.n_molecules = comp_size[A[tid].comp] / A[tid].ms;
-  }
-}
 
 __global__ void advance_step_kernel(uint64_t* step, int64_t nsteps) { *step += (uint64_t)nsteps; }
 
@@ -446,6 +57,7 @@ struct grx_gcmc_batch {
   size_t smem = 0;
   int chunk_mult = 1;
   int nwarps = 8;  // warps per box (block size / 32): 8, 12 or 24
+  int cluster = 1; // CTAs per box (1, or 2 / 4 / 8 with 24 warps each)
   void* mem = nullptr;
   grx_arena* arena = nullptr;
   BoxDev* d_boxes = nullptr;
@@ -554,6 +166,7 @@ static grx_status set_gcmc_smem() {
                        set_smem_one<GRX_MIXED, 8>(), set_smem_one<GRX_MIXED, 12>(), set_smem_one<GRX_MIXED, 24>(),
                        set_smem_one<GRX_FP32, 8>(), set_smem_one<GRX_FP32, 12>(), set_smem_one<GRX_FP32, 24>()})
     if (r && !st) st = r;
+  if (!st) GRX_CHECK_CUDA(set_gcmc_cluster_smem(kGcmcDynSmem), "gcmc cluster shared memory attribute");
   if (!st && dev >= 0 && dev < 64) done[dev] = true;
   return st;
 }
@@ -584,13 +197,22 @@ static void launch_shape(grx_precision prec, int nboxes, const BoxDev* dboxes, c
     gcmc_kernel<GRX_FP32, NW><<<nboxes, NW * 32, smem, stream>>>(dboxes, dargs, dfirst, dstep, nsteps, dstats);
 }
 
-// Enqueues one persistent launch of nw warps per box and the step-counter advance (no host sync).
+// Enqueues one persistent launch of nw warps per box (a cluster of cl such blocks per box
+// when cl > 1, nw = 24) and the step-counter advance (no host sync).
 static grx_status enqueue_gcmc(grx_precision prec, int nw, int nboxes, const BoxDev* dboxes, const GcmcArgs* dargs,
                                const int* dfirst, uint64_t* dstep, int64_t nsteps, grx_gcmc_stats* dstats,
-                               size_t smem, cudaStream_t stream) {
-  if (nw == 24) launch_shape<24>(prec, nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem, stream);
-  else if (nw == 12) launch_shape<12>(prec, nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem, stream);
-  else launch_shape<8>(prec, nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem, stream);
+                               size_t smem, cudaStream_t stream, int cl = 1) {
+  if (cl > 1) {
+    GRX_REQUIRE(nw == 24, "grx_gcmc: cluster launches use 24 warps per block");
+    GRX_CHECK_CUDA(launch_gcmc_cluster(prec, cl, nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem, stream),
+                   "gcmc cluster launch");
+  } else if (nw == 24) {
+    launch_shape<24>(prec, nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem, stream);
+  } else if (nw == 12) {
+    launch_shape<12>(prec, nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem, stream);
+  } else {
+    launch_shape<8>(prec, nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem, stream);
+  }
   advance_step_kernel<<<1, 1, 0, stream>>>(dstep, nsteps);
   count_launch();
   count_launch();
@@ -778,7 +400,7 @@ extern "C" grx_status grx_gcmc_batch_launch(grx_gcmc_batch* B, int64_t nsteps, v
   if (nsteps == 0) return GRX_OK;
   B->last_stream = s;
   return enqueue_gcmc(B->prec, B->nwarps, (int)B->boxes.size(), B->d_boxes, B->d_args, B->d_first, B->d_step, nsteps,
-                      B->d_stats, B->smem, s);
+                      B->d_stats, B->smem, s, B->cluster);
 }
 
 extern "C" grx_status grx_gcmc_batch_run_graph(grx_gcmc_batch* B, int64_t nsteps, int32_t nlaunch, void* stream) {
@@ -793,7 +415,7 @@ extern "C" grx_status grx_gcmc_batch_run_graph(grx_gcmc_batch* B, int64_t nsteps
     const uint64_t before = grx_launch_count();
     for (int k = 0; k < nlaunch && st == GRX_OK; ++k)
       st = enqueue_gcmc(B->prec, B->nwarps, (int)B->boxes.size(), B->d_boxes, B->d_args, B->d_first, B->d_step, nsteps,
-                        B->d_stats, B->smem, cap);
+                        B->d_stats, B->smem, cap, B->cluster);
     count_launch(0 - (grx_launch_count() - before));  // capture records the kernels, it launches nothing
     cudaGraph_t g = nullptr;
     const cudaError_t ec = cudaStreamEndCapture(cap, &g);
@@ -855,6 +477,7 @@ extern "C" grx_status grx_gcmc_batch_set_shape(grx_gcmc_batch* B, int32_t nwarps
   if (st) return st;
   B->nwarps = nwarps;
   B->chunk_mult = chunk_mult;
+  if (nwarps != 24) B->cluster = 1;
   drop_graph(B);
   return GRX_OK;
 }
@@ -863,6 +486,39 @@ extern "C" grx_status grx_gcmc_batch_get_shape(grx_gcmc_batch* B, int32_t* nwarp
   GRX_REQUIRE(B, "grx_gcmc_batch_get_shape: null batch");
   if (nwarps) *nwarps = B->nwarps;
   if (chunk_mult) *chunk_mult = B->chunk_mult;
+  return GRX_OK;
+}
+
+// The largest cluster size (8, 4 or 2) for which every box of the batch gets its own
+// resident cluster, or 1 when the boxes already fill the SMs.
+static int max_cluster(const grx_gcmc_batch* B) {
+  const int nb = (int)B->boxes.size();
+  for (int cl : {8, 4, 2})
+    if (gcmc_cluster_capacity(B->prec, cl, B->smem) >= nb) return cl;
+  return 1;
+}
+
+extern "C" grx_status grx_gcmc_batch_set_cluster(grx_gcmc_batch* B, int32_t cluster) {
+  GRX_REQUIRE(B, "grx_gcmc_batch_set_cluster: null batch");
+  GRX_REQUIRE(cluster == 1 || cluster == 2 || cluster == 4 || cluster == 8,
+              "grx_gcmc_batch_set_cluster: cluster must be 1, 2, 4 or 8");
+  GRX_REQUIRE(cluster == 1 || B->nwarps == 24, "grx_gcmc_batch_set_cluster: clusters use 24 warps per block");
+  GRX_CHECK_CUDA(cudaStreamSynchronize(B->stream), "set cluster");
+  if (cluster > 1) {
+    GRX_CHECK_CUDA(cudaSetDevice(B->device), "set device");
+    grx_status st = set_gcmc_smem();
+    if (st) return st;
+    GRX_REQUIRE(gcmc_cluster_capacity(B->prec, cluster, B->smem) >= (int)B->boxes.size(),
+                "grx_gcmc_batch_set_cluster: not every box gets a resident cluster of this size");
+  }
+  B->cluster = cluster;
+  drop_graph(B);
+  return GRX_OK;
+}
+
+extern "C" grx_status grx_gcmc_batch_get_cluster(grx_gcmc_batch* B, int32_t* cluster) {
+  GRX_REQUIRE(B && cluster, "grx_gcmc_batch_get_cluster: bad argument");
+  *cluster = B->cluster;
   return GRX_OK;
 }
 
@@ -887,8 +543,11 @@ static double trial_energies(const grx_gcmc_batch* B, const std::vector<grx_gcmc
 // with CUDA events, and keeps the shape with the most trial energies per second. The
 // chains change while they are probed (boxes fill up from empty), so each candidate
 // is timed twice, in a forward and a reverse sweep, and ranked by work per time.
-// ms_per_candidate reports the mean time of one probe. The probe steps are ordinary
-// Monte Carlo steps: the chains advance by 2 * GRX_GCMC_TUNE_CANDIDATES * nsteps.
+// ms_per_candidate reports the mean time of one probe. When the boxes leave SMs idle
+// (a cluster of 2, 4 or 8 CTAs per box is resident for every box), the best shape is then
+// probed against clusters of 24-warp CTAs with the best 24-warp items per warp, in the
+// order plain, cluster, cluster, plain, and the faster kept. The probe steps are ordinary
+// Monte Carlo steps: the chains advance by up to 2 * (GRX_GCMC_TUNE_CANDIDATES + 2) * nsteps.
 extern "C" grx_status grx_gcmc_batch_autotune(grx_gcmc_batch* B, int64_t nsteps, int32_t* chosen,
                                               float* ms_per_candidate) {
   GRX_REQUIRE(B && nsteps >= 1, "grx_gcmc_batch_autotune: bad argument");
@@ -898,46 +557,66 @@ extern "C" grx_status grx_gcmc_batch_autotune(grx_gcmc_batch* B, int64_t nsteps,
   cudaEvent_t e0, e1;
   GRX_CHECK_CUDA(cudaEventCreate(&e0), "event");
   GRX_CHECK_CUDA(cudaEventCreate(&e1), "event");
-  double ms_sum[GRX_GCMC_TUNE_CANDIDATES] = {}, te_sum[GRX_GCMC_TUNE_CANDIDATES] = {};
   std::vector<grx_gcmc_stats> before(B->nentries), after(B->nentries);
   auto read = [&](std::vector<grx_gcmc_stats>& v) {
     return cudaMemcpy(v.data(), B->d_stats, B->nentries * sizeof(grx_gcmc_stats), cudaMemcpyDeviceToHost);
   };
-  GRX_CHECK_CUDA(cudaStreamSynchronize(B->stream), "tune sync");
-  for (int k = 0; k < 2 * GRX_GCMC_TUNE_CANDIDATES; ++k) {
-    const int c = k < GRX_GCMC_TUNE_CANDIDATES ? k : 2 * GRX_GCMC_TUNE_CANDIDATES - 1 - k;
-    const int nw = warps[c / 3], mult = mults[c % 3];
+  // one timed probe of a shape: adds its milliseconds and trial energies
+  auto probe = [&](int nw, int mult, int cl, double& ms_acc, double& te_acc) -> grx_status {
     grx_status st = upload_mult(B, mult);
     if (st) return st;
     GRX_CHECK_CUDA(read(before), "tune stats");
     GRX_CHECK_CUDA(cudaEventRecord(e0, B->stream), "event");
     st = enqueue_gcmc(B->prec, nw, nb, B->d_boxes, B->d_args, B->d_first, B->d_step, nsteps, B->d_stats, B->smem,
-                      B->stream);
+                      B->stream, cl);
     if (st) return st;
     GRX_CHECK_CUDA(cudaEventRecord(e1, B->stream), "event");
     GRX_CHECK_CUDA(cudaEventSynchronize(e1), "event");
     float ms = 0.f;
     GRX_CHECK_CUDA(cudaEventElapsedTime(&ms, e0, e1), "event");
     GRX_CHECK_CUDA(read(after), "tune stats");
-    ms_sum[c] += ms;
-    te_sum[c] += trial_energies(B, after) - trial_energies(B, before);
+    ms_acc += ms;
+    te_acc += trial_energies(B, after) - trial_energies(B, before);
+    return GRX_OK;
+  };
+  auto rate = [](double te, double ms) { return te > 0.0 ? te / ms : 1.0 / ms; };
+  GRX_CHECK_CUDA(cudaStreamSynchronize(B->stream), "tune sync");
+  double ms_sum[GRX_GCMC_TUNE_CANDIDATES] = {}, te_sum[GRX_GCMC_TUNE_CANDIDATES] = {};
+  for (int k = 0; k < 2 * GRX_GCMC_TUNE_CANDIDATES; ++k) {
+    const int c = k < GRX_GCMC_TUNE_CANDIDATES ? k : 2 * GRX_GCMC_TUNE_CANDIDATES - 1 - k;
+    grx_status st = probe(warps[c / 3], mults[c % 3], 1, ms_sum[c], te_sum[c]);
+    if (st) return st;
+  }
+  int best = 0, best24 = 6;
+  for (int c = 0; c < GRX_GCMC_TUNE_CANDIDATES; ++c) {
+    if (ms_per_candidate) ms_per_candidate[c] = (float)(ms_sum[c] / 2.0);
+    if (rate(te_sum[c], ms_sum[c]) > rate(te_sum[best], ms_sum[best])) best = c;
+    if (c >= 6 && rate(te_sum[c], ms_sum[c]) > rate(te_sum[best24], ms_sum[best24])) best24 = c;
+  }
+  int best_w = warps[best / 3], best_m = mults[best % 3], best_cl = 1;
+  const int clmax = max_cluster(B);
+  if (clmax > 1) {
+    double ms_p = 0.0, te_p = 0.0, ms_c = 0.0, te_c = 0.0;
+    for (int k = 0; k < 4; ++k) {
+      const bool plain = k == 0 || k == 3;
+      grx_status st = plain ? probe(best_w, best_m, 1, ms_p, te_p) : probe(24, mults[best24 % 3], clmax, ms_c, te_c);
+      if (st) return st;
+    }
+    if (rate(te_c, ms_c) > rate(te_p, ms_p)) {
+      best_w = 24;
+      best_m = mults[best24 % 3];
+      best_cl = clmax;
+    }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  int best = 0;
-  double best_rate = -1.0;
-  for (int c = 0; c < GRX_GCMC_TUNE_CANDIDATES; ++c) {
-    const double rate = te_sum[c] > 0.0 ? te_sum[c] / ms_sum[c] : 1.0 / ms_sum[c];
-    if (ms_per_candidate) ms_per_candidate[c] = (float)(ms_sum[c] / 2.0);
-    if (rate > best_rate) { best_rate = rate; best = c; }
-  }
-  const int best_w = warps[best / 3], best_m = mults[best % 3];
   grx_status st = upload_mult(B, best_m);
   if (st) return st;
   B->nwarps = best_w;
   B->chunk_mult = best_m;
+  B->cluster = best_cl;
   drop_graph(B);
-  if (chosen) *chosen = best_w * 100 + best_m;
+  if (chosen) *chosen = (best_cl - 1) * 10000 + best_w * 100 + best_m;
   return GRX_OK;
 }
 

@@ -425,13 +425,16 @@ __device__ __forceinline__ PassSplit pass_split(const BoxDev& b, int nb, int nwa
 
 constexpr int kMaxItems = 320;
 
-// One pass of `nb` beads (shared memory) over every atom by a whole block. Items are
-// taken dynamically by warps; the partial of bead `bead` within item `item` lands in
-// ipart[(item + bead)*4 + q] and iflag[item + bead]. Caller syncs before reading them.
+// One pass of `nb` beads (shared memory) over every atom by a whole block. Items
+// [item0, item1) (all of them when item1 < 0) are taken dynamically by warps; the partial
+// of bead `bead` within item `item` lands in ipart[(item + bead)*4 + q] and
+// iflag[item + bead]. Caller syncs before reading them.
 template <int PREC>
 __device__ __noinline__ void block_bead_pass(const BoxDev& b, const Bead* beads, int nb, int component,
                                                 int newmol, int excl_comp, int excl_mol, int* qbuf,
-                                                double* ipart, int* iflag, int* counter, PassSplit sp) {
+                                                double* ipart, int* iflag, int* counter, PassSplit sp,
+                                                int item0 = 0, int item1 = -1) {
+  if (item1 < 0) item1 = (int)sp.items;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int* q = qbuf + warp * kQueue;
   const int nt = b.ntiles;
@@ -443,9 +446,9 @@ __device__ __noinline__ void block_bead_pass(const BoxDev& b, const Bead* beads,
   }
   for (;;) {
     int item = 0;
-    if (lane == 0) item = atomicAdd(counter, 1);
+    if (lane == 0) item = item0 + atomicAdd(counter, 1);
     item = __shfl_sync(kFull, item, 0);
-    if (item >= (int)sp.items) break;
+    if (item >= item1) break;
     unsigned lo, hi;
     sp.range((unsigned)item, lo, hi);
     while (lo < hi) {
@@ -465,6 +468,40 @@ __device__ __noinline__ void block_bead_pass(const BoxDev& b, const Bead* beads,
       lo += (unsigned)(u1 - u0);
     }
   }
+}
+
+// ---------------------------------------------------------------- thread-block clusters
+// A cluster of CTAs may share one chain: each CTA evaluates a contiguous share of a pass's
+// items and writes its partial slots into every peer's shared memory (PTX mapa + generic
+// stores), so all CTAs reduce identical slots in identical order. barrier.cluster with
+// release / acquire semantics orders those stores and the CTAs' global writes.
+__device__ __forceinline__ unsigned cluster_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+template <class T>
+__device__ __forceinline__ T* cluster_map(T* p, unsigned rank) {  // the same shared variable in CTA `rank`
+  uint64_t out;
+  asm volatile("mapa.u64 %0, %1, %2;" : "=l"(out) : "l"(reinterpret_cast<uint64_t>(p)), "r"(rank));
+  return reinterpret_cast<T*>(out);
+}
+
+// Items of a pass for CTA `rank` of a CL-CTA cluster: [i0, i1), contiguous.
+__device__ __forceinline__ void cluster_items(const PassSplit& sp, int cl, unsigned rank, int& i0, int& i1) {
+  const unsigned per = (sp.items + (unsigned)cl - 1u) / (unsigned)cl;
+  i0 = (int)min(sp.items, rank * per);
+  i1 = (int)min(sp.items, (unsigned)i0 + per);
+}
+
+// Active k vectors of CTA `rank` of a CL-CTA cluster: [k0, k1), contiguous.
+__device__ __forceinline__ void cluster_k_range(int nact, int cl, unsigned rank, int& k0, int& k1) {
+  const int per = (nact + cl - 1) / cl;
+  k0 = min(nact, (int)rank * per);
+  k1 = min(nact, k0 + per);
 }
 
 // Item partials: FP64 in the FP64 / FP32 forms, a float pair in the mixed form.

@@ -137,7 +137,8 @@ EXPORTS = [
     "grx_widom_insertions", "grx_widom_insertions_async", "grx_launch_count", "grx_last_transfer", "grx_probe_fp32_fma", "grx_trial_energies_noalloc", "grx_gcmc_run",
     "grx_box_write_molecule", "grx_box_remove_molecule", "grx_gcmc_batch_create", "grx_gcmc_batch_destroy",
     "grx_gcmc_batch_set_step", "grx_gcmc_batch_launch", "grx_gcmc_batch_run_graph", "grx_gcmc_batch_stats",
-    "grx_gcmc_batch_reset_stats", "grx_gcmc_batch_autotune", "grx_gcmc_batch_set_shape", "grx_gcmc_batch_get_shape", "grx_arena_create", "grx_arena_destroy",
+    "grx_gcmc_batch_reset_stats", "grx_gcmc_batch_autotune", "grx_gcmc_batch_set_shape", "grx_gcmc_batch_get_shape",
+    "grx_gcmc_batch_set_cluster", "grx_gcmc_batch_get_cluster", "grx_arena_create", "grx_arena_destroy",
     "grx_arena_usage", "grx_box_create_in", "grx_box_footprint", "grx_server_create", "grx_server_destroy",
     "grx_server_submit", "grx_server_progress", "grx_server_poll", "grx_server_time", "grx_server_launch_count",
     "grx_box_create_replica",
@@ -213,6 +214,8 @@ def load(path=LIB_PATH):
     L.grx_gcmc_batch_autotune.argtypes = [C.c_void_p, C.c_int64, P(C.c_int32), P(C.c_float)]
     L.grx_gcmc_batch_set_shape.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
     L.grx_gcmc_batch_get_shape.argtypes = [C.c_void_p, P(C.c_int32), P(C.c_int32)]
+    L.grx_gcmc_batch_set_cluster.argtypes = [C.c_void_p, C.c_int32]
+    L.grx_gcmc_batch_get_cluster.argtypes = [C.c_void_p, P(C.c_int32)]
     L.grx_arena_create.argtypes = [C.c_size_t, P(C.c_void_p)]
     L.grx_arena_destroy.argtypes = [C.c_void_p]
     L.grx_arena_usage.argtypes = [C.c_void_p, P(C.c_size_t), P(C.c_size_t), P(C.c_size_t)]
@@ -778,14 +781,27 @@ class GcmcBatch:
         check(self.L.grx_gcmc_batch_get_shape(self.h, C.byref(w), C.byref(m)), "grx_gcmc_batch_get_shape")
         return w.value, m.value
 
+    def set_cluster(self, cluster):
+        """CTAs per box (1, or 2 / 4 / 8 with 24 warps per block): one chain per
+        thread-block cluster."""
+        check(self.L.grx_gcmc_batch_set_cluster(self.h, cluster), "grx_gcmc_batch_set_cluster")
+
+    def cluster(self):
+        c = C.c_int32()
+        check(self.L.grx_gcmc_batch_get_cluster(self.h, C.byref(c)), "grx_gcmc_batch_get_cluster")
+        return c.value
+
     def autotune(self, nsteps):
         """Times the GCMC_TUNE_CANDIDATES launch shapes on real steps (forward and
-        reverse sweep, ranked by trial energies per second) and keeps the best:
-        returns ((nwarps, chunk_mult), mean ms per candidate probe)."""
+        reverse sweep, ranked by trial energies per second), then, when the boxes leave
+        SMs idle, the best shape against thread-block clusters, and keeps the best:
+        returns ((nwarps, chunk_mult), mean ms per plain candidate probe); the cluster
+        size kept is cluster()."""
         ch = C.c_int32()
         ms = (C.c_float * GCMC_TUNE_CANDIDATES)()
         check(self.L.grx_gcmc_batch_autotune(self.h, nsteps, C.byref(ch), ms), "grx_gcmc_batch_autotune")
-        return (ch.value // 100, ch.value % 100), list(ms)
+        rest = ch.value % 10000
+        return (rest // 100, rest % 100), list(ms)
 
 
 def cbmc_select(logw, seed, stream, move, word):

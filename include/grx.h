@@ -420,13 +420,25 @@ grx_status grx_gcmc_batch_reset_stats(grx_gcmc_batch* batch);
  * with chunk_mult 1. */
 grx_status grx_gcmc_batch_set_shape(grx_gcmc_batch* batch, int32_t nwarps, int32_t chunk_mult);
 grx_status grx_gcmc_batch_get_shape(grx_gcmc_batch* batch, int32_t* nwarps, int32_t* chunk_mult);
+/* Thread-block clusters: with cluster 2, 4 or 8 (nwarps must be 24) every box runs on a
+ * cluster of that many CTAs, one per SM: the bead passes are split over the cluster and
+ * the partial sums exchanged through distributed shared memory, so one chain spans
+ * several SMs (batches with fewer boxes than SMs). Refused when not every box gets a
+ * resident cluster of that size. Setting a shape with nwarps other than 24 returns to 1.
+ * Same decisions as the one-block launch in the oracle tests; the summation order of the
+ * partials differs. */
+grx_status grx_gcmc_batch_set_cluster(grx_gcmc_batch* batch, int32_t cluster);
+grx_status grx_gcmc_batch_get_cluster(grx_gcmc_batch* batch, int32_t* cluster);
 /* Autotuner of the launch shape: runs nsteps real steps for each of the
  * GRX_GCMC_TUNE_CANDIDATES shapes (nwarps 8, 12, 24 x chunk_mult 1, 2, 4, in that
  * order), in a forward and a reverse sweep timed with CUDA events, and keeps the shape
- * with the most trial energies per second for this batch. chosen receives
- * nwarps * 100 + chunk_mult; ms_per_candidate receives GRX_GCMC_TUNE_CANDIDATES mean
- * probe times (or NULL). The probe steps are ordinary Monte Carlo steps: the chains
- * advance by 2 * GRX_GCMC_TUNE_CANDIDATES * nsteps. */
+ * with the most trial energies per second for this batch. When the boxes leave SMs idle
+ * (clusters of 2, 4 or 8 fit, the largest is taken), the best shape is then timed
+ * against that cluster size with 24 warps (order: plain, cluster, cluster, plain) and the
+ * faster kept. chosen receives (cluster - 1) * 10000 + nwarps * 100 + chunk_mult;
+ * ms_per_candidate receives GRX_GCMC_TUNE_CANDIDATES mean probe times of the plain shapes
+ * (or NULL). The probe steps are ordinary Monte Carlo steps: the chains advance by up to
+ * 2 * (GRX_GCMC_TUNE_CANDIDATES + 2) * nsteps. */
 #define GRX_GCMC_TUNE_CANDIDATES 9
 grx_status grx_gcmc_batch_autotune(grx_gcmc_batch* batch, int64_t nsteps, int32_t* chosen,
                                    float* ms_per_candidate);

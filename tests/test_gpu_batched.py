@@ -116,9 +116,12 @@ def test_autotune_keeps_chains_valid(grx_lib):
     chosen, ms = batch.autotune(20)
     assert chosen[0] in (8, 12, 24) and chosen[1] in (1, 2, 4) and batch.shape() == chosen
     assert len(ms) == grx_lib.GCMC_TUNE_CANDIDATES and all(m > 0 for m in ms)
+    # two boxes leave SMs idle: the best shape is also probed against clusters of 8
+    # (plain, cluster, cluster, plain) and the faster kept
+    assert batch.cluster() in (1, 8) and (batch.cluster() == 1 or chosen[0] == 24)
     batch.launch(100)
     st, nxt = batch.stats()
-    assert nxt == 2 * 20 * grx_lib.GCMC_TUNE_CANDIDATES + 100
+    assert nxt == 2 * 20 * grx_lib.GCMC_TUNE_CANDIDATES + 4 * 20 + 100
     batch.close()
     for i, b in enumerate(boxes):
         esum = st[2 * i].energy[3] + st[2 * i + 1].energy[3]

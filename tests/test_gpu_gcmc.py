@@ -189,11 +189,65 @@ def test_gcmc_launch_shapes_match_oracle(grx_lib, shape):
         grx_lib.GcmcBatch([box], [d], grx_lib.GRX_FP64).set_shape(16, 1)
 
 
-def test_gcmc_mixed_ewald_row_products_match_oracle(grx_lib):
+@pytest.mark.parametrize("cl,prec", [(2, "GRX_FP64"), (4, "GRX_FP64"), (8, "GRX_FP64"), (8, "GRX_MIXED")])
+def test_gcmc_cluster_matches_oracle(grx_lib, cl, prec):
+    """One chain per thread-block cluster of cl CTAs (24 warps each): the bead passes are
+    split across the cluster and the partial sums exchanged through distributed shared
+    memory, every CTA reduces them in the same order and takes the same decisions. Two
+    boxes (two clusters) with different streams, each against its own oracle chain: FP64
+    decisions, positions and energies as the oracle; mixed the same decisions and positions,
+    energies within beta*|dE| <= 1e-5. Charged CO2, so the Ewald delta and the S(k) commit
+    (computed by every CTA) are exercised with the commit barrier."""
+    s = co2_system(n_co2=5)
+    descs = [params(grx_lib, pressure_pa=1e6, stream=k) for k in range(2)]
+    boxes = [make_box(grx_lib, s) for _ in range(2)]
+    batch = grx_lib.GcmcBatch(boxes, descs, getattr(grx_lib, prec))
+    batch.set_shape(24, 2)
+    batch.set_cluster(cl)
+    assert batch.cluster() == cl
+    batch.run_graph(150, 2)
+    st, nxt = batch.stats()
+    batch.close()
+    assert nxt == 300
+    nfw = s["comp_start"][1]
+    for k in range(2):
+        ost, after, _ = O.OracleSystem(s).gcmc(ora_params(descs[k]), [nfw, CAP], 0, 300)
+        assert list(st[k].attempts) == list(ost.attempts) and list(st[k].accepted) == list(ost.accepted)
+        assert st[k].n_molecules == ost.n_molecules
+        assert np.max(np.abs(boxes[k].positions(1) - after["pos"][nfw:])) <= 1e-9
+        for e in range(4):
+            if prec == "GRX_FP64":
+                assert abs(st[k].energy[e] - ost.energy[e]) <= 1e-9 * max(1.0, abs(ost.energy[e]))
+            else:
+                assert descs[k].beta * abs(st[k].energy[e] - ost.energy[e]) <= 1e-5
+    assert sum(st[0].accepted) > 30
+
+
+def test_gcmc_cluster_shape_rules(grx_lib):
+    """Clusters need 24 warps per block; a shape with fewer warps returns to one block."""
+    s = co2_system(n_co2=2)
+    box = make_box(grx_lib, s)
+    batch = grx_lib.GcmcBatch([box], [params(grx_lib)], grx_lib.GRX_FP64)
+    batch.set_shape(12, 1)
+    with pytest.raises(grx_lib.GrxError):
+        batch.set_cluster(2)
+    with pytest.raises(grx_lib.GrxError):
+        batch.set_cluster(3)
+    batch.set_shape(24, 1)
+    batch.set_cluster(4)
+    batch.set_shape(8, 1)
+    assert batch.cluster() == 1
+    batch.close()
+
+
+@pytest.mark.parametrize("cl", [1, 8])
+def test_gcmc_mixed_ewald_row_products_match_oracle(grx_lib, cl):
     """A charged box with many k vectors per (kx, ky) row (automatic Ewald set-up of a
     2,500-atom framework: kmax 10/16/15, 8,466 active k, 23 per row) takes the row-product
     form of the double-float Ewald delta; the mixed chain still takes the oracle's exact
-    decisions and positions, with energies within beta*|dE| <= 1e-5 over the run."""
+    decisions and positions, with energies within beta*|dE| <= 1e-5 over the run. With a
+    cluster of 8 CTAs the k vectors are split across the cluster as well (each CTA stages
+    and commits its own range of S(k))."""
     from graspa_gb300 import synth
     s = synth.adsorbate_system("CO2", 12, n_atoms=2500)
     S = O.OracleSystem(s)
@@ -203,11 +257,25 @@ def test_gcmc_mixed_ewald_row_products_match_oracle(grx_lib):
     d = params(grx_lib, pressure_pa=1e6)
     nfw = s["comp_start"][1]
     box = make_box(grx_lib, s)
-    st = grx_lib.gcmc_run([box], [d], 0, 250, grx_lib.GRX_MIXED)[0]
+    if cl == 1:
+        st = grx_lib.gcmc_run([box], [d], 0, 250, grx_lib.GRX_MIXED)[0]
+    else:
+        batch = grx_lib.GcmcBatch([box], [d], grx_lib.GRX_MIXED)
+        batch.set_shape(24, 1)
+        batch.set_cluster(cl)
+        batch.launch(250)
+        st = batch.stats()[0][0]
+        batch.close()
     ost, after, _ = S.gcmc(ora_params(d), [nfw, CAP], 0, 250)
     assert sum(st.accepted) > 20
     assert list(st.accepted) == list(ost.accepted) and st.n_molecules == ost.n_molecules
     assert np.max(np.abs(box.positions(1) - after["pos"][nfw:])) <= 1e-9
     for k in range(4):
         assert d.beta * abs(st.energy[k] - ost.energy[k]) <= 1e-5
+    # the committed adsorbate S(k) (every CTA's range of k) equals S(k) recomputed from
+    # the final positions
+    _, s_run, _ = box.structure_factors()
+    box.ewald_total()
+    _, s_new, _ = box.structure_factors()
+    assert np.max(np.abs(s_run - s_new)) <= 1e-9 * max(1.0, np.max(np.abs(s_new)))
     box.close()
