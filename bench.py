@@ -248,7 +248,8 @@ def bench_gcmc(args, grx, torch, stream, flush, rank, world, dist):
         b.ewald_total()
     batch = grx.GcmcBatch(boxes, descs, grx.GRX_MIXED)
     shape, cand = batch.autotune(S)   # real steps at the timed launch length; picks the launch shape
-    out["autotune"] = {"warps_per_box": shape[0], "chunk_mult": shape[1], "ms_per_candidate": cand}
+    out["autotune"] = {"warps_per_box": shape[0], "chunk_mult": shape[1], "cluster": batch.cluster(),
+                       "ms_per_candidate": cand}
     l0 = grx.launch_count()
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
     clocks.start()
@@ -427,7 +428,7 @@ def bench_serving(args, grx):
     g = np.random.default_rng(7)
     arrivals = np.cumsum(g.exponential(1.0 / rate, n))
     srv = grx.Server(args.serve_hbm_gb * (1 << 30), max_resident=args.serve_slots, prec=grx.GRX_MIXED,
-                     widom_slice=0, gcmc_slice=args.serve_gcmc_slice)
+                     widom_slice=0, gcmc_slice=args.serve_gcmc_slice, cluster_atoms=args.serve_cluster_atoms)
     out = serving.run_stream(srv, jobs, arrivals, timeout=600.0)
     srv.close()
     summ = serving.summarize(out)
@@ -443,6 +444,7 @@ def bench_serving(args, grx):
     svc = np.array([r.t_done - r.t_admit for (r, _) in out64.values()])
     te64 = sum(serving.trial_energies_of(sub[i], r) for i, (r, _) in out64.items())
     return {"jobs": n, "arrival_rate_per_s": rate, "slots": args.serve_slots, "gcmc_cycles": args.serve_gcmc_cycles,
+            "cluster_atoms": args.serve_cluster_atoms,
             "widom_insertions": 5000, "species": "CH4 CO2 N2 Xe Kr uniform", "framework_atoms": "200-20000 log-uniform",
             **summ,
             "plain_fp64_one_at_a_time": {"jobs": len(sub), "jobs_per_s": len(sub) / dt,
@@ -565,6 +567,7 @@ def bench_other(args, grx, torch, stream, flush, which):
         prec = grx.GRX_MIXED
         batch = grx.GcmcBatch(boxes, descs, prec)
         chosen, cand_ms = batch.autotune(args.mc_steps)
+        cluster = batch.cluster()   # 64 boxes leave SMs idle: clusters of 2 CTAs are probed
         times, stats = timed_graph(torch, batch, stream, args.mc_steps, args.steps, args.warmup, flush)
         batch.close()
         te = 0.0
@@ -585,7 +588,8 @@ def bench_other(args, grx, torch, stream, flush, which):
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * t / args.steps,
                 "workload": "batched_ch4_xe_64_triclinic (mixture GCMC, 8-32 trials, LJ only)",
                 "mc_steps_per_step": args.mc_steps,
-                "autotune": {"warps_per_box": chosen[0], "chunk_mult": chosen[1], "ms_per_candidate": cand_ms},
+                "autotune": {"warps_per_box": chosen[0], "chunk_mult": chosen[1], "cluster": cluster,
+                             "ms_per_candidate": cand_ms},
                 "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak(grx), "unit": "TFLOP/s",
                              "frac": achieved / fp32_peak(grx), "model": "40 FLOP/pair (LJ only)"},
                 "framework_atoms": [int(s["comp_start"][1]) for s in systems[:8]]}
@@ -727,6 +731,8 @@ def main():
     ap.add_argument("--serve-gcmc-cycles", type=int, default=100, help="GCMC cycles of 20 steps per serving job")
     ap.add_argument("--serve-gcmc-slice", type=int, default=500)
     ap.add_argument("--serve-fp64-jobs", type=int, default=6)
+    ap.add_argument("--serve-cluster-atoms", type=int, default=2500,
+                    help="GCMC jobs of N atoms run on clusters of up to N / this many CTAs (0: off)")
     ap.add_argument("--profile", action="store_true", help="only the timed mixed GCMC steps (launch lists)")
     args = ap.parse_args()
     if args.impl == "reference":

@@ -117,6 +117,15 @@ grx_status admit_job(grx_server* S, ServerJob* j) {
   if (st == GRX_OK && j->kind == GRX_JOB_GCMC) {
     const int32_t nm = (int32_t)j->gcmc.size();
     st = grx_gcmc_batch_create(&j->box, 1, j->gcmc.data(), &nm, S->cfg.precision, &j->batch);
+    if (st == GRX_OK && S->cfg.cluster_atoms > 0) {  // a large box spans several SMs
+      int64_t natoms = 0;
+      for (int c = 0; c < j->desc.ncomponents; ++c) natoms += (int64_t)j->size[c];
+      for (int32_t cl : {8, 4, 2}) {
+        if (natoms < cl * S->cfg.cluster_atoms) continue;
+        if (grx_gcmc_batch_set_shape(j->batch, 24, 1) == GRX_OK && grx_gcmc_batch_set_cluster(j->batch, cl) == GRX_OK)
+          break;
+      }
+    }
   }
   if (st == GRX_OK && j->kind == GRX_JOB_WIDOM) {
     j->d_results = (grx_widom_result*)arena_alloc(S->arena, std::max<int64_t>(j->total, 1) * sizeof(grx_widom_result));

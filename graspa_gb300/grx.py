@@ -109,7 +109,7 @@ GCMC_TUNE_CANDIDATES = 9  # GRX_GCMC_TUNE_CANDIDATES: warps per box 8/12/24 x it
 
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_resident", C.c_int32), ("precision", C.c_int32),
-                ("widom_slice", C.c_int64), ("gcmc_slice", C.c_int64)]
+                ("widom_slice", C.c_int64), ("gcmc_slice", C.c_int64), ("cluster_atoms", C.c_int64)]
 
 
 class JobDesc(C.Structure):
@@ -591,9 +591,11 @@ def box_footprint(system, capacity=None):
 class Server:
     """grx_server: continuous-batching Widom / GCMC job server."""
 
-    def __init__(self, hbm_budget_bytes, max_resident, prec=GRX_MIXED, widom_slice=0, gcmc_slice=0):
+    def __init__(self, hbm_budget_bytes, max_resident, prec=GRX_MIXED, widom_slice=0, gcmc_slice=0,
+                 cluster_atoms=0):
         self.L = load()
-        cfg = ServerConfig(int(hbm_budget_bytes), int(max_resident), int(prec), int(widom_slice), int(gcmc_slice))
+        cfg = ServerConfig(int(hbm_budget_bytes), int(max_resident), int(prec), int(widom_slice), int(gcmc_slice),
+                           int(cluster_atoms))
         h = C.c_void_p()
         check(self.L.grx_server_create(C.byref(cfg), None, C.byref(h)), "grx_server_create")
         self.h = h

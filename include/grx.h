@@ -467,6 +467,10 @@ typedef struct {
   grx_precision precision;
   int64_t widom_slice;          /* insertions per launch (<= 0: whole job) */
   int64_t gcmc_slice;           /* steps per launch (<= 0: whole job) */
+  int64_t cluster_atoms;        /* > 0: a GCMC job of N atoms runs on a thread-block cluster of
+                                   the largest of 8, 4, 2 CTAs not above N / cluster_atoms
+                                   (grx_gcmc_batch_set_cluster; one block when it does not fit);
+                                   0: one block per job */
 } grx_server_config;
 
 typedef struct {

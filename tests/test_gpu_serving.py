@@ -102,3 +102,21 @@ def test_admission_by_footprint_and_slots(grx_lib):
     out = serving.run_stream(tiny, jobs[:1])
     tiny.close()
     assert out[0][0].status == 3                          # GRX_ERR_OUT_OF_MEMORY
+
+
+def test_cluster_jobs_take_the_same_decisions(grx_lib):
+    """GCMC jobs whose boxes pass the cluster policy (cluster_atoms) run on thread-block
+    clusters of up to 8 CTAs; in FP64 they take the same decisions as on one block, with
+    energies equal to 1e-9 (the partials are summed in another order)."""
+    jobs = [J for J in small_jobs(16) if J["kind"] == "gcmc"][:4]
+    assert len(jobs) == 4
+    natoms = [int(J["system"]["comp_start"][-1]) for J in jobs]
+    assert max(natoms) >= 2 * 300   # at least one job runs on a cluster
+    fp = max(grx_lib.box_footprint(J["system"], J["capacity"]) for J in jobs)
+    out = []
+    for cl_atoms in (300, 0):
+        srv = grx_lib.Server(8 * fp, max_resident=4, prec=grx_lib.GRX_FP64, gcmc_slice=100, cluster_atoms=cl_atoms)
+        out.append(serving.run_stream(srv, jobs))
+        srv.close()
+    for i in range(len(jobs)):
+        same(out[0][i][0], out[1][i][0])
