@@ -731,7 +731,7 @@ def main():
     ap.add_argument("--serve-gcmc-cycles", type=int, default=100, help="GCMC cycles of 20 steps per serving job")
     ap.add_argument("--serve-gcmc-slice", type=int, default=500)
     ap.add_argument("--serve-fp64-jobs", type=int, default=6)
-    ap.add_argument("--serve-cluster-atoms", type=int, default=2500,
+    ap.add_argument("--serve-cluster-atoms", type=int, default=1000,
                     help="GCMC jobs of N atoms run on clusters of up to N / this many CTAs (0: off)")
     ap.add_argument("--profile", action="store_true", help="only the timed mixed GCMC steps (launch lists)")
     args = ap.parse_args()

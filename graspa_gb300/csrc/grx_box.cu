@@ -6,6 +6,8 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <vector>
 
 #include "grx_host.h"
@@ -168,7 +170,48 @@ static void pbc_host(const BoxDev& b, double* d) {
 // the FP32 bits. Each piece is the degree-5 interpolant at Chebyshev nodes, fitted in
 // long double from erfcl; the worst relative error found on a dense sample is kept in
 // ctab_maxrel (about 1e-14 for the benchmark systems).
+struct CoulombTable {
+  int base = 0, n = 0;
+  double maxrel = 0.0;
+  std::vector<double> tab;  // 8 per piece: s0, 1/width, 6 coefficients
+  std::vector<float4> tf;   // the double-float copy
+};
+
+static void fit_coulomb_table(double alpha, double cut2, CoulombTable& T);
+
+// The table depends on (alpha, cutoff^2) only, and its long-double fit costs tens of
+// milliseconds (software quad precision on some hosts): fitted once per pair of values in
+// the process, then uploaded per box.
+static const CoulombTable& coulomb_table(double alpha, double cut2) {
+  static std::mutex m;
+  static std::map<std::pair<uint64_t, uint64_t>, CoulombTable> cache;
+  uint64_t ka, kc;
+  std::memcpy(&ka, &alpha, 8);
+  std::memcpy(&kc, &cut2, 8);
+  std::lock_guard<std::mutex> g(m);
+  auto it = cache.find({ka, kc});
+  if (it != cache.end()) return it->second;
+  if (cache.size() >= 64) cache.clear();
+  CoulombTable& T = cache[{ka, kc}];
+  fit_coulomb_table(alpha, cut2, T);
+  return T;
+}
+
 static grx_status build_coulomb_table(grx_box* b, double alpha, double cut2) {
+  const CoulombTable& T = coulomb_table(alpha, cut2);
+  b->ctab_base = T.base;
+  b->ctab_n = T.n;
+  b->ctab_maxrel = T.maxrel;
+  GRX_CHECK_CUDA(dev_alloc(b, (void**)&b->ctab, T.tab.size() * sizeof(double)), "alloc Coulomb table");
+  GRX_CHECK_CUDA(cudaMemcpy(b->ctab, T.tab.data(), T.tab.size() * sizeof(double), cudaMemcpyHostToDevice),
+                 "upload Coulomb table");
+  GRX_CHECK_CUDA(dev_alloc(b, (void**)&b->ctabf, T.tf.size() * sizeof(float4)), "alloc Coulomb table (float pairs)");
+  GRX_CHECK_CUDA(cudaMemcpy(b->ctabf, T.tf.data(), T.tf.size() * sizeof(float4), cudaMemcpyHostToDevice),
+                 "upload Coulomb table (float pairs)");
+  return GRX_OK;
+}
+
+static void fit_coulomb_table(double alpha, double cut2, CoulombTable& T) {
   const float s_lo = 0.25f;
   uint32_t lo_bits, hi_bits;
   std::memcpy(&lo_bits, &s_lo, 4);
@@ -216,9 +259,9 @@ static grx_status build_coulomb_table(grx_box* b, double alpha, double cut2) {
       maxrel = std::max(maxrel, (double)fabsl((pv - ex) / ex));
     }
   }
-  b->ctab_base = base;
-  b->ctab_n = n;
-  b->ctab_maxrel = maxrel;
+  T.base = base;
+  T.n = n;
+  T.maxrel = maxrel;
   // double-float copy: s0 and 1/width are exact floats (width is a power of two)
   std::vector<float4> tf(4 * (size_t)n);
   for (int k = 0; k < n; ++k) {
@@ -233,13 +276,8 @@ static grx_status build_coulomb_table(grx_box* b, double alpha, double cut2) {
     tf[4 * k + 2] = make_float4(c[3].x, c[3].y, c[4].x, c[4].y);
     tf[4 * k + 3] = make_float4(c[5].x, c[5].y, 0.0f, 0.0f);
   }
-  GRX_CHECK_CUDA(dev_alloc(b, (void**)&b->ctab, tab.size() * sizeof(double)), "alloc Coulomb table");
-  GRX_CHECK_CUDA(cudaMemcpy(b->ctab, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice),
-                 "upload Coulomb table");
-  GRX_CHECK_CUDA(dev_alloc(b, (void**)&b->ctabf, tf.size() * sizeof(float4)), "alloc Coulomb table (float pairs)");
-  GRX_CHECK_CUDA(cudaMemcpy(b->ctabf, tf.data(), tf.size() * sizeof(float4), cudaMemcpyHostToDevice),
-                 "upload Coulomb table (float pairs)");
-  return GRX_OK;
+  T.tab = std::move(tab);
+  T.tf = std::move(tf);
 }
 
 // Storage order of host atoms: recursive bisection of the wrapped Cartesian positions
