@@ -476,6 +476,11 @@ def run_grx(args):
         if rank == 0:
             print(json.dumps(line), flush=True)
         return
+    if args.workload == "cluster":
+        line = bench_cluster(args, grx, torch, stream, flush)
+        if rank == 0:
+            print(json.dumps(line), flush=True)
+        return
     if args.workload == "serving":
         s = bench_serving(args, grx)
         if rank == 0:
@@ -629,6 +634,40 @@ def bench_other(args, grx, torch, stream, flush, which):
             "speedup_mixed_over_fp64": out["mixed"]["value"] / out["fp64"]["value"]}
 
 
+def bench_cluster(args, grx, torch, stream, flush):
+    """Single-chain latency on thread-block clusters: one CO2 box in a charged framework of
+    5,000 or 20,000 atoms (the large serving jobs; automatic Ewald set-up), 200 GCMC steps per
+    launch in mixed precision, on one 24-warp block and on clusters of 2, 4 and 8 CTAs. Each
+    size runs the same chain (same seed and stream) from the same start; ms per launch by CUDA
+    events, L2 flushed before each launch."""
+    from graspa_gb300 import synth
+    S = 200
+    out = {}
+    for natoms in (5000, 20000):
+        s = synth.adsorbate_system("CO2", 7, n_atoms=natoms)
+        nfw = s["comp_start"][1]
+        d = grx.gcmc_desc(1, p_translation=0.25, p_rotation=0.5, p_reinsertion=0.5, p_swap=1.0, pressure_pa=1e5,
+                          seed=42, stream=0)
+        row = {}
+        for cl in (1, 2, 4, 8):
+            box = grx.Box(s, capacity=[nfw, 3 * 200])
+            box.set_stream(stream.cuda_stream)
+            box.ewald_total()
+            batch = grx.GcmcBatch([box], [d], grx.GRX_MIXED)
+            batch.set_shape(24, 1)
+            if cl > 1:
+                batch.set_cluster(cl)
+            times, stats = timed_graph(torch, batch, stream, S, args.steps, args.warmup, flush)
+            row[f"cluster_{cl}_ms"] = 1000 * sum(times) / len(times)
+            batch.close()
+            box.close()
+        row["speedup_8"] = row["cluster_1_ms"] / row["cluster_8_ms"]
+        out[f"co2_{natoms}_atoms"] = row
+    return {"metric": "ms per launch of 200 GCMC steps (one chain)", "unit": "ms", "higher_is_better": False,
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "workload": "single CO2 chain on 1 block and on clusters of 2/4/8 CTAs (mixed)", **out}
+
+
 # ------------------------------------------------------------------ reference arm
 def _oracle_chain(system, desc, first, nsteps):
     from graspa_gb300 import grx
@@ -718,7 +757,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="grx", choices=["grx", "reference"])
-    ap.add_argument("--workload", default="gcmc", choices=["gcmc", "widom", "batched", "water", "serving"])
+    ap.add_argument("--workload", default="gcmc", choices=["gcmc", "widom", "batched", "water", "serving", "cluster"])
     ap.add_argument("--chains", type=int, default=0, help="GCMC chains (default: three per SM)")
     ap.add_argument("--mc-steps", type=int, default=100, help="Monte Carlo steps of every chain per step")
     ap.add_argument("--insertions", type=int, default=20000, help="Widom insertions per launch")
