@@ -66,6 +66,32 @@ def test_mixture_gcmc_matches_oracle(grx_lib):
         assert np.max(np.abs(box.positions(c) - after["pos"][a:b]), initial=0.0) <= 1e-9
 
 
+@pytest.mark.parametrize("cl", [2, 8])
+def test_mixture_gcmc_on_clusters_matches_oracle(grx_lib, cl):
+    """Two triclinic CH4 / Xe boxes (LJ only, two moved components each) on thread-block
+    clusters: every box's FP64 chain takes its oracle chain's decisions, counts and positions."""
+    seeds = (3, 5)
+    systems = [synth.ch4_xe_system(k, n_ch4=5, n_xe=5) for k in seeds]
+    descs = [mix_descs(grx_lib, stream=k) for k in range(2)]
+    boxes = [make_box(grx_lib, s) for s in systems]
+    batch = grx_lib.GcmcBatch(boxes, descs, grx_lib.GRX_FP64)
+    batch.set_shape(24, 1)
+    batch.set_cluster(cl)
+    batch.launch(300)
+    st, _ = batch.stats()
+    batch.close()
+    for i, s in enumerate(systems):
+        ost, after, _ = O.OracleSystem(s).gcmc([ora_params(d) for d in descs[i]], [s["comp_start"][1], CAP, CAP],
+                                               0, 300)
+        for k in range(2):
+            assert list(st[2 * i + k].attempts) == list(ost[k].attempts)
+            assert list(st[2 * i + k].accepted) == list(ost[k].accepted)
+            assert st[2 * i + k].n_molecules == ost[k].n_molecules and st[2 * i + k].sum_n == ost[k].sum_n
+        for c in (1, 2):
+            a, b = after["comp_start"][c], after["comp_start"][c + 1]
+            assert np.max(np.abs(boxes[i].positions(c) - after["pos"][a:b]), initial=0.0) <= 1e-9
+
+
 def test_batch_launch_graph_and_resume(grx_lib):
     seeds = [0, 3, 5, 7]
     systems = [synth.ch4_xe_system(k) for k in seeds]
