@@ -132,20 +132,22 @@ __device__ __noinline__ void gen_orientations(const BoxDev& b, WK& W, uint64_t s
 }
 
 // Energies of ntr = nb / chain trials of `chain` beads each (W.beads) against every
-// atom, with the atoms of (comp, newmol) excluded: W.te[4 t + k], W.tflag[t].
+// atom, with the atoms of (comp, newmol) and of (excl_comp, excl_mol) excluded (the
+// ExcludeList of an identity swap): W.te[4 t + k], W.tflag[t].
 // With CL > 1 the block is one CTA of a cluster that shares the chain: the pass is split
 // over the cluster's warps (items per warp capped so the slots fit the workspace), each
 // CTA copies its slots into its peers' workspaces, and every CTA reduces all slots. The
 // second cluster barrier keeps a CTA from writing the next pass's slots into a peer that
 // is still reducing this one.
-template <int PREC, int CL = 1, class WK>
-__device__ __noinline__ void trial_pass(const BoxDev& b, WK& W, int nb, int chain, int comp, int newmol) {
+template <int PREC, int CL, class WK>
+__device__ __forceinline__ void trial_pass_body(const BoxDev& b, WK& W, int nb, int chain, int comp, int newmol,
+                                                int excl_comp, int excl_mol) {
   if (threadIdx.x == 0) W.counter = 0;
   __syncthreads();
   const int nw = (int)(blockDim.x >> 5);
   if constexpr (CL == 1) {
     const PassSplit sp = pass_split(b, nb, nw, b.chunk_mult);
-    block_bead_pass<PREC>(b, W.beads, nb, comp, newmol, -1, -1, W.qbuf, W.ipart, W.iflag, &W.counter, sp);
+    block_bead_pass<PREC>(b, W.beads, nb, comp, newmol, excl_comp, excl_mol, W.qbuf, W.ipart, W.iflag, &W.counter, sp);
     __syncthreads();
     reduce_items<PREC>(W.ipart, W.iflag, nb / chain, chain, sp, W.te, W.tflag);
     __syncthreads();
@@ -154,7 +156,7 @@ __device__ __noinline__ void trial_pass(const BoxDev& b, WK& W, int nb, int chai
     const unsigned rank = cluster_rank();
     int i0, i1;
     cluster_items(sp, CL, rank, i0, i1);
-    block_bead_pass<PREC>(b, W.beads, nb, comp, newmol, -1, -1, W.qbuf, W.ipart, W.iflag, &W.counter, sp, i0, i1);
+    block_bead_pass<PREC>(b, W.beads, nb, comp, newmol, excl_comp, excl_mol, W.qbuf, W.ipart, W.iflag, &W.counter, sp, i0, i1);
     __syncthreads();
     if (sp.nu > 0 && i0 < i1) {  // this CTA's slots [s0, s0 + n): item + bead, increasing
       unsigned lo, hi;
@@ -179,6 +181,17 @@ __device__ __noinline__ void trial_pass(const BoxDev& b, WK& W, int nb, int chai
     __syncthreads();
     cluster_sync_all();
   }
+}
+
+template <int PREC, int CL = 1, class WK>
+__device__ __noinline__ void trial_pass(const BoxDev& b, WK& W, int nb, int chain, int comp, int newmol) {
+  trial_pass_body<PREC, CL>(b, W, nb, chain, comp, newmol, -1, -1);
+}
+// The same with a second excluded molecule (excl_comp, excl_mol).
+template <int PREC, int CL = 1, class WK>
+__device__ __noinline__ void trial_pass_excl(const BoxDev& b, WK& W, int nb, int chain, int comp, int newmol,
+                                               int excl_comp, int excl_mol) {
+  trial_pass_body<PREC, CL>(b, W, nb, chain, comp, newmol, excl_comp, excl_mol);
 }
 
 // CBMC weight of one growth step (warp 0 computes, results in W.ok/sel/w/nok/wraw).

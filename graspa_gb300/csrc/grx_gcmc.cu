@@ -58,6 +58,7 @@ struct grx_gcmc_batch {
   int chunk_mult = 1;
   int nwarps = 8;  // warps per box (block size / 32): 8, 12 or 24
   int cluster = 1; // CTAs per box (1, or 2 / 4 / 8 with 24 warps each)
+  bool swaps = false;  // a move set with identity swaps: the IDS kernel
   void* mem = nullptr;
   grx_arena* arena = nullptr;
   BoxDev* d_boxes = nullptr;
@@ -80,6 +81,13 @@ namespace grx {
 // (kx, ky) row products (at most kEwRowBytes); with the largest static workspace (24 warps)
 // it stays within the 227 KB of one block.
 constexpr size_t kGcmcDynSmem = 160 * 1024;
+
+// A move set with identity swaps (a range of p_identity_swap above p_reinsertion).
+static bool has_swaps(const grx_gcmc_desc* descs, int n) {
+  for (int e = 0; e < n; ++e)
+    if (descs[e].p_identity_swap > descs[e].p_reinsertion) return true;
+  return false;
+}
 
 // Validates the boxes and move sets and fills the per-box state and per-entry args.
 static grx_status prepare_gcmc(grx_box* const* boxes, int32_t nboxes, const grx_gcmc_desc* descs,
@@ -122,6 +130,10 @@ static grx_status prepare_gcmc(grx_box* const* boxes, int32_t nboxes, const grx_
                   "grx_gcmc: norient * (molecule size - 1) must be <= 128");
       GRX_REQUIRE(2 * ms <= kCbmcBeads, "grx_gcmc: molecule too large");
       GRX_REQUIRE(d.beta > 0 && d.pressure > 0 && d.ideal_rosenbluth > 0, "grx_gcmc: bad thermodynamic state");
+      GRX_REQUIRE(d.p_identity_swap == 0.0 || (d.p_identity_swap >= d.p_reinsertion && d.p_identity_swap <= d.p_swap),
+                  "grx_gcmc: p_identity_swap must lie between p_reinsertion and p_swap (cumulative)");
+      GRX_REQUIRE(d.p_identity_swap <= d.p_reinsertion || d.tail_insert == 0.0,
+                  "grx_gcmc: identity swaps with tail corrections are not supported");
       GcmcArgs a{};
       a.d = d;
       a.comp = d.component;
@@ -167,6 +179,7 @@ static grx_status set_gcmc_smem() {
                        set_smem_one<GRX_FP32, 8>(), set_smem_one<GRX_FP32, 12>(), set_smem_one<GRX_FP32, 24>()})
     if (r && !st) st = r;
   if (!st) GRX_CHECK_CUDA(set_gcmc_cluster_smem(kGcmcDynSmem), "gcmc cluster shared memory attribute");
+  if (!st) GRX_CHECK_CUDA(set_gcmc_swap_smem(kGcmcDynSmem), "gcmc identity-swap shared memory attribute");
   if (!st && dev >= 0 && dev < 64) done[dev] = true;
   return st;
 }
@@ -201,8 +214,12 @@ static void launch_shape(grx_precision prec, int nboxes, const BoxDev* dboxes, c
 // when cl > 1, nw = 24) and the step-counter advance (no host sync).
 static grx_status enqueue_gcmc(grx_precision prec, int nw, int nboxes, const BoxDev* dboxes, const GcmcArgs* dargs,
                                const int* dfirst, uint64_t* dstep, int64_t nsteps, grx_gcmc_stats* dstats,
-                               size_t smem, cudaStream_t stream, int cl = 1) {
-  if (cl > 1) {
+                               size_t smem, cudaStream_t stream, int cl = 1, bool swaps = false) {
+  if (swaps) {
+    GRX_REQUIRE(cl == 1, "grx_gcmc: identity swaps run on one block per box");
+    GRX_CHECK_CUDA(launch_gcmc_swap(prec, nw, nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem, stream),
+                   "gcmc identity-swap launch");
+  } else if (cl > 1) {
     GRX_REQUIRE(nw == 24, "grx_gcmc: cluster launches use 24 warps per block");
     GRX_CHECK_CUDA(launch_gcmc_cluster(prec, cl, nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem, stream),
                    "gcmc cluster launch");
@@ -293,7 +310,7 @@ extern "C" grx_status grx_gcmc_run(grx_box* const* boxes, int32_t nboxes, const 
     st = set_gcmc_smem();
     if (st) return st;
     st = enqueue_gcmc(prec, default_warps(nboxes), nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem,
-                      b0->stream);
+                      b0->stream, 1, has_swaps(descs, ne));
     if (st) return st;
   }
   GRX_CHECK_CUDA(cudaMemcpyAsync(stats, dstats, ne * sizeof(grx_gcmc_stats), cudaMemcpyDefault, b0->stream),
@@ -325,6 +342,7 @@ extern "C" grx_status grx_gcmc_batch_create(grx_box* const* boxes, int32_t nboxe
   B->nwarps = default_warps(nboxes);
   B->boxes.assign(boxes, boxes + nboxes);
   B->descs.assign(descs, descs + B->nentries);
+  B->swaps = has_swaps(descs, B->nentries);
   B->device = boxes[0]->device;
   B->stream = boxes[0]->stream;
   auto al = [](size_t n) { return (n + 255) / 256 * 256; };
@@ -400,7 +418,7 @@ extern "C" grx_status grx_gcmc_batch_launch(grx_gcmc_batch* B, int64_t nsteps, v
   if (nsteps == 0) return GRX_OK;
   B->last_stream = s;
   return enqueue_gcmc(B->prec, B->nwarps, (int)B->boxes.size(), B->d_boxes, B->d_args, B->d_first, B->d_step, nsteps,
-                      B->d_stats, B->smem, s, B->cluster);
+                      B->d_stats, B->smem, s, B->cluster, B->swaps);
 }
 
 extern "C" grx_status grx_gcmc_batch_run_graph(grx_gcmc_batch* B, int64_t nsteps, int32_t nlaunch, void* stream) {
@@ -415,7 +433,7 @@ extern "C" grx_status grx_gcmc_batch_run_graph(grx_gcmc_batch* B, int64_t nsteps
     const uint64_t before = grx_launch_count();
     for (int k = 0; k < nlaunch && st == GRX_OK; ++k)
       st = enqueue_gcmc(B->prec, B->nwarps, (int)B->boxes.size(), B->d_boxes, B->d_args, B->d_first, B->d_step, nsteps,
-                        B->d_stats, B->smem, cap, B->cluster);
+                        B->d_stats, B->smem, cap, B->cluster, B->swaps);
     count_launch(0 - (grx_launch_count() - before));  // capture records the kernels, it launches nothing
     cudaGraph_t g = nullptr;
     const cudaError_t ec = cudaStreamEndCapture(cap, &g);
@@ -492,6 +510,7 @@ extern "C" grx_status grx_gcmc_batch_get_shape(grx_gcmc_batch* B, int32_t* nwarp
 // The largest cluster size (8, 4 or 2) for which every box of the batch gets its own
 // resident cluster, or 1 when the boxes already fill the SMs.
 static int max_cluster(const grx_gcmc_batch* B) {
+  if (B->swaps) return 1;  // identity swaps run on one block per box
   const int nb = (int)B->boxes.size();
   for (int cl : {8, 4, 2})
     if (gcmc_cluster_capacity(B->prec, cl, B->smem) >= nb) return cl;
@@ -503,6 +522,7 @@ extern "C" grx_status grx_gcmc_batch_set_cluster(grx_gcmc_batch* B, int32_t clus
   GRX_REQUIRE(cluster == 1 || cluster == 2 || cluster == 4 || cluster == 8,
               "grx_gcmc_batch_set_cluster: cluster must be 1, 2, 4 or 8");
   GRX_REQUIRE(cluster == 1 || B->nwarps == 24, "grx_gcmc_batch_set_cluster: clusters use 24 warps per block");
+  GRX_REQUIRE(cluster == 1 || !B->swaps, "grx_gcmc_batch_set_cluster: identity swaps run on one block per box");
   GRX_CHECK_CUDA(cudaStreamSynchronize(B->stream), "set cluster");
   if (cluster > 1) {
     GRX_CHECK_CUDA(cudaSetDevice(B->device), "set device");
@@ -568,7 +588,7 @@ extern "C" grx_status grx_gcmc_batch_autotune(grx_gcmc_batch* B, int64_t nsteps,
     GRX_CHECK_CUDA(read(before), "tune stats");
     GRX_CHECK_CUDA(cudaEventRecord(e0, B->stream), "event");
     st = enqueue_gcmc(B->prec, nw, nb, B->d_boxes, B->d_args, B->d_first, B->d_step, nsteps, B->d_stats, B->smem,
-                      B->stream, cl);
+                      B->stream, cl, B->swaps);
     if (st) return st;
     GRX_CHECK_CUDA(cudaEventRecord(e1, B->stream), "event");
     GRX_CHECK_CUDA(cudaEventSynchronize(e1), "event");

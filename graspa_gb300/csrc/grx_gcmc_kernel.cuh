@@ -19,7 +19,7 @@
 
 namespace grx {
 
-enum : uint32_t { SLOT_MOVE = 4096u, SLOT_DISP = 4097u };
+enum : uint32_t { SLOT_MOVE = 4096u, SLOT_DISP = 4097u, SLOT_SWAP = 4099u };
 constexpr int kMaxMoved = 4;  // moved components per box in one GCMC run
 
 struct GcmcArgs {
@@ -86,12 +86,162 @@ __device__ __forceinline__ void ewald_delta_move(const BoxDev& b, WK& W, int na,
   else ewald_move<PREC, WK, false, CL>(b, W, na, eik, b.s_tmp, same, cross);
 }
 
+// Identity swap of one step (mc_swap_moves.h:199-420), out of line so the kernel body keeps
+// its register allocation. The reference redraws the old and new component until the old one
+// holds a molecule: the old component is uniform over the moved components holding molecules,
+// the new one uniform over all moved components. Swap slot words: {old component, new
+// component, old molecule, acceptance}, as the host layer's IdentitySwapMove; the orientation
+// selection takes u_orient (word 1 of the selection slot). Called by every thread of the block.
+template <int PREC, int CL, class WK>
+__device__ __noinline__ void identity_swap_step(const BoxDev& b, const GcmcArgs* A, int nm, grx_gcmc_stats* ST, WK& W,
+                                                double2* eik, int* comp_size, uint64_t move, double beta,
+                                                double u_orient, int& s_accept, double* s_e1, double& s_w1,
+                                                double* s_dE, double* s_r1, double& s_wr) {
+  const int tid = threadIdx.x;
+  uint32_t wx[4];
+  draw4(A[0].d.seed, A[0].d.stream, move, SLOT_SWAP, wx);
+  int have[kMaxMoved], nh = 0;
+  for (int e = 0; e < nm; ++e)
+    if (comp_size[A[e].comp] >= A[e].ms) have[nh++] = e;
+  if (nh > 0) {
+    const int eo = have[min(nh - 1, (int)(u01(wx[0]) * (double)nh))];
+    const int en = min(nm - 1, (int)(u01(wx[1]) * (double)nm));
+    const GcmcArgs& ao = A[eo];
+    const GcmcArgs& an = A[en];
+    const int mso = ao.ms, msn = an.ms;
+    const int No = comp_size[ao.comp] / mso, Nn = comp_size[an.comp] / msn;
+    const int omol = (int)(u01(wx[2]) * (double)No);
+    const int o0 = ao.off + omol * mso;
+    const bool charged = ao.charged || an.charged;
+    if (tid == 0) {
+      ST[eo].identity_out[0]++;
+      ST[en].identity_in[0]++;
+    }
+    if (tid < mso) {  // [0, mso): the old molecule (charge negated); [mso, mso + msn): the new one
+      const double4 p = b.pos64[o0 + tid];
+      W.mx[tid] = p.x; W.my[tid] = p.y; W.mz[tid] = p.z; W.mq[tid] = -p.w;
+    }
+    __syncthreads();
+    // the new species: one first-bead trial on the old first bead (not averaged) and its
+    // orientations, the old molecule excluded
+    gen_first_trials(b, W, A[0].d.seed, A[0].d.stream, move, 1, b.charge[an.off], 1.0, b.meta[an.off].x, true, W.mx[0],
+                     W.my[0], W.mz[0]);
+    trial_pass_excl<PREC, CL>(b, W, 1, 1, an.comp, Nn, ao.comp, omol);
+    step_weight(W, 1, beta, an.bias, 0.0, 1.0, false);
+    bool ok = W.ok && W.w > 1e-150;
+    if (ok && tid == 0) {
+      for (int k = 0; k < 4; ++k) s_e1[k] = W.te[k];
+      s_w1 = W.w;
+      W.mx[mso] = W.mx[0]; W.my[mso] = W.my[0]; W.mz[mso] = W.mz[0]; W.mq[mso] = b.charge[an.off];
+    }
+    __syncthreads();
+    double rosen = ok ? s_w1 : 0.0;
+    double e2[4] = {0, 0, 0, 0};
+    if (ok && msn > 1) {
+      gen_orientations(b, W, A[0].d.seed, A[0].d.stream, move, an.d.norient, msn - 1, an.off, 1.0, 1.0, W.mx[0], W.my[0],
+                       W.mz[0], false, nullptr, nullptr, nullptr);
+      trial_pass_excl<PREC, CL>(b, W, an.d.norient * (msn - 1), msn - 1, an.comp, Nn, ao.comp, omol);
+      step_weight(W, an.d.norient, beta, an.bias, u_orient, (double)an.d.norient, false);
+      ok = W.ok;
+      if (ok) {
+        rosen *= W.w;
+        for (int k = 0; k < 4; ++k) e2[k] = W.te[4 * W.sel + k];
+        if (rosen <= 1e-150) ok = false;
+        if (tid < msn - 1) {
+          const Bead& bd = W.beads[W.sel * (msn - 1) + tid];
+          W.mx[mso + 1 + tid] = bd.x; W.my[mso + 1 + tid] = bd.y; W.mz[mso + 1 + tid] = bd.z;
+          W.mq[mso + 1 + tid] = b.charge[an.off + 1 + tid];
+        }
+      }
+      __syncthreads();
+    }
+    if (ok) {
+      // retrace of the old molecule: its own first bead (not averaged), then its orientation
+      // among trials from the retrace slots
+      gen_first_trials(b, W, A[0].d.seed, A[0].d.stream, move, 1, b.charge[ao.off], 1.0, b.meta[ao.off].x, true, W.mx[0],
+                       W.my[0], W.mz[0]);
+      trial_pass<PREC, CL>(b, W, 1, 1, ao.comp, omol);
+      step_weight(W, 1, beta, ao.bias, 0.0, 1.0, true);
+      bool ok2 = W.ok;
+      if (ok2 && tid == 0) {
+        for (int k = 0; k < 4; ++k) s_r1[k] = W.te[k];
+        s_wr = W.w;
+      }
+      __syncthreads();
+      double rosen_old = ok2 ? s_wr : 0.0;
+      double r2[4] = {0, 0, 0, 0};
+      if (ok2 && mso > 1) {
+        gen_orientations(b, W, A[0].d.seed, A[0].d.stream, move, ao.d.norient, mso - 1, ao.off, 1.0, 1.0, W.mx[0], W.my[0],
+                         W.mz[0], true, W.mx + 1, W.my + 1, W.mz + 1, SLOT_RETRACE);
+        trial_pass<PREC, CL>(b, W, ao.d.norient * (mso - 1), mso - 1, ao.comp, omol);
+        step_weight(W, ao.d.norient, beta, ao.bias, 0.0, (double)ao.d.norient, true);
+        ok2 = W.ok;
+        if (ok2) {
+          rosen_old *= W.w;
+          for (int k = 0; k < 4; ++k) r2[k] = W.te[4 * W.sel + k];
+        }
+        __syncthreads();
+      }
+      if (ok2) {
+        double same = 0.0, cross = 0.0;
+        if (charged) ewald_delta_move<PREC, CL>(b, W, mso + msn, eik, same, cross);
+        if (tid == 0) {
+          double ew = 0.0;
+          if (charged) {  // rigid exclusions: the new molecule arrives, the old one leaves
+            if (an.rigid && an.charged) same -= an.excl;
+            if (ao.rigid && ao.charged) same += ao.excl;
+            ew = same + 2.0 * cross;
+          }
+          rosen *= exp(-beta * ew);
+          const double pre = beta * an.big_p / (1.0 + (double)Nn) * ((double)No / (beta * ao.big_p));
+          const double pacc = pre * (rosen / an.d.ideal_rosenbluth) / (rosen_old / ao.d.ideal_rosenbluth);
+          s_accept = u01(wx[3]) < pacc;
+          if (s_accept && an.comp != ao.comp && (Nn + 1) * msn > an.cap) {
+            s_accept = 0;
+            ST[en].capacity_hits++;
+          }
+          s_dE[0] = (s_e1[0] + s_e1[2] + e2[0] + e2[2]) - (s_r1[0] + s_r1[2] + r2[0] + r2[2]);
+          s_dE[1] = (s_e1[1] + s_e1[3] + e2[1] + e2[3]) - (s_r1[1] + s_r1[3] + r2[1] + r2[3]);
+          s_dE[2] = ew;
+        }
+      }
+    }
+    __syncthreads();
+    if constexpr (CL > 1) cluster_sync_all();  // every CTA past its reads of this move
+    if (s_accept) {
+      if (an.comp != ao.comp) {  // the old molecule leaves (the last one fills its slot)
+        const int last = ao.off + (No - 1) * mso;
+        if (o0 != last && tid < mso) copy_atom(b, o0 + tid, last + tid, omol);
+        if (tid < msn)
+          store_atom(b, an.off + Nn * msn + tid, W.mx[mso + tid], W.my[mso + tid], W.mz[mso + tid],
+                     b.charge[an.off + tid], 1.0, 1.0, b.meta[an.off + tid].x, Nn);
+        __syncthreads();
+        if (tid == 0) {
+          comp_size[ao.comp] = (No - 1) * mso;
+          comp_size[an.comp] = (Nn + 1) * msn;
+        }
+      } else if (tid < msn) {  // same species: the new configuration replaces the old one
+        store_position(b, o0 + tid, W.mx[mso + tid], W.my[mso + tid], W.mz[mso + tid]);
+      }
+      if (charged) commit_sk<CL>(b, b.s_tmp);
+      if (tid == 0) {
+        ST[eo].identity_out[1]++;
+        ST[en].identity_in[1]++;
+        grx_gcmc_stats& sn = ST[en];
+        sn.energy[0] += s_dE[0]; sn.energy[1] += s_dE[1]; sn.energy[2] += s_dE[2];
+        sn.energy[3] += s_dE[0] + s_dE[1] + s_dE[2];
+      }
+    }
+  }
+}
+
 // One block of NW warps per box (NW = 8, 12 or 24: 24 warps per SM in every shape), or,
 // with CL > 1, one cluster of CL such blocks per box (launched with cluster dimension CL).
 // The box's moved components are entries [first[box], first[box + 1]) of args /
 // stats; every step picks one of them uniformly with word 3 of the displacement slot
 // (Select_Box_Component_Molecule, axpy.cu:74-100). All entries of a box share its seed
-// and stream.
+// and stream. IDS instantiations (grx_gcmc_swap.cu) also run identity swaps
+// (identity_swap_step); the others never test for them, so their code is unchanged.
 //
 // In a cluster every CTA runs the whole chain: the bead passes are split across the CTAs
 // and their partials exchanged (trial_pass), everything else is computed redundantly from
@@ -99,7 +249,7 @@ __device__ __forceinline__ void ewald_delta_move(const BoxDev& b, WK& W, int na,
 // barriers. Global state is written by every CTA with identical values (molecule counts
 // are assigned, never incremented); a cluster barrier before each commit keeps a CTA from
 // updating S(k) while a peer still reads it. Statistics are written by CTA 0.
-template <int PREC, int NW, int CL = 1>
+template <int PREC, int NW, int CL = 1, bool IDS = false>
 __global__ void __launch_bounds__(NW * 32, 24 / NW) gcmc_kernel(const BoxDev* boxes, const GcmcArgs* args,
                                                               const int* first, const uint64_t* step0,
                                                               int64_t nsteps, grx_gcmc_stats* stats) {
@@ -139,6 +289,7 @@ __global__ void __launch_bounds__(NW * 32, 24 / NW) gcmc_kernel(const BoxDev* bo
     if (r < d.p_translation) kind = 0;
     else if (r < d.p_rotation) kind = 1;
     else if (r < d.p_reinsertion) kind = 4;
+    else if (IDS && r < d.p_identity_swap) kind = 5;
     else if (r < d.p_swap) kind = (u01(w[2]) < 0.5) ? 2 : 3;
     const double uacc = u01(w[3]);
     if (tid == 0) s_accept = 0;
@@ -392,6 +543,10 @@ __global__ void __launch_bounds__(NW * 32, 24 / NW) gcmc_kernel(const BoxDev* bo
           st.energy[3] += s_dE[0] + s_dE[1] + s_dE[2];
         }
       }
+    } else if (IDS && kind == 5) {
+      if constexpr (IDS)
+        identity_swap_step<PREC, CL>(b, A, nm, ST, W, eik, comp_size, move, d.beta, u01(ws[1]), s_accept, s_e1,
+                                     s_w1, s_dE, s_r1, s_wr);
     }
     __syncthreads();
     if (tid < nm) ST[tid].sum_n += (double)(comp_size[A[tid].comp] / A[tid].ms);
@@ -406,6 +561,10 @@ __global__ void __launch_bounds__(NW * 32, 24 / NW) gcmc_kernel(const BoxDev* bo
     for (int k = 0; k < 4; ++k) o.energy[k] += ST[tid].energy[k];
     o.capacity_hits += ST[tid].capacity_hits;
     o.sum_n += ST[tid].sum_n;
+    for (int k = 0; k < 2; ++k) {
+      o.identity_out[k] += ST[tid].identity_out[k];
+      o.identity_in[k] += ST[tid].identity_in[k];
+    }
     o.n_molecules = comp_size[A[tid].comp] / A[tid].ms;
   }
 }
@@ -418,6 +577,11 @@ cudaError_t launch_gcmc_cluster(grx_precision prec, int cl, int nboxes, const Bo
                                 const int* dfirst, const uint64_t* dstep, int64_t nsteps, grx_gcmc_stats* dstats,
                                 size_t smem, cudaStream_t stream);
 cudaError_t set_gcmc_cluster_smem(size_t dyn_smem);
+// Launches of the kernel with identity swaps (grx_gcmc_swap.cu): one block of nw warps per box.
+cudaError_t launch_gcmc_swap(grx_precision prec, int nw, int nboxes, const BoxDev* dboxes, const GcmcArgs* dargs,
+                             const int* dfirst, const uint64_t* dstep, int64_t nsteps, grx_gcmc_stats* dstats,
+                             size_t smem, cudaStream_t stream);
+cudaError_t set_gcmc_swap_smem(size_t dyn_smem);
 // Clusters of `cl` CTAs that can be resident at once with `smem` bytes of dynamic shared memory.
 int gcmc_cluster_capacity(grx_precision prec, int cl, size_t smem);
 }  // namespace grx

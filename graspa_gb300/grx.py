@@ -96,12 +96,14 @@ class GcmcDesc(C.Structure):
                 ("p_reinsertion", C.c_double), ("p_swap", C.c_double), ("max_translation", C.c_double * 3), ("max_rotation", C.c_double * 3),
                 ("beta", C.c_double), ("pressure", C.c_double), ("fugacity_coeff", C.c_double),
                 ("mol_fraction", C.c_double), ("ideal_rosenbluth", C.c_double), ("tail_insert", C.c_double),
-                ("seed", C.c_uint64), ("stream", C.c_uint32), ("pad2_", C.c_uint32)]
+                ("seed", C.c_uint64), ("stream", C.c_uint32), ("pad2_", C.c_uint32),
+                ("p_identity_swap", C.c_double)]
 
 
 class GcmcStats(C.Structure):
     _fields_ = [("attempts", C.c_int64 * 5), ("accepted", C.c_int64 * 5), ("n_molecules", C.c_int64),
-                ("capacity_hits", C.c_int64), ("energy", C.c_double * 4), ("sum_n", C.c_double)]
+                ("capacity_hits", C.c_int64), ("energy", C.c_double * 4), ("sum_n", C.c_double),
+                ("identity_out", C.c_int64 * 2), ("identity_in", C.c_int64 * 2)]
 
 JOB_WIDOM, JOB_GCMC = 0, 1
 GCMC_TUNE_CANDIDATES = 9  # GRX_GCMC_TUNE_CANDIDATES: warps per box 8/12/24 x items per warp 1/2/4
@@ -688,7 +690,7 @@ def widom_desc(system, component, ntrials=10, norient=10, temperature=None, seed
 
 def gcmc_desc(component, ntrials=10, norient=10, p_translation=0.25, p_rotation=0.5, p_reinsertion=None, p_swap=1.0,
               max_translation=1.0, max_rotation=0.5, temperature=300.0, pressure_pa=1e5, fugacity_coeff=1.0,
-              mol_fraction=1.0, ideal_rosenbluth=1.0, tail_insert=0.0, seed=42, stream=0):
+              mol_fraction=1.0, ideal_rosenbluth=1.0, tail_insert=0.0, seed=42, stream=0, p_identity_swap=0.0):
     """GCMC move mix of one box; probabilities are cumulative as in Move_Statistics,
     pressure in Pa converted to internal units (fxn_main.h:120)."""
     d = GcmcDesc()
@@ -703,6 +705,7 @@ def gcmc_desc(component, ntrials=10, norient=10, p_translation=0.25, p_rotation=
     d.fugacity_coeff, d.mol_fraction, d.ideal_rosenbluth = fugacity_coeff, mol_fraction, ideal_rosenbluth
     d.tail_insert = tail_insert
     d.seed, d.stream = seed, stream
+    d.p_identity_swap = p_identity_swap
     return d
 
 

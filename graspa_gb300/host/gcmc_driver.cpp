@@ -10,6 +10,8 @@
 //   transfer <n>     runs n GibbsParticleTransfer calls of the moved component between the
 //                    box and an identical copy
 //   swap   <n>       runs n IdentitySwapMove calls (every adsorbate component takes part)
+//   swap_device <n>  the same identity swaps in one device run (RunMoves_Device_All, every
+//                    adsorbate component with identity swaps only)
 //   lambda 0         two CB/CFC lambda steps of molecule 0 (CBCF_LambdaChange)
 // and prints the move statistics, the accepted-energy sum and the drift check,
 // then the adsorbate positions, as plain text.
@@ -121,7 +123,7 @@ void read_system(const char* path, Variables& V, std::vector<size_t>& n_stored, 
 
 int main(int argc, char** argv) {
   if (argc < 4) {
-    std::fprintf(stderr, "usage: %s <system file> host|device|widom|volume|gibbs|transfer|swap|lambda <nsteps>\n",
+    std::fprintf(stderr, "usage: %s <system file> host|device|widom|volume|gibbs|transfer|swap|swap_device|lambda <nsteps>\n",
                  argv[0]);
     return 2;
   }
@@ -191,6 +193,27 @@ int main(int argc, char** argv) {
       std::printf("drift_b %.17g\n", (e1b.total() - e0b.total()) - (C1.deltaE.total() - C1.deltaE.TailE));
       std::printf("energy_scale %.17g\n", std::fabs(e1.total()) + std::fabs(e1b.total()));
       Destroy_Box(V, 1);
+    } else if (mode == "swap_device") {
+      for (int c = C.NComponents.y; c < C.NComponents.x; ++c) {
+        Move_Statistics& M = C.Moves[c];
+        M.TranslationProb = M.RotationProb = M.ReinsertionProb = 0.0;
+        M.IdentitySwapProb = M.SwapProb = 1.0;
+      }
+      std::vector<size_t> moved;
+      const std::vector<grx_gcmc_stats> st = RunMoves_Device_All(V, 0, nsteps, &moved);
+      double esum = 0.0;
+      for (const grx_gcmc_stats& x : st) esum += x.energy[3];
+      const MoveEnergy e1 = Total_Energy(V.Sims[0]);
+      std::printf("energy_sum %.17g\n", esum);
+      std::printf("drift %.17g\n", (e1.total() - e0.total()) - esum);
+      for (size_t k = 0; k < moved.size(); ++k)
+        std::printf("count %zu %zu %lld %lld\n", moved[k], C.NumberOfMolecule_for_Component[moved[k]],
+                    (long long)st[k].identity_in[1], (long long)st[k].identity_out[1]);
+      for (int c = C.NComponents.y; c < C.NComponents.x; ++c) {
+        const Atoms& A = V.Sims[0].d_a[c];
+        std::printf("positions %zu\n", A.size);
+        for (size_t i = 0; i < A.size; ++i) std::printf("%.17g %.17g %.17g\n", A.pos[i].x, A.pos[i].y, A.pos[i].z);
+      }
     } else if (mode == "swap") {
       // identity swaps among the adsorbate components
       for (long long k = 0; k < nsteps; ++k) {

@@ -1447,6 +1447,7 @@ static grx_gcmc_desc device_desc(Variables& Vars, size_t systemId, size_t comp) 
   d.p_rotation = MS.RotationProb;
   d.p_reinsertion = MS.ReinsertionProb;
   d.p_swap = MS.SwapProb;
+  d.p_identity_swap = MS.IdentitySwapProb;
   d.max_translation[0] = MS.MaxTranslation.x; d.max_translation[1] = MS.MaxTranslation.y;
   d.max_translation[2] = MS.MaxTranslation.z;
   d.max_rotation[0] = MS.MaxRotation.x; d.max_rotation[1] = MS.MaxRotation.y; d.max_rotation[2] = MS.MaxRotation.z;
@@ -1495,6 +1496,7 @@ grx_gcmc_stats RunMoves_Device(Variables& Vars, size_t systemId, size_t comp, in
   d.p_rotation = MS.RotationProb;
   d.p_reinsertion = MS.ReinsertionProb;
   d.p_swap = MS.SwapProb;
+  d.p_identity_swap = MS.IdentitySwapProb;
   d.max_translation[0] = MS.MaxTranslation.x; d.max_translation[1] = MS.MaxTranslation.y;
   d.max_translation[2] = MS.MaxTranslation.z;
   d.max_rotation[0] = MS.MaxRotation.x; d.max_rotation[1] = MS.MaxRotation.y; d.max_rotation[2] = MS.MaxRotation.z;

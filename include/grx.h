@@ -371,6 +371,11 @@ typedef struct {
   uint64_t seed;              /* Philox key */
   uint32_t stream;            /* Philox counter word 3 (chain id) */
   uint32_t pad2_;
+  double p_identity_swap;     /* IdentitySwapProb (cumulative, between reinsertion and swap;
+                                 0: none). An identity swap (mc_swap_moves.h:199-420) replaces a
+                                 molecule of a moved component holding molecules (uniform) by one
+                                 of a moved component (uniform) grown on its first bead. Needs
+                                 tail_insert 0. */
 } grx_gcmc_desc;
 
 typedef struct {
@@ -380,6 +385,9 @@ typedef struct {
   int64_t capacity_hits;      /* insertions refused for lack of component capacity */
   double energy[4];           /* sum of accepted dE: VDW, real Coulomb, Ewald Fourier, total */
   double sum_n;               /* sum over steps of N (loading average = sum_n / steps) */
+  int64_t identity_out[2];    /* identity swaps removing this component: attempts, accepted */
+  int64_t identity_in[2];     /* identity swaps adding this component: attempts, accepted (the
+                                 accepted swaps' dE count in this entry's energy sums) */
 } grx_gcmc_stats;
 
 /* nsteps GCMC moves on each of nboxes independent boxes (Markov chains), all on the

@@ -297,3 +297,35 @@ def test_host_layer_gibbs_particle_transfer(grx_lib, tmp_path):
     assert out["transfer_attempts"] == 40.0 and out["transfer_accepted"] >= 1
     tol = 1e-8 * out["energy_scale"] + 1e-6
     assert abs(out["drift"]) <= tol and abs(out["drift_b"]) <= tol
+
+
+@pytest.mark.parametrize("prec", ["GRX_FP64", "GRX_MIXED"])
+def test_device_identity_swap_matches_host_layer(grx_lib, tmp_path, prec):
+    """The identity swap of the device GCMC kernel (p_identity_swap) draws what the host
+    layer's IdentitySwapMove draws (swap slot, orientation and retrace slots, selection word 1),
+    so a device run of identity swaps only (every adsorbate component moved) equals the host
+    driver's swaps move for move: FP64 the same counts, positions within 1e-9 A and energy sums
+    within 1e-9 relative; mixed the same counts and positions, energies within beta*|dE| <= 1e-5."""
+    from graspa_gb300 import synth
+    s = synth.silica_co2_n2(n_co2=4, n_n2=4)
+    d = params(grx_lib, pressure_pa=1e6)
+    cs = s["comp_start"]
+    f = os.path.join(str(tmp_path), "system.txt")
+    system_file.write_system(f, s, [cs[1], CAP, CAP], d, precision=grx.GRX_FP64)
+    fd = os.path.join(str(tmp_path), "system_dev.txt")
+    system_file.write_system(fd, s, [cs[1], CAP, CAP], d, precision=getattr(grx, prec))
+    runs = {}
+    for mode, path in (("swap", f), ("swap_device", fd)):
+        r = subprocess.run([B.DRIVER, path, mode, "60"], capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr
+        runs[mode] = system_file.parse_driver_output(r.stdout)
+    host, dev = runs["swap"], runs["swap_device"]
+    assert dev["count"] == host["count"]
+    assert sum(v[1] for v in host["count"].values()) >= 2
+    for a, b in zip(host["positions_all"], dev["positions_all"]):
+        assert a.shape == b.shape and np.max(np.abs(a - b), initial=0.0) <= 1e-9
+    if prec == "GRX_FP64":
+        assert abs(dev["energy_sum"] - host["energy_sum"]) <= 1e-9 * max(1.0, abs(host["energy_sum"]))
+        assert abs(dev["drift"]) <= 1e-8 * max(1.0, abs(dev["energy_sum"])) + 1e-6
+    else:
+        assert d.beta * abs(dev["energy_sum"] - host["energy_sum"]) <= 1e-5
