@@ -360,6 +360,26 @@ static grx_status build_tiles(grx_box* b) {
     }
   }
   b->ntiles = (int)b->h_tile_r.size();
+  // Visiting order: a stride permutation of the k-d order (stride near 0.618 nt, coprime to
+  // nt). The tiles that survive a bead's cutoff cull are spatial neighbours, adjacent in k-d
+  // order; scattered through the list, they spread evenly over the contiguous item ranges of
+  // a bead pass instead of falling into one or two warps' items. Atoms keep their k-d order.
+  const int nt = b->ntiles;
+  if (nt > 2) {
+    int stride = std::max(1, (int)(0.6180339887 * nt));
+    auto gcd = [](int x, int y) { while (y) { const int t = x % y; x = y; y = t; } return x; };
+    while (gcd(stride, nt) != 1) ++stride;
+    std::vector<float4> c2(2 * (size_t)nt);
+    std::vector<int4> r2(nt);
+    for (int j = 0; j < nt; ++j) {
+      const int t = (int)((int64_t)j * stride % nt);
+      c2[2 * j] = b->h_tile_c[2 * t];
+      c2[2 * j + 1] = b->h_tile_c[2 * t + 1];
+      r2[j] = b->h_tile_r[t];
+    }
+    b->h_tile_c.swap(c2);
+    b->h_tile_r.swap(r2);
+  }
   if ((size_t)b->ntiles > b->tile_cap) {
     dev_free(b, b->tile_c);
     dev_free(b, b->tile_r);
