@@ -46,11 +46,11 @@ FLOP_PER_PAIR_LJ = 40.0
 L2_FLUSH_BYTES = 256 << 20
 PEAK_FP32_NOMINAL = 152 * 128 * 2 * 2070e6 / 1e12   # TFLOP/s, 128 FMA lanes per SM at the maximum clock
 # DRAM bytes (read + write) of gcmc_kernel<mixed> per chain and Monte Carlo step: ncu
-# dram__bytes_read.sum + dram__bytes_write.sum = 29.3 + 47.2 MB for one launch of 456
+# dram__bytes_read.sum + dram__bytes_write.sum = 29.4 + 47.5 MB for one launch of 456
 # chains x 20 steps (bench.py --profile --chains 456 --mc-steps 20, ncu --set full -k
 # regex:gcmc_kernel -s 20 -c 1: the third warm-up launch after the 18 autotune probes),
 # scaled by chains x steps to the timed launch.
-DRAM_BYTES_PER_CHAIN_STEP = (29.279e6 + 47.194e6) / (456 * 20)
+DRAM_BYTES_PER_CHAIN_STEP = (29.3952e6 + 47.450368e6) / (456 * 20)
 _FP32_PEAK = []
 
 
