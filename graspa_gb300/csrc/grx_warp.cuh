@@ -122,6 +122,17 @@ __device__ __forceinline__ df coul_table_df(const BoxDev& b, df s) {
   return df_add(df_mul(p1, t), df{c0.z, c0.w});
 }
 
+// Cold paths of the mixed-precision pair evaluation, kept out of line so the inlined copies of
+// pair_dense stay small: LJ with a non-unit scaling or the 12-6-4 form, and g(s) outside the
+// Coulomb table's range.
+static __device__ __noinline__ double vdw64_cold(const BoxDev& b, int row, double rr, double scaling) {
+  return vdw64(b, row, rr, scaling);
+}
+static __device__ __noinline__ double coul_g_cold(const BoxDev& b, double rr) {
+  const double r = sqrt(rr);
+  return erfc(b.alpha * r) / r;
+}
+
 // Accumulators of one lane: FP64 for the FP64 and FP32 forms, double-float for mixed.
 template <int PREC> struct LaneAcc { double v = 0.0, r = 0.0; };
 template <> struct LaneAcc<GRX_MIXED> { df v = {0.f, 0.f}, r = {0.f, 0.f}; };
@@ -170,7 +181,7 @@ __device__ __forceinline__ void pair_dense(const BoxDev& b, int i, const Bead& b
         df e;
         if (unit && s.hi > f.w) e = df{vdw32(f, s.hi), 0.0f};
         else if (unit) e = lj_df(b, row, s);
-        else e = df_from(vdw64(b, row, df_to(s), SC[i] * bd.scale));
+        else e = df_from(vdw64_cold(b, row, df_to(s), SC[i] * bd.scale));
         if (e.hi > b.overlapf) flag = 1;
         if (s.hi < 0.01f) flag = 1;
         acc.v = df_add(acc.v, e);
@@ -179,7 +190,7 @@ __device__ __forceinline__ void pair_dense(const BoxDev& b, int i, const Bead& b
         df g;
         const int k = (__float_as_int(s.hi) >> 17) - b.ctab_base;
         if (k >= 0 && k < b.ctab_n) g = coul_table_df(b, s);
-        else { const double rr = df_to(s), r = sqrt(rr); g = df_from(erfc(b.alpha * r) / r); }
+        else g = df_from(coul_g_cold(b, df_to(s)));
         const float2 qa = QDF[i];
         acc.r = df_add(acc.r, df_mul(g, df{qa.x, qa.y}));  // prefactor * q_bead applied once per item
       }
