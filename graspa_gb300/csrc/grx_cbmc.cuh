@@ -156,7 +156,8 @@ __device__ __forceinline__ void trial_pass_body(const BoxDev& b, WK& W, int nb, 
     const unsigned rank = cluster_rank();
     int i0, i1;
     cluster_items(sp, CL, rank, i0, i1);
-    block_bead_pass<PREC>(b, W.beads, nb, comp, newmol, excl_comp, excl_mol, W.qbuf, W.ipart, W.iflag, &W.counter, sp, i0, i1);
+    block_bead_pass<PREC>(b, W.beads, nb, comp, newmol, excl_comp, excl_mol, W.qbuf, W.ipart, W.iflag, &W.counter, sp,
+                          i0, i1);
     __syncthreads();
     if (sp.nu > 0 && i0 < i1) {  // this CTA's slots [s0, s0 + n): item + bead, increasing
       unsigned lo, hi;

@@ -31,8 +31,10 @@ template <int CL>
 static cudaError_t launch_prec(grx_precision prec, int nboxes, const BoxDev* dboxes, const GcmcArgs* dargs,
                                const int* dfirst, const uint64_t* dstep, int64_t nsteps, grx_gcmc_stats* dstats,
                                size_t smem, cudaStream_t stream) {
-  if (prec == GRX_FP64) return launch_cl<GRX_FP64, CL>(nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem, stream);
-  if (prec == GRX_MIXED) return launch_cl<GRX_MIXED, CL>(nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem, stream);
+  if (prec == GRX_FP64)
+    return launch_cl<GRX_FP64, CL>(nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem, stream);
+  if (prec == GRX_MIXED)
+    return launch_cl<GRX_MIXED, CL>(nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem, stream);
   return launch_cl<GRX_FP32, CL>(nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem, stream);
 }
 
@@ -51,10 +53,11 @@ static cudaError_t attr_one(size_t dyn_smem) {
 }
 
 cudaError_t set_gcmc_cluster_smem(size_t dyn_smem) {
-  for (cudaError_t e : {attr_one<GRX_FP64, 2>(dyn_smem), attr_one<GRX_FP64, 4>(dyn_smem), attr_one<GRX_FP64, 8>(dyn_smem),
-                        attr_one<GRX_MIXED, 2>(dyn_smem), attr_one<GRX_MIXED, 4>(dyn_smem),
-                        attr_one<GRX_MIXED, 8>(dyn_smem), attr_one<GRX_FP32, 2>(dyn_smem),
-                        attr_one<GRX_FP32, 4>(dyn_smem), attr_one<GRX_FP32, 8>(dyn_smem)})
+  for (cudaError_t e : {attr_one<GRX_FP64, 2>(dyn_smem), attr_one<GRX_FP64, 4>(dyn_smem),
+                        attr_one<GRX_FP64, 8>(dyn_smem), attr_one<GRX_MIXED, 2>(dyn_smem),
+                        attr_one<GRX_MIXED, 4>(dyn_smem), attr_one<GRX_MIXED, 8>(dyn_smem),
+                        attr_one<GRX_FP32, 2>(dyn_smem), attr_one<GRX_FP32, 4>(dyn_smem),
+                        attr_one<GRX_FP32, 8>(dyn_smem)})
     if (e != cudaSuccess) return e;
   return cudaSuccess;
 }

@@ -138,8 +138,8 @@ __device__ __noinline__ void identity_swap_step(const BoxDev& b, const GcmcArgs*
     double rosen = ok ? s_w1 : 0.0;
     double e2[4] = {0, 0, 0, 0};
     if (ok && msn > 1) {
-      gen_orientations(b, W, A[0].d.seed, A[0].d.stream, move, an.d.norient, msn - 1, an.off, 1.0, 1.0, W.mx[0], W.my[0],
-                       W.mz[0], false, nullptr, nullptr, nullptr);
+      gen_orientations(b, W, A[0].d.seed, A[0].d.stream, move, an.d.norient, msn - 1, an.off, 1.0, 1.0, W.mx[0],
+                       W.my[0], W.mz[0], false, nullptr, nullptr, nullptr);
       trial_pass_excl<PREC, CL>(b, W, an.d.norient * (msn - 1), msn - 1, an.comp, Nn, ao.comp, omol);
       step_weight(W, an.d.norient, beta, an.bias, u_orient, (double)an.d.norient, false);
       ok = W.ok;
@@ -158,8 +158,8 @@ __device__ __noinline__ void identity_swap_step(const BoxDev& b, const GcmcArgs*
     if (ok) {
       // retrace of the old molecule: its own first bead (not averaged), then its orientation
       // among trials from the retrace slots
-      gen_first_trials(b, W, A[0].d.seed, A[0].d.stream, move, 1, b.charge[ao.off], 1.0, b.meta[ao.off].x, true, W.mx[0],
-                       W.my[0], W.mz[0]);
+      gen_first_trials(b, W, A[0].d.seed, A[0].d.stream, move, 1, b.charge[ao.off], 1.0, b.meta[ao.off].x, true,
+                       W.mx[0], W.my[0], W.mz[0]);
       trial_pass<PREC, CL>(b, W, 1, 1, ao.comp, omol);
       step_weight(W, 1, beta, ao.bias, 0.0, 1.0, true);
       bool ok2 = W.ok;
@@ -171,8 +171,8 @@ __device__ __noinline__ void identity_swap_step(const BoxDev& b, const GcmcArgs*
       double rosen_old = ok2 ? s_wr : 0.0;
       double r2[4] = {0, 0, 0, 0};
       if (ok2 && mso > 1) {
-        gen_orientations(b, W, A[0].d.seed, A[0].d.stream, move, ao.d.norient, mso - 1, ao.off, 1.0, 1.0, W.mx[0], W.my[0],
-                         W.mz[0], true, W.mx + 1, W.my + 1, W.mz + 1, SLOT_RETRACE);
+        gen_orientations(b, W, A[0].d.seed, A[0].d.stream, move, ao.d.norient, mso - 1, ao.off, 1.0, 1.0, W.mx[0],
+                         W.my[0], W.mz[0], true, W.mx + 1, W.my + 1, W.mz + 1, SLOT_RETRACE);
         trial_pass<PREC, CL>(b, W, ao.d.norient * (mso - 1), mso - 1, ao.comp, omol);
         step_weight(W, ao.d.norient, beta, ao.bias, 0.0, (double)ao.d.norient, true);
         ok2 = W.ok;

@@ -19,8 +19,10 @@ template <int NW>
 static cudaError_t launch_prec(grx_precision prec, int nboxes, const BoxDev* dboxes, const GcmcArgs* dargs,
                                const int* dfirst, const uint64_t* dstep, int64_t nsteps, grx_gcmc_stats* dstats,
                                size_t smem, cudaStream_t stream) {
-  if (prec == GRX_FP64) return launch_ids<GRX_FP64, NW>(nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem, stream);
-  if (prec == GRX_MIXED) return launch_ids<GRX_MIXED, NW>(nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem, stream);
+  if (prec == GRX_FP64)
+    return launch_ids<GRX_FP64, NW>(nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem, stream);
+  if (prec == GRX_MIXED)
+    return launch_ids<GRX_MIXED, NW>(nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem, stream);
   return launch_ids<GRX_FP32, NW>(nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem, stream);
 }
 
@@ -39,10 +41,11 @@ static cudaError_t attr_one(size_t dyn_smem) {
 }
 
 cudaError_t set_gcmc_swap_smem(size_t dyn_smem) {
-  for (cudaError_t e : {attr_one<GRX_FP64, 8>(dyn_smem), attr_one<GRX_FP64, 12>(dyn_smem), attr_one<GRX_FP64, 24>(dyn_smem),
-                        attr_one<GRX_MIXED, 8>(dyn_smem), attr_one<GRX_MIXED, 12>(dyn_smem),
-                        attr_one<GRX_MIXED, 24>(dyn_smem), attr_one<GRX_FP32, 8>(dyn_smem),
-                        attr_one<GRX_FP32, 12>(dyn_smem), attr_one<GRX_FP32, 24>(dyn_smem)})
+  for (cudaError_t e : {attr_one<GRX_FP64, 8>(dyn_smem), attr_one<GRX_FP64, 12>(dyn_smem),
+                        attr_one<GRX_FP64, 24>(dyn_smem), attr_one<GRX_MIXED, 8>(dyn_smem),
+                        attr_one<GRX_MIXED, 12>(dyn_smem), attr_one<GRX_MIXED, 24>(dyn_smem),
+                        attr_one<GRX_FP32, 8>(dyn_smem), attr_one<GRX_FP32, 12>(dyn_smem),
+                        attr_one<GRX_FP32, 24>(dyn_smem)})
     if (e != cudaSuccess) return e;
   return cudaSuccess;
 }
