@@ -215,8 +215,12 @@ static void launch_shape(grx_precision prec, int nboxes, const BoxDev* dboxes, c
 static grx_status enqueue_gcmc(grx_precision prec, int nw, int nboxes, const BoxDev* dboxes, const GcmcArgs* dargs,
                                const int* dfirst, uint64_t* dstep, int64_t nsteps, grx_gcmc_stats* dstats,
                                size_t smem, cudaStream_t stream, int cl = 1, bool swaps = false) {
-  if (swaps) {
-    GRX_REQUIRE(cl == 1, "grx_gcmc: identity swaps run on one block per box");
+  if (swaps && cl > 1) {
+    GRX_REQUIRE(nw == 24, "grx_gcmc: cluster launches use 24 warps per block");
+    GRX_CHECK_CUDA(launch_gcmc_swap_cluster(prec, cl, nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem,
+                                            stream),
+                   "gcmc identity-swap cluster launch");
+  } else if (swaps) {
     GRX_CHECK_CUDA(launch_gcmc_swap(prec, nw, nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem, stream),
                    "gcmc identity-swap launch");
   } else if (cl > 1) {
@@ -510,7 +514,6 @@ extern "C" grx_status grx_gcmc_batch_get_shape(grx_gcmc_batch* B, int32_t* nwarp
 // The largest cluster size (8, 4 or 2) for which every box of the batch gets its own
 // resident cluster, or 1 when the boxes already fill the SMs.
 static int max_cluster(const grx_gcmc_batch* B) {
-  if (B->swaps) return 1;  // identity swaps run on one block per box
   const int nb = (int)B->boxes.size();
   for (int cl : {8, 4, 2})
     if (gcmc_cluster_capacity(B->prec, cl, B->smem) >= nb) return cl;
@@ -522,7 +525,6 @@ extern "C" grx_status grx_gcmc_batch_set_cluster(grx_gcmc_batch* B, int32_t clus
   GRX_REQUIRE(cluster == 1 || cluster == 2 || cluster == 4 || cluster == 8,
               "grx_gcmc_batch_set_cluster: cluster must be 1, 2, 4 or 8");
   GRX_REQUIRE(cluster == 1 || B->nwarps == 24, "grx_gcmc_batch_set_cluster: clusters use 24 warps per block");
-  GRX_REQUIRE(cluster == 1 || !B->swaps, "grx_gcmc_batch_set_cluster: identity swaps run on one block per box");
   GRX_CHECK_CUDA(cudaStreamSynchronize(B->stream), "set cluster");
   if (cluster > 1) {
     GRX_CHECK_CUDA(cudaSetDevice(B->device), "set device");

@@ -577,10 +577,14 @@ cudaError_t launch_gcmc_cluster(grx_precision prec, int cl, int nboxes, const Bo
                                 const int* dfirst, const uint64_t* dstep, int64_t nsteps, grx_gcmc_stats* dstats,
                                 size_t smem, cudaStream_t stream);
 cudaError_t set_gcmc_cluster_smem(size_t dyn_smem);
-// Launches of the kernel with identity swaps (grx_gcmc_swap.cu): one block of nw warps per box.
+// Launches of the kernel with identity swaps (grx_gcmc_swap.cu): one block of nw warps per box,
+// or one cluster of cl CTAs of 24 warps.
 cudaError_t launch_gcmc_swap(grx_precision prec, int nw, int nboxes, const BoxDev* dboxes, const GcmcArgs* dargs,
                              const int* dfirst, const uint64_t* dstep, int64_t nsteps, grx_gcmc_stats* dstats,
                              size_t smem, cudaStream_t stream);
+cudaError_t launch_gcmc_swap_cluster(grx_precision prec, int cl, int nboxes, const BoxDev* dboxes,
+                                     const GcmcArgs* dargs, const int* dfirst, const uint64_t* dstep, int64_t nsteps,
+                                     grx_gcmc_stats* dstats, size_t smem, cudaStream_t stream);
 cudaError_t set_gcmc_swap_smem(size_t dyn_smem);
 // Clusters of `cl` CTAs that can be resident at once with `smem` bytes of dynamic shared memory.
 int gcmc_cluster_capacity(grx_precision prec, int cl, size_t smem);

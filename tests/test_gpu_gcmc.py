@@ -279,3 +279,38 @@ def test_gcmc_mixed_ewald_row_products_match_oracle(grx_lib, cl):
     _, s_new, _ = box.structure_factors()
     assert np.max(np.abs(s_run - s_new)) <= 1e-9 * max(1.0, np.max(np.abs(s_new)))
     box.close()
+
+
+@pytest.mark.parametrize("cl", [2, 8])
+def test_identity_swaps_on_clusters(grx_lib, cl):
+    """Identity swaps only (CO2 + N2 mixture, both components moved) on a thread-block cluster
+    take the one-block chain's decisions in FP64: the same swap counts and molecule numbers,
+    positions within 1e-9 A, energy sums within 1e-9 relative."""
+    from graspa_gb300 import synth
+    s = synth.silica_co2_n2(n_co2=4, n_n2=4)
+    cap = [s["comp_start"][1], CAP, CAP]
+    kw = dict(p_translation=0.0, p_rotation=0.0, p_reinsertion=0.0, p_identity_swap=1.0, p_swap=1.0,
+              pressure_pa=1e6)
+    descs = [grx_lib.gcmc_desc(1, **kw), grx_lib.gcmc_desc(2, **kw)]
+    runs = []
+    for c in (1, cl):
+        box = grx_lib.Box(s, capacity=cap)
+        box.ewald_total()
+        batch = grx_lib.GcmcBatch([box], [descs], grx_lib.GRX_FP64)
+        batch.set_shape(24, 1)
+        if c > 1:
+            batch.set_cluster(c)
+        batch.launch(80)
+        st, _ = batch.stats()
+        batch.close()
+        runs.append((st, [box.positions(1), box.positions(2)]))
+        box.close()
+    (a, pa), (b, pb) = runs
+    for k in range(2):
+        assert list(a[k].identity_in) == list(b[k].identity_in)
+        assert list(a[k].identity_out) == list(b[k].identity_out)
+        assert a[k].n_molecules == b[k].n_molecules
+        assert abs(a[k].energy[3] - b[k].energy[3]) <= 1e-9 * max(1.0, abs(a[k].energy[3]))
+    assert a[0].identity_in[1] + a[1].identity_in[1] >= 2
+    for x, y in zip(pa, pb):
+        assert x.shape == y.shape and np.max(np.abs(x - y), initial=0.0) <= 1e-9
