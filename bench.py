@@ -9,8 +9,9 @@ CBMC deletion = 1:1:1:1, 10 trial positions and 10 orientations, boxes starting
 empty (0-120 molecules). Independent Markov chains (three per SM, different Philox
 streams) run in one persistent launch replayed as a CUDA graph; one benchmark
 "step" is S Monte Carlo steps of every chain. A trial energy is one trial
-configuration against every atom (2 per translation / rotation, 20 per CBMC
-insertion or deletion of CO2).
+configuration evaluated against every atom, as the kernel counts them: 2 per
+translation / rotation, 10 first-bead positions per CBMC insertion or deletion plus
+10 orientations when the first bead was grown.
 
   value      trial energies/s of the batched mixed-precision form, state resident
   fp64       the same batch in FP64, and the plain FP64 single-box form
@@ -47,8 +48,9 @@ L2_FLUSH_BYTES = 256 << 20
 PEAK_FP32_NOMINAL = 152 * 128 * 2 * 2070e6 / 1e12   # TFLOP/s, 128 FMA lanes per SM at the maximum clock
 # DRAM bytes (read + write) of gcmc_kernel<mixed> per chain and Monte Carlo step: ncu
 # dram__bytes_read.sum + dram__bytes_write.sum = 29.4 + 47.5 MB for one launch of 456
-# chains x 20 steps (bench.py --profile --chains 456 --mc-steps 20, ncu --set full -k
-# regex:gcmc_kernel -s 20 -c 1: the third warm-up launch after the 18 autotune probes),
+# chains x 20 steps (bench.py --profile --chains 456 --mc-steps 20, ncu --set full
+# --clock-control none -k regex:gcmc_kernel -s 20 -c 1: the third warm-up launch after the
+# 18 autotune probes),
 # scaled by chains x steps to the timed launch.
 DRAM_BYTES_PER_CHAIN_STEP = (29.3952e6 + 47.450368e6) / (456 * 20)
 _FP32_PEAK = []
@@ -162,19 +164,17 @@ def gcmc_descs(grx, n, seed=42):
 
 
 def work_of(stats, ms, nfw):
-    """(trial energies, pair evaluations) of a list of GCMC statistics. Pairs are
-    beads x (framework atoms + guest atoms at the run's mean loading)."""
-    chain = ms - 1
-    g_te = NTRIALS + (NORIENT if chain else 0)
-    g_beads = NTRIALS + NORIENT * chain
+    """(trial energies, pair evaluations) of a list of GCMC statistics, from the kernel's
+    own counts: the trial configurations it evaluated (trial_configs: first-bead positions,
+    orientations grown after a successful first bead, the two configurations of a
+    translation / rotation) and their beads. Pairs are beads x (framework atoms + guest
+    atoms at the run's mean loading)."""
     te = pairs = 0.0
     for st in stats:
-        a = list(st.attempts)
-        te += 2 * (a[0] + a[1]) + g_te * (a[2] + a[3]) + (g_te + 1 + (NORIENT if chain else 0)) * a[4]
-        beads = 2 * ms * (a[0] + a[1]) + g_beads * (a[2] + a[3]) + (g_beads + 1 + NORIENT * chain) * a[4]
-        steps = max(1, sum(a))
-        guests = ms * st.sum_n / max(steps, 1)
-        pairs += beads * (nfw + guests)
+        steps = max(1, sum(st.attempts))
+        guests = ms * st.sum_n / steps
+        te += st.trial_configs
+        pairs += st.trial_beads * (nfw + guests)
     return te, pairs
 
 
@@ -532,8 +532,10 @@ def run_grx(args):
                          "model": f"{FLOP_PER_PAIR_CHARGED:.0f} FLOP/pair x {g['pairs'] / args.steps:.4g} pairs "
                                   "per launch (beads x (framework + guest atoms))"},
             "cpu_baseline": {"value": cpu_val, "unit": "trial_energies/s", "cores": cores, "kind": "port",
-                             "sample": f"{chains} chains x {steps} GCMC steps ({cpu_te:.0f} trial energies, "
-                                       f"{cpu_dt:.1f} s), FP64 C++ oracle, one chain per thread"},
+                             "cpu_model": cpu_model(),
+                             "sample": f"{chains} resident chains x {steps} GCMC steps ({cpu_te:.0f} trial "
+                                       f"energies, {cpu_dt:.1f} s of moves; set-up and Ewald totals before "
+                                       "timing), FP64 C++ oracle, one chain per thread"},
             "e2e": g["e2e"],
             "gpu_launches": int(g["launches"]),
             "clocks": {"sm_mhz": clk["sm_mhz"], "sm_max_mhz": clk["sm_max_mhz"], "reasons": clk["reasons"]},
@@ -580,11 +582,8 @@ def bench_other(args, grx, torch, stream, flush, which):
         for k, s in enumerate(systems):
             for e in range(2):
                 st = stats[2 * k + e]
-                a = list(st.attempts)
-                nt = descs[k][e].ntrials
-                te += 2 * (a[0] + a[1]) + nt * (a[2] + a[3]) + (nt + 1) * a[4]
-                beads = 2 * (a[0] + a[1]) + nt * (a[2] + a[3]) + (nt + 1) * a[4]
-                pairs += beads * (s["comp_start"][1] + st.sum_n / max(1, sum(a)))
+                te += st.trial_configs
+                pairs += st.trial_beads * (s["comp_start"][1] + st.sum_n / max(1, sum(st.attempts)))
         t = sum(times)
         for b in boxes:
             b.close()
@@ -669,11 +668,10 @@ def bench_cluster(args, grx, torch, stream, flush):
 
 
 # ------------------------------------------------------------------ reference arm
-def _oracle_chain(system, desc, first, nsteps):
-    from graspa_gb300 import grx
+def _oracle_params(desc):
     from oracle import oracle as O
     g = O.OraGcmc()
-    g.component, g.ntrials, g.norient = 1, desc.ntrials, desc.norient
+    g.component, g.ntrials, g.norient = desc.component, desc.ntrials, desc.norient
     g.p_translation, g.p_rotation, g.p_reinsertion, g.p_swap = (desc.p_translation, desc.p_rotation,
                                                                 desc.p_reinsertion, desc.p_swap)
     for k in range(3):
@@ -682,29 +680,70 @@ def _oracle_chain(system, desc, first, nsteps):
     g.beta, g.pressure = desc.beta, desc.pressure
     g.fugacity_coeff, g.mol_fraction, g.ideal_rosenbluth = desc.fugacity_coeff, desc.mol_fraction, 1.0
     g.seed, g.stream = desc.seed, desc.stream
-    st, after, _ = O.OracleSystem(system).gcmc(g, [system["comp_start"][1], 3 * 160], first, nsteps)
-    return st, after
+    return g
+
+
+def oracle_chains(system, descs):
+    """Resident FP64 oracle chains, one per move set: atoms, molecule counts and both
+    structure factors stay in host memory across calls, and the full FP64 Ewald totals
+    (framework exclusion included) are computed once here, outside any timing, as the
+    GPU arm computes its framework S(k) once before timing."""
+    from oracle import oracle as O
+    osys = O.OracleSystem(system)
+    _, s_fw, s_ads = osys.ewald_total(list(system["molsize"]))
+    cap = [system["comp_start"][1], 3 * 160]
+    return [O.OracleChain(osys, _oracle_params(d), cap, ewald=(s_fw, s_ads)) for d in descs]
+
+
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the platform string)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+def run_oracle_slices(chains, first, n_step, threads):
+    """n_step moves of every resident chain, one chain per host thread; returns (stats, s)."""
+    t0 = time.perf_counter()
+    with concurrent.futures.ThreadPoolExecutor(threads) as ex:
+        res = list(ex.map(lambda c: c.run(first, n_step)[0], chains))
+    return res, time.perf_counter() - t0
 
 
 def cpu_gcmc_rate(seconds, threads=None):
-    """The FP64 oracle on the same GCMC workload, one chain per host thread, for about
-    `seconds`. Returns (trial energies/s, trial energies, seconds, threads, chains, steps)."""
+    """The FP64 oracle on the same GCMC workload, one resident chain per host thread, for
+    about `seconds` of moves (set-up excluded). Returns (trial energies/s, trial energies,
+    seconds, threads, chains, steps)."""
     from graspa_gb300 import grx
     from oracle import oracle as O
     O.lib()
     system = co2_system()
     threads = threads or os.cpu_count() or 1
-    descs = gcmc_descs(grx, threads)
-    t0 = time.perf_counter()
-    _oracle_chain(system, descs[0], 0, 20)
-    per_step = (time.perf_counter() - t0) / 20
-    steps = int(max(20, min(5000, seconds / max(per_step, 1e-6))))
-    t0 = time.perf_counter()
-    with concurrent.futures.ThreadPoolExecutor(threads) as ex:
-        res = list(ex.map(lambda d: _oracle_chain(system, d, 0, steps)[0], descs))
-    dt = time.perf_counter() - t0
-    te, _ = work_of(res, 3, system["comp_start"][1])
-    return te / dt, te, dt, threads, threads, steps
+    chains = oracle_chains(system, gcmc_descs(grx, threads))
+    # per-step cost of the moves alone, on resident state (warm-up steps of every chain)
+    warm = 40
+    _, dt = run_oracle_slices(chains, 0, warm, threads)
+    chunk = int(max(20, min(5000, 0.5 * warm / max(dt, 1e-6))))   # slices of about half a second
+    first, steps, te, tot = warm, 0, 0.0, 0.0
+    while tot < seconds:
+        res, dt = run_oracle_slices(chains, first, chunk, threads)
+        first += chunk
+        steps += chunk
+        tot += dt
+        te += work_of(res, 3, system["comp_start"][1])[0]
+    return te / tot, te, tot, threads, threads, steps
 
 
 def run_reference(args):
@@ -716,26 +755,21 @@ def run_reference(args):
     O.lib()
     system = co2_system()
     threads = os.cpu_count() or 1
-    descs = gcmc_descs(grx, threads)
-    t0 = time.perf_counter()
-    _oracle_chain(system, descs[0], 0, 20)
-    per_step = (time.perf_counter() - t0) / 20
+    chains = oracle_chains(system, gcmc_descs(grx, threads))
+    _, dt = run_oracle_slices(chains, 0, 20, threads)
+    per_step = dt / 20
+    first = 20
     n_step = int(max(10, min(args.mc_steps, 4.0 / max(per_step, 1e-9))))
-    state = [system] * threads
-    first = 0
     times, te_tot = [], 0.0
     for i in range(args.warmup + args.steps):
-        t0 = time.perf_counter()
-        with concurrent.futures.ThreadPoolExecutor(threads) as ex:
-            res = list(ex.map(lambda k: _oracle_chain(state[k], descs[k], first, n_step), range(threads)))
-        dt = time.perf_counter() - t0
-        state = [r[1] for r in res]
+        res, dt = run_oracle_slices(chains, first, n_step, threads)
         first += n_step
         if i >= args.warmup:
             times.append(dt)
-            te_tot += work_of([r[0] for r in res], 3, system["comp_start"][1])[0]
+            te_tot += work_of(res, 3, system["comp_start"][1])[0]
     tot = sum(times)
     value = te_tot / tot
+    model = cpu_model()
     line = {
         "metric": "CBMC trial energies/s", "value": value, "unit": "trial_energies/s", "impl": "reference",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
@@ -743,9 +777,11 @@ def run_reference(args):
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded Philox)",
         "config": {"workload": "gcmc_co2_silica_3456 (1:1:1:1 translation/rotation/insertion/deletion, k=10)",
                    "chains": threads, "mc_steps_per_step": n_step},
-        "cpu_baseline": {"value": value, "unit": "trial_energies/s", "cores": threads, "kind": "port",
-                         "sample": f"{threads} chains x {n_step} GCMC steps per step, FP64 C++ oracle, "
-                                   "one chain per thread"},
+        "cpu_baseline": {"value": value, "unit": "trial_energies/s", "cores": threads, "cpu_model": model,
+                         "kind": "port",
+                         "sample": f"{threads} resident chains x {n_step} GCMC steps per step (state and "
+                                   "structure factors kept across steps, Ewald totals computed once before "
+                                   f"timing), FP64 C++ oracle, one chain per thread on {model}"},
         "e2e": {"value": value, "unit": "trial_energies/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)

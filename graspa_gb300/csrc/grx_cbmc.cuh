@@ -53,6 +53,8 @@ struct CbmcWork {
   double wsum[2][NW];
   float2 qd[2 * kMolWork];
   int counter;
+  long long cfg;    // trial configurations evaluated since the caller last cleared it
+  long long cbeads; // their beads
   int ok;       // step constructed
   int sel;      // chosen (or retraced) trial index
   int nok;      // trials without overlap
@@ -142,7 +144,11 @@ __device__ __noinline__ void gen_orientations(const BoxDev& b, WK& W, uint64_t s
 template <int PREC, int CL, class WK>
 __device__ __forceinline__ void trial_pass_body(const BoxDev& b, WK& W, int nb, int chain, int comp, int newmol,
                                                 int excl_comp, int excl_mol) {
-  if (threadIdx.x == 0) W.counter = 0;
+  if (threadIdx.x == 0) {
+    W.counter = 0;
+    W.cfg += nb / chain;
+    W.cbeads += nb;
+  }
   __syncthreads();
   const int nw = (int)(blockDim.x >> 5);
   if constexpr (CL == 1) {

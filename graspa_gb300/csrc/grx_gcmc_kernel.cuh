@@ -264,7 +264,11 @@ __global__ void __launch_bounds__(NW * 32, 24 / NW) gcmc_kernel(const BoxDev* bo
   extern __shared__ double2 eik[];
   const int tid = threadIdx.x;
   const int e0 = first[box], nm = first[box + 1] - e0;
-  if (tid == 0) b = boxes[box];
+  if (tid == 0) {
+    b = boxes[box];
+    W.cfg = 0;
+    W.cbeads = 0;
+  }
   if (tid < nm) {
     A[tid] = args[e0 + tid];
     ST[tid] = grx_gcmc_stats{};
@@ -521,6 +525,12 @@ __global__ void __launch_bounds__(NW * 32, 24 / NW) gcmc_kernel(const BoxDev* bo
           s_dE[0] = sg * ev; s_dE[1] = sg * er; s_dE[2] = ew;
         }
       }
+      if (!del && tid == 0) {  // RecordRosen of the insertion: W, 0 when the growth failed
+        const double wr = ok ? rosen : 0.0;
+        st.rosen[0] += wr;
+        st.rosen[1] += wr * wr;
+        st.rosen[2] += 1.0;
+      }
       __syncthreads();
       if constexpr (CL > 1) cluster_sync_all();  // every CTA past its reads of this move
       if (s_accept) {
@@ -550,6 +560,12 @@ __global__ void __launch_bounds__(NW * 32, 24 / NW) gcmc_kernel(const BoxDev* bo
     }
     __syncthreads();
     if (tid < nm) ST[tid].sum_n += (double)(comp_size[A[tid].comp] / A[tid].ms);
+    if (tid == 0) {
+      st.trial_configs += W.cfg;
+      st.trial_beads += W.cbeads;
+      W.cfg = 0;
+      W.cbeads = 0;
+    }
     __syncthreads();
   }
   if (tid < nm && (CL == 1 || cluster_rank() == 0)) {  // accumulate into the caller's running statistics
@@ -559,6 +575,9 @@ __global__ void __launch_bounds__(NW * 32, 24 / NW) gcmc_kernel(const BoxDev* bo
       o.accepted[k] += ST[tid].accepted[k];
     }
     for (int k = 0; k < 4; ++k) o.energy[k] += ST[tid].energy[k];
+    for (int k = 0; k < 3; ++k) o.rosen[k] += ST[tid].rosen[k];
+    o.trial_configs += ST[tid].trial_configs;
+    o.trial_beads += ST[tid].trial_beads;
     o.capacity_hits += ST[tid].capacity_hits;
     o.sum_n += ST[tid].sum_n;
     for (int k = 0; k < 2; ++k) {

@@ -13,8 +13,9 @@
 //  * at most GRX_NOALLOC_MAX_BEADS (= ntrials * chainsize) trial beads per call;
 //    larger requests fail with GRX_ERR_CAPACITY and touch nothing;
 //  * the first call on a device looks the array up with cudaGetSymbolAddress
-//    (once per device, with that device current); make that first call before any
-//    stream capture is started;
+//    (once per device, with the box's device made current for the call and the
+//    caller's device restored after); make that first call before any stream capture
+//    is started;
 //  * all calls share the one array and it keeps the last call's contents. The
 //    parts that must start at zero (overlap flags) are cleared on every call.
 //    Calls that overlap on the GPU (two host threads, two streams) race on the
@@ -55,10 +56,23 @@ constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 unsigned char* g_scratch_ptr[kMaxDevices] = {};
 
-// Device address of the scratch array for the current device (set-up once per device).
-grx_status scratch_address(unsigned char** out) {
-  int dev = 0;
-  GRX_CHECK_CUDA(cudaGetDevice(&dev), "grx_trial_energies_noalloc: cudaGetDevice");
+// Makes `dev` current for the life of the guard and restores the caller's device after.
+struct DeviceGuard {
+  int prev = -1;
+  cudaError_t err = cudaSuccess;
+  explicit DeviceGuard(int dev) {
+    err = cudaGetDevice(&prev);
+    if (err == cudaSuccess && prev != dev) err = cudaSetDevice(dev);
+    else if (err == cudaSuccess) prev = -1;
+  }
+  ~DeviceGuard() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
+
+// Device address of the scratch array on device `dev`, which must be current (set-up
+// once per device).
+grx_status scratch_address(int dev, unsigned char** out) {
   if (dev < 0 || dev >= kMaxDevices) {
     set_error("grx_trial_energies_noalloc: device ordinal %d out of range", dev);
     return GRX_ERR_UNSUPPORTED;
@@ -87,33 +101,6 @@ __global__ void noalloc_beads_kernel(const double* pos, const double* scale, con
   const double q = has_charge ? charge[j] : 0.0;
   const double scc = has_scale_coul ? scale_coul[j] : 1.0;
   make_bead(beads[j], pos[3 * j], pos[3 * j + 1], pos[3 * j + 2], q * scc, sc, (int)type[j], prefactor);
-}
-
-template <int PREC>
-__global__ void __launch_bounds__(GRX_THREADS) noalloc_bead_pass_kernel(BoxDev b, const Bead* beads, int component,
-                                                                        int newmol, int excl_comp, int excl_mol,
-                                                                        double* part, int* flags) {
-  __shared__ double ipart[kMaxItems * 4];
-  __shared__ int iflag[kMaxItems];
-  __shared__ int qbuf[(GRX_THREADS / 32) * kQueue];
-  __shared__ int counter;
-  if (threadIdx.x == 0) counter = 0;
-  __syncthreads();
-  const PassSplit sp = pass_split(b, 1, GRX_THREADS / 32, 4);
-  const int nch = (int)sp.items;  // one bead: slot = item
-  block_bead_pass<PREC>(b, beads + blockIdx.x, 1, component, newmol, excl_comp, excl_mol, qbuf, ipart, iflag,
-                        &counter, sp);
-  __syncthreads();
-  if (threadIdx.x < 4) {
-    double s = 0.0;
-    for (int c = 0; c < nch; ++c) s += item_get<PREC>(ipart, c * 4 + threadIdx.x);
-    part[blockIdx.x * 4 + threadIdx.x] = s;
-  }
-  if (threadIdx.x == 0) {
-    int f = 0;
-    for (int c = 0; c < nch; ++c) f |= iflag[c];
-    flags[blockIdx.x] = f;
-  }
 }
 
 __global__ void noalloc_reduce_kernel(const double* part, const int* flags, int nb, int chain, double* out,
@@ -148,15 +135,18 @@ extern "C" grx_status grx_trial_energies_noalloc(grx_box* b, const grx_trials* t
   GRX_REQUIRE(component >= 0 && component < b->ncomp, "grx_trial_energies_noalloc: component out of range");
   if (t->ntrials == 0) return GRX_OK;
   GRX_REQUIRE(t->pos && t->type, "grx_trial_energies_noalloc: bead arrays missing");
-  const size_t nb64 = t->ntrials * t->chainsize;
-  if (t->chainsize > (size_t)kNoallocBeads || nb64 > (size_t)kNoallocBeads) {
-    set_error("grx_trial_energies_noalloc: %zu trial beads (%zu trials x %zu) exceed the fixed maximum of %d",
-              nb64, t->ntrials, t->chainsize, kNoallocBeads);
+  // checked before multiplying, so no trial count can wrap the product below the maximum
+  if (t->chainsize > (size_t)kNoallocBeads || t->ntrials > (size_t)kNoallocBeads / t->chainsize) {
+    set_error("grx_trial_energies_noalloc: %zu trials x %zu beads exceed the fixed maximum of %d trial beads",
+              t->ntrials, t->chainsize, kNoallocBeads);
     return GRX_ERR_CAPACITY;
   }
-  const int nb = (int)nb64;
+  const int nb = (int)(t->ntrials * t->chainsize);
+  // the box's stream belongs to the box's device: work there, whatever the caller's current device
+  DeviceGuard guard(b->device);
+  GRX_CHECK_CUDA(guard.err, "grx_trial_energies_noalloc: select the box's device");
   unsigned char* base = nullptr;
-  grx_status st = scratch_address(&base);
+  grx_status st = scratch_address(b->device, &base);
   if (st) return st;
   refresh_dev(b);
   cudaStream_t s = b->stream;
@@ -185,11 +175,11 @@ extern "C" grx_status grx_trial_energies_noalloc(grx_box* b, const grx_trials* t
                                                         b->dev.prefactor, beads);
   const int ec = (int)exclude_comp, em = (int)exclude_molid, nm = (int)t->molid;
   if (prec == GRX_FP64)
-    noalloc_bead_pass_kernel<GRX_FP64><<<nb, GRX_THREADS, 0, s>>>(b->dev, beads, component, nm, ec, em, part, flags);
+    trial_bead_kernel<GRX_FP64><<<nb, GRX_THREADS, 0, s>>>(b->dev, beads, component, nm, ec, em, part, flags);
   else if (prec == GRX_MIXED)
-    noalloc_bead_pass_kernel<GRX_MIXED><<<nb, GRX_THREADS, 0, s>>>(b->dev, beads, component, nm, ec, em, part, flags);
+    trial_bead_kernel<GRX_MIXED><<<nb, GRX_THREADS, 0, s>>>(b->dev, beads, component, nm, ec, em, part, flags);
   else
-    noalloc_bead_pass_kernel<GRX_FP32><<<nb, GRX_THREADS, 0, s>>>(b->dev, beads, component, nm, ec, em, part, flags);
+    trial_bead_kernel<GRX_FP32><<<nb, GRX_THREADS, 0, s>>>(b->dev, beads, component, nm, ec, em, part, flags);
   const int ntr = (int)t->ntrials;
   noalloc_reduce_kernel<<<(ntr * 4 + 127) / 128, 128, 0, s>>>(part, flags, nb, (int)t->chainsize, dout, dover);
   count_launch(3);

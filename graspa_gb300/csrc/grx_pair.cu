@@ -9,35 +9,6 @@
 
 namespace grx {
 
-// Trial energies of one bead per block (compacted pair engine, grx_warp.cuh);
-// per-bead sums go to part[bead][4] and the overlap flag to flags[bead].
-template <int PREC>
-__global__ void __launch_bounds__(GRX_THREADS) trial_bead_kernel(BoxDev b, const Bead* beads, int component,
-                                                                 int newmol, int excl_comp, int excl_mol,
-                                                                 double* part, int* flags) {
-  __shared__ double ipart[kMaxItems * 4];
-  __shared__ int iflag[kMaxItems];
-  __shared__ int qbuf[(GRX_THREADS / 32) * kQueue];
-  __shared__ int counter;
-  if (threadIdx.x == 0) counter = 0;
-  __syncthreads();
-  const PassSplit sp = pass_split(b, 1, GRX_THREADS / 32, 4);
-  const int nch = (int)sp.items;  // one bead: slot = item
-  block_bead_pass<PREC>(b, beads + blockIdx.x, 1, component, newmol, excl_comp, excl_mol, qbuf, ipart, iflag,
-                        &counter, sp);
-  __syncthreads();
-  if (threadIdx.x < 4) {
-    double s = 0.0;
-    for (int c = 0; c < nch; ++c) s += item_get<PREC>(ipart, c * 4 + threadIdx.x);
-    part[blockIdx.x * 4 + threadIdx.x] = s;
-  }
-  if (threadIdx.x == 0) {
-    int f = 0;
-    for (int c = 0; c < nch; ++c) f |= iflag[c];
-    flags[blockIdx.x] = f;
-  }
-}
-
 // Fixed-order reduction: trial t, quantity q = sum over blocks, then chain beads.
 __global__ void trial_reduce_kernel(const double* part, const int* flags, int nblk, int nb, int chain,
                                     double* out, int* tflag) {

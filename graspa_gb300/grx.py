@@ -103,7 +103,9 @@ class GcmcDesc(C.Structure):
 class GcmcStats(C.Structure):
     _fields_ = [("attempts", C.c_int64 * 5), ("accepted", C.c_int64 * 5), ("n_molecules", C.c_int64),
                 ("capacity_hits", C.c_int64), ("energy", C.c_double * 4), ("sum_n", C.c_double),
-                ("identity_out", C.c_int64 * 2), ("identity_in", C.c_int64 * 2)]
+                ("identity_out", C.c_int64 * 2), ("identity_in", C.c_int64 * 2),
+                ("rosen", C.c_double * 3), ("trial_configs", C.c_int64),
+                ("trial_beads", C.c_int64)]
 
 JOB_WIDOM, JOB_GCMC = 0, 1
 GCMC_TUNE_CANDIDATES = 9  # GRX_GCMC_TUNE_CANDIDATES: warps per box 8/12/24 x items per warp 1/2/4
@@ -512,14 +514,15 @@ class Box:
         return e, flag
 
     def trial_energies_noalloc(self, pos, charge, types, molid, ntrials, chainsize, component, prec=GRX_FP64,
-                               excl_comp=-1, excl_molid=-1):
-        """grx_trial_energies_noalloc: the same call with its scratch in a fixed device array."""
-        nb = ntrials * chainsize
+                               excl_comp=-1, excl_molid=-1, scale=None, scale_coul=None):
+        """grx_trial_energies_noalloc: the same call with its scratch in a fixed device array.
+        charge, scale or scale_coul None pass a null pointer (charges 0, scalings 1)."""
         pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1)
-        charge = np.ascontiguousarray(charge, dtype=np.float64)
         types = np.ascontiguousarray(types, dtype=np.uint64)
-        ones = np.ones(nb)
-        t = Trials(_d(pos), _d(ones), _d(charge), _d(ones), _sz(types), molid, ntrials, chainsize)
+        keep = [np.ascontiguousarray(a, dtype=np.float64) if a is not None else None
+                for a in (scale, charge, scale_coul)]
+        ptr = [_d(a) if a is not None else None for a in keep]
+        t = Trials(_d(pos), ptr[0], ptr[1], ptr[2], _sz(types), molid, ntrials, chainsize)
         out = (TrialEnergy * ntrials)()
         flag = np.zeros(ntrials, dtype=np.uint8)
         st = self.L.grx_trial_energies_noalloc(self.h, C.byref(t), component, excl_comp, excl_molid, prec, out,

@@ -388,6 +388,17 @@ typedef struct {
   int64_t identity_out[2];    /* identity swaps removing this component: attempts, accepted */
   int64_t identity_in[2];     /* identity swaps adding this component: attempts, accepted (the
                                  accepted swaps' dE count in this entry's energy sums) */
+  double rosen[3];            /* Rosenbluth weight W of every CBMC insertion attempt (W_first x
+                                 W_chain x exp(-beta dE_Fourier) x exp(-beta tail), 0 when the
+                                 growth fails; RecordRosen, data_struct.h:627-652): sum W,
+                                 sum W^2, attempts. <W> gives mu_ex and the Henry coefficient
+                                 (ComputeFugacity, print_statistics.cuh:99-109) */
+  int64_t trial_configs;      /* trial configurations the kernel evaluated against every atom:
+                                 first-bead positions, orientations (grown only after a
+                                 successful first bead) and the two configurations of a
+                                 translation / rotation (steps that picked this entry) */
+  int64_t trial_beads;        /* beads of those configurations (each evaluated against every
+                                 framework and guest atom) */
 } grx_gcmc_stats;
 
 /* nsteps GCMC moves on each of nboxes independent boxes (Markov chains), all on the
@@ -530,10 +541,11 @@ grx_status grx_server_launch_count(grx_server* server, uint64_t* launches);
  * grx_trial_energies; the scratch lives in one fixed device array of
  * GRX_NOALLOC_SCRATCH_BYTES held by every GPU that loads the library until exit.
  * Limit: ntrials * chainsize <= GRX_NOALLOC_MAX_BEADS, else GRX_ERR_CAPACITY.
- * The first call on a device looks up the array's device address (make it before
- * any stream capture). All calls share the array: calls that overlap on the GPU
- * race, so issue them one after another. The box is created beforehand with
- * grx_box_create. */
+ * The call works on the box's device (made current for the call, the caller's
+ * device restored after). The first call on a device looks up the array's device
+ * address (make it before any stream capture). All calls share the array: calls
+ * that overlap on the GPU race, so issue them one after another. The box is created
+ * beforehand with grx_box_create. */
 #define GRX_NOALLOC_MAX_BEADS 256
 #define GRX_NOALLOC_SCRATCH_BYTES 65536
 grx_status grx_trial_energies_noalloc(grx_box* box, const grx_trials* trials, int32_t component,

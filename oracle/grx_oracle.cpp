@@ -856,6 +856,7 @@ struct Grow {
   double stored = 0.0; // reinsertion: first-bead weight sum minus the selected trial
   double e1[4] = {0, 0, 0, 0}, e2[4] = {0, 0, 0, 0};
   std::vector<double> pos, qs;  // chosen (insertion) or existing (deletion) molecule
+  int64_t configs = 0, beads = 0;  // trial configurations evaluated and their beads
 };
 
 // RotationAroundAxis, mc_utilities.h:459-481, for a coordinate axis.
@@ -916,6 +917,8 @@ Grow cbmc_grow(const ora_box* box, const ora_ff* ff, const ora_atoms* at, int64_
   std::vector<double> e1(4 * nt);
   std::vector<uint8_t> f1(nt);
   ora_trial_energies(box, ff, at, &tr1, comp, -1, -1, e1.data(), f1.data());
+  g.configs += nt;
+  g.beads += nt;
   // log-weights of the trials without overlap (Host_sum_Widom_HGGG_SEPARATE)
   auto logw_of = [&](const std::vector<double>& e, const std::vector<uint8_t>& f, int64_t n,
                      std::vector<double>& lw, std::vector<int64_t>& idx) {
@@ -973,6 +976,8 @@ Grow cbmc_grow(const ora_box* box, const ora_ff* ff, const ora_atoms* at, int64_
     std::vector<double> e2(4 * no);
     std::vector<uint8_t> f2(no);
     ora_trial_energies(box, ff, at, &tr2, comp, -1, -1, e2.data(), f2.data());
+    g.configs += no;
+    g.beads += no * chain;
     std::vector<double> lw2;
     std::vector<int64_t> idx2;
     logw_of(e2, f2, no, lw2, idx2);
@@ -1002,7 +1007,7 @@ Grow cbmc_grow(const ora_box* box, const ora_ff* ff, const ora_atoms* at, int64_
 
 extern "C" void ora_gcmc_run_mix(const ora_box* box, const ora_ff* ff, double* pos, double* charge,
                                  int64_t* type, int64_t* molid, int64_t ncomp, int64_t nhost, int64_t* comp_size,
-                                 const int64_t* comp_off, const int64_t* molsize, const double* const* mol_pos_k,
+                                 const int64_t* comp_off, const int64_t* molsize, double* const* mol_pos_k,
                                  const double* const* mol_charge_k, const int64_t* const* mol_type_k,
                                  const double* excl_intra_k, const double* excl_self_k, double* s_fw, double* s_ads,
                                  const ora_gcmc* gk, int64_t ng, uint64_t first_step, int64_t nsteps,
@@ -1065,6 +1070,8 @@ extern "C" void ora_gcmc_run_mix(const ora_box* box, const ora_ff* ff, double* p
     if (kind == 0 || kind == 1) {
       if (N > 0) {
         st->attempts[kind]++;
+        st->trial_configs += 2;
+        st->trial_beads += 2 * ms;
         const int64_t m0 = a0 + mol * ms;
         std::vector<double> oldp(S.pos.begin() + 3 * m0, S.pos.begin() + 3 * (m0 + ms)), newp(3 * ms);
         if (kind == 0) {  // get_new_position TRANSLATION (mc_utilities.h:500-515)
@@ -1121,9 +1128,13 @@ extern "C" void ora_gcmc_run_mix(const ora_box* box, const ora_ff* ff, double* p
       ora_atoms at = S.view();
       Grow gi = cbmc_grow(box, ff, &at, comp, ms, slot0.data(), mol_charge, mol_type, g->ntrials, g->norient,
                           g->beta, g->seed, g->stream, move, mol, G_REINS, nullptr);
+      st->trial_configs += gi.configs;
+      st->trial_beads += gi.beads;
       if (gi.ok) {
         Grow gr = cbmc_grow(box, ff, &at, comp, ms, slot0.data(), mol_charge, mol_type, g->ntrials, g->norient,
                             g->beta, g->seed, g->stream, move, mol, G_RETRACE, oldp.data(), gi.stored);
+        st->trial_configs += gr.configs;
+        st->trial_beads += gr.beads;
         if (gr.ok) {
           double rosen = gi.rosen, ew = 0.0;
           if (charged) {  // Calculate_AdjustRosenbluth: old molecule out, new in, no exclusion change
@@ -1153,6 +1164,9 @@ extern "C" void ora_gcmc_run_mix(const ora_box* box, const ora_ff* ff, double* p
       ora_atoms at = S.view();
       Grow gr = cbmc_grow(box, ff, &at, comp, ms, slot0.data(), mol_charge, mol_type, g->ntrials, g->norient,
                           g->beta, g->seed, g->stream, move, N, G_INSERT, nullptr);
+      st->trial_configs += gr.configs;
+      st->trial_beads += gr.beads;
+      double rosen_rec = 0.0;  // RecordRosen: W of the insertion, 0 when the growth failed
       if (gr.ok) {
         double ew = 0.0, rosen = gr.rosen;
         if (charged) {
@@ -1164,6 +1178,7 @@ extern "C" void ora_gcmc_run_mix(const ora_box* box, const ora_ff* ff, double* p
           rosen *= std::exp(-g->beta * ew);
         }
         rosen *= std::exp(-g->beta * g->tail_insert);  // Insertion_Body (mc_swap_utilities.h:105-108)
+        rosen_rec = rosen;
         const double pre = g->beta * bigP / (1.0 + (double)N);  // GetPrefactor INSERTION
         const double pacc = pre * rosen / g->ideal_rosenbluth;
         if (rosen > 1e-150 && uacc < pacc) {
@@ -1188,6 +1203,9 @@ extern "C" void ora_gcmc_run_mix(const ora_box* box, const ora_ff* ff, double* p
           st->energy[3] += ev + er + ew;
         }
       }
+      st->rosen[0] += rosen_rec;
+      st->rosen[1] += rosen_rec * rosen_rec;
+      st->rosen[2] += 1.0;
     } else if (kind == 3 && N > 0) {  // CBMC deletion (DeletionMove::Run, move_struct.h:148-167)
       st->attempts[3]++;
       const int64_t m0 = a0 + mol * ms;
@@ -1195,6 +1213,8 @@ extern "C" void ora_gcmc_run_mix(const ora_box* box, const ora_ff* ff, double* p
       ora_atoms at = S.view();
       Grow gr = cbmc_grow(box, ff, &at, comp, ms, slot0.data(), mol_charge, mol_type, g->ntrials, g->norient,
                           g->beta, g->seed, g->stream, move, mol, G_DELETE, oldp.data());
+      st->trial_configs += gr.configs;
+      st->trial_beads += gr.beads;
       if (gr.ok) {
         double rosen = gr.rosen, ew = 0.0;
         std::vector<double> q(S.charge.begin() + m0, S.charge.begin() + m0 + ms);
@@ -1254,7 +1274,11 @@ extern "C" void ora_gcmc_run_mix(const ora_box* box, const ora_ff* ff, double* p
       molid[k] = S.molid[j];
     }
   }
-  for (int64_t k = 0; k < ng; ++k) stk[k].n_molecules = comp_size[gk[k].component] / molsize[gk[k].component];
+  for (int64_t k = 0; k < ng; ++k) {
+    stk[k].n_molecules = comp_size[gk[k].component] / molsize[gk[k].component];
+    // the slot-0 coordinates the orientations grow from, for a later call that continues the chain
+    std::copy(slot0s[k].begin(), slot0s[k].end(), mol_pos_k[k]);
+  }
 }
 
 extern "C" void ora_gcmc_run(const ora_box* box, const ora_ff* ff, double* pos, double* charge, int64_t* type,
@@ -1263,6 +1287,8 @@ extern "C" void ora_gcmc_run(const ora_box* box, const ora_ff* ff, double* pos, 
                              const double* mol_charge, const int64_t* mol_type, double excl_intra,
                              double excl_self, double* s_fw, double* s_ads, const ora_gcmc* g,
                              uint64_t first_step, int64_t nsteps, ora_gcmc_stats* st) {
-  ora_gcmc_run_mix(box, ff, pos, charge, type, molid, ncomp, nhost, comp_size, comp_off, molsize, &mol_pos,
+  std::vector<double> slot0(mol_pos, mol_pos + 3 * molsize[g->component]);
+  double* slot0_p = slot0.data();
+  ora_gcmc_run_mix(box, ff, pos, charge, type, molid, ncomp, nhost, comp_size, comp_off, molsize, &slot0_p,
                    &mol_charge, &mol_type, &excl_intra, &excl_self, s_fw, s_ads, g, 1, first_step, nsteps, st);
 }

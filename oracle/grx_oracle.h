@@ -204,6 +204,11 @@ typedef struct {
   int64_t n_molecules;
   double energy[4];       /* running sums of accepted dE: vdw, real, ewald, total */
   double sum_n;           /* sum of N after every step (loading average) */
+  double rosen[3];        /* insertion attempts' Rosenbluth weights (RecordRosen): sum W, sum W^2,
+                             attempts; W = 0 when the growth failed */
+  int64_t trial_configs;  /* trial configurations evaluated (first beads, orientations grown after
+                             a successful first bead, 2 per translation / rotation) */
+  int64_t trial_beads;    /* their beads */
 } ora_gcmc_stats;
 
 /* Runs nsteps moves on one box. atoms/s_ads are updated in place (guest component
@@ -218,10 +223,11 @@ void ora_gcmc_run(const ora_box* box, const ora_ff* ff, double* pos, double* cha
 /* Mixture form: ng moved components (gk[k], one template / exclusion pair each;
  * seed and stream from gk[0]); every step picks entry floor(u * ng) with word 3 of
  * the displacement slot (Select_Box_Component_Molecule, axpy.cu:74-100). stk[k]
- * receives entry k's counts. */
+ * receives entry k's counts. mol_pos_k[k] holds the component's slot-0 coordinates the
+ * orientations grow from, in and out, so a later call continues the same chain. */
 void ora_gcmc_run_mix(const ora_box* box, const ora_ff* ff, double* pos, double* charge, int64_t* type,
                       int64_t* molid, int64_t ncomp, int64_t nhost, int64_t* comp_size, const int64_t* comp_off,
-                      const int64_t* molsize, const double* const* mol_pos_k, const double* const* mol_charge_k,
+                      const int64_t* molsize, double* const* mol_pos_k, const double* const* mol_charge_k,
                       const int64_t* const* mol_type_k, const double* excl_intra_k, const double* excl_self_k,
                       double* s_fw, double* s_ads, const ora_gcmc* gk, int64_t ng, uint64_t first_step,
                       int64_t nsteps, ora_gcmc_stats* stk);

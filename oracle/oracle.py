@@ -70,7 +70,8 @@ class OraGcmc(C.Structure):
 
 class OraGcmcStats(C.Structure):
     _fields_ = [("attempts", C.c_int64 * 5), ("accepted", C.c_int64 * 5), ("n_molecules", C.c_int64),
-                ("energy", C.c_double * 4), ("sum_n", C.c_double)]
+                ("energy", C.c_double * 4), ("sum_n", C.c_double), ("rosen", C.c_double * 3),
+                ("trial_configs", C.c_int64), ("trial_beads", C.c_int64)]
 
 
 def build(force=False):
@@ -276,72 +277,9 @@ class OracleSystem:
         """Run nsteps GCMC moves (oracle). params: one OraGcmc, or a list of them for a
         mixture (one per moved component). Returns (stats, system_after, s_ads_after),
         stats a list when params is a list."""
-        plist = list(params) if isinstance(params, (list, tuple)) else [params]
-        sysd = self.s
-        cs = list(sysd["comp_start"])
-        ncomp = len(cs) - 1
-        sizes = np.array([cs[c + 1] - cs[c] for c in range(ncomp)], dtype=np.int64)
-        offs = np.zeros(ncomp, dtype=np.int64)
-        caps = [max(sizes[c], capacity[c]) for c in range(ncomp)]
-        for c in range(1, ncomp):
-            offs[c] = offs[c - 1] + caps[c - 1]
-        tot = int(offs[-1] + caps[-1])
-        pos = np.zeros(3 * tot)
-        q = np.zeros(tot)
-        ty = np.zeros(tot, dtype=np.int64)
-        mol = np.zeros(tot, dtype=np.int64)
-        P_ = np.asarray(sysd["pos"], dtype=np.float64).reshape(-1, 3)
-        for c in range(ncomp):
-            a, b = cs[c], cs[c + 1]
-            o = offs[c]
-            pos[3 * o:3 * (o + b - a)] = P_[a:b].reshape(-1)
-            q[o:o + b - a] = np.asarray(sysd["charge"])[a:b]
-            ty[o:o + b - a] = np.asarray(sysd["type"])[a:b]
-            mol[o:o + b - a] = np.asarray(sysd["molid"])[a:b]
-        ms = np.array(sysd["molsize"], dtype=np.int64)
-        keep = []
-        mps, mqs, mts, ein, esf = [], [], [], [], []
-        for pr in plist:
-            comp = pr.component
-            tm = sysd["templates"][comp]
-            a, b = cs[comp], cs[comp + 1]
-            mp = np.ascontiguousarray((P_[a:a + ms[comp]] if b > a else tm["pos"]).reshape(-1), dtype=np.float64)
-            mq = np.ascontiguousarray(tm["charge"], dtype=np.float64)
-            mt = np.ascontiguousarray(tm["type"], dtype=np.int64)
-            intra, self_ = self.rigid_exclusion(mp, mq, np.ones(len(mq)))
-            keep += [mp, mq, mt]
-            mps.append(_d(mp))
-            mqs.append(_d(mq))
-            mts.append(_i(mt))
-            ein.append(intra)
-            esf.append(self_)
-        ng = len(plist)
-        _, s_fw, s_ads = self.ewald_total(list(ms))
-        st = (OraGcmcStats * ng)()
-        gk = (OraGcmc * ng)(*plist)
-        lib().ora_gcmc_run_mix(C.byref(self.box), C.byref(self.ff), _d(pos), _d(q), _i(ty), _i(mol), ncomp,
-                               sysd["nhost"], _i(sizes), _i(offs), _i(ms), (_dp * ng)(*mps), (_dp * ng)(*mqs),
-                               (_i64p * ng)(*mts), (C.c_double * ng)(*ein), (C.c_double * ng)(*esf), _d(s_fw),
-                               _d(s_ads), gk, ng, first_step, nsteps, st)
-        after = dict(sysd)
-        newpos, newq, newt, newm = [], [], [], []
-        starts = [0]
-        for c in range(ncomp):
-            o, n = offs[c], sizes[c]
-            newpos.append(pos[3 * o:3 * (o + n)].reshape(-1, 3))
-            newq.append(q[o:o + n])
-            newt.append(ty[o:o + n])
-            newm.append(mol[o:o + n])
-            starts.append(starts[-1] + n)
-        after["pos"] = np.concatenate(newpos)
-        after["charge"] = np.concatenate(newq)
-        after["type"] = np.concatenate(newt)
-        after["molid"] = np.concatenate(newm)
-        after["scale"] = np.ones(starts[-1])
-        after["scale_coul"] = np.ones(starts[-1])
-        after["comp_start"] = starts
-        stats = list(st) if isinstance(params, (list, tuple)) else st[0]
-        return stats, after, s_ads
+        ch = OracleChain(self, params, capacity)
+        stats = ch.run(first_step, nsteps)
+        return (stats if isinstance(params, (list, tuple)) else stats[0]), ch.state(), ch.s_ads
 
     def widom(self, params, s_fw, s_ads, first_move, n, nthreads=0):
         res = (OraWidomResult * n)()
@@ -383,3 +321,102 @@ def mix_lb(eps_K, sigma, shifted, cutoff_vdw):
     lib().ora_mix_lorentz_berthelot(n, _d(e), _d(s), sh.ctypes.data_as(C.POINTER(C.c_int32)),
                                     cutoff_vdw ** 2, _d(eo), _d(so), _d(sho))
     return eo, so, sho
+
+
+class OracleChain:
+    """One GCMC chain whose state stays resident in host memory across calls: atoms,
+    molecule counts, both structure factors and the slot-0 templates the orientations grow
+    from. The FP64 Ewald totals (framework S(k) and the adsorbate S(k), framework
+    exclusions included) are computed once here, at set-up; `run` then only makes moves,
+    continuing the chain where the last call left it (the same trajectory as one long
+    call)."""
+
+    def __init__(self, osys, params, capacity, ewald=None):
+        """ewald: (s_fw, s_ads) of the starting state when already known (copied), else
+        computed here."""
+        self.osys = osys if isinstance(osys, OracleSystem) else OracleSystem(osys)
+        plist = list(params) if isinstance(params, (list, tuple)) else [params]
+        sysd = self.osys.s
+        cs = list(sysd["comp_start"])
+        ncomp = len(cs) - 1
+        sizes = np.array([cs[c + 1] - cs[c] for c in range(ncomp)], dtype=np.int64)
+        offs = np.zeros(ncomp, dtype=np.int64)
+        caps = [max(sizes[c], capacity[c]) for c in range(ncomp)]
+        for c in range(1, ncomp):
+            offs[c] = offs[c - 1] + caps[c - 1]
+        tot = int(offs[-1] + caps[-1])
+        self.pos = np.zeros(3 * tot)
+        self.q = np.zeros(tot)
+        self.ty = np.zeros(tot, dtype=np.int64)
+        self.mol = np.zeros(tot, dtype=np.int64)
+        P_ = np.asarray(sysd["pos"], dtype=np.float64).reshape(-1, 3)
+        for c in range(ncomp):
+            a, b = cs[c], cs[c + 1]
+            o = offs[c]
+            self.pos[3 * o:3 * (o + b - a)] = P_[a:b].reshape(-1)
+            self.q[o:o + b - a] = np.asarray(sysd["charge"])[a:b]
+            self.ty[o:o + b - a] = np.asarray(sysd["type"])[a:b]
+            self.mol[o:o + b - a] = np.asarray(sysd["molid"])[a:b]
+        self.ms = np.array(sysd["molsize"], dtype=np.int64)
+        self.sizes, self.offs, self.ncomp = sizes, offs, ncomp
+        self.keep = []
+        mps, mqs, mts, ein, esf = [], [], [], [], []
+        for pr in plist:
+            comp = pr.component
+            tm = sysd["templates"][comp]
+            a, b = cs[comp], cs[comp + 1]
+            mp = np.ascontiguousarray((P_[a:a + self.ms[comp]] if b > a else tm["pos"]).reshape(-1),
+                                      dtype=np.float64).copy()
+            mq = np.ascontiguousarray(tm["charge"], dtype=np.float64)
+            mt = np.ascontiguousarray(tm["type"], dtype=np.int64)
+            intra, self_ = self.osys.rigid_exclusion(mp, mq, np.ones(len(mq)))
+            self.keep += [mp, mq, mt]
+            mps.append(_d(mp))
+            mqs.append(_d(mq))
+            mts.append(_i(mt))
+            ein.append(intra)
+            esf.append(self_)
+        ng = len(plist)
+        self.ng = ng
+        if ewald is None:
+            _, self.s_fw, self.s_ads = self.osys.ewald_total(list(self.ms))
+        else:
+            self.s_fw, self.s_ads = np.array(ewald[0], dtype=np.float64), np.array(ewald[1], dtype=np.float64)
+        self.mps = (_dp * ng)(*mps)
+        self.mqs = (_dp * ng)(*mqs)
+        self.mts = (_i64p * ng)(*mts)
+        self.ein = (C.c_double * ng)(*ein)
+        self.esf = (C.c_double * ng)(*esf)
+        self.gk = (OraGcmc * ng)(*plist)
+
+    def run(self, first_step, nsteps):
+        """nsteps moves from Philox move index first_step; returns one OraGcmcStats per
+        moved component, counted over this call."""
+        st = (OraGcmcStats * self.ng)()
+        sysd = self.osys.s
+        lib().ora_gcmc_run_mix(C.byref(self.osys.box), C.byref(self.osys.ff), _d(self.pos), _d(self.q), _i(self.ty),
+                               _i(self.mol), self.ncomp, sysd["nhost"], _i(self.sizes), _i(self.offs), _i(self.ms),
+                               self.mps, self.mqs, self.mts, self.ein, self.esf, _d(self.s_fw), _d(self.s_ads),
+                               self.gk, self.ng, first_step, nsteps, st)
+        return list(st)
+
+    def state(self):
+        """The chain's atoms as a system dict (components compacted)."""
+        after = dict(self.osys.s)
+        newpos, newq, newt, newm = [], [], [], []
+        starts = [0]
+        for c in range(self.ncomp):
+            o, n = self.offs[c], self.sizes[c]
+            newpos.append(self.pos[3 * o:3 * (o + n)].reshape(-1, 3))
+            newq.append(self.q[o:o + n])
+            newt.append(self.ty[o:o + n])
+            newm.append(self.mol[o:o + n])
+            starts.append(starts[-1] + n)
+        after["pos"] = np.concatenate(newpos)
+        after["charge"] = np.concatenate(newq)
+        after["type"] = np.concatenate(newt)
+        after["molid"] = np.concatenate(newm)
+        after["scale"] = np.ones(starts[-1])
+        after["scale_coul"] = np.ones(starts[-1])
+        after["comp_start"] = starts
+        return after

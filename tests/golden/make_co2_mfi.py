@@ -13,7 +13,7 @@ tests/golden/co2_mfi/ and writes the printed values to tests/golden/co2_mfi/expe
 It runs only where the reference tree is mounted; the fixture is committed so nothing
 at test time reads the reference.
 
-Usage: python tests/golden/make_co2_mfi.py [/path/to/reference]
+Usage: python tests/golden/make_co2_mfi.py /path/to/gRASPA  (the reference checkout; required)
 """
 import json
 import os
@@ -55,4 +55,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_co2_mfi.py /path/to/gRASPA")
+    main(sys.argv[1])

@@ -14,7 +14,7 @@ LJ parameters) and the printed totals, and writes one compact JSON per box to
 tests/golden/nist_spce_box{N}.json. It runs only where the reference tree is
 mounted; the JSON files are committed so nothing at test time reads the reference.
 
-Usage: python tests/golden/make_nist_spce.py [/path/to/reference]
+Usage: python tests/golden/make_nist_spce.py /path/to/gRASPA  (the reference checkout; required)
 """
 import json
 import math
@@ -144,7 +144,9 @@ def make_box(ref, n):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_nist_spce.py /path/to/gRASPA")
+    ref = sys.argv[1]
     for n in (1, 2, 3, 4):
         box = make_box(ref, n)
         path = os.path.join(HERE, f"nist_spce_box{n}.json")
