@@ -420,37 +420,73 @@ def widom_accuracy(box, grx, system, n=200):
 
 
 def bench_serving(args, grx):
+    """configs[4]'s serving stream: jobs of Widom (5k insertions) or GCMC (2k cycles of 20
+    steps), five species, frameworks of 200-20,000 atoms, through grx_server (continuous
+    batching, admission by HBM footprint). First all jobs at once (saturation: jobs/s and
+    trial energies/s at capacity), then Poisson arrivals at fractions of that rate (jobs/s,
+    p50 / p99 latency per rate). The plain one-job-at-a-time FP64 form runs a sample of the
+    same jobs with GCMC shortened to serve_fp64_cycles cycles; its trial energies/s do not
+    depend on the job length, and its job rate is extrapolated to full-length jobs by the
+    per-job service time scaled by steps."""
     from graspa_gb300 import serving, synth
     n = args.serve_jobs
-    jobs = [synth.serving_job(j, widom_insertions=5000, gcmc_cycles=args.serve_gcmc_cycles)
-            for j in range(n)]
-    rate = args.serve_rate
+    t0 = time.perf_counter()
+    jobs = [synth.serving_job(j, widom_insertions=5000, gcmc_cycles=args.serve_gcmc_cycles) for j in range(n)]
+    t_gen = time.perf_counter() - t0
+
+    def stream(arrivals):
+        srv = grx.Server(args.serve_hbm_gb * (1 << 30), max_resident=args.serve_slots, prec=grx.GRX_MIXED,
+                         widom_slice=0, gcmc_slice=args.serve_gcmc_slice, cluster_atoms=args.serve_cluster_atoms)
+        out = serving.run_stream(srv, jobs, arrivals, timeout=1800.0)
+        srv.close()
+        summ = serving.summarize(out)
+        te = sum(serving.trial_energies_of(jobs[i], r) for i, (r, _) in out.items())
+        summ["trial_energies_per_s"] = te / summ["makespan_s"]
+        summ["trial_energies"] = te
+        return summ
+
+    sat = stream(None)   # every job at t = 0: throughput at capacity
+    rate_sat = sat["jobs_per_s"]
+    sweep = []
     g = np.random.default_rng(7)
-    arrivals = np.cumsum(g.exponential(1.0 / rate, n))
-    srv = grx.Server(args.serve_hbm_gb * (1 << 30), max_resident=args.serve_slots, prec=grx.GRX_MIXED,
-                     widom_slice=0, gcmc_slice=args.serve_gcmc_slice, cluster_atoms=args.serve_cluster_atoms)
-    out = serving.run_stream(srv, jobs, arrivals, timeout=600.0)
-    srv.close()
-    summ = serving.summarize(out)
-    te = sum(serving.trial_energies_of(jobs[i], r) for i, (r, _) in out.items())
-    summ["trial_energies_per_s"] = te / summ["makespan_s"]
-    # the plain one-job-at-a-time FP64 form on a subsample: service times, no overlap
-    sub = jobs[: args.serve_fp64_jobs]
+    for f in args.serve_rate_fractions:
+        rate = f * rate_sat
+        arrivals = np.cumsum(g.exponential(1.0 / rate, n))
+        r = stream(arrivals)
+        r.update(arrival_rate_per_s=rate, fraction_of_saturation=f)
+        sweep.append(r)
+    # the plain one-job-at-a-time FP64 form on a sample (GCMC shortened, scaled back by steps)
+    sub = []
+    for k in range(args.serve_fp64_jobs):
+        J = dict(jobs[k])
+        if J["kind"] == "gcmc":
+            J["gcmc_steps"] = args.serve_fp64_cycles * 20
+        sub.append(J)
     plain = grx.Server(args.serve_hbm_gb * (1 << 30), max_resident=1, prec=grx.GRX_FP64)
     t0 = time.perf_counter()
-    out64 = serving.run_stream(plain, sub, None, timeout=600.0)
+    out64 = serving.run_stream(plain, sub, None, timeout=1800.0)
     dt = time.perf_counter() - t0
     plain.close()
-    svc = np.array([r.t_done - r.t_admit for (r, _) in out64.values()])
+    svc, svc_full = [], []
+    for i, (r, _) in out64.items():
+        t = r.t_done - r.t_admit
+        svc.append(t)
+        svc_full.append(t * (jobs[i]["gcmc_steps"] / sub[i]["gcmc_steps"] if sub[i]["kind"] == "gcmc" else 1.0))
     te64 = sum(serving.trial_energies_of(sub[i], r) for i, (r, _) in out64.items())
-    return {"jobs": n, "arrival_rate_per_s": rate, "slots": args.serve_slots, "gcmc_cycles": args.serve_gcmc_cycles,
-            "cluster_atoms": args.serve_cluster_atoms,
-            "widom_insertions": 5000, "species": "CH4 CO2 N2 Xe Kr uniform", "framework_atoms": "200-20000 log-uniform",
-            **summ,
-            "plain_fp64_one_at_a_time": {"jobs": len(sub), "jobs_per_s": len(sub) / dt,
-                                         "service_p50_s": float(np.percentile(svc, 50)),
-                                         "service_p99_s": float(np.percentile(svc, 99)),
-                                         "trial_energies_per_s": te64 / dt}}
+    plain_te = te64 / dt
+    return {"jobs": n, "slots": args.serve_slots, "gcmc_cycles": args.serve_gcmc_cycles,
+            "gcmc_steps_per_job": args.serve_gcmc_cycles * 20, "widom_insertions": 5000,
+            "cluster_atoms": args.serve_cluster_atoms, "species": "CH4 CO2 N2 Xe Kr uniform",
+            "framework_atoms": "200-20000 log-uniform", "job_generation_s": t_gen,
+            "saturation": sat, "sweep": sweep,
+            "p50_s": sweep[0]["p50_s"] if sweep else sat["p50_s"],
+            "p99_s": sweep[0]["p99_s"] if sweep else sat["p99_s"],
+            "plain_fp64_one_at_a_time": {
+                "jobs": len(sub), "gcmc_cycles": args.serve_fp64_cycles, "trial_energies_per_s": plain_te,
+                "service_p50_s": float(np.percentile(svc, 50)),
+                "jobs_per_s_full_length": len(svc_full) / float(np.sum(svc_full)),
+                "note": "GCMC jobs shortened to gcmc_cycles; full-length service times scaled by steps"},
+            "saturation_speedup_over_plain_fp64": sat["trial_energies_per_s"] / plain_te}
 
 
 def run_grx(args):
@@ -545,6 +581,8 @@ def run_grx(args):
         if serve:
             line["p99_job_latency_s"] = serve["p99_s"]
             line["p50_job_latency_s"] = serve["p50_s"]
+            line["latency_at"] = "Poisson arrivals at %.2f of the saturation rate" % (
+                args.serve_rate_fractions[0] if args.serve_rate_fractions else 1.0)
     if dist:
         dist.barrier()
         dist.destroy_process_group()
@@ -799,13 +837,15 @@ def main():
     ap.add_argument("--insertions", type=int, default=20000, help="Widom insertions per launch")
     ap.add_argument("--widom-steps", type=int, default=5)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
-    ap.add_argument("--serve-jobs", type=int, default=48)
-    ap.add_argument("--serve-rate", type=float, default=40.0, help="Poisson arrival rate, jobs/s")
+    ap.add_argument("--serve-jobs", type=int, default=1000, help="jobs per stream (the full configs[4] sweep: 10000)")
+    ap.add_argument("--serve-rate-fractions", type=float, nargs="*", default=[0.5, 0.8, 1.2],
+                    help="Poisson arrival rates swept, as fractions of the measured saturation rate")
     ap.add_argument("--serve-slots", type=int, default=152)
-    ap.add_argument("--serve-hbm-gb", type=float, default=8.0)
-    ap.add_argument("--serve-gcmc-cycles", type=int, default=100, help="GCMC cycles of 20 steps per serving job")
-    ap.add_argument("--serve-gcmc-slice", type=int, default=500)
-    ap.add_argument("--serve-fp64-jobs", type=int, default=6)
+    ap.add_argument("--serve-hbm-gb", type=float, default=16.0)
+    ap.add_argument("--serve-gcmc-cycles", type=int, default=2000, help="GCMC cycles of 20 steps per serving job")
+    ap.add_argument("--serve-gcmc-slice", type=int, default=2000)
+    ap.add_argument("--serve-fp64-jobs", type=int, default=24)
+    ap.add_argument("--serve-fp64-cycles", type=int, default=50, help="GCMC cycles of the plain FP64 sample's jobs")
     ap.add_argument("--serve-cluster-atoms", type=int, default=1000,
                     help="GCMC jobs of N atoms run on clusters of up to N / this many CTAs (0: off)")
     ap.add_argument("--profile", action="store_true", help="only the timed mixed GCMC steps (launch lists)")

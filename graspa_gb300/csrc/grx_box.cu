@@ -136,6 +136,11 @@ void refresh_dev(grx_box* b) {
   d.hscale = h->scale;
   d.hqdf = h->qdf;
   d.shared_host = b->parent ? 1 : 0;
+  d.vox = h->vox_on;
+  d.vmeta = h->vmeta;
+  d.vlist = h->vlist;
+  for (int k = 0; k < 3; ++k) d.vn[k] = h->vn[k];
+  d.vchunks = h->vchunks;
 }
 
 static float2 split_df(double x) {
@@ -702,6 +707,7 @@ grx_status grx_box_footprint(const grx_box_desc* desc, size_t* bytes) {
   t += al(na * sizeof(int4)) + al(na * sizeof(double)) + 3 * al(nv * sizeof(double2)) + 2 * al(na * sizeof(float4)) +
        al(na * sizeof(float2));
   t += al(ntiles * sizeof(float4)) + al(ntiles * sizeof(int4));
+
   if (!desc->forcefield.no_charges) {
     const float s_lo = 0.25f, s_hi = (float)(desc->forcefield.cutoff_coul_sq * (1.0 + 1e-4) + 1e-2);
     uint32_t lb, hb;
@@ -795,7 +801,7 @@ grx_status grx_box_destroy(grx_box* b) {
   void* ptrs[] = {b->pos64, b->hi, b->lo, b->meta, b->scale, b->charge, b->d_size, b->ff64,
                   b->ffc10, b->ff32, b->kact, b->ktemp, b->s_fw, b->s_ads, b->s_tmp,
                   b->scratch, b->d_results, b->tile_c, b->tile_r, b->ctab, b->ctabf, b->qdf,
-                  b->ffdf, b->ffdf2, b->ewA, b->ewF, b->ewT};
+                  b->ffdf, b->ffdf2, b->ewA, b->ewF, b->ewT, b->vmeta, b->vlist};
   for (void* p : ptrs) dev_free(b, p);
   if (b->pinned) cudaFreeHost(b->pinned);
   delete b;
@@ -916,6 +922,8 @@ grx_status grx_box_set_component(grx_box* b, int32_t comp, const grx_atoms* a, i
                  "upload sizes");
   if (comp < b->nhost) {
     grx_status st = build_tiles(b);
+    if (st) return st;
+    st = build_voxels(b);
     if (st) return st;
   }
   b->sk_valid = false;

@@ -41,6 +41,7 @@ struct CbmcWork {
   Bead beads[kCbmcBeads];
   double ipart[kItems * 4];
   int iflag[kItems];
+  int tdead[kCbmcBeads];  // per trial of a pass: early overlap rejection flag (-1: evaluated in full)
   int qbuf[NW * kQueue];
   double te[kMaxTrials * 4];
   int tflag[kMaxTrials];
@@ -135,7 +136,10 @@ __device__ __noinline__ void gen_orientations(const BoxDev& b, WK& W, uint64_t s
 
 // Energies of ntr = nb / chain trials of `chain` beads each (W.beads) against every
 // atom, with the atoms of (comp, newmol) and of (excl_comp, excl_mol) excluded (the
-// ExcludeList of an identity swap): W.te[4 t + k], W.tflag[t].
+// ExcludeList of an identity swap): W.te[4 t + k], W.tflag[t]. The first `early` trials
+// (all of them when early < 0) stop at their first overlap (early overlap rejection):
+// their flags are exact, their energies are not computed in full and must not be used
+// when flagged, which is how every CBMC step treats a flagged trial.
 // With CL > 1 the block is one CTA of a cluster that shares the chain: the pass is split
 // over the cluster's warps (items per warp capped so the slots fit the workspace), each
 // CTA copies its slots into its peers' workspaces, and every CTA reduces all slots. The
@@ -143,17 +147,19 @@ __device__ __noinline__ void gen_orientations(const BoxDev& b, WK& W, uint64_t s
 // is still reducing this one.
 template <int PREC, int CL, class WK>
 __device__ __forceinline__ void trial_pass_body(const BoxDev& b, WK& W, int nb, int chain, int comp, int newmol,
-                                                int excl_comp, int excl_mol) {
+                                                int excl_comp, int excl_mol, int early) {
   if (threadIdx.x == 0) {
     W.counter = 0;
     W.cfg += nb / chain;
     W.cbeads += nb;
   }
+  for (int t = threadIdx.x; t < nb / chain; t += blockDim.x) W.tdead[t] = (early < 0 || t < early) ? 0 : -1;
   __syncthreads();
   const int nw = (int)(blockDim.x >> 5);
   if constexpr (CL == 1) {
     const PassSplit sp = pass_split(b, nb, nw, b.chunk_mult);
-    block_bead_pass<PREC>(b, W.beads, nb, comp, newmol, excl_comp, excl_mol, W.qbuf, W.ipart, W.iflag, &W.counter, sp);
+    block_bead_pass<PREC>(b, W.beads, nb, comp, newmol, excl_comp, excl_mol, W.qbuf, W.ipart, W.iflag, &W.counter, sp,
+                          0, -1, chain, W.tdead);
     __syncthreads();
     reduce_items<PREC>(W.ipart, W.iflag, nb / chain, chain, sp, W.te, W.tflag);
     __syncthreads();
@@ -163,7 +169,7 @@ __device__ __forceinline__ void trial_pass_body(const BoxDev& b, WK& W, int nb, 
     int i0, i1;
     cluster_items(sp, CL, rank, i0, i1);
     block_bead_pass<PREC>(b, W.beads, nb, comp, newmol, excl_comp, excl_mol, W.qbuf, W.ipart, W.iflag, &W.counter, sp,
-                          i0, i1);
+                          i0, i1, chain, W.tdead);
     __syncthreads();
     if (sp.nu > 0 && i0 < i1) {  // this CTA's slots [s0, s0 + n): item + bead, increasing
       unsigned lo, hi;
@@ -191,14 +197,15 @@ __device__ __forceinline__ void trial_pass_body(const BoxDev& b, WK& W, int nb, 
 }
 
 template <int PREC, int CL = 1, class WK>
-__device__ __noinline__ void trial_pass(const BoxDev& b, WK& W, int nb, int chain, int comp, int newmol) {
-  trial_pass_body<PREC, CL>(b, W, nb, chain, comp, newmol, -1, -1);
+__device__ __noinline__ void trial_pass(const BoxDev& b, WK& W, int nb, int chain, int comp, int newmol,
+                                          int early = -1) {
+  trial_pass_body<PREC, CL>(b, W, nb, chain, comp, newmol, -1, -1, early);
 }
 // The same with a second excluded molecule (excl_comp, excl_mol).
 template <int PREC, int CL = 1, class WK>
 __device__ __noinline__ void trial_pass_excl(const BoxDev& b, WK& W, int nb, int chain, int comp, int newmol,
                                                int excl_comp, int excl_mol) {
-  trial_pass_body<PREC, CL>(b, W, nb, chain, comp, newmol, excl_comp, excl_mol);
+  trial_pass_body<PREC, CL>(b, W, nb, chain, comp, newmol, excl_comp, excl_mol, -1);
 }
 
 // CBMC weight of one growth step (warp 0 computes, results in W.ok/sel/w/nok/wraw).

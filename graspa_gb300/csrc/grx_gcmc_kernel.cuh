@@ -325,7 +325,9 @@ __global__ void __launch_bounds__(NW * 32, 24 / NW) gcmc_kernel(const BoxDev* bo
         make_bead(W.beads[ms + tid], p.x, p.y, p.z, p.w, sc, type, b.prefactor);
       }
       __syncthreads();
-      trial_pass<PREC, CL>(b, W, 2 * ms, ms, comp, mol);  // te[0..3] new, te[4..7] old
+      // te[0..3] new, te[4..7] old; the new configuration may stop at an overlap (the move is
+      // then rejected), the old one is evaluated in full
+      trial_pass<PREC, CL>(b, W, 2 * ms, ms, comp, mol, 1);
       if (!W.tflag[0]) {
         double same = 0.0, cross = 0.0;
         if (a.charged) ewald_delta_move<PREC, CL>(b, W, 2 * ms, eik, same, cross);

@@ -60,6 +60,14 @@ struct grx_box {
   size_t tile_cap = 0;
   int ntiles = 0;
   std::vector<int> perm[GRX_MAX_COMPONENTS];  // storage slot -> caller index
+  // candidate lists of host atoms per voxel (grx_voxel.cu); a replica uses its parent's
+  int vox_mode = 1;          // 1: build them when they fit, 0: tile path only
+  int vox_on = 0;
+  int vn[3] = {0, 0, 0};
+  int vchunks = 0;
+  size_t vox_entries = 0;
+  int4* vmeta = nullptr;
+  uint32_t* vlist = nullptr;
   // double-float copies for the mixed-precision pair path
   float2* qdf = nullptr;     // q * scaleCoul per atom as hi/lo floats
   float4* ffdf = nullptr;    // per type pair {4eps hi, lo, 1/sigma^2 hi, lo}
@@ -97,6 +105,8 @@ cudaError_t dev_alloc(grx_box* b, void** p, size_t bytes);
 // for replicas) and marks them valid.
 grx_status ewald_df_refresh(grx_box* b);
 void dev_free(grx_box* b, void* p);
+// Voxel candidate lists of the machine's host atoms (grx_voxel.cu), rebuilt after the tiles.
+grx_status build_voxels(grx_box* b);
 }  // namespace grx
 
 #define GRX_CHECK_CUDA(call, what)                                    \

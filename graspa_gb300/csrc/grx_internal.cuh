@@ -77,6 +77,12 @@ struct BoxDev {
   const float4* tile_c;  // per tile: {x, y, z, bounding radius}, {box half extents, 0}
   const int4* tile_r;    // {first atom, end atom, component, 0}
   int ntiles;
+  // voxel candidate lists of host atoms (grx_voxel.cu); used instead of the tiles when vox
+  const int4* vmeta;     // per voxel {first entry, sure atoms, all atoms, 0}
+  const unsigned* vlist; // entries: storage index | lattice shift << 20
+  int vox;
+  int vn[3];             // voxels along a, b, c
+  int vchunks;           // 32-entry chunks of the longest list
   int cull;              // tile culling on
   float cull_r;          // screening radius used by the tile test
   float cellf[9];

@@ -90,6 +90,9 @@ grx_status admit_job(grx_server* S, ServerJob* j) {
   grx_arena_usage(S->arena, &before, nullptr, nullptr);
   grx_status st = grx_box_create_in(&j->desc, S->arena, &j->box);
   if (st) return st;
+  // voxel candidate lists pay for their host-side build over the thousands of moves of a
+  // GCMC job; a Widom job is short, so its box keeps the tile path and is admitted sooner
+  if (j->kind == GRX_JOB_WIDOM) j->box->vox_mode = 0;
   if (!S->streams.empty()) {
     j->stream = S->streams.back();
     S->streams.pop_back();
@@ -179,11 +182,15 @@ grx_status collect(grx_server* S, ServerJob* j, grx_job_result& r) {
                      "widom results");
     GRX_CHECK_CUDA(cudaStreamSynchronize(j->stream), "widom results");
     double s = 0.0, s2 = 0.0;
+    const bool chain = j->box && j->box->molsize[j->widom.component] > 1;
+    int64_t cfg = 0;
     for (const grx_widom_result& x : h) {
       const double w = x.success ? x.rosenbluth : 0.0;
       s += w;
       s2 += w * w;
+      cfg += j->widom.ntrials + (chain && x.w_first > 0.0 ? j->widom.norient : 0);
     }
+    r.widom_trial_configs = cfg;
     r.widom_n = j->total;
     r.widom_mean_w = j->total ? s / (double)j->total : 0.0;
     r.widom_mean_w2 = j->total ? s2 / (double)j->total : 0.0;

@@ -211,24 +211,102 @@ __device__ __forceinline__ void pair_dense(const BoxDev& b, int i, const Bead& b
   }
 }
 
-// One work item: bead `bd` against host tiles [t0, t1) and, when `guests`, every live
-// guest atom. acc = {hg_vdw, hg_real, gg_vdw, gg_real} (valid on every lane, summed
-// later); flag is per lane.
-template <int PREC>
+// One work item: bead `bd` against host units [t0, t1) (tiles, or with VOX 32-entry chunks
+// of the bead's voxel list) and, when `guests`, every live guest atom. acc = {hg_vdw,
+// hg_real, gg_vdw, gg_real} (valid on every lane, summed later); flag is per lane.
+//
+// Early overlap rejection: with `dead` (the bead's trial's flag in shared memory, null
+// when the trial must be evaluated in full) the warp stops as soon as the trial is known
+// to overlap: after a dense batch that set an overlap flag (it then marks the trial), or
+// when another warp has marked it. An overlapping trial takes no part in the Rosenbluth
+// weight, and its flag is still raised by the warp that found the overlap, so the trial
+// flags (and every used energy) are the same as without the early exit.
+template <int PREC, bool VOX>
 __device__ __forceinline__ void warp_item(const BoxDev& b, const Bead& bd, int t0, int t1, int g0, int g1,
                                           int component, int newmol, int excl_comp, int excl_mol, int* q,
-                                          LaneAcc<PREC>& hacc, LaneAcc<PREC>& gacc, int& flag) {
+                                          LaneAcc<PREC>& hacc, LaneAcc<PREC>& gacc, int& flag,
+                                          volatile int* dead) {
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
   unsigned head = 0, tail = 0;
+  // the trial is dead (checked by lane 0, the answer shared, so the warp stays converged)
+  auto is_dead = [&]() { return dead && __shfl_sync(kFull, lane == 0 ? *dead : 0, 0) > 0; };
+  // after a dense batch: an overlap found by this warp kills the trial
+  auto found_overlap = [&]() {
+    if (!dead || !__any_sync(kFull, flag != 0)) return false;
+    if (lane == 0) *dead = 1;
+    return true;
+  };
+  bool stop = false;
   const df pq = {bd.pq.x, bd.pq.y};
   const float bx = bd.h.x + bd.l.x, by = bd.h.y + bd.l.y, bz = bd.h.z + bd.l.z;
   LaneAcc<PREC>& la = hacc;
+  if constexpr (VOX) {
+    // Host units are 32-entry chunks of the bead's voxel list (grx_voxel.cu): entries below
+    // vm.y are inside the cutoff for every bead of the voxel and are queued unscreened; the
+    // others are screened at the stored image against the bead wrapped into the home cell.
+    if (t1 > t0) {
+      const float fx = b.invf[0] * bx + b.invf[3] * by + b.invf[6] * bz;
+      const float fy = b.invf[1] * bx + b.invf[4] * by + b.invf[7] * bz;
+      const float fz = b.invf[2] * bx + b.invf[5] * by + b.invf[8] * bz;
+      const float mx = floorf(fx), my = floorf(fy), mz = floorf(fz);
+      const int ix = min(b.vn[0] - 1, max(0, (int)((fx - mx) * (float)b.vn[0])));
+      const int iy = min(b.vn[1] - 1, max(0, (int)((fy - my) * (float)b.vn[1])));
+      const int iz = min(b.vn[2] - 1, max(0, (int)((fz - mz) * (float)b.vn[2])));
+      const int4 vm = b.vmeta[(iz * b.vn[1] + iy) * b.vn[0] + ix];
+      const float wx = bd.h.x - (mx * b.cellf[0] + my * b.cellf[3] + mz * b.cellf[6]);
+      const float wy = bd.h.y - (mx * b.cellf[1] + my * b.cellf[4] + mz * b.cellf[7]);
+      const float wz = bd.h.z - (mx * b.cellf[2] + my * b.cellf[5] + mz * b.cellf[8]);
+      const unsigned* L = b.vlist + vm.x;
+      const bool hcheck = component < b.nhost || (excl_comp >= 0 && excl_comp < b.nhost);
+      const int cend = min(t1, (vm.z + 31) >> 5);
+      for (int ch = t0; ch < cend; ++ch) {
+        if (is_dead()) { stop = true; break; }
+        const int j = (ch << 5) + lane;
+        bool in = false;
+        int i = 0;
+        if (j < vm.z) {
+          const unsigned w = __ldg(L + j);
+          i = (int)(w & 0xFFFFFu);
+          if (j < vm.y) {
+            in = true;
+          } else if (PREC == GRX_FP64) {
+            in = pair_screen<PREC, true>(b, i, bd);
+          } else {
+            const float nx = (float)((int)((w >> 20) & 7u) - 4), ny = (float)((int)((w >> 23) & 7u) - 4),
+                        nz = (float)((int)((w >> 26) & 7u) - 4);
+            const float4 ah = b.hhi[i];
+            const float x = ah.x - wx - (nx * b.cellf[0] + ny * b.cellf[3] + nz * b.cellf[6]);
+            const float y = ah.y - wy - (nx * b.cellf[1] + ny * b.cellf[4] + nz * b.cellf[7]);
+            const float z = ah.z - wz - (nx * b.cellf[2] + ny * b.cellf[5] + nz * b.cellf[8]);
+            in = x * x + y * y + z * z < b.screen2;
+          }
+          if (in && hcheck) {  // a host component is moved or excluded: skip its molecule
+            int tz = 0;
+            while (tz + 1 < b.nhost && i >= b.comp_off[tz + 1]) ++tz;
+            const int mol = b.hmeta[i].y;
+            if ((tz == excl_comp && mol == excl_mol) || (tz == component && mol == newmol)) in = false;
+          }
+        }
+        const unsigned m = __ballot_sync(kFull, in);
+        if (in) q[(tail + __popc(m & lt)) & (kQueue - 1)] = i;
+        tail += __popc(m);
+        if (tail - head >= 32) {
+          __syncwarp();
+          const int jq = q[(head + lane) & (kQueue - 1)];
+          __syncwarp();
+          pair_dense<PREC, true>(b, jq, bd, pq, la, flag);
+          head += 32;
+          if (found_overlap()) { stop = true; break; }
+        }
+      }
+    }
+  } else {
   // Tiles are tested 32 at a time, one per lane; survivors are then screened one
   // tile at a time by the whole warp. When a tile lies inside one periodic image of
   // the bead (stored positions compact, the tile sphere clear of the rounding
   // boundaries), the image shift is applied once to the bead instead of per atom.
-  for (int base = t0; base < t1; base += 32) {
+  for (int base = t0; base < t1 && !stop; base += 32) {
     const int tl = base + lane;
     bool pass = tl < t1;
     float sx = 0.f, sy = 0.f, sz = 0.f;  // image shift of the bead for this tile
@@ -279,6 +357,7 @@ __device__ __forceinline__ void warp_item(const BoxDev& b, const Bead& bd, int t
     }
     unsigned mask = __ballot_sync(kFull, pass);
     while (mask) {
+      if (is_dead()) { stop = true; break; }
       const int src = __ffs(mask) - 1;
       mask &= mask - 1;
       const int i = __shfl_sync(kFull, trl.x, src) + lane, tz = __shfl_sync(kFull, trl.z, src);
@@ -313,13 +392,16 @@ __device__ __forceinline__ void warp_item(const BoxDev& b, const Bead& bd, int t
         __syncwarp();
         pair_dense<PREC, true>(b, j, bd, pq, la, flag);
         head += 32;
+        if (found_overlap()) { stop = true; break; }
       }
     }
   }
+  }
+  if (stop) return;
   __syncwarp();
   if (lane < (int)(tail - head)) pair_dense<PREC, true>(b, q[(head + lane) & (kQueue - 1)], bd, pq, la, flag);
   __syncwarp();
-  if (g1 <= g0) return;
+  if (g1 <= g0 || found_overlap()) return;
   head = tail = 0;
   // guest atoms [g0, g1) of the concatenated adsorbate components
   for (int c = b.nhost, base = 0; c < b.ncomp && base < g1; ++c) {
@@ -330,6 +412,7 @@ __device__ __forceinline__ void warp_item(const BoxDev& b, const Bead& bd, int t
     if (hi <= lo) continue;
     const bool check = (c == component) || (c == excl_comp);
     for (int i0 = lo; i0 < hi; i0 += 32) {
+      if (is_dead()) return;
       const int i = off + i0 + lane;
       bool in = false;
       if (i0 + lane < hi) {
@@ -349,12 +432,14 @@ __device__ __forceinline__ void warp_item(const BoxDev& b, const Bead& bd, int t
         __syncwarp();
         pair_dense<PREC, false>(b, j, bd, pq, gacc, flag);
         head += 32;
+        if (found_overlap()) return;
       }
     }
   }
   __syncwarp();
   if (lane < (int)(tail - head)) pair_dense<PREC, false>(b, q[(head + lane) & (kQueue - 1)], bd, pq, gacc, flag);
   __syncwarp();
+  found_overlap();
 }
 
 // Fixed-order warp sums (lane 0 receives the total). The double-float form keeps the
@@ -403,7 +488,8 @@ __device__ __forceinline__ int guest_atoms(const BoxDev& b) {
   for (int c = b.nhost; c < b.ncomp; ++c) g += b.comp_size[c];
   return g;
 }
-__device__ __forceinline__ int work_tiles(const BoxDev& b) { return b.ntiles + (guest_atoms(b) + 31) / 32; }
+__device__ __forceinline__ int host_units(const BoxDev& b) { return b.vox ? b.vchunks : b.ntiles; }
+__device__ __forceinline__ int work_tiles(const BoxDev& b) { return host_units(b) + (guest_atoms(b) + 31) / 32; }
 
 // Work split of one bead pass. The flattened space of nb beads x nu work units (host
 // tiles, then guest atoms in groups of 32) is cut into `items` contiguous ranges of equal
@@ -440,15 +526,15 @@ constexpr int kMaxItems = 320;
 // [item0, item1) (all of them when item1 < 0) are taken dynamically by warps; the partial
 // of bead `bead` within item `item` lands in ipart[(item + bead)*4 + q] and
 // iflag[item + bead]. Caller syncs before reading them.
-template <int PREC>
-__device__ __noinline__ void block_bead_pass(const BoxDev& b, const Bead* beads, int nb, int component,
-                                                int newmol, int excl_comp, int excl_mol, int* qbuf,
-                                                double* ipart, int* iflag, int* counter, PassSplit sp,
-                                                int item0 = 0, int item1 = -1) {
+template <int PREC, bool VOX>
+__device__ __noinline__ void block_bead_pass_impl(const BoxDev& b, const Bead* beads, int nb, int component,
+                                                     int newmol, int excl_comp, int excl_mol, int* qbuf,
+                                                     double* ipart, int* iflag, int* counter, PassSplit sp,
+                                                     int item0, int item1, int chain, int* dead) {
   if (item1 < 0) item1 = (int)sp.items;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int* q = qbuf + warp * kQueue;
-  const int nt = b.ntiles;
+  const int nt = VOX ? b.vchunks : b.ntiles;
   const int ng = guest_atoms(b);
   if (sp.nu == 0) {  // nothing to interact with: zero partials, one item per bead slot
     for (int k = threadIdx.x; k < nb * 4; k += blockDim.x) ipart[k] = 0.0;
@@ -469,16 +555,38 @@ __device__ __noinline__ void block_bead_pass(const BoxDev& b, const Bead* beads,
       // only the ranges reaching past the host tiles touch guest atoms
       const int t0 = min(u0, nt), t1 = min(u1, nt);
       const int g0 = min(32 * max(u0 - nt, 0), ng), g1 = min(32 * max(u1 - nt, 0), ng);
-      const Bead bd = beads[bead];
+      // the bead is read from shared memory where it is used (fewer live registers around
+      // the inlined dense evaluations: no spills in either pass)
+      const Bead& bd = beads[bead];
       LaneAcc<PREC> hacc, gacc;
       int flag = 0;
-      warp_item<PREC>(b, bd, t0, t1, g0, g1, component, newmol, excl_comp, excl_mol, q, hacc, gacc, flag);
+      // trials of `chain` beads; dead[t] < 0: evaluated in full, else the early-exit flag
+      volatile int* dt = nullptr;
+      if (dead && dead[bead / chain] >= 0) dt = dead + bead / chain;
+      warp_item<PREC, VOX>(b, bd, t0, t1, g0, g1, component, newmol, excl_comp, excl_mol, q, hacc, gacc, flag, dt);
       const unsigned fm = __ballot_sync(kFull, flag != 0);
       warp_store<PREC>(hacc, gacc, ipart + (item + bead) * 4, df{bd.pq.x, bd.pq.y}, g1 > g0);
       if (lane == 0) iflag[item + bead] = fm ? 1 : 0;
       lo += (unsigned)(u1 - u0);
     }
   }
+}
+
+// The pass through voxel lists or through tiles: two instantiations, so each keeps its own
+// register allocation (the box decides, uniformly for the whole block).
+// dead: per trial of `chain` beads, 0 for early overlap rejection, -1 to evaluate the trial
+// in full (set by the caller before the pass; null: every trial in full).
+template <int PREC>
+__device__ __forceinline__ void block_bead_pass(const BoxDev& b, const Bead* beads, int nb, int component, int newmol,
+                                                int excl_comp, int excl_mol, int* qbuf, double* ipart, int* iflag,
+                                                int* counter, PassSplit sp, int item0 = 0, int item1 = -1,
+                                                int chain = 1, int* dead = nullptr) {
+  if (b.vox)
+    block_bead_pass_impl<PREC, true>(b, beads, nb, component, newmol, excl_comp, excl_mol, qbuf, ipart, iflag,
+                                     counter, sp, item0, item1, chain, dead);
+  else
+    block_bead_pass_impl<PREC, false>(b, beads, nb, component, newmol, excl_comp, excl_mol, qbuf, ipart, iflag,
+                                      counter, sp, item0, item1, chain, dead);
 }
 
 // ---------------------------------------------------------------- thread-block clusters

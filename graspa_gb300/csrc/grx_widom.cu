@@ -136,6 +136,7 @@ __global__ void __launch_bounds__(GRX_THREADS, 3) widom_kernel(BoxDev b, WidomAr
   __shared__ int counter;
   __shared__ double te[kMaxTrials * 4];
   __shared__ int tflag[kMaxTrials];
+  __shared__ int tdead[kMaxTrials];  // early overlap rejection flags of a pass's trials
   __shared__ double sbuf[32];
   __shared__ double newx[GRX_MAX_MOLSIZE], newy[GRX_MAX_MOLSIZE], newz[GRX_MAX_MOLSIZE], newq[GRX_MAX_MOLSIZE];
   __shared__ grx_widom_result res;
@@ -160,6 +161,7 @@ __global__ void __launch_bounds__(GRX_THREADS, 3) widom_kernel(BoxDev b, WidomAr
     }
     // 1. first-bead trials (mc_widom.h:133-139)
     const int nt = a.ntrials;
+    if (tid < nt) tdead[tid] = 0;
     if (tid < nt) {
       uint32_t r[4];
       draw4(a.seed, a.stream, move, SLOT_FIRST + tid, r);
@@ -170,7 +172,8 @@ __global__ void __launch_bounds__(GRX_THREADS, 3) widom_kernel(BoxDev b, WidomAr
     // 2. pair energies of the first-bead trials
     {
       const PassSplit sp = pass_split(b, nt, GRX_THREADS / 32, kWidomItemsPerWarp);
-      block_bead_pass<PREC>(b, beads, nt, a.comp, a.newmol, -1, -1, qbuf, ipart, iflag, &counter, sp);
+      block_bead_pass<PREC>(b, beads, nt, a.comp, a.newmol, -1, -1, qbuf, ipart, iflag, &counter, sp, 0, -1, 1,
+                            tdead);
       __syncthreads();
       reduce_items<PREC>(ipart, iflag, nt, 1, sp, te, tflag);
       __syncthreads();
@@ -208,10 +211,12 @@ __global__ void __launch_bounds__(GRX_THREADS, 3) widom_kernel(BoxDev b, WidomAr
                   b.meta[off + 1 + at].x, b.prefactor);
       }
       if (tid == 0) counter = 0;
+      if (tid < no) tdead[tid] = 0;
       __syncthreads();
       // 5. pair energies of the orientations
       const PassSplit sp = pass_split(b, nb, GRX_THREADS / 32, kWidomItemsPerWarp);
-      block_bead_pass<PREC>(b, beads, nb, a.comp, a.newmol, -1, -1, qbuf, ipart, iflag, &counter, sp);
+      block_bead_pass<PREC>(b, beads, nb, a.comp, a.newmol, -1, -1, qbuf, ipart, iflag, &counter, sp, 0, -1, chain,
+                            tdead);
       __syncthreads();
       reduce_items<PREC>(ipart, iflag, no, chain, sp, te, tflag);
       __syncthreads();

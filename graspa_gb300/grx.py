@@ -128,7 +128,7 @@ class JobResult(C.Structure):
                 ("t_submit", C.c_double), ("t_admit", C.c_double), ("t_done", C.c_double),
                 ("footprint_bytes", C.c_size_t), ("widom_n", C.c_int64), ("widom_mean_w", C.c_double),
                 ("widom_mean_w2", C.c_double), ("gcmc_steps", C.c_int64), ("ncomp_moved", C.c_int32),
-                ("pad_", C.c_int32), ("gcmc", GcmcStats * 4)]
+                ("pad_", C.c_int32), ("gcmc", GcmcStats * 4), ("widom_trial_configs", C.c_int64)]
 
 
 # every symbol include/grx.h declares
@@ -145,7 +145,7 @@ EXPORTS = [
     "grx_gcmc_batch_set_cluster", "grx_gcmc_batch_get_cluster", "grx_arena_create", "grx_arena_destroy",
     "grx_arena_usage", "grx_box_create_in", "grx_box_footprint", "grx_server_create", "grx_server_destroy",
     "grx_server_submit", "grx_server_progress", "grx_server_poll", "grx_server_time", "grx_server_launch_count",
-    "grx_box_create_replica",
+    "grx_box_create_replica", "grx_box_set_voxel_lists", "grx_box_get_voxel_lists",
 ]
 
 _lib = None
@@ -226,6 +226,8 @@ def load(path=LIB_PATH):
     L.grx_box_create_in.argtypes = [P(BoxDesc), C.c_void_p, P(C.c_void_p)]
     L.grx_box_footprint.argtypes = [P(BoxDesc), P(C.c_size_t)]
     L.grx_box_create_replica.argtypes = [C.c_void_p, P(C.c_void_p)]
+    L.grx_box_set_voxel_lists.argtypes = [C.c_void_p, C.c_int32]
+    L.grx_box_get_voxel_lists.argtypes = [C.c_void_p, P(C.c_int32), P(C.c_int32), P(C.c_int64)]
     L.grx_server_create.argtypes = [P(ServerConfig), C.c_void_p, P(C.c_void_p)]
     L.grx_server_destroy.argtypes = [C.c_void_p]
     L.grx_server_submit.argtypes = [C.c_void_p, P(JobDesc), P(C.c_uint64)]
@@ -305,10 +307,13 @@ def box_desc(system, capacity=None):
     d.geometry = geometry_from_system(system)
     ff = ForceField()
     ff.ntypes = nt
-    ff.use_1264 = 0
+    # 12-6-4 mode (UseLJ1264): epsilon / sigma / z / c10 hold C12 / C6 / C4 / C10 per type pair
+    ff.use_1264 = int(system.get("use_1264", 0))
     ff.epsilon, ff.sigma, ff.shift = _d(eps), _d(sig), _d(shift)
-    ff.z = _dp()
-    ff.c10 = _dp()
+    z = np.ascontiguousarray(system.get("z", np.zeros(nt * nt)), dtype=np.float64)
+    c10 = np.ascontiguousarray(system.get("c10", np.zeros(nt * nt)), dtype=np.float64)
+    ff.z = _d(z) if ff.use_1264 else _dp()
+    ff.c10 = _d(c10) if ff.use_1264 else _dp()
     ff.no_charges = int(system.get("no_charges", 0))
     ff.vdw_real_bias = int(system.get("vdw_real_bias", 1))
     ff.overlap_criteria = float(system.get("overlap_criteria", 1e6))
@@ -325,7 +330,7 @@ def box_desc(system, capacity=None):
         cap = capacity[c] if capacity is not None else max(n, ms)
         d.capacity[c] = max(cap, ms)
         d.molsize[c] = ms
-    return d, (eps, sig, shift)
+    return d, (eps, sig, shift, z, c10)
 
 
 def component_atoms(system, c):
@@ -564,6 +569,19 @@ class Box:
 
     def set_stream(self, stream_ptr):
         check(self.L.grx_box_set_stream(self.h, C.c_void_p(stream_ptr)), "grx_box_set_stream")
+
+    def set_voxel_lists(self, on):
+        """grx_box_set_voxel_lists: 1 builds the framework's voxel candidate lists (when they
+        fit), 0 frees them (the tile path)."""
+        check(self.L.grx_box_set_voxel_lists(self.h, int(on)), "grx_box_set_voxel_lists")
+
+    def voxel_lists(self):
+        """(on, voxels per axis, list entries) of grx_box_get_voxel_lists."""
+        on = C.c_int32()
+        dims = (C.c_int32 * 3)()
+        n = C.c_int64()
+        check(self.L.grx_box_get_voxel_lists(self.h, C.byref(on), dims, C.byref(n)), "grx_box_get_voxel_lists")
+        return bool(on.value), tuple(dims), int(n.value)
 
 
 class Arena:

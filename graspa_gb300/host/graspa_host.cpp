@@ -131,8 +131,8 @@ static grx_box* create_box(const Boxsize& B, const ForceField& FF, const Compone
   d.ncomponents = SC.NComponents.x;
   d.nhost_components = SC.NComponents.y;
   for (int c = 0; c < SC.NComponents.x; ++c) {
-    d.capacity[c] = SC.Allocate_size[c];
-    d.molsize[c] = SC.Moleculesize[c];
+    d.capacity[c] = std::max<size_t>(1, SC.Allocate_size[c]);  // a framework may have no atoms
+    d.molsize[c] = std::max<size_t>(1, SC.Moleculesize[c]);
   }
   grx_box* box = nullptr;
   check(grx_box_create(&d, &box), "grx_box_create");
@@ -346,6 +346,8 @@ static void pbc_host(const Boxsize& B, double3& v) {
   v = double3{C[0] * s[0] + C[3] * s[1] + C[6] * s[2], C[1] * s[0] + C[4] * s[1] + C[7] * s[2],
               C[2] * s[0] + C[5] * s[1] + C[8] * s[2]};
 }
+
+void Minimum_Image(const Boxsize& Box, double3& v) { pbc_host(Box, v); }
 
 // The box geometry with every length scaled by s (ScalePositions :71-84): kmax from the
 // precision factor tol1, or, with explicit k vectors (tol1 = 0), the same kmax and the
@@ -1435,6 +1437,60 @@ double WidomChemicalPotential(const Components& SC, size_t comp) {
   return -SC.Temperature * std::log(WidomAverageRosenbluth(SC, comp));
 }
 
+// Atoms of every pseudo-atom type in the box: framework atoms of the host mirrors plus the
+// molecules of each adsorbate component (its template types times the molecule count).
+static std::vector<double> type_counts(const Variables& Vars, size_t systemId, size_t extra_comp) {
+  const Components& SC = Vars.SystemComponents[systemId];
+  const Simulations& S = Vars.Sims[systemId];
+  std::vector<double> n(Vars.device_FF.size, 0.0);
+  for (int c = 0; c < SC.NComponents.x; ++c) {
+    const HostAtoms& H = S.host[c];
+    if (c < SC.NComponents.y) {
+      for (size_t i = 0; i < SC.Moleculesize[c] && i < H.Type.size(); ++i) n[H.Type[i]] += 1.0;
+    } else {
+      const double nm = (double)SC.NumberOfMolecule_for_Component[c] + ((size_t)c == extra_comp ? 1.0 : 0.0);
+      for (size_t a = 0; a < SC.Moleculesize[c] && a < H.Type.size(); ++a) n[H.Type[a]] += nm;
+    }
+  }
+  return n;
+}
+
+static double tail_energy(const Variables& Vars, size_t systemId, const std::vector<double>& n) {
+  const ForceField& FF = Vars.device_FF;
+  if (FF.tail.empty()) return 0.0;
+  const double V = Vars.Sims[systemId].Box.Volume;
+  const double rc = std::sqrt(FF.CutOffVDW), rc3 = rc * rc * rc, rc9 = rc3 * rc3 * rc3;
+  const double pi = 3.14159265358979323846;
+  double e = 0.0;
+  for (size_t i = 0; i < FF.size; ++i)
+    for (size_t j = 0; j < FF.size; ++j) {
+      const size_t k = i * FF.size + j;
+      if (!FF.tail[k] || n[i] == 0.0 || n[j] == 0.0) continue;
+      const double s3 = FF.sigma[k] * FF.sigma[k] * FF.sigma[k], s6 = s3 * s3;
+      e += 2.0 * pi * n[i] * n[j] / V * 4.0 * FF.epsilon[k] * (s6 * s6 / (9.0 * rc9) - s6 / (3.0 * rc3));
+    }
+  return e;
+}
+
+double TailCorrectionEnergy(const Variables& Vars, size_t systemId) {
+  return tail_energy(Vars, systemId, type_counts(Vars, systemId, (size_t)-1));
+}
+
+double TailCorrectionInsertion(const Variables& Vars, size_t systemId, size_t comp) {
+  return tail_energy(Vars, systemId, type_counts(Vars, systemId, comp)) -
+         tail_energy(Vars, systemId, type_counts(Vars, systemId, (size_t)-1));
+}
+
+double FrameworkDensity(const Components& SC, const Boxsize& Box) {
+  const double avogadro = 6.02214076e23;
+  return SC.FrameworkMass * 1.0e-3 / (avogadro * Box.Volume * 1.0e-30);
+}
+
+double WidomHenryCoefficient(const Components& SC, const Boxsize& Box, double AverageW) {
+  const double gas_constant = 8.314462618;  // J/mol/K
+  return AverageW / (gas_constant * SC.Temperature * FrameworkDensity(SC, Box));
+}
+
 // ------------------------------------------------------------------ device-resident moves
 static grx_gcmc_desc device_desc(Variables& Vars, size_t systemId, size_t comp) {
   Components& SC = Vars.SystemComponents[systemId];
@@ -1462,17 +1518,24 @@ static grx_gcmc_desc device_desc(Variables& Vars, size_t systemId, size_t comp) 
   return d;
 }
 
+std::vector<grx_gcmc_desc> Device_Move_Descs(Variables& Vars, size_t systemId, std::vector<size_t>* moved) {
+  Components& SC = Vars.SystemComponents[systemId];
+  std::vector<grx_gcmc_desc> descs;
+  if (moved) moved->clear();
+  for (int c = SC.NComponents.y; c < SC.NComponents.x; ++c)
+    if (SC.Moves[c].SwapProb > 1e-10) {  // cumulative: the total of this component's moves
+      descs.push_back(device_desc(Vars, systemId, (size_t)c));
+      if (moved) moved->push_back((size_t)c);
+    }
+  return descs;
+}
+
 std::vector<grx_gcmc_stats> RunMoves_Device_All(Variables& Vars, size_t systemId, int64_t nsteps,
                                                 std::vector<size_t>* moved) {
   Components& SC = Vars.SystemComponents[systemId];
   Simulations& Sims = Vars.Sims[systemId];
-  std::vector<grx_gcmc_desc> descs;
   std::vector<size_t> comps;
-  for (int c = SC.NComponents.y; c < SC.NComponents.x; ++c)
-    if (SC.Moves[c].SwapProb > 1e-10) {  // cumulative: the total of this component's moves
-      descs.push_back(device_desc(Vars, systemId, (size_t)c));
-      comps.push_back((size_t)c);
-    }
+  std::vector<grx_gcmc_desc> descs = Device_Move_Descs(Vars, systemId, &comps);
   if (descs.empty()) throw std::runtime_error("RunMoves_Device_All: no component has moves");
   std::vector<grx_gcmc_stats> st(descs.size());
   grx_box* b = Sims.Box.handle;

@@ -84,6 +84,7 @@ struct HostAtoms {  // owner of one Atoms' arrays
 
 struct ForceField {
   std::vector<double> epsilon, sigma, z, shift, C10;  // size*size, internal units
+  std::vector<int> tail;      // size*size: 1 where the pair has the LJ tail correction
   bool noCharges = false;
   bool VDWRealBias = true;
   bool Use1264 = false;
@@ -163,6 +164,8 @@ struct Components {
   std::vector<bool> rigid, hasPartialCharge;
   std::vector<double> ExclusionIntra, ExclusionAtom;
   std::vector<double> IdealRosenbluthWeight, FugacityCoeff, MolFraction;
+  std::vector<double> Tc, Pc, Accentric;             // critical constants of the molecule .def files
+  double FrameworkMass = 0.0;                        // g/mol of all framework atoms (loadings per kg)
   std::vector<double> TailCorrectionInsert;          // host-guest tail delta of one insertion
   std::vector<Move_Statistics> Moves;
   std::vector<RosenbluthWeight> Rosen_Widom;
@@ -279,6 +282,15 @@ MoveEnergy CBCF_LambdaChange(Variables& Vars, size_t systemId, size_t SelectedMo
                              int MoveType, bool& SuccessConstruction);
 // VDW_Coulomb.cu:1580 + Ewald_Energy_Functions.h:1272 (FP64 drift-check totals).
 MoveEnergy Total_Energy(Simulations& Sims);
+// The single-image rounding of PBC (maths.cuh:427-450) applied to a displacement in place.
+void Minimum_Image(const Boxsize& Box, double3& v);
+// LJ tail correction energy of the box (internal units): over the type pairs with the tail
+// on, 2 pi N_i N_j / V * 4 eps_ij (sigma_ij^12 / (9 rc^9) - sigma_ij^6 / (3 rc^3)), N_i the
+// atoms of type i in the box (framework and adsorbates), rc the VDW cutoff.
+double TailCorrectionEnergy(const Variables& Vars, size_t systemId);
+// The change of that energy when one molecule of component comp is inserted at the
+// current counts (the TailCorrectionDifference of an insertion).
+double TailCorrectionInsertion(const Variables& Vars, size_t systemId, size_t comp);
 // GetPrefactor (mc_utilities.h:315-351).
 double GetPrefactor(Components& SystemComponents, Simulations& Sims, size_t comp, int MoveType);
 
@@ -340,9 +352,18 @@ MoveEnergy RunMoves(Variables& Vars, size_t systemId, size_t comp);
 void RecordRosen(Components& SystemComponents, size_t comp, size_t block, double W);
 double WidomChemicalPotential(const Components& SystemComponents, size_t comp);   // mu_ex in K
 double WidomAverageRosenbluth(const Components& SystemComponents, size_t comp);
+// FrameworkDensity (print_statistics.cuh:75-98): framework mass over the box volume, kg/m^3.
+double FrameworkDensity(const Components& SystemComponents, const Boxsize& Box);
+// The Henry coefficient of ComputeFugacity (print_statistics.cuh:99-109) for a rigid
+// molecule: <W> / (R T rho_framework), mol/kg/Pa.
+double WidomHenryCoefficient(const Components& SystemComponents, const Boxsize& Box, double AverageW);
 
 // The same moves fully on the device: nsteps steps of grx_gcmc_run for one box.
 grx_gcmc_stats RunMoves_Device(Variables& Vars, size_t systemId, size_t comp, int64_t nsteps);
+
+// The device move set of every adsorbate component with a move probability, in component
+// order (the entries RunMoves_Device_All runs); `moved` receives the components.
+std::vector<grx_gcmc_desc> Device_Move_Descs(Variables& Vars, size_t systemId, std::vector<size_t>* moved);
 
 // Every adsorbate component with a move probability, picked uniformly per step
 // (Select_Box_Component_Molecule, axpy.cu:74-100): nsteps steps of grx_gcmc_run, one

@@ -71,7 +71,12 @@ SimulationInput read_simulation_input(const std::string& path) {
     }
     if (cur) {
       if (ieq(k, "IdealGasRosenbluthWeight")) { cur->IdealGasRosenbluthWeight = num(1); continue; }
-      if (ieq(k, "FugacityCoefficient")) { cur->FugacityCoefficient = num(1); continue; }
+      if (ieq(k, "FugacityCoefficient")) {  // a number, or PR-EOS (stored as -1, the reference's flag)
+        if (t.size() > 1 && ieq(t[1], "PR-EOS")) cur->FugacityCoefficient = -1.0;
+        else cur->FugacityCoefficient = num(1);
+        continue;
+      }
+      if (ieq(k, "IdentityChangeProbability")) { cur->IdentityChangeProbability = num(1); continue; }
       if (ieq(k, "MolFraction")) { cur->MolFraction = num(1); continue; }
       if (ieq(k, "TranslationProbability")) { cur->TranslationProbability = num(1); continue; }
       if (ieq(k, "RotationProbability")) { cur->RotationProbability = num(1); continue; }
@@ -90,6 +95,7 @@ SimulationInput read_simulation_input(const std::string& path) {
     else if (ieq(k, "UseMaxStep")) in.UseMaxStep = t.size() > 1 && yes(t[1]);
     else if (ieq(k, "MaxStepPerCycle")) in.MaxStepPerCycle = (size_t)num(1);
     else if (ieq(k, "UseChargesFromCIFFile")) in.UseChargesFromCIFFile = t.size() > 1 && yes(t[1]);
+    else if (ieq(k, "RestartFile")) in.RestartFile = t.size() > 1 && yes(t[1]);
     else if (ieq(k, "RandomSeed")) in.RandomSeed = (uint64_t)num(1);
     else if (ieq(k, "InputFileType")) in.InputFileType = t.size() > 1 ? t[1] : "cif";
     else if (ieq(k, "FrameworkName")) in.FrameworkName = t.size() > 1 ? t[1] : "";
@@ -156,6 +162,71 @@ MixingRules read_mixing_rules(const std::string& path) {
   return m;
 }
 
+// OverWriteFFTerms / the force_field.def reader (read_data.cpp:831-1000): a count of rule
+// overrides "A B shifted|truncated yes|no" (the last word switches the tail correction), a
+// count of explicit pairs "A B lennard-jones eps sigma", and a count of mixing overrides
+// (only 0 is supported). Comment lines start with '#'.
+PairOverrides read_force_field_overrides(const std::string& path) {
+  PairOverrides o;
+  std::vector<std::vector<std::string>> rows;
+  for (const std::string& l : lines_of(path)) {
+    const auto t = tokens(l);
+    if (t.empty() || t[0][0] == '#') continue;
+    rows.push_back(t);
+  }
+  size_t r = 0;
+  auto count = [&]() -> size_t {
+    if (r >= rows.size()) return 0;
+    return (size_t)std::stoul(rows[r++][0]);
+  };
+  const size_t nrules = count();
+  for (size_t k = 0; k < nrules && r < rows.size(); ++k, ++r) {
+    const auto& t = rows[r];
+    if (t.size() < 3) throw std::runtime_error("force_field.def: short rule: " + t[0]);
+    PairOverrides::Rule x;
+    x.a = t[0];
+    x.b = t[1];
+    x.shifted = ieq(t[2], "shifted");
+    x.tail = t.size() > 3 && yes(t[3]);
+    o.rules.push_back(x);
+  }
+  const size_t npairs = count();
+  for (size_t k = 0; k < npairs && r < rows.size(); ++k, ++r) {
+    const auto& t = rows[r];
+    if (t.size() < 5 || !ieq(t[2], "lennard-jones"))
+      throw std::runtime_error("force_field.def: only lennard-jones pairs are supported: " + t[0] + " " + t[1]);
+    o.pairs.push_back({t[0], t[1], std::stod(t[3]), std::stod(t[4])});
+  }
+  if (count() != 0) throw std::runtime_error("force_field.def: mixing-rule overrides are not supported");
+  return o;
+}
+
+std::vector<RestartComponent> read_restart(const std::string& path, size_t ncomponents) {
+  std::vector<RestartComponent> out(ncomponents);
+  int cur = -1;
+  for (const std::string& line : lines_of(path)) {
+    const auto t = tokens(line);
+    if (t.empty()) continue;
+    if (t[0] == "Component:" && t.size() >= 4 && t[2] == "Adsorbate") {
+      cur = std::stoi(t[1]);
+      if (cur < 0 || cur >= (int)ncomponents) throw std::runtime_error("restart file: unknown component " + t[1]);
+      out[cur].molecules = (size_t)std::stoul(t[3]);
+      continue;
+    }
+    if (cur < 0) continue;
+    RestartComponent& R = out[cur];
+    if (t[0] == "Adsorbate-atom-position:" && t.size() >= 6) {
+      R.molid.push_back((size_t)std::stoul(t[1]));
+      R.pos.push_back(double3{std::stod(t[3]), std::stod(t[4]), std::stod(t[5])});
+    } else if (t[0] == "Adsorbate-atom-charge:" && t.size() >= 4) {
+      R.charge.push_back(std::stod(t[3]));
+    } else if (t[0] == "Adsorbate-atom-scaling:" && t.size() >= 4) {
+      R.lambda.push_back(std::stod(t[3]));
+    }
+  }
+  return out;
+}
+
 // MoleculeDefinitionParser (read_data.cpp:2044-2140): line 1 Tc, 2 Pc, 3 acentric factor,
 // 5 atom count, 9 rigid, positions from line 13 (index name x y z).
 MoleculeDefinition read_molecule_def(const std::string& path) {
@@ -172,9 +243,12 @@ MoleculeDefinition read_molecule_def(const std::string& path) {
     else if (i == 9) {
       if (!ieq(t[0], "rigid")) throw std::runtime_error(path + ": only rigid molecules are supported");
     } else if (i >= 13 && d.names.size() < n) {
-      if (t.size() < 5) throw std::runtime_error(path + ": short position line: " + L[i]);
+      // "index name x y z"; a position line without coordinates puts the atom at the origin
+      // (single-atom molecules such as Kr.def of the XeKr example)
+      if (t.size() < 2 || (t.size() > 2 && t.size() < 5))
+        throw std::runtime_error(path + ": short position line: " + L[i]);
       d.names.push_back(t[1]);
-      d.pos.push_back(double3{std::stod(t[2]), std::stod(t[3]), std::stod(t[4])});
+      d.pos.push_back(t.size() >= 5 ? double3{std::stod(t[2]), std::stod(t[3]), std::stod(t[4])} : double3{0.0, 0.0, 0.0});
     }
   }
   if (d.names.size() != n || n == 0) throw std::runtime_error(path + ": atom positions missing");
@@ -242,6 +316,7 @@ FrameworkData read_cif(const std::string& path, const PseudoAtomTable& pa, const
     if (ty < 0) throw std::runtime_error(path + ": atom label [" + name + "] not defined");
     fpos.push_back(double3{std::stod(t[col_x]), std::stod(t[col_y]), std::stod(t[col_z])});
     type.push_back((size_t)ty);
+    F.mass += pa.mass[ty] * (double)(uc[0] * uc[1] * uc[2]);
     q.push_back(charges_from_cif && col_q >= 0 ? std::stod(t[col_q]) : pa.charge[ty]);
   }
   const double sx = 1.0 / uc[0], sy = 1.0 / uc[1], sz = 1.0 / uc[2];
@@ -256,6 +331,62 @@ FrameworkData read_cif(const std::string& path, const PseudoAtomTable& pa, const
           F.charge.push_back(q[k]);
         }
   return F;
+}
+
+std::vector<double> PengRobinsonFugacity(const std::vector<double>& Tc, const std::vector<double>& Pc,
+                                         const std::vector<double>& w, const std::vector<double>& x, double T,
+                                         double P) {
+  const size_t n = Tc.size();
+  double xs = 0.0;
+  for (double v : x) xs += v;
+  if (std::fabs(xs - 1.0) > 1e-4) throw std::runtime_error("PR-EOS: mole fractions do not sum to 1");
+  // per-component attraction and co-volume in reduced form: A_i = a_i P / (R T)^2, B_i = b_i P / (R T)
+  // (R cancels), a_i = 0.45724 alpha_i (R Tc_i)^2 / Pc_i, b_i = 0.07780 R Tc_i / Pc_i
+  std::vector<double> A(n), B(n);
+  for (size_t i = 0; i < n; ++i) {
+    const double kappa = 0.37464 + 1.54226 * w[i] - 0.26992 * w[i] * w[i];
+    const double sq = 1.0 + kappa * (1.0 - std::sqrt(T / Tc[i]));
+    const double alpha = sq * sq;
+    A[i] = 0.45724 * alpha * (Tc[i] / T) * (Tc[i] / T) * P / Pc[i];
+    B[i] = 0.07780 * (Tc[i] / T) * P / Pc[i];
+  }
+  double Am = 0.0, Bm = 0.0;
+  for (size_t i = 0; i < n; ++i) {
+    Bm += x[i] * B[i];
+    for (size_t j = 0; j < n; ++j) Am += x[i] * x[j] * std::sqrt(A[i] * A[j]);
+  }
+  // Z^3 + c2 Z^2 + c1 Z + c0 = 0, solved by the depressed cubic t^3 + p t + q (Z = t - c2/3)
+  const double c2 = Bm - 1.0, c1 = Am - 3.0 * Bm * Bm - 2.0 * Bm, c0 = -(Am * Bm - Bm * Bm - Bm * Bm * Bm);
+  const double p = c1 - c2 * c2 / 3.0, q = 2.0 * c2 * c2 * c2 / 27.0 - c2 * c1 / 3.0 + c0;
+  const double disc = q * q / 4.0 + p * p * p / 27.0;
+  std::vector<double> Z;
+  if (disc > 0.0) {
+    const double sd = std::sqrt(disc);
+    Z.push_back(std::cbrt(-q / 2.0 + sd) + std::cbrt(-q / 2.0 - sd) - c2 / 3.0);
+  } else {
+    const double r = std::sqrt(-p / 3.0);
+    const double cphi = r > 0.0 ? std::max(-1.0, std::min(1.0, -q / (2.0 * r * r * r))) : 0.0;
+    const double phi = std::acos(cphi), pi = 3.14159265358979323846;
+    for (int k = 0; k < 3; ++k) Z.push_back(2.0 * r * std::cos((phi + 2.0 * pi * k) / 3.0) - c2 / 3.0);
+    std::sort(Z.begin(), Z.end(), [](double a, double b) { return a > b; });
+  }
+  auto phi_of = [&](size_t i, double z) {
+    double sa = 0.0;
+    for (size_t k = 0; k < n; ++k) sa += 2.0 * x[k] * std::sqrt(A[i] * A[k]);
+    const double r2 = std::sqrt(2.0);
+    return std::exp(B[i] / Bm * (z - 1.0) - std::log(z - Bm) -
+                    Am / (2.0 * r2 * Bm) * (sa / Am - B[i] / Bm) * std::log((z + (1.0 + r2) * Bm) / (z + (1.0 - r2) * Bm)));
+  };
+  std::vector<double> out(n);
+  for (size_t i = 0; i < n; ++i) {
+    if (Z.size() == 1 || Z[2] <= 0.0) {
+      out[i] = phi_of(i, Z[0]);
+    } else {  // vapour-like and liquid-like roots: the smaller coefficient (the stable phase)
+      const double f0 = phi_of(i, Z[0]), f2 = phi_of(i, Z[2]);
+      out[i] = f2 < f0 ? f2 : f0;
+    }
+  }
+  return out;
 }
 
 void Setup_Box_Geometry(Boxsize& B, const SimulationInput& in) {
@@ -329,6 +460,34 @@ void Setup_From_Directory(Variables& V, const std::string& dir, SimulationInput&
         FF.shift[i * nt + j] = 4.0 * ep * (rri3 * (rri3 - 1.0));
       }
     }
+  // force_field.def: per-pair shifted / truncated and tail rules, explicit pairs
+  FF.tail.assign(nt * nt, mr.tail ? 1 : 0);
+  {
+    std::ifstream probe(d + "force_field.def");
+    if (probe) {
+      const PairOverrides ov = read_force_field_overrides(d + "force_field.def");
+      auto apply = [&](const std::string& a, const std::string& b, auto&& f) {
+        const int i = pa.index(a), j = pa.index(b);
+        if (i < 0 || j < 0) return;  // a pseudo atom the system does not use
+        f((size_t)i * nt + (size_t)j);
+        f((size_t)j * nt + (size_t)i);
+      };
+      for (const auto& p : ov.pairs)
+        apply(p.a, p.b, [&](size_t k) {
+          FF.epsilon[k] = p.eps / 1.20272430057;
+          FF.sigma[k] = p.sigma;
+        });
+      for (const auto& x : ov.rules)
+        apply(x.a, x.b, [&](size_t k) {
+          FF.tail[k] = x.tail ? 1 : 0;
+          FF.shift[k] = 0.0;
+          if (x.shifted && FF.sigma[k] > 0.0) {
+            const double tt = rc2 / (FF.sigma[k] * FF.sigma[k]), rri3 = 1.0 / (tt * tt * tt);
+            FF.shift[k] = 4.0 * FF.epsilon[k] * (rri3 * (rri3 - 1.0));
+          }
+        });
+    }
+  }
   FF.CutOffVDW = rc2;
   FF.CutOffCoul = in.CutOffCoulomb * in.CutOffCoulomb;
   FF.OverlapCriteria = in.OverlapCriteria;
@@ -341,7 +500,7 @@ void Setup_From_Directory(Variables& V, const std::string& dir, SimulationInput&
     fw = read_cif(d + in.FrameworkName + ".cif", pa, in.UnitCells, in.UseChargesFromCIFFile);
     std::copy(fw.cell, fw.cell + 9, S.Box.Cell);
   } else {
-    throw std::runtime_error("an example without a CIF framework needs a restart file (not supported)");
+    throw std::runtime_error("an example needs a CIF framework (it defines the box, possibly without atoms)");
   }
   Setup_Box_Geometry(S.Box, in);
   // components: 0 framework, then the adsorbates
@@ -365,9 +524,9 @@ void Setup_From_Directory(Variables& V, const std::string& dir, SimulationInput&
   S.d_a.assign(nc, Atoms());
   n_stored.assign(nc, 0);
   SC.Moleculesize[0] = fw.pos.size();
-  SC.Allocate_size[0] = fw.pos.size();
+  SC.Allocate_size[0] = std::max<size_t>(1, fw.pos.size());  // a CIF may only define the box
   SC.rigid[0] = false;
-  S.host[0].allocate(fw.pos.size());
+  S.host[0].allocate(SC.Allocate_size[0]);
   for (size_t i = 0; i < fw.pos.size(); ++i) {
     S.host[0].pos[i] = fw.pos[i];
     S.host[0].charge[i] = FF.noCharges ? 0.0 : fw.charge[i];
@@ -376,6 +535,9 @@ void Setup_From_Directory(Variables& V, const std::string& dir, SimulationInput&
   }
   S.d_a[0] = S.host[0].view(fw.pos.size(), fw.pos.size());
   n_stored[0] = fw.pos.size();
+  std::vector<RestartComponent> restart;
+  if (in.RestartFile) restart = read_restart(d + "RestartInitial/System_0/restartfile", (size_t)nads);
+  size_t first_molid = 0;  // molecule ids of the file count through the components
   for (int k = 0; k < nads; ++k) {
     const InputComponent& ic = in.Components[k];
     const int c = 1 + k;
@@ -390,6 +552,7 @@ void Setup_From_Directory(Variables& V, const std::string& dir, SimulationInput&
     M.TranslationProb = ic.TranslationProbability;
     M.RotationProb = ms > 1 ? ic.RotationProbability : 0.0;
     M.ReinsertionProb = ic.ReinsertionProbability;
+    M.IdentitySwapProb = ic.IdentityChangeProbability;
     M.SwapProb = ic.SwapProbability;
     M.NormalizeProbabilities();
     M.NumberOfTrials = in.NumberOfTrialPositions;
@@ -398,18 +561,72 @@ void Setup_From_Directory(Variables& V, const std::string& dir, SimulationInput&
     const double r30 = 30.0 / (180 / 3.1415);
     M.MaxRotation = double3{r30, r30, r30};
     HostAtoms& H = S.host[c];
+    const RestartComponent* R = restart.empty() ? nullptr : &restart[k];
+    const size_t nmol = R ? R->molecules : 0;
+    if (nmol * ms > SC.Allocate_size[c]) SC.Allocate_size[c] = nmol * ms;
     H.allocate(SC.Allocate_size[c]);
+    std::vector<size_t> types(ms);
     for (size_t a = 0; a < ms; ++a) {  // the empty component stores its template
       const int ty = pa.index(md.names[a]);
       if (ty < 0) throw std::runtime_error(ic.MoleculeName + ".def: atom [" + md.names[a] + "] not in pseudo_atoms.def");
+      types[a] = (size_t)ty;
       H.pos[a] = md.pos[a];
       H.charge[a] = FF.noCharges ? 0.0 : pa.charge[ty];
       H.Type[a] = (size_t)ty;
       H.MolID[a] = 0;
     }
-    S.d_a[c] = H.view(ms, 0);
-    n_stored[c] = ms;
+    if (nmol > 0) {
+      // RestartFileParser (read_data.cpp:3085-3200): molecule ids relative to the component,
+      // every atom brought to the image nearest the molecule's first atom, charges from the file
+      if (R->pos.size() != nmol * ms) throw std::runtime_error("restart file: component " + std::to_string(k) +
+                                                              " has the wrong number of atom positions");
+      for (double l : R->lambda)
+        if (l < 1.0) throw std::runtime_error("restart file: fractional molecules (lambda < 1) are not supported");
+      for (size_t m = 0; m < nmol; ++m)
+        for (size_t a = 0; a < ms; ++a) {
+          const size_t i = m * ms + a;
+          double3 p = R->pos[i];
+          if (a > 0) {
+            double3 dv{p.x - H.pos[m * ms].x, p.y - H.pos[m * ms].y, p.z - H.pos[m * ms].z};
+            Minimum_Image(S.Box, dv);
+            p = double3{H.pos[m * ms].x + dv.x, H.pos[m * ms].y + dv.y, H.pos[m * ms].z + dv.z};
+          }
+          H.pos[i] = p;
+          H.charge[i] = FF.noCharges ? 0.0 : (R->charge.size() == R->pos.size() ? R->charge[i] : pa.charge[types[a]]);
+          H.Type[i] = types[a];
+          H.MolID[i] = R->molid[i] - first_molid;
+        }
+      first_molid += nmol;
+      SC.NumberOfMolecule_for_Component[c] = nmol;
+    }
+    S.d_a[c] = H.view(ms, nmol * ms);
+    n_stored[c] = std::max(ms, nmol * ms);
   }
+  // FugacityCoefficient PR-EOS on any adsorbate: all coefficients from the Peng-Robinson
+  // mixture (equations_of_state.h:130-143)
+  bool need_eos = false;
+  for (const InputComponent& ic : in.Components) need_eos |= ic.FugacityCoefficient < 0.0;
+  SC.Tc.assign(nc, 0.0);
+  SC.Pc.assign(nc, 0.0);
+  SC.Accentric.assign(nc, 0.0);
+  for (int k = 0; k < nads; ++k) {
+    const MoleculeDefinition md = read_molecule_def(d + in.Components[k].MoleculeName + ".def");
+    SC.Tc[1 + k] = md.Tc;
+    SC.Pc[1 + k] = md.Pc;
+    SC.Accentric[1 + k] = md.w;
+  }
+  if (need_eos && nads > 0) {
+    std::vector<double> tc, pc, w, x;
+    for (int k = 0; k < nads; ++k) {
+      tc.push_back(SC.Tc[1 + k]);
+      pc.push_back(SC.Pc[1 + k]);
+      w.push_back(SC.Accentric[1 + k]);
+      x.push_back(in.Components[k].MolFraction);
+    }
+    const std::vector<double> phi = PengRobinsonFugacity(tc, pc, w, x, in.Temperature, in.Pressure);
+    for (int k = 0; k < nads; ++k) SC.FugacityCoeff[1 + k] = phi[k];
+  }
+  SC.FrameworkMass = fw.mass;
   V.Widom[0].NumberWidomTrials = in.NumberOfTrialPositions;
   V.Widom[0].NumberWidomTrialsOrientations = in.NumberOfTrialOrientations;
   V.Random.Seed = in.RandomSeed;

@@ -69,13 +69,9 @@ def summarize(out):
 
 
 def trial_energies_of(J, r):
-    """Trial-energy evaluations a finished job performed (first-bead trials plus
-    orientation trials per CBMC growth; 2 configurations per translation / rotation)."""
-    kind, wd, gd = job_work(J)
-    ms = int(J["system"]["molsize"][1])
-    per_growth = 10 + (10 if ms > 1 else 0)
-    if kind == grx.JOB_WIDOM:
-        return J["widom_insertions"] * per_growth
-    st = r.gcmc[0]
-    a = list(st.attempts)
-    return 2 * (a[0] + a[1]) + per_growth * (a[2] + a[3]) + 2 * per_growth * a[4]
+    """Trial-energy evaluations a finished job performed, as the device counted them:
+    first-bead positions, orientations of the growths whose first bead succeeded, and the
+    2 configurations of a translation / rotation."""
+    if r.kind == grx.JOB_WIDOM:
+        return int(r.widom_trial_configs)
+    return sum(int(r.gcmc[k].trial_configs) for k in range(max(1, r.ncomp_moved)))

@@ -206,6 +206,18 @@ grx_status grx_box_destroy(grx_box* box);   /* refused while the box has live re
  * counterpart in the reference (one box per simulation). */
 grx_status grx_box_create_replica(grx_box* parent, grx_box** out);
 
+/* Voxel candidate lists of the framework (host) atoms: the cell is cut into voxels of
+ * about 1.5-4 A and each voxel lists every host atom within the screening radius of any
+ * point of the voxel, with its periodic image, the atoms inside the cutoff for the whole
+ * voxel first. The pair engine then walks a bead's voxel list instead of culling the
+ * framework's 32-atom tiles (the cutoff tests stay exact, so results change only in the
+ * summation order). Built by default when the lists fit 32 MB and the cell is wider than
+ * twice the list radius; mode 0 frees them (tile path), mode 1 rebuilds them. Refused on
+ * a box with replicas (they share the lists). No counterpart in the reference (it tests
+ * every framework atom per trial). get: on (0/1), voxels per axis, list entries. */
+grx_status grx_box_set_voxel_lists(grx_box* box, int32_t mode);
+grx_status grx_box_get_voxel_lists(grx_box* box, int32_t* on, int32_t* dims, int64_t* entries);
+
 /* ---- device memory arena -------------------------------------------------- */
 /* One reserved region of device memory that boxes are carved from by a host-side
  * first-fit allocator (256-byte granules). A box created in an arena takes every
@@ -219,8 +231,10 @@ grx_status grx_arena_create(size_t bytes, grx_arena** out);
 grx_status grx_arena_destroy(grx_arena* arena);      /* every box in it destroyed first */
 grx_status grx_arena_usage(grx_arena* arena, size_t* in_use, size_t* largest_free, size_t* peak);
 grx_status grx_box_create_in(const grx_box_desc* desc, grx_arena* arena, grx_box** out);
-/* Upper estimate of the device bytes a box of this description takes, including its
- * first scratch and Widom result buffers. */
+/* Upper estimate of the device bytes a box of this description needs, including its
+ * first scratch and Widom result buffers. The framework's voxel candidate lists (up to
+ * 32 MB, grx_box_set_voxel_lists) come on top when the arena or device has room for
+ * them; without room the box keeps the tile path, so this is the admission minimum. */
 grx_status grx_box_footprint(const grx_box_desc* desc, size_t* bytes);
 /* All later work of the box goes to this stream (cudaStream_t, NULL = default). */
 grx_status grx_box_set_stream(grx_box* box, void* cuda_stream);
@@ -519,6 +533,8 @@ typedef struct {
   int32_t ncomp_moved;
   int32_t pad_;
   grx_gcmc_stats gcmc[4];
+  int64_t widom_trial_configs;  /* Widom: trial configurations evaluated (first-bead positions, plus
+                                   the orientations of insertions whose first bead was grown) */
 } grx_job_result;
 
 typedef struct grx_server grx_server;

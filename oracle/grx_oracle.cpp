@@ -632,6 +632,16 @@ static inline double u01(uint32_t w) { return (double)w * 2.3283064365386963e-10
 
 // SelectTrialPosition, mc_widom.h:14-39: shift by the largest log-weight, cumulative
 // search against u * sum (guarded against running past the end).
+// Smallest decision margin of the moves since the last reset (test diagnostics): for a
+// trial selection the distance of u * sum from the nearest cumulative boundary relative to
+// the sum, for an acceptance |ln u - ln Pacc|; both are the relative change of the weights
+// (about beta |dE|) that would flip the decision.
+static thread_local double g_margin = 1e300;
+static void note_margin(double m) { g_margin = std::min(g_margin, std::fabs(m)); }
+static void note_acceptance(double u, double pacc) {
+  if (u > 0.0 && pacc > 0.0) note_margin(std::log(u) - std::log(pacc));
+}
+
 int64_t ora_select_trial(const double* logw, int64_t n, double u) {
   if (n <= 0) return -1;
   double mx = logw[0];
@@ -643,6 +653,11 @@ int64_t ora_select_trial(const double* logw, int64_t n, double u) {
   double cumw = w[0];
   const double ws = u * sum;
   while (cumw < ws && sel + 1 < n) cumw += w[++sel];
+  if (n > 1) {
+    double m = (cumw - ws) / sum;
+    if (sel > 0) m = std::min(m, (ws - (cumw - w[sel])) / sum);
+    note_margin(m);
+  }
   return sel;
 }
 
@@ -1041,6 +1056,7 @@ extern "C" void ora_gcmc_run_mix(const ora_box* box, const ora_ff* ff, double* p
   const uint64_t seed = gk[0].seed;
   const uint32_t stream = gk[0].stream;
   for (int64_t step = 0; step < nsteps; ++step) {
+    g_margin = 1e300;
     const uint64_t move = first_step + (uint64_t)step;
     uint32_t w[4], w2[4];
     ora_draw(seed, stream, move, 4096u, w);
@@ -1108,6 +1124,7 @@ extern "C" void ora_gcmc_run_mix(const ora_box* box, const ora_ff* ff, double* p
           }
           const double tot = e6[0] + e6[1] + e6[2] + e6[3] + e6[4] + e6[5] + ew;
           const double pacc = std::exp(-g->beta * tot);
+          note_acceptance(uacc, pacc);
           if (uacc < pacc) {
             st->accepted[kind]++;
             for (int64_t k = 0; k < 3 * ms; ++k) S.pos[3 * m0 + k] = newp[k];
@@ -1145,6 +1162,7 @@ extern "C" void ora_gcmc_run_mix(const ora_box* box, const ora_ff* ff, double* p
             rosen *= std::exp(-g->beta * ew);
           }
           const double pacc = rosen / gr.rosen;
+          note_acceptance(uacc, pacc);
           if (uacc < pacc) {
             st->accepted[4]++;
             for (int64_t k = 0; k < 3 * ms; ++k) S.pos[3 * m0 + k] = gi.pos[k];
@@ -1181,6 +1199,7 @@ extern "C" void ora_gcmc_run_mix(const ora_box* box, const ora_ff* ff, double* p
         rosen_rec = rosen;
         const double pre = g->beta * bigP / (1.0 + (double)N);  // GetPrefactor INSERTION
         const double pacc = pre * rosen / g->ideal_rosenbluth;
+        note_acceptance(uacc, pacc);
         if (rosen > 1e-150 && uacc < pacc) {
           st->accepted[2]++;
           const int64_t at0 = S.comp_start[comp + 1];
@@ -1231,6 +1250,7 @@ extern "C" void ora_gcmc_run_mix(const ora_box* box, const ora_ff* ff, double* p
         rosen /= std::exp(-g->beta * -g->tail_insert);
         const double pre = (double)N / (g->beta * bigP);  // GetPrefactor DELETION
         const double pacc = pre * g->ideal_rosenbluth / rosen;
+        note_acceptance(uacc, pacc);
         if (uacc < pacc) {
           st->accepted[3]++;
           const int64_t last = a0 + (N - 1) * ms;
@@ -1261,6 +1281,7 @@ extern "C" void ora_gcmc_run_mix(const ora_box* box, const ora_ff* ff, double* p
     for (int64_t k = 0; k < ng; ++k) {
       const int64_t ck = gk[k].component;
       stk[k].sum_n += (double)((S.comp_start[ck + 1] - S.comp_start[ck]) / molsize[ck]);
+      stk[k].last_margin = g_margin;
     }
   }
   // write the state back (component regions from comp_off)

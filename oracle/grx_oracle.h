@@ -209,6 +209,8 @@ typedef struct {
   int64_t trial_configs;  /* trial configurations evaluated (first beads, orientations grown after
                              a successful first bead, 2 per translation / rotation) */
   int64_t trial_beads;    /* their beads */
+  double last_margin;     /* smallest decision margin of the last step (trial selections and
+                             acceptance; relative weight change that flips it); test diagnostics */
 } ora_gcmc_stats;
 
 /* Runs nsteps moves on one box. atoms/s_ads are updated in place (guest component

@@ -71,7 +71,7 @@ class OraGcmc(C.Structure):
 class OraGcmcStats(C.Structure):
     _fields_ = [("attempts", C.c_int64 * 5), ("accepted", C.c_int64 * 5), ("n_molecules", C.c_int64),
                 ("energy", C.c_double * 4), ("sum_n", C.c_double), ("rosen", C.c_double * 3),
-                ("trial_configs", C.c_int64), ("trial_beads", C.c_int64)]
+                ("trial_configs", C.c_int64), ("trial_beads", C.c_int64), ("last_margin", C.c_double)]
 
 
 def build(force=False):
@@ -159,11 +159,13 @@ class OracleSystem:
         self.sig = np.ascontiguousarray(system["sigma"], dtype=np.float64)
         self.shift = np.ascontiguousarray(system["shift"], dtype=np.float64)
         self.zero = np.zeros(nt * nt)
+        self.z = np.ascontiguousarray(system.get("z", self.zero), dtype=np.float64)
+        self.c10 = np.ascontiguousarray(system.get("c10", self.zero), dtype=np.float64)
         ff = OraFF()
         ff.ntypes = nt
         ff.epsilon, ff.sigma, ff.shift = _d(self.eps), _d(self.sig), _d(self.shift)
-        ff.z, ff.c10 = _d(self.zero), _d(self.zero)
-        ff.use_1264 = 0
+        ff.z, ff.c10 = _d(self.z), _d(self.c10)
+        ff.use_1264 = int(system.get("use_1264", 0))
         ff.no_charges = int(system.get("no_charges", 0))
         ff.vdw_real_bias = int(system.get("vdw_real_bias", 1))
         ff.overlap_criteria = system.get("overlap_criteria", 1e6)

@@ -52,3 +52,31 @@ def test_co2_mfi_short_run(prec):
     acc = sum(int(x) for x in re.findall(r"(\d+)/\d+", out.split("moves:")[1].split("\n")[0])[::1])
     bound = 1e-7 if prec == "fp64" else 1e-6 * (acc + 1)
     assert beta * abs(drift) <= bound, (drift, acc)
+
+
+NIST = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "nist_spce")
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4])
+def test_nist_spce_box_end_to_end(n):
+    """Examples/Reference_NIST_SPCE/Box-n from the reference's own files (restart file with
+    the SPC/E molecules, atom-less CIF cell, O-O tail correction) through graspa_run: the
+    device FP64 totals reproduce the values Box-n/output.txt printed (5 decimals)."""
+    B.build()
+    r = subprocess.run([B.RUNNER, os.path.join(NIST, f"Box-{n}"), "--max-cycles", "0", "--precision", "fp64"],
+                       capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr
+    out = r.stdout
+    e = json.load(open(os.path.join(NIST, "expected.json")))["boxes"][f"Box-{n}"]
+
+    def close(x, ref):
+        return abs(x - ref) <= 1e-5 + 1e-12 * abs(ref)
+
+    m = re.search(r"Total HHVDW \S+ HHReal \S+ HGVDW \S+ HGReal \S+ GGVDW (\S+) GGReal (\S+) HHEwald \S+ HGEwald \S+ "
+                  r"GGEwald (\S+)", out)
+    assert close(float(m.group(1)), e["gg_vdw"]) and close(float(m.group(2)), e["gg_real"])
+    assert close(float(m.group(3)), e["gg_ewald"])
+    assert close(float(re.search(r"Fourier GG (\S+)", out).group(1)), e["fourier_gg"])
+    assert close(float(re.search(r"SelfAtomE all (\S+)", out).group(1)), e["self_atoms"])
+    assert close(abs(float(re.search(r"IntraExclusionE all (\S+)", out).group(1))), e["intra_exclusion"])
+    assert close(float(re.search(r"TailE (\S+)", out).group(1)), e["tail"])

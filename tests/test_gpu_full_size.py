@@ -7,7 +7,11 @@
     results to 2e-6.
   - GCMC, 456 chains (three per SM, replicas of one framework) for 200 steps: at least 95 %
     of the chains take the same decisions in mixed as in FP64, and sampled chains take the
-    FP64 oracle's decisions exactly.
+    FP64 oracle's decisions exactly. Every chain whose mixed and FP64 runs part is replayed
+    step by step to its first divergent step; the FP64 oracle, continuing the same chain,
+    shows that step's closest decision (a trial selection or an acceptance) within 1e-6 of
+    a tie in relative weight (about beta |dE|): the runs part only where a 1e-6 perturbation
+    may flip a decision.
 """
 import numpy as np
 import pytest
@@ -63,3 +67,46 @@ def test_gcmc_full_size_chains(grx_lib):
         ost, _, _ = S.gcmc(ora_params(descs[k]), [nfw, 3 * 160], 0, 200)
         assert list(res["fp64"][k].accepted) == list(ost.accepted)
         assert res["fp64"][k].n_molecules == ost.n_molecules
+    # the divergent chains: first divergent step, and the oracle's decision margin there
+    div = [k for k in range(R) if not same[k]]
+    if not div:
+        return
+    runs = {}
+    for name, p in (("fp64", grx_lib.GRX_FP64), ("mixed", grx_lib.GRX_MIXED)):
+        parent = grx_lib.Box(s, capacity=[nfw, 3 * 160])
+        parent.ewald_total()
+        runs[name] = [parent] + [parent.replica() for _ in range(len(div) - 1)]
+    sub = [descs[k] for k in div]
+    first_div = {}
+    acc = {n: [np.zeros(5, dtype=np.int64) for _ in div] for n in runs}
+    for step in range(200):
+        st = {n: grx_lib.gcmc_run(runs[n], sub, step, 1, p)
+              for n, p in (("fp64", grx_lib.GRX_FP64), ("mixed", grx_lib.GRX_MIXED))}
+        for j, k in enumerate(div):
+            if k in first_div:
+                continue
+            for n in runs:
+                acc[n][j] += np.array(st[n][j].accepted)
+            nf, nm = st["fp64"][j].n_molecules, st["mixed"][j].n_molecules
+            diff = not np.array_equal(acc["fp64"][j], acc["mixed"][j]) or nf != nm
+            if not diff and nf > 0:
+                pf = runs["fp64"][j].positions(1, 3 * nf)
+                pm = runs["mixed"][j].positions(1, 3 * nm)
+                diff = np.max(np.abs(pf - pm)) > 1e-6
+            if diff:
+                first_div[k] = step
+        if len(first_div) == len(div):
+            break
+    for n in runs:
+        for b in reversed(runs[n]):
+            b.close()
+    report = []
+    for k in div:
+        step = first_div[k]
+        ch = O.OracleChain(S, ora_params(descs[k]), [nfw, 3 * 160])
+        if step > 0:
+            ch.run(0, step)
+        last = ch.run(step, 1)[0]
+        report.append((k, step, last.last_margin))
+    print("divergent chains (chain, first divergent step, oracle decision margin):", report)
+    assert all(m <= 1e-6 for _, _, m in report), report

@@ -314,3 +314,35 @@ def test_identity_swaps_on_clusters(grx_lib, cl):
     assert a[0].identity_in[1] + a[1].identity_in[1] >= 2
     for x, y in zip(pa, pb):
         assert x.shape == y.shape and np.max(np.abs(x - y), initial=0.0) <= 1e-9
+
+
+def test_gcmc_vdw_real_bias_off_matches_oracle(grx_lib):
+    """VDWRealBias = false in the device GCMC kernel: the oracle's decisions in FP64."""
+    s = dict(co2_system(n_co2=5))
+    s["vdw_real_bias"] = 0
+    d = params(grx_lib, pressure_pa=1e6)
+    box, st, ost, after = run_pair(grx_lib, s, d, 400, grx_lib.GRX_FP64)
+    assert list(st.attempts) == list(ost.attempts)
+    assert list(st.accepted) == list(ost.accepted)
+    assert st.n_molecules == ost.n_molecules
+    assert abs(st.energy[3] - ost.energy[3]) <= 1e-9 * max(1.0, abs(ost.energy[3]))
+
+
+def test_gcmc_counts_and_rosenbluth_match_oracle(grx_lib):
+    """The kernel's own work and Widom counters: trial configurations evaluated, their
+    beads, and the Rosenbluth sums of the insertion attempts (RecordRosen) equal the
+    oracle's over the same chain, in FP64; the mixed chain's weights agree to 1e-6."""
+    s = co2_system(n_co2=5)
+    d = params(grx_lib, pressure_pa=1e6)
+    box, st, ost, after = run_pair(grx_lib, s, d, 400, grx_lib.GRX_FP64)
+    assert st.trial_configs == ost.trial_configs and st.trial_beads == ost.trial_beads
+    assert st.rosen[2] == ost.rosen[2] == st.attempts[2]
+    assert abs(st.rosen[0] - ost.rosen[0]) <= 1e-10 * max(1e-300, ost.rosen[0])
+    assert abs(st.rosen[1] - ost.rosen[1]) <= 1e-10 * max(1e-300, ost.rosen[1])
+    # orientations are grown only after a successful first bead: fewer than 20 per growth
+    assert st.trial_configs < 2 * (st.attempts[0] + st.attempts[1]) + 20 * (st.attempts[2] + st.attempts[3]) + \
+        41 * st.attempts[4]
+    box_m = make_box(grx_lib, s)
+    sm = grx_lib.gcmc_run([box_m], [d], 0, 400, grx_lib.GRX_MIXED)[0]
+    if list(sm.accepted) == list(st.accepted):
+        assert abs(sm.rosen[0] - st.rosen[0]) <= 1e-6 * st.rosen[0]

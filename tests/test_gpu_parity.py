@@ -18,6 +18,8 @@ from tests.systems import co2_system, nist_system
 pytestmark = pytest.mark.gpu
 
 BETA300 = None
+# Mixed bars are asserted per energy component (host-guest and guest-guest VDW and real
+# Coulomb separately), so errors of opposite sign in two components cannot cancel.
 
 
 def beta(T=300.0):
@@ -116,7 +118,8 @@ def test_trial_energies_co2(grx_lib, n_co2, chain):
         em, fm = box.trial_energies(pos, q, ty, newmol, ntr, chain, 1, prec=grx_lib.GRX_MIXED)
         assert np.array_equal(fm, rflag)
         ok = rflag == 0
-        assert mixed_close(em[ok].sum(1), ref[ok].sum(1)), np.max(np.abs(em - ref))
+        # every component (host-guest / guest-guest x VDW / real Coulomb) on its own
+        assert mixed_close(em[ok], ref[ok]), np.max(np.abs(em[ok] - ref[ok]))
         e32, f32 = box.trial_energies(pos, q, ty, newmol, ntr, chain, 1, prec=grx_lib.GRX_FP32)
         assert np.all(np.abs(e32[ok] - ref[ok]) <= 1e-2 * np.maximum(np.abs(ref[ok]), 1.0 / beta()))
 
@@ -152,7 +155,7 @@ def test_trial_energies_triclinic_water(grx_lib):
     em, fm = box.trial_energies(pos, q, ty, 400, 16, 1, 1, prec=grx_lib.GRX_MIXED)
     ok = rf == 0
     assert np.array_equal(fm, rf)
-    assert mixed_close(em[ok].sum(1), ref[ok].sum(1))
+    assert mixed_close(em[ok], ref[ok])
 
 
 # ---------------------------------------------------------------- single body
@@ -191,7 +194,7 @@ def test_single_body_translation(grx_lib):
                                 ctypes.byref(tn), 1, 1, 1, O._d(ref), rf.ctypes.data_as(O._u8p))
         assert flag == rf[0]
         gm, _ = box.single_body(old, new, 1, prec=grx_lib.GRX_MIXED)
-        assert mixed_close(gm.sum(), ref.sum())
+        assert np.all(beta() * np.abs(gm - ref) <= 1e-6), gm - ref   # per component
 
 
 # ---------------------------------------------------------------- Ewald delta
@@ -352,3 +355,70 @@ def test_widom_edge_cases(grx_lib):
     assert np.all(np.abs(got["rosenbluth"] - R) <= 1e-10 * np.maximum(R, 1e-300))
     # zero insertions is a no-op
     assert len(box3.widom(grx_lib.widom_desc(s3, 1, 1, 1), 0, 0)) == 0
+
+
+# ---------------------------------------------------------------- 12-6-4 and VDWRealBias off
+def lj1264_system(n_co2=6, seed=17):
+    """The CO2/silica system in the 12-6-4 form of VDW (maths.cuh:454-475): per type pair
+    C12 = 4 eps sigma^12 and C6 = 4 eps sigma^6 of the LJ pair plus a seeded C4 and C10."""
+    s = dict(co2_system(n_co2=n_co2))
+    eps, sig = np.asarray(s["epsilon"]), np.asarray(s["sigma"])
+    rng = np.random.default_rng(seed)
+    nt = int(s["ntypes"])
+    c4 = rng.uniform(-2000.0, 0.0, nt * nt)   # +C4 / r^4: negative C4 attracts (ion-induced dipole)
+    c10 = rng.uniform(0.0, 2e5, nt * nt) * (rng.uniform(0, 1, nt * nt) < 0.5)
+    c4 = 0.5 * (c4.reshape(nt, nt) + c4.reshape(nt, nt).T).reshape(-1)
+    c10 = 0.5 * (c10.reshape(nt, nt) + c10.reshape(nt, nt).T).reshape(-1)
+    s.update(use_1264=1, epsilon=4.0 * eps * sig ** 12, sigma=4.0 * eps * sig ** 6, z=c4, c10=c10,
+             shift=np.zeros(nt * nt))
+    return s
+
+
+@pytest.mark.parametrize("chain", [1, 2])
+def test_trial_energies_1264(grx_lib, chain):
+    s = lj1264_system()
+    n_co2 = 6
+    box = grx_lib.Box(s, capacity=[len(s["pos"]) - 3 * n_co2, 3 * 64])
+    S = O.OracleSystem(s)
+    rng = np.random.default_rng(32)   # a stream whose chain trials are not all in the framework walls
+    ntr = 48
+    pos, q, ty = _random_beads(s, 1, ntr, chain, rng)
+    ref, rflag = S.trial_energies(pos, np.ones(len(q)), q, np.ones(len(q)), ty, n_co2, ntr, chain, 1)
+    e64, f64 = box.trial_energies(pos, q, ty, n_co2, ntr, chain, 1, prec=grx_lib.GRX_FP64)
+    assert np.array_equal(f64, rflag)
+    assert fp64_close(e64, ref), np.max(np.abs(e64 - ref))
+    em, fm = box.trial_energies(pos, q, ty, n_co2, ntr, chain, 1, prec=grx_lib.GRX_MIXED)
+    ok = rflag == 0
+    assert ok.sum() > 0 and np.array_equal(fm, rflag)
+    assert mixed_close(em[ok], ref[ok]), np.max(np.abs(em[ok] - ref[ok]))
+    # the 12-6-4 terms change the energies (the test is not a plain LJ one)
+    lj, _ = grx_lib.Box(co2_system(n_co2=n_co2), capacity=[len(s["pos"]) - 3 * n_co2, 3 * 64]).trial_energies(
+        pos, q, ty, n_co2, ntr, chain, 1, prec=grx_lib.GRX_FP64)
+    assert np.max(np.abs(lj[ok, 0] - e64[ok, 0])) > 1.0 and np.max(np.abs(lj[ok, 2] - e64[ok, 2])) > 1e-3
+
+
+def test_widom_vdw_real_bias_off(grx_lib):
+    """VDWRealBias = false: trials are selected on the VDW energy alone and the chosen
+    trial's real-space Coulomb weight multiplies the step weight (mc_widom.h:368-369)."""
+    s = dict(co2_system(n_co2=0))
+    s["vdw_real_bias"] = 0
+    nfw = s["comp_start"][1]
+    box = grx_lib.Box(s, capacity=[nfw, 3 * 32])
+    box.ewald_total()
+    n = 300
+    ref, _ = oracle_widom(s, 1, n)
+    R, sf, so, ok, E = _fields(ref)
+    d = grx_lib.widom_desc(s, 1, 10, 10, seed=42)
+    got = box.widom(d, 0, n, prec=grx_lib.GRX_FP64)
+    assert np.array_equal(got["success"], ok) and np.array_equal(got["sel_first"], sf)
+    assert np.array_equal(got["sel_orient"], so)
+    assert np.all(np.abs(got["rosenbluth"] - R) <= 1e-10 * np.maximum(R, 1e-300))
+    # the selection differs from the biased one on this stream
+    s_b = co2_system(n_co2=0)
+    ref_b, _ = oracle_widom(s_b, 1, n)
+    assert not np.array_equal(_fields(ref_b)[1], sf)
+    mixed = box.widom(d, 0, n, prec=grx_lib.GRX_MIXED)
+    same = (mixed["sel_first"] == sf) & (mixed["sel_orient"] == so) & (mixed["success"] == ok)
+    assert same.mean() >= 0.99
+    r = same & (R > 0)
+    assert np.max(np.abs(mixed["rosenbluth"][r] - R[r]) / R[r]) <= 2e-6

@@ -85,13 +85,17 @@ def test_admission_by_footprint_and_slots(grx_lib):
     big.close()
     fpa = [done[i].footprint_bytes for i in range(len(jobs))]
     assert all(f > 0 for f in fpa)
-    # memory-bound residency
-    budget = int(2.5 * max(fpa))
+    # memory-bound residency: room for every job alone, not for all of them at once. Budgets
+    # come from the admission minimum (grx_box_footprint: without the voxel candidate lists,
+    # which a GCMC box adds only when the arena has room for them)
+    fmin = [grx_lib.box_footprint(J["system"], J["capacity"]) for J in jobs]
+    budget = max(int(1.2 * max(fmin)), int(0.5 * sum(fmin)))
     srv = grx_lib.Server(budget, max_resident=8, prec=grx_lib.GRX_MIXED, widom_slice=32, gcmc_slice=50)
     most, done = drive(srv, jobs)
     srv.close()
     assert len(done) == len(jobs) and all(r.status == 0 for r in done.values())
-    assert 1 <= most <= budget // min(fpa) and most < len(jobs)
+    held = [done[i].footprint_bytes for i in range(len(jobs))]
+    assert 1 <= most <= budget // min(held) and most < len(jobs)
     # slot-bound residency
     srv = grx_lib.Server(1 << 30, max_resident=3, prec=grx_lib.GRX_MIXED, widom_slice=32, gcmc_slice=50)
     most, done = drive(srv, jobs)
