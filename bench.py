@@ -436,7 +436,9 @@ def bench_serving(args, grx):
 
     def stream(arrivals):
         srv = grx.Server(args.serve_hbm_gb * (1 << 30), max_resident=args.serve_slots, prec=grx.GRX_MIXED,
-                         widom_slice=0, gcmc_slice=args.serve_gcmc_slice, cluster_atoms=args.serve_cluster_atoms)
+                         widom_slice=0, gcmc_slice=args.serve_gcmc_slice,
+                         cluster_atoms=0 if args.serve_batching else args.serve_cluster_atoms,
+                         gcmc_batching=args.serve_batching)
         out = serving.run_stream(srv, jobs, arrivals, timeout=1800.0)
         srv.close()
         summ = serving.summarize(out)
@@ -475,6 +477,7 @@ def bench_serving(args, grx):
     te64 = sum(serving.trial_energies_of(sub[i], r) for i, (r, _) in out64.items())
     plain_te = te64 / dt
     return {"jobs": n, "slots": args.serve_slots, "gcmc_cycles": args.serve_gcmc_cycles,
+            "gcmc_batching": args.serve_batching, "gcmc_slice": args.serve_gcmc_slice,
             "gcmc_steps_per_job": args.serve_gcmc_cycles * 20, "widom_insertions": 5000,
             "cluster_atoms": args.serve_cluster_atoms, "species": "CH4 CO2 N2 Xe Kr uniform",
             "framework_atoms": "200-20000 log-uniform", "job_generation_s": t_gen,
@@ -840,10 +843,13 @@ def main():
     ap.add_argument("--serve-jobs", type=int, default=1000, help="jobs per stream (the full configs[4] sweep: 10000)")
     ap.add_argument("--serve-rate-fractions", type=float, nargs="*", default=[0.5, 0.8, 1.2],
                     help="Poisson arrival rates swept, as fractions of the measured saturation rate")
-    ap.add_argument("--serve-slots", type=int, default=152)
+    ap.add_argument("--serve-slots", type=int, default=512)
+    ap.add_argument("--serve-batching", type=int, default=1,
+                    help="1: resident GCMC jobs advance together in shared rounds (grx_server gcmc_batching)")
     ap.add_argument("--serve-hbm-gb", type=float, default=16.0)
     ap.add_argument("--serve-gcmc-cycles", type=int, default=2000, help="GCMC cycles of 20 steps per serving job")
-    ap.add_argument("--serve-gcmc-slice", type=int, default=2000)
+    ap.add_argument("--serve-gcmc-slice", type=int, default=800,
+                    help="steps per launch (batching: per round, for a job of 1000 pair evaluations per step)")
     ap.add_argument("--serve-fp64-jobs", type=int, default=24)
     ap.add_argument("--serve-fp64-cycles", type=int, default=50, help="GCMC cycles of the plain FP64 sample's jobs")
     ap.add_argument("--serve-cluster-atoms", type=int, default=1000,

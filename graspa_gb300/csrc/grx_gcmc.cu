@@ -73,6 +73,7 @@ struct grx_gcmc_batch {
   int graph_nlaunch = 0;
   cudaStream_t graph_stream = nullptr;
   cudaStream_t last_stream = nullptr;  // stream of the latest launch
+  std::vector<GcmcArgs> h_args;        // host copy of the move sets (per-box step windows)
 };
 
 namespace grx {
@@ -145,6 +146,8 @@ static grx_status prepare_gcmc(grx_box* const* boxes, int32_t nboxes, const grx_
       a.bias = b->dev.vdw_real_bias;
       a.excl = b->excl_intra[d.component] + b->excl_self[d.component];
       a.big_p = d.mol_fraction * d.pressure * d.fugacity_coeff * b->dev.volume;
+      a.step_off = 0;
+      a.nsteps_cap = -1;
       ha.push_back(a);
       size_t need = (size_t)(b->dev.kmax[0] + b->dev.kmax[1] + b->dev.kmax[2] + 3) * 2 * ms *
                     (sizeof(double2) + sizeof(float4));
@@ -343,6 +346,7 @@ extern "C" grx_status grx_gcmc_batch_create(grx_box* const* boxes, int32_t nboxe
   grx_status st = prepare_gcmc(boxes, nboxes, descs, ncomp_moved, hb, ha, B->first, B->smem, B->chunk_mult);
   if (st) { delete B; return st; }
   B->nentries = B->first[nboxes];
+  B->h_args = ha;
   B->nwarps = default_warps(nboxes);
   B->boxes.assign(boxes, boxes + nboxes);
   B->descs.assign(descs, descs + B->nentries);
@@ -413,6 +417,27 @@ extern "C" grx_status grx_gcmc_batch_set_step(grx_gcmc_batch* B, uint64_t step) 
   GRX_CHECK_CUDA(cudaMemcpyAsync(B->d_step, &step, sizeof(uint64_t), cudaMemcpyHostToDevice, B->stream),
                  "set step");
   GRX_CHECK_CUDA(cudaStreamSynchronize(B->stream), "set step");
+  return GRX_OK;
+}
+
+extern "C" grx_status grx_gcmc_batch_set_box_steps(grx_gcmc_batch* B, const uint64_t* next_move,
+                                                   const int64_t* nsteps) {
+  GRX_REQUIRE(B && next_move, "grx_gcmc_batch_set_box_steps: bad argument");
+  GRX_CHECK_CUDA(cudaStreamSynchronize(B->stream), "set box steps");
+  if (B->last_stream) GRX_CHECK_CUDA(cudaStreamSynchronize(B->last_stream), "set box steps");
+  uint64_t counter = 0;  // the launch counter the next launch starts from
+  GRX_CHECK_CUDA(cudaMemcpy(&counter, B->d_step, sizeof(uint64_t), cudaMemcpyDeviceToHost), "read step counter");
+  const int nb = (int)B->boxes.size();
+  for (int i = 0; i < nb; ++i) {
+    GRX_REQUIRE(!nsteps || nsteps[i] >= 0, "grx_gcmc_batch_set_box_steps: negative step count");
+    for (int e = B->first[i]; e < B->first[i + 1]; ++e) {
+      B->h_args[e].step_off = (int64_t)(next_move[i] - counter);  // modulo 2^64
+      B->h_args[e].nsteps_cap = nsteps ? nsteps[i] : -1;
+    }
+  }
+  GRX_CHECK_CUDA(cudaMemcpy(B->d_args, B->h_args.data(), B->nentries * sizeof(GcmcArgs), cudaMemcpyHostToDevice),
+                 "upload box steps");
+  drop_graph(B);
   return GRX_OK;
 }
 

@@ -34,6 +34,10 @@ struct GcmcArgs {
   int pad_;
   double excl;  // ExclusionIntra + ExclusionAtom of the component
   double big_p; // MolFraction * Pressure * FugacityCoefficient * Volume
+  // per box (the same in all its entries): Philox move index of step s of a launch =
+  // launch counter + s + step_off; steps taken = min(launch steps, nsteps_cap) (cap < 0: all)
+  int64_t step_off;
+  int64_t nsteps_cap;
 };
 
 // RotationAroundAxis (mc_utilities.h:459-481) for a coordinate axis.
@@ -275,8 +279,10 @@ __global__ void __launch_bounds__(NW * 32, 24 / NW) gcmc_kernel(const BoxDev* bo
   }
   __syncthreads();
   int* comp_size = const_cast<int*>(b.comp_size);
-  for (int64_t step = 0; step < nsteps; ++step) {
-    const uint64_t move = first_step + (uint64_t)step;
+  const int64_t nsb = (A[0].nsteps_cap >= 0 && A[0].nsteps_cap < nsteps) ? A[0].nsteps_cap : nsteps;
+  const uint64_t move0 = first_step + (uint64_t)A[0].step_off;
+  for (int64_t step = 0; step < nsb; ++step) {
+    const uint64_t move = move0 + (uint64_t)step;
     uint32_t w[4], w2[4], ws[4];
     draw4(A[0].d.seed, A[0].d.stream, move, SLOT_MOVE, w);
     draw4(A[0].d.seed, A[0].d.stream, move, SLOT_DISP, w2);

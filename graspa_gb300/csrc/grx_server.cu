@@ -11,7 +11,16 @@
 // A job's arithmetic is independent of the other resident jobs: it sees only its own
 // box, and its Philox stream is fixed by its own seed, so its result is the same alone
 // and in any mix.
+//
+// With gcmc_batching, GCMC jobs are not launched one by one: every round advances all
+// resident GCMC jobs in one persistent launch of 8 warps per job (three jobs per SM, the
+// shape of the batched benchmark), each job drawing from its own move stream and taking a
+// number of steps set by its estimated cost per step, so that the jobs of a round end at
+// about the same time. Jobs are admitted and retired between rounds; the round's batch is
+// rebuilt when its membership changes. Widom jobs keep their own launches and streams.
+#include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <deque>
 #include <mutex>
 #include <vector>
@@ -44,6 +53,11 @@ struct ServerJob {
   size_t footprint = 0;
   double t_submit = 0, t_admit = 0, t_done = 0;
   grx_status status = GRX_OK;
+  // batched GCMC rounds
+  std::vector<grx_gcmc_stats> acc;  // statistics summed over the rounds, one per move set
+  int64_t tick_n = 0;               // steps of the round in flight
+  bool in_tick = false;
+  double cost = 1.0;                // estimated pair evaluations per step
 };
 
 }  // namespace grx
@@ -62,6 +76,12 @@ struct grx_server {
   uint64_t next_id = 1;
   uint64_t launches = 0;
   std::mutex m;
+  // batched GCMC rounds (cfg.gcmc_batching)
+  grx_gcmc_batch* tick = nullptr;
+  std::vector<ServerJob*> tick_jobs;  // the batch's boxes, in order
+  bool tick_inflight = false;
+  cudaEvent_t tick_ev = nullptr;
+  cudaStream_t tick_stream = nullptr;
   double now() const {
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   }
@@ -117,7 +137,23 @@ grx_status admit_job(grx_server* S, ServerJob* j) {
     st = grx_ewald_total(j->box, out8);
   }
   if (st == GRX_OK) st = grx_box_set_stream(j->box, j->stream);
-  if (st == GRX_OK && j->kind == GRX_JOB_GCMC) {
+  if (st == GRX_OK && j->kind == GRX_JOB_GCMC && S->cfg.gcmc_batching) {
+    // cost per step in pair evaluations: the moved molecule's beads against the framework
+    // atoms within the cutoff (at most all of them) and the guests, plus the Fourier
+    // delta's k-vector updates of a charged molecule (weighted as 0.2 pair each)
+    const grx_box* b = j->box;
+    const int nh = (int)b->off[b->nhost];
+    const double rc = std::sqrt(std::max(b->dev.cut_vdw2, b->dev.no_charges ? 0.0 : b->dev.cut_coul2));
+    const double near = std::min((double)nh, 1.5 * nh / std::fabs(b->dev.volume) * 4.18879 * rc * rc * rc);
+    double c = 0.0;
+    for (const grx_gcmc_desc& d : j->gcmc) {
+      const double ms = (double)b->molsize[d.component];
+      c += ms * (near + 20.0);
+      if (!b->dev.no_charges && b->has_charge[d.component]) c += 0.2 * b->nact * ms;
+    }
+    j->cost = std::max(1.0, c / (double)j->gcmc.size());
+    j->acc.assign(j->gcmc.size(), grx_gcmc_stats{});
+  } else if (st == GRX_OK && j->kind == GRX_JOB_GCMC) {
     const int32_t nm = (int32_t)j->gcmc.size();
     st = grx_gcmc_batch_create(&j->box, 1, j->gcmc.data(), &nm, S->cfg.precision, &j->batch);
     if (st == GRX_OK && S->cfg.cluster_atoms > 0) {  // a large box spans several SMs
@@ -196,13 +232,124 @@ grx_status collect(grx_server* S, ServerJob* j, grx_job_result& r) {
     r.widom_mean_w2 = j->total ? s2 / (double)j->total : 0.0;
   } else if (j->status == GRX_OK) {
     std::vector<grx_gcmc_stats> st(j->gcmc.size());
-    grx_status e = grx_gcmc_batch_stats(j->batch, st.data(), nullptr);
-    if (e) return e;
+    if (j->batch) {
+      grx_status e = grx_gcmc_batch_stats(j->batch, st.data(), nullptr);
+      if (e) return e;
+    } else {
+      st = j->acc;
+    }
     r.ncomp_moved = (int32_t)st.size();
     for (size_t k = 0; k < st.size() && k < 4; ++k) r.gcmc[k] = st[k];
     r.gcmc_steps = j->total;
   }
   r.t_done = S->now();
+  return GRX_OK;
+}
+
+void add_stats(grx_gcmc_stats& a, const grx_gcmc_stats& b) {
+  for (int k = 0; k < 5; ++k) {
+    a.attempts[k] += b.attempts[k];
+    a.accepted[k] += b.accepted[k];
+  }
+  a.n_molecules = b.n_molecules;
+  a.capacity_hits += b.capacity_hits;
+  for (int k = 0; k < 4; ++k) a.energy[k] += b.energy[k];
+  a.sum_n += b.sum_n;
+  for (int k = 0; k < 2; ++k) {
+    a.identity_out[k] += b.identity_out[k];
+    a.identity_in[k] += b.identity_in[k];
+  }
+  for (int k = 0; k < 3; ++k) a.rosen[k] += b.rosen[k];
+  a.trial_configs += b.trial_configs;
+  a.trial_beads += b.trial_beads;
+}
+
+// Ends the GCMC round in flight once its event completed: each member's statistics and steps.
+grx_status finish_tick(grx_server* S) {
+  if (!S->tick_inflight) return GRX_OK;
+  const cudaError_t e = cudaEventQuery(S->tick_ev);
+  if (e == cudaErrorNotReady) return GRX_OK;
+  S->tick_inflight = false;
+  grx_status st = e == cudaSuccess ? GRX_OK : cuda_status(e, "gcmc round");
+  std::vector<grx_gcmc_stats> v;
+  if (!st) {
+    size_t ne = 0;
+    for (ServerJob* j : S->tick_jobs) ne += j->gcmc.size();
+    v.resize(ne);
+    st = grx_gcmc_batch_stats(S->tick, v.data(), nullptr);
+    if (!st) st = grx_gcmc_batch_reset_stats(S->tick);
+  }
+  size_t e0 = 0;
+  for (ServerJob* j : S->tick_jobs) {
+    if (st) j->status = st;
+    else
+      for (size_t k = 0; k < j->gcmc.size(); ++k) add_stats(j->acc[k], v[e0 + k]);
+    e0 += j->gcmc.size();
+    if (j->in_tick) {
+      j->issued += j->tick_n;
+      j->tick_n = 0;
+      j->in_tick = false;
+    }
+  }
+  return GRX_OK;
+}
+
+// Starts the next GCMC round over every resident GCMC job with steps left (the batch is
+// rebuilt when the members changed). A job of estimated cost c pair evaluations per step
+// takes gcmc_slice * 1000 / c steps, so the members of a round end at about the same time.
+grx_status start_tick(grx_server* S) {
+  if (S->tick_inflight) return GRX_OK;
+  std::vector<ServerJob*> members;
+  for (ServerJob* j : S->resident)
+    if (j->kind == GRX_JOB_GCMC && j->status == GRX_OK && j->issued < j->total) members.push_back(j);
+  if (members.empty()) return GRX_OK;
+  if (!S->tick || members != S->tick_jobs) {
+    if (S->tick) grx_gcmc_batch_destroy(S->tick);
+    S->tick = nullptr;
+    S->tick_jobs.clear();
+    std::vector<grx_box*> boxes;
+    std::vector<grx_gcmc_desc> descs;
+    std::vector<int32_t> nm;
+    for (ServerJob* j : members) {
+      boxes.push_back(j->box);
+      descs.insert(descs.end(), j->gcmc.begin(), j->gcmc.end());
+      nm.push_back((int32_t)j->gcmc.size());
+    }
+    grx_status st = grx_gcmc_batch_create(boxes.data(), (int32_t)boxes.size(), descs.data(), nm.data(),
+                                          S->cfg.precision, &S->tick);
+    if (st == GRX_ERR_OUT_OF_MEMORY) {  // no room for the round's descriptors now: the next round retries
+      cudaGetLastError();
+      S->tick = nullptr;
+      return GRX_OK;
+    }
+    if (st) return st;
+    // one shape for every round (the same arithmetic alone and in any mix)
+    st = grx_gcmc_batch_set_shape(S->tick, 8, 1);
+    if (st) return st;
+    for (ServerJob* j : members) GRX_CHECK_CUDA(cudaStreamSynchronize(j->stream), "gcmc round set-up");
+    S->tick_jobs = members;
+  }
+  std::vector<uint64_t> next(members.size());
+  std::vector<int64_t> n(members.size());
+  int64_t nmax = 0;
+  for (size_t i = 0; i < members.size(); ++i) {
+    ServerJob* j = members[i];
+    const double want = (double)S->cfg.gcmc_slice * 1000.0 / j->cost;
+    n[i] = std::max<int64_t>(1, std::min<int64_t>(j->total - j->issued, (int64_t)std::llround(want)));
+    next[i] = (uint64_t)j->issued;
+    nmax = std::max(nmax, n[i]);
+  }
+  grx_status st = grx_gcmc_batch_set_box_steps(S->tick, next.data(), n.data());
+  if (st) return st;
+  st = grx_gcmc_batch_launch(S->tick, nmax, S->tick_stream);
+  if (st) return st;
+  GRX_CHECK_CUDA(cudaEventRecord(S->tick_ev, S->tick_stream), "gcmc round event");
+  for (size_t i = 0; i < members.size(); ++i) {
+    members[i]->tick_n = n[i];
+    members[i]->in_tick = true;
+  }
+  S->tick_inflight = true;
+  S->launches++;
   return GRX_OK;
 }
 
@@ -227,6 +374,16 @@ extern "C" grx_status grx_server_create(const grx_server_config* cfg, grx_arena*
     }
     S->own_arena = true;
   }
+  if (S->cfg.gcmc_batching) {
+    if (cudaStreamCreateWithFlags(&S->tick_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&S->tick_ev, cudaEventDisableTiming) != cudaSuccess) {
+      const cudaError_t e = cudaGetLastError();
+      if (S->tick_stream) cudaStreamDestroy(S->tick_stream);
+      if (S->own_arena) grx_arena_destroy(S->arena);
+      delete S;
+      return cuda_status(e, "grx_server_create: round stream");
+    }
+  }
   S->t0 = std::chrono::steady_clock::now();
   *out = S;
   return GRX_OK;
@@ -234,6 +391,9 @@ extern "C" grx_status grx_server_create(const grx_server_config* cfg, grx_arena*
 
 extern "C" grx_status grx_server_destroy(grx_server* S) {
   if (!S) return GRX_OK;
+  if (S->tick_stream) cudaStreamSynchronize(S->tick_stream);
+  if (S->tick) grx_gcmc_batch_destroy(S->tick);
+  S->tick = nullptr;
   for (ServerJob* j : S->resident) {
     if (j->stream) cudaStreamSynchronize(j->stream);
     release_job(S, j);
@@ -241,6 +401,8 @@ extern "C" grx_status grx_server_destroy(grx_server* S) {
   }
   for (ServerJob* j : S->pending) delete j;
   for (cudaStream_t s : S->streams) cudaStreamDestroy(s);
+  if (S->tick_ev) cudaEventDestroy(S->tick_ev);
+  if (S->tick_stream) cudaStreamDestroy(S->tick_stream);
   if (S->own_arena) grx_arena_destroy(S->arena);
   delete S;
   return GRX_OK;
@@ -307,22 +469,34 @@ extern "C" grx_status grx_server_submit(grx_server* S, const grx_job_desc* jd, u
 extern "C" grx_status grx_server_progress(grx_server* S, int32_t* n_resident, int32_t* n_pending) {
   GRX_REQUIRE(S, "grx_server_progress: null server");
   std::lock_guard<std::mutex> g(S->m);
+  if (S->cfg.gcmc_batching) {
+    grx_status st = finish_tick(S);
+    if (st) return st;
+  }
   // retire / advance resident jobs
   for (size_t i = 0; i < S->resident.size();) {
     ServerJob* j = S->resident[i];
-    if (j->inflight) {
+    if (j->kind == GRX_JOB_GCMC && S->cfg.gcmc_batching) {  // advanced by the rounds
+      if (j->in_tick || (j->status == GRX_OK && j->issued < j->total)) { ++i; continue; }
+    } else if (j->inflight) {
       const cudaError_t e = cudaEventQuery(j->ev);
       if (e == cudaErrorNotReady) { ++i; continue; }
       j->inflight = false;
       if (e != cudaSuccess) j->status = cuda_status(e, "job slice");
     }
-    if (j->status == GRX_OK && j->issued < j->total) {
+    if (j->status == GRX_OK && j->issued < j->total && !(j->kind == GRX_JOB_GCMC && S->cfg.gcmc_batching)) {
       j->status = launch_slice(S, j);
       if (j->status == GRX_OK) { ++i; continue; }
     }
     grx_job_result r;
     grx_status st = collect(S, j, r);
     if (st && r.status == GRX_OK) r.status = st;
+    if (std::find(S->tick_jobs.begin(), S->tick_jobs.end(), j) != S->tick_jobs.end()) {
+      // the (idle) round batch holds this job's box: drop it before the box goes
+      grx_gcmc_batch_destroy(S->tick);
+      S->tick = nullptr;
+      S->tick_jobs.clear();
+    }
     release_job(S, j);
     S->done.push_back(r);
     delete j;
@@ -349,7 +523,11 @@ extern "C" grx_status grx_server_progress(grx_server* S, int32_t* n_resident, in
     }
     j->t_admit = S->now();
     S->resident.push_back(j);
-    j->status = j->total > 0 ? launch_slice(S, j) : GRX_OK;
+    if (!(j->kind == GRX_JOB_GCMC && S->cfg.gcmc_batching)) j->status = j->total > 0 ? launch_slice(S, j) : GRX_OK;
+  }
+  if (S->cfg.gcmc_batching) {
+    grx_status st = start_tick(S);
+    if (st) return st;
   }
   if (n_resident) *n_resident = (int32_t)S->resident.size();
   if (n_pending) *n_pending = (int32_t)S->pending.size();

@@ -113,7 +113,8 @@ GCMC_TUNE_CANDIDATES = 9  # GRX_GCMC_TUNE_CANDIDATES: warps per box 8/12/24 x it
 
 class ServerConfig(C.Structure):
     _fields_ = [("hbm_budget_bytes", C.c_size_t), ("max_resident", C.c_int32), ("precision", C.c_int32),
-                ("widom_slice", C.c_int64), ("gcmc_slice", C.c_int64), ("cluster_atoms", C.c_int64)]
+                ("widom_slice", C.c_int64), ("gcmc_slice", C.c_int64), ("cluster_atoms", C.c_int64),
+                ("gcmc_batching", C.c_int32), ("pad_", C.c_int32)]
 
 
 class JobDesc(C.Structure):
@@ -145,7 +146,7 @@ EXPORTS = [
     "grx_gcmc_batch_set_cluster", "grx_gcmc_batch_get_cluster", "grx_arena_create", "grx_arena_destroy",
     "grx_arena_usage", "grx_box_create_in", "grx_box_footprint", "grx_server_create", "grx_server_destroy",
     "grx_server_submit", "grx_server_progress", "grx_server_poll", "grx_server_time", "grx_server_launch_count",
-    "grx_box_create_replica", "grx_box_set_voxel_lists", "grx_box_get_voxel_lists",
+    "grx_box_create_replica", "grx_box_set_voxel_lists", "grx_box_get_voxel_lists", "grx_gcmc_batch_set_box_steps",
 ]
 
 _lib = None
@@ -227,6 +228,7 @@ def load(path=LIB_PATH):
     L.grx_box_footprint.argtypes = [P(BoxDesc), P(C.c_size_t)]
     L.grx_box_create_replica.argtypes = [C.c_void_p, P(C.c_void_p)]
     L.grx_box_set_voxel_lists.argtypes = [C.c_void_p, C.c_int32]
+    L.grx_gcmc_batch_set_box_steps.argtypes = [C.c_void_p, P(C.c_uint64), P(C.c_int64)]
     L.grx_box_get_voxel_lists.argtypes = [C.c_void_p, P(C.c_int32), P(C.c_int32), P(C.c_int64)]
     L.grx_server_create.argtypes = [P(ServerConfig), C.c_void_p, P(C.c_void_p)]
     L.grx_server_destroy.argtypes = [C.c_void_p]
@@ -615,10 +617,10 @@ class Server:
     """grx_server: continuous-batching Widom / GCMC job server."""
 
     def __init__(self, hbm_budget_bytes, max_resident, prec=GRX_MIXED, widom_slice=0, gcmc_slice=0,
-                 cluster_atoms=0):
+                 cluster_atoms=0, gcmc_batching=0):
         self.L = load()
         cfg = ServerConfig(int(hbm_budget_bytes), int(max_resident), int(prec), int(widom_slice), int(gcmc_slice),
-                           int(cluster_atoms))
+                           int(cluster_atoms), int(gcmc_batching), 0)
         h = C.c_void_p()
         check(self.L.grx_server_create(C.byref(cfg), None, C.byref(h)), "grx_server_create")
         self.h = h
@@ -784,6 +786,15 @@ class GcmcBatch:
 
     def launch(self, nsteps, stream=None):
         check(self.L.grx_gcmc_batch_launch(self.h, nsteps, C.c_void_p(stream or 0)), "grx_gcmc_batch_launch")
+
+    def set_box_steps(self, next_move, nsteps=None):
+        """grx_gcmc_batch_set_box_steps: per box, the next Philox move index and the most
+        steps it takes per launch (None: every step of the launch)."""
+        nm = np.ascontiguousarray(next_move, dtype=np.uint64)
+        ns = None if nsteps is None else np.ascontiguousarray(nsteps, dtype=np.int64)
+        check(self.L.grx_gcmc_batch_set_box_steps(self.h, nm.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                                  ns.ctypes.data_as(C.POINTER(C.c_int64)) if ns is not None
+                                                  else C.POINTER(C.c_int64)()), "grx_gcmc_batch_set_box_steps")
 
     def run_graph(self, nsteps, nlaunch, stream=None):
         check(self.L.grx_gcmc_batch_run_graph(self.h, nsteps, nlaunch, C.c_void_p(stream or 0)),

@@ -440,6 +440,12 @@ grx_status grx_gcmc_batch_set_step(grx_gcmc_batch* batch, uint64_t step);
  * advances the device step counter; no host synchronization, so it can be captured
  * into a CUDA graph. Statistics accumulate on the device. */
 grx_status grx_gcmc_batch_launch(grx_gcmc_batch* batch, int64_t nsteps, void* stream);
+/* Per-box step windows for the following launches (continuous batching of jobs that
+ * joined at different times): box i draws Philox move indices from next_move[i] on (its
+ * own chain continues where it stopped, whatever the other boxes do) and takes at most
+ * nsteps[i] steps per launch (NULL: all of the launch's steps; 0: the box idles). Waits for
+ * the batch's launches. No counterpart in the reference. */
+grx_status grx_gcmc_batch_set_box_steps(grx_gcmc_batch* batch, const uint64_t* next_move, const int64_t* nsteps);
 /* nlaunch launches of nsteps steps each, captured once into a CUDA graph (re-captured
  * when nsteps or nlaunch change) and replayed on `stream`. */
 grx_status grx_gcmc_batch_run_graph(grx_gcmc_batch* batch, int64_t nsteps, int32_t nlaunch, void* stream);
@@ -504,6 +510,15 @@ typedef struct {
                                    the largest of 8, 4, 2 CTAs not above N / cluster_atoms
                                    (grx_gcmc_batch_set_cluster; one block when it does not fit);
                                    0: one block per job */
+  int32_t gcmc_batching;        /* 1: every resident GCMC job advances in one shared persistent
+                                   launch per round (8 warps per job, up to 3 jobs per SM): jobs
+                                   join and leave between rounds, each draws from its own move
+                                   stream (grx_gcmc_batch_set_box_steps), and each takes a step
+                                   count proportional to gcmc_slice / its estimated cost per step,
+                                   so a round lasts about gcmc_slice steps of a job of 1000 pair
+                                   evaluations per step; cluster_atoms is not used. 0: one
+                                   launch per job on its own stream */
+  int32_t pad_;
 } grx_server_config;
 
 typedef struct {

@@ -9,6 +9,7 @@ import pytest
 
 from graspa_gb300 import synth
 from oracle import oracle as O
+from tests.systems import co2_system
 from tests.test_gpu_gcmc import ora_params
 from tests.test_gpu_parity import beta, fp64_close, mixed_close
 
@@ -155,3 +156,43 @@ def test_autotune_keeps_chains_valid(grx_lib):
         e1 = sum(b.total_energy().values())
         # mixed precision: each accepted move's dE within 1e-6 kT of FP64
         assert beta() * abs((e1 - totals0[i]) - esum) <= 1e-6 * (nacc + 1)
+
+
+def test_box_step_windows_continue_each_chain(grx_lib):
+    """grx_gcmc_batch_set_box_steps: boxes advanced in launches of different lengths, each
+    from its own move index, take exactly the decisions of one long launch per box (FP64)."""
+    s = co2_system()
+    nfw = s["comp_start"][1]
+    descs = [grx_lib.gcmc_desc(1, p_translation=0.25, p_rotation=0.5, p_reinsertion=0.5, p_swap=1.0,
+                               pressure_pa=1e6, seed=42, stream=k) for k in range(4)]
+    total = 120
+
+    def boxes():
+        parent = grx_lib.Box(s, capacity=[nfw, 3 * 64])
+        parent.ewald_total()
+        return [parent] + [parent.replica() for _ in range(3)]
+
+    ref_boxes = boxes()
+    ref = grx_lib.gcmc_run(ref_boxes, descs, 0, total, grx_lib.GRX_FP64)
+    win_boxes = boxes()
+    batch = grx_lib.GcmcBatch(win_boxes, descs, grx_lib.GRX_FP64)
+    batch.set_step(10_000)   # the launch counter is unrelated to the boxes' own move indices
+    done = np.zeros(4, dtype=np.int64)
+    sizes = [7, 13, 40, 120]
+    acc = np.zeros((4, 5), dtype=np.int64)
+    while (done < total).any():
+        n = np.minimum(sizes, total - done)
+        batch.set_box_steps(done.astype(np.uint64), n)
+        batch.launch(int(n.max()))
+        st, _ = batch.stats()
+        batch.reset_stats()
+        for i in range(4):
+            acc[i] += np.array(st[i].accepted)
+        done += n
+    st_final = batch.stats()[0]
+    batch.close()
+    for i in range(4):
+        assert list(acc[i]) == list(ref[i].accepted)
+        assert st_final[i].n_molecules == ref[i].n_molecules
+        np.testing.assert_allclose(win_boxes[i].positions(1, 3 * ref[i].n_molecules),
+                                   ref_boxes[i].positions(1, 3 * ref[i].n_molecules), atol=1e-9)

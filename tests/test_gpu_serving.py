@@ -33,18 +33,23 @@ def same(a, b):
             assert abs(e1 - e2) <= 1e-9 * max(1.0, abs(e2))
 
 
+@pytest.mark.parametrize("batching", [0, 1])
 @pytest.mark.parametrize("prec", ["GRX_MIXED", "GRX_FP64"])
-def test_results_alone_equal_results_in_the_mix(grx_lib, prec):
+def test_results_alone_equal_results_in_the_mix(grx_lib, prec, batching):
+    """batching 1: the GCMC jobs advance together in shared rounds, joining and leaving
+    between rounds, each with its own step count per round."""
     jobs = small_jobs(10)
     p = getattr(grx_lib, prec)
     fp = max(grx_lib.box_footprint(J["system"], J["capacity"]) for J in jobs)
     # room for about three boxes: jobs wait for memory as well as for slots
-    mix = grx_lib.Server(3.5 * fp, max_resident=6, prec=p, widom_slice=64, gcmc_slice=100)
+    mix = grx_lib.Server(3.5 * fp, max_resident=6, prec=p, widom_slice=64, gcmc_slice=100, gcmc_batching=batching)
     out_mix = serving.run_stream(mix, jobs)
     mix.close()
     assert len(out_mix) == len(jobs)
     for i, J in enumerate(jobs):
-        alone = grx_lib.Server(4 * fp, max_resident=1, prec=p)   # one slice per job, nothing else resident
+        # one slice (or, batching, rounds of another length) per job, nothing else resident
+        alone = grx_lib.Server(4 * fp, max_resident=1, prec=p, gcmc_slice=1000 if batching else 0,
+                               gcmc_batching=batching)
         out = serving.run_stream(alone, [J])
         alone.close()
         same(out_mix[i][0], out[0][0])
