@@ -109,7 +109,9 @@ __device__ __forceinline__ void rotate_quaternion(double& x, double& y, double& 
 // Trial orientations about the chosen first bead (fx, fy, fz): the vectors from the
 // component's slot-0 atom to its chain atoms, rotated by Philox quaternions. With
 // `retrace`, orientation 0 is the existing chain (ox/oy/oz arrays, chain atoms).
-template <class WK>
+// The mixed and FP32 forms rotate in double-float on the FP32 pipe (df_rotate_quaternion),
+// the FP64 form in FP64 (the oracle's arithmetic).
+template <int PREC, class WK>
 __device__ __noinline__ void gen_orientations(const BoxDev& b, WK& W, uint64_t seed, uint32_t stream,
                                                  uint64_t move, int no, int chain, int off, double scale_coul,
                                                  double scale, double fx, double fy, double fz, bool retrace,
@@ -127,7 +129,8 @@ __device__ __noinline__ void gen_orientations(const BoxDev& b, WK& W, uint64_t s
       const double4 t0 = b.pos64[off];
       const double4 pa = b.pos64[off + 1 + at];
       double vx = pa.x - t0.x, vy = pa.y - t0.y, vz = pa.z - t0.z;
-      rotate_quaternion(vx, vy, vz, u01(r[0]), u01(r[1]), u01(r[2]));
+      if constexpr (PREC == GRX_FP64) rotate_quaternion(vx, vy, vz, u01(r[0]), u01(r[1]), u01(r[2]));
+      else df_rotate_quaternion(vx, vy, vz, r[0], r[1], r[2]);
       make_bead(W.beads[tid], fx + vx, fy + vy, fz + vz, q, scale, type, b.prefactor);
     }
   }
@@ -310,20 +313,26 @@ __device__ __noinline__ void ewald_move(const BoxDev& b, WK& W, int na, double2*
   const double PI2 = 2.0 * 3.14159265358979323846;
   if (tid < 3 * na) {  // eik recurrence per atom and axis (Initialize_Vectors_thread)
     const int at = tid % na, d = tid / na;
-    const double s = (b.inv[d] * W.mx[at] + b.inv[3 + d] * W.my[at] + b.inv[6 + d] * W.mz[at]) * PI2;
-    double2* tab = d == 0 ? ex : (d == 1 ? ey : ez);
+    const double f = b.inv[d] * W.mx[at] + b.inv[3 + d] * W.my[at] + b.inv[6 + d] * W.mz[at];
     const int km = b.kmax[d];
-    tab[at] = make_double2(1.0, 0.0);
-    if (km >= 1) {
-      double sn, cs;
-      sincos(s, &sn, &cs);
-      const double2 e1 = make_double2(cs, sn);
-      double2 e = e1;
-      tab[at + na] = e1;
-      for (int k = 2; k <= km; ++k) {
-        e = cmul(e, e1);
-        tab[at + k * na] = e;
+    if constexpr (PREC == GRX_FP64) {
+      double2* tab = d == 0 ? ex : (d == 1 ? ey : ez);
+      tab[at] = make_double2(1.0, 0.0);
+      if (km >= 1) {
+        double sn, cs;
+        sincos(f * PI2, &sn, &cs);
+        const double2 e1 = make_double2(cs, sn);
+        double2 e = e1;
+        tab[at + na] = e1;
+        for (int k = 2; k <= km; ++k) {
+          e = cmul(e, e1);
+          tab[at + k * na] = e;
+        }
       }
+    } else {  // straight into the double-float tables read below (after the FP64 ones)
+      float4* f0 = reinterpret_cast<float4*>(ez + (b.kmax[2] + 1) * na);
+      float4* tab = f0 + (d == 0 ? 0 : (d == 1 ? kx1 * na : (kx1 + ky1) * na));
+      df_eik_row(f, km, tab + at, na);
     }
   }
   __syncthreads();
@@ -356,10 +365,6 @@ __device__ __noinline__ void ewald_move(const BoxDev& b, WK& W, int na, double2*
   } else {
     float4* fx = reinterpret_cast<float4*>(ez + (b.kmax[2] + 1) * na);
     const int ntab = (b.kmax[0] + b.kmax[1] + b.kmax[2] + 3) * na;
-    for (int e = tid; e < ntab; e += blockDim.x) {
-      const df re = df_from(ex[e].x), im = df_from(ex[e].y);
-      fx[e] = make_float4(re.hi, re.lo, im.hi, im.lo);
-    }
     if (tid < na) { const df q = df_from(W.mq[tid]); W.qd[tid] = make_float2(q.hi, q.lo); }
     __syncthreads();
     const float4* fy = fx + kx1 * na;

@@ -40,10 +40,22 @@ struct GcmcArgs {
   int64_t nsteps_cap;
 };
 
-// RotationAroundAxis (mc_utilities.h:459-481) for a coordinate axis.
+// sin and cos of an angle in double-float (theta / 2 pi through df_sincos_2pi), out of line so
+// the kernel body keeps its register allocation.
+static __device__ __noinline__ void df_sincos_angle(double theta, double& s, double& c) {
+  df sd, cd;
+  df_sincos_2pi(df_mul(df_from(theta), df{0.15915494f, 6.4206382e-09f}), sd, cd);
+  s = df_to(sd);
+  c = df_to(cd);
+}
+
+// RotationAroundAxis (mc_utilities.h:459-481) for a coordinate axis; the mixed and FP32 forms
+// take sin and cos in double-float, the FP64 form in FP64.
+template <int PREC>
 __device__ __forceinline__ void rotate_axis(double& x, double& y, double& z, double theta, int axis) {
   double s, c;
-  sincos(theta, &s, &c);
+  if constexpr (PREC == GRX_FP64) sincos(theta, &s, &c);
+  else df_sincos_angle(theta, s, c);
   const double w = 1.0 - c;
   const double ax = axis == 0, ay = axis == 1, az = axis == 2;
   const double r0 = ax * ax * w + c, r1 = ax * ay * w + az * s, r2 = ax * az * w - ay * s;
@@ -142,7 +154,7 @@ __device__ __noinline__ void identity_swap_step(const BoxDev& b, const GcmcArgs*
     double rosen = ok ? s_w1 : 0.0;
     double e2[4] = {0, 0, 0, 0};
     if (ok && msn > 1) {
-      gen_orientations(b, W, A[0].d.seed, A[0].d.stream, move, an.d.norient, msn - 1, an.off, 1.0, 1.0, W.mx[0],
+      gen_orientations<PREC>(b, W, A[0].d.seed, A[0].d.stream, move, an.d.norient, msn - 1, an.off, 1.0, 1.0, W.mx[0],
                        W.my[0], W.mz[0], false, nullptr, nullptr, nullptr);
       trial_pass_excl<PREC, CL>(b, W, an.d.norient * (msn - 1), msn - 1, an.comp, Nn, ao.comp, omol);
       step_weight(W, an.d.norient, beta, an.bias, u_orient, (double)an.d.norient, false);
@@ -175,7 +187,7 @@ __device__ __noinline__ void identity_swap_step(const BoxDev& b, const GcmcArgs*
       double rosen_old = ok2 ? s_wr : 0.0;
       double r2[4] = {0, 0, 0, 0};
       if (ok2 && mso > 1) {
-        gen_orientations(b, W, A[0].d.seed, A[0].d.stream, move, ao.d.norient, mso - 1, ao.off, 1.0, 1.0, W.mx[0],
+        gen_orientations<PREC>(b, W, A[0].d.seed, A[0].d.stream, move, ao.d.norient, mso - 1, ao.off, 1.0, 1.0, W.mx[0],
                          W.my[0], W.mz[0], true, W.mx + 1, W.my + 1, W.mz + 1, SLOT_RETRACE);
         trial_pass<PREC, CL>(b, W, ao.d.norient * (mso - 1), mso - 1, ao.comp, omol);
         step_weight(W, ao.d.norient, beta, ao.bias, 0.0, (double)ao.d.norient, true);
@@ -318,9 +330,9 @@ __global__ void __launch_bounds__(NW * 32, 24 / NW) gcmc_kernel(const BoxDev* bo
           nz = p.z + d.max_translation[2] * 2.0 * (u01(w2[2]) - 0.5);
         } else {
           double vx = p.x - p0.x, vy = p.y - p0.y, vz = p.z - p0.z;
-          rotate_axis(vx, vy, vz, d.max_rotation[0] * 2.0 * (u01(w2[0]) - 0.5), 0);
-          rotate_axis(vx, vy, vz, d.max_rotation[1] * 2.0 * (u01(w2[1]) - 0.5), 1);
-          rotate_axis(vx, vy, vz, d.max_rotation[2] * 2.0 * (u01(w2[2]) - 0.5), 2);
+          rotate_axis<PREC>(vx, vy, vz, d.max_rotation[0] * 2.0 * (u01(w2[0]) - 0.5), 0);
+          rotate_axis<PREC>(vx, vy, vz, d.max_rotation[1] * 2.0 * (u01(w2[1]) - 0.5), 1);
+          rotate_axis<PREC>(vx, vy, vz, d.max_rotation[2] * 2.0 * (u01(w2[2]) - 0.5), 2);
           nx = vx + p0.x; ny = vy + p0.y; nz = vz + p0.z;
         }
         W.mx[tid] = p.x; W.my[tid] = p.y; W.mz[tid] = p.z; W.mq[tid] = -p.w;
@@ -388,7 +400,7 @@ __global__ void __launch_bounds__(NW * 32, 24 / NW) gcmc_kernel(const BoxDev* bo
       double rosen = ok ? s_w1 : 0.0;
       double e2[4] = {0, 0, 0, 0};
       if (ok && chain > 0) {
-        gen_orientations(b, W, d.seed, d.stream, move, d.norient, chain, off, 1.0, 1.0, fx, fy, fz, false, nullptr,
+        gen_orientations<PREC>(b, W, d.seed, d.stream, move, d.norient, chain, off, 1.0, 1.0, fx, fy, fz, false, nullptr,
                          nullptr, nullptr);
         trial_pass<PREC, CL>(b, W, d.norient * chain, chain, comp, mol);
         step_weight(W, d.norient, d.beta, a.bias, u01(ws[1]), (double)d.norient, false);
@@ -419,7 +431,7 @@ __global__ void __launch_bounds__(NW * 32, 24 / NW) gcmc_kernel(const BoxDev* bo
         double rosen_old = ok2 ? s_wr : 0.0;
         double r2[4] = {0, 0, 0, 0};
         if (ok2 && chain > 0) {
-          gen_orientations(b, W, d.seed, d.stream, move, d.norient, chain, off, 1.0, 1.0, W.mx[0], W.my[0], W.mz[0],
+          gen_orientations<PREC>(b, W, d.seed, d.stream, move, d.norient, chain, off, 1.0, 1.0, W.mx[0], W.my[0], W.mz[0],
                            true, W.mx + 1, W.my + 1, W.mz + 1, SLOT_RETRACE);
           trial_pass<PREC, CL>(b, W, d.norient * chain, chain, comp, mol);
           step_weight(W, d.norient, d.beta, a.bias, 0.0, (double)d.norient, true);
@@ -485,7 +497,7 @@ __global__ void __launch_bounds__(NW * 32, 24 / NW) gcmc_kernel(const BoxDev* bo
       double rosen = ok ? s_w1 : 0.0;
       double e2[4] = {0, 0, 0, 0};
       if (ok && chain > 0) {
-        gen_orientations(b, W, d.seed, d.stream, move, d.norient, chain, off, 1.0, 1.0, fx, fy, fz, del,
+        gen_orientations<PREC>(b, W, d.seed, d.stream, move, d.norient, chain, off, 1.0, 1.0, fx, fy, fz, del,
                          W.mx + 1, W.my + 1, W.mz + 1);
         trial_pass<PREC, CL>(b, W, d.norient * chain, chain, comp, newmol);
         step_weight(W, d.norient, d.beta, a.bias, u01(ws[1]), (double)d.norient, del);

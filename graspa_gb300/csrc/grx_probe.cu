@@ -3,6 +3,7 @@
 //
 // Every thread runs kChains independent FMA chains (enough instruction-level
 // parallelism to cover the FMA latency); the grid fills every SM with 1024 threads.
+#include "grx_df.cuh"
 #include "grx_host.h"
 
 namespace grx {
@@ -25,9 +26,46 @@ __global__ void __launch_bounds__(256) fma_probe_kernel(float* out, int iters, f
   out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// The double-float elementary functions of the mixed-precision CBMC stages, one value per
+// thread: sin and cos of 2 pi v, and the quaternion rotation of (1, 0.5, -0.25) by the
+// Philox words of w (checked against FP64 by the tests).
+__global__ void df_functions_probe_kernel(const double* v, const uint32_t* w, int n, double* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  df s, c;
+  df_sincos_2pi(df_from(v[i]), s, c);
+  double x = 1.0, y = 0.5, z = -0.25;
+  df_rotate_quaternion(x, y, z, w[3 * i], w[3 * i + 1], w[3 * i + 2]);
+  out[5 * i] = df_to(s);
+  out[5 * i + 1] = df_to(c);
+  out[5 * i + 2] = x;
+  out[5 * i + 3] = y;
+  out[5 * i + 4] = z;
+}
+
 }  // namespace grx
 
 using namespace grx;
+
+extern "C" grx_status grx_probe_df_functions(const double* v, const uint32_t* words, int64_t n, double* out5) {
+  GRX_REQUIRE(v && words && out5 && n >= 1 && n <= (1 << 24), "grx_probe_df_functions: bad argument");
+  void* mem = nullptr;
+  const size_t bv = n * sizeof(double), bw = 3 * n * sizeof(uint32_t), bo = 5 * n * sizeof(double);
+  GRX_CHECK_CUDA(cudaMalloc(&mem, bv + bw + bo), "probe buffers");
+  char* m = (char*)mem;
+  cudaError_t e = cudaMemcpy(m, v, bv, cudaMemcpyDefault);
+  if (e == cudaSuccess) e = cudaMemcpy(m + bv, words, bw, cudaMemcpyDefault);
+  if (e == cudaSuccess) {
+    df_functions_probe_kernel<<<(int)((n + 127) / 128), 128>>>((const double*)m, (const uint32_t*)(m + bv), (int)n,
+                                                              (double*)(m + bv + bw));
+    count_launch();
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(out5, m + bv + bw, bo, cudaMemcpyDefault);
+  cudaFree(mem);
+  GRX_CHECK_CUDA(e, "grx_probe_df_functions");
+  return GRX_OK;
+}
 
 extern "C" grx_status grx_probe_fp32_fma(int32_t iters, double* tflops, float* ms) {
   GRX_REQUIRE(tflops && iters >= 1, "grx_probe_fp32_fma: bad argument");

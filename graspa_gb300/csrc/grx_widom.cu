@@ -206,7 +206,8 @@ __global__ void __launch_bounds__(GRX_THREADS, 3) widom_kernel(BoxDev b, WidomAr
         draw4(a.seed, a.stream, move, SLOT_ORIENT + o, r);
         const double4 pa = b.pos64[off + 1 + at];
         double vx = pa.x - t0.x, vy = pa.y - t0.y, vz = pa.z - t0.z;
-        rotate_quaternion(vx, vy, vz, u01(r[0]), u01(r[1]), u01(r[2]));
+        if constexpr (PREC == GRX_FP64) rotate_quaternion(vx, vy, vz, u01(r[0]), u01(r[1]), u01(r[2]));
+        else df_rotate_quaternion(vx, vy, vz, r[0], r[1], r[2]);
         make_bead(beads[tid], fx + vx, fy + vy, fz + vz, b.charge[off + 1 + at] * a.scale_coul, a.scale,
                   b.meta[off + 1 + at].x, b.prefactor);
       }
@@ -251,20 +252,26 @@ __global__ void __launch_bounds__(GRX_THREADS, 3) widom_kernel(BoxDev b, WidomAr
       const double PI2 = 2.0 * 3.14159265358979323846;
       if (tid < 3 * ms) {
         const int at = tid % ms, d = tid / ms;
-        const double s = (b.inv[d] * newx[at] + b.inv[3 + d] * newy[at] + b.inv[6 + d] * newz[at]) * PI2;
-        double2* tab = d == 0 ? ex : (d == 1 ? ey : ez);
+        const double f = b.inv[d] * newx[at] + b.inv[3 + d] * newy[at] + b.inv[6 + d] * newz[at];
         const int km = b.kmax[d];
-        tab[at] = make_double2(1.0, 0.0);
-        if (km >= 1) {
-          double sn, cs;
-          sincos(s, &sn, &cs);
-          const double2 e1 = make_double2(cs, sn);
-          double2 e = e1;
-          tab[at + ms] = e1;
-          for (int k = 2; k <= km; ++k) {
-            e = cmul(e, e1);
-            tab[at + k * ms] = e;
+        if constexpr (PREC == GRX_FP64) {
+          double2* tab = d == 0 ? ex : (d == 1 ? ey : ez);
+          tab[at] = make_double2(1.0, 0.0);
+          if (km >= 1) {
+            double sn, cs;
+            sincos(f * PI2, &sn, &cs);
+            const double2 e1 = make_double2(cs, sn);
+            double2 e = e1;
+            tab[at + ms] = e1;
+            for (int k = 2; k <= km; ++k) {
+              e = cmul(e, e1);
+              tab[at + k * ms] = e;
+            }
           }
+        } else {  // straight into the double-float tables (after the FP64 ones)
+          float4* f0 = reinterpret_cast<float4*>(ez + (b.kmax[2] + 1) * ms);
+          float4* tab = f0 + (d == 0 ? 0 : (d == 1 ? kx1 * ms : (kx1 + ky1) * ms));
+          df_eik_row(f, km, tab + at, ms);
         }
       }
       __syncthreads();
@@ -295,11 +302,6 @@ __global__ void __launch_bounds__(GRX_THREADS, 3) widom_kernel(BoxDev b, WidomAr
       } else {
         // double-float copies of the eik tables (same shared buffer, after the FP64 ones)
         float4* fx = reinterpret_cast<float4*>(ez + (b.kmax[2] + 1) * ms);
-        const int ntab = (b.kmax[0] + b.kmax[1] + b.kmax[2] + 3) * ms;
-        for (int e = tid; e < ntab; e += blockDim.x) {
-          const df re = df_from(ex[e].x), im = df_from(ex[e].y);
-          fx[e] = make_float4(re.hi, re.lo, im.hi, im.lo);
-        }
         __shared__ float2 qd[GRX_MAX_MOLSIZE];
         if (tid < ms) { const df q = df_from(newq[tid]); qd[tid] = make_float2(q.hi, q.lo); }
         __syncthreads();

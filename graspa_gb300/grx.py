@@ -147,6 +147,7 @@ EXPORTS = [
     "grx_arena_usage", "grx_box_create_in", "grx_box_footprint", "grx_server_create", "grx_server_destroy",
     "grx_server_submit", "grx_server_progress", "grx_server_poll", "grx_server_time", "grx_server_launch_count",
     "grx_box_create_replica", "grx_box_set_voxel_lists", "grx_box_get_voxel_lists", "grx_gcmc_batch_set_box_steps",
+    "grx_probe_df_functions",
 ]
 
 _lib = None
@@ -229,6 +230,7 @@ def load(path=LIB_PATH):
     L.grx_box_create_replica.argtypes = [C.c_void_p, P(C.c_void_p)]
     L.grx_box_set_voxel_lists.argtypes = [C.c_void_p, C.c_int32]
     L.grx_gcmc_batch_set_box_steps.argtypes = [C.c_void_p, P(C.c_uint64), P(C.c_int64)]
+    L.grx_probe_df_functions.argtypes = [_dp, P(C.c_uint32), C.c_int64, _dp]
     L.grx_box_get_voxel_lists.argtypes = [C.c_void_p, P(C.c_int32), P(C.c_int32), P(C.c_int64)]
     L.grx_server_create.argtypes = [P(ServerConfig), C.c_void_p, P(C.c_void_p)]
     L.grx_server_destroy.argtypes = [C.c_void_p]
@@ -866,3 +868,13 @@ def probe_fp32_fma(iters=20000):
     t, ms = C.c_double(), C.c_float()
     check(load().grx_probe_fp32_fma(iters, C.byref(t), C.byref(ms)), "grx_probe_fp32_fma")
     return t.value
+
+
+def probe_df_functions(v, words):
+    """grx_probe_df_functions: (sin 2 pi v, cos 2 pi v, rotated (1, 0.5, -0.25)) per value."""
+    v = np.ascontiguousarray(v, dtype=np.float64)
+    w = np.ascontiguousarray(words, dtype=np.uint32).reshape(-1)
+    out = np.zeros(5 * len(v))
+    check(load().grx_probe_df_functions(_d(v), w.ctypes.data_as(C.POINTER(C.c_uint32)), len(v), _d(out)),
+          "grx_probe_df_functions")
+    return out.reshape(-1, 5)

@@ -487,6 +487,11 @@ grx_status grx_gcmc_batch_autotune(grx_gcmc_batch* batch, int64_t nsteps, int32_
  * FMA chains on every SM, timed with CUDA events over `iters` x 128 FMAs per thread.
  * The roofline denominator of the pair kernels (no gRASPA counterpart). */
 grx_status grx_probe_fp32_fma(int32_t iters, double* tflops, float* ms);
+/* The double-float functions of the mixed-precision CBMC stages evaluated on the device, for
+ * accuracy tests: out5[5i..5i+4] = sin(2 pi v[i]), cos(2 pi v[i]) and the rotation of
+ * (1, 0.5, -0.25) by the uniform quaternion of Rotate_Quaternions (mc_utilities.h:423-457)
+ * whose uniforms are words[3i..3i+2] * 2^-32. No counterpart in the reference. */
+grx_status grx_probe_df_functions(const double* v, const uint32_t* words, int64_t n, double* out5);
 
 /* ---- serving ----------------------------------------------------------------- */
 /* A continuous-batching job server. Each job is one box (its description and atoms,
