@@ -62,6 +62,7 @@ struct grx_box {
   std::vector<int> perm[GRX_MAX_COMPONENTS];  // storage slot -> caller index
   // candidate lists of host atoms per voxel (grx_voxel.cu); a replica uses its parent's
   int vox_mode = 1;          // 1: build them when they fit, 0: tile path only
+  size_t vox_max_bytes = 32u << 20;  // byte cap of the lists (coarser voxels to stay below it)
   int vox_on = 0;
   int vn[3] = {0, 0, 0};
   int vchunks = 0;

@@ -110,9 +110,9 @@ grx_status admit_job(grx_server* S, ServerJob* j) {
   grx_arena_usage(S->arena, &before, nullptr, nullptr);
   grx_status st = grx_box_create_in(&j->desc, S->arena, &j->box);
   if (st) return st;
-  // voxel candidate lists pay for their host-side build over the thousands of moves of a
-  // GCMC job; a Widom job is short, so its box keeps the tile path and is admitted sooner
-  if (j->kind == GRX_JOB_WIDOM) j->box->vox_mode = 0;
+  // server boxes keep the tile path: voxel candidate lists would take arena memory only when
+  // room allows, and a job's arithmetic must not depend on what else is resident
+  j->box->vox_mode = 0;
   if (!S->streams.empty()) {
     j->stream = S->streams.back();
     S->streams.pop_back();

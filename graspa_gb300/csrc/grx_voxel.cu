@@ -52,16 +52,16 @@ inline double image(const Geo& G, double* d, int* n, double half_wmin) {
   return std::max(std::fabs(r[0]) * G.w[0], std::max(std::fabs(r[1]) * G.w[1], std::fabs(r[2]) * G.w[2]));
 }
 
-constexpr size_t kVoxelListMaxBytes = 32u << 20;  // per framework (shared by its replicas)
 constexpr double kMargin = 0.02;                  // A, on the voxel bounding radius
+constexpr size_t kArenaHeadroom = 4u << 20;       // arena bytes left free for the box's other buffers
 
 }  // namespace
 
 // Voxel grid of a cell: the finest edge g in {1.5, 2, 2.5, 3, 4} A whose lists fit the byte
-// cap (estimated from the host-atom density) and leave the cell wider than 2 r_list. Returns
+// cap max_bytes (estimated from the host-atom density) and leave the cell wider than 2 r_list. Returns
 // false when none does (the tile path then serves the box).
-static bool choose_voxels(const double* C, double volume, int nh_atoms, double r_screen, Geo& G, double& half_wmin,
-                          int nv[3], double& h, double& est_bytes) {
+static bool choose_voxels(const double* C, double volume, int nh_atoms, double r_screen, size_t max_bytes, Geo& G,
+                          double& half_wmin, int nv[3], double& h, double& est_bytes) {
   const double av[3] = {C[0], C[1], C[2]}, bv[3] = {C[3], C[4], C[5]}, cv[3] = {C[6], C[7], C[8]};
   auto cross_norm = [](const double* u, const double* v) {
     const double x = u[1] * v[2] - u[2] * v[1], y = u[2] * v[0] - u[0] * v[2], z = u[0] * v[1] - u[1] * v[0];
@@ -91,7 +91,7 @@ static bool choose_voxels(const double* C, double volume, int nh_atoms, double r
     const double rl = r_screen + hm;
     const double est = (double)n[0] * n[1] * n[2] * (dens * 4.18879 * rl * rl * rl * 1.25 + 32.0) * 4.0 +
                        (double)n[0] * n[1] * n[2] * 16.0;
-    if (est <= (double)kVoxelListMaxBytes) {
+    if (est <= (double)max_bytes) {
       for (int k = 0; k < 3; ++k) nv[k] = n[k];
       h = hm;
       est_bytes = est;
@@ -125,7 +125,7 @@ grx_status build_voxels(grx_box* b) {
   const double r_screen = std::sqrt((double)d.screen2);
   int nv[3] = {0, 0, 0};
   double h = 0.0, half_wmin = 0.0, est = 0.0;
-  if (!choose_voxels(C, d.volume, nh_atoms, r_screen, G, half_wmin, nv, h, est)) {
+  if (!choose_voxels(C, d.volume, nh_atoms, r_screen, b->vox_max_bytes, G, half_wmin, nv, h, est)) {
     refresh_dev(b);
     return GRX_OK;
   }
@@ -208,6 +208,14 @@ grx_status build_voxels(grx_box* b) {
   flat.reserve(total);
   for (const auto& l : lists) flat.insert(flat.end(), l.begin(), l.end());
   if (flat.empty()) flat.push_back(0);
+  if (b->arena) {  // in an arena the lists are optional: take them only with room to spare
+    size_t used = 0, largest = 0;
+    grx_arena_usage(b->arena, &used, &largest, nullptr);
+    if (largest < nvox * sizeof(int4) + flat.size() * sizeof(uint32_t) + kArenaHeadroom) {
+      refresh_dev(b);
+      return GRX_OK;
+    }
+  }
   if (dev_alloc(b, (void**)&b->vmeta, nvox * sizeof(int4)) != cudaSuccess ||
       dev_alloc(b, (void**)&b->vlist, flat.size() * sizeof(uint32_t)) != cudaSuccess) {
     cudaGetLastError();  // no room: the tile path serves the box

@@ -107,7 +107,8 @@ def test_admission_by_footprint_and_slots(grx_lib):
     srv.close()
     assert len(done) == len(jobs) and most == 3
     # a job that cannot fit even alone is reported, not queued forever
-    tiny = grx_lib.Server(max(fpa) // 4, max_resident=2, prec=grx_lib.GRX_MIXED)
+    tiny = grx_lib.Server(grx_lib.box_footprint(jobs[0]["system"], jobs[0]["capacity"]) // 4, max_resident=2,
+                          prec=grx_lib.GRX_MIXED)
     out = serving.run_stream(tiny, jobs[:1])
     tiny.close()
     assert out[0][0].status == 3                          # GRX_ERR_OUT_OF_MEMORY
