@@ -16,7 +16,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libgrx.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["grx_box.cu", "grx_pair.cu", "grx_ewald.cu", "grx_widom.cu", "grx_noalloc.cu", "grx_gcmc.cu", "grx_gcmc_cluster.cu", "grx_gcmc_swap.cu", "grx_arena.cu", "grx_server.cu", "grx_probe.cu", "grx_voxel.cu"]
-HEADERS = ["grx_internal.cuh", "grx_host.h", "grx_warp.cuh", "grx_df.cuh", "grx_cbmc.cuh"]
+HEADERS = ["grx_internal.cuh", "grx_host.h", "grx_warp.cuh", "grx_df.cuh", "grx_cbmc.cuh", "grx_gcmc_kernel.cuh"]
 HOST = os.path.join(HERE, "host")
 HOST_SOURCES = ["graspa_host.cpp", "graspa_input.cpp"]
 HOST_PROGRAMS = {"gcmc_driver": "gcmc_driver.cpp", "graspa_run": "graspa_run.cpp"}

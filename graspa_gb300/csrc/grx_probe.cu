@@ -50,11 +50,13 @@ using namespace grx;
 extern "C" grx_status grx_probe_df_functions(const double* v, const uint32_t* words, int64_t n, double* out5) {
   GRX_REQUIRE(v && words && out5 && n >= 1 && n <= (1 << 24), "grx_probe_df_functions: bad argument");
   void* mem = nullptr;
-  const size_t bv = n * sizeof(double), bw = 3 * n * sizeof(uint32_t), bo = 5 * n * sizeof(double);
+  // each segment starts on a 256-byte boundary (the word segment's length is a multiple of 4 only)
+  auto up = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const size_t bv = up(n * sizeof(double)), bw = up(3 * n * sizeof(uint32_t)), bo = 5 * n * sizeof(double);
   GRX_CHECK_CUDA(cudaMalloc(&mem, bv + bw + bo), "probe buffers");
   char* m = (char*)mem;
-  cudaError_t e = cudaMemcpy(m, v, bv, cudaMemcpyDefault);
-  if (e == cudaSuccess) e = cudaMemcpy(m + bv, words, bw, cudaMemcpyDefault);
+  cudaError_t e = cudaMemcpy(m, v, n * sizeof(double), cudaMemcpyDefault);
+  if (e == cudaSuccess) e = cudaMemcpy(m + bv, words, 3 * n * sizeof(uint32_t), cudaMemcpyDefault);
   if (e == cudaSuccess) {
     df_functions_probe_kernel<<<(int)((n + 127) / 128), 128>>>((const double*)m, (const uint32_t*)(m + bv), (int)n,
                                                               (double*)(m + bv + bw));

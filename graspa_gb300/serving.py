@@ -63,9 +63,22 @@ def summarize(out):
     t_first = min(arr for (_, arr) in out.values())
     t_last = max(r.t_done for (r, _) in out.values())
     span = max(t_last - t_first, 1e-9)
+    done = np.sort([r.t_done for (r, _) in out.values()])
+    lo, hi = steady_window(out)
+    mid = int(np.sum((done >= lo) & (done <= hi)))
     return dict(jobs=len(out), jobs_per_s=len(out) / span, p50_s=float(np.percentile(lat, 50)),
                 p99_s=float(np.percentile(lat, 99)), makespan_s=span,
+                steady_jobs_per_s=mid / max(hi - lo, 1e-9),
                 failed=sum(1 for (r, _) in out.values() if r.status != 0))
+
+
+def steady_window(out):
+    """(t10, t90): the server-clock times of the 10th- and 90th-percentile completions. Rates
+    over this window leave out the ramp-up and the tail of the longest jobs, which a stream of
+    finite length always has."""
+    done = np.sort([r.t_done for (r, _) in out.values()])
+    n = len(done)
+    return float(done[int(0.1 * (n - 1))]), float(done[int(0.9 * (n - 1))])
 
 
 def trial_energies_of(J, r):
