@@ -75,7 +75,7 @@ __device__ __noinline__ void gen_first_trials(const BoxDev& b, WK& W, uint64_t s
       make_bead(W.beads[0], ox, oy, oz, q, scale, type, b.prefactor);
     } else {
       uint32_t r[4];
-      draw4(seed, stream, move, SLOT_FIRST + t, r);
+      draw4_dev(seed, stream, move, SLOT_FIRST + t, r);
       make_bead(W.beads[t], b.cell[0] * u01(r[0]), b.cell[4] * u01(r[1]), b.cell[8] * u01(r[2]), q, scale, type,
                 b.prefactor);
     }
@@ -125,7 +125,7 @@ __device__ __noinline__ void gen_orientations(const BoxDev& b, WK& W, uint64_t s
       make_bead(W.beads[tid], ox[at], oy[at], oz[at], q, scale, type, b.prefactor);
     } else {
       uint32_t r[4];
-      draw4(seed, stream, move, slot_base + o, r);
+      draw4_dev(seed, stream, move, slot_base + o, r);
       const double4 t0 = b.pos64[off];
       const double4 pa = b.pos64[off + 1 + at];
       double vx = pa.x - t0.x, vy = pa.y - t0.y, vz = pa.z - t0.z;
@@ -226,6 +226,7 @@ __device__ __noinline__ void step_weight(WK& W, int nt, double beta, int bias, d
     bool ok[2];
     double mx = -INFINITY;
     int cnt = 0;
+#pragma unroll
     for (int r = 0; r < 2; ++r) {
       const int t = lane + 32 * r;
       ok[r] = t < nt && !W.tflag[t];
@@ -242,11 +243,12 @@ __device__ __noinline__ void step_weight(WK& W, int nt, double beta, int bias, d
       mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
       cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
     }
+#pragma unroll 1
     for (int r = 0; r < 2; ++r) {
       const int t = lane + 32 * r;
       if (t < nt) {
-        W.sel_ws[t] = ok[r] ? exp(__dsub_rn(lw[r], mx)) : 0.0;
-        W.sel_wa[t] = ok[r] ? exp(lw[r]) : 0.0;
+        W.sel_ws[t] = ok[r] ? exp_move(__dsub_rn(lw[r], mx)) : 0.0;
+        W.sel_wa[t] = ok[r] ? exp_move(lw[r]) : 0.0;
       }
     }
     __syncwarp();
@@ -256,15 +258,18 @@ __device__ __noinline__ void step_weight(WK& W, int nt, double beta, int bias, d
       if (cnt > 0) {
         int s = -1;
         if (retrace) {
+#pragma unroll 1
           for (int t = 0; t < nt; ++t)
             if (!W.tflag[t]) { s = t; break; }
         } else {
           double sum = 0.0;
+#pragma unroll 1
           for (int t = 0; t < nt; ++t)
             if (!W.tflag[t]) sum += W.sel_ws[t];
           const double wsel = u * sum;
           int left = cnt;
           double cum = 0.0;
+#pragma unroll 1
           for (int t = 0; t < nt; ++t) {
             if (W.tflag[t]) continue;
             cum += W.sel_ws[t];
@@ -274,12 +279,13 @@ __device__ __noinline__ void step_weight(WK& W, int nt, double beta, int bias, d
           }
         }
         double w = 0.0;
+#pragma unroll 1
         for (int t = 0; t < nt; ++t)
           if (!W.tflag[t]) w += W.sel_wa[t];
         W.wraw = w;
         if (retrace || !(w < 1e-150)) {
           double avg = (w + stored) / navg;
-          if (!bias) avg *= exp(-beta * (W.te[4 * s + 1] + W.te[4 * s + 3]));
+          if (!bias) avg *= exp_move(-beta * (W.te[4 * s + 1] + W.te[4 * s + 3]));
           W.ok = 1;
           W.sel = s;
           W.w = avg;
@@ -409,6 +415,7 @@ __device__ __noinline__ void ewald_move(const BoxDev& b, WK& W, int na, double2*
         const int az = abs(k.z);
         const float sz = k.z < 0 ? -1.f : 1.f;
         df cre = {0.f, 0.f}, cim = {0.f, 0.f};
+#pragma unroll 1
         for (int at = 0; at < na; ++at) {
           const float4 R = P[at], Z = fz[at + na * az];
           const df pr = {R.x, R.y}, pi = {R.z, R.w};
@@ -424,6 +431,7 @@ __device__ __noinline__ void ewald_move(const BoxDev& b, WK& W, int na, double2*
         df cre = {0.f, 0.f}, cim = {0.f, 0.f};
         const int ay = abs(k.y), az = abs(k.z);
         const float sy = k.y < 0 ? -1.f : 1.f, sz = k.z < 0 ? -1.f : 1.f;
+#pragma unroll 1
         for (int at = 0; at < na; ++at) {
           const float4 X = fx[at + na * k.x], Y = fy[at + na * ay], Z = fz[at + na * az];
           const df xr = {X.x, X.y}, xi = {X.z, X.w};
@@ -477,7 +485,7 @@ __device__ __noinline__ void ewald_move(const BoxDev& b, WK& W, int na, double2*
 // Make the staged structure factor current and refresh its double-float table (in a
 // cluster, the CTA's own range of k).
 template <int CL = 1>
-__device__ __forceinline__ void commit_sk(const BoxDev& b, const double2* s_tmp) {
+__device__ __noinline__ void commit_sk(const BoxDev& b, const double2* s_tmp) {
   float4* ewA = const_cast<float4*>(b.ewA);
   int k0 = 0, k1 = b.nact;
   if constexpr (CL > 1) cluster_k_range(b.nact, CL, cluster_rank(), k0, k1);
@@ -493,7 +501,7 @@ __device__ __forceinline__ void commit_sk(const BoxDev& b, const double2* s_tmp)
 }
 
 // Write one atom into the box storage (all representations).
-__device__ __forceinline__ void store_atom(const BoxDev& b, int idx, double x, double y, double z, double charge,
+static __device__ __noinline__ void store_atom(const BoxDev& b, int idx, double x, double y, double z, double charge,
                                            double scale_coul, double scale, int type, int molid) {
   const double qe = charge * scale_coul;
   const_cast<double4*>(b.pos64)[idx] = make_double4(x, y, z, qe);

@@ -104,10 +104,12 @@ __device__ __forceinline__ df df_sqrt(df a) {
   return fast_two_sum(r, __fdiv_rn(e, __fmul_rn(2.0f, r)));
 }
 
-// Exact double-float of a Philox uniform w * 2^-32: the top 24 and the low 8 bits of w.
+// Exact double-float of a Philox uniform w * 2^-32: the top 24 and the low 8 bits of w, then
+// normalised (the low part below half an ulp of the high one; for w < 2^8 the high part is 0
+// and the value moves into it, which df_sqrt and the products need).
 __device__ __forceinline__ df df_u01(uint32_t w) {
-  return {__fmul_rn((float)(w & 0xffffff00u), 2.3283064365386963e-10f), __fmul_rn((float)(w & 0xffu),
-                                                                                  2.3283064365386963e-10f)};
+  return fast_two_sum(__fmul_rn((float)(w & 0xffffff00u), 2.3283064365386963e-10f),
+                      __fmul_rn((float)(w & 0xffu), 2.3283064365386963e-10f));
 }
 
 // sin(2 pi v) and cos(2 pi v) for any v of moderate size (|4 v| < 2^22), ~1e-14 absolute:
@@ -115,7 +117,8 @@ __device__ __forceinline__ df df_u01(uint32_t w) {
 // sin x and cos x from their Taylor series in Horner form, the orders up to x^9 / x^8 in
 // double-float, the smaller tail (below 3e-8 of the result) in FP32; the quadrant q mod 4
 // then swaps and negates (sin(x + q pi/2), cos(x + q pi/2)).
-__device__ __forceinline__ void df_sincos_2pi(df v, df& s, df& c) {
+__device__ __forceinline__ float4 df_sincos_2pi_inl(float vhi, float vlo) {
+  const df v = {vhi, vlo};
   const float q = rintf(4.0f * v.hi);
   const df r = df_add_f(v, -0.25f * q);
   const df x = df_mul(r, df{6.2831855f, -1.7484555e-07f});
@@ -138,8 +141,20 @@ __device__ __forceinline__ void df_sincos_2pi(df v, df& s, df& c) {
   pc = df_add_f(df_mul(x2, pc), 1.0f);
   const int quad = ((int)q) & 3;
   const df ns = {-sx.hi, -sx.lo}, nc = {-pc.hi, -pc.lo};
-  s = quad == 0 ? sx : (quad == 1 ? pc : (quad == 2 ? ns : nc));
-  c = quad == 0 ? pc : (quad == 1 ? ns : (quad == 2 ? nc : sx));
+  const df s = quad == 0 ? sx : (quad == 1 ? pc : (quad == 2 ? ns : nc));
+  const df c = quad == 0 ? pc : (quad == 1 ? ns : (quad == 2 ? nc : sx));
+  return make_float4(s.hi, s.lo, c.hi, c.lo);
+}
+
+// The same out of line (one copy per kernel for the orientation, rotation and eik call
+// sites: these run once per move on few lanes, where instruction fetch, not arithmetic,
+// sets the time), the result returned in registers.
+static __device__ __noinline__ float4 df_sincos_2pi_out(float vhi, float vlo) { return df_sincos_2pi_inl(vhi, vlo); }
+
+__device__ __forceinline__ void df_sincos_2pi(df v, df& s, df& c) {
+  const float4 r = df_sincos_2pi_out(v.hi, v.lo);
+  s = df{r.x, r.y};
+  c = df{r.z, r.w};
 }
 
 // e^{i 2 pi k f} for k = 0..km as double-float complex {re hi, re lo, im hi, im lo} in
@@ -152,6 +167,7 @@ __device__ __forceinline__ void df_eik_row(double f, int km, float4* tab, int st
   df_sincos_2pi(df_from(f), ei, er);
   df r = er, i = ei;
   tab[stride] = make_float4(r.hi, r.lo, i.hi, i.lo);
+#pragma unroll 1
   for (int k = 2; k <= km; ++k) {
     const df nr = df_add(df_mul(r, er), df_mul(df{-i.hi, -i.lo}, ei));
     const df ni = df_add(df_mul(r, ei), df_mul(i, er));
@@ -163,9 +179,9 @@ __device__ __forceinline__ void df_eik_row(double f, int km, float4* tab, int st
 
 // (x, y, z) rotated by the quaternion of Rotate_Quaternions (mc_utilities.h:423-457, uniform
 // rotation from three uniforms) with the uniforms given as Philox words, in double-float on
-// the FP32 pipe: the same rotation as the FP64 form to ~1e-14 relative.
-__device__ __forceinline__ void df_rotate_quaternion(double& x, double& y, double& z, uint32_t wu, uint32_t wv,
-                                                     uint32_t ww) {
+// the FP32 pipe: the same rotation as the FP64 form to ~1e-13 relative.
+__device__ __forceinline__ void df_rotate_quaternion_inl(double& x, double& y, double& z, uint32_t wu, uint32_t wv,
+                                                         uint32_t ww) {
   const df u = df_u01(wu);
   df s1, c1, s2, c2;
   df_sincos_2pi(df_u01(wv), s1, c1);
@@ -188,6 +204,22 @@ __device__ __forceinline__ void df_rotate_quaternion(double& x, double& y, doubl
   x = df_to(nx);
   y = df_to(ny);
   z = df_to(nz);
+}
+
+// Out of line (the orientation stages run it once per trial on few lanes; a smaller kernel
+// fetches fewer instructions), the result returned in registers.
+static __device__ __noinline__ double4 df_rotate_quaternion_out(double x, double y, double z, uint32_t wu,
+                                                                uint32_t wv, uint32_t ww) {
+  df_rotate_quaternion_inl(x, y, z, wu, wv, ww);
+  return make_double4(x, y, z, 0.0);
+}
+
+__device__ __forceinline__ void df_rotate_quaternion(double& x, double& y, double& z, uint32_t wu, uint32_t wv,
+                                                     uint32_t ww) {
+  const double4 r = df_rotate_quaternion_out(x, y, z, wu, wv, ww);
+  x = r.x;
+  y = r.y;
+  z = r.z;
 }
 
 }  // namespace grx

@@ -42,20 +42,23 @@ struct GcmcArgs {
 
 // sin and cos of an angle in double-float (theta / 2 pi through df_sincos_2pi), out of line so
 // the kernel body keeps its register allocation.
-static __device__ __noinline__ void df_sincos_angle(double theta, double& s, double& c) {
+static __device__ __noinline__ double2 df_sincos_angle(double theta) {
   df sd, cd;
   df_sincos_2pi(df_mul(df_from(theta), df{0.15915494f, 6.4206382e-09f}), sd, cd);
-  s = df_to(sd);
-  c = df_to(cd);
+  return make_double2(df_to(sd), df_to(cd));
 }
 
 // RotationAroundAxis (mc_utilities.h:459-481) for a coordinate axis; the mixed and FP32 forms
 // take sin and cos in double-float, the FP64 form in FP64.
 template <int PREC>
-__device__ __forceinline__ void rotate_axis(double& x, double& y, double& z, double theta, int axis) {
+__device__ __noinline__ double4 rotate_axis_out(double x, double y, double z, double theta, int axis) {
   double s, c;
   if constexpr (PREC == GRX_FP64) sincos(theta, &s, &c);
-  else df_sincos_angle(theta, s, c);
+  else {
+    const double2 sc = df_sincos_angle(theta);
+    s = sc.x;
+    c = sc.y;
+  }
   const double w = 1.0 - c;
   const double ax = axis == 0, ay = axis == 1, az = axis == 2;
   const double r0 = ax * ax * w + c, r1 = ax * ay * w + az * s, r2 = ax * az * w - ay * s;
@@ -64,7 +67,13 @@ __device__ __forceinline__ void rotate_axis(double& x, double& y, double& z, dou
   const double nx = x * r0 + y * r1 + z * r2;
   const double ny = x * r3 + y * r4 + z * r5;
   const double nz = x * r6 + y * r7 + z * r8;
-  x = nx; y = ny; z = nz;
+  return make_double4(nx, ny, nz, 0.0);
+}
+
+template <int PREC>
+__device__ __forceinline__ void rotate_axis(double& x, double& y, double& z, double theta, int axis) {
+  const double4 r = rotate_axis_out<PREC>(x, y, z, theta, axis);
+  x = r.x; y = r.y; z = r.z;
 }
 
 __device__ __forceinline__ void store_position(const BoxDev& b, int idx, double x, double y, double z) {
@@ -115,7 +124,7 @@ __device__ __noinline__ void identity_swap_step(const BoxDev& b, const GcmcArgs*
                                                 double* s_dE, double* s_r1, double& s_wr) {
   const int tid = threadIdx.x;
   uint32_t wx[4];
-  draw4(A[0].d.seed, A[0].d.stream, move, SLOT_SWAP, wx);
+  draw4_dev(A[0].d.seed, A[0].d.stream, move, SLOT_SWAP, wx);
   int have[kMaxMoved], nh = 0;
   for (int e = 0; e < nm; ++e)
     if (comp_size[A[e].comp] >= A[e].ms) have[nh++] = e;
@@ -208,7 +217,7 @@ __device__ __noinline__ void identity_swap_step(const BoxDev& b, const GcmcArgs*
             if (ao.rigid && ao.charged) same += ao.excl;
             ew = same + 2.0 * cross;
           }
-          rosen *= exp(-beta * ew);
+          rosen *= exp_move(-beta * ew);
           const double pre = beta * an.big_p / (1.0 + (double)Nn) * ((double)No / (beta * ao.big_p));
           const double pacc = pre * (rosen / an.d.ideal_rosenbluth) / (rosen_old / ao.d.ideal_rosenbluth);
           s_accept = u01(wx[3]) < pacc;
@@ -296,9 +305,9 @@ __global__ void __launch_bounds__(NW * 32, 24 / NW) gcmc_kernel(const BoxDev* bo
   for (int64_t step = 0; step < nsb; ++step) {
     const uint64_t move = move0 + (uint64_t)step;
     uint32_t w[4], w2[4], ws[4];
-    draw4(A[0].d.seed, A[0].d.stream, move, SLOT_MOVE, w);
-    draw4(A[0].d.seed, A[0].d.stream, move, SLOT_DISP, w2);
-    draw4(A[0].d.seed, A[0].d.stream, move, SLOT_SELECT, ws);
+    draw4_dev(A[0].d.seed, A[0].d.stream, move, SLOT_MOVE, w);
+    draw4_dev(A[0].d.seed, A[0].d.stream, move, SLOT_DISP, w2);
+    draw4_dev(A[0].d.seed, A[0].d.stream, move, SLOT_SELECT, ws);
     const int sel = nm > 1 ? min(nm - 1, (int)(u01(w2[3]) * (double)nm)) : 0;
     const GcmcArgs& a = A[sel];
     const grx_gcmc_desc& d = a.d;
@@ -353,7 +362,7 @@ __global__ void __launch_bounds__(NW * 32, 24 / NW) gcmc_kernel(const BoxDev* bo
           const double dv = (W.te[0] + W.te[2]) - (W.te[4] + W.te[6]);
           const double dr = (W.te[1] + W.te[3]) - (W.te[5] + W.te[7]);
           const double ew = same + 2.0 * cross;
-          const double pacc = exp(-d.beta * (dv + dr + ew));
+          const double pacc = exp_move(-d.beta * (dv + dr + ew));
           s_accept = uacc < pacc;
           s_dE[0] = dv; s_dE[1] = dr; s_dE[2] = ew;
         }
@@ -447,7 +456,7 @@ __global__ void __launch_bounds__(NW * 32, 24 / NW) gcmc_kernel(const BoxDev* bo
           if (a.charged) ewald_delta_move<PREC, CL>(b, W, 2 * ms, eik, same, cross);
           if (tid == 0) {
             const double ew = a.charged ? same + 2.0 * cross : 0.0;
-            rosen *= exp(-d.beta * ew);
+            rosen *= exp_move(-d.beta * ew);
             const double pacc = rosen / rosen_old;
             s_accept = uacc < pacc;
             s_dE[0] = s_e1[0] + s_e1[2] + e2[0] + e2[2] - (s_r1[0] + s_r1[2] + r2[0] + r2[2]);
@@ -525,8 +534,8 @@ __global__ void __launch_bounds__(NW * 32, 24 / NW) gcmc_kernel(const BoxDev* bo
           }
           double pacc;
           if (!del) {
-            rosen *= exp(-d.beta * ew);
-            rosen *= exp(-d.beta * d.tail_insert);
+            rosen *= exp_move(-d.beta * ew);
+            rosen *= exp_move(-d.beta * d.tail_insert);
             pacc = d.beta * a.big_p / (1.0 + (double)N) * rosen / d.ideal_rosenbluth;
             s_accept = rosen > 1e-150 && uacc < pacc;
             if (s_accept && (N + 1) * ms > a.cap) {
@@ -534,8 +543,8 @@ __global__ void __launch_bounds__(NW * 32, 24 / NW) gcmc_kernel(const BoxDev* bo
               st.capacity_hits++;
             }
           } else {
-            rosen /= exp(-d.beta * ew);
-            rosen /= exp(d.beta * d.tail_insert);  // the deletion's tail difference is -tail_insert
+            rosen /= exp_move(-d.beta * ew);
+            rosen /= exp_move(d.beta * d.tail_insert);  // the deletion's tail difference is -tail_insert
             pacc = (double)N / (d.beta * a.big_p) * d.ideal_rosenbluth / rosen;
             s_accept = uacc < pacc;
           }

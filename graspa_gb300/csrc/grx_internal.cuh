@@ -153,6 +153,22 @@ __host__ __device__ inline void draw4(uint64_t seed, uint32_t stream, uint64_t m
 
 __host__ __device__ inline double u01(uint32_t w) { return (double)w * 2.3283064365386963e-10; }
 
+// Out-of-line forms for the per-move code of the persistent kernels: one copy of the Philox
+// rounds and of the library FP64 exp serves every call site of a kernel. These run once per
+// move, on few lanes, where instruction fetch rather than arithmetic sets the time, so a
+// smaller kernel is a faster one. Results are those of draw4 and exp.
+static __device__ __noinline__ uint4 draw4_out(uint64_t seed, uint32_t stream, uint64_t move, uint32_t slot) {
+  uint32_t w[4];
+  draw4(seed, stream, move, slot, w);
+  return make_uint4(w[0], w[1], w[2], w[3]);
+}
+__device__ __forceinline__ void draw4_dev(uint64_t seed, uint32_t stream, uint64_t move, uint32_t slot,
+                                          uint32_t out[4]) {
+  const uint4 r = draw4_out(seed, stream, move, slot);
+  out[0] = r.x; out[1] = r.y; out[2] = r.z; out[3] = r.w;
+}
+static __device__ __noinline__ double exp_move(double x) { return exp(x); }
+
 enum : uint32_t { SLOT_FIRST = 0u, SLOT_ORIENT = 1024u, SLOT_SELECT = 2048u, SLOT_RETRACE = 3072u };
 
 // ---------------------------------------------------------------- geometry

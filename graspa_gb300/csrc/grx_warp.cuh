@@ -123,8 +123,12 @@ __device__ __forceinline__ df coul_table_df(const BoxDev& b, df s) {
 }
 
 // Cold paths of the mixed-precision pair evaluation, kept out of line so the inlined copies of
-// pair_dense stay small: LJ with a non-unit scaling or the 12-6-4 form, and g(s) outside the
-// Coulomb table's range.
+// pair_dense stay small: LJ inside 1.1 sigma (double-float), LJ with a non-unit scaling or the
+// 12-6-4 form, and g(s) outside the Coulomb table's range.
+static __device__ __noinline__ float2 lj_df_cold(const BoxDev& b, int row, float rhi, float rlo) {
+  const df e = lj_df(b, row, df{rhi, rlo});
+  return make_float2(e.hi, e.lo);
+}
 static __device__ __noinline__ double vdw64_cold(const BoxDev& b, int row, double rr, double scaling) {
   return vdw64(b, row, rr, scaling);
 }
@@ -143,33 +147,30 @@ template <int PREC> __device__ __forceinline__ double acc_value(const LaneAcc<PR
 }
 
 // Dense evaluation of one screened pair: exact cutoff tests, LJ, real Coulomb,
-// overlap flag (VDW_Coulomb.cu:1287-1322). pq = prefactor * q_bead (double-float
-// in the mixed form).
-template <int PREC, bool HOST>
-__device__ __forceinline__ void pair_dense(const BoxDev& b, int i, const Bead& bd, df pq,
-                                           LaneAcc<PREC>& acc, int& flag) {
-  const double4* P64 = HOST ? b.hpos64 : b.pos64;
-  const float4* HI = HOST ? b.hhi : b.hi;
-  const float4* LO = HOST ? b.hlo : b.lo;
-  const double* SC = HOST ? b.hscale : b.scale;
-  const float2* QDF = HOST ? b.hqdf : b.qdf;
-  const int2 mt = (HOST ? b.hmeta : b.meta)[i];
+// overlap flag (VDW_Coulomb.cu:1287-1322). `host`: atom i is a framework (host) atom, else a
+// guest atom; the arrays are selected at run time so that a work item has one inlined copy
+// of this evaluation for both kinds of atoms and for full and final batches (the hot code of
+// a move then fits the instruction cache better).
+template <int PREC>
+__device__ __forceinline__ void pair_dense(const BoxDev& b, bool host, int i, const Bead& bd, LaneAcc<PREC>& acc,
+                                           int& flag) {
+  const int2 mt = (host ? b.hmeta : b.meta)[i];
   const int row = mt.x * b.ntypes + bd.type;
   if constexpr (PREC == GRX_FP64) {
-    const double4 p = P64[i];
+    const double4 p = (host ? b.hpos64 : b.pos64)[i];
     double x = p.x - bd.x, y = p.y - bd.y, z = p.z - bd.z;
     pbc64(b, x, y, z);
     const double rr = x * x + y * y + z * z;
     if (rr < b.cut_vdw2) {
-      const double e = vdw64(b, row, rr, SC[i] * bd.scale);
+      const double e = vdw64(b, row, rr, (host ? b.hscale : b.scale)[i] * bd.scale);
       if (e > b.overlap) flag = 1;
       if (rr < 0.01) flag = 1;
       acc.v += e;
     }
     if (!b.no_charges && rr < b.cut_coul2) acc.r += coul64(b, p.w * bd.q, rr);
   } else {
-    const float4 ah = HI[i];
-    const float4 al = LO[i];
+    const float4 ah = (host ? b.hhi : b.hi)[i];
+    const float4 al = (host ? b.hlo : b.lo)[i];
     float3 dh = make_float3(ah.x - bd.h.x, ah.y - bd.h.y, ah.z - bd.h.z);
     float3 dl = make_float3(al.x - bd.l.x, al.y - bd.l.y, al.z - bd.l.z);
     image_split(b, dh, dl);
@@ -180,8 +181,11 @@ __device__ __forceinline__ void pair_dense(const BoxDev& b, int i, const Bead& b
         const bool unit = (al.w == 1.0f) && bd.unit && !b.use_1264;
         df e;
         if (unit && s.hi > f.w) e = df{vdw32(f, s.hi), 0.0f};
-        else if (unit) e = lj_df(b, row, s);
-        else e = df_from(vdw64_cold(b, row, df_to(s), SC[i] * bd.scale));
+        else if (unit) {
+          const float2 c = lj_df_cold(b, row, s.hi, s.lo);
+          e = df{c.x, c.y};
+        }
+        else e = df_from(vdw64_cold(b, row, df_to(s), (host ? b.hscale : b.scale)[i] * bd.scale));
         if (e.hi > b.overlapf) flag = 1;
         if (s.hi < 0.01f) flag = 1;
         acc.v = df_add(acc.v, e);
@@ -191,7 +195,7 @@ __device__ __forceinline__ void pair_dense(const BoxDev& b, int i, const Bead& b
         const int k = (__float_as_int(s.hi) >> 17) - b.ctab_base;
         if (k >= 0 && k < b.ctab_n) g = coul_table_df(b, s);
         else g = df_from(coul_g_cold(b, df_to(s)));
-        const float2 qa = QDF[i];
+        const float2 qa = (host ? b.hqdf : b.qdf)[i];
         acc.r = df_add(acc.r, df_mul(g, df{qa.x, qa.y}));  // prefactor * q_bead applied once per item
       }
     } else {  // GRX_FP32
@@ -212,8 +216,15 @@ __device__ __forceinline__ void pair_dense(const BoxDev& b, int i, const Bead& b
 }
 
 // One work item: bead `bd` against host units [t0, t1) (tiles, or with VOX 32-entry chunks
-// of the bead's voxel list) and, when `guests`, every live guest atom. acc = {hg_vdw,
-// hg_real, gg_vdw, gg_real} (valid on every lane, summed later); flag is per lane.
+// of the bead's voxel list) and, when g1 > g0, the live guest atoms [g0, g1). hacc / gacc =
+// {vdw, real} of the host and the guest atoms (valid on every lane, summed later); flag is
+// per lane.
+//
+// A generator step screens up to 32 candidates of the current phase (host, then guests) and
+// appends the ones inside the screening radius to the warp's ring buffer. Whenever 32 are
+// queued, or the phase has no candidates left, the warp evaluates the next batch at the one
+// dense site; a phase ends with its buffer drained. Batches are the queue order, so the sums
+// do not depend on how the candidates were produced.
 //
 // Early overlap rejection: with `dead` (the bead's trial's flag in shared memory, null
 // when the trial must be evaluated in full) the warp stops as soon as the trial is known
@@ -237,14 +248,27 @@ __device__ __forceinline__ void warp_item(const BoxDev& b, const Bead& bd, int t
     if (lane == 0) *dead = 1;
     return true;
   };
-  bool stop = false;
-  const df pq = {bd.pq.x, bd.pq.y};
+  auto push = [&](bool in, int i) {
+    const unsigned m = __ballot_sync(kFull, in);
+    if (in) q[(tail + __popc(m & lt)) & (kQueue - 1)] = i;
+    tail += __popc(m);
+  };
   const float bx = bd.h.x + bd.l.x, by = bd.h.y + bd.l.y, bz = bd.h.z + bd.l.z;
-  LaneAcc<PREC>& la = hacc;
+
+  // host generator state. VOX: chunks [ch, cend) of the bead's voxel list; entries below
+  // vm.y are inside the cutoff for every bead of the voxel (queued unscreened), the others are
+  // screened at the stored image against the bead wrapped into the home cell. Tiles: groups of
+  // 32 tiles from `base`, culled one per lane; `mask` holds the group's surviving tiles.
+  int ch = t0, cend = t0;
+  int4 vm = make_int4(0, 0, 0, 0);
+  float wx = 0.f, wy = 0.f, wz = 0.f;
+  bool hcheck = false;
+  int base = t0;
+  unsigned mask = 0;
+  float sx = 0.f, sy = 0.f, sz = 0.f;  // this lane's tile: image shift of the bead
+  bool one_image = false;
+  int4 trl = make_int4(0, 0, -1, 0);   // this lane's tile range, shuffled to the warp below
   if constexpr (VOX) {
-    // Host units are 32-entry chunks of the bead's voxel list (grx_voxel.cu): entries below
-    // vm.y are inside the cutoff for every bead of the voxel and are queued unscreened; the
-    // others are screened at the stored image against the bead wrapped into the home cell.
     if (t1 > t0) {
       const float fx = b.invf[0] * bx + b.invf[3] * by + b.invf[6] * bz;
       const float fy = b.invf[1] * bx + b.invf[4] * by + b.invf[7] * bz;
@@ -253,111 +277,105 @@ __device__ __forceinline__ void warp_item(const BoxDev& b, const Bead& bd, int t
       const int ix = min(b.vn[0] - 1, max(0, (int)((fx - mx) * (float)b.vn[0])));
       const int iy = min(b.vn[1] - 1, max(0, (int)((fy - my) * (float)b.vn[1])));
       const int iz = min(b.vn[2] - 1, max(0, (int)((fz - mz) * (float)b.vn[2])));
-      const int4 vm = b.vmeta[(iz * b.vn[1] + iy) * b.vn[0] + ix];
-      const float wx = bd.h.x - (mx * b.cellf[0] + my * b.cellf[3] + mz * b.cellf[6]);
-      const float wy = bd.h.y - (mx * b.cellf[1] + my * b.cellf[4] + mz * b.cellf[7]);
-      const float wz = bd.h.z - (mx * b.cellf[2] + my * b.cellf[5] + mz * b.cellf[8]);
-      const unsigned* L = b.vlist + vm.x;
-      const bool hcheck = component < b.nhost || (excl_comp >= 0 && excl_comp < b.nhost);
-      const int cend = min(t1, (vm.z + 31) >> 5);
-      for (int ch = t0; ch < cend; ++ch) {
-        if (is_dead()) { stop = true; break; }
-        const int j = (ch << 5) + lane;
-        bool in = false;
-        int i = 0;
-        if (j < vm.z) {
-          const unsigned w = __ldg(L + j);
-          i = (int)(w & 0xFFFFFu);
-          if (j < vm.y) {
-            in = true;
-          } else if (PREC == GRX_FP64) {
-            in = pair_screen<PREC, true>(b, i, bd);
-          } else {
-            const float nx = (float)((int)((w >> 20) & 7u) - 4), ny = (float)((int)((w >> 23) & 7u) - 4),
-                        nz = (float)((int)((w >> 26) & 7u) - 4);
-            const float4 ah = b.hhi[i];
-            const float x = ah.x - wx - (nx * b.cellf[0] + ny * b.cellf[3] + nz * b.cellf[6]);
-            const float y = ah.y - wy - (nx * b.cellf[1] + ny * b.cellf[4] + nz * b.cellf[7]);
-            const float z = ah.z - wz - (nx * b.cellf[2] + ny * b.cellf[5] + nz * b.cellf[8]);
-            in = x * x + y * y + z * z < b.screen2;
-          }
-          if (in && hcheck) {  // a host component is moved or excluded: skip its molecule
-            int tz = 0;
-            while (tz + 1 < b.nhost && i >= b.comp_off[tz + 1]) ++tz;
-            const int mol = b.hmeta[i].y;
-            if ((tz == excl_comp && mol == excl_mol) || (tz == component && mol == newmol)) in = false;
-          }
-        }
-        const unsigned m = __ballot_sync(kFull, in);
-        if (in) q[(tail + __popc(m & lt)) & (kQueue - 1)] = i;
-        tail += __popc(m);
-        if (tail - head >= 32) {
-          __syncwarp();
-          const int jq = q[(head + lane) & (kQueue - 1)];
-          __syncwarp();
-          pair_dense<PREC, true>(b, jq, bd, pq, la, flag);
-          head += 32;
-          if (found_overlap()) { stop = true; break; }
-        }
-      }
+      vm = b.vmeta[(iz * b.vn[1] + iy) * b.vn[0] + ix];
+      wx = bd.h.x - (mx * b.cellf[0] + my * b.cellf[3] + mz * b.cellf[6]);
+      wy = bd.h.y - (mx * b.cellf[1] + my * b.cellf[4] + mz * b.cellf[7]);
+      wz = bd.h.z - (mx * b.cellf[2] + my * b.cellf[5] + mz * b.cellf[8]);
+      hcheck = component < b.nhost || (excl_comp >= 0 && excl_comp < b.nhost);
+      cend = min(t1, (vm.z + 31) >> 5);
     }
-  } else {
-  // Tiles are tested 32 at a time, one per lane; survivors are then screened one
-  // tile at a time by the whole warp. When a tile lies inside one periodic image of
-  // the bead (stored positions compact, the tile sphere clear of the rounding
-  // boundaries), the image shift is applied once to the bead instead of per atom.
-  for (int base = t0; base < t1 && !stop; base += 32) {
-    const int tl = base + lane;
-    bool pass = tl < t1;
-    float sx = 0.f, sy = 0.f, sz = 0.f;  // image shift of the bead for this tile
-    bool one_image = false;
-    int4 trl = make_int4(0, 0, -1, 0);   // this lane's tile range, shuffled to the warp below
-    if (pass) trl = b.tile_r[tl];
-    if (pass && b.cull) {
-      const float4 tc = b.tile_c[2 * tl];
-      float dx = tc.x - bx, dy = tc.y - by, dz = tc.z - bz;
-      const float lim = b.cull_r + tc.w;
-      const float m = tc.w + 1e-2f;
-      if (b.cubic) {
-        // Bounding box of the tile at the centre's rounded image. Per axis the distance to
-        // the box bounds every atom's rounded-image distance from below: an atom whose
-        // rounding differs from the centre's lies at least half a cell minus the half
-        // extent away on that axis.
-        const float4 th = b.tile_c[2 * tl + 1];
-        const float nx = rnd(dx * b.invf[0]), ny = rnd(dy * b.invf[4]), nz = rnd(dz * b.invf[8]);
-        dx = __fmaf_rn(-nx, b.cellf[0], dx);
-        dy = __fmaf_rn(-ny, b.cellf[4], dy);
-        dz = __fmaf_rn(-nz, b.cellf[8], dz);
-        const float qx = fmaxf(fabsf(dx) - th.x, 0.f), qy = fmaxf(fabsf(dy) - th.y, 0.f),
-                    qz = fmaxf(fabsf(dz) - th.z, 0.f);
-        pass = qx * qx + qy * qy + qz * qz <= b.cull_r * b.cull_r;
-        one_image = trl.w != 0 && fabsf(dx) + th.x + 1e-2f < 0.5f * b.cellf[0] &&
-                    fabsf(dy) + th.y + 1e-2f < 0.5f * b.cellf[4] && fabsf(dz) + th.z + 1e-2f < 0.5f * b.cellf[8];
-        sx = nx * b.cell_hi[0]; sy = ny * b.cell_hi[4]; sz = nz * b.cell_hi[8];
-      } else {
-        const float fx = b.invf[0] * dx + b.invf[3] * dy + b.invf[6] * dz;
-        const float fy = b.invf[1] * dx + b.invf[4] * dy + b.invf[7] * dz;
-        const float fz = b.invf[2] * dx + b.invf[5] * dy + b.invf[8] * dz;
-        const float nx = rnd(fx), ny = rnd(fy), nz = rnd(fz);
-        sx = nx * b.cellf[0] + ny * b.cellf[3] + nz * b.cellf[6];
-        sy = nx * b.cellf[1] + ny * b.cellf[4] + nz * b.cellf[7];
-        sz = nx * b.cellf[2] + ny * b.cellf[5] + nz * b.cellf[8];
-        dx -= sx; dy -= sy; dz -= sz;
-        const float d2 = dx * dx + dy * dy + dz * dz;
-        const float rx = fabsf(fx - nx), ry = fabsf(fy - ny), rz = fabsf(fz - nz);
-        if (d2 <= b.half_wmin2) {
-          pass = d2 <= lim * lim;
+  }
+  // one host step: screen the next chunk / surviving tile; false when none is left
+  auto host_step = [&]() -> bool {
+    if constexpr (VOX) {
+      if (ch >= cend) return false;
+      const int j = (ch << 5) + lane;
+      ++ch;
+      bool in = false;
+      int i = 0;
+      if (j < vm.z) {
+        const unsigned w = __ldg(b.vlist + vm.x + j);
+        i = (int)(w & 0xFFFFFu);
+        if (j < vm.y) {
+          in = true;
+        } else if (PREC == GRX_FP64) {
+          in = pair_screen<PREC, true>(b, i, bd);
         } else {
-          const float lb = fmaxf(fmaxf(rx * b.wperp[0], ry * b.wperp[1]), rz * b.wperp[2]);
-          pass = lb - 1e-3f <= lim;
+          const float nx = (float)((int)((w >> 20) & 7u) - 4), ny = (float)((int)((w >> 23) & 7u) - 4),
+                      nz = (float)((int)((w >> 26) & 7u) - 4);
+          const float4 ah = b.hhi[i];
+          const float x = ah.x - wx - (nx * b.cellf[0] + ny * b.cellf[3] + nz * b.cellf[6]);
+          const float y = ah.y - wy - (nx * b.cellf[1] + ny * b.cellf[4] + nz * b.cellf[7]);
+          const float z = ah.z - wz - (nx * b.cellf[2] + ny * b.cellf[5] + nz * b.cellf[8]);
+          in = x * x + y * y + z * z < b.screen2;
         }
-        one_image = trl.w != 0 && rx + m / b.wperp[0] < 0.5f - 1e-4f &&
-                    ry + m / b.wperp[1] < 0.5f - 1e-4f && rz + m / b.wperp[2] < 0.5f - 1e-4f;
+        if (in && hcheck) {  // a host component is moved or excluded: skip its molecule
+          int tz = 0;
+          while (tz + 1 < b.nhost && i >= b.comp_off[tz + 1]) ++tz;
+          const int mol = b.hmeta[i].y;
+          if ((tz == excl_comp && mol == excl_mol) || (tz == component && mol == newmol)) in = false;
+        }
       }
-    }
-    unsigned mask = __ballot_sync(kFull, pass);
-    while (mask) {
-      if (is_dead()) { stop = true; break; }
+      push(in, i);
+      return true;
+    } else {
+      // Tiles are tested 32 at a time, one per lane; survivors are then screened one tile at
+      // a time by the whole warp. When a tile lies inside one periodic image of the bead
+      // (stored positions compact, the tile sphere clear of the rounding boundaries), the
+      // image shift is applied once to the bead instead of per atom.
+      while (mask == 0) {
+        if (base >= t1) return false;
+        const int tl = base + lane;
+        base += 32;
+        bool pass = tl < t1;
+        sx = sy = sz = 0.f;
+        one_image = false;
+        trl = make_int4(0, 0, -1, 0);
+        if (pass) trl = b.tile_r[tl];
+        if (pass && b.cull) {
+          const float4 tc = b.tile_c[2 * tl];
+          float dx = tc.x - bx, dy = tc.y - by, dz = tc.z - bz;
+          const float lim = b.cull_r + tc.w;
+          const float m = tc.w + 1e-2f;
+          if (b.cubic) {
+            // Bounding box of the tile at the centre's rounded image. Per axis the distance to
+            // the box bounds every atom's rounded-image distance from below: an atom whose
+            // rounding differs from the centre's lies at least half a cell minus the half
+            // extent away on that axis.
+            const float4 th = b.tile_c[2 * tl + 1];
+            const float nx = rnd(dx * b.invf[0]), ny = rnd(dy * b.invf[4]), nz = rnd(dz * b.invf[8]);
+            dx = __fmaf_rn(-nx, b.cellf[0], dx);
+            dy = __fmaf_rn(-ny, b.cellf[4], dy);
+            dz = __fmaf_rn(-nz, b.cellf[8], dz);
+            const float qx = fmaxf(fabsf(dx) - th.x, 0.f), qy = fmaxf(fabsf(dy) - th.y, 0.f),
+                        qz = fmaxf(fabsf(dz) - th.z, 0.f);
+            pass = qx * qx + qy * qy + qz * qz <= b.cull_r * b.cull_r;
+            one_image = trl.w != 0 && fabsf(dx) + th.x + 1e-2f < 0.5f * b.cellf[0] &&
+                        fabsf(dy) + th.y + 1e-2f < 0.5f * b.cellf[4] && fabsf(dz) + th.z + 1e-2f < 0.5f * b.cellf[8];
+            sx = nx * b.cell_hi[0]; sy = ny * b.cell_hi[4]; sz = nz * b.cell_hi[8];
+          } else {
+            const float fx = b.invf[0] * dx + b.invf[3] * dy + b.invf[6] * dz;
+            const float fy = b.invf[1] * dx + b.invf[4] * dy + b.invf[7] * dz;
+            const float fz = b.invf[2] * dx + b.invf[5] * dy + b.invf[8] * dz;
+            const float nx = rnd(fx), ny = rnd(fy), nz = rnd(fz);
+            sx = nx * b.cellf[0] + ny * b.cellf[3] + nz * b.cellf[6];
+            sy = nx * b.cellf[1] + ny * b.cellf[4] + nz * b.cellf[7];
+            sz = nx * b.cellf[2] + ny * b.cellf[5] + nz * b.cellf[8];
+            dx -= sx; dy -= sy; dz -= sz;
+            const float d2 = dx * dx + dy * dy + dz * dz;
+            const float rx = fabsf(fx - nx), ry = fabsf(fy - ny), rz = fabsf(fz - nz);
+            if (d2 <= b.half_wmin2) {
+              pass = d2 <= lim * lim;
+            } else {
+              const float lb = fmaxf(fmaxf(rx * b.wperp[0], ry * b.wperp[1]), rz * b.wperp[2]);
+              pass = lb - 1e-3f <= lim;
+            }
+            one_image = trl.w != 0 && rx + m / b.wperp[0] < 0.5f - 1e-4f &&
+                        ry + m / b.wperp[1] < 0.5f - 1e-4f && rz + m / b.wperp[2] < 0.5f - 1e-4f;
+          }
+        }
+        mask = __ballot_sync(kFull, pass);
+      }
       const int src = __ffs(mask) - 1;
       mask &= mask - 1;
       const int i = __shfl_sync(kFull, trl.x, src) + lane, tz = __shfl_sync(kFull, trl.z, src);
@@ -383,63 +401,68 @@ __device__ __forceinline__ void warp_item(const BoxDev& b, const Bead& bd, int t
           }
         }
       }
-      const unsigned m = __ballot_sync(kFull, in);
-      if (in) q[(tail + __popc(m & lt)) & (kQueue - 1)] = i;
-      tail += __popc(m);
-      if (tail - head >= 32) {
-        __syncwarp();
-        const int j = q[(head + lane) & (kQueue - 1)];
-        __syncwarp();
-        pair_dense<PREC, true>(b, j, bd, pq, la, flag);
-        head += 32;
-        if (found_overlap()) { stop = true; break; }
-      }
+      push(in, i);
+      return true;
+    }
+  };
+  // one batch at the phase's dense site: 32 queued pairs, or the final ones when the phase has
+  // no candidates left (got false); true when the warp must stop (the trial overlaps)
+  auto batch = [&](bool host, bool got, LaneAcc<PREC>& acc) -> bool {
+    const unsigned avail = tail - head;
+    if (avail >= 32u || (!got && avail > 0u)) {
+      const int n = (int)min(avail, 32u);
+      __syncwarp();
+      const int j = q[(head + lane) & (kQueue - 1)];  // entries past n are stale and unused
+      __syncwarp();
+      if (lane < n) pair_dense<PREC>(b, host, j, bd, acc, flag);
+      head += (unsigned)n;
+      if (found_overlap()) return true;
+    }
+    return false;
+  };
+  if (t1 > t0) {
+    for (;;) {
+      if (is_dead()) return;
+      const bool got = host_step();
+      if (batch(true, got, hacc)) return;
+      if (!got && tail == head) break;
     }
   }
-  }
-  if (stop) return;
-  __syncwarp();
-  if (lane < (int)(tail - head)) pair_dense<PREC, true>(b, q[(head + lane) & (kQueue - 1)], bd, pq, la, flag);
-  __syncwarp();
-  if (g1 <= g0 || found_overlap()) return;
+  if (g1 <= g0) return;
   head = tail = 0;
-  // guest atoms [g0, g1) of the concatenated adsorbate components
-  for (int c = b.nhost, base = 0; c < b.ncomp && base < g1; ++c) {
-    const int n = b.comp_size[c];
-    const int off = b.comp_off[c];
-    const int lo = max(g0 - base, 0), hi = min(g1 - base, n);
-    base += n;
-    if (hi <= lo) continue;
-    const bool check = (c == component) || (c == excl_comp);
-    for (int i0 = lo; i0 < hi; i0 += 32) {
-      if (is_dead()) return;
-      const int i = off + i0 + lane;
+  // guest atoms [g0, g1) of the concatenated adsorbate components: component gc, its atoms
+  // [gi, ghi) still to screen (indices within the component), gbase = the first concatenated
+  // guest index after gc
+  int gc = b.nhost, gbase = 0, gi = 0, ghi = 0;
+  for (;;) {
+    if (is_dead()) return;
+    bool got = false;
+    while (gi >= ghi && gc < b.ncomp && gbase < g1) {  // next component overlapping [g0, g1)
+      const int n = b.comp_size[gc];
+      gi = max(g0 - gbase, 0);
+      ghi = min(g1 - gbase, n);
+      gbase += n;
+      ++gc;
+    }
+    if (gi < ghi) {
+      const int c = gc - 1;
+      const int i = b.comp_off[c] + gi + lane;
       bool in = false;
-      if (i0 + lane < hi) {
+      if (gi + lane < ghi) {
         bool skip = false;
-        if (check) {
+        if (c == component || c == excl_comp) {
           const int mol = b.meta[i].y;
           skip = (c == excl_comp && mol == excl_mol) || (c == component && mol == newmol);
         }
         if (!skip) in = pair_screen<PREC, false>(b, i, bd);
       }
-      const unsigned m = __ballot_sync(kFull, in);
-      if (in) q[(tail + __popc(m & lt)) & (kQueue - 1)] = i;
-      tail += __popc(m);
-      if (tail - head >= 32) {
-        __syncwarp();
-        const int j = q[(head + lane) & (kQueue - 1)];
-        __syncwarp();
-        pair_dense<PREC, false>(b, j, bd, pq, gacc, flag);
-        head += 32;
-        if (found_overlap()) return;
-      }
+      gi += 32;
+      push(in, i);
+      got = true;
     }
+    if (batch(false, got, gacc)) return;
+    if (!got && tail == head) return;
   }
-  __syncwarp();
-  if (lane < (int)(tail - head)) pair_dense<PREC, false>(b, q[(head + lane) & (kQueue - 1)], bd, pq, gacc, flag);
-  __syncwarp();
-  found_overlap();
 }
 
 // Fixed-order warp sums (lane 0 receives the total). The double-float form keeps the
@@ -449,7 +472,22 @@ __device__ __forceinline__ double warp_sum(double x) {
   return x;
 }
 
+// Out of line: called once per work item and per Ewald delta, so one copy serves them all.
+static __device__ __noinline__ float2 warp_sum_df_out(float hi, float lo) {
+  df x = {hi, lo};
+  for (int o = 16; o > 0; o >>= 1) {
+    const df y = {__shfl_down_sync(kFull, x.hi, o), __shfl_down_sync(kFull, x.lo, o)};
+    x = df_add(x, y);
+  }
+  return make_float2(x.hi, x.lo);
+}
+
 __device__ __forceinline__ df warp_sum_df(df x) {
+  const float2 r = warp_sum_df_out(x.hi, x.lo);
+  return df{r.x, r.y};
+}
+
+__device__ __forceinline__ df warp_sum_df_inl(df x) {
   for (int o = 16; o > 0; o >>= 1) {
     const df y = {__shfl_down_sync(kFull, x.hi, o), __shfl_down_sync(kFull, x.lo, o)};
     x = df_add(x, y);
@@ -651,9 +689,11 @@ __device__ __forceinline__ void reduce_items(const double* ipart, const int* ifl
     int f = 0;
     if constexpr (PREC == GRX_MIXED) {
       df s = {0.f, 0.f};
+#pragma unroll 1
       for (int a = 0; a < chain; ++a) {
         int s0, s1;
         bead_slots(sp, t * chain + a, s0, s1);
+#pragma unroll 1
         for (int c = s0; c <= s1; ++c) {
           const float2 v = reinterpret_cast<const float2*>(ipart)[c * 4 + k];
           s = df_add(s, df{v.x, v.y});
@@ -663,9 +703,11 @@ __device__ __forceinline__ void reduce_items(const double* ipart, const int* ifl
       te[4 * t + k] = df_to(s);
     } else {
       double s = 0.0;
+#pragma unroll 1
       for (int a = 0; a < chain; ++a) {
         int s0, s1;
         bead_slots(sp, t * chain + a, s0, s1);
+#pragma unroll 1
         for (int c = s0; c <= s1; ++c) {
           s += ipart[c * 4 + k];
           f |= iflag[c];
