@@ -335,8 +335,8 @@ __device__ __noinline__ void ewald_move(const BoxDev& b, WK& W, int na, double2*
           tab[at + k * na] = e;
         }
       }
-    } else {  // straight into the double-float tables read below (after the FP64 ones)
-      float4* f0 = reinterpret_cast<float4*>(ez + (b.kmax[2] + 1) * na);
+    } else {  // straight into the double-float tables read below (the FP64 ones are not used)
+      float4* f0 = reinterpret_cast<float4*>(eik);
       float4* tab = f0 + (d == 0 ? 0 : (d == 1 ? kx1 * na : (kx1 + ky1) * na));
       df_eik_row(f, km, tab + at, na);
     }
@@ -369,7 +369,7 @@ __device__ __noinline__ void ewald_move(const BoxDev& b, WK& W, int na, double2*
     same = block_sum(same, W.sbuf);
     cross = block_sum(cross, W.sbuf);
   } else {
-    float4* fx = reinterpret_cast<float4*>(ez + (b.kmax[2] + 1) * na);
+    float4* fx = reinterpret_cast<float4*>(eik);
     const int ntab = (b.kmax[0] + b.kmax[1] + b.kmax[2] + 3) * na;
     if (tid < na) { const df q = df_from(W.mq[tid]); W.qd[tid] = make_float2(q.hi, q.lo); }
     __syncthreads();

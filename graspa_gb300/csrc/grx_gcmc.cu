@@ -93,7 +93,7 @@ static bool has_swaps(const grx_gcmc_desc* descs, int n) {
 // Validates the boxes and move sets and fills the per-box state and per-entry args.
 static grx_status prepare_gcmc(grx_box* const* boxes, int32_t nboxes, const grx_gcmc_desc* descs,
                                const int32_t* ncomp_moved, std::vector<BoxDev>& hb, std::vector<GcmcArgs>& ha,
-                               std::vector<int>& first, size_t& smem, int chunk_mult) {
+                               std::vector<int>& first, size_t& smem, int chunk_mult, grx_precision prec) {
   GRX_REQUIRE(boxes && descs && nboxes >= 1, "grx_gcmc: bad argument");
   hb.assign(nboxes, BoxDev{});
   ha.clear();
@@ -149,8 +149,10 @@ static grx_status prepare_gcmc(grx_box* const* boxes, int32_t nboxes, const grx_
       a.step_off = 0;
       a.nsteps_cap = -1;
       ha.push_back(a);
+      // eik tables of the moved atoms: FP64 (double2) in the FP64 form, double-float (float4)
+      // in the others
       size_t need = (size_t)(b->dev.kmax[0] + b->dev.kmax[1] + b->dev.kmax[2] + 3) * 2 * ms *
-                    (sizeof(double2) + sizeof(float4));
+                    (prec == GRX_FP64 ? sizeof(double2) : sizeof(float4));
       if (b->dev.ew_rows) need += (size_t)ew_rows(b->dev.kmax) * 2 * msmax * sizeof(float4);
       smem = std::max(smem, need);
     }
@@ -286,7 +288,8 @@ extern "C" grx_status grx_gcmc_run(grx_box* const* boxes, int32_t nboxes, const 
   std::vector<GcmcArgs> ha;
   std::vector<int> first;
   size_t smem = 0;
-  grx_status st = prepare_gcmc(boxes, nboxes, descs, ncomp_moved, hb, ha, first, smem, boxes[0]->dev.chunk_mult);
+  grx_status st =
+      prepare_gcmc(boxes, nboxes, descs, ncomp_moved, hb, ha, first, smem, boxes[0]->dev.chunk_mult, prec);
   if (st) return st;
   const int ne = first[nboxes];
   grx_box* b0 = boxes[0];
@@ -343,7 +346,7 @@ extern "C" grx_status grx_gcmc_batch_create(grx_box* const* boxes, int32_t nboxe
   B->prec = prec;
   std::vector<BoxDev> hb;
   std::vector<GcmcArgs> ha;
-  grx_status st = prepare_gcmc(boxes, nboxes, descs, ncomp_moved, hb, ha, B->first, B->smem, B->chunk_mult);
+  grx_status st = prepare_gcmc(boxes, nboxes, descs, ncomp_moved, hb, ha, B->first, B->smem, B->chunk_mult, prec);
   if (st) { delete B; return st; }
   B->nentries = B->first[nboxes];
   B->h_args = ha;
