@@ -135,6 +135,8 @@ void refresh_dev(grx_box* b) {
   d.hmeta = h->meta;
   d.hscale = h->scale;
   d.hqdf = h->qdf;
+  d.hrec = h->hrec;
+  d.htype = h->htype;
   d.shared_host = b->parent ? 1 : 0;
   d.vox = h->vox_on;
   d.vmeta = h->vmeta;
@@ -645,6 +647,9 @@ static grx_status box_create(const grx_box_desc* desc, grx_arena* arena, grx_box
   if ((e = dev_alloc(b, (void**)&b->ffdf, nt2 * sizeof(float4))) != cudaSuccess) return fail(e, "alloc ffdf");
   if ((e = dev_alloc(b, (void**)&b->ffdf2, nt2 * sizeof(float2))) != cudaSuccess) return fail(e, "alloc ffdf2");
   if ((e = dev_alloc(b, (void**)&b->qdf, n * sizeof(float2))) != cudaSuccess) return fail(e, "alloc qdf");
+  const size_t nh = std::max<size_t>(b->off[b->nhost], 1);
+  if ((e = dev_alloc(b, (void**)&b->hrec, 2 * nh * sizeof(float4))) != cudaSuccess) return fail(e, "alloc hrec");
+  if ((e = dev_alloc(b, (void**)&b->htype, nh * sizeof(uint16_t))) != cudaSuccess) return fail(e, "alloc htype");
   const size_t nv = std::max(b->nvec, 1), na = std::max(b->nact, 1);
   if ((e = dev_alloc(b, (void**)&b->kact, na * sizeof(int4))) != cudaSuccess) return fail(e, "alloc kact");
   if ((e = dev_alloc(b, (void**)&b->ktemp, na * sizeof(double))) != cudaSuccess) return fail(e, "alloc ktemp");
@@ -670,6 +675,8 @@ static grx_status box_create(const grx_box_desc* desc, grx_arena* arena, grx_box
   cudaMemcpy(b->ffdf, fdf.data(), nt2 * sizeof(float4), cudaMemcpyHostToDevice);
   cudaMemcpy(b->ffdf2, fdf2.data(), nt2 * sizeof(float2), cudaMemcpyHostToDevice);
   cudaMemset(b->qdf, 0, n * sizeof(float2));
+  cudaMemset(b->hrec, 0, 2 * nh * sizeof(float4));
+  cudaMemset(b->htype, 0, nh * sizeof(uint16_t));
   if (b->nact) {
     cudaMemcpy(b->kact, b->h_kact.data(), b->nact * sizeof(int4), cudaMemcpyHostToDevice);
     cudaMemcpy(b->ktemp, b->h_ktemp.data(), b->nact * sizeof(double), cudaMemcpyHostToDevice);
@@ -691,11 +698,15 @@ grx_status grx_box_footprint(const grx_box_desc* desc, size_t* bytes) {
   GRX_REQUIRE(desc && bytes, "grx_box_footprint: null argument");
   GRX_REQUIRE(desc->ncomponents >= 1 && desc->ncomponents <= GRX_MAX_COMPONENTS, "grx_box_footprint: bad components");
   auto al = [](size_t n) { return (n + 255) / 256 * 256; };
-  size_t acc = 0, ntiles = 0;
+  size_t acc = 0, ntiles = 0, nh = 0;
   for (int c = 0; c < desc->ncomponents; ++c) {
     acc += (desc->capacity[c] + 31) / 32 * 32;
-    if (c < desc->nhost_components) ntiles += (desc->capacity[c] + 31) / 32;
+    if (c < desc->nhost_components) {
+      ntiles += (desc->capacity[c] + 31) / 32;
+      nh += (desc->capacity[c] + 31) / 32 * 32;
+    }
   }
+  nh = std::max<size_t>(nh, 1);
   const size_t n = std::max<size_t>(acc, 32);
   const size_t nt2 = (size_t)desc->forcefield.ntypes * desc->forcefield.ntypes;
   grx_box tmp;
@@ -707,6 +718,7 @@ grx_status grx_box_footprint(const grx_box_desc* desc, size_t* bytes) {
   t += al(na * sizeof(int4)) + al(na * sizeof(double)) + 3 * al(nv * sizeof(double2)) + 2 * al(na * sizeof(float4)) +
        al(na * sizeof(float2));
   t += al(ntiles * sizeof(float4)) + al(ntiles * sizeof(int4));
+  t += al(2 * nh * sizeof(float4)) + al(nh * sizeof(uint16_t));  // host atom records
 
   if (!desc->forcefield.no_charges) {
     const float s_lo = 0.25f, s_hi = (float)(desc->forcefield.cutoff_coul_sq * (1.0 + 1e-4) + 1e-2);
@@ -801,7 +813,7 @@ grx_status grx_box_destroy(grx_box* b) {
   void* ptrs[] = {b->pos64, b->hi, b->lo, b->meta, b->scale, b->charge, b->d_size, b->ff64,
                   b->ffc10, b->ff32, b->kact, b->ktemp, b->s_fw, b->s_ads, b->s_tmp,
                   b->scratch, b->d_results, b->tile_c, b->tile_r, b->ctab, b->ctabf, b->qdf,
-                  b->ffdf, b->ffdf2, b->ewA, b->ewF, b->ewT, b->vmeta, b->vlist};
+                  b->ffdf, b->ffdf2, b->ewA, b->ewF, b->ewT, b->vmeta, b->vlist, b->hrec, b->htype};
   for (void* p : ptrs) dev_free(b, p);
   if (b->pinned) cudaFreeHost(b->pinned);
   delete b;
@@ -917,6 +929,19 @@ grx_status grx_box_set_component(grx_box* b, int32_t comp, const grx_atoms* a, i
     GRX_CHECK_CUDA(cudaMemcpy(b->scale + o, sc.data(), nst * sizeof(double), cudaMemcpyHostToDevice), "upload scale");
     GRX_CHECK_CUDA(cudaMemcpy(b->charge + o, q.data(), nst * sizeof(double), cudaMemcpyHostToDevice), "upload charge");
     GRX_CHECK_CUDA(cudaMemcpy(b->qdf + o, qd.data(), nst * sizeof(float2), cudaMemcpyHostToDevice), "upload qdf");
+    if (comp < b->nhost) {  // the pair engine's host records
+      std::vector<float4> rec(2 * nst);
+      std::vector<uint16_t> ht(nst);
+      for (size_t i = 0; i < nst; ++i) {
+        rec[2 * i] = make_float4(h[i].x, h[i].y, h[i].z, qd[i].x);
+        rec[2 * i + 1] = make_float4(l[i].x, l[i].y, l[i].z, qd[i].y);
+        ht[i] = (uint16_t)(m[i].x | (sc[i] != 1.0 ? 0x8000 : 0));
+      }
+      GRX_CHECK_CUDA(cudaMemcpy(b->hrec + 2 * o, rec.data(), 2 * nst * sizeof(float4), cudaMemcpyHostToDevice),
+                     "upload host records");
+      GRX_CHECK_CUDA(cudaMemcpy(b->htype + o, ht.data(), nst * sizeof(uint16_t), cudaMemcpyHostToDevice),
+                     "upload host types");
+    }
   }
   GRX_CHECK_CUDA(cudaMemcpy(b->d_size, b->size, GRX_MAX_COMPONENTS * sizeof(int), cudaMemcpyHostToDevice),
                  "upload sizes");

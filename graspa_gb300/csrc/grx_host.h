@@ -71,6 +71,11 @@ struct grx_box {
   uint32_t* vlist = nullptr;
   // double-float copies for the mixed-precision pair path
   float2* qdf = nullptr;     // q * scaleCoul per atom as hi/lo floats
+  // host (framework) atoms [0, off[nhost]) as the pair engine reads them: two float4 per atom,
+  // {x_hi, y_hi, z_hi, q_hi} {x_lo, y_lo, z_lo, q_lo}, and the type with bit 15 set when the
+  // atom's scale is not 1 (replicas use the parent's)
+  float4* hrec = nullptr;
+  uint16_t* htype = nullptr;
   float4* ffdf = nullptr;    // per type pair {4eps hi, lo, 1/sigma^2 hi, lo}
   float2* ffdf2 = nullptr;   // per type pair {shift hi, lo}
   float4* ctabf = nullptr;   // Coulomb table, 4 float4 per piece

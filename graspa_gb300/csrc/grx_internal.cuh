@@ -78,6 +78,8 @@ struct BoxDev {
   const int4* tile_r;    // {first atom, end atom, component, 0}
   int ntiles;
   // voxel candidate lists of host atoms (grx_voxel.cu); used instead of the tiles when vox
+  const float4* hrec;            // host atoms: {hi xyz, q hi}, {lo xyz, q lo} per atom
+  const unsigned short* htype;   // host atoms: type | 0x8000 when scale != 1
   const int4* vmeta;     // per voxel {first entry, sure atoms, all atoms, 0}
   const unsigned* vlist; // entries: storage index | lattice shift << 20
   int vox;

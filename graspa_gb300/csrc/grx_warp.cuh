@@ -91,7 +91,7 @@ __device__ __forceinline__ bool pair_screen(const BoxDev& b, int i, const Bead& 
     const double rr = x * x + y * y + z * z;
     return rr < b.cut_vdw2 || (!b.no_charges && rr < b.cut_coul2);
   } else {
-    return screen_hi(b, (HOST ? b.hhi : b.hi)[i], bd);
+    return screen_hi(b, HOST ? b.hrec[2 * i] : b.hi[i], bd);
   }
 }
 
@@ -154,9 +154,8 @@ template <int PREC> __device__ __forceinline__ double acc_value(const LaneAcc<PR
 template <int PREC>
 __device__ __forceinline__ void pair_dense(const BoxDev& b, bool host, int i, const Bead& bd, LaneAcc<PREC>& acc,
                                            int& flag) {
-  const int2 mt = (host ? b.hmeta : b.meta)[i];
-  const int row = mt.x * b.ntypes + bd.type;
   if constexpr (PREC == GRX_FP64) {
+    const int row = (host ? b.hmeta : b.meta)[i].x * b.ntypes + bd.type;
     const double4 p = (host ? b.hpos64 : b.pos64)[i];
     double x = p.x - bd.x, y = p.y - bd.y, z = p.z - bd.z;
     pbc64(b, x, y, z);
@@ -169,8 +168,27 @@ __device__ __forceinline__ void pair_dense(const BoxDev& b, bool host, int i, co
     }
     if (!b.no_charges && rr < b.cut_coul2) acc.r += coul64(b, p.w * bd.q, rr);
   } else {
-    const float4 ah = (host ? b.hhi : b.hi)[i];
-    const float4 al = (host ? b.hlo : b.lo)[i];
+    // host atoms from their records (one 32-byte sector: split position and charge, plus the
+    // 2-byte type); guest atoms from the per-field arrays
+    float4 ah, al;
+    int ty;
+    bool sc1;  // the atom's scale is 1
+    float2 qa;
+    if (host) {
+      ah = b.hrec[2 * i];
+      al = b.hrec[2 * i + 1];
+      const unsigned t = b.htype[i];
+      ty = (int)(t & 0x7fffu);
+      sc1 = !(t & 0x8000u);
+      qa = make_float2(ah.w, al.w);
+    } else {
+      ah = b.hi[i];
+      al = b.lo[i];
+      ty = b.meta[i].x;
+      sc1 = al.w == 1.0f;
+      qa = b.qdf[i];
+    }
+    const int row = ty * b.ntypes + bd.type;
     float3 dh = make_float3(ah.x - bd.h.x, ah.y - bd.h.y, ah.z - bd.h.z);
     float3 dl = make_float3(al.x - bd.l.x, al.y - bd.l.y, al.z - bd.l.z);
     image_split(b, dh, dl);
@@ -178,7 +196,7 @@ __device__ __forceinline__ void pair_dense(const BoxDev& b, bool host, int i, co
       const df s = df_norm2_split(dh, dl);
       if (df_lt(s, df{b.cut_vdw2_df.x, b.cut_vdw2_df.y})) {
         const float4 f = b.ff32[row];
-        const bool unit = (al.w == 1.0f) && bd.unit && !b.use_1264;
+        const bool unit = sc1 && bd.unit && !b.use_1264;
         df e;
         if (unit && s.hi > f.w) e = df{vdw32(f, s.hi), 0.0f};
         else if (unit) {
@@ -195,14 +213,13 @@ __device__ __forceinline__ void pair_dense(const BoxDev& b, bool host, int i, co
         const int k = (__float_as_int(s.hi) >> 17) - b.ctab_base;
         if (k >= 0 && k < b.ctab_n) g = coul_table_df(b, s);
         else g = df_from(coul_g_cold(b, df_to(s)));
-        const float2 qa = (host ? b.hqdf : b.qdf)[i];
         acc.r = df_add(acc.r, df_mul(g, df{qa.x, qa.y}));  // prefactor * q_bead applied once per item
       }
     } else {  // GRX_FP32
       const float fx = dh.x + dl.x, fy = dh.y + dl.y, fz = dh.z + dl.z;
       const float rr32 = fx * fx + fy * fy + fz * fz;
       if (rr32 < b.cut_vdw2f) {
-        const float sc = al.w * (float)bd.scale;
+        const float sc = (host ? (sc1 ? 1.0f : (float)b.hscale[i]) : al.w) * (float)bd.scale;
         float e;
         if (sc == 1.0f && !b.use_1264) e = vdw32(b.ff32[row], rr32);
         else e = (float)vdw64(b, row, (double)rr32, (double)sc);
@@ -303,7 +320,7 @@ __device__ __forceinline__ void warp_item(const BoxDev& b, const Bead& bd, int t
         } else {
           const float nx = (float)((int)((w >> 20) & 7u) - 4), ny = (float)((int)((w >> 23) & 7u) - 4),
                       nz = (float)((int)((w >> 26) & 7u) - 4);
-          const float4 ah = b.hhi[i];
+          const float4 ah = b.hrec[2 * i];
           const float x = ah.x - wx - (nx * b.cellf[0] + ny * b.cellf[3] + nz * b.cellf[6]);
           const float y = ah.y - wy - (nx * b.cellf[1] + ny * b.cellf[4] + nz * b.cellf[7]);
           const float z = ah.z - wz - (nx * b.cellf[2] + ny * b.cellf[5] + nz * b.cellf[8]);
@@ -391,7 +408,7 @@ __device__ __forceinline__ void warp_item(const BoxDev& b, const Bead& bd, int t
         }
         if (!skip) {
           if (PREC != GRX_FP64 && oi) {
-            const float4 ah = b.hhi[i];
+            const float4 ah = b.hrec[2 * i];
             const float x = ah.x - (bd.h.x + tsx);
             const float y = ah.y - (bd.h.y + tsy);
             const float z = ah.z - (bd.h.z + tsz);
