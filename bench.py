@@ -47,12 +47,12 @@ FLOP_PER_PAIR_LJ = 40.0
 L2_FLUSH_BYTES = 256 << 20
 PEAK_FP32_NOMINAL = 152 * 128 * 2 * 2070e6 / 1e12   # TFLOP/s, 128 FMA lanes per SM at the maximum clock
 # DRAM bytes (read + write) of gcmc_kernel<mixed> per chain and Monte Carlo step: ncu
-# dram__bytes_read.sum + dram__bytes_write.sum = 29.4 + 47.5 MB for one launch of 456
-# chains x 20 steps (bench.py --profile --chains 456 --mc-steps 20, ncu --set full
-# --clock-control none -k regex:gcmc_kernel -s 20 -c 1: the third warm-up launch after the
-# 18 autotune probes),
-# scaled by chains x steps to the timed launch.
-DRAM_BYTES_PER_CHAIN_STEP = (29.3952e6 + 47.450368e6) / (456 * 20)
+# dram__bytes_read.sum + dram__bytes_write.sum = 64.98 + 104.78 MB for one launch of 456
+# chains x 20 steps of the kernel of commit 5cb704c (bench.py --profile --chains 456
+# --mc-steps 20, ncu --set full --clock-control none -k regex:gcmc_kernel -s 20 -c 1: the third
+# warm-up launch after the 18 autotune probes), scaled by chains x steps to the timed launch.
+DRAM_BYTES_PER_CHAIN_STEP = (64.982784e6 + 104.780544e6) / (456 * 20)
+DRAM_CAPTURE = "ncu capture of commit 5cb704c (20-step launch of 456 chains, scaled by chain-steps)"
 _FP32_PEAK = []
 
 
@@ -565,6 +565,7 @@ def run_grx(args):
                          "frac": achieved / peak,
                          "traffic": DRAM_BYTES_PER_CHAIN_STEP * g["chains"] * g["mc_steps_per_step"],
                          "traffic_unit": "bytes per launch (ncu DRAM read + write, 20-step capture scaled)",
+                         "traffic_source": DRAM_CAPTURE,
                          "hbm_gbs_achieved": DRAM_BYTES_PER_CHAIN_STEP * g["chains"] * g["mc_steps_per_step"]
                                              / t_launch / 1e9,
                          "hbm_peak_gbs": HBM_PEAK_GBS,
