@@ -41,6 +41,7 @@ struct CbmcWork {
   Bead beads[kCbmcBeads];
   double ipart[kItems * 4];
   int iflag[kItems];
+  VoxStage vst[NW];       // per warp: voxel-list staging buffer and its mbarrier
   int tdead[kCbmcBeads];  // per trial of a pass: early overlap rejection flag (-1: evaluated in full)
   int qbuf[NW * kQueue];
   double te[kMaxTrials * 4];
@@ -162,7 +163,7 @@ __device__ __forceinline__ void trial_pass_body(const BoxDev& b, WK& W, int nb, 
   if constexpr (CL == 1) {
     const PassSplit sp = pass_split(b, nb, nw, b.chunk_mult);
     block_bead_pass<PREC>(b, W.beads, nb, comp, newmol, excl_comp, excl_mol, W.qbuf, W.ipart, W.iflag, &W.counter, sp,
-                          0, -1, chain, W.tdead);
+                          0, -1, chain, W.tdead, W.vst);
     __syncthreads();
     reduce_items<PREC>(W.ipart, W.iflag, nb / chain, chain, sp, W.te, W.tflag);
     __syncthreads();

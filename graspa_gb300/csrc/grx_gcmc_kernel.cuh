@@ -294,6 +294,8 @@ __global__ void __launch_bounds__(NW * 32, 24 / NW) gcmc_kernel(const BoxDev* bo
     W.cfg = 0;
     W.cbeads = 0;
   }
+  if (tid < NW) stage_init(W.vst[tid]);
+  stage_fence_init();
   if (tid < nm) {
     A[tid] = args[e0 + tid];
     ST[tid] = grx_gcmc_stats{};

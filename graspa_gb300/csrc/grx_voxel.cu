@@ -207,7 +207,9 @@ grx_status build_voxels(grx_box* b) {
   std::vector<uint32_t> flat;
   flat.reserve(total);
   for (const auto& l : lists) flat.insert(flat.end(), l.begin(), l.end());
-  if (flat.empty()) flat.push_back(0);
+  // 8 zero entries of padding: the pass stages list ranges with bulk copies rounded out to
+  // 16-byte boundaries, which may read up to 3 entries past the last list
+  flat.insert(flat.end(), 8, 0u);
   if (b->arena) {  // in an arena the lists are optional: take them only with room to spare
     size_t used = 0, largest = 0;
     grx_arena_usage(b->arena, &used, &largest, nullptr);

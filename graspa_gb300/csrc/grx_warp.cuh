@@ -19,6 +19,75 @@ namespace grx {
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kQueue = 64;  // ring buffer entries per warp
 
+// ---------------------------------------------------------------- voxel-list staging
+// A warp walking a bead's voxel list stages the next 8 chunks (256 entries) into its own shared
+// buffer with one bulk copy (cp.async.bulk, completion on an mbarrier) instead of one dependent
+// global load per chunk. The copied range is rounded out to 16-byte boundaries (the list array
+// carries 8 entries of padding), so the buffer holds up to 264 entries.
+constexpr int kStageChunks = 8;
+constexpr int kStageBuf = 32 * kStageChunks + 8;
+struct alignas(16) VoxStage {
+  unsigned buf[kStageBuf];
+  unsigned long long mbar;
+  unsigned phase;  // parity of the mbarrier phase the next copy completes
+  unsigned ok;     // 0 after a wait gave up: the warp reads the lists directly from then on
+};
+constexpr int kStageSpin = 1 << 20;  // try_wait rounds before a wait gives up
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+  return static_cast<unsigned>(__cvta_generic_to_shared(p));
+}
+// Called by one thread per stage before first use, then fenced and barrier-synchronised.
+__device__ __forceinline__ void stage_init(VoxStage& st) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&st.mbar)) : "memory");
+  st.phase = 0;
+  st.ok = 1;
+}
+__device__ __forceinline__ void stage_fence_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// Lane 0: expect `bytes` on the mbarrier and start the bulk copy of [src, src + bytes).
+__device__ __forceinline__ void stage_issue(VoxStage& st, const unsigned* src, unsigned bytes) {
+  const unsigned mb = smem_addr(&st.mbar);
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the warp's reads of the old contents first
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mb), "r"(bytes) : "memory");
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(smem_addr(st.buf)), "l"(src), "r"(bytes), "r"(mb) : "memory");
+}
+// Wait for the phase `parity` of the stage's mbarrier, at most kStageSpin rounds; true when done.
+__device__ __forceinline__ bool stage_wait(const VoxStage& st, unsigned parity) {
+  const unsigned mb = smem_addr(&st.mbar);
+  for (int it = 0; it < kStageSpin; ++it) {
+    unsigned done;
+    asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+                 : "=r"(done) : "r"(mb), "r"(parity) : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// The whole warp stages list entries [a0, a1) (absolute indices): one bulk copy of the range
+// rounded out to 16 bytes, issued by lane 0, awaited by every lane. Returns the first staged
+// entry, or -1 when the wait gave up (after waiting once more for the copy); the stage is then
+// switched off and the warp reads the lists directly. Out of line: it runs once per 8 chunks.
+static __device__ __noinline__ int stage_refill(VoxStage* st, const unsigned* vlist, unsigned a0, unsigned a1) {
+  const int lane = threadIdx.x & 31;
+  const unsigned g0 = a0 & ~3u, g1 = (a1 + 3u) & ~3u;
+  __syncwarp();
+  if (lane == 0) stage_issue(*st, vlist + g0, (g1 - g0) * 4u);
+  __syncwarp();
+  const unsigned par = st->phase;
+  const bool done = __all_sync(kFull, stage_wait(*st, par));
+  if (lane == 0) st->phase = par ^ 1u;
+  if (!done) {
+    stage_wait(*st, par);
+    if (lane == 0) st->ok = 0;
+  }
+  __syncwarp();
+  return done ? (int)g0 : -1;
+}
+
 // g(s) = erfc(alpha sqrt s)/sqrt s from the piecewise quintic table; pieces are found
 // from the FP32 bits of s. Below the table (s < 0.25 A^2) the library erfc is used.
 __device__ __forceinline__ double coul_table(const BoxDev& b, float s32, double s64) {
@@ -253,7 +322,7 @@ template <int PREC, bool VOX>
 __device__ __forceinline__ void warp_item(const BoxDev& b, const Bead& bd, int t0, int t1, int g0, int g1,
                                           int component, int newmol, int excl_comp, int excl_mol, int* q,
                                           LaneAcc<PREC>& hacc, LaneAcc<PREC>& gacc, int& flag,
-                                          volatile int* dead) {
+                                          volatile int* dead, VoxStage* stage) {
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
   unsigned head = 0, tail = 0;
@@ -277,6 +346,8 @@ __device__ __forceinline__ void warp_item(const BoxDev& b, const Bead& bd, int t
   // screened at the stored image against the bead wrapped into the home cell. Tiles: groups of
   // 32 tiles from `base`, culled one per lane; `mask` holds the group's surviving tiles.
   int ch = t0, cend = t0;
+  int win_off = 0, win_end = t0;  // staged list window: entry j at buf[j + win_off], chunks below win_end
+  if (stage && !stage->ok) stage = nullptr;
   int4 vm = make_int4(0, 0, 0, 0);
   float wx = 0.f, wy = 0.f, wz = 0.f;
   bool hcheck = false;
@@ -306,12 +377,22 @@ __device__ __forceinline__ void warp_item(const BoxDev& b, const Bead& bd, int t
   auto host_step = [&]() -> bool {
     if constexpr (VOX) {
       if (ch >= cend) return false;
+      if (stage && ch >= win_end) {  // stage chunks [ch, ch + 8) of the list (clipped to cend)
+        const int g0 = stage_refill(stage, b.vlist, (unsigned)vm.x + 32u * (unsigned)ch,
+                                    (unsigned)vm.x + (unsigned)min(32 * min(ch + kStageChunks, cend), vm.z));
+        if (g0 >= 0) {
+          win_off = vm.x - g0;
+          win_end = min(ch + kStageChunks, cend);
+        } else {
+          stage = nullptr;
+        }
+      }
       const int j = (ch << 5) + lane;
       ++ch;
       bool in = false;
       int i = 0;
       if (j < vm.z) {
-        const unsigned w = __ldg(b.vlist + vm.x + j);
+        const unsigned w = stage ? stage->buf[j + win_off] : __ldg(b.vlist + vm.x + j);
         i = (int)(w & 0xFFFFFu);
         if (j < vm.y) {
           in = true;
@@ -585,7 +666,8 @@ template <int PREC, bool VOX>
 __device__ __noinline__ void block_bead_pass_impl(const BoxDev& b, const Bead* beads, int nb, int component,
                                                      int newmol, int excl_comp, int excl_mol, int* qbuf,
                                                      double* ipart, int* iflag, int* counter, PassSplit sp,
-                                                     int item0, int item1, int chain, int* dead) {
+                                                     int item0, int item1, int chain, int* dead,
+                                                     VoxStage* stages) {
   if (item1 < 0) item1 = (int)sp.items;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int* q = qbuf + warp * kQueue;
@@ -618,7 +700,8 @@ __device__ __noinline__ void block_bead_pass_impl(const BoxDev& b, const Bead* b
       // trials of `chain` beads; dead[t] < 0: evaluated in full, else the early-exit flag
       volatile int* dt = nullptr;
       if (dead && dead[bead / chain] >= 0) dt = dead + bead / chain;
-      warp_item<PREC, VOX>(b, bd, t0, t1, g0, g1, component, newmol, excl_comp, excl_mol, q, hacc, gacc, flag, dt);
+      warp_item<PREC, VOX>(b, bd, t0, t1, g0, g1, component, newmol, excl_comp, excl_mol, q, hacc, gacc, flag, dt,
+                           stages ? stages + warp : nullptr);
       const unsigned fm = __ballot_sync(kFull, flag != 0);
       warp_store<PREC>(hacc, gacc, ipart + (item + bead) * 4, df{bd.pq.x, bd.pq.y}, g1 > g0);
       if (lane == 0) iflag[item + bead] = fm ? 1 : 0;
@@ -635,13 +718,13 @@ template <int PREC>
 __device__ __forceinline__ void block_bead_pass(const BoxDev& b, const Bead* beads, int nb, int component, int newmol,
                                                 int excl_comp, int excl_mol, int* qbuf, double* ipart, int* iflag,
                                                 int* counter, PassSplit sp, int item0 = 0, int item1 = -1,
-                                                int chain = 1, int* dead = nullptr) {
+                                                int chain = 1, int* dead = nullptr, VoxStage* stages = nullptr) {
   if (b.vox)
     block_bead_pass_impl<PREC, true>(b, beads, nb, component, newmol, excl_comp, excl_mol, qbuf, ipart, iflag,
-                                     counter, sp, item0, item1, chain, dead);
+                                     counter, sp, item0, item1, chain, dead, stages);
   else
     block_bead_pass_impl<PREC, false>(b, beads, nb, component, newmol, excl_comp, excl_mol, qbuf, ipart, iflag,
-                                      counter, sp, item0, item1, chain, dead);
+                                      counter, sp, item0, item1, chain, dead, nullptr);
 }
 
 // ---------------------------------------------------------------- thread-block clusters
