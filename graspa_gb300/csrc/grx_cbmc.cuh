@@ -41,7 +41,7 @@ struct CbmcWork {
   Bead beads[kCbmcBeads];
   double ipart[kItems * 4];
   int iflag[kItems];
-  VoxStage* vst;          // per warp: voxel-list staging buffers and mbarriers (null: direct loads)
+  VoxStage vst[NW];       // per warp: voxel-list staging buffer and its mbarrier
   int tdead[kCbmcBeads];  // per trial of a pass: early overlap rejection flag (-1: evaluated in full)
   int qbuf[NW * kQueue];
   double te[kMaxTrials * 4];
@@ -416,6 +416,7 @@ __device__ __noinline__ void ewald_move(const BoxDev& b, WK& W, int na, double2*
         const int az = abs(k.z);
         const float sz = k.z < 0 ? -1.f : 1.f;
         df cre = {0.f, 0.f}, cim = {0.f, 0.f};
+#pragma unroll 1
         for (int at = 0; at < na; ++at) {
           const float4 R = P[at], Z = fz[at + na * az];
           const df pr = {R.x, R.y}, pi = {R.z, R.w};
@@ -431,6 +432,7 @@ __device__ __noinline__ void ewald_move(const BoxDev& b, WK& W, int na, double2*
         df cre = {0.f, 0.f}, cim = {0.f, 0.f};
         const int ay = abs(k.y), az = abs(k.z);
         const float sy = k.y < 0 ? -1.f : 1.f, sz = k.z < 0 ? -1.f : 1.f;
+#pragma unroll 1
         for (int at = 0; at < na; ++at) {
           const float4 X = fx[at + na * k.x], Y = fy[at + na * ay], Z = fz[at + na * az];
           const df xr = {X.x, X.y}, xi = {X.z, X.w};

@@ -59,7 +59,6 @@ struct grx_gcmc_batch {
   int nwarps = 8;  // warps per box (block size / 32): 8, 12 or 24
   int cluster = 1; // CTAs per box (1, or 2 / 4 / 8 with 24 warps each)
   bool swaps = false;  // a move set with identity swaps: the IDS kernel
-  bool stage = false;  // every box has voxel lists: plain launches stage list chunks (GcmcArgs::stage)
   void* mem = nullptr;
   grx_arena* arena = nullptr;
   BoxDev* d_boxes = nullptr;
@@ -94,8 +93,7 @@ static bool has_swaps(const grx_gcmc_desc* descs, int n) {
 // Validates the boxes and move sets and fills the per-box state and per-entry args.
 static grx_status prepare_gcmc(grx_box* const* boxes, int32_t nboxes, const grx_gcmc_desc* descs,
                                const int32_t* ncomp_moved, std::vector<BoxDev>& hb, std::vector<GcmcArgs>& ha,
-                               std::vector<int>& first, size_t& smem, int chunk_mult, grx_precision prec,
-                               bool& stage) {
+                               std::vector<int>& first, size_t& smem, int chunk_mult, grx_precision prec) {
   GRX_REQUIRE(boxes && descs && nboxes >= 1, "grx_gcmc: bad argument");
   hb.assign(nboxes, BoxDev{});
   ha.clear();
@@ -166,11 +164,6 @@ static grx_status prepare_gcmc(grx_box* const* boxes, int32_t nboxes, const grx_
   }
   first[nboxes] = e;
   GRX_REQUIRE(smem <= kGcmcDynSmem, "grx_gcmc: Ewald tables exceed the shared-memory budget");
-  // voxel-list staging buffers (one per warp, at most 24 warps) when every box walks voxel lists
-  // and they fit beside the Ewald tables; boxes on the tile path take no staging memory
-  stage = smem + 24 * sizeof(VoxStage) <= kGcmcDynSmem;
-  for (int i = 0; i < nboxes; ++i) stage = stage && hb[i].vox;
-  for (GcmcArgs& a : ha) a.stage = stage ? 1 : 0;
   return GRX_OK;
 }
 
@@ -226,8 +219,7 @@ static void launch_shape(grx_precision prec, int nboxes, const BoxDev* dboxes, c
 // when cl > 1, nw = 24) and the step-counter advance (no host sync).
 static grx_status enqueue_gcmc(grx_precision prec, int nw, int nboxes, const BoxDev* dboxes, const GcmcArgs* dargs,
                                const int* dfirst, uint64_t* dstep, int64_t nsteps, grx_gcmc_stats* dstats,
-                               size_t smem, cudaStream_t stream, int cl = 1, bool swaps = false, bool stage = false) {
-  if (stage && cl == 1) smem += (size_t)nw * sizeof(VoxStage);  // the stages open the dynamic shared memory
+                               size_t smem, cudaStream_t stream, int cl = 1, bool swaps = false) {
   if (swaps && cl > 1) {
     GRX_REQUIRE(nw == 24, "grx_gcmc: cluster launches use 24 warps per block");
     GRX_CHECK_CUDA(launch_gcmc_swap_cluster(prec, cl, nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem,
@@ -296,9 +288,8 @@ extern "C" grx_status grx_gcmc_run(grx_box* const* boxes, int32_t nboxes, const 
   std::vector<GcmcArgs> ha;
   std::vector<int> first;
   size_t smem = 0;
-  bool stage = false;
   grx_status st =
-      prepare_gcmc(boxes, nboxes, descs, ncomp_moved, hb, ha, first, smem, boxes[0]->dev.chunk_mult, prec, stage);
+      prepare_gcmc(boxes, nboxes, descs, ncomp_moved, hb, ha, first, smem, boxes[0]->dev.chunk_mult, prec);
   if (st) return st;
   const int ne = first[nboxes];
   grx_box* b0 = boxes[0];
@@ -329,7 +320,7 @@ extern "C" grx_status grx_gcmc_run(grx_box* const* boxes, int32_t nboxes, const 
     st = set_gcmc_smem();
     if (st) return st;
     st = enqueue_gcmc(prec, default_warps(nboxes), nboxes, dboxes, dargs, dfirst, dstep, nsteps, dstats, smem,
-                      b0->stream, 1, has_swaps(descs, ne), stage);
+                      b0->stream, 1, has_swaps(descs, ne));
     if (st) return st;
   }
   GRX_CHECK_CUDA(cudaMemcpyAsync(stats, dstats, ne * sizeof(grx_gcmc_stats), cudaMemcpyDefault, b0->stream),
@@ -355,8 +346,7 @@ extern "C" grx_status grx_gcmc_batch_create(grx_box* const* boxes, int32_t nboxe
   B->prec = prec;
   std::vector<BoxDev> hb;
   std::vector<GcmcArgs> ha;
-  grx_status st =
-      prepare_gcmc(boxes, nboxes, descs, ncomp_moved, hb, ha, B->first, B->smem, B->chunk_mult, prec, B->stage);
+  grx_status st = prepare_gcmc(boxes, nboxes, descs, ncomp_moved, hb, ha, B->first, B->smem, B->chunk_mult, prec);
   if (st) { delete B; return st; }
   B->nentries = B->first[nboxes];
   B->h_args = ha;
@@ -460,7 +450,7 @@ extern "C" grx_status grx_gcmc_batch_launch(grx_gcmc_batch* B, int64_t nsteps, v
   if (nsteps == 0) return GRX_OK;
   B->last_stream = s;
   return enqueue_gcmc(B->prec, B->nwarps, (int)B->boxes.size(), B->d_boxes, B->d_args, B->d_first, B->d_step, nsteps,
-                      B->d_stats, B->smem, s, B->cluster, B->swaps, B->stage);
+                      B->d_stats, B->smem, s, B->cluster, B->swaps);
 }
 
 extern "C" grx_status grx_gcmc_batch_run_graph(grx_gcmc_batch* B, int64_t nsteps, int32_t nlaunch, void* stream) {
@@ -475,7 +465,7 @@ extern "C" grx_status grx_gcmc_batch_run_graph(grx_gcmc_batch* B, int64_t nsteps
     const uint64_t before = grx_launch_count();
     for (int k = 0; k < nlaunch && st == GRX_OK; ++k)
       st = enqueue_gcmc(B->prec, B->nwarps, (int)B->boxes.size(), B->d_boxes, B->d_args, B->d_first, B->d_step, nsteps,
-                        B->d_stats, B->smem, cap, B->cluster, B->swaps, B->stage);
+                        B->d_stats, B->smem, cap, B->cluster, B->swaps);
     count_launch(0 - (grx_launch_count() - before));  // capture records the kernels, it launches nothing
     cudaGraph_t g = nullptr;
     const cudaError_t ec = cudaStreamEndCapture(cap, &g);
@@ -628,7 +618,7 @@ extern "C" grx_status grx_gcmc_batch_autotune(grx_gcmc_batch* B, int64_t nsteps,
     GRX_CHECK_CUDA(read(before), "tune stats");
     GRX_CHECK_CUDA(cudaEventRecord(e0, B->stream), "event");
     st = enqueue_gcmc(B->prec, nw, nb, B->d_boxes, B->d_args, B->d_first, B->d_step, nsteps, B->d_stats, B->smem,
-                      B->stream, cl, B->swaps, B->stage);
+                      B->stream, cl, B->swaps);
     if (st) return st;
     GRX_CHECK_CUDA(cudaEventRecord(e1, B->stream), "event");
     GRX_CHECK_CUDA(cudaEventSynchronize(e1), "event");

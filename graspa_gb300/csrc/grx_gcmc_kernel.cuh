@@ -31,7 +31,7 @@ struct GcmcArgs {
   int rigid;
   int charged;
   int bias;
-  int stage;    // per batch: voxel-list staging buffers open the dynamic shared memory (plain launches)
+  int pad_;
   double excl;  // ExclusionIntra + ExclusionAtom of the component
   double big_p; // MolFraction * Pressure * FugacityCoefficient * Volume
   // per box (the same in all its entries): Philox move index of step s of a launch =
@@ -286,7 +286,7 @@ __global__ void __launch_bounds__(NW * 32, 24 / NW) gcmc_kernel(const BoxDev* bo
   __shared__ grx_gcmc_stats ST[kMaxMoved];
   __shared__ int s_accept;
   __shared__ double s_e1[4], s_w1, s_dE[3], s_stored, s_r1[4], s_wr;
-  extern __shared__ __align__(16) unsigned char dyn_smem[];
+  extern __shared__ double2 eik[];
   const int tid = threadIdx.x;
   const int e0 = first[box], nm = first[box + 1] - e0;
   if (tid == 0) {
@@ -294,18 +294,12 @@ __global__ void __launch_bounds__(NW * 32, 24 / NW) gcmc_kernel(const BoxDev* bo
     W.cfg = 0;
     W.cbeads = 0;
   }
+  if (tid < NW) stage_init(W.vst[tid]);
+  stage_fence_init();
   if (tid < nm) {
     A[tid] = args[e0 + tid];
     ST[tid] = grx_gcmc_stats{};
   }
-  __syncthreads();
-  // dynamic shared memory: [NW voxel-list stages when the batch stages] [eik tables]
-  const bool staged = CL == 1 && A[0].stage;
-  VoxStage* vst = reinterpret_cast<VoxStage*>(dyn_smem);
-  double2* eik = reinterpret_cast<double2*>(dyn_smem + (staged ? NW * sizeof(VoxStage) : 0));
-  if (tid == 0) W.vst = staged ? vst : nullptr;
-  if (staged && tid < NW) stage_init(vst[tid]);
-  stage_fence_init();
   __syncthreads();
   int* comp_size = const_cast<int*>(b.comp_size);
   const int64_t nsb = (A[0].nsteps_cap >= 0 && A[0].nsteps_cap < nsteps) ? A[0].nsteps_cap : nsteps;
