@@ -585,14 +585,6 @@ __device__ __forceinline__ df warp_sum_df(df x) {
   return df{r.x, r.y};
 }
 
-__device__ __forceinline__ df warp_sum_df_inl(df x) {
-  for (int o = 16; o > 0; o >>= 1) {
-    const df y = {__shfl_down_sync(kFull, x.hi, o), __shfl_down_sync(kFull, x.lo, o)};
-    x = df_add(x, y);
-  }
-  return x;
-}
-
 template <int PREC>
 __device__ __forceinline__ void warp_store(const LaneAcc<PREC>& h, const LaneAcc<PREC>& g, double* out4, df pq,
                                            bool with_guests) {
